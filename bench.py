@@ -1,0 +1,340 @@
+"""Benchmark: photon histories per second on one GB300 for the CT helical workload.
+
+Workload (the configuration the headline metric is quoted on): 120 kVp CT
+helical scan (2.5 mm Al, 40 mm collimation, pitch 1, 1 degree steps, heel
+effect) over a seeded 512 x 512 x 200 body phantom (0.8 x 0.8 x 2.5 mm voxels,
+air / soft tissue / lung / bone), 1e8 histories per step, LIVERMORE model,
+FP32 transport with FP64 tallies.
+
+* value: histories/s with world, LUT and source tables resident in HBM; one
+  step = one transport job (tally clear + transport kernel), timed with CUDA
+  events on the job's stream.  The voxel grid (420 MB) and the tallies (1 GB)
+  exceed the 129 MB L2, so no explicit L2 flush is needed between steps.
+* e2e: the same metric through the public API with host buffers: world H2D
+  from pinned memory, device max-density scan, host LUT build and upload, job,
+  device post-processing and D2H of dose, variance and event counts.
+* roofline: algorithmic bytes of the transport kernel per launch,
+  5 B per Woodcock step (u8 material + f32 density) + 20 B per deposit
+  (FP64 energy + FP64 energy^2 + u32 count), from the kernel's own step and
+  deposit counters, over the kernel's CUDA-event duration, against the
+  measured HBM copy bandwidth.
+* cpu_baseline / --impl reference: the oracle port (a C++ restatement of the
+  reference transport, oracle/port) on the host cores, on a bounded sample of
+  the same workload (a subset of the exposures).
+
+Multi-GPU (torchrun, N > 1): every rank runs an independent replica of the job
+(histories are independent; no data-path collective), barrier + max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self._proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200",
+                                           "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._thread = threading.Thread(target=self._read, daemon=True)
+            self._thread.start()
+        except Exception:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return None
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for i, n in enumerate(names):
+                if len(s) > 5 + i and s[5 + i].lower() == "active":
+                    reasons.add(n)
+        loaded = sorted(sm)[len(sm) // 2:] if sm else []
+        return {"sm_mhz": float(np.median(loaded)) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def measured_peaks():
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """DRAM bytes per launch of the transport kernel from the committed ncu summary (if any)."""
+    p = REPO / "profiles" / "transport_kernel_ct_helical.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return None
+    return None
+
+
+def build_workload(histories: int):
+    from dxmclib_gb300 import workloads
+    return workloads.ct_helical(histories=histories)
+
+
+def cpu_sample(wl, lut_info, target_seconds: float, n_threads: int, model: int):
+    """Runs the oracle port on a bounded, evenly spread subset of the workload's exposures."""
+    sys.path.insert(0, str(REPO / "oracle" / "port"))
+    import binding as port
+    world = wl.world
+    src = wl.source
+    ex = src.exposures().as_matrix()
+    spec = src.spectrum()
+    heel = src.heel()
+    heel_d = None if heel is None else dict(energy_start=heel.energy_start, energy_step=heel.energy_step,
+                                             energy_size=heel.energy_size, angle_start=heel.angle_start,
+                                             angle_step=heel.angle_step, angle_size=heel.angle_size, weights=heel.weights)
+    dens = world.densityArray().astype(np.float64)
+    mat = world.materialIndexArray()
+
+    def run(n_exp, hpe):
+        idx = np.linspace(0, len(ex) - 1, n_exp).astype(np.int64)
+        sub = ex[idx].copy()
+        sub[:, 17] = hpe
+        e, e2, nev, secs, steps = port.transport(lut_info, world.dimensions(), world.spacing(), dens, mat, sub,
+                                                 model=model, n_threads=n_threads, seed=99,
+                                                 spectrum=(spec.energies, spec.weights), heel=heel_d)
+        return n_exp * hpe, secs
+
+    n_pilot, secs = run(64, 200)
+    rate = n_pilot / max(secs, 1e-3)
+    hist = int(max(rate * target_seconds, 64 * 200))
+    n_exp = min(len(ex), 450)
+    hpe = max(hist // n_exp, 1)
+    n, secs = run(n_exp, hpe)
+    return n, secs, f"{n_exp} of {len(ex)} exposures evenly spaced x {hpe} histories ({n} histories)"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--histories", type=float, default=1e8)
+    ap.add_argument("--model", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    ws, rank, local = _dist()
+    metric = "histories/s"
+    histories = int(args.histories)
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from dxmclib_gb300 import LutBlob, build as b
+        b.build()
+        wl = build_workload(histories)
+        md = np.zeros(len(wl.world.materialMap()))
+        np.maximum.at(md, wl.world.materialIndexArray(), wl.world.densityArray().astype(np.float64))
+        info = LutBlob(wl.world.materialMap(), md, wl.source.maxPhotonEnergyProduced()).info()
+        threads = os.cpu_count() or 1
+        rates = []
+        sample = ""
+        for step in range(args.warmup + args.steps):
+            n, secs, sample = cpu_sample(wl, info, args.cpu_seconds / 2, threads, args.model)
+            if step >= args.warmup:
+                rates.append(n / secs)
+        v = float(np.mean(rates))
+        line = {"metric": metric, "value": v, "unit": "histories/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * histories / v, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": wl.name, "histories_per_step": histories, "model": "LIVERMORE"},
+                "impl": "reference",
+                "cpu_baseline": {"value": v, "unit": "histories/s", "cores": threads, "kind": "port", "sample": sample},
+                "e2e": {"value": v, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    from dxmclib_gb300 import build as b
+    b.build()
+    device = local if ws > 1 else 0
+    torch.cuda.set_device(device)
+    dist = None
+    if ws > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist = tdist
+
+    wl = build_workload(histories)
+    world, src = wl.world, wl.source
+    ctx = dx.GpuContext(device=device)
+    dworld = dx.DeviceWorld(ctx, world)
+    md = dworld.max_density()
+    blob = dx.LutBlob(world.materialMap(), md, src.maxPhotonEnergyProduced())
+    dlut = dx.DeviceLut(ctx, blob)
+    exposures = src.exposures(world.directionCosines())
+    spec, heel = src.spectrum(), src.heel()
+    n_hist = int(np.sum(exposures.n_histories))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    def run_job(seed):
+        job = dx.Job(ctx, dworld, dlut, exposures, spec, heel, None, seed=seed, model=args.model)
+        job.wait()
+        st = dx.api.A.JobStats()
+        A.check(ctx.lib.dxmc_gpu_job_result(job.handle, A.OUTPUT_RAW, 1.0, None, None, None, dx.api.C.byref(st)),
+                ctx.handle, "job_result")
+        job.close()
+        return st
+
+    for w in range(args.warmup):
+        run_job(1000 + w)
+    barrier()
+    with ClockSampler(device) as clocks:
+        stats = [run_job(2000 + s) for s in range(args.steps)]
+        barrier()
+    job_ms = np.array([s.job_ms for s in stats])
+    kern_ms = np.array([s.kernel_ms for s in stats])
+    total_ms = float(job_ms.sum())
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = ws * n_hist * args.steps / (total_ms / 1e3)
+    steps_per_hist = float(np.mean([s.steps for s in stats])) / n_hist
+    deps_per_hist = float(np.mean([s.deposits for s in stats])) / n_hist
+    alg_bytes = 5.0 * np.mean([s.steps for s in stats]) + 20.0 * np.mean([s.deposits for s in stats])
+    achieved = alg_bytes / (float(kern_ms.mean()) / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = committed_traffic()
+
+    # ---- e2e through the public API with pinned host buffers -------------------------
+    n_vox = world.size()
+    pin_d = torch.empty(n_vox, dtype=torch.float32, pin_memory=True)
+    pin_m = torch.empty(n_vox, dtype=torch.uint8, pin_memory=True)
+    pin_d.numpy()[:] = world.densityArray()
+    pin_m.numpy()[:] = world.materialIndexArray()
+    e2e_world = dx.World()
+    e2e_world.setDimensions(world.dimensions())
+    e2e_world.setSpacing(world.spacing())
+    e2e_world.setDensityArray(pin_d.numpy())
+    e2e_world.setMaterialIndexArray(pin_m.numpy())
+    for m in world.materialMap():
+        e2e_world.addMaterialToMap(m)
+    assert e2e_world.isValid()
+    out_d = torch.empty(n_vox, dtype=torch.float64, pin_memory=True).numpy()
+    out_v = torch.empty(n_vox, dtype=torch.float64, pin_memory=True).numpy()
+    out_n = torch.empty(n_vox, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    e2e_steps = max(1, min(args.steps, 3))
+
+    def e2e_step(seed):
+        dw = dx.DeviceWorld(ctx, e2e_world)
+        bl = dx.LutBlob(e2e_world.materialMap(), dw.max_density(), src.maxPhotonEnergyProduced())
+        dl = dx.DeviceLut(ctx, bl)
+        ex = src.exposures(e2e_world.directionCosines())
+        job = dx.Job(ctx, dw, dl, ex, src.spectrum(), src.heel(), None, seed=seed, model=args.model)
+        job.result(A.OUTPUT_EV_PER_HISTORY, out=(out_d, out_v, out_n))
+        job.close()
+        dl.close()
+        bl.close()
+        dw.close()
+
+    e2e_step(1)
+    barrier()
+    t0 = time.perf_counter()
+    for s in range(e2e_steps):
+        e2e_step(3000 + s)
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = ws * n_hist * e2e_steps / e2e_s
+    h2d = n_vox * 5 + len(exposures) * 80
+    d2h = n_vox * (8 + 8 + 4)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        n, secs, sample = cpu_sample(wl, blob.info(), args.cpu_seconds, threads, args.model)
+        cpu = {"value": n / secs, "unit": "histories/s", "cores": threads, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": metric, "value": value, "unit": "histories/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl.name, "histories_per_step": n_hist, "exposures": len(exposures),
+                       "model": ["NONE", "LIVERMORE", "IA"][args.model], "tally": "fp64",
+                       "l2": "inputs larger than L2 (420 MB voxels + 1 GB tallies)", "parallelism": f"replicas{ws}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind,
+                         "traffic": None if not traffic else traffic.get("dram_bytes_per_launch_scaled"),
+                         "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": float(kern_ms.mean()),
+                         "steps_per_history": steps_per_hist, "deposits_per_history": deps_per_hist},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "histories/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "steps": e2e_steps},
+            "gpu_launches": args.steps,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    dlut.close()
+    dworld.close()
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

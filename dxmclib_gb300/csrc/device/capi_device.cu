@@ -1,0 +1,841 @@
+// Device-side entry points of the C ABI (include/dxmc_gpu.h): context,
+// resident worlds and LUTs, job submission on the context stream, result
+// post-processing and the component probes.  Every entry point returns an int
+// status and records a message retrievable with dxmc_gpu_last_error.
+#include "dxmc_gpu.h"
+
+#include "../host/lut_builder.hpp"
+#include "../kernels/transport.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+using namespace dxmc_gb300;
+
+struct dxmc_gpu_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    dxmc_gpu_options options {};
+    std::mutex mutex;
+    std::string last_error;
+    uint64_t budget = 0;
+    uint64_t in_use = 0;
+    size_t max_smem_optin = 0;
+};
+
+struct dxmc_world {
+    dxmc_gpu_ctx* ctx = nullptr;
+    dev::Voxel* voxels = nullptr;
+    uint64_t dims[3] {};
+    double spacing[3] {};
+    double origin[3] {};
+    double cosines[6] {};
+    int n_materials = 0;
+    bool has_measurement = false;
+    uint64_t bytes = 0;
+    dev::WorldParams params {};
+};
+
+struct dxmc_lut {
+    dxmc_gpu_ctx* ctx = nullptr;
+    float* image = nullptr;
+    dev::LutMeta meta {};
+    uint64_t bytes = 0;
+};
+
+struct dxmc_job {
+    dxmc_gpu_ctx* ctx = nullptr;
+    dxmc_world* world = nullptr;
+    double* tally = nullptr;
+    float* tally_f32 = nullptr;
+    uint32_t* n_events = nullptr;
+    dev::JobCounters* counters = nullptr;
+    unsigned char* tables = nullptr;
+    int* cancel_host = nullptr;  // pinned, mapped
+    int* cancel_dev = nullptr;
+    cudaEvent_t begin = nullptr, start = nullptr, stop = nullptr; // job begin, kernel start, kernel end
+    uint64_t histories = 0;
+    int tally_mode = 0;
+    uint64_t bytes = 0;
+    bool cancelled = false;
+    bool overflowed = false;
+};
+
+namespace {
+
+int fail(dxmc_gpu_ctx* ctx, int code, const std::string& msg)
+{
+    if (ctx)
+        ctx->last_error = msg;
+    return code;
+}
+
+int cuda_fail(dxmc_gpu_ctx* ctx, cudaError_t e, const char* what)
+{
+    return fail(ctx, DXMC_ERR_DEVICE, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define DXMC_CUDA(ctx, call)                         \
+    do {                                             \
+        cudaError_t e_ = (call);                     \
+        if (e_ != cudaSuccess)                       \
+            return cuda_fail((ctx), e_, #call);      \
+    } while (0)
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Safe extents exactly as World<float>::updateMatrixExtent (world.hpp:55-68).
+void world_extents(const uint64_t dims[3], const double spacing[3], const double origin[3], float lo[3], float hi[3])
+{
+    for (int i = 0; i < 3; ++i) {
+        const float sp = static_cast<float>(spacing[i]);
+        const float half = (static_cast<float>(dims[i]) * sp) * 0.5f;
+        const float o = static_cast<float>(origin[i]);
+        const float lower = o - half;
+        const float upper = o + half;
+        lo[i] = std::nextafter(lower, upper);
+        hi[i] = std::nextafter(upper, lower);
+    }
+}
+
+__global__ void pack_voxels_kernel(const float* __restrict__ density, const uint8_t* __restrict__ material,
+    const uint8_t* __restrict__ measurement, uint64_t n, dev::Voxel* __restrict__ out)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        dev::Voxel v;
+        v.density = density[i];
+        v.material = material[i];
+        v.measurement = measurement ? measurement[i] : 0;
+        v.pad = 0;
+        out[i] = v;
+    }
+}
+
+__global__ void check_materials_kernel(const uint8_t* __restrict__ material, uint64_t n, int n_materials, unsigned int* bad)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        if (material[i] >= n_materials)
+            atomicOr(bad, 1u);
+}
+
+} // namespace
+
+extern "C" {
+
+int dxmc_gpu_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out)
+{
+    if (!out)
+        return DXMC_ERR_INVALID;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+        return DXMC_ERR_NO_DEVICE;
+    auto* ctx = new (std::nothrow) dxmc_gpu_ctx;
+    if (!ctx)
+        return DXMC_ERR_OOM;
+    if (options)
+        ctx->options = *options;
+    ctx->device = ctx->options.device;
+    if (ctx->device < 0 || ctx->device >= count) {
+        delete ctx;
+        return DXMC_ERR_INVALID;
+    }
+    if (cudaSetDevice(ctx->device) != cudaSuccess) {
+        delete ctx;
+        return DXMC_ERR_DEVICE;
+    }
+    cudaDeviceProp prop {};
+    cudaGetDeviceProperties(&prop, ctx->device);
+    ctx->sm_count = prop.multiProcessorCount;
+    ctx->max_smem_optin = prop.sharedMemPerBlockOptin;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return DXMC_ERR_DEVICE;
+    }
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    ctx->budget = ctx->options.memory_budget ? ctx->options.memory_budget : static_cast<uint64_t>(free_b * 0.9);
+    *out = ctx;
+    return DXMC_OK;
+}
+
+void dxmc_gpu_ctx_destroy(dxmc_gpu_ctx* ctx)
+{
+    if (!ctx)
+        return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* dxmc_gpu_last_error(const dxmc_gpu_ctx* ctx)
+{
+    return ctx ? ctx->last_error.c_str() : "no context";
+}
+
+int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_world** out)
+{
+    if (!ctx || !d || !out)
+        return DXMC_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    *out = nullptr;
+    const uint64_t n = d->dims[0] * d->dims[1] * d->dims[2];
+    // World::validate (world.hpp:182-227)
+    if (n == 0 || !(d->spacing[0] * d->spacing[1] * d->spacing[2] > 0) || !d->density || !d->material || d->n_materials <= 0 || d->n_materials > 255)
+        return fail(ctx, DXMC_ERR_INVALID, "invalid world: dimensions, spacing, arrays or material count");
+    if (d->dims[0] > 0xffffffffull || d->dims[1] > 0xffffffffull || d->dims[2] > 0xffffffffull)
+        return fail(ctx, DXMC_ERR_INVALID, "invalid world: dimension exceeds 2^32");
+    {
+        const double* c = d->direction_cosines;
+        const double n1 = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        const double n2 = std::sqrt(c[3] * c[3] + c[4] * c[4] + c[5] * c[5]);
+        if (!(n1 > 0) || !(n2 > 0))
+            return fail(ctx, DXMC_ERR_INVALID, "invalid world: zero direction cosine");
+        const double x[3] = { c[0] / n1, c[1] / n1, c[2] / n1 };
+        const double y[3] = { c[3] / n2, c[4] / n2, c[5] / n2 };
+        const double z[3] = { x[1] * y[2] - x[2] * y[1], x[2] * y[0] - x[0] * y[2], x[0] * y[1] - x[1] * y[0] };
+        const double ortho = (z[0] * x[0] + z[1] * x[1] + z[2] * x[2]) + (z[0] * y[0] + z[1] * y[1] + z[2] * y[2]) + (x[0] * y[0] + x[1] * y[1] + x[2] * y[2]);
+        if (std::abs(ortho) > 0.001)
+            return fail(ctx, DXMC_ERR_INVALID, "invalid world: direction cosines are not orthogonal");
+    }
+    const uint64_t bytes = n * sizeof(dev::Voxel);
+    if (ctx->in_use + bytes > ctx->budget)
+        return fail(ctx, DXMC_ERR_OOM, "world exceeds the device memory budget");
+    cudaSetDevice(ctx->device);
+    auto* w = new (std::nothrow) dxmc_world;
+    if (!w)
+        return DXMC_ERR_OOM;
+    w->ctx = ctx;
+    // stage raw arrays, validate and pack on the device
+    float* d_density = nullptr;
+    uint8_t* d_material = nullptr;
+    uint8_t* d_meas = nullptr;
+    unsigned int* d_bad = nullptr;
+    cudaError_t e = cudaMalloc(&w->voxels, bytes);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&d_density, n * sizeof(float), ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&d_material, n, ctx->stream);
+    if (e == cudaSuccess && d->measurement)
+        e = cudaMallocAsync(&d_meas, n, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&d_bad, sizeof(unsigned int), ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_density, d->density, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_material, d->material, n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && d_meas)
+        e = cudaMemcpyAsync(d_meas, d->measurement, n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), ctx->stream);
+    unsigned int bad = 0;
+    if (e == cudaSuccess) {
+        const int grid = ctx->sm_count * 8;
+        check_materials_kernel<<<grid, 256, 0, ctx->stream>>>(d_material, n, d->n_materials, d_bad);
+        pack_voxels_kernel<<<grid, 256, 0, ctx->stream>>>(d_density, d_material, d_meas, n, w->voxels);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&bad, d_bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (d_density)
+        cudaFreeAsync(d_density, ctx->stream);
+    if (d_material)
+        cudaFreeAsync(d_material, ctx->stream);
+    if (d_meas)
+        cudaFreeAsync(d_meas, ctx->stream);
+    if (d_bad)
+        cudaFreeAsync(d_bad, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        if (w->voxels)
+            cudaFree(w->voxels);
+        delete w;
+        return cuda_fail(ctx, e, "world upload");
+    }
+    if (bad) {
+        cudaFree(w->voxels);
+        delete w;
+        return fail(ctx, DXMC_ERR_INVALID, "invalid world: material index >= n_materials");
+    }
+    for (int i = 0; i < 3; ++i) {
+        w->dims[i] = d->dims[i];
+        w->spacing[i] = d->spacing[i];
+        w->origin[i] = d->origin[i];
+    }
+    std::memcpy(w->cosines, d->direction_cosines, sizeof(w->cosines));
+    w->n_materials = d->n_materials;
+    w->has_measurement = d->measurement != nullptr;
+    w->bytes = bytes;
+    ctx->in_use += bytes;
+    auto& P = w->params;
+    P.voxels = w->voxels;
+    for (int i = 0; i < 3; ++i) {
+        P.dims[i] = static_cast<uint32_t>(d->dims[i]);
+        P.inv_spacing[i] = static_cast<float>(1.0 / static_cast<double>(static_cast<float>(d->spacing[i])));
+    }
+    world_extents(d->dims, d->spacing, d->origin, P.lo, P.hi);
+    P.nxy = d->dims[0] * d->dims[1];
+    P.n_voxels = n;
+    *out = w;
+    return DXMC_OK;
+}
+
+int dxmc_gpu_world_max_density(dxmc_world* w, double* out, int n_materials)
+{
+    if (!w || !out || n_materials <= 0)
+        return DXMC_ERR_INVALID;
+    dxmc_gpu_ctx* ctx = w->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    cudaSetDevice(ctx->device);
+    unsigned int* d_bits = nullptr;
+    DXMC_CUDA(ctx, cudaMallocAsync(&d_bits, n_materials * sizeof(unsigned int), ctx->stream));
+    DXMC_CUDA(ctx, cudaMemsetAsync(d_bits, 0, n_materials * sizeof(unsigned int), ctx->stream));
+    DXMC_CUDA(ctx, dev::launch_max_density(w->voxels, w->params.n_voxels, d_bits, n_materials, ctx->stream));
+    std::vector<unsigned int> bits(n_materials);
+    DXMC_CUDA(ctx, cudaMemcpyAsync(bits.data(), d_bits, n_materials * sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream));
+    cudaFreeAsync(d_bits, ctx->stream);
+    DXMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < n_materials; ++i) {
+        float f;
+        std::memcpy(&f, &bits[i], sizeof(float));
+        out[i] = f;
+    }
+    return DXMC_OK;
+}
+
+void dxmc_gpu_world_free(dxmc_world* w)
+{
+    if (!w)
+        return;
+    std::lock_guard<std::mutex> lock(w->ctx->mutex);
+    cudaSetDevice(w->ctx->device);
+    cudaStreamSynchronize(w->ctx->stream);
+    cudaFree(w->voxels);
+    w->ctx->in_use -= w->bytes;
+    delete w;
+}
+
+int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* b, dxmc_lut** out)
+{
+    if (!ctx || !b || !out || b->n_materials <= 0)
+        return DXMC_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    *out = nullptr;
+    const int nm = b->n_materials;
+    const int R = static_cast<int>(b->resolution());
+    dev::LutMeta m {};
+    m.n_materials = nm;
+    m.R = R;
+    m.linear_index = static_cast<int>(b->linear_index);
+    m.linear_step = static_cast<float>(b->linear_step);
+    m.inv_linear_step = static_cast<float>(1.0 / b->linear_step);
+    m.linear_energy = static_cast<float>(b->linear_energy);
+    m.max_energy = static_cast<float>(b->max_energy);
+    size_t off = 0;
+    m.off_x = static_cast<int>(off);
+    off = align_up(off + R, 4);
+    m.off_coef = static_cast<int>(off);
+    off = align_up(off + static_cast<size_t>(nm) * R * 6, 4);
+    m.off_maxcoef = static_cast<int>(off);
+    off = align_up(off + static_cast<size_t>(R) * 2, 4);
+    m.off_rita = static_cast<int>(off);
+    off = align_up(off + static_cast<size_t>(nm) * 4 * dev::RITA_N, 4);
+    m.off_spline = static_cast<int>(off);
+    off = align_up(off + static_cast<size_t>(nm) * dev::SPLINE_FLOATS, 4);
+    m.off_shells = static_cast<int>(off);
+    off = align_up(off + static_cast<size_t>(nm) * dev::N_SHELLS * dev::SHELL_FLOATS, 4);
+    m.total_floats = static_cast<int>(off);
+    std::vector<float> img(off, 0.0f);
+    for (int i = 0; i < R; ++i)
+        img[m.off_x + i] = static_cast<float>(b->log_energy[i]);
+    for (size_t i = 0; i < static_cast<size_t>(nm) * R * 6; ++i)
+        img[m.off_coef + i] = static_cast<float>(b->coefficients[i]);
+    for (int i = 0; i < R * 2; ++i)
+        img[m.off_maxcoef + i] = static_cast<float>(b->max_coefficients[i]);
+    for (int mat = 0; mat < nm; ++mat) {
+        for (int k = 0; k < 4 * dev::RITA_N; ++k)
+            img[m.off_rita + mat * 4 * dev::RITA_N + k] = static_cast<float>(b->rita[mat][k]);
+        float* sp = img.data() + m.off_spline + mat * dev::SPLINE_FLOATS;
+        for (int k = 0; k < 60; ++k)
+            sp[k] = static_cast<float>(b->spline[mat][k]);
+        sp[60] = static_cast<float>(b->spline[mat][76]);
+        sp[61] = static_cast<float>(b->spline[mat][77]);
+        sp[62] = static_cast<float>(b->spline[mat][78]);
+        for (int s = 0; s < dev::N_SHELLS; ++s) {
+            const auto& c = b->shells[mat][s];
+            float* o = img.data() + m.off_shells + (mat * dev::N_SHELLS + s) * dev::SHELL_FLOATS;
+            o[0] = static_cast<float>(c.binding_energy);
+            o[1] = static_cast<float>(c.number_electrons);
+            o[2] = static_cast<float>(c.hartree_fock_j0);
+            o[3] = static_cast<float>(c.photo_ionization_probability);
+            o[4] = static_cast<float>(c.fluorescence_yield);
+            for (int k = 0; k < 3; ++k) {
+                o[5 + k] = static_cast<float>(c.line_probabilities[k]);
+                o[8 + k] = static_cast<float>(c.line_energies[k]);
+            }
+        }
+    }
+    cudaSetDevice(ctx->device);
+    auto* lut = new (std::nothrow) dxmc_lut;
+    if (!lut)
+        return DXMC_ERR_OOM;
+    lut->ctx = ctx;
+    lut->meta = m;
+    lut->bytes = img.size() * sizeof(float);
+    cudaError_t e = cudaMalloc(&lut->image, lut->bytes);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(lut->image, img.data(), lut->bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        if (lut->image)
+            cudaFree(lut->image);
+        delete lut;
+        return cuda_fail(ctx, e, "lut upload");
+    }
+    ctx->in_use += lut->bytes;
+    *out = lut;
+    return DXMC_OK;
+}
+
+void dxmc_gpu_lut_free(dxmc_lut* lut)
+{
+    if (!lut)
+        return;
+    std::lock_guard<std::mutex> lock(lut->ctx->mutex);
+    cudaSetDevice(lut->ctx->device);
+    cudaStreamSynchronize(lut->ctx->stream);
+    cudaFree(lut->image);
+    lut->ctx->in_use -= lut->bytes;
+    delete lut;
+}
+
+namespace {
+
+void free_job_device(dxmc_job* j)
+{
+    cudaStream_t s = j->ctx->stream;
+    if (j->tally)
+        cudaFreeAsync(j->tally, s);
+    if (j->tally_f32)
+        cudaFreeAsync(j->tally_f32, s);
+    if (j->n_events)
+        cudaFreeAsync(j->n_events, s);
+    if (j->counters)
+        cudaFreeAsync(j->counters, s);
+    if (j->tables)
+        cudaFreeAsync(j->tables, s);
+    j->tally = nullptr;
+    j->tally_f32 = nullptr;
+    j->n_events = nullptr;
+    j->counters = nullptr;
+    j->tables = nullptr;
+}
+
+} // namespace
+
+int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_job_desc* jd, dxmc_job** out)
+{
+    if (!ctx || !world || !lut || !jd || !out)
+        return DXMC_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    *out = nullptr;
+    if (world->ctx != ctx || lut->ctx != ctx)
+        return fail(ctx, DXMC_ERR_INVALID, "world or lut belongs to another context");
+    if (!jd->exposures || jd->n_exposures == 0 || jd->n_exposures > 0xffffffffull)
+        return fail(ctx, DXMC_ERR_INVALID, "job needs at least one exposure");
+    if (jd->model < 0 || jd->model > 2)
+        return fail(ctx, DXMC_ERR_INVALID, "unknown low-energy correction model");
+    if (lut->meta.n_materials < world->n_materials)
+        return fail(ctx, DXMC_ERR_INVALID, "lut has fewer materials than the world");
+    const int tally_mode = jd->tally_mode >= 0 ? jd->tally_mode : ctx->options.tally_mode;
+    if (tally_mode < 0 || tally_mode > 2)
+        return fail(ctx, DXMC_ERR_INVALID, "unknown tally mode");
+
+    // ---- host-side tables: exposures, prefix offsets, spectrum, heel, bow-tie ----
+    const uint64_t ne = jd->n_exposures;
+    std::vector<dev::DevExposure> ex(ne);
+    std::vector<uint64_t> offsets(ne + 1, 0);
+    for (uint64_t i = 0; i < ne; ++i) {
+        const dxmc_exposure& s = jd->exposures[i];
+        dev::DevExposure& d = ex[i];
+        std::memset(&d, 0, sizeof(d));
+        for (int k = 0; k < 3; ++k) {
+            d.pos[k] = static_cast<float>(s.position[k]);
+            d.cosx[k] = static_cast<float>(s.direction_cosines[k]);
+            d.cosy[k] = static_cast<float>(s.direction_cosines[3 + k]);
+            d.beam[k] = static_cast<float>(s.beam_direction[k]);
+        }
+        for (int k = 0; k < 4; ++k)
+            d.coll[k] = static_cast<float>(s.collimation[k]);
+        d.weight = static_cast<float>(s.weight);
+        d.mono_energy = static_cast<float>(s.mono_energy);
+        offsets[i + 1] = offsets[i] + s.n_histories;
+    }
+    const uint64_t total = offsets[ne];
+    if (total == 0)
+        return fail(ctx, DXMC_ERR_INVALID, "job has no histories");
+    std::vector<float> spec_e, spec_p;
+    std::vector<uint32_t> spec_a;
+    if (jd->spectrum) {
+        const int n = jd->spectrum->n;
+        if (n <= 0 || !jd->spectrum->energies || !jd->spectrum->weights)
+            return fail(ctx, DXMC_ERR_INVALID, "invalid spectrum");
+        std::vector<double> w(jd->spectrum->weights, jd->spectrum->weights + n), probs;
+        std::vector<uint64_t> alias;
+        host::build_alias_table(w, probs, alias);
+        for (int i = 0; i < n; ++i) {
+            spec_e.push_back(static_cast<float>(jd->spectrum->energies[i]));
+            spec_p.push_back(static_cast<float>(probs[i]));
+            spec_a.push_back(static_cast<uint32_t>(alias[i]));
+        }
+    }
+    std::vector<float> heel;
+    if (jd->heel) {
+        const auto* h = jd->heel;
+        if (h->energy_size <= 0 || h->angle_size <= 0 || !h->weights || !(h->energy_step > 0) || !(h->angle_step != 0))
+            return fail(ctx, DXMC_ERR_INVALID, "invalid heel table");
+        for (int i = 0; i < h->energy_size * h->angle_size; ++i)
+            heel.push_back(static_cast<float>(h->weights[i]));
+    }
+    std::vector<float> bt_a, bt_w;
+    if (jd->bowtie) {
+        // BowTieFilter constructor: |angle|, sort, normalise to mean 1 (beamfilters.hpp:86-100)
+        const int n = jd->bowtie->n;
+        if (n <= 0 || !jd->bowtie->angles || !jd->bowtie->weights)
+            return fail(ctx, DXMC_ERR_INVALID, "invalid bow-tie table");
+        std::vector<std::pair<double, double>> data(n);
+        for (int i = 0; i < n; ++i)
+            data[i] = { std::abs(jd->bowtie->angles[i]), jd->bowtie->weights[i] };
+        std::sort(data.begin(), data.end());
+        double mean = 0;
+        for (auto& p : data)
+            mean += p.second;
+        mean /= n;
+        for (auto& p : data) {
+            bt_a.push_back(static_cast<float>(p.first));
+            bt_w.push_back(static_cast<float>(p.second / mean));
+        }
+    }
+    // one device buffer for all tables
+    size_t off = 0;
+    const size_t off_ex = off;
+    off = align_up(off + ne * sizeof(dev::DevExposure), 256);
+    const size_t off_offsets = off;
+    off = align_up(off + (ne + 1) * sizeof(uint64_t), 256);
+    const size_t off_se = off;
+    off = align_up(off + spec_e.size() * 4, 256);
+    const size_t off_sp = off;
+    off = align_up(off + spec_p.size() * 4, 256);
+    const size_t off_sa = off;
+    off = align_up(off + spec_a.size() * 4, 256);
+    const size_t off_heel = off;
+    off = align_up(off + heel.size() * 4, 256);
+    const size_t off_bta = off;
+    off = align_up(off + bt_a.size() * 4, 256);
+    const size_t off_btw = off;
+    off = align_up(off + bt_w.size() * 4, 256);
+    const size_t table_bytes = off;
+    std::vector<unsigned char> tables(table_bytes, 0);
+    std::memcpy(tables.data() + off_ex, ex.data(), ne * sizeof(dev::DevExposure));
+    std::memcpy(tables.data() + off_offsets, offsets.data(), (ne + 1) * sizeof(uint64_t));
+    std::memcpy(tables.data() + off_se, spec_e.data(), spec_e.size() * 4);
+    std::memcpy(tables.data() + off_sp, spec_p.data(), spec_p.size() * 4);
+    std::memcpy(tables.data() + off_sa, spec_a.data(), spec_a.size() * 4);
+    std::memcpy(tables.data() + off_heel, heel.data(), heel.size() * 4);
+    std::memcpy(tables.data() + off_bta, bt_a.data(), bt_a.size() * 4);
+    std::memcpy(tables.data() + off_btw, bt_w.data(), bt_w.size() * 4);
+
+    const uint64_t nv = world->params.n_voxels;
+    const uint64_t tally_bytes = tally_mode == 1 ? nv * 2 * sizeof(float) : nv * 2 * sizeof(double);
+    const uint64_t job_bytes = tally_bytes + nv * sizeof(uint32_t) + table_bytes + sizeof(dev::JobCounters);
+    if (ctx->in_use + job_bytes > ctx->budget)
+        return fail(ctx, DXMC_ERR_OOM, "job exceeds the device memory budget");
+
+    cudaSetDevice(ctx->device);
+    auto* j = new (std::nothrow) dxmc_job;
+    if (!j)
+        return DXMC_ERR_OOM;
+    j->ctx = ctx;
+    j->world = world;
+    j->histories = total;
+    j->tally_mode = tally_mode;
+    j->bytes = job_bytes;
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaSuccess;
+    if (tally_mode == 1)
+        e = cudaMallocAsync(&j->tally_f32, tally_bytes, s);
+    else
+        e = cudaMallocAsync(&j->tally, tally_bytes, s);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&j->n_events, nv * sizeof(uint32_t), s);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&j->counters, sizeof(dev::JobCounters), s);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&j->tables, table_bytes, s);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&j->begin);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(j->begin, s);
+    if (e == cudaSuccess)
+        e = cudaHostAlloc(&j->cancel_host, sizeof(int), cudaHostAllocMapped);
+    if (e == cudaSuccess) {
+        *j->cancel_host = 0;
+        e = cudaHostGetDevicePointer(&j->cancel_dev, j->cancel_host, 0);
+    }
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(j->tally ? static_cast<void*>(j->tally) : static_cast<void*>(j->tally_f32), 0, tally_bytes, s);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(j->n_events, 0, nv * sizeof(uint32_t), s);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(j->counters, 0, sizeof(dev::JobCounters), s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(j->tables, tables.data(), table_bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&j->start);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&j->stop);
+    if (e != cudaSuccess) {
+        free_job_device(j);
+        if (j->cancel_host)
+            cudaFreeHost(j->cancel_host);
+        delete j;
+        return cuda_fail(ctx, e, "job allocation");
+    }
+
+    dev::TransportParams p {};
+    p.world = world->params;
+    auto& S = p.source;
+    S.exposures = reinterpret_cast<const dev::DevExposure*>(j->tables + off_ex);
+    S.history_offsets = reinterpret_cast<const uint64_t*>(j->tables + off_offsets);
+    S.n_exposures = static_cast<uint32_t>(ne);
+    S.spec_n = static_cast<int>(spec_e.size());
+    S.spec_energy = reinterpret_cast<const float*>(j->tables + off_se);
+    S.spec_prob = reinterpret_cast<const float*>(j->tables + off_sp);
+    S.spec_alias = reinterpret_cast<const uint32_t*>(j->tables + off_sa);
+    if (jd->heel) {
+        S.heel_weights = reinterpret_cast<const float*>(j->tables + off_heel);
+        S.heel_e_start = static_cast<float>(jd->heel->energy_start);
+        S.heel_e_step = static_cast<float>(jd->heel->energy_step);
+        S.heel_e_size = jd->heel->energy_size;
+        S.heel_a_size = jd->heel->angle_size;
+        S.heel_a_start = static_cast<float>(jd->heel->angle_start);
+        S.heel_a_step = static_cast<float>(jd->heel->angle_step);
+    }
+    if (jd->bowtie) {
+        S.bowtie_angle = reinterpret_cast<const float*>(j->tables + off_bta);
+        S.bowtie_weight = reinterpret_cast<const float*>(j->tables + off_btw);
+        S.bowtie_n = static_cast<int>(bt_a.size());
+    }
+    p.lut = lut->image;
+    p.lut_meta = lut->meta;
+    p.tally = j->tally;
+    p.tally_f32 = j->tally_f32;
+    p.n_events = j->n_events;
+    p.counters = j->counters;
+    p.cancel = j->cancel_dev;
+    p.total_histories = total;
+    p.seed = jd->seed;
+    p.tally_mode = tally_mode;
+
+    const size_t lut_bytes = static_cast<size_t>(lut->meta.total_floats) * sizeof(float);
+    const size_t smem_limit = std::min<size_t>(ctx->max_smem_optin, 96 * 1024);
+    p.lut_in_smem = lut_bytes <= smem_limit ? 1 : 0;
+    const size_t smem = p.lut_in_smem ? lut_bytes : 0;
+    const int block = ctx->options.block_size > 0 ? ctx->options.block_size : 256;
+    // also sets the kernel's dynamic shared-memory limit for this launch
+    const int occ = dev::transport_max_blocks_per_sm(jd->model, block, smem);
+    int per_sm = ctx->options.blocks_per_sm > 0 ? ctx->options.blocks_per_sm : occ;
+    if (per_sm <= 0)
+        per_sm = 1;
+    const int grid = ctx->sm_count * per_sm;
+    e = cudaEventRecord(j->start, s);
+    if (e == cudaSuccess)
+        e = dev::launch_transport(p, jd->model, grid, block, smem, s);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(j->stop, s);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(s);
+        free_job_device(j);
+        cudaFreeHost(j->cancel_host);
+        delete j;
+        return cuda_fail(ctx, e, "transport launch");
+    }
+    ctx->in_use += job_bytes;
+    *out = j;
+    return DXMC_OK;
+}
+
+int dxmc_gpu_job_wait(dxmc_job* j, int64_t timeout_ms)
+{
+    if (!j)
+        return DXMC_ERR_INVALID;
+    dxmc_gpu_ctx* ctx = j->ctx;
+    cudaSetDevice(ctx->device);
+    const auto t0 = std::chrono::steady_clock::now();
+    while (true) {
+        const cudaError_t e = cudaEventQuery(j->stop);
+        if (e == cudaSuccess)
+            return DXMC_OK;
+        if (e != cudaErrorNotReady)
+            return cuda_fail(ctx, e, "job wait");
+        if (timeout_ms >= 0) {
+            const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+            if (ms >= timeout_ms)
+                return fail(ctx, DXMC_ERR_TIMEOUT, "job wait timed out");
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+}
+
+int dxmc_gpu_job_cancel(dxmc_job* j)
+{
+    if (!j)
+        return DXMC_ERR_INVALID;
+    *reinterpret_cast<volatile int*>(j->cancel_host) = 1;
+    j->cancelled = true;
+    return DXMC_OK;
+}
+
+int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double* dose, double* variance, uint32_t* n_events, dxmc_job_stats* stats)
+{
+    if (!j || output_mode < 0 || output_mode > 2)
+        return DXMC_ERR_INVALID;
+    dxmc_gpu_ctx* ctx = j->ctx;
+    const int wrc = dxmc_gpu_job_wait(j, -1);
+    if (wrc != DXMC_OK)
+        return wrc;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    if (!j->tally && !j->tally_f32)
+        return fail(ctx, DXMC_ERR_STATE, "job results were already released");
+    dev::JobCounters c {};
+    DXMC_CUDA(ctx, cudaMemcpyAsync(&c, j->counters, sizeof(c), cudaMemcpyDeviceToHost, s));
+    DXMC_CUDA(ctx, cudaStreamSynchronize(s));
+    const uint64_t nv = j->world->params.n_voxels;
+    if (stats) {
+        stats->histories = c.histories_done;
+        stats->steps = c.steps;
+        stats->deposits = c.deposits;
+        stats->rejection_overflows = c.overflows;
+        float ms = 0, jms = 0;
+        cudaEventElapsedTime(&ms, j->start, j->stop);
+        cudaEventElapsedTime(&jms, j->begin, j->stop);
+        stats->kernel_ms = ms;
+        stats->job_ms = jms;
+    }
+    if (j->cancelled) {
+        // transport.hpp:176-185: a cancelled run reports zeros
+        if (dose)
+            std::memset(dose, 0, nv * sizeof(double));
+        if (variance)
+            std::memset(variance, 0, nv * sizeof(double));
+        if (n_events)
+            std::memset(n_events, 0, nv * sizeof(uint32_t));
+        return fail(ctx, DXMC_ERR_CANCELLED, "job was cancelled");
+    }
+    if (dose || variance) {
+        double* d_out = nullptr;
+        const uint64_t out_elems = (dose ? nv : 0) + (variance ? nv : 0);
+        DXMC_CUDA(ctx, cudaMallocAsync(&d_out, out_elems * sizeof(double), s));
+        double* d_dose = dose ? d_out : nullptr;
+        double* d_var = variance ? d_out + (dose ? nv : 0) : nullptr;
+        const double vv = j->world->spacing[0] * j->world->spacing[1] * j->world->spacing[2] / 1000.0;
+        cudaError_t e;
+        if (j->tally_mode == 1)
+            e = dev::launch_postprocess_f32(j->tally_f32, j->n_events, j->world->voxels, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, s);
+        else
+            e = dev::launch_postprocess(j->tally, j->n_events, j->world->voxels, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, s);
+        if (e == cudaSuccess && dose)
+            e = cudaMemcpyAsync(dose, d_dose, nv * sizeof(double), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && variance)
+            e = cudaMemcpyAsync(variance, d_var, nv * sizeof(double), cudaMemcpyDeviceToHost, s);
+        cudaFreeAsync(d_out, s);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "result post-processing");
+    }
+    if (n_events)
+        DXMC_CUDA(ctx, cudaMemcpyAsync(n_events, j->n_events, nv * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    DXMC_CUDA(ctx, cudaStreamSynchronize(s));
+    if (c.overflows)
+        return fail(ctx, DXMC_ERR_REJECTION_CAP, "sampling loops hit the rejection cap in " + std::to_string(c.overflows) + " events");
+    return DXMC_OK;
+}
+
+void dxmc_gpu_job_free(dxmc_job* j)
+{
+    if (!j)
+        return;
+    dxmc_gpu_ctx* ctx = j->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    free_job_device(j);
+    cudaStreamSynchronize(ctx->stream);
+    if (j->cancel_host)
+        cudaFreeHost(j->cancel_host);
+    if (j->begin)
+        cudaEventDestroy(j->begin);
+    if (j->start)
+        cudaEventDestroy(j->start);
+    if (j->stop)
+        cudaEventDestroy(j->stop);
+    ctx->in_use -= j->bytes;
+    delete j;
+}
+
+int dxmc_gpu_probe_lut(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, const double* energies, int n, double* out_att, double* out_maxinv)
+{
+    if (!ctx || !lut || !energies || n <= 0 || !out_att || !out_maxinv || material < 0 || material >= lut->meta.n_materials)
+        return DXMC_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    double* buf = nullptr;
+    DXMC_CUDA(ctx, cudaMallocAsync(&buf, static_cast<size_t>(n) * 5 * sizeof(double), s));
+    DXMC_CUDA(ctx, cudaMemcpyAsync(buf, energies, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    DXMC_CUDA(ctx, dev::launch_probe_lut(lut->image, lut->meta, material, buf, n, buf + n, buf + 4 * static_cast<size_t>(n), s));
+    DXMC_CUDA(ctx, cudaMemcpyAsync(out_att, buf + n, 3 * static_cast<size_t>(n) * sizeof(double), cudaMemcpyDeviceToHost, s));
+    DXMC_CUDA(ctx, cudaMemcpyAsync(out_maxinv, buf + 4 * static_cast<size_t>(n), n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    cudaFreeAsync(buf, s);
+    DXMC_CUDA(ctx, cudaStreamSynchronize(s));
+    return DXMC_OK;
+}
+
+int dxmc_gpu_probe_interactions(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, int model, int kind, double energy, uint64_t n, uint64_t seed,
+    float* out_cos, float* out_energy, float* out_dep)
+{
+    if (!ctx || !lut || n == 0 || !out_cos || !out_energy || !out_dep || material < 0 || material >= lut->meta.n_materials || model < 0 || model > 2 || kind < 0 || kind > 2 || !(energy > 0))
+        return DXMC_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    float* buf = nullptr;
+    DXMC_CUDA(ctx, cudaMallocAsync(&buf, n * 3 * sizeof(float), s));
+    DXMC_CUDA(ctx, dev::launch_probe_interactions(lut->image, lut->meta, material, model, kind, static_cast<float>(energy), n, seed, buf, buf + n, buf + 2 * n, s));
+    DXMC_CUDA(ctx, cudaMemcpyAsync(out_cos, buf, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+    DXMC_CUDA(ctx, cudaMemcpyAsync(out_energy, buf + n, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+    DXMC_CUDA(ctx, cudaMemcpyAsync(out_dep, buf + 2 * n, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+    cudaFreeAsync(buf, s);
+    DXMC_CUDA(ctx, cudaStreamSynchronize(s));
+    return DXMC_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,230 @@
+// Host-only entry points of the C ABI (no CUDA calls): project physics
+// materials, LUT build and introspection, spectrum alias tables.
+#include "dxmc_gpu.h"
+
+#include "../physics/physics_model.hpp"
+#include "lut_builder.hpp"
+#include "../kernels/philox.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <string>
+
+namespace phys = dxmc_gb300::physics;
+namespace host = dxmc_gb300::host;
+
+namespace {
+
+struct PhysicsMaterial {
+    phys::Composition composition;
+};
+
+PhysicsMaterial* pm(void* u) { return static_cast<PhysicsMaterial*>(u); }
+
+double cb_photo(void* u, double e) { return phys::mass_attenuation_photo(pm(u)->composition, e); }
+double cb_compton(void* u, double e) { return phys::mass_attenuation_compton(pm(u)->composition, e); }
+double cb_rayleigh(void* u, double e) { return phys::mass_attenuation_rayleigh(pm(u)->composition, e); }
+double cb_ff2(void* u, double q) { return phys::form_factor_squared(pm(u)->composition, q); }
+double cb_sf(void* u, double q) { return phys::normalized_scatter_factor(pm(u)->composition, q); }
+int cb_edges(void* u, double minE, double* out, int cap)
+{
+    const auto e = phys::binding_energies(pm(u)->composition, minE);
+    const int n = static_cast<int>(e.size());
+    for (int i = 0; i < std::min(n, cap); ++i)
+        out[i] = e[i];
+    return n;
+}
+void cb_shells(void* u, dxmc_shell_config out[12])
+{
+    const auto s = phys::electron_configuration(pm(u)->composition);
+    for (int i = 0; i < 12; ++i) {
+        out[i].binding_energy = s[i].bindingEnergy;
+        out[i].number_electrons = s[i].numberElectrons;
+        out[i].hartree_fock_j0 = s[i].hartreeFockOrbital_0;
+        out[i].photo_ionization_probability = s[i].photoIonizationProbability;
+        out[i].fluorescence_yield = s[i].fluorescenceYield;
+        for (int k = 0; k < 3; ++k) {
+            out[i].line_probabilities[k] = s[i].fluorLineProbabilities[k];
+            out[i].line_energies[k] = s[i].fluorLineEnergies[k];
+        }
+        out[i].Z = s[i].Z;
+        out[i].shell = s[i].shell;
+    }
+}
+
+void fill_provider(PhysicsMaterial* m, double density, dxmc_material_provider* out)
+{
+    out->user = m;
+    out->standard_density = density;
+    out->photoelectric = cb_photo;
+    out->compton = cb_compton;
+    out->rayleigh = cb_rayleigh;
+    out->form_factor_squared = cb_ff2;
+    out->scatter_factor = cb_sf;
+    out->binding_energies = cb_edges;
+    out->shells = cb_shells;
+}
+
+bool provider_ok(const dxmc_material_provider& p)
+{
+    return p.photoelectric && p.compton && p.rayleigh && p.form_factor_squared && p.scatter_factor && p.binding_energies && p.shells;
+}
+
+} // namespace
+
+extern "C" {
+
+int dxmc_gpu_abi_version(void) { return DXMC_GPU_ABI_VERSION; }
+
+int dxmc_physics_material(const char* name, double density, dxmc_material_provider* out)
+{
+    if (!name || !out)
+        return DXMC_ERR_INVALID;
+    phys::Composition c;
+    double standard = -1;
+    const std::string n(name);
+    if (!phys::named_material(n, c, standard)) {
+        if (!phys::parse_formula(n, c))
+            return DXMC_ERR_INVALID;
+        if (c.Z.size() == 1)
+            standard = phys::element(c.Z[0]).density;
+    }
+    const double d = density > 0 ? density : standard;
+    if (!(d > 0))
+        return DXMC_ERR_INVALID; // like Material::isValid without a density (material.hpp:64)
+    auto* m = new (std::nothrow) PhysicsMaterial { c };
+    if (!m)
+        return DXMC_ERR_OOM;
+    fill_provider(m, d, out);
+    return DXMC_OK;
+}
+
+int dxmc_physics_element_material(int Z, dxmc_material_provider* out)
+{
+    if (Z < 1 || Z > phys::MAX_Z || !out)
+        return DXMC_ERR_INVALID;
+    return dxmc_physics_material(phys::element(Z).symbol.c_str(), -1, out);
+}
+
+void dxmc_physics_material_free(dxmc_material_provider* provider)
+{
+    if (provider && provider->user) {
+        delete pm(provider->user);
+        provider->user = nullptr;
+    }
+}
+
+int dxmc_lut_build_max_density(const dxmc_material_provider* materials, int n_materials,
+    const double* max_density, double max_energy, dxmc_lut_blob** out)
+{
+    if (!materials || n_materials <= 0 || n_materials > 255 || !max_density || !out)
+        return DXMC_ERR_INVALID;
+    std::vector<host::MaterialData> mats;
+    for (int i = 0; i < n_materials; ++i) {
+        if (!provider_ok(materials[i]))
+            return DXMC_ERR_INVALID;
+        mats.push_back(host::MaterialData { &materials[i] });
+    }
+    auto* blob = new (std::nothrow) dxmc_lut_blob;
+    if (!blob)
+        return DXMC_ERR_OOM;
+    const std::vector<double> md(max_density, max_density + n_materials);
+    const int rc = host::build_lut(mats, md, max_energy, *blob);
+    if (rc != DXMC_OK) {
+        delete blob;
+        return rc;
+    }
+    *out = blob;
+    return DXMC_OK;
+}
+
+int dxmc_lut_build(const dxmc_material_provider* materials, int n_materials,
+    const float* density, const uint8_t* material, uint64_t n_voxels,
+    double max_energy, dxmc_lut_blob** out)
+{
+    if (!density || !material || n_voxels == 0 || n_materials <= 0 || n_materials > 255)
+        return DXMC_ERR_INVALID;
+    std::vector<double> md(n_materials, 0.0);
+    for (uint64_t i = 0; i < n_voxels; ++i) {
+        const int m = material[i];
+        if (m < n_materials)
+            md[m] = std::max(md[m], static_cast<double>(density[i]));
+    }
+    return dxmc_lut_build_max_density(materials, n_materials, md.data(), max_energy, out);
+}
+
+void dxmc_lut_blob_free(dxmc_lut_blob* blob) { delete blob; }
+
+int dxmc_lut_attenuation(const dxmc_lut_blob* blob, int material, double energy, double out[3])
+{
+    if (!blob || material < 0 || material >= blob->n_materials || !out)
+        return DXMC_ERR_INVALID;
+    const auto a = host::lut_attenuation(*blob, material, energy);
+    out[0] = a[0];
+    out[1] = a[1];
+    out[2] = a[2];
+    return DXMC_OK;
+}
+
+double dxmc_lut_max_attenuation_inverse(const dxmc_lut_blob* blob, double energy)
+{
+    return blob ? host::lut_max_inverse(*blob, energy) : 0.0;
+}
+
+double dxmc_lut_scatter_factor(const dxmc_lut_blob* blob, int material, double q)
+{
+    if (!blob || material < 0 || material >= blob->n_materials)
+        return 0.0;
+    return host::lut_scatter_factor(*blob, material, q);
+}
+
+int dxmc_lut_get_info(const dxmc_lut_blob* blob, dxmc_lut_info* info)
+{
+    if (!blob || !info)
+        return DXMC_ERR_INVALID;
+    std::memset(info, 0, sizeof(*info));
+    info->n_materials = blob->n_materials;
+    info->n_energy = static_cast<int32_t>(blob->resolution());
+    info->linear_index = static_cast<int32_t>(blob->linear_index);
+    info->linear_step = blob->linear_step;
+    info->linear_energy = blob->linear_energy;
+    info->min_energy = blob->min_energy;
+    info->max_energy = blob->max_energy;
+    info->log_energy = blob->log_energy.data();
+    info->coefficients = blob->coefficients.data();
+    info->max_coefficients = blob->max_coefficients.data();
+    info->rita = blob->rita.empty() ? nullptr : blob->rita[0].data();
+    info->spline = blob->spline.empty() ? nullptr : blob->spline[0].data();
+    info->shells = blob->shells.empty() ? nullptr : blob->shells[0].data();
+    return DXMC_OK;
+}
+
+int dxmc_philox4x32_10(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4])
+{
+    if (!counter || !key || !out)
+        return DXMC_ERR_INVALID;
+    uint32_t c0 = counter[0], c1 = counter[1], c2 = counter[2], c3 = counter[3];
+    dxmc_gb300::philox4x32_10(c0, c1, c2, c3, key[0], key[1]);
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+    return DXMC_OK;
+}
+
+int dxmc_alias_table(const double* weights, int n, double* probs, uint64_t* alias)
+{
+    if (!weights || n <= 0 || !probs || !alias)
+        return DXMC_ERR_INVALID;
+    std::vector<double> w(weights, weights + n), p;
+    std::vector<std::uint64_t> a;
+    host::build_alias_table(w, p, a);
+    for (int i = 0; i < n; ++i) {
+        probs[i] = p[i];
+        alias[i] = a[i];
+    }
+    return DXMC_OK;
+}
+
+} // extern "C"

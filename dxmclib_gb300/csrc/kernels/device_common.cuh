@@ -1,0 +1,251 @@
+// Device-side data layouts, counter-based RNG and table lookups shared by the
+// transport kernel, the probe kernels and the post-processing kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "philox.hpp"
+
+namespace dxmc_gb300::dev {
+
+// ---------------------------------------------------------------------------
+// Layouts in HBM
+// ---------------------------------------------------------------------------
+
+// One voxel: density, material index and forced-interaction flag packed into
+// one 8-byte word so a Woodcock step needs a single 32-byte-sector gather.
+struct alignas(8) Voxel {
+    float density;
+    std::uint8_t material;
+    std::uint8_t measurement;
+    std::uint16_t pad;
+};
+static_assert(sizeof(Voxel) == 8, "voxel must pack into 8 bytes");
+
+// One exposure after Exposure::alignToDirectionCosines (exposure.hpp:268-278).
+struct alignas(16) DevExposure {
+    float pos[3];
+    float weight;
+    float cosx[3];
+    float mono_energy;
+    float cosy[3];
+    float pad0;
+    float beam[3];
+    float pad1;
+    float coll[4]; // x0, x1, y0, y1
+};
+static_assert(sizeof(DevExposure) == 80, "exposure record is 80 bytes");
+
+// Float LUT image: one contiguous buffer so a block can stage it into shared
+// memory with a single cooperative copy.  Offsets are in floats.
+struct LutMeta {
+    int n_materials;
+    int R;           // energy nodes / segments
+    int linear_index;
+    int total_floats;
+    float linear_step;
+    float inv_linear_step;
+    float linear_energy;
+    float max_energy;
+    int off_x;       // R log10 energies
+    int off_coef;    // n_materials * R * 6
+    int off_maxcoef; // R * 2
+    int off_rita;    // n_materials * 4 * 56 (x, e, a, b)
+    int off_spline;  // n_materials * 64 (60 coefficients, start, step, stop, pad)
+    int off_shells;  // n_materials * 12 * SHELL_FLOATS
+    int pad0, pad1;
+};
+
+constexpr int RITA_N = 56;
+constexpr int SPLINE_N = 16;
+constexpr int SPLINE_FLOATS = 64;
+constexpr int SHELL_FLOATS = 12; // binding, nElectrons, J0, photoProb, yield, lineP[3], lineE[3], pad
+constexpr int N_SHELLS = 12;
+
+constexpr float KEV_TO_ANGSTROM = 12.398520f;
+constexpr float ELECTRON_REST_MASS = 510.9989461f;
+constexpr float PI_F = 3.14159265358979f;
+constexpr float ENERGY_CUTOFF = 1.0f;           // transport.hpp:827-830
+constexpr float ROULETTE_THRESHOLD = 5.0f;      // transport.hpp:823-826
+constexpr float ROULETTE_PROBABILITY = 0.8f;    // transport.hpp:819-822
+constexpr float N_ERROR = 1.0e-9f;              // transport.hpp:831-834
+constexpr int REJECTION_CAP = 4096;             // iteration cap on every sampling loop
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): counter-based, one
+// independent stream per (seed, history) pair.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1)
+{
+    dxmc_gb300::philox4x32_10(c.x, c.y, c.z, c.w, k0, k1);
+    return c;
+}
+
+struct Rng {
+    uint4 buf;
+    uint32_t k0, k1;
+    uint32_t hist_lo, hist_hi;
+    uint32_t block;
+    uint32_t left;
+
+    __device__ void init(uint64_t seed, uint64_t history)
+    {
+        k0 = static_cast<uint32_t>(seed);
+        k1 = static_cast<uint32_t>(seed >> 32);
+        hist_lo = static_cast<uint32_t>(history);
+        hist_hi = static_cast<uint32_t>(history >> 32);
+        block = 0;
+        left = 0;
+    }
+    __device__ __forceinline__ uint32_t next()
+    {
+        if (left == 0) {
+            buf = philox4x32_10(make_uint4(block++, hist_lo, hist_hi, 0x44584d43u), k0, k1);
+            left = 4;
+        }
+        const uint32_t r = buf.x;
+        buf.x = buf.y;
+        buf.y = buf.z;
+        buf.z = buf.w;
+        --left;
+        return r;
+    }
+    // [0, 1) with 24 random bits
+    __device__ __forceinline__ float uniform() { return static_cast<float>(next() >> 8) * 0x1p-24f; }
+    // (0, 1] for logarithms
+    __device__ __forceinline__ float uniform_open() { return static_cast<float>((next() >> 8) + 1u) * 0x1p-24f; }
+    // integer in [0, n) by the multiply-high method (Lemire)
+    __device__ __forceinline__ uint32_t below(uint32_t n) { return __umulhi(next(), n); }
+};
+
+// ---------------------------------------------------------------------------
+// Math helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float exp10_fast(float y) { return exp2f(y * 3.32192809488736f); }
+
+// vectormath::rotate (vectormath.hpp:83-99): Rodrigues rotation about a (not
+// necessarily unit) axis.
+__device__ __forceinline__ void rotate(float& vx, float& vy, float& vz, float ax, float ay, float az, float angle)
+{
+    float s, c;
+    sincosf(angle, &s, &c);
+    const float midt = (1.0f - c) * (vx * ax + vy * ay + vz * az);
+    const float ox = c * vx + midt * ax + s * (ay * vz - az * vy);
+    const float oy = c * vy + midt * ay + s * (-ax * vz + az * vx);
+    const float oz = c * vz + midt * az + s * (ax * vy - ay * vx);
+    vx = ox;
+    vy = oy;
+    vz = oz;
+}
+
+// vectormath::peturb (vectormath.hpp:197-221), including its quirk: the
+// orthogonal axis cross(vec, e_k) is never normalised, so |dir| shrinks after
+// every direction change exactly as in the reference.  Takes cos(theta).
+__device__ __forceinline__ void peturb(float& vx, float& vy, float& vz, float cos_theta, float phi)
+{
+    const float ax = fabsf(vx), ay = fabsf(vy), az = fabsf(vz);
+    const int k = ax <= ay ? (ax <= az ? 0 : 2) : (ay <= az ? 1 : 2);
+    // cross(vec, e_k)
+    float ux, uy, uz;
+    if (k == 0) {
+        ux = 0.0f;
+        uy = vz;
+        uz = -vy;
+    } else if (k == 1) {
+        ux = -vz;
+        uy = 0.0f;
+        uz = vx;
+    } else {
+        ux = vy;
+        uy = -vx;
+        uz = 0.0f;
+    }
+    rotate(ux, uy, uz, vx, vy, vz, phi);
+    const float st = sqrtf(fmaxf(0.0f, 1.0f - cos_theta * cos_theta));
+    vx = vx * cos_theta + ux * st;
+    vy = vy * cos_theta + uy * st;
+    vz = vz * cos_theta + uz * st;
+}
+
+// ---------------------------------------------------------------------------
+// LUT lookups (attenuationinterpolator.hpp:207-248, attenuationlut.hpp:124-204,
+// interpolation.hpp:169-176, dxmcrandom.hpp:483-500)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int upper_bound_f(const float* x, int n, float v)
+{
+    int lo = 0, count = n;
+    while (count > 0) {
+        const int step = count >> 1;
+        if (!(v < x[lo + step])) {
+            lo += step + 1;
+            count -= step + 1;
+        } else {
+            count = step;
+        }
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int lut_segment(const float* L, const LutMeta& m, float logE)
+{
+    if (logE > m.linear_energy) {
+        const int idx = static_cast<int>((logE - m.linear_energy) * m.inv_linear_step) + m.linear_index;
+        return min(idx, m.R - 1);
+    }
+    const int pos = upper_bound_f(L + m.off_x, m.R, logE);
+    return pos < m.R ? pos : m.R - 1;
+}
+
+__device__ __forceinline__ void lut_attenuation(const float* L, const LutMeta& m, int material, float logE, int seg, float& photo, float& compt, float& rayl)
+{
+    const float2* c = reinterpret_cast<const float2*>(L + m.off_coef + (material * m.R + seg) * 6);
+    const float2 p = c[0], q = c[1], r = c[2];
+    photo = exp10_fast(fmaf(p.y, logE, p.x));
+    compt = exp10_fast(fmaf(q.y, logE, q.x));
+    rayl = exp10_fast(fmaf(r.y, logE, r.x));
+}
+
+__device__ __forceinline__ float lut_max_inverse(const float* L, const LutMeta& m, float logE, int seg)
+{
+    const float2 c = reinterpret_cast<const float2*>(L + m.off_maxcoef)[seg];
+    return exp10_fast(fmaf(c.y, logE, c.x));
+}
+
+__device__ __forceinline__ float lut_scatter_factor(const float* L, const LutMeta& m, int material, float q)
+{
+    const float* s = L + m.off_spline + material * SPLINE_FLOATS;
+    const float start = s[60], step = s[61], stop = s[62];
+    const float x = fminf(fmaxf(q, start), stop);
+    const int index = x > start ? static_cast<int>((x - start) / step) : 0;
+    const int off = index < SPLINE_N - 1 ? index * 4 : (SPLINE_N - 2) * 4;
+    return s[off] + s[off + 1] * x + s[off + 2] * x * x + s[off + 3] * x * x * x;
+}
+
+// RITA::operator()(state, maxValue): truncated rational inverse transform.
+// Returns false if the rejection cap is hit.
+__device__ __forceinline__ bool rita_sample(const float* L, const LutMeta& m, int material, float max_value, Rng& rng, float& out)
+{
+    const float* x = L + m.off_rita + material * 4 * RITA_N;
+    const float* e = x + RITA_N;
+    const float* a = e + RITA_N;
+    const float* b = a + RITA_N;
+    const int ub = upper_bound_f(x, RITA_N, max_value);
+    const float modifier = ub < RITA_N ? e[ub] : 1.0f;
+    for (int it = 0; it < REJECTION_CAP; ++it) {
+        const float r1 = rng.uniform() * modifier;
+        int i = upper_bound_f(e, RITA_N, r1) - 1;
+        i = min(max(i, 0), RITA_N - 2);
+        const float v = r1 - e[i];
+        const float d = e[i + 1] - e[i];
+        const float res = x[i] + (1.0f + a[i] + b[i]) * d * v / (d * d + a[i] * d * v + b[i] * v * v) * (x[i + 1] - x[i]);
+        if (!(res > max_value)) {
+            out = res;
+            return true;
+        }
+    }
+    out = 0.0f;
+    return false;
+}
+
+} // namespace dxmc_gb300::dev

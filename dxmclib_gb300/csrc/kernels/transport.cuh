@@ -1,0 +1,75 @@
+// Parameters of the photon-transport kernels and the host-side launchers.
+#pragma once
+
+#include "device_common.cuh"
+
+namespace dxmc_gb300::dev {
+
+struct WorldParams {
+    const Voxel* voxels;
+    uint32_t dims[3];
+    uint32_t pad;
+    float lo[3];          // nextafter-safe lower extent (world.hpp:55-68)
+    float hi[3];          // nextafter-safe upper extent
+    float inv_spacing[3]; // 1 / spacing (mm)
+    uint64_t nxy;
+    uint64_t n_voxels;
+};
+
+struct SourceParams {
+    const DevExposure* exposures;
+    const uint64_t* history_offsets; // n_exposures + 1 prefix sums
+    uint32_t n_exposures;
+    int spec_n;                      // 0: monoenergetic
+    const float* spec_energy;
+    const float* spec_prob;
+    const uint32_t* spec_alias;
+    const float* heel_weights;       // nullptr: no heel
+    float heel_e_start, heel_e_step;
+    int heel_e_size, heel_a_size;
+    float heel_a_start, heel_a_step;
+    const float* bowtie_angle;       // nullptr: no bow-tie
+    const float* bowtie_weight;
+    int bowtie_n;
+    int pad;
+};
+
+// Counters shared by all blocks of one job (device scratch).
+struct JobCounters {
+    unsigned long long next_history;   // work queue head
+    unsigned long long histories_done;
+    unsigned long long steps;          // Woodcock steps inside the grid
+    unsigned long long deposits;       // depositing events
+    unsigned long long overflows;      // rejection-cap hits
+    unsigned long long pad[3];
+};
+
+struct TransportParams {
+    WorldParams world;
+    SourceParams source;
+    const float* lut;   // global LUT image
+    LutMeta lut_meta;
+    double* tally;      // interleaved (energy, energy^2) per voxel, FP64
+    float* tally_f32;   // interleaved, FP32 tally mode
+    uint32_t* n_events;
+    JobCounters* counters;
+    const volatile int* cancel; // host-mapped flag, may be null
+    uint64_t total_histories;
+    uint64_t seed;
+    int tally_mode;
+    int lut_in_smem;
+};
+
+// Launchers (defined in transport_kernels.cu).
+cudaError_t launch_transport(const TransportParams& p, int model, int grid, int block, size_t smem, cudaStream_t stream);
+int transport_max_blocks_per_sm(int model, int block, size_t smem);
+cudaError_t launch_postprocess(const double* tally, const uint32_t* n_events, const Voxel* voxels, uint64_t n,
+    int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream);
+cudaError_t launch_postprocess_f32(const float* tally, const uint32_t* n_events, const Voxel* voxels, uint64_t n,
+    int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream);
+cudaError_t launch_max_density(const Voxel* voxels, uint64_t n, unsigned int* out_bits, int n_materials, cudaStream_t stream);
+cudaError_t launch_probe_lut(const float* lut, LutMeta meta, int material, const double* energies, int n, double* out_att, double* out_maxinv, cudaStream_t stream);
+cudaError_t launch_probe_interactions(const float* lut, LutMeta meta, int material, int model, int kind, float energy,
+    uint64_t n, uint64_t seed, float* out_cos, float* out_energy, float* out_dep, cudaStream_t stream);
+
+} // namespace dxmc_gb300::dev

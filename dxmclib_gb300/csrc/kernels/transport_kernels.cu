@@ -1,0 +1,839 @@
+// Photon-transport kernels for sm_103a.
+//
+// One persistent launch per job: every lane owns one photon history at a
+// time and, inside a warp-synchronous loop, performs one Woodcock step per
+// iteration.  Lanes whose history ended take the next history id from a
+// warp-local pool that one lane refills from a global work queue, so warps
+// stay full until the job runs dry.  Physics follows DXMClib's
+// Transport<T> (include/dxmc/transport.hpp) function by function; each
+// device function names the reference lines it restates.
+#include "transport.cuh"
+
+#include <algorithm>
+
+namespace dxmc_gb300::dev {
+
+namespace {
+
+    constexpr unsigned FULL_MASK = 0xffffffffu;
+    constexpr int WARP_POOL_CHUNK = 256; // histories fetched per queue access
+    constexpr uint32_t MAX_STEPS_PER_HISTORY = 1u << 20; // guard against unbounded histories
+
+    struct Photon {
+        float px, py, pz;
+        float dx, dy, dz;
+        float energy;
+        float weight;
+    };
+
+    // ---- scoring (transport.hpp:208-214, 598-609) ------------------------------
+    __device__ __forceinline__ void score(const TransportParams& p, uint64_t idx, float e)
+    {
+        if (p.tally_mode == 1) {
+            float* t = p.tally_f32 + 2 * idx;
+            atomicAdd(t, e);
+            atomicAdd(t + 1, e * e);
+        } else {
+            double* t = p.tally + 2 * idx;
+            const double ed = static_cast<double>(e);
+            atomicAdd(t, ed);
+            atomicAdd(t + 1, ed * ed);
+        }
+        atomicAdd(p.n_events + idx, 1u);
+    }
+
+    // Warp-aggregated scoring: lanes depositing into the same voxel in the same
+    // iteration are combined by __match_any_sync and one leader issues the
+    // atomics (FP32 partial sums flushed to the FP64 accumulators).
+    __device__ __forceinline__ void score_aggregated(const TransportParams& p, unsigned active, uint64_t idx, float e)
+    {
+        const unsigned peers = __match_any_sync(active, idx);
+        const int leader = __ffs(peers) - 1;
+        const int lane = threadIdx.x & 31;
+        float sum = 0.0f, sum2 = 0.0f;
+        unsigned count = 0;
+        // each peer group reduces over its members (group sizes are small)
+        for (unsigned m = peers; m; m &= m - 1) {
+            const int src = __ffs(m) - 1;
+            const float v = __shfl_sync(peers, e, src);
+            sum += v;
+            sum2 += v * v;
+            ++count;
+        }
+        if (lane == leader) {
+            double* t = p.tally + 2 * idx;
+            atomicAdd(t, static_cast<double>(sum));
+            atomicAdd(t + 1, static_cast<double>(sum2));
+            atomicAdd(p.n_events + idx, count);
+        }
+    }
+
+    // ---- photoelectric (transport.hpp:216-263) ---------------------------------
+    template <int MODEL>
+    __device__ __forceinline__ float photo_absorption(const float* L, const LutMeta& m, Photon& ph, int material, Rng& rng)
+    {
+        const float E = ph.energy;
+        ph.energy = 0.0f;
+        if constexpr (MODEL < 2) {
+            return E;
+        } else {
+            const float* shells = L + m.off_shells + material * N_SHELLS * SHELL_FLOATS;
+            float total = 0.0f;
+#pragma unroll
+            for (int s = 0; s < N_SHELLS; ++s)
+                total += E > shells[s * SHELL_FLOATS] ? shells[s * SHELL_FLOATS + 3] : 0.0f;
+            const float sample = total * rng.uniform();
+            float cum = 0.0f;
+            int idx = 0;
+            for (int s = 0; s < N_SHELLS; ++s) {
+                cum += E > shells[s * SHELL_FLOATS] ? shells[s * SHELL_FLOATS + 3] : 0.0f;
+                idx = s;
+                if (!(cum < sample) || s == N_SHELLS - 1)
+                    break;
+            }
+            const float* sh = shells + idx * SHELL_FLOATS;
+            const float binding = sh[0];
+            if (binding > E || binding < ENERGY_CUTOFF)
+                return E;
+            const float r1 = rng.uniform();
+            if (r1 <= sh[4]) {
+                int line = 0;
+                float r3 = rng.uniform() - sh[5];
+                while (r3 > 0.0f && line < 2) {
+                    ++line;
+                    r3 -= sh[5 + line];
+                }
+                ph.energy = sh[8 + line];
+                const float theta = rng.uniform() * PI_F;
+                const float phi = rng.uniform() * (2.0f * PI_F);
+                peturb(ph.dx, ph.dy, ph.dz, cosf(theta), phi);
+                return E - ph.energy;
+            }
+            return E;
+        }
+    }
+
+    // ---- Rayleigh (transport.hpp:264-298) ---------------------------------------
+    template <int MODEL>
+    __device__ __forceinline__ bool rayleigh_scatter(const float* L, const LutMeta& m, Photon& ph, int material, Rng& rng)
+    {
+        if constexpr (MODEL == 0) {
+            constexpr float extreme = 1.08866210790363f; // 4 sqrt(2) / (3 sqrt(3))
+            for (int it = 0; it < REJECTION_CAP; ++it) {
+                const float r1 = rng.uniform() * extreme;
+                const float theta = rng.uniform() * PI_F;
+                float s, c;
+                sincosf(theta, &s, &c);
+                if (!(r1 > (2.0f - s * s) * s)) {
+                    const float phi = rng.uniform() * (2.0f * PI_F);
+                    peturb(ph.dx, ph.dy, ph.dz, c, phi);
+                    return true;
+                }
+            }
+            return false;
+        } else {
+            const float qmax = ph.energy * (1.0f / KEV_TO_ANGSTROM);
+            const float qmax2 = qmax * qmax;
+            const float invE = KEV_TO_ANGSTROM / ph.energy;
+            for (int it = 0; it < REJECTION_CAP; ++it) {
+                float q2;
+                if (!rita_sample(L, m, material, qmax2, rng, q2))
+                    return false;
+                const float cosA = 1.0f - 2.0f * q2 * invE * invE;
+                if (!((1.0f + cosA * cosA) * 0.5f < rng.uniform())) {
+                    const float phi = rng.uniform() * (2.0f * PI_F);
+                    peturb(ph.dx, ph.dy, ph.dz, cosA, phi);
+                    return true;
+                }
+            }
+            return false;
+        }
+    }
+
+    // ---- Compton, impulse approximation (transport.hpp:342-483) -----------------
+    __device__ __forceinline__ bool compton_ia(const float* L, const LutMeta& m, Photon& ph, int material, Rng& rng, float& deposit)
+    {
+        const float* shells = L + m.off_shells + material * N_SHELLS * SHELL_FLOATS;
+        float total = 0.0f;
+#pragma unroll
+        for (int s = 0; s < N_SHELLS; ++s)
+            total += (shells[s * SHELL_FLOATS] < ph.energy && shells[s * SHELL_FLOATS + 2] > 0.0f) ? shells[s * SHELL_FLOATS + 1] : 0.0f;
+        const float sample = total * rng.uniform();
+        float cum = 0.0f;
+        int shell = 0;
+        for (int s = 0; s < N_SHELLS; ++s) {
+            cum += (shells[s * SHELL_FLOATS] < ph.energy && shells[s * SHELL_FLOATS + 2] > 0.0f) ? shells[s * SHELL_FLOATS + 1] : 0.0f;
+            shell = s;
+            if (!(cum < sample) || s == N_SHELLS - 1)
+                break;
+        }
+        const float* sh = shells + shell * SHELL_FLOATS;
+        const float U = sh[0] / ELECTRON_REST_MASS;
+        const float pU = sqrtf(2.0f * U + U * U);
+        const float J0 = sh[2];
+        const float k = ph.energy / ELECTRON_REST_MASS;
+        if (U > k) {
+            deposit = 0.0f; // interaction rejected (corrects the cross section)
+            return true;
+        }
+        const float emin = 1.0f / (1.0f + 2.0f * k);
+        const float gmax_inv = 1.0f / (1.0f / emin + emin);
+        constexpr float sp2 = 2.50662827463100f; // 1 / (1/sqrt(pi) / sqrt(2)) = sqrt(2 pi)
+        constexpr float a1 = 0.34802f, a2 = -0.0958798f, a3 = 0.7478556f;
+        const float sqrte = 1.64872127070013f;
+        float e = 1.0f, cosA = 1.0f;
+        bool accepted = false;
+        for (int it = 0; it < REJECTION_CAP && !accepted; ++it) {
+            const float r1 = rng.uniform();
+            e = r1 + (1.0f - r1) * emin;
+            const float t = (1.0f - e) / (k * e);
+            const float sin2 = t * (2.0f - t);
+            cosA = 1.0f - t;
+            const float g = (1.0f / e + e - sin2) * gmax_inv;
+            const float r2 = rng.uniform();
+            if (r2 > g)
+                continue;
+            const float pi = (k * (k - U) * (1.0f - cosA) - U) / sqrtf(2.0f * k * (k - U) * (1.0f - cosA) + U * U);
+            const float kc = k * e;
+            const float qc = sqrtf(k * k + kc * kc - 2.0f * k * kc * cosA);
+            const float alpha = qc * (1.0f + kc * (kc - k * cosA) / (qc * qc)) / k;
+            const float b_part = 1.0f + 2.0f * J0 * fabsf(pi);
+            const float b = (b_part * b_part + 1.0f) * 0.5f;
+            const float expb = expf(-b);
+            float S;
+            if (pi <= -pU) {
+                S = (1.0f - alpha * pU) * expb * 0.5f;
+            } else if (pi < pU) {
+                const float part1 = alpha * sp2 / (4.0f * J0);
+                const float tp = 1.0f / (1.0f + 0.332673f * (1.0f + 2.0f * J0 * fabsf(pU)));
+                const float tpi = 1.0f / (1.0f + 0.332673f * (1.0f + 2.0f * J0 * fabsf(pi)));
+                const float part2p = sqrte - expb * tp * (a1 + a2 * tp + a3 * tp * tp);
+                const float part2pi = sqrte - expb * tpi * (a1 + a2 * tpi + a3 * tpi * tpi);
+                if (pi <= 0.0f)
+                    S = (1.0f - alpha * pi) * expb * 0.5f - part1 * (part2p - part2pi);
+                else
+                    S = 1.0f - (1.0f - alpha * pi) * expb * 0.5f - part1 * (part2p - part2pi);
+            } else {
+                S = 1.0f - (1.0f - alpha * pU) * expb * 0.5f;
+            }
+            const float r3 = rng.uniform();
+            if (r3 > S)
+                continue;
+            float Fmax;
+            if (pi <= -pU)
+                Fmax = 1.0f - alpha * pU;
+            else if (pi >= pU)
+                Fmax = 1.0f + alpha * pU;
+            else
+                Fmax = 1.0f + alpha * pi;
+            const float r4 = rng.uniform();
+            const float rbar2 = 2.0f * r4 * expb;
+            float pz;
+            if (rbar2 < 1.0f) {
+                const float part = sqrtf(1.0f - 2.0f * logf(rbar2));
+                pz = (1.0f - part) / (2.0f * J0) / ELECTRON_REST_MASS;
+            } else {
+                const float part = sqrtf(1.0f - 2.0f * logf(2.0f - rbar2));
+                pz = (part - 1.0f) / (2.0f * J0) / ELECTRON_REST_MASS;
+            }
+            float Fpz;
+            if (pz <= -pU)
+                Fpz = 1.0f - alpha * pU;
+            else if (pz >= pU)
+                Fpz = 1.0f + alpha * pU;
+            else
+                Fpz = 1.0f + alpha * pz;
+            const float r5 = rng.uniform();
+            if (r5 > Fpz / Fmax)
+                continue;
+            const float part = sqrtf(1.0f - 2.0f * e * cosA + e * e * (1.0f - pz * pz * sin2));
+            const float kbar = kc / (1.0f - pz * pz * e * e) * (1.0f - pz * pz * e * cosA + pz * part);
+            e = kbar / k;
+            accepted = true;
+        }
+        if (!accepted)
+            return false;
+        const float phi = rng.uniform() * (2.0f * PI_F);
+        peturb(ph.dx, ph.dy, ph.dz, cosA, phi);
+        const float E = ph.energy;
+        ph.energy *= e;
+        deposit = E - ph.energy;
+        return true;
+    }
+
+    // ---- Compton, Klein-Nishina with optional scatter factor (transport.hpp:300-340)
+    template <int MODEL>
+    __device__ __forceinline__ bool compton_scatter(const float* L, const LutMeta& m, Photon& ph, int material, Rng& rng, float& deposit)
+    {
+        if constexpr (MODEL == 2) {
+            return compton_ia(L, m, ph, material, rng, deposit);
+        } else {
+            const float E = ph.energy;
+            const float k = E / ELECTRON_REST_MASS;
+            const float emin = 1.0f / (1.0f + 2.0f * k);
+            const float gmax_inv = 1.0f / (1.0f / emin + emin);
+            for (int it = 0; it < REJECTION_CAP; ++it) {
+                const float r1 = rng.uniform();
+                const float e = r1 + (1.0f - r1) * emin;
+                const float t = (1.0f - e) / (k * e);
+                const float sin2 = t * (2.0f - t);
+                const float cosA = 1.0f - t;
+                const float g = (1.0f / e + e - sin2) * gmax_inv;
+                const float r2 = rng.uniform();
+                bool rejected;
+                if constexpr (MODEL == 1) {
+                    // momentumTransferFromCos (attenuationlut.hpp:175-179)
+                    const float q = E * (1.0f / KEV_TO_ANGSTROM) * sqrtf(fmaxf(0.5f - cosA * 0.5f, 0.0f));
+                    rejected = r2 > g * lut_scatter_factor(L, m, material, q);
+                } else {
+                    rejected = r2 > g;
+                }
+                if (!rejected) {
+                    const float phi = rng.uniform() * (2.0f * PI_F);
+                    peturb(ph.dx, ph.dy, ph.dz, cosA, phi);
+                    ph.energy = E * e;
+                    deposit = E - ph.energy;
+                    return true;
+                }
+            }
+            return false;
+        }
+    }
+
+    // ---- photon generation: Exposure::sampleParticle (exposure.hpp:280-304) -----
+    __device__ __forceinline__ void sample_particle(const SourceParams& s, const DevExposure& ex, Rng& rng, Photon& ph)
+    {
+        const float theta = ex.coll[0] + rng.uniform() * (ex.coll[1] - ex.coll[0]);
+        const float phi = ex.coll[2] + rng.uniform() * (ex.coll[3] - ex.coll[2]);
+        ph.px = ex.pos[0];
+        ph.py = ex.pos[1];
+        ph.pz = ex.pos[2];
+        ph.dx = ex.beam[0];
+        ph.dy = ex.beam[1];
+        ph.dz = ex.beam[2];
+        ph.weight = ex.weight;
+        rotate(ph.dx, ph.dy, ph.dz, ex.cosy[0], ex.cosy[1], ex.cosy[2], theta);
+        rotate(ph.dx, ph.dy, ph.dz, ex.cosx[0], ex.cosx[1], ex.cosx[2], phi);
+        if (s.spec_n > 0) {
+            // SpecterDistribution::sampleValue (dxmcrandom.hpp:322-326)
+            const float r = rng.uniform();
+            const uint32_t k = rng.below(static_cast<uint32_t>(s.spec_n));
+            const uint32_t idx = r < __ldg(s.spec_prob + k) ? k : __ldg(s.spec_alias + k);
+            if (idx + 1 < static_cast<uint32_t>(s.spec_n)) {
+                const float e0 = __ldg(s.spec_energy + idx), e1 = __ldg(s.spec_energy + idx + 1);
+                ph.energy = e0 + rng.uniform() * (e1 - e0);
+            } else {
+                ph.energy = __ldg(s.spec_energy + idx);
+            }
+        } else {
+            ph.energy = ex.mono_energy;
+        }
+        if (s.bowtie_angle) {
+            // BowTieFilter::sampleIntensityWeight (beamfilters.hpp:150-190)
+            const float angle = fabsf(theta);
+            int first = 0, last = s.bowtie_n - 1;
+            int it = first + (last - first) / 2;
+            while (it != first) {
+                if (angle < __ldg(s.bowtie_angle + it)) {
+                    last = it;
+                    it = first;
+                } else {
+                    first = it;
+                }
+                it += (last - first) / 2;
+            }
+            float w;
+            if (angle < __ldg(s.bowtie_angle + first))
+                w = __ldg(s.bowtie_weight);
+            else if (angle > __ldg(s.bowtie_angle + last))
+                w = __ldg(s.bowtie_weight + s.bowtie_n - 1);
+            else {
+                const float x0 = __ldg(s.bowtie_angle + first), x1 = __ldg(s.bowtie_angle + last);
+                const float y0 = __ldg(s.bowtie_weight + first), y1 = __ldg(s.bowtie_weight + last);
+                w = y0 + (angle - x0) * (y1 - y0) / (x1 - x0);
+            }
+            ph.weight *= w;
+        }
+        if (s.heel_weights) {
+            // HeelFilter::sampleIntensityWeight (beamfilters.hpp:514-538)
+            const float energy = ph.energy;
+            int e_index = static_cast<int>((energy - s.heel_e_start + 0.5f * s.heel_e_step) / s.heel_e_step);
+            if (e_index >= s.heel_e_size || e_index < 0)
+                e_index = e_index < 0 ? 0 : s.heel_e_size - 1;
+            if (energy < s.heel_e_start)
+                e_index = 0;
+            int a_index = static_cast<int>((phi - s.heel_a_start) / s.heel_a_step);
+            if (a_index >= s.heel_a_size || a_index < 0)
+                a_index = a_index < 0 ? 0 : s.heel_a_size - 1;
+            if (phi < s.heel_a_start)
+                a_index = 0;
+            const int w_index = e_index * s.heel_a_size + a_index;
+            float w;
+            if (a_index < s.heel_a_size - 1) {
+                const float a0 = s.heel_a_start + s.heel_a_step * a_index;
+                const float a1 = s.heel_a_start + s.heel_a_step * (a_index + 1);
+                const float w0 = __ldg(s.heel_weights + w_index), w1 = __ldg(s.heel_weights + w_index + 1);
+                w = w0 + (w1 - w0) * (phi - a0) / (a1 - a0);
+            } else {
+                w = __ldg(s.heel_weights + w_index);
+            }
+            ph.weight *= w;
+        }
+    }
+
+    __device__ __forceinline__ bool inside(const WorldParams& w, float x, float y, float z)
+    {
+        return (x > w.lo[0] && x < w.hi[0]) && (y > w.lo[1] && y < w.hi[1]) && (z > w.lo[2] && z < w.hi[2]);
+    }
+
+    // transportParticleToWorld (transport.hpp:702-728)
+    __device__ __forceinline__ bool transport_to_world(const WorldParams& w, Photon& ph)
+    {
+        if (inside(w, ph.px, ph.py, ph.pz))
+            return true;
+        float amin = -3.402823466e38f, amax = 3.402823466e38f;
+        const float pos[3] = { ph.px, ph.py, ph.pz };
+        const float dir[3] = { ph.dx, ph.dy, ph.dz };
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (fabsf(dir[i]) > N_ERROR) {
+                const float a0 = (w.lo[i] - pos[i]) / dir[i];
+                const float an = (w.hi[i] - pos[i]) / dir[i];
+                amin = fmaxf(amin, fminf(a0, an));
+                amax = fminf(amax, fmaxf(a0, an));
+            }
+        }
+        if (amin < amax && amin > 0.0f) {
+            ph.px += amin * ph.dx;
+            ph.py += amin * ph.dy;
+            ph.pz += amin * ph.dz;
+            return true;
+        }
+        return false;
+    }
+
+    __device__ __forceinline__ uint32_t find_exposure(const SourceParams& s, uint64_t h)
+    {
+        // last exposure whose offset <= h
+        uint32_t lo = 0, hi = s.n_exposures;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(s.history_offsets + mid) <= h)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        return lo;
+    }
+
+    __device__ __forceinline__ void load_exposure(const DevExposure* ptr, DevExposure& ex)
+    {
+        const float4* src = reinterpret_cast<const float4*>(ptr);
+        float4* dst = reinterpret_cast<float4*>(&ex);
+#pragma unroll
+        for (int i = 0; i < 5; ++i)
+            dst[i] = __ldg(src + i);
+    }
+
+    // ---- the transport kernel ----------------------------------------------------
+    template <int MODEL>
+    __global__ void __launch_bounds__(256) transport_kernel(const __grid_constant__ TransportParams p)
+    {
+        extern __shared__ float4 smem_f4[];
+        const float* L = p.lut;
+        if (p.lut_in_smem) {
+            float4* dst = smem_f4;
+            const float4* src = reinterpret_cast<const float4*>(p.lut);
+            const int n4 = (p.lut_meta.total_floats + 3) / 4;
+            for (int i = threadIdx.x; i < n4; i += blockDim.x)
+                dst[i] = __ldg(src + i);
+            __syncthreads();
+            L = reinterpret_cast<const float*>(smem_f4);
+        }
+        const LutMeta& m = p.lut_meta;
+        const WorldParams& w = p.world;
+        const int lane = threadIdx.x & 31;
+        const unsigned lanemask_lt = (1u << lane) - 1u;
+
+        Photon ph {};
+        Rng rng;
+        bool alive = false;
+        float maxInv = 0.0f, logE = 0.0f;
+        int seg = 0;
+        bool updateMax = true;
+        int cached_mat = -1;
+        uint32_t hist_steps = 0;
+        float att0 = 0.0f, att1 = 0.0f, att2 = 0.0f;
+        unsigned long long my_steps = 0, my_deposits = 0, my_overflows = 0, my_histories = 0;
+
+        // warp-uniform pool of history ids [pool_next, pool_end)
+        uint64_t pool_next = 0, pool_end = 0;
+        bool exhausted = false;
+
+        while (true) {
+            // ---- regenerate finished lanes from the warp pool ------------------------
+            const unsigned need = __ballot_sync(FULL_MASK, !alive && !exhausted);
+            if (need) {
+                if (pool_next >= pool_end) {
+                    unsigned long long base = 0;
+                    if (lane == 0) {
+                        const bool cancelled = p.cancel && *p.cancel;
+                        base = cancelled ? static_cast<unsigned long long>(p.total_histories) : atomicAdd(&p.counters->next_history, (unsigned long long)WARP_POOL_CHUNK);
+                    }
+                    base = __shfl_sync(FULL_MASK, base, 0);
+                    if (base >= p.total_histories) {
+                        exhausted = true;
+                    } else {
+                        pool_next = base;
+                        pool_end = min(static_cast<uint64_t>(base + WARP_POOL_CHUNK), p.total_histories);
+                    }
+                }
+                if (!exhausted) {
+                    const uint64_t avail = pool_end - pool_next;
+                    const unsigned rank = __popc(need & lanemask_lt);
+                    const bool mine = (need >> lane) & 1u;
+                    if (mine && rank < avail) {
+                        const uint64_t h = pool_next + rank;
+                        rng.init(p.seed, h);
+                        const uint32_t ei = find_exposure(p.source, h);
+                        DevExposure ex;
+                        load_exposure(p.source.exposures + ei, ex);
+                        sample_particle(p.source, ex, rng, ph);
+                        ++my_histories;
+                        alive = transport_to_world(w, ph);
+                        updateMax = true;
+                        cached_mat = -1;
+                        hist_steps = 0;
+                    }
+                    pool_next += min(static_cast<uint64_t>(__popc(need)), avail);
+                }
+            }
+            const unsigned stepping = __ballot_sync(FULL_MASK, alive);
+            if (exhausted && stepping == 0u)
+                break;
+
+            bool do_score = false;
+            float deposit = 0.0f; // energy imparted x weight to score
+            uint64_t vidx = 0;
+            if (alive) {
+                // ---- one Woodcock step (transport.hpp:650-699) ---------------------------
+                if (updateMax) {
+                    logE = __log10f(ph.energy);
+                    seg = lut_segment(L, m, logE);
+                    maxInv = lut_max_inverse(L, m, logE, seg);
+                    updateMax = false;
+                    cached_mat = -1;
+                }
+                const float step = -__logf(rng.uniform_open()) * maxInv * 10.0f; // cm -> mm
+                ph.px = fmaf(ph.dx, step, ph.px);
+                ph.py = fmaf(ph.dy, step, ph.py);
+                ph.pz = fmaf(ph.dz, step, ph.pz);
+                if (!inside(w, ph.px, ph.py, ph.pz)) {
+                    alive = false;
+                } else if (++hist_steps > MAX_STEPS_PER_HISTORY) {
+                    // bounded work per history: end it and report the overflow
+                    ++my_overflows;
+                    alive = false;
+                } else {
+                    const uint32_t ix = min(static_cast<uint32_t>((ph.px - w.lo[0]) * w.inv_spacing[0]), w.dims[0] - 1);
+                    const uint32_t iy = min(static_cast<uint32_t>((ph.py - w.lo[1]) * w.inv_spacing[1]), w.dims[1] - 1);
+                    const uint32_t iz = min(static_cast<uint32_t>((ph.pz - w.lo[2]) * w.inv_spacing[2]), w.dims[2] - 1);
+                    vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
+                    const uint2 raw = __ldg(reinterpret_cast<const uint2*>(w.voxels) + vidx);
+                    const float density = __uint_as_float(raw.x);
+                    const int mat = static_cast<int>(raw.y & 0xffu);
+                    const bool measured = ((raw.y >> 8) & 0xffu) != 0u;
+                    ++my_steps;
+                    if (mat != cached_mat) {
+                        lut_attenuation(L, m, mat, logE, seg, att0, att1, att2);
+                        cached_mat = mat;
+                    }
+                    const float attTot = att0 + att1 + att2;
+                    const float eventProb = attTot * density * maxInv;
+
+                    bool cont = true;
+                    if (!measured) {
+                        // naive sampling (computeInteractions, transport.hpp:583-638)
+                        if (rng.uniform() < eventProb) {
+                            const float r3 = rng.uniform() * attTot;
+                            if (r3 < att0) {
+                                const float e = photo_absorption<MODEL>(L, m, ph, mat, rng);
+                                do_score = true;
+                                if (ph.energy < ENERGY_CUTOFF) {
+                                    deposit = (e + ph.energy) * ph.weight;
+                                    ph.energy = 0.0f;
+                                    cont = false;
+                                } else {
+                                    deposit = e * ph.weight;
+                                    updateMax = true;
+                                }
+                            } else if (r3 < att0 + att1) {
+                                float e = 0.0f;
+                                if (!compton_scatter<MODEL>(L, m, ph, mat, rng, e)) {
+                                    ++my_overflows;
+                                    cont = false;
+                                } else {
+                                    do_score = true;
+                                    if (ph.energy < ENERGY_CUTOFF) {
+                                        deposit = (e + ph.energy) * ph.weight;
+                                        ph.energy = 0.0f;
+                                        cont = false;
+                                    } else {
+                                        deposit = e * ph.weight;
+                                        updateMax = true;
+                                    }
+                                }
+                            } else {
+                                if (!rayleigh_scatter<MODEL>(L, m, ph, mat, rng)) {
+                                    ++my_overflows;
+                                    cont = false;
+                                }
+                            }
+                        }
+                    } else {
+                        // forced photoelectric scoring (computeInteractionsForced, transport.hpp:523-581)
+                        const float photoProb = att0 / attTot;
+                        const float wc = eventProb * photoProb;
+                        {
+                            Photon forced = ph;
+                            const float ef = photo_absorption<MODEL>(L, m, forced, mat, rng);
+                            deposit = (forced.energy < ENERGY_CUTOFF ? (ef + forced.energy) : ef) * forced.weight * wc;
+                            do_score = true;
+                        }
+                        if (rng.uniform() < eventProb * (1.0f - photoProb)) {
+                            const float r2 = rng.uniform() * (att1 + att2);
+                            if (r2 < att1) {
+                                float e = 0.0f;
+                                if (!compton_scatter<MODEL>(L, m, ph, mat, rng, e)) {
+                                    ++my_overflows;
+                                    cont = false;
+                                } else {
+                                    // the forced photoelectric deposit and the Compton deposit are two events
+                                    score(p, vidx, deposit);
+                                    ++my_deposits;
+                                    if (ph.energy < ENERGY_CUTOFF) {
+                                        deposit = (e + ph.energy) * ph.weight;
+                                        ph.energy = 0.0f;
+                                        cont = false;
+                                    } else {
+                                        deposit = e * ph.weight;
+                                        updateMax = true;
+                                    }
+                                }
+                            } else {
+                                if (!rayleigh_scatter<MODEL>(L, m, ph, mat, rng)) {
+                                    ++my_overflows;
+                                    cont = false;
+                                }
+                            }
+                        }
+                        if (cont)
+                            ph.weight *= (1.0f - wc);
+                    }
+                    if (cont) {
+                        // Russian roulette (transport.hpp:684-694)
+                        if (ph.energy * ph.weight < ROULETTE_THRESHOLD) {
+                            if (rng.uniform() < ROULETTE_PROBABILITY)
+                                cont = false;
+                            else
+                                ph.weight *= 1.0f / (1.0f - ROULETTE_PROBABILITY);
+                        }
+                    }
+                    alive = cont;
+                }
+            }
+            // ---- scoring; the warp is converged here ----------------------------------------
+            if (p.tally_mode == 2) {
+                const unsigned scoring = __ballot_sync(FULL_MASK, do_score);
+                if (do_score)
+                    score_aggregated(p, scoring, vidx, deposit);
+            } else if (do_score) {
+                score(p, vidx, deposit);
+            }
+            if (do_score)
+                ++my_deposits;
+        }
+
+        // ---- per-warp counter flush ------------------------------------------------------
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            my_steps += __shfl_down_sync(FULL_MASK, my_steps, off);
+            my_deposits += __shfl_down_sync(FULL_MASK, my_deposits, off);
+            my_overflows += __shfl_down_sync(FULL_MASK, my_overflows, off);
+            my_histories += __shfl_down_sync(FULL_MASK, my_histories, off);
+        }
+        if (lane == 0) {
+            atomicAdd(&p.counters->steps, my_steps);
+            atomicAdd(&p.counters->deposits, my_deposits);
+            if (my_overflows)
+                atomicAdd(&p.counters->overflows, my_overflows);
+            atomicAdd(&p.counters->histories_done, my_histories);
+        }
+    }
+
+    // ---- post-processing (transport.hpp:780-816) -------------------------------------
+    template <typename TallyT>
+    __global__ void postprocess_kernel(const TallyT* __restrict__ tally, const Voxel* __restrict__ voxels, uint64_t n, int mode,
+        double histories, double voxel_volume_cm3, double calibration, double* __restrict__ dose, double* __restrict__ variance)
+    {
+        const double h_inv = 1.0 / (histories - 1.0);
+        const double h_d = 1.0e3 / histories;
+        const double h_v = 1.0e6 / histories;
+        for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+            const double e = static_cast<double>(tally[2 * i]);
+            const double ee = static_cast<double>(tally[2 * i + 1]);
+            double d = e, v = ee;
+            if (mode == 1) { // EV_PER_HISTORY: normalizeScoring
+                d = e * h_d;
+                v = (ee * h_v - d * d) * h_inv;
+            } else if (mode == 2) { // DOSE: energyImpartedToDose
+                const double de = static_cast<double>(voxels[i].density);
+                const double mass = de * voxel_volume_cm3 * 0.001;
+                const double f = calibration / mass;
+                d = de > 0.0 ? e * f : 0.0;
+                v = de > 0.0 ? ee * f * f : 0.0;
+            }
+            if (dose)
+                dose[i] = d;
+            if (variance)
+                variance[i] = v;
+        }
+    }
+
+    // ---- per-material maximum density (attenuationinterpolator.hpp:48-60) ------------
+    __global__ void max_density_kernel(const Voxel* __restrict__ voxels, uint64_t n, unsigned int* out_bits, int n_materials)
+    {
+        extern __shared__ unsigned int sbits[];
+        for (int i = threadIdx.x; i < n_materials; i += blockDim.x)
+            sbits[i] = 0u;
+        __syncthreads();
+        for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+            const uint2 raw = __ldg(reinterpret_cast<const uint2*>(voxels) + i);
+            const int mat = raw.y & 0xffu;
+            const float d = __uint_as_float(raw.x);
+            if (mat < n_materials && d > 0.0f)
+                atomicMax(&sbits[mat], raw.x); // non-negative floats order like their bits
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < n_materials; i += blockDim.x)
+            if (sbits[i])
+                atomicMax(out_bits + i, sbits[i]);
+    }
+
+    // ---- probes ------------------------------------------------------------------------
+    __global__ void probe_lut_kernel(const float* L, LutMeta m, int material, const double* energies, int n, double* out_att, double* out_maxinv)
+    {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x;
+        if (i >= n)
+            return;
+        const float E = static_cast<float>(energies[i]);
+        const float logE = __log10f(E);
+        const int seg = lut_segment(L, m, logE);
+        float a, b, c;
+        lut_attenuation(L, m, material, logE, seg, a, b, c);
+        out_att[3 * i] = a;
+        out_att[3 * i + 1] = b;
+        out_att[3 * i + 2] = c;
+        out_maxinv[i] = lut_max_inverse(L, m, logE, seg);
+    }
+
+    template <int MODEL>
+    __global__ void probe_interactions_kernel(const float* L, LutMeta m, int material, int kind, float energy, uint64_t n, uint64_t seed,
+        float* out_cos, float* out_energy, float* out_dep)
+    {
+        for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+            Rng rng;
+            rng.init(seed, i);
+            Photon ph { 0, 0, 0, 0, 0, 1, energy, 1 };
+            float dep = 0.0f;
+            bool ok = true;
+            if (kind == 0)
+                dep = photo_absorption<MODEL>(L, m, ph, material, rng);
+            else if (kind == 1)
+                ok = compton_scatter<MODEL>(L, m, ph, material, rng, dep);
+            else
+                ok = rayleigh_scatter<MODEL>(L, m, ph, material, rng);
+            const float len = sqrtf(ph.dx * ph.dx + ph.dy * ph.dy + ph.dz * ph.dz);
+            out_cos[i] = ok ? (len > 0 ? ph.dz / len : 1.0f) : 2.0f;
+            out_energy[i] = ph.energy;
+            out_dep[i] = dep;
+        }
+    }
+
+} // namespace
+
+cudaError_t launch_transport(const TransportParams& p, int model, int grid, int block, size_t smem, cudaStream_t stream)
+{
+    if (model == 0)
+        transport_kernel<0><<<grid, block, smem, stream>>>(p);
+    else if (model == 1)
+        transport_kernel<1><<<grid, block, smem, stream>>>(p);
+    else
+        transport_kernel<2><<<grid, block, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+int transport_max_blocks_per_sm(int model, int block, size_t smem)
+{
+    int n = 0;
+    cudaError_t e;
+    if (model == 0) {
+        cudaFuncSetAttribute(transport_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transport_kernel<0>, block, smem);
+    } else if (model == 1) {
+        cudaFuncSetAttribute(transport_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transport_kernel<1>, block, smem);
+    } else {
+        cudaFuncSetAttribute(transport_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transport_kernel<2>, block, smem);
+    }
+    return e == cudaSuccess ? n : 0;
+}
+
+cudaError_t launch_postprocess(const double* tally, const uint32_t*, const Voxel* voxels, uint64_t n, int mode, double histories,
+    double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream)
+{
+    const int block = 256;
+    const int grid = static_cast<int>(std::min<uint64_t>((n + block - 1) / block, 152ull * 16));
+    postprocess_kernel<double><<<grid, block, 0, stream>>>(tally, voxels, n, mode, histories, voxel_volume_cm3, calibration, dose, variance);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_postprocess_f32(const float* tally, const uint32_t*, const Voxel* voxels, uint64_t n, int mode, double histories,
+    double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream)
+{
+    const int block = 256;
+    const int grid = static_cast<int>(std::min<uint64_t>((n + block - 1) / block, 152ull * 16));
+    postprocess_kernel<float><<<grid, block, 0, stream>>>(tally, voxels, n, mode, histories, voxel_volume_cm3, calibration, dose, variance);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_max_density(const Voxel* voxels, uint64_t n, unsigned int* out_bits, int n_materials, cudaStream_t stream)
+{
+    const int block = 256;
+    const int grid = static_cast<int>(std::min<uint64_t>((n + block - 1) / block, 152ull * 8));
+    max_density_kernel<<<grid, block, n_materials * sizeof(unsigned int), stream>>>(voxels, n, out_bits, n_materials);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_probe_lut(const float* lut, LutMeta meta, int material, const double* energies, int n, double* out_att, double* out_maxinv, cudaStream_t stream)
+{
+    probe_lut_kernel<<<(n + 127) / 128, 128, 0, stream>>>(lut, meta, material, energies, n, out_att, out_maxinv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_probe_interactions(const float* lut, LutMeta meta, int material, int model, int kind, float energy,
+    uint64_t n, uint64_t seed, float* out_cos, float* out_energy, float* out_dep, cudaStream_t stream)
+{
+    const int block = 256;
+    const int grid = static_cast<int>(std::min<uint64_t>((n + block - 1) / block, 152ull * 8));
+    if (model == 0)
+        probe_interactions_kernel<0><<<grid, block, 0, stream>>>(lut, meta, material, kind, energy, n, seed, out_cos, out_energy, out_dep);
+    else if (model == 1)
+        probe_interactions_kernel<1><<<grid, block, 0, stream>>>(lut, meta, material, kind, energy, n, seed, out_cos, out_energy, out_dep);
+    else
+        probe_interactions_kernel<2><<<grid, block, 0, stream>>>(lut, meta, material, kind, energy, n, seed, out_cos, out_energy, out_dep);
+    return cudaGetLastError();
+}
+
+} // namespace dxmc_gb300::dev

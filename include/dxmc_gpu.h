@@ -1,0 +1,273 @@
+/*
+ * dxmc_gpu.h — C ABI of the GB300 (sm_103a) photon-transport engine.
+ *
+ * This is the drop-in boundary for DXMClib's photon-transport hot path.  In
+ * DXMClib the path sits behind C++ templates (include/dxmc/transport.hpp:
+ * Transport<T>::operator()(world, source, progress, useSourceDoseCalibration),
+ * lines 135-202).  Everything on the GPU side of that call is reached through
+ * the plain-C entry points below: opaque handles, plain pointers and sizes,
+ * an int status on every call, no exceptions and no torch types.  The C++
+ * adapter include/dxmc_gpu/transport.hpp maps DXMClib's World / Source /
+ * Material objects onto these calls; ctypes / cgo / JNI bindings can use them
+ * directly.
+ *
+ * Units follow DXMClib: lengths in mm, energies in keV, densities in g/cm3,
+ * mass attenuation in cm2/g, momentum transfer in 1/angstrom.
+ */
+#ifndef DXMC_GPU_H
+#define DXMC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DXMC_GPU_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------- */
+enum {
+    DXMC_OK = 0,
+    DXMC_ERR_INVALID = -1,      /* invalid argument / invalid world or source */
+    DXMC_ERR_OOM = -2,          /* allocation failed or admission budget exceeded */
+    DXMC_ERR_DEVICE = -3,       /* CUDA runtime error */
+    DXMC_ERR_REJECTION_CAP = -4,/* a sampling loop hit its iteration cap (histories ended early) */
+    DXMC_ERR_TIMEOUT = -5,      /* dxmc_gpu_job_wait timed out */
+    DXMC_ERR_CANCELLED = -6,    /* job was cancelled; results are zero */
+    DXMC_ERR_NO_DEVICE = -7,    /* no CUDA device / extension not usable */
+    DXMC_ERR_STATE = -8         /* call not valid in the object's current state */
+};
+
+/* Low-energy correction models: include/dxmc/lowenergycorrectionmodel.hpp:22-26 */
+enum { DXMC_MODEL_NONE = 0, DXMC_MODEL_LIVERMORE = 1, DXMC_MODEL_IA = 2 };
+
+/* Output modes: Transport<T>::OUTPUTMODE (transport.hpp:117-120) plus the raw tally. */
+enum {
+    DXMC_OUTPUT_RAW = 0,            /* sum of energy imparted (keV) and sum of its squares */
+    DXMC_OUTPUT_EV_PER_HISTORY = 1, /* normalizeScoring, transport.hpp:780-794 */
+    DXMC_OUTPUT_DOSE = 2            /* energyImpartedToDose, transport.hpp:796-816 */
+};
+
+/* Tally precision modes for the per-voxel accumulators. */
+enum {
+    DXMC_TALLY_F64 = 0,         /* FP64 atomics for every deposit (reference semantics) */
+    DXMC_TALLY_F32 = 1,         /* FP32 atomics only (precision study) */
+    DXMC_TALLY_WARP_F64 = 2     /* FP32 warp-aggregated partials flushed to FP64 */
+};
+
+/* ---- physics data for the host LUT build -------------------------------- */
+/* One electron shell, mirrors dxmc::ElectronShellConfiguration (material.hpp:29-58). */
+typedef struct dxmc_shell_config {
+    double binding_energy;
+    double number_electrons;
+    double hartree_fock_j0;
+    double photo_ionization_probability;
+    double fluorescence_yield;
+    double line_probabilities[3];
+    double line_energies[3];
+    int32_t Z;
+    int32_t shell;
+} dxmc_shell_config;
+
+/* Host callbacks answering the dxmc::Material queries that the LUT build makes
+ * (material.hpp:60-101; attenuationlut.hpp:212-265; attenuationinterpolator.hpp:
+ * 119-205).  A DXMClib user wraps their xraylib-backed Material; the project
+ * physics model provides one through dxmc_physics_material(). */
+typedef struct dxmc_material_provider {
+    void* user;
+    double standard_density;
+    double (*photoelectric)(void* user, double energy_kev);
+    double (*compton)(void* user, double energy_kev);
+    double (*rayleigh)(void* user, double energy_kev);
+    double (*form_factor_squared)(void* user, double momentum_transfer);
+    double (*scatter_factor)(void* user, double momentum_transfer);
+    /* binding energies above min_energy, descending; returns the count (may exceed capacity) */
+    int (*binding_energies)(void* user, double min_energy, double* out, int capacity);
+    void (*shells)(void* user, dxmc_shell_config out[12]);
+} dxmc_material_provider;
+
+/* Project physics model (closed-form; replaces xraylib).  name is a named
+ * material ("Water, Liquid", ...), a chemical formula ("H2O") or an element
+ * symbol; density <= 0 keeps the standard density.  The provider stays valid
+ * until dxmc_physics_material_free. */
+int dxmc_physics_material(const char* name, double density, dxmc_material_provider* out);
+void dxmc_physics_material_free(dxmc_material_provider* provider);
+int dxmc_physics_element_material(int atomic_number, dxmc_material_provider* out);
+
+/* ---- host LUT (AttenuationLut<T>::generate, attenuationlut.hpp:64-96) ---- */
+typedef struct dxmc_lut_blob dxmc_lut_blob;
+
+/* Builds the attenuation / form-factor / scatter-factor / shell tables for
+ * materials [0, n_materials) of a world.  The majorant uses the maximum
+ * density of each material over the voxels (attenuationinterpolator.hpp:48-84).
+ * max_energy is the source's maximum photon energy (transport.hpp:155-157). */
+int dxmc_lut_build(const dxmc_material_provider* materials, int n_materials,
+    const float* density, const uint8_t* material, uint64_t n_voxels,
+    double max_energy, dxmc_lut_blob** out);
+/* Same, with the per-material maximum density supplied by the caller
+ * (for example from dxmc_gpu_world_max_density). */
+int dxmc_lut_build_max_density(const dxmc_material_provider* materials, int n_materials,
+    const double* max_density, double max_energy, dxmc_lut_blob** out);
+void dxmc_lut_blob_free(dxmc_lut_blob* blob);
+/* Host evaluation of the tables (AttenuationLut public lookups, attenuationlut.hpp:105-153). */
+int dxmc_lut_attenuation(const dxmc_lut_blob* blob, int material, double energy, double out_photo_compt_rayl[3]);
+double dxmc_lut_max_attenuation_inverse(const dxmc_lut_blob* blob, double energy);
+double dxmc_lut_scatter_factor(const dxmc_lut_blob* blob, int material, double momentum_transfer);
+/* Introspection for tests: table sizes and raw arrays (double precision). */
+typedef struct dxmc_lut_info {
+    int32_t n_materials;
+    int32_t n_energy;          /* number of energy nodes / segments */
+    int32_t linear_index;
+    int32_t pad;
+    double linear_step;
+    double linear_energy;
+    double min_energy;
+    double max_energy;
+    const double* log_energy;  /* n_energy */
+    const double* coefficients;/* n_materials * n_energy * 6 : (b, a) for photo, compton, rayleigh */
+    const double* max_coefficients; /* n_energy * 2 */
+    const double* rita;        /* n_materials * 4 * 56 : x, e, a, b */
+    const double* spline;      /* n_materials * 79 : 60 coefficients, 16 knots, start, step, stop */
+    const dxmc_shell_config* shells; /* n_materials * 12 */
+} dxmc_lut_info;
+int dxmc_lut_get_info(const dxmc_lut_blob* blob, dxmc_lut_info* info);
+
+/* ---- sources: per-exposure table (Source::getExposure + alignToDirectionCosines) ---- */
+typedef struct dxmc_exposure {
+    double position[3];          /* mm, world basis */
+    double direction_cosines[6]; /* x then y direction cosine, world basis */
+    double beam_direction[3];
+    double collimation[4];       /* x0, x1, y0, y1 in radians (exposure.hpp:40) */
+    double weight;               /* beam intensity weight */
+    uint64_t n_histories;
+    double mono_energy;          /* keV, used when the job has no spectrum */
+} dxmc_exposure;
+
+/* Spectrum: SpecterDistribution (dxmcrandom.hpp:284-330). The alias table is built
+ * on the host from the weights (squaring-the-histogram, dxmcrandom.hpp:229-274). */
+typedef struct dxmc_spectrum_desc {
+    int32_t n;
+    const double* energies;  /* keV, increasing */
+    const double* weights;
+} dxmc_spectrum_desc;
+
+/* Heel table: HeelFilter (beamfilters.hpp:435-569). */
+typedef struct dxmc_heel_desc {
+    double energy_start, energy_step;
+    int32_t energy_size;
+    int32_t angle_size;
+    double angle_start, angle_step;
+    const double* weights; /* energy_size * angle_size, angle fastest */
+} dxmc_heel_desc;
+
+/* Bow-tie: BowTieFilter (beamfilters.hpp:78-198): angle/weight pairs; the
+ * library takes |angle|, sorts and normalises the weights to mean 1. */
+typedef struct dxmc_bowtie_desc {
+    int32_t n;
+    const double* angles;
+    const double* weights;
+} dxmc_bowtie_desc;
+
+/* Philox4x32-10, the counter-based generator the kernels draw from (one stream
+ * per history), exposed for known-answer tests. */
+int dxmc_philox4x32_10(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4]);
+
+/* Alias table of a spectrum (host), exposed for parity tests. */
+int dxmc_alias_table(const double* weights, int n, double* probs, uint64_t* alias);
+
+/* ---- device context ------------------------------------------------------ */
+typedef struct dxmc_gpu_ctx dxmc_gpu_ctx;
+typedef struct dxmc_world dxmc_world;
+typedef struct dxmc_lut dxmc_lut;
+typedef struct dxmc_job dxmc_job;
+
+typedef struct dxmc_gpu_options {
+    int32_t device;          /* CUDA device ordinal */
+    int32_t block_size;      /* threads per block, 0 = default (256) */
+    int32_t blocks_per_sm;   /* resident blocks per SM, 0 = occupancy-derived */
+    int32_t tally_mode;      /* DXMC_TALLY_* */
+    uint64_t memory_budget;  /* admission budget in bytes, 0 = 90% of free memory */
+} dxmc_gpu_options;
+
+int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out);
+void dxmc_gpu_ctx_destroy(dxmc_gpu_ctx* ctx);
+const char* dxmc_gpu_last_error(const dxmc_gpu_ctx* ctx);
+int dxmc_gpu_device_count(void);
+int dxmc_gpu_abi_version(void);
+
+/* ---- world (World<T>, world.hpp:37-227) ---------------------------------- */
+typedef struct dxmc_world_desc {
+    uint64_t dims[3];
+    double spacing[3];            /* mm */
+    double origin[3];             /* mm, centre of the grid */
+    double direction_cosines[6];
+    const float* density;         /* g/cm3, x fastest; host pointer */
+    const uint8_t* material;      /* material index, host pointer */
+    const uint8_t* measurement;   /* forced-interaction map, may be NULL */
+    int32_t n_materials;          /* material indices must be < n_materials */
+    int32_t pad;
+} dxmc_world_desc;
+
+/* Validates like World::validate (world.hpp:182-227) and copies the arrays to
+ * the device; the caller keeps ownership of the host arrays. */
+int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* desc, dxmc_world** out);
+/* Per-material maximum density of a resident world, computed on the device. */
+int dxmc_gpu_world_max_density(dxmc_world* world, double* out, int n_materials);
+void dxmc_gpu_world_free(dxmc_world* world);
+
+/* ---- LUT on the device --------------------------------------------------- */
+int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* blob, dxmc_lut** out);
+void dxmc_gpu_lut_free(dxmc_lut* lut);
+
+/* ---- jobs ---------------------------------------------------------------- */
+typedef struct dxmc_job_desc {
+    const dxmc_exposure* exposures;
+    uint64_t n_exposures;
+    const dxmc_spectrum_desc* spectrum; /* NULL: monoenergetic exposures */
+    const dxmc_heel_desc* heel;         /* NULL: no heel effect */
+    const dxmc_bowtie_desc* bowtie;     /* NULL: no bow-tie filter */
+    uint64_t seed;                      /* counter-based RNG key */
+    int32_t model;                      /* DXMC_MODEL_* */
+    int32_t tally_mode;                 /* DXMC_TALLY_*; -1 = context default */
+} dxmc_job_desc;
+
+typedef struct dxmc_job_stats {
+    uint64_t histories;        /* histories simulated */
+    uint64_t steps;            /* Woodcock steps inside the grid (S) */
+    uint64_t deposits;         /* depositing events (D) */
+    uint64_t rejection_overflows;
+    double kernel_ms;          /* device time of the transport kernel */
+    double job_ms;             /* device time from the job's first stream operation to the kernel's end */
+} dxmc_job_stats;
+
+/* Non-blocking: enqueues upload + transport on the context's stream. */
+int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut,
+    const dxmc_job_desc* job, dxmc_job** out);
+/* Waits for completion; timeout_ms < 0 waits forever. Returns DXMC_ERR_TIMEOUT on expiry. */
+int dxmc_gpu_job_wait(dxmc_job* job, int64_t timeout_ms);
+/* Requests cancellation: the kernel stops taking new histories; results read as zero
+ * (transport.hpp:176-185). */
+int dxmc_gpu_job_cancel(dxmc_job* job);
+/* Post-processes on the device (output_mode) and copies to host buffers of
+ * world size; any output pointer may be NULL.  calibration multiplies DOSE. */
+int dxmc_gpu_job_result(dxmc_job* job, int output_mode, double calibration,
+    double* dose, double* variance, uint32_t* n_events, dxmc_job_stats* stats);
+void dxmc_gpu_job_free(dxmc_job* job);
+
+/* ---- device probes for component parity tests ----------------------------- */
+/* Runs the device LUT lookup on energies[n]: out_att[n*3], out_maxinv[n]. */
+int dxmc_gpu_probe_lut(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, const double* energies, int n,
+    double* out_att, double* out_maxinv);
+/* Runs n independent interaction samples of one kind (0 photo, 1 Compton,
+ * 2 Rayleigh) at a fixed energy in one material on the device, starting from
+ * direction +z; writes cos(theta) of the new direction, the outgoing energy
+ * and the energy imparted for each sample. */
+int dxmc_gpu_probe_interactions(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, int model, int kind,
+    double energy, uint64_t n, uint64_t seed, float* out_cos, float* out_energy, float* out_deposit);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DXMC_GPU_H */

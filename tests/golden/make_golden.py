@@ -1,0 +1,228 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Runs DXMClib (headers compiled unmodified from the reference checkout, plus
+the project Material backend; see oracle/Makefile) through
+tests/golden/ref_binding.py and stores, as small .npz files:
+
+* lut_*.npz         AttenuationLut<double> tables and public lookups for a
+                    4-material world (attenuationlut.hpp, attenuationinterpolator.hpp);
+* alias.npz         SpecterDistribution alias tables (dxmcrandom.hpp:229-274);
+* source_*.npz      Source::getExposure tables, spectrum and heel tables for
+                    Pencil / Isotropic / DX / CT spiral sources (source.hpp);
+* transport_*.npz   Transport<double> tallies in EV_PER_HISTORY mode for the
+                    pencil-beam and heterogeneous cone-beam cases, stored
+                    for voxels above 0.2 % of the maximum dose plus depth and
+                    lateral profiles and the total energy imparted;
+* interactions_*.npz histograms of the reference interaction samplers.
+
+Usage:  make -C oracle && python tests/golden/make_golden.py [--quick]
+The generator needs the reference checkout and is not run by the test suite.
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+import ref_binding as R  # noqa: E402
+
+MATERIALS4 = ["Water, Liquid", "Bone, Cortical (ICRP)", "Tissue, Soft (ICRP)", "Air, Dry (near sea level)"]
+
+
+def hetero_world(n=48, spacing=4.0, seed=7):
+    """Seeded heterogeneous phantom: soft-tissue box with bone and lung-density inclusions in air."""
+    rng = np.random.default_rng(seed)
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    c = (n - 1) / 2
+    mat = np.full((n, n, n), 3, np.uint8)  # air
+    body = ((x - c) / (0.42 * n)) ** 2 + ((y - c) / (0.32 * n)) ** 2 <= 1.0
+    mat[body] = 2
+    dens = np.where(mat == 3, 0.0012, 1.03).astype(np.float64)
+    for _ in range(6):
+        cx, cy, cz = rng.uniform(0.3 * n, 0.7 * n, 3)
+        r = rng.uniform(0.05 * n, 0.12 * n)
+        sph = (x - cx) ** 2 + (y - cy) ** 2 + (z - cz) ** 2 <= r * r
+        sph &= body
+        m = int(rng.integers(0, 2))
+        mat[sph] = m
+        dens[sph] = rng.uniform(0.2, 2.0)
+    return mat.ravel(), dens.ravel()
+
+
+def sparse_tally(dose, var, nev, dims, frac=0.002):
+    d3 = dose.reshape(dims[2], dims[1], dims[0])
+    keep = np.nonzero(dose > frac * dose.max())[0].astype(np.uint32)
+    return dict(
+        idx=keep, dose=dose[keep], var=var[keep], nev=nev[keep].astype(np.uint32),
+        depth=d3.sum(axis=(1, 2)), lateral_x=d3.sum(axis=(0, 1)), lateral_y=d3.sum(axis=(0, 2)),
+        total=np.array([dose.sum()]), total_events=np.array([nev.sum()], np.float64),
+    )
+
+
+def gen_lut(out: Path):
+    n = 16
+    rng = np.random.default_rng(1)
+    mat = rng.integers(0, 4, n ** 3).astype(np.uint8)
+    dens = (np.array([1.0, 1.92, 1.03, 0.0012])[mat] * rng.uniform(0.5, 1.5, n ** 3)).astype(np.float32)
+    w = R.WorldArgs((n, n, n), (1, 1, 1), dens.astype(np.float64), mat, MATERIALS4)
+    for maxE in (60.0, 120.0):
+        E = np.concatenate([np.linspace(1.0, maxE, 600), np.geomspace(1.0, maxE, 200)])
+        q = np.linspace(0, 12, 200)
+        t = R.lut_dump(w, maxE, E, q)
+        np.savez_compressed(out / f"lut_4mat_{int(maxE)}kev.npz", material=mat, density=dens, energies=E, q=q,
+                            names=np.array(MATERIALS4), max_energy=maxE, **t)
+
+
+def gen_alias(out: Path):
+    rng = np.random.default_rng(3)
+    cases = {}
+    for k, n in enumerate([1, 2, 7, 60, 150]):
+        w = rng.uniform(0, 1, n) ** 3
+        if n > 3:
+            w[rng.integers(0, n, 2)] = 0.0
+        p, a = R.alias_table(w)
+        cases[f"w{k}"] = w
+        cases[f"p{k}"] = p
+        cases[f"a{k}"] = a
+    np.savez_compressed(out / "alias.npz", **cases)
+
+
+def gen_sources(out: Path):
+    n = 32
+    w = R.WorldArgs((n, n, n), (4, 4, 4), np.ones(n ** 3), np.zeros(n ** 3, np.uint8), ["Water, Liquid"])
+    cases = {
+        "pencil": R.SourceArgs(R.PENCIL, position=(3, -2, -300), cosines=(1, 0, 0, 0, 1, 0), energy=60.0,
+                               histories_per_exposure=1000, total_exposures=3),
+        "isotropic": R.SourceArgs(R.ISOTROPIC, position=(0, 0, -400), cosines=(1, 0, 0, 0, 1, 0),
+                                  collimation=(-0.2, 0.2, -0.1, 0.15), spec_energies=np.arange(20, 81, 5.0),
+                                  spec_weights=np.linspace(1, 3, 13), histories_per_exposure=500, total_exposures=2),
+        "dx": R.SourceArgs(R.DX, position=(10, 5, -20), kvp=80, al_mm=3.0, field_size=(200, 150), sdd=1000,
+                           source_angles_deg=(15, -10), tube_rotation_deg=0, heel=1, histories_per_exposure=800,
+                           total_exposures=2),
+        "ctspiral": R.SourceArgs(R.CTSPIRAL, position=(0, 0, -30), kvp=120, al_mm=2.5, ct_collimation=40, pitch=1.0,
+                                 scan_length=80, angle_step_deg=1.0, start_angle_deg=0, fov=500, sdd=1190,
+                                 tilt_deg=0.0, heel=1, histories_per_exposure=100),
+        "ctspiral_tilt": R.SourceArgs(R.CTSPIRAL, position=(0, 0, 0), kvp=100, al_mm=7.0, ct_collimation=20, pitch=1.5,
+                                      scan_length=40, angle_step_deg=2.0, start_angle_deg=30, fov=400, sdd=1000,
+                                      tilt_deg=12.0, heel=0, histories_per_exposure=100),
+    }
+    for name, s in cases.items():
+        t = R.source_tables(s, w)
+        np.savez_compressed(out / f"source_{name}.npz", **t)
+
+
+def gen_transport(out: Path, quick: bool):
+    scale = 0.1 if quick else 1.0
+    # pencil 60 keV in a 64^3 water cube of 2 mm voxels (spec configuration 1)
+    n = 64
+    dims = (n, n, n)
+    w = R.WorldArgs(dims, (2.0, 2.0, 2.0), np.ones(n ** 3), np.zeros(n ** 3, np.uint8), ["Water, Liquid"])
+    for model in (0, 1, 2):
+        hist = int(2e6 * scale)
+        s = R.SourceArgs(R.PENCIL, position=(0, 0, -200), cosines=(1, 0, 0, 0, 1, 0), energy=60.0,
+                         histories_per_exposure=hist // 10, total_exposures=10)
+        t0 = time.time()
+        dose, var, nev, N, st = R.transport(w, s, model=model)
+        print(f"pencil model {model}: {N} histories {st:.2f} s ({N / st:.3g} hist/s)", flush=True)
+        np.savez_compressed(out / f"transport_pencil_m{model}.npz", dims=np.array(dims), spacing=np.array([2.0] * 3),
+                            histories=N, seconds=st, **sparse_tally(dose, var, nev, dims))
+    # heterogeneous cone beam with a spectrum
+    mat, dens = hetero_world()
+    n = 48
+    dims = (n, n, n)
+    w = R.WorldArgs(dims, (4.0, 4.0, 4.0), dens, mat, MATERIALS4)
+    spec_e = np.arange(20.0, 101.0, 1.0)
+    spec_w = np.exp(-0.5 * ((spec_e - 55) / 15) ** 2) + 0.2
+    for model in (1, 2):
+        hist = int(4e6 * scale)
+        s = R.SourceArgs(R.ISOTROPIC, position=(0, 0, -500), cosines=(1, 0, 0, 0, 1, 0),
+                         collimation=(-0.12, 0.12, -0.1, 0.1), spec_energies=spec_e, spec_weights=spec_w,
+                         histories_per_exposure=hist // 8, total_exposures=8)
+        dose, var, nev, N, st = R.transport(w, s, model=model)
+        print(f"cone model {model}: {N} histories {st:.2f} s ({N / st:.3g} hist/s)", flush=True)
+        np.savez_compressed(out / f"transport_cone_m{model}.npz", dims=np.array(dims), spacing=np.array([4.0] * 3),
+                            material=mat, density=dens.astype(np.float32), names=np.array(MATERIALS4),
+                            spec_energies=spec_e, spec_weights=spec_w, histories=N, seconds=st,
+                            **sparse_tally(dose, var, nev, dims))
+    # forced-interaction (measurement map) case: water slab with a measured cylinder
+    n = 40
+    dims = (n, n, n)
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    meas = (((x - 20) ** 2 + (y - 20) ** 2) <= 16).astype(np.uint8).ravel()
+    w = R.WorldArgs(dims, (2.0, 2.0, 2.0), np.ones(n ** 3), np.zeros(n ** 3, np.uint8), ["Water, Liquid"],
+                    measurement=meas)
+    hist = int(2e6 * scale)
+    s = R.SourceArgs(R.ISOTROPIC, position=(0, 0, -300), cosines=(1, 0, 0, 0, 1, 0),
+                     collimation=(-0.05, 0.05, -0.05, 0.05), spec_energies=np.array([50.0]),
+                     spec_weights=np.array([1.0]), histories_per_exposure=hist // 8, total_exposures=8)
+    dose, var, nev, N, st = R.transport(w, s, model=1)
+    print(f"forced: {N} histories {st:.2f} s", flush=True)
+    np.savez_compressed(out / "transport_forced_m1.npz", dims=np.array(dims), spacing=np.array([2.0] * 3),
+                        measurement=meas, histories=N, seconds=st, **sparse_tally(dose, var, nev, dims))
+
+
+def gen_ct(out: Path, quick: bool):
+    """Reference CT-spiral run on a small phantom; the fixture carries the reference's
+    own exposure, spectrum and heel tables so the GPU run consumes identical inputs."""
+    mat, dens = hetero_world(n=48, spacing=4.0, seed=11)
+    n = 48
+    dims = (n, n, n)
+    w = R.WorldArgs(dims, (4.0, 4.0, 4.0), dens, mat, MATERIALS4)
+    hpe = 2000 if quick else 12000
+    s = R.SourceArgs(R.CTSPIRAL, position=(0, 0, -20), kvp=120, al_mm=2.5, ct_collimation=40, pitch=1.0,
+                     scan_length=40, angle_step_deg=1.0, start_angle_deg=0, fov=500, sdd=1190, heel=1,
+                     histories_per_exposure=hpe)
+    tabs = R.source_tables(s, w)
+    dose, var, nev, N, st = R.transport(w, s, model=1)
+    print(f"ct: {N} histories {st:.2f} s", flush=True)
+    np.savez_compressed(out / "transport_ct_m1.npz", dims=np.array(dims), spacing=np.array([4.0] * 3), material=mat,
+                        density=dens.astype(np.float32), names=np.array(MATERIALS4), histories=N, seconds=st,
+                        exposures=tabs["exposures"], spec_energies=tabs["spec_energies"],
+                        spec_weights=tabs["spec_weights"], heel_meta=tabs["heel_meta"],
+                        heel_weights=tabs.get("heel_weights", np.zeros(0)), max_energy=tabs["max_energy"],
+                        **sparse_tally(dose, var, nev, dims))
+
+
+def gen_interactions(out: Path, quick: bool):
+    n = 8
+    w = R.WorldArgs((n, n, n), (1, 1, 1), np.ones(n ** 3) * 1.92, np.zeros(n ** 3, np.uint8),
+                    ["Bone, Cortical (ICRP)"])
+    N = int(4e5 if quick else 2e6)
+    res = {}
+    for model in (0, 1, 2):
+        for kind, name in ((1, "compton"), (2, "rayleigh"), (0, "photo")):
+            for energy in (20.0, 60.0):
+                hc, he, sums = R.interactions(w, 120.0, model, kind, energy, N, nbins=100, seed=model * 10 + kind)
+                key = f"m{model}_{name}_{int(energy)}"
+                res[key + "_cos"] = hc
+                res[key + "_e"] = he
+                res[key + "_sums"] = sums
+    np.savez_compressed(out / "interactions_bone.npz", n=N, **res)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--quick", action="store_true")
+    ap.add_argument("--only", default="")
+    a = ap.parse_args()
+    if not R.available():
+        raise SystemExit("oracle/_ref/libdxmc_ref.so missing: run `make -C oracle` where the reference checkout exists")
+    out = HERE
+    steps = dict(lut=lambda: gen_lut(out), alias=lambda: gen_alias(out), sources=lambda: gen_sources(out),
+                 transport=lambda: gen_transport(out, a.quick), ct=lambda: gen_ct(out, a.quick),
+                 interactions=lambda: gen_interactions(out, a.quick))
+    for name, fn in steps.items():
+        if a.only and name not in a.only.split(","):
+            continue
+        t = time.time()
+        fn()
+        print(f"{name}: {time.time() - t:.1f} s", flush=True)
+
+
+if __name__ == "__main__":
+    main()

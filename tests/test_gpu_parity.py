@@ -1,0 +1,202 @@
+"""GPU parity tests: the sm_103a kernels against DXMClib's own CPU transport.
+
+Every reference number comes from a golden fixture produced by the reference
+(tests/golden/make_golden.py); the GPU runs the same world, source tables,
+spectrum and heel tables through the C ABI and must agree statistically:
+per-voxel differences within 3 combined standard errors in voxels above 1 %
+of the maximum dose (>= 99 % of voxels, 99.7 % expected), total energy
+imparted within 0.5 %, mean per-voxel relative difference within 1 %.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from parity import assert_parity, compare_sparse
+
+pytestmark = pytest.mark.gpu
+
+
+def _world(dims, spacing, material, density, names, measurement=None):
+    import dxmclib_gb300 as dx
+    w = dx.World()
+    w.setDimensions(dims)
+    w.setSpacing(spacing)
+    w.setDensityArray(np.asarray(density, np.float32))
+    w.setMaterialIndexArray(np.asarray(material, np.uint8))
+    if measurement is not None:
+        w.setMeasurementMapArray(measurement)
+    for n in names:
+        assert w.addMaterialToMap(dx.Material(str(n)))
+    assert w.isValid()
+    return w
+
+
+def _run(ctx, world, exposures, max_energy, spectrum=None, heel=None, model=1, seed=11, tally_mode=-1):
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    dworld = dx.DeviceWorld(ctx, world)
+    md = dworld.max_density()
+    blob = dx.LutBlob(world.materialMap(), md, max_energy)
+    dlut = dx.DeviceLut(ctx, blob)
+    job = dx.Job(ctx, dworld, dlut, exposures, spectrum, heel, None, seed=seed, model=model, tally_mode=tally_mode)
+    dose, var, nev, stats = job.result(A.OUTPUT_EV_PER_HISTORY)
+    assert stats["histories"] == int(np.sum(exposures.n_histories))
+    assert stats["rejection_overflows"] == 0
+    job.close()
+    dlut.close()
+    dworld.close()
+    return dose, var, nev, stats
+
+
+def _pencil(ctx, golden, model, scale=2):
+    import dxmclib_gb300 as dx
+    g = golden(f"transport_pencil_m{model}.npz")
+    n = 64
+    world = _world((n, n, n), (2.0, 2.0, 2.0), np.zeros(n ** 3), np.ones(n ** 3), ["Water, Liquid"])
+    src = dx.PencilSource()
+    src.setPosition((0, 0, -200))
+    src.setDirectionCosines((1, 0, 0, 0, 1, 0))
+    src.setPhotonEnergy(60.0)
+    src.setTotalExposures(10)
+    src.setHistoriesPerExposure(int(g["histories"]) * scale // 10)
+    return g, _run(ctx, world, src.exposures(), src.maxPhotonEnergyProduced(), model=model)
+
+
+@pytest.mark.parametrize("model", [0, 1, 2])
+def test_pencil_beam_matches_reference(gpu_ctx, golden, model):
+    """60 keV pencil beam, 64^3 water, 2 mm voxels (configuration 1) per correction model."""
+    g, (dose, var, nev, stats) = _pencil(gpu_ctx, golden, model)
+    s = compare_sparse(g, dose, var)
+    assert_parity(s, f"pencil m{model}")
+    # depth-dose profile (sum over each slice) within 1 %
+    d3 = dose.reshape(64, 64, 64).sum(axis=(1, 2))
+    ref = g["depth"]
+    sel = ref > 0.05 * ref.max()
+    np.testing.assert_allclose(d3[sel], ref[sel], rtol=0.01)
+
+
+@pytest.mark.parametrize("model", [1, 2])
+def test_heterogeneous_cone_beam_matches_reference(gpu_ctx, golden, model):
+    """Spectral cone beam on a 4-material seeded phantom."""
+    import dxmclib_gb300 as dx
+    g = golden(f"transport_cone_m{model}.npz")
+    dims = tuple(int(x) for x in g["dims"])
+    world = _world(dims, tuple(g["spacing"]), g["material"], g["density"], g["names"])
+    src = dx.IsotropicSource()
+    src.setPosition((0, 0, -500))
+    src.setDirectionCosines((1, 0, 0, 0, 1, 0))
+    src.setCollimationAngles(-0.12, 0.12, -0.1, 0.1)
+    src.setSpecter(g["spec_weights"], g["spec_energies"])
+    src.setTotalExposures(8)
+    src.setHistoriesPerExposure(int(g["histories"]) * 2 // 8)
+    dose, var, nev, stats = _run(gpu_ctx, world, src.exposures(), src.maxPhotonEnergyProduced(), src.spectrum(),
+                                 model=model)
+    s = compare_sparse(g, dose, var)
+    assert_parity(s, f"cone m{model}")
+
+
+def test_ct_spiral_matches_reference(gpu_ctx, golden):
+    """CT helical exposures, 120 kVp spectrum and heel table exactly as the reference produced them."""
+    import dxmclib_gb300 as dx
+    g = golden("transport_ct_m1.npz")
+    dims = tuple(int(x) for x in g["dims"])
+    world = _world(dims, tuple(g["spacing"]), g["material"], g["density"], g["names"])
+    ex = g["exposures"]
+    table = dx.ExposureTable(ex[:, 0:3].copy(), ex[:, 3:9].copy(), ex[:, 9:12].copy(), ex[:, 12:16].copy(),
+                             ex[:, 16].copy(), (ex[:, 17] * 2).astype(np.uint64), np.zeros(len(ex)))
+    spec = dx.Spectrum(g["spec_energies"], g["spec_weights"])
+    hm = g["heel_meta"]
+    heel = dx.HeelTable(hm[1], hm[2], int(hm[3]), hm[4], hm[5], int(hm[6]), g["heel_weights"])
+    dose, var, nev, stats = _run(gpu_ctx, world, table, float(g["max_energy"]), spec, heel, model=1)
+    s = compare_sparse(g, dose, var)
+    assert_parity(s, "ct spiral")
+
+
+def test_forced_interactions_match_reference(gpu_ctx, golden):
+    """Measurement map -> forced photoelectric scoring (transport.hpp:523-581)."""
+    import dxmclib_gb300 as dx
+    g = golden("transport_forced_m1.npz")
+    dims = tuple(int(x) for x in g["dims"])
+    n = int(np.prod(dims))
+    world = _world(dims, tuple(g["spacing"]), np.zeros(n), np.ones(n), ["Water, Liquid"], g["measurement"])
+    src = dx.IsotropicSource()
+    src.setPosition((0, 0, -300))
+    src.setDirectionCosines((1, 0, 0, 0, 1, 0))
+    src.setCollimationAngles(-0.05, 0.05, -0.05, 0.05)
+    src.setSpecter([1.0], [50.0])
+    src.setTotalExposures(8)
+    src.setHistoriesPerExposure(int(g["histories"]) * 2 // 8)
+    dose, var, nev, stats = _run(gpu_ctx, world, src.exposures(), src.maxPhotonEnergyProduced(), src.spectrum(),
+                                 model=1)
+    s = compare_sparse(g, dose, var)
+    assert_parity(s, "forced")
+
+
+def test_warp_aggregated_tally_matches_reference(gpu_ctx, golden):
+    """FP32 warp partials flushed to FP64 give the same pencil-beam dose."""
+    from dxmclib_gb300 import _capi as A
+    import dxmclib_gb300 as dx
+    g = golden("transport_pencil_m1.npz")
+    n = 64
+    world = _world((n, n, n), (2.0, 2.0, 2.0), np.zeros(n ** 3), np.ones(n ** 3), ["Water, Liquid"])
+    src = dx.PencilSource()
+    src.setPosition((0, 0, -200))
+    src.setPhotonEnergy(60.0)
+    src.setTotalExposures(10)
+    src.setHistoriesPerExposure(int(g["histories"]) * 2 // 10)
+    dose, var, nev, stats = _run(gpu_ctx, world, src.exposures(), 60.0, model=1, tally_mode=A.TALLY_WARP_F64)
+    assert_parity(compare_sparse(g, dose, var), "pencil warp-aggregated")
+
+
+def test_device_lut_lookups_match_reference(gpu_ctx, golden):
+    """Device AttenuationLut lookups (FP32) against the reference's public lookups."""
+    import dxmclib_gb300 as dx
+    g = golden("lut_4mat_120kev.npz")
+    mats = [dx.Material(str(n)) for n in g["names"]]
+    md = np.zeros(len(mats))
+    np.maximum.at(md, g["material"].astype(np.int64), g["density"].astype(np.float64))
+    blob = dx.LutBlob(mats, md, float(g["max_energy"]))
+    dlut = dx.DeviceLut(gpu_ctx, blob)
+    E = g["energies"]
+    for m in range(len(mats)):
+        att, mi = dlut.probe(m, E)
+        np.testing.assert_allclose(att, g["att"][m], rtol=2e-4)
+        np.testing.assert_allclose(mi, g["maxinv"], rtol=2e-4)
+    dlut.close()
+
+
+def _two_sample_chi2(h1, h2):
+    n1, n2 = h1.sum(), h2.sum()
+    k1, k2 = np.sqrt(n2 / n1), np.sqrt(n1 / n2)
+    sel = (h1 + h2) > 0
+    chi2 = np.sum((k1 * h1[sel] - k2 * h2[sel]) ** 2 / (h1[sel] + h2[sel]))
+    return chi2 / max(sel.sum() - 1, 1)
+
+
+@pytest.mark.parametrize("model", [0, 1, 2])
+def test_interaction_samplers_match_reference(gpu_ctx, golden, model):
+    """Photoelectric / Compton / Rayleigh samplers (transport.hpp:216-483) in bone:
+    angular and energy histograms against the reference's samplers."""
+    import dxmclib_gb300 as dx
+    g = golden("interactions_bone.npz")
+    n = 8
+    world = _world((n, n, n), (1, 1, 1), np.zeros(n ** 3), np.full(n ** 3, 1.92), ["Bone, Cortical (ICRP)"])
+    dworld = dx.DeviceWorld(gpu_ctx, world)
+    blob = dx.LutBlob(world.materialMap(), dworld.max_density(), 120.0)
+    dlut = dx.DeviceLut(gpu_ctx, blob)
+    N = int(g["n"]) * 2
+    for kind, name in ((1, "compton"), (2, "rayleigh"), (0, "photo")):
+        for energy in (20.0, 60.0):
+            key = f"m{model}_{name}_{int(energy)}"
+            c, e, d = dlut.probe_interactions(0, model, kind, energy, N, seed=1234 + kind)
+            assert np.all(c <= 1.0 + 1e-5), key  # no rejection-cap hits
+            hc = np.bincount(np.clip(((c.astype(np.float64) + 1) * 0.5 * 100).astype(np.int64), 0, 99), minlength=100)
+            he = np.bincount(np.clip((e.astype(np.float64) / energy * 100).astype(np.int64), 0, 99), minlength=100)
+            if kind != 0 or model == 2:
+                assert _two_sample_chi2(g[key + "_cos"], hc.astype(np.float64)) < 1.6, key
+            assert _two_sample_chi2(g[key + "_e"], he.astype(np.float64)) < 1.6, key
+            ref_mean_dep = g[key + "_sums"][0] / g["n"]
+            assert abs(d.astype(np.float64).mean() - ref_mean_dep) <= 0.002 * energy + 5 * d.std() / np.sqrt(N), key
+    dlut.close()
+    dworld.close()

@@ -1,0 +1,229 @@
+"""CPU tests: the host-side tables of the GPU path against the reference.
+
+Golden fixtures come from DXMClib itself (tests/golden/make_golden.py runs the
+reference headers compiled unmodified with the project Material backend).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+REPO = Path(__file__).resolve().parents[1]
+
+
+def _materials(names):
+    from dxmclib_gb300 import Material
+    return [Material(str(n)) for n in names]
+
+
+@pytest.mark.parametrize("max_energy", [60, 120])
+def test_lut_tables_match_reference(lib, golden, max_energy):
+    """AttenuationLut<double>::generate (attenuationlut.hpp:64-96) table by table."""
+    from dxmclib_gb300 import LutBlob
+    g = golden(f"lut_4mat_{max_energy}kev.npz")
+    mats = _materials(g["names"])
+    md = np.zeros(len(mats))
+    np.maximum.at(md, g["material"].astype(np.int64), g["density"].astype(np.float64))
+    blob = LutBlob(mats, md, float(g["max_energy"]))
+    info = blob.info()
+    meta = g["meta"]
+    assert info["n_energy"] == int(meta[0])
+    assert info["linear_index"] == int(meta[1])
+    assert info["linear_step"] == pytest.approx(meta[2], rel=1e-14)
+    assert info["linear_energy"] == pytest.approx(meta[3], rel=1e-14)
+    assert info["min_energy"] == meta[4] and info["max_energy"] == meta[5]
+    np.testing.assert_array_equal(info["x"], g["x"])
+    np.testing.assert_allclose(info["coef"], g["coef"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(info["maxcoef"], g["maxcoef"], rtol=0, atol=1e-9)
+    # RITA form-factor and Compton scatter-factor tables: bit-exact
+    np.testing.assert_array_equal(info["rita"], g["rita"])
+    np.testing.assert_array_equal(info["spline"], g["spline"])
+    np.testing.assert_allclose(info["shells"], g["shells"], rtol=1e-12, atol=1e-15)
+    # public lookups on a dense energy grid
+    E, q = g["energies"], g["q"]
+    for m in range(len(mats)):
+        att = np.array([blob.attenuation(m, e) for e in E])
+        np.testing.assert_allclose(att, g["att"][m], rtol=1e-12)
+        sf = np.array([blob.scatter_factor(m, x) for x in q])
+        np.testing.assert_allclose(sf, g["sf"][m], rtol=1e-12, atol=1e-15)
+    mi = np.array([blob.max_attenuation_inverse(e) for e in E])
+    np.testing.assert_allclose(mi, g["maxinv"], rtol=1e-12)
+
+
+def test_alias_tables_match_reference(lib, golden):
+    """RandomDistribution::generateTable (dxmcrandom.hpp:229-274)."""
+    from dxmclib_gb300 import _capi as A
+    g = golden("alias.npz")
+    k = 0
+    while f"w{k}" in g:
+        w = np.ascontiguousarray(g[f"w{k}"])
+        p = np.zeros(len(w))
+        a = np.zeros(len(w), np.uint64)
+        assert lib.dxmc_alias_table(w.ctypes.data_as(A.DP), len(w), p.ctypes.data_as(A.DP), a.ctypes.data_as(A.U64P)) == 0
+        np.testing.assert_array_equal(p, g[f"p{k}"])
+        np.testing.assert_array_equal(a, g[f"a{k}"])
+        k += 1
+    assert k >= 4
+
+
+def test_alias_table_distribution(lib):
+    """Sampling the alias table reproduces the weights (statistical check of the table)."""
+    from dxmclib_gb300 import _capi as A
+    rng = np.random.default_rng(0)
+    w = rng.uniform(0, 1, 40)
+    p = np.zeros(40)
+    a = np.zeros(40, np.uint64)
+    lib.dxmc_alias_table(w.ctypes.data_as(A.DP), 40, p.ctypes.data_as(A.DP), a.ctypes.data_as(A.U64P))
+    implied = p.copy()
+    for k in range(40):
+        implied[a[k]] += 1 - p[k]
+    np.testing.assert_allclose(implied / 40, w / w.sum(), rtol=1e-12)
+
+
+def test_philox_known_answers(lib):
+    """Philox4x32-10 known-answer vectors from the Random123 distribution (Salmon et al., SC'11)."""
+    from dxmclib_gb300 import _capi as A
+    cases = [
+        ([0, 0, 0, 0], [0, 0], [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
+        ([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2, [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
+        ([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0],
+         [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]),
+    ]
+    for c, k, want in cases:
+        c = np.array(c, np.uint32)
+        k = np.array(k, np.uint32)
+        o = np.zeros(4, np.uint32)
+        assert lib.dxmc_philox4x32_10(c.ctypes.data_as(A.U32P), k.ctypes.data_as(A.U32P), o.ctypes.data_as(A.U32P)) == 0
+        assert o.tolist() == want
+
+
+def _dx_source():
+    import dxmclib_gb300 as dx
+    s = dx.DXSource()
+    s.tube().setVoltage(80)
+    s.tube().setAlFiltration(3.0)
+    s.setPosition((10, 5, -20))
+    s.setSourceDetectorDistance(1000)
+    s.setFieldSize((200, 150))
+    s.setTubeRotationDeg(0)
+    s.setSourceAnglesDeg(15, -10)
+    s.setModelHeelEffect(True)
+    s.setHistoriesPerExposure(800)
+    s.setTotalExposures(2)
+    return s
+
+
+def _ct_source(tilt=False):
+    import dxmclib_gb300 as dx
+    s = dx.CTSpiralSource()
+    if not tilt:
+        s.tube().setVoltage(120)
+        s.tube().setAlFiltration(2.5)
+        s.setPosition((0, 0, -30))
+        s.setSourceDetectorDistance(1190)
+        s.setCollimation(40)
+        s.setFieldOfView(500)
+        s.setGantryTiltAngleDeg(0)
+        s.setStartAngleDeg(0)
+        s.setExposureAngleStepDeg(1.0)
+        s.setPitch(1.0)
+        s.setScanLenght(80)
+    else:
+        s.tube().setVoltage(100)
+        s.tube().setAlFiltration(7.0)
+        s.setPitch(1.5)
+        s.setPosition((0, 0, 0))
+        s.setSourceDetectorDistance(1000)
+        s.setCollimation(20)
+        s.setFieldOfView(400)
+        s.setGantryTiltAngleDeg(12.0)
+        s.setStartAngleDeg(30)
+        s.setExposureAngleStepDeg(2.0)
+        s.setScanLenght(40)
+    s.setHistoriesPerExposure(100)
+    return s
+
+
+def test_source_exposure_tables_match_reference(lib, golden):
+    """Source::getExposure + Exposure::alignToDirectionCosines for the host sources (source.hpp)."""
+    import dxmclib_gb300 as dx
+    pen = dx.PencilSource()
+    pen.setPosition((3, -2, -300))
+    pen.setDirectionCosines((1, 0, 0, 0, 1, 0))
+    pen.setPhotonEnergy(60.0)
+    pen.setHistoriesPerExposure(1000)
+    pen.setTotalExposures(3)
+    iso = dx.IsotropicSource()
+    iso.setPosition((0, 0, -400))
+    iso.setDirectionCosines((1, 0, 0, 0, 1, 0))
+    iso.setCollimationAngles(-0.2, 0.2, -0.1, 0.15)
+    iso.setSpecter(np.linspace(1, 3, 13), np.arange(20, 81, 5.0))
+    iso.setHistoriesPerExposure(500)
+    iso.setTotalExposures(2)
+    cases = {"pencil": pen, "isotropic": iso, "dx": _dx_source(), "ctspiral": _ct_source(False),
+             "ctspiral_tilt": _ct_source(True)}
+    for name, src in cases.items():
+        g = golden(f"source_{name}.npz")
+        ex = src.exposures().as_matrix()
+        assert ex.shape == g["exposures"].shape, name
+        np.testing.assert_allclose(ex, g["exposures"], rtol=0, atol=1e-9, err_msg=name)
+        assert src.maxPhotonEnergyProduced() == pytest.approx(g["max_energy"]), name
+
+
+def test_heel_table_layout_matches_reference(lib, golden):
+    """HeelFilter grid (beamfilters.hpp:455-505): energy bins and angular span."""
+    g = golden("source_dx.npz")
+    h = _dx_source().heel()
+    meta = g["heel_meta"]
+    assert meta[0] == 1
+    assert (h.energy_start, h.energy_step, h.energy_size) == (meta[1], meta[2], int(meta[3]))
+    assert h.angle_start == pytest.approx(meta[4], rel=1e-12)
+    assert h.angle_step == pytest.approx(meta[5], rel=1e-12)
+    assert h.angle_size == int(meta[6])
+    # weights are normalised to mean 1 per energy bin, like the reference's
+    w = h.weights.reshape(h.energy_size, h.angle_size)
+    np.testing.assert_allclose(w.mean(axis=1), 1.0, rtol=1e-12)
+    gw = g["heel_weights"].reshape(int(meta[3]), int(meta[6]))
+    np.testing.assert_allclose(gw.mean(axis=1), 1.0, rtol=1e-12)
+
+
+def test_tube_spectrum_is_physical(lib):
+    import dxmclib_gb300 as dx
+    t = dx.Tube(120)
+    t.setAlFiltration(2.5)
+    e = t.getEnergy()
+    s = t.getSpecter(e)
+    assert e[0] == 1 and e[-1] == 120 and len(e) == 120
+    assert s.sum() == pytest.approx(1.0)
+    mean = float((e * s).sum())
+    assert 45 < mean < 70
+    assert s[:10].sum() < 1e-6  # filtered away
+    t2 = dx.Tube(120)
+    t2.setAlFiltration(6.0)
+    assert float((e * t2.getSpecter(e)).sum()) > mean  # more filtration hardens the beam
+
+
+def test_capi_exports_every_declared_symbol(lib):
+    header = (REPO / "include" / "dxmc_gpu.h").read_text()
+    names = set(re.findall(r"^\s*(?:const\s+)?\w+[\s\*]+(dxmc_\w+)\s*\(", header, re.MULTILINE))
+    assert len(names) >= 25
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+    assert lib.dxmc_gpu_abi_version() == 1
+
+
+def test_invalid_inputs_are_rejected(lib):
+    from dxmclib_gb300 import _capi as A
+    prov = A.MaterialProvider()
+    assert lib.dxmc_physics_material(b"NotAMaterial42", -1.0, C.byref(prov)) == A.DXMC_ERR_INVALID
+    assert lib.dxmc_physics_material(b"H2O", -1.0, C.byref(prov)) == A.DXMC_ERR_INVALID  # formula without density
+    assert lib.dxmc_physics_material(b"H2O", 1.0, C.byref(prov)) == A.DXMC_OK
+    blob = C.c_void_p()
+    md = np.array([1.0])
+    assert lib.dxmc_lut_build_max_density(C.byref(prov), 0, md.ctypes.data_as(A.DP), 60.0, C.byref(blob)) == A.DXMC_ERR_INVALID
+    assert lib.dxmc_lut_build_max_density(C.byref(prov), 1, md.ctypes.data_as(A.DP), -5.0, C.byref(blob)) == A.DXMC_ERR_INVALID
+    lib.dxmc_physics_material_free(C.byref(prov))

@@ -1,0 +1,104 @@
+"""CPU tests: the oracle port (oracle/port, a C++ restatement of DXMClib's
+transport) against the reference's own results (golden fixtures), so the
+port can stand in for the reference where the reference cannot be built."""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from parity import assert_parity, compare_sparse
+
+REPO = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(REPO / "oracle" / "port"))
+import binding as port  # noqa: E402
+
+
+def _lut(names, material, density, max_energy):
+    import dxmclib_gb300 as dx
+    mats = [dx.Material(str(n)) for n in names]
+    md = np.zeros(len(mats))
+    np.maximum.at(md, np.asarray(material, np.int64).ravel(), np.asarray(density, np.float64).ravel())
+    return dx.LutBlob(mats, md, max_energy).info()
+
+
+def _pencil_exposures(histories):
+    import dxmclib_gb300 as dx
+    s = dx.PencilSource()
+    s.setPosition((0, 0, -200))
+    s.setPhotonEnergy(60.0)
+    s.setTotalExposures(10)
+    s.setHistoriesPerExposure(histories // 10)
+    m = s.exposures().as_matrix()
+    m[:, 18] = 60.0
+    return m
+
+
+@pytest.mark.parametrize("model", [0, 1, 2])
+def test_port_pencil_matches_reference(lib, golden, model):
+    g = golden(f"transport_pencil_m{model}.npz")
+    n = 64
+    mat = np.zeros(n ** 3, np.uint8)
+    dens = np.ones(n ** 3)
+    info = _lut(["Water, Liquid"], mat, dens, 60.0)
+    N = int(g["histories"])
+    e, e2, nev, secs, steps = port.transport(info, (n, n, n), (2, 2, 2), dens, mat, _pencil_exposures(N), model=model,
+                                             seed=17 + model)
+    d, v = port.ev_per_history(e, e2, N)
+    assert_parity(compare_sparse(g, d, v), f"port pencil m{model}")
+
+
+def test_port_cone_matches_reference(lib, golden):
+    import dxmclib_gb300 as dx
+    g = golden("transport_cone_m1.npz")
+    dims = tuple(int(x) for x in g["dims"])
+    info = _lut(g["names"], g["material"], g["density"], float(g["spec_energies"].max()))
+    src = dx.IsotropicSource()
+    src.setPosition((0, 0, -500))
+    src.setCollimationAngles(-0.12, 0.12, -0.1, 0.1)
+    src.setSpecter(g["spec_weights"], g["spec_energies"])
+    src.setTotalExposures(8)
+    N = int(g["histories"])
+    src.setHistoriesPerExposure(N // 8)
+    e, e2, nev, secs, steps = port.transport(info, dims, tuple(g["spacing"]), g["density"], g["material"],
+                                             src.exposures().as_matrix(), model=1, seed=5,
+                                             spectrum=(g["spec_energies"], g["spec_weights"]))
+    d, v = port.ev_per_history(e, e2, N)
+    assert_parity(compare_sparse(g, d, v), "port cone m1")
+
+
+def test_port_ct_matches_reference(lib, golden):
+    g = golden("transport_ct_m1.npz")
+    dims = tuple(int(x) for x in g["dims"])
+    info = _lut(g["names"], g["material"], g["density"], float(g["max_energy"]))
+    hm = g["heel_meta"]
+    heel = dict(energy_start=hm[1], energy_step=hm[2], energy_size=hm[3], angle_start=hm[4], angle_step=hm[5],
+                angle_size=hm[6], weights=g["heel_weights"])
+    e, e2, nev, secs, steps = port.transport(info, dims, tuple(g["spacing"]), g["density"], g["material"],
+                                             g["exposures"], model=1, seed=9,
+                                             spectrum=(g["spec_energies"], g["spec_weights"]), heel=heel)
+    d, v = port.ev_per_history(e, e2, int(g["histories"]))
+    assert_parity(compare_sparse(g, d, v), "port ct")
+
+
+def test_port_forced_matches_reference(lib, golden):
+    import dxmclib_gb300 as dx
+    g = golden("transport_forced_m1.npz")
+    dims = tuple(int(x) for x in g["dims"])
+    n = int(np.prod(dims))
+    mat = np.zeros(n, np.uint8)
+    dens = np.ones(n)
+    info = _lut(["Water, Liquid"], mat, dens, 50.0)
+    src = dx.IsotropicSource()
+    src.setPosition((0, 0, -300))
+    src.setCollimationAngles(-0.05, 0.05, -0.05, 0.05)
+    src.setSpecter([1.0], [50.0])
+    src.setTotalExposures(8)
+    N = int(g["histories"])
+    src.setHistoriesPerExposure(N // 8)
+    e, e2, nev, secs, steps = port.transport(info, dims, tuple(g["spacing"]), dens, mat, src.exposures().as_matrix(),
+                                             model=1, seed=3, spectrum=([50.0], [1.0]), measurement=g["measurement"])
+    d, v = port.ev_per_history(e, e2, N)
+    assert_parity(compare_sparse(g, d, v), "port forced")
