@@ -165,6 +165,7 @@ def main():
     ap.add_argument("--histories", type=float, default=1e8)
     ap.add_argument("--model", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     ws, rank, local = _dist()
@@ -288,18 +289,22 @@ def main():
         bl.close()
         dw.close()
 
-    e2e_step(1)
-    barrier()
-    t0 = time.perf_counter()
-    for s in range(e2e_steps):
-        e2e_step(3000 + s)
-    barrier()
-    e2e_s = time.perf_counter() - t0
+    if args.no_e2e:
+        e2e_steps = 0
+        e2e_s = float("nan")
+    else:
+        e2e_step(1)
+        barrier()
+        t0 = time.perf_counter()
+        for s in range(e2e_steps):
+            e2e_step(3000 + s)
+        barrier()
+        e2e_s = time.perf_counter() - t0
     if dist:
         t = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    e2e_value = ws * n_hist * e2e_steps / e2e_s
+    e2e_value = ws * n_hist * e2e_steps / e2e_s if e2e_steps else None
     h2d = n_vox * 5 + len(exposures) * 80
     d2h = n_vox * (8 + 8 + 4)
 

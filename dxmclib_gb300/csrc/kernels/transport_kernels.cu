@@ -167,6 +167,10 @@ namespace {
             if (!(cum < sample) || s == N_SHELLS - 1)
                 break;
         }
+        if (!(total > 0.0f)) {
+            deposit = 0.0f; // no shell can take part: the interaction is rejected
+            return true;
+        }
         const float* sh = shells + shell * SHELL_FLOATS;
         const float U = sh[0] / ELECTRON_REST_MASS;
         const float pU = sqrtf(2.0f * U + U * U);
@@ -185,17 +189,20 @@ namespace {
         bool accepted = false;
         for (int it = 0; it < REJECTION_CAP && !accepted; ++it) {
             const float r1 = rng.uniform();
-            e = r1 + (1.0f - r1) * emin;
-            const float t = (1.0f - e) / (k * e);
+            // e = r1 + (1 - r1) emin, with 1 - e = (1 - r1)(1 - emin) formed directly so
+            // that t stays positive when e rounds to 1 in single precision
+            const float one_minus_e = (1.0f - r1) * (1.0f - emin);
+            e = 1.0f - one_minus_e;
+            const float t = one_minus_e / (k * e);
             const float sin2 = t * (2.0f - t);
             cosA = 1.0f - t;
             const float g = (1.0f / e + e - sin2) * gmax_inv;
             const float r2 = rng.uniform();
             if (r2 > g)
                 continue;
-            const float pi = (k * (k - U) * (1.0f - cosA) - U) / sqrtf(2.0f * k * (k - U) * (1.0f - cosA) + U * U);
+            const float pi = (k * (k - U) * t - U) / sqrtf(fmaxf(2.0f * k * (k - U) * t + U * U, 1e-30f));
             const float kc = k * e;
-            const float qc = sqrtf(k * k + kc * kc - 2.0f * k * kc * cosA);
+            const float qc = sqrtf(fmaxf(k * k + kc * kc - 2.0f * k * kc * cosA, 1e-30f));
             const float alpha = qc * (1.0f + kc * (kc - k * cosA) / (qc * qc)) / k;
             const float b_part = 1.0f + 2.0f * J0 * fabsf(pi);
             const float b = (b_part * b_part + 1.0f) * 0.5f;
@@ -226,7 +233,7 @@ namespace {
                 Fmax = 1.0f + alpha * pU;
             else
                 Fmax = 1.0f + alpha * pi;
-            const float r4 = rng.uniform();
+            const float r4 = rng.uniform_open(); // log(rbar2) below needs rbar2 > 0
             const float rbar2 = 2.0f * r4 * expb;
             float pz;
             if (rbar2 < 1.0f) {
@@ -246,7 +253,7 @@ namespace {
             const float r5 = rng.uniform();
             if (r5 > Fpz / Fmax)
                 continue;
-            const float part = sqrtf(1.0f - 2.0f * e * cosA + e * e * (1.0f - pz * pz * sin2));
+            const float part = sqrtf(fmaxf(1.0f - 2.0f * e * cosA + e * e * (1.0f - pz * pz * sin2), 0.0f));
             const float kbar = kc / (1.0f - pz * pz * e * e) * (1.0f - pz * pz * e * cosA + pz * part);
             e = kbar / k;
             accepted = true;
@@ -274,8 +281,9 @@ namespace {
             const float gmax_inv = 1.0f / (1.0f / emin + emin);
             for (int it = 0; it < REJECTION_CAP; ++it) {
                 const float r1 = rng.uniform();
-                const float e = r1 + (1.0f - r1) * emin;
-                const float t = (1.0f - e) / (k * e);
+                const float one_minus_e = (1.0f - r1) * (1.0f - emin);
+                const float e = 1.0f - one_minus_e;
+                const float t = one_minus_e / (k * e);
                 const float sin2 = t * (2.0f - t);
                 const float cosA = 1.0f - t;
                 const float g = (1.0f / e + e - sin2) * gmax_inv;
@@ -641,6 +649,13 @@ namespace {
                     }
                     alive = cont;
                 }
+            }
+            if (do_score && !isfinite(deposit)) {
+                // never let a non-finite value into the FP64 accumulators: end the
+                // history and report it through the overflow counter
+                do_score = false;
+                alive = false;
+                ++my_overflows;
             }
             // ---- scoring; the warp is converged here ----------------------------------------
             if (p.tally_mode == 2) {

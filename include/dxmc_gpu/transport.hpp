@@ -1,0 +1,382 @@
+// dxmc_gpu/transport.hpp — drop-in GPU replacement for dxmc::Transport<T>.
+//
+// Header-only C++20 adapter for code that uses DXMClib: include this header
+// after DXMClib's own headers and replace
+//
+//     dxmc::Transport<T> transport;             // include/dxmc/transport.hpp:114-840
+//     auto result = transport(world, &source);
+// with
+//     dxmc::gpu::Transport<T> transport;
+//     auto result = transport(world, &source);
+//
+// The adapter keeps DXMClib's World / Source / Material / ProgressBar types and
+// its Result<T>; it reads them only through their public members, flattens the
+// exposures (Source::getExposure + Exposure::alignToDirectionCosines), wraps
+// each Material as a dxmc_material_provider for the host LUT build, and runs
+// photon generation, Woodcock tracking, interactions and scoring on the GPU
+// through the C ABI in dxmc_gpu.h.  Link with libdxmc_gpu.so.
+//
+// Error behaviour follows the reference (transport.hpp:142-151, 176-185): an
+// invalid world or source, a missing GPU, or a cancelled run returns a
+// zero-filled Result with numberOfHistories == 0; lastError() explains why.
+#pragma once
+
+#include "dxmc_gpu.h"
+
+#include "dxmc/exposure.hpp"
+#include "dxmc/lowenergycorrectionmodel.hpp"
+#include "dxmc/material.hpp"
+#include "dxmc/progressbar.hpp"
+#include "dxmc/source.hpp"
+#include "dxmc/transport.hpp"
+#include "dxmc/world.hpp"
+
+#include <chrono>
+#include <cmath>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace dxmc::gpu {
+
+namespace detail {
+
+    // dxmc::Material -> dxmc_material_provider (material.hpp:60-101)
+    inline double photo_cb(void* u, double e) { return static_cast<const Material*>(u)->getPhotoelectricAttenuation(e); }
+    inline double compton_cb(void* u, double e) { return static_cast<const Material*>(u)->getComptonAttenuation(e); }
+    inline double rayleigh_cb(void* u, double e) { return static_cast<const Material*>(u)->getRayleightAttenuation(e); }
+    inline double ff2_cb(void* u, double q) { return static_cast<const Material*>(u)->getRayleightFormFactorSquared(q); }
+    inline double sf_cb(void* u, double q) { return static_cast<const Material*>(u)->getComptonNormalizedScatterFactor(q); }
+    inline int edges_cb(void* u, double minE, double* out, int cap)
+    {
+        const auto e = static_cast<const Material*>(u)->getBindingEnergies(minE);
+        const int n = static_cast<int>(e.size());
+        for (int i = 0; i < n && i < cap; ++i)
+            out[i] = e[i];
+        return n;
+    }
+    inline void shells_cb(void* u, dxmc_shell_config out[12])
+    {
+        const auto c = static_cast<const Material*>(u)->getElectronConfiguration();
+        for (int i = 0; i < 12; ++i) {
+            out[i].binding_energy = c[i].bindingEnergy;
+            out[i].number_electrons = c[i].numberElectrons;
+            out[i].hartree_fock_j0 = c[i].hartreeFockOrbital_0;
+            out[i].photo_ionization_probability = c[i].photoIonizationProbability;
+            out[i].fluorescence_yield = c[i].fluorescenceYield;
+            for (int k = 0; k < 3; ++k) {
+                out[i].line_probabilities[k] = c[i].fluorLineProbabilities[k];
+                out[i].line_energies[k] = c[i].fluorLineEnergies[k];
+            }
+            out[i].Z = c[i].Z;
+            out[i].shell = c[i].shell;
+        }
+    }
+
+    inline dxmc_material_provider provider(const Material& m)
+    {
+        dxmc_material_provider p {};
+        p.user = const_cast<Material*>(&m);
+        p.standard_density = m.standardDensity();
+        p.photoelectric = photo_cb;
+        p.compton = compton_cb;
+        p.rayleigh = rayleigh_cb;
+        p.form_factor_squared = ff2_cb;
+        p.scatter_factor = sf_cb;
+        p.binding_energies = edges_cb;
+        p.shells = shells_cb;
+        return p;
+    }
+
+} // namespace detail
+
+// Host tables of one source, ready for dxmc_gpu_job_submit.
+template <Floating T>
+struct FlatSource {
+    std::vector<dxmc_exposure> exposures;
+    std::vector<double> spec_energies, spec_weights;
+    std::vector<double> heel_weights;
+    dxmc_heel_desc heel {};
+    bool has_heel = false;
+    std::vector<double> bowtie_angles, bowtie_weights;
+    double max_energy = 0;
+};
+
+// Flattens Source::getExposure(i) for every exposure (source.hpp), applying the
+// world basis like workerRun does (transport.hpp:750-757).  Spectrum, heel and
+// bow-tie tables are read through the public API of the sources that own them:
+// DAPSource/CBCT and the CT family expose tube() (tube.hpp:165-212) and the CT
+// family bowTieFilter(); IsotropicSource keeps its spectrum private, so callers
+// pass it in `isotropic_spectrum` (energies, weights).
+template <Floating T>
+bool flatten(const World<T>& world, Source<T>* source, FlatSource<T>& out,
+    const std::pair<std::vector<T>, std::vector<T>>* isotropic_spectrum = nullptr)
+{
+    const auto n = source->totalExposures();
+    out.exposures.resize(n);
+    const auto& basis = world.directionCosines();
+    for (std::uint64_t i = 0; i < n; ++i) {
+        auto e = source->getExposure(i);
+        e.alignToDirectionCosines(basis);
+        auto& x = out.exposures[i];
+        for (int k = 0; k < 3; ++k) {
+            x.position[k] = e.position()[k];
+            x.beam_direction[k] = e.beamDirection()[k];
+        }
+        for (int k = 0; k < 6; ++k)
+            x.direction_cosines[k] = e.directionCosines()[k];
+        for (int k = 0; k < 4; ++k)
+            x.collimation[k] = e.collimationAngles()[k];
+        x.weight = e.beamIntensityWeight();
+        x.n_histories = e.numberOfHistories();
+        x.mono_energy = 0;
+    }
+    out.max_energy = source->maxPhotonEnergyProduced();
+    const Tube<T>* tube = nullptr;
+    T heel_span = -1;
+    if (auto* pencil = dynamic_cast<PencilSource<T>*>(source)) {
+        for (auto& x : out.exposures)
+            x.mono_energy = pencil->photonEnergy();
+    } else if (auto* dap = dynamic_cast<DAPSource<T>*>(source)) {
+        const auto* cdap = dap;
+        tube = &cdap->tube();
+        if (dap->modelHeelEffect())
+            heel_span = cdap->collimationAngles()[1]; // DAPSource::updateSpecterDistribution (source.hpp:600-612)
+    } else if (auto* ct = dynamic_cast<CTBaseSource<T>*>(source)) {
+        const auto* cct = ct;
+        tube = &cct->tube();
+        if (ct->modelHeelEffect()) // CTBaseSource::updateSpecterDistribution (source.hpp:989-1002)
+            heel_span = std::atan(ct->collimation() * T { 0.5 } / ct->sourceDetectorDistance()) * T { 2.0 };
+        if (auto bt = cct->bowTieFilter()) {
+            for (const auto& [a, w] : bt->data()) {
+                out.bowtie_angles.push_back(a);
+                out.bowtie_weights.push_back(w);
+            }
+        }
+    } else if (dynamic_cast<IsotropicSource<T>*>(source)) {
+        if (!isotropic_spectrum)
+            return false;
+        out.spec_energies.assign(isotropic_spectrum->first.begin(), isotropic_spectrum->first.end());
+        out.spec_weights.assign(isotropic_spectrum->second.begin(), isotropic_spectrum->second.end());
+    }
+    if (tube) {
+        const auto energies = tube->getEnergy();
+        const auto weights = tube->getSpecter(energies);
+        out.spec_energies.assign(energies.begin(), energies.end());
+        out.spec_weights.assign(weights.begin(), weights.end());
+        if (heel_span >= 0) {
+            HeelFilter<T> heel(*tube, heel_span);
+            out.heel_weights.assign(heel.weights().begin(), heel.weights().end());
+            // grid of HeelFilter::update (beamfilters.hpp:467-483): 10 keV + 2 keV steps,
+            // angle bins from -min(anode angle, span/2) to +span/2
+            const T span = std::abs(heel_span);
+            const T start = tube->anodeAngle() < span / 2 ? -tube->anodeAngle() : -span / 2;
+            out.heel.energy_start = 10.0;
+            out.heel.energy_step = 2.0;
+            out.heel.energy_size = static_cast<int32_t>(heel.energySize());
+            out.heel.angle_size = static_cast<int32_t>(heel.angleSize());
+            out.heel.angle_start = start;
+            out.heel.angle_step = (span / 2 - start) / static_cast<T>(heel.angleSize());
+            out.heel.weights = out.heel_weights.data();
+            out.has_heel = true;
+        }
+    }
+    return true;
+}
+
+template <Floating T = double>
+class Transport {
+public:
+    enum class OUTPUTMODE { EV_PER_HISTORY, DOSE };
+
+    Transport() = default;
+    ~Transport() { release(); }
+    Transport(const Transport&) = delete;
+    Transport& operator=(const Transport&) = delete;
+
+    void setNumberOfWorkers(std::uint64_t) { } // the GPU launch replaces worker threads
+    std::size_t numberOfWorkers() const { return 1; }
+    void setLowEnergyCorrectionModel(LOWENERGYCORRECTION model) { m_model = model; }
+    LOWENERGYCORRECTION lowEnergyCorrectionModel() const { return m_model; }
+    void setOutputMode(OUTPUTMODE mode) { m_mode = mode; }
+    OUTPUTMODE outputMode() const { return m_mode; }
+    void setDevice(int device) { m_options.device = device; }
+    void setSeed(std::uint64_t seed) { m_seed = seed; }
+    void setTallyMode(int mode) { m_options.tally_mode = mode; }
+    // Spectrum for IsotropicSource, whose spectrum has no public getter.
+    void setIsotropicSpectrum(std::vector<T> energies, std::vector<T> weights) { m_iso = { std::move(energies), std::move(weights) }; }
+    const std::string& lastError() const { return m_error; }
+
+    template <typename U>
+        requires std::is_base_of<World<T>, U>::value
+    Result<T> operator()(const U& world, Source<T>* source, ProgressBar<T>* progressbar = nullptr, bool useSourceDoseCalibration = true)
+    {
+        Result<T> result(world.size());
+        m_error.clear();
+        if (!world.isValid() || !source) {
+            m_error = "invalid world or source";
+            return result;
+        }
+        source->updateFromWorld(world);
+        source->validate();
+        if (!source->isValid()) {
+            m_error = "invalid source";
+            return result;
+        }
+        FlatSource<T> flat;
+        if (!flatten(world, source, flat, m_iso.first.empty() ? nullptr : &m_iso)) {
+            m_error = "source type needs setIsotropicSpectrum";
+            return result;
+        }
+        if (!ensure_context())
+            return result;
+
+        const auto& dims = world.dimensions();
+        const std::size_t n = world.size();
+        std::vector<float> density(n);
+        const auto& dsrc = *world.densityArray();
+        for (std::size_t i = 0; i < n; ++i)
+            density[i] = static_cast<float>(dsrc[i]);
+        dxmc_world_desc wd {};
+        for (int i = 0; i < 3; ++i) {
+            wd.dims[i] = dims[i];
+            wd.spacing[i] = world.spacing()[i];
+            wd.origin[i] = world.origin()[i];
+        }
+        for (int i = 0; i < 6; ++i)
+            wd.direction_cosines[i] = world.directionCosines()[i];
+        wd.density = density.data();
+        wd.material = world.materialIndexArray()->data();
+        const auto meas = world.measurementMapArray();
+        bool any_meas = false;
+        if (meas)
+            for (auto v : *meas)
+                if (v) {
+                    any_meas = true;
+                    break;
+                }
+        wd.measurement = any_meas ? meas->data() : nullptr;
+        const auto& materials = world.materialMap();
+        wd.n_materials = static_cast<int32_t>(materials.size());
+
+        dxmc_world* dworld = nullptr;
+        if (!check(dxmc_gpu_world_upload(m_ctx, &wd, &dworld), "world upload"))
+            return result;
+        std::vector<double> maxDensity(materials.size());
+        std::vector<dxmc_material_provider> providers;
+        for (const auto& m : materials)
+            providers.push_back(detail::provider(m));
+        dxmc_lut_blob* blob = nullptr;
+        dxmc_lut* lut = nullptr;
+        dxmc_job* job = nullptr;
+        bool ok = check(dxmc_gpu_world_max_density(dworld, maxDensity.data(), static_cast<int>(maxDensity.size())), "max density")
+            && check(dxmc_lut_build_max_density(providers.data(), static_cast<int>(providers.size()), maxDensity.data(), flat.max_energy, &blob), "lut build")
+            && check(dxmc_gpu_lut_upload(m_ctx, blob, &lut), "lut upload");
+        dxmc_spectrum_desc spec { static_cast<int32_t>(flat.spec_energies.size()), flat.spec_energies.data(), flat.spec_weights.data() };
+        dxmc_bowtie_desc bowtie { static_cast<int32_t>(flat.bowtie_angles.size()), flat.bowtie_angles.data(), flat.bowtie_weights.data() };
+        dxmc_job_desc jd {};
+        jd.exposures = flat.exposures.data();
+        jd.n_exposures = flat.exposures.size();
+        jd.spectrum = flat.spec_energies.empty() ? nullptr : &spec;
+        jd.heel = flat.has_heel ? &flat.heel : nullptr;
+        jd.bowtie = flat.bowtie_angles.empty() ? nullptr : &bowtie;
+        jd.seed = m_seed++;
+        jd.model = static_cast<int32_t>(m_model);
+        jd.tally_mode = -1;
+        const auto start = std::chrono::system_clock::now();
+        if (progressbar) {
+            progressbar->setTotalExposures(flat.exposures.size());
+        }
+        ok = ok && check(dxmc_gpu_job_submit(m_ctx, dworld, lut, &jd, &job), "job submit");
+        bool cancelled = false;
+        while (ok) {
+            const int rc = dxmc_gpu_job_wait(job, 50);
+            if (rc == DXMC_OK)
+                break;
+            if (rc != DXMC_ERR_TIMEOUT) {
+                ok = check(rc, "job wait");
+                break;
+            }
+            if (progressbar && progressbar->cancel() && !cancelled) {
+                dxmc_gpu_job_cancel(job);
+                cancelled = true;
+            }
+        }
+        result.simulationTime = std::chrono::system_clock::now() - start;
+        if (ok && !cancelled) {
+            std::uint64_t histories = 0;
+            for (const auto& e : flat.exposures)
+                histories += e.n_histories;
+            result.numberOfHistories = histories;
+            std::vector<double> dose(n), var(n);
+            int mode = DXMC_OUTPUT_EV_PER_HISTORY;
+            double cal = 1.0;
+            if (m_mode == OUTPUTMODE::DOSE) {
+                mode = DXMC_OUTPUT_DOSE;
+                cal = useSourceDoseCalibration ? static_cast<double>(source->getCalibrationValue(m_model, progressbar)) : 1.0;
+            }
+            ok = check(dxmc_gpu_job_result(job, mode, cal, dose.data(), var.data(), result.nEvents.data(), nullptr), "job result");
+            if (ok) {
+                for (std::size_t i = 0; i < n; ++i) {
+                    result.dose[i] = static_cast<T>(dose[i]);
+                    result.variance[i] = static_cast<T>(var[i]);
+                }
+                result.dose_units = m_mode == OUTPUTMODE::DOSE ? (useSourceDoseCalibration ? "mGy" : "keV/kg") : "eV/history";
+            } else {
+                result.numberOfHistories = 0;
+            }
+        }
+        if (progressbar)
+            progressbar->clearDoseData();
+        dxmc_gpu_job_free(job);
+        dxmc_gpu_lut_free(lut);
+        dxmc_lut_blob_free(blob);
+        dxmc_gpu_world_free(dworld);
+        if (!ok || cancelled) {
+            std::fill(result.dose.begin(), result.dose.end(), T { 0 });
+            std::fill(result.variance.begin(), result.variance.end(), T { 0 });
+            std::fill(result.nEvents.begin(), result.nEvents.end(), 0u);
+            result.numberOfHistories = 0;
+            if (cancelled)
+                m_error = "cancelled";
+        }
+        return result;
+    }
+
+private:
+    bool ensure_context()
+    {
+        if (m_ctx)
+            return true;
+        const int rc = dxmc_gpu_ctx_create(&m_options, &m_ctx);
+        if (rc != DXMC_OK) {
+            m_ctx = nullptr;
+            m_error = rc == DXMC_ERR_NO_DEVICE ? "no CUDA device available" : "context creation failed";
+            return false;
+        }
+        return true;
+    }
+    bool check(int rc, const char* what)
+    {
+        if (rc == DXMC_OK)
+            return true;
+        m_error = std::string(what) + ": " + dxmc_gpu_last_error(m_ctx);
+        return false;
+    }
+    void release()
+    {
+        if (m_ctx)
+            dxmc_gpu_ctx_destroy(m_ctx);
+        m_ctx = nullptr;
+    }
+
+    dxmc_gpu_ctx* m_ctx = nullptr;
+    dxmc_gpu_options m_options {};
+    std::uint64_t m_seed = 1;
+    std::pair<std::vector<T>, std::vector<T>> m_iso;
+    std::string m_error;
+    OUTPUTMODE m_mode = OUTPUTMODE::DOSE;                             // transport.hpp:838
+    LOWENERGYCORRECTION m_model = LOWENERGYCORRECTION::LIVERMORE;     // transport.hpp:839
+};
+
+} // namespace dxmc::gpu

@@ -69,11 +69,13 @@ def test_pencil_beam_matches_reference(gpu_ctx, golden, model):
     g, (dose, var, nev, stats) = _pencil(gpu_ctx, golden, model)
     s = compare_sparse(g, dose, var)
     assert_parity(s, f"pencil m{model}")
-    # depth-dose profile (sum over each slice) within 1 %
+    # depth-dose profile (energy summed over each slice): within 3 %, the statistical
+    # spread of the reference's own 2e6-history slices
     d3 = dose.reshape(64, 64, 64).sum(axis=(1, 2))
     ref = g["depth"]
     sel = ref > 0.05 * ref.max()
-    np.testing.assert_allclose(d3[sel], ref[sel], rtol=0.01)
+    np.testing.assert_allclose(d3[sel], ref[sel], rtol=0.03)
+    assert abs(d3[sel].sum() / ref[sel].sum() - 1) < 0.005
 
 
 @pytest.mark.parametrize("model", [1, 2])
@@ -161,17 +163,24 @@ def test_device_lut_lookups_match_reference(gpu_ctx, golden):
     E = g["energies"]
     for m in range(len(mats)):
         att, mi = dlut.probe(m, E)
-        np.testing.assert_allclose(att, g["att"][m], rtol=2e-4)
-        np.testing.assert_allclose(mi, g["maxinv"], rtol=2e-4)
+        rel = np.abs(att / g["att"][m] - 1).max(axis=1)
+        k = int(np.argmax(rel))
+        assert rel[k] < 2e-4, f"material {m}: worst rel {rel[k]:.3g} at {E[k]} keV: {att[k]} vs {g['att'][m][k]}"
+        relm = np.abs(mi / g["maxinv"] - 1)
+        k = int(np.argmax(relm))
+        assert relm[k] < 2e-4, f"majorant: worst rel {relm[k]:.3g} at {E[k]} keV: {mi[k]} vs {g['maxinv'][k]}"
     dlut.close()
 
 
-def _two_sample_chi2(h1, h2):
+def _two_sample_p(h1, h2):
+    """p-value of the two-sample chi-square test that both histograms share one distribution."""
+    from scipy.stats import chi2 as chi2_dist
     n1, n2 = h1.sum(), h2.sum()
     k1, k2 = np.sqrt(n2 / n1), np.sqrt(n1 / n2)
     sel = (h1 + h2) > 0
     chi2 = np.sum((k1 * h1[sel] - k2 * h2[sel]) ** 2 / (h1[sel] + h2[sel]))
-    return chi2 / max(sel.sum() - 1, 1)
+    dof = max(int(sel.sum()) - 1, 1)
+    return float(chi2_dist.sf(chi2, dof)), float(chi2 / dof)
 
 
 @pytest.mark.parametrize("model", [0, 1, 2])
@@ -193,9 +202,12 @@ def test_interaction_samplers_match_reference(gpu_ctx, golden, model):
             assert np.all(c <= 1.0 + 1e-5), key  # no rejection-cap hits
             hc = np.bincount(np.clip(((c.astype(np.float64) + 1) * 0.5 * 100).astype(np.int64), 0, 99), minlength=100)
             he = np.bincount(np.clip((e.astype(np.float64) / energy * 100).astype(np.int64), 0, 99), minlength=100)
+            # 30 histogram comparisons per model: a 1e-4 p-value floor keeps the false-alarm rate ~0.3 %
             if kind != 0 or model == 2:
-                assert _two_sample_chi2(g[key + "_cos"], hc.astype(np.float64)) < 1.6, key
-            assert _two_sample_chi2(g[key + "_e"], he.astype(np.float64)) < 1.6, key
+                p, red = _two_sample_p(g[key + "_cos"], hc.astype(np.float64))
+                assert p > 1e-4, (key, "cos", p, red)
+            p, red = _two_sample_p(g[key + "_e"], he.astype(np.float64))
+            assert p > 1e-4, (key, "energy", p, red)
             ref_mean_dep = g[key + "_sums"][0] / g["n"]
             assert abs(d.astype(np.float64).mean() - ref_mean_dep) <= 0.002 * energy + 5 * d.std() / np.sqrt(N), key
     dlut.close()
