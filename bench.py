@@ -324,7 +324,9 @@ def main():
                        "l2": "inputs larger than L2 (420 MB voxels + 1 GB tallies)", "parallelism": f"replicas{ws}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind,
-                         "traffic": None if not traffic else traffic.get("dram_bytes_per_launch_scaled"),
+                         # DRAM bytes per launch from the committed ncu capture of a 1e7-history
+                         # launch, scaled by histories (traffic grows in proportion)
+                         "traffic": None if not traffic else traffic["dram_bytes_per_history"] * n_hist,
                          "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": float(kern_ms.mean()),
                          "steps_per_history": steps_per_hist, "deposits_per_history": deps_per_hist},
             "cpu_baseline": cpu,
