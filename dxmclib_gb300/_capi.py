@@ -156,6 +156,7 @@ SIGNATURES = {
     "dxmc_gpu_job_result": (C.c_int, [VP, C.c_int, D, DP, DP, U32P, C.POINTER(JobStats)]),
     "dxmc_gpu_job_free": (None, [VP]),
     "dxmc_gpu_probe_lut": (C.c_int, [VP, VP, C.c_int, DP, C.c_int, DP, DP]),
+    "dxmc_gpu_transport_noalloc": (C.c_int, [VP, VP, VP, C.POINTER(JobDesc), VP, VP, C.POINTER(JobStats)]),
     "dxmc_gpu_probe_interactions": (C.c_int, [VP, VP, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_uint64, FP, FP, FP]),
 }
 

@@ -31,6 +31,7 @@ HOST_SOURCES = [
 CUDA_SOURCES = [
     CSRC / "kernels" / "transport_kernels.cu",
     CSRC / "device" / "capi_device.cu",
+    CSRC / "device" / "noalloc.cu",
 ]
 INCLUDES = [f"-I{REPO / 'include'}", f"-I{CSRC}"]
 

@@ -839,3 +839,25 @@ int dxmc_gpu_probe_interactions(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, 
 }
 
 } // extern "C"
+
+// Read-only accessors used by the no-allocation entry point (noalloc.cu).
+namespace dxmc_gb300::capi {
+int ctx_device(const dxmc_gpu_ctx* ctx) { return ctx->device; }
+cudaStream_t ctx_stream(const dxmc_gpu_ctx* ctx) { return ctx->stream; }
+int ctx_sm_count(const dxmc_gpu_ctx* ctx) { return ctx->sm_count; }
+size_t ctx_max_smem(const dxmc_gpu_ctx* ctx) { return ctx->max_smem_optin; }
+void ctx_set_error(dxmc_gpu_ctx* ctx, const std::string& msg) { ctx->last_error = msg; }
+std::mutex& ctx_mutex(dxmc_gpu_ctx* ctx) { return ctx->mutex; }
+const dev::WorldParams* world_params(const dxmc_world* w, const dxmc_gpu_ctx** owner, int* n_materials)
+{
+    *owner = w->ctx;
+    *n_materials = w->n_materials;
+    return &w->params;
+}
+const float* lut_image(const dxmc_lut* l, dev::LutMeta* meta, const dxmc_gpu_ctx** owner)
+{
+    *owner = l->ctx;
+    *meta = l->meta;
+    return l->image;
+}
+} // namespace dxmc_gb300::capi

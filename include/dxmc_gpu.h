@@ -255,6 +255,27 @@ int dxmc_gpu_job_result(dxmc_job* job, int output_mode, double calibration,
     double* dose, double* variance, uint32_t* n_events, dxmc_job_stats* stats);
 void dxmc_gpu_job_free(dxmc_job* job);
 
+/* ---- transport without allocation ------------------------------------------ */
+/* No counterpart in the reference.  Runs the same transport as
+ * dxmc_gpu_job_submit + dxmc_gpu_job_result(DXMC_OUTPUT_RAW) for callers that
+ * cannot allocate device memory once they are running (an application that
+ * hands the library a fixed arena, a real-time loop that must not reach the
+ * allocator): every piece of scratch the job needs lives in one fixed-size
+ * static device array inside the library (about 2.2 MB per device, held until
+ * the process exits), and the call makes no cudaMalloc / cudaFree or other
+ * allocating call.  The caller passes the resident world and LUT and its own
+ * device outputs: tally[2 * n_voxels] (voxel i: energy imparted sum at 2i,
+ * sum of squares at 2i + 1, keV) and n_events[n_voxels]; both are cleared by
+ * the call.  Limits: 8192 exposures, 2048 spectrum bins, 8192 heel weights,
+ * 1024 bow-tie points; larger jobs return DXMC_ERR_INVALID with a message.
+ * FP64 tallies only (job->tally_mode is ignored).  The call blocks until the
+ * transport has finished; stats may be NULL (its times are host wall time).
+ * All calls share the static array, so calls that overlap on the GPU race:
+ * issue them one at a time.  The first call on a device looks the array up on
+ * that device; make it before any stream capture. */
+int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_job_desc* job,
+    double* tally, uint32_t* n_events, dxmc_job_stats* stats);
+
 /* ---- device probes for component parity tests ----------------------------- */
 /* Runs the device LUT lookup on energies[n]: out_att[n*3], out_maxinv[n]. */
 int dxmc_gpu_probe_lut(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, const double* energies, int n,
