@@ -167,6 +167,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--regen", type=int, default=0, help="warp refill threshold (0 = library default)")
+    ap.add_argument("--interact", type=int, default=0, help="interaction-pass threshold (0 = library default)")
+    ap.add_argument("--layout", type=int, default=0, help="0 = compact palette when possible, 1 = 8-byte voxels")
+    ap.add_argument("--block-size", type=int, default=0)
+    ap.add_argument("--blocks-per-sm", type=int, default=0)
     args = ap.parse_args()
     ws, rank, local = _dist()
     metric = "histories/s"
@@ -214,8 +219,9 @@ def main():
 
     wl = build_workload(histories)
     world, src = wl.world, wl.source
-    ctx = dx.GpuContext(device=device)
-    dworld = dx.DeviceWorld(ctx, world)
+    ctx = dx.GpuContext(device=device, block_size=args.block_size, blocks_per_sm=args.blocks_per_sm,
+                        regen_threshold=args.regen, interact_threshold=args.interact)
+    dworld = dx.DeviceWorld(ctx, world, layout=args.layout)
     md = dworld.max_density()
     blob = dx.LutBlob(world.materialMap(), md, src.maxPhotonEnergyProduced())
     dlut = dx.DeviceLut(ctx, blob)
@@ -278,7 +284,7 @@ def main():
     e2e_steps = max(1, min(args.steps, 3))
 
     def e2e_step(seed):
-        dw = dx.DeviceWorld(ctx, e2e_world)
+        dw = dx.DeviceWorld(ctx, e2e_world, layout=args.layout)
         bl = dx.LutBlob(e2e_world.materialMap(), dw.max_density(), src.maxPhotonEnergyProduced())
         dl = dx.DeviceLut(ctx, bl)
         ex = src.exposures(e2e_world.directionCosines())
@@ -321,7 +327,9 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": wl.name, "histories_per_step": n_hist, "exposures": len(exposures),
                        "model": ["NONE", "LIVERMORE", "IA"][args.model], "tally": "fp64",
-                       "l2": "inputs larger than L2 (420 MB voxels + 1 GB tallies)", "parallelism": f"replicas{ws}"},
+                       "l2": "inputs larger than L2 (420 MB voxels + 1 GB tallies)", "parallelism": f"replicas{ws}",
+                       "voxel_layout": "palette-u8" if args.layout == 0 else "8-byte",
+                       "regen_threshold": args.regen or "default", "interact_threshold": args.interact or "default"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind,
                          # DRAM bytes per launch from the committed ncu capture of a 1e7-history

@@ -101,13 +101,14 @@ class GpuOptions(C.Structure):
     _fields_ = [
         ("device", C.c_int32), ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32),
         ("tally_mode", C.c_int32), ("memory_budget", C.c_uint64),
+        ("regen_threshold", C.c_int32), ("interact_threshold", C.c_int32),
     ]
 
 
 class WorldDesc(C.Structure):
     _fields_ = [
         ("dims", C.c_uint64 * 3), ("spacing", D * 3), ("origin", D * 3), ("direction_cosines", D * 6),
-        ("density", FP), ("material", U8P), ("measurement", U8P), ("n_materials", C.c_int32), ("pad", C.c_int32),
+        ("density", FP), ("material", U8P), ("measurement", U8P), ("n_materials", C.c_int32), ("layout", C.c_int32),
     ]
 
 

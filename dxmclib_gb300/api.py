@@ -726,9 +726,10 @@ class GpuContext:
     """Owns a dxmc_gpu_ctx; one per device per process is enough."""
 
     def __init__(self, device: int = 0, block_size: int = 0, blocks_per_sm: int = 0, tally_mode: int = A.TALLY_F64,
-                 memory_budget: int = 0):
+                 memory_budget: int = 0, regen_threshold: int = 0, interact_threshold: int = 0):
         self.lib = A.load()
-        opts = A.GpuOptions(device, block_size, blocks_per_sm, tally_mode, memory_budget)
+        opts = A.GpuOptions(device, block_size, blocks_per_sm, tally_mode, memory_budget, regen_threshold,
+                            interact_threshold)
         self.handle = C.c_void_p()
         A.check(self.lib.dxmc_gpu_ctx_create(C.byref(opts), C.byref(self.handle)), None, "dxmc_gpu_ctx_create")
 
@@ -745,7 +746,7 @@ class GpuContext:
 
 
 class DeviceWorld:
-    def __init__(self, ctx: GpuContext, world: World):
+    def __init__(self, ctx: GpuContext, world: World, layout: int = 0):
         if not world.isValid():
             raise ValueError("invalid world")
         self.ctx = ctx
@@ -762,6 +763,7 @@ class DeviceWorld:
         d.material = mat.ctypes.data_as(A.U8P)
         d.measurement = meas.ctypes.data_as(A.U8P) if meas is not None and meas.any() else None
         d.n_materials = len(world.materialMap())
+        d.layout = int(layout)
         self.handle = C.c_void_p()
         A.check(ctx.lib.dxmc_gpu_world_upload(ctx.handle, C.byref(d), C.byref(self.handle)), ctx.handle, "dxmc_gpu_world_upload")
 

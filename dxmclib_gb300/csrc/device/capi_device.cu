@@ -19,6 +19,11 @@
 
 using namespace dxmc_gb300;
 
+// Warp scheduling of the transport kernel: refill idle lanes once this many
+// are idle; run the per-type interaction passes once this many lanes wait.
+constexpr int DEFAULT_REGEN_THRESHOLD = 16;
+constexpr int DEFAULT_INTERACT_THRESHOLD = 8;
+
 struct dxmc_gpu_ctx {
     int device = 0;
     int sm_count = 0;
@@ -34,6 +39,8 @@ struct dxmc_gpu_ctx {
 struct dxmc_world {
     dxmc_gpu_ctx* ctx = nullptr;
     dev::Voxel* voxels = nullptr;
+    uint8_t* palette_index = nullptr;      // compact layout, null if not used
+    dev::PaletteEntry* palette = nullptr;
     uint64_t dims[3] {};
     double spacing[3] {};
     double origin[3] {};
@@ -92,6 +99,8 @@ int cuda_fail(dxmc_gpu_ctx* ctx, cudaError_t e, const char* what)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+size_t dev_palette_table_bytes();
+
 // Safe extents exactly as World<float>::updateMatrixExtent (world.hpp:55-68).
 void world_extents(const uint64_t dims[3], const double spacing[3], const double origin[3], float lo[3], float hi[3])
 {
@@ -125,6 +134,82 @@ __global__ void check_materials_kernel(const uint8_t* __restrict__ material, uin
         if (material[i] >= n_materials)
             atomicOr(bad, 1u);
 }
+
+// ---- compact palette layout ---------------------------------------------------------
+// Distinct (density, material, measurement) triples are collected in an
+// open-addressing hash table; with at most PALETTE_MAX of them every voxel is
+// stored as a 1-byte palette index (exact: the palette holds the f32 density).
+constexpr int PALETTE_TABLE = 4096; // hash slots (power of two)
+constexpr uint64_t PALETTE_EMPTY = 0ull;
+
+__device__ __forceinline__ uint64_t palette_key(float density, uint8_t material, uint8_t measurement)
+{
+    return (1ull << 63) | (static_cast<uint64_t>(__float_as_uint(density)) << 16) | (static_cast<uint64_t>(material) << 8) | measurement;
+}
+
+__device__ __forceinline__ uint32_t palette_hash(uint64_t key)
+{
+    key ^= key >> 33;
+    key *= 0xff51afd7ed558ccdull;
+    key ^= key >> 33;
+    return static_cast<uint32_t>(key) & (PALETTE_TABLE - 1);
+}
+
+__global__ void palette_insert_kernel(const float* __restrict__ density, const uint8_t* __restrict__ material,
+    const uint8_t* __restrict__ measurement, uint64_t n, unsigned long long* table, unsigned int* count)
+{
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x); base < n; base += stride) {
+        const uint64_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        const uint64_t key = valid ? palette_key(density[i], material[i], measurement ? measurement[i] : 0) : PALETTE_EMPTY;
+        const unsigned active = __ballot_sync(0xffffffffu, valid);
+        if (!valid)
+            continue;
+        const unsigned peers = __match_any_sync(active, key);
+        if ((threadIdx.x & 31) != __ffs(peers) - 1)
+            continue; // one lane per distinct key of the warp probes the table
+        if (*reinterpret_cast<volatile unsigned int*>(count) > static_cast<unsigned>(dev::PALETTE_MAX))
+            continue; // already too many distinct voxels: the 8-byte layout will be used
+        uint32_t h = palette_hash(key);
+        for (int probe = 0; probe < PALETTE_TABLE; ++probe) {
+            const unsigned long long cur = table[h];
+            if (cur == key)
+                break;
+            if (cur == PALETTE_EMPTY) {
+                const unsigned long long prev = atomicCAS(table + h, PALETTE_EMPTY, key);
+                if (prev == PALETTE_EMPTY) {
+                    atomicAdd(count, 1u);
+                    break;
+                }
+                if (prev == key)
+                    break;
+            }
+            h = (h + 1) & (PALETTE_TABLE - 1);
+        }
+    }
+}
+
+__global__ void palette_map_kernel(const float* __restrict__ density, const uint8_t* __restrict__ material,
+    const uint8_t* __restrict__ measurement, uint64_t n, const unsigned long long* __restrict__ table,
+    const uint8_t* __restrict__ slot_index, uint8_t* __restrict__ out)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const uint64_t key = palette_key(density[i], material[i], measurement ? measurement[i] : 0);
+        uint32_t h = palette_hash(key);
+        uint8_t idx = 0;
+        for (int probe = 0; probe < PALETTE_TABLE; ++probe) {
+            if (table[h] == key) {
+                idx = slot_index[h];
+                break;
+            }
+            h = (h + 1) & (PALETTE_TABLE - 1);
+        }
+        out[i] = idx;
+    }
+}
+
+size_t dev_palette_table_bytes() { return PALETTE_TABLE * sizeof(unsigned long long); }
 
 } // namespace
 
@@ -254,6 +339,66 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     }
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(&bad, d_bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream);
+    // compact palette layout when the world has few distinct voxels
+    unsigned long long* d_table = nullptr;
+    unsigned int* d_count = nullptr;
+    unsigned int distinct = 0;
+    std::vector<dev::PaletteEntry> palette;
+    if (e == cudaSuccess && d->layout == 0) {
+        e = cudaMallocAsync(&d_table, dev_palette_table_bytes(), ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaMallocAsync(&d_count, sizeof(unsigned int), ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(d_table, 0, dev_palette_table_bytes(), ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(d_count, 0, sizeof(unsigned int), ctx->stream);
+        if (e == cudaSuccess) {
+            palette_insert_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(d_density, d_material, d_meas, n, d_table, d_count);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&distinct, d_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(ctx->stream);
+        if (e == cudaSuccess && distinct >= 1 && distinct <= static_cast<unsigned>(dev::PALETTE_MAX)) {
+            std::vector<unsigned long long> table(PALETTE_TABLE);
+            e = cudaMemcpy(table.data(), d_table, dev_palette_table_bytes(), cudaMemcpyDeviceToHost);
+            std::vector<uint8_t> slot_index(PALETTE_TABLE, 0);
+            for (int slot = 0; slot < PALETTE_TABLE && e == cudaSuccess; ++slot) {
+                const unsigned long long key = table[slot];
+                if (key == PALETTE_EMPTY)
+                    continue;
+                dev::PaletteEntry pe;
+                const uint32_t bits = static_cast<uint32_t>(key >> 16);
+                std::memcpy(&pe.density, &bits, sizeof(float));
+                pe.code = static_cast<uint32_t>(key & 0xffffu); // material | measurement << 8
+                pe.code = (pe.code >> 8) | ((pe.code & 0xffu) << 8);
+                slot_index[slot] = static_cast<uint8_t>(palette.size());
+                palette.push_back(pe);
+            }
+            uint8_t* d_slots = nullptr;
+            if (e == cudaSuccess)
+                e = cudaMallocAsync(&d_slots, PALETTE_TABLE, ctx->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(d_slots, slot_index.data(), PALETTE_TABLE, cudaMemcpyHostToDevice, ctx->stream);
+            if (e == cudaSuccess)
+                e = cudaMalloc(&w->palette_index, n);
+            if (e == cudaSuccess)
+                e = cudaMalloc(&w->palette, dev::PALETTE_MAX * sizeof(dev::PaletteEntry));
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(w->palette, palette.data(), palette.size() * sizeof(dev::PaletteEntry), cudaMemcpyHostToDevice, ctx->stream);
+            if (e == cudaSuccess) {
+                palette_map_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(d_density, d_material, d_meas, n, d_table, d_slots, w->palette_index);
+                e = cudaGetLastError();
+            }
+            if (d_slots)
+                cudaFreeAsync(d_slots, ctx->stream);
+        }
+    }
+    if (d_table)
+        cudaFreeAsync(d_table, ctx->stream);
+    if (d_count)
+        cudaFreeAsync(d_count, ctx->stream);
     if (d_density)
         cudaFreeAsync(d_density, ctx->stream);
     if (d_material)
@@ -267,11 +412,19 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     if (e != cudaSuccess) {
         if (w->voxels)
             cudaFree(w->voxels);
+        if (w->palette_index)
+            cudaFree(w->palette_index);
+        if (w->palette)
+            cudaFree(w->palette);
         delete w;
         return cuda_fail(ctx, e, "world upload");
     }
     if (bad) {
         cudaFree(w->voxels);
+        if (w->palette_index)
+            cudaFree(w->palette_index);
+        if (w->palette)
+            cudaFree(w->palette);
         delete w;
         return fail(ctx, DXMC_ERR_INVALID, "invalid world: material index >= n_materials");
     }
@@ -283,10 +436,13 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     std::memcpy(w->cosines, d->direction_cosines, sizeof(w->cosines));
     w->n_materials = d->n_materials;
     w->has_measurement = d->measurement != nullptr;
-    w->bytes = bytes;
-    ctx->in_use += bytes;
+    w->bytes = bytes + (w->palette_index ? n + dev::PALETTE_MAX * sizeof(dev::PaletteEntry) : 0);
+    ctx->in_use += w->bytes;
     auto& P = w->params;
     P.voxels = w->voxels;
+    P.palette_index = w->palette_index;
+    P.palette = w->palette;
+    P.palette_n = static_cast<int>(palette.size());
     for (int i = 0; i < 3; ++i) {
         P.dims[i] = static_cast<uint32_t>(d->dims[i]);
         P.inv_spacing[i] = static_cast<float>(1.0 / static_cast<double>(static_cast<float>(d->spacing[i])));
@@ -329,6 +485,10 @@ void dxmc_gpu_world_free(dxmc_world* w)
     cudaSetDevice(w->ctx->device);
     cudaStreamSynchronize(w->ctx->stream);
     cudaFree(w->voxels);
+    if (w->palette_index)
+        cudaFree(w->palette_index);
+    if (w->palette)
+        cudaFree(w->palette);
     w->ctx->in_use -= w->bytes;
     delete w;
 }
@@ -653,14 +813,25 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
     p.total_histories = total;
     p.seed = jd->seed;
     p.tally_mode = tally_mode;
+    p.uniform_hpe = 0;
+    {
+        bool uniform = true;
+        for (uint64_t i = 1; i < ne && uniform; ++i)
+            uniform = jd->exposures[i].n_histories == jd->exposures[0].n_histories;
+        if (uniform)
+            p.uniform_hpe = jd->exposures[0].n_histories;
+    }
+    p.regen_threshold = ctx->options.regen_threshold > 0 ? std::min(ctx->options.regen_threshold, 32) : DEFAULT_REGEN_THRESHOLD;
+    p.interact_threshold = ctx->options.interact_threshold > 0 ? std::min(ctx->options.interact_threshold, 32) : DEFAULT_INTERACT_THRESHOLD;
 
     const size_t lut_bytes = static_cast<size_t>(lut->meta.total_floats) * sizeof(float);
     const size_t smem_limit = std::min<size_t>(ctx->max_smem_optin, 96 * 1024);
     p.lut_in_smem = lut_bytes <= smem_limit ? 1 : 0;
-    const size_t smem = p.lut_in_smem ? lut_bytes : 0;
+    const bool palette = world->palette_index != nullptr;
+    const size_t smem = dev::transport_smem_bytes(lut_bytes, p.lut_in_smem != 0, palette);
     const int block = ctx->options.block_size > 0 ? ctx->options.block_size : 256;
     // also sets the kernel's dynamic shared-memory limit for this launch
-    const int occ = dev::transport_max_blocks_per_sm(jd->model, block, smem);
+    const int occ = dev::transport_max_blocks_per_sm(jd->model, palette, block, smem);
     int per_sm = ctx->options.blocks_per_sm > 0 ? ctx->options.blocks_per_sm : occ;
     if (per_sm <= 0)
         per_sm = 1;
@@ -848,6 +1019,14 @@ int ctx_sm_count(const dxmc_gpu_ctx* ctx) { return ctx->sm_count; }
 size_t ctx_max_smem(const dxmc_gpu_ctx* ctx) { return ctx->max_smem_optin; }
 void ctx_set_error(dxmc_gpu_ctx* ctx, const std::string& msg) { ctx->last_error = msg; }
 std::mutex& ctx_mutex(dxmc_gpu_ctx* ctx) { return ctx->mutex; }
+int ctx_regen_threshold(const dxmc_gpu_ctx* ctx)
+{
+    return ctx->options.regen_threshold > 0 ? std::min(ctx->options.regen_threshold, 32) : DEFAULT_REGEN_THRESHOLD;
+}
+int ctx_interact_threshold(const dxmc_gpu_ctx* ctx)
+{
+    return ctx->options.interact_threshold > 0 ? std::min(ctx->options.interact_threshold, 32) : DEFAULT_INTERACT_THRESHOLD;
+}
 const dev::WorldParams* world_params(const dxmc_world* w, const dxmc_gpu_ctx** owner, int* n_materials)
 {
     *owner = w->ctx;

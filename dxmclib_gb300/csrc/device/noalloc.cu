@@ -209,6 +209,8 @@ int ctx_sm_count(const dxmc_gpu_ctx* ctx);
 size_t ctx_max_smem(const dxmc_gpu_ctx* ctx);
 void ctx_set_error(dxmc_gpu_ctx* ctx, const std::string& msg);
 std::mutex& ctx_mutex(dxmc_gpu_ctx* ctx);
+int ctx_regen_threshold(const dxmc_gpu_ctx* ctx);
+int ctx_interact_threshold(const dxmc_gpu_ctx* ctx);
 const dev::WorldParams* world_params(const dxmc_world* w, const dxmc_gpu_ctx** owner, int* n_materials);
 const float* lut_image(const dxmc_lut* l, dev::LutMeta* meta, const dxmc_gpu_ctx** owner);
 }
@@ -330,12 +332,16 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         p.total_histories = total;
         p.seed = jd->seed;
         p.tally_mode = 0; // FP64 atomics
+        p.uniform_hpe = 0; // exposure found by binary search over the prefix sums
+        p.regen_threshold = capi::ctx_regen_threshold(ctx);
+        p.interact_threshold = capi::ctx_interact_threshold(ctx);
         const size_t lut_bytes = static_cast<size_t>(meta.total_floats) * sizeof(float);
         const size_t smem_limit = std::min<size_t>(capi::ctx_max_smem(ctx), 96 * 1024);
         p.lut_in_smem = lut_bytes <= smem_limit ? 1 : 0;
-        const size_t smem = p.lut_in_smem ? lut_bytes : 0;
+        const bool palette = wp->palette_index != nullptr;
+        const size_t smem = dev::transport_smem_bytes(lut_bytes, p.lut_in_smem != 0, palette);
         const int block = 256;
-        int per_sm = dev::transport_max_blocks_per_sm(jd->model, block, smem);
+        int per_sm = dev::transport_max_blocks_per_sm(jd->model, palette, block, smem);
         if (per_sm <= 0)
             per_sm = 1;
         e = dev::launch_transport(p, jd->model, capi::ctx_sm_count(ctx) * per_sm, block, smem, stream);

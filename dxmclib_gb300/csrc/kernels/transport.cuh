@@ -5,8 +5,20 @@
 
 namespace dxmc_gb300::dev {
 
+// Palette entry of the compact voxel layout: density and (material | measurement << 8).
+struct PaletteEntry {
+    float density;
+    uint32_t code;
+};
+
+constexpr int PALETTE_MAX = 256;
+
 struct WorldParams {
-    const Voxel* voxels;
+    const Voxel* voxels;            // 8-byte layout (always present)
+    const uint8_t* palette_index;   // 1-byte layout, or nullptr when the world has > 256 distinct voxels
+    const PaletteEntry* palette;    // PALETTE_MAX entries
+    int palette_n;
+    int pad_palette;
     uint32_t dims[3];
     uint32_t pad;
     float lo[3];          // nextafter-safe lower extent (world.hpp:55-68)
@@ -56,13 +68,19 @@ struct TransportParams {
     const volatile int* cancel; // host-mapped flag, may be null
     uint64_t total_histories;
     uint64_t seed;
+    uint64_t uniform_hpe;   // histories per exposure when every exposure has the same count, else 0
     int tally_mode;
     int lut_in_smem;
+    int regen_threshold;    // refill finished lanes once at least this many are idle (1..32)
+    int interact_threshold; // run the interaction passes once at least this many lanes wait (1..32)
 };
 
 // Launchers (defined in transport_kernels.cu).
 cudaError_t launch_transport(const TransportParams& p, int model, int grid, int block, size_t smem, cudaStream_t stream);
-int transport_max_blocks_per_sm(int model, int block, size_t smem);
+// blocks per SM for this configuration; also raises the kernel's dynamic shared-memory limit
+int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem);
+// dynamic shared memory the transport kernel needs for a LUT image of lut_bytes
+size_t transport_smem_bytes(size_t lut_bytes, bool lut_in_smem, bool palette);
 cudaError_t launch_postprocess(const double* tally, const uint32_t* n_events, const Voxel* voxels, uint64_t n,
     int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream);
 cudaError_t launch_postprocess_f32(const float* tally, const uint32_t* n_events, const Voxel* voxels, uint64_t n,

@@ -444,34 +444,72 @@ namespace {
     }
 
     // ---- the transport kernel ----------------------------------------------------
-    template <int MODEL>
+    //
+    // Warp-synchronous loop.  Each iteration every lane with a live photon and no
+    // pending interaction takes one Woodcock step; a real event only records its
+    // type (photoelectric / Compton / Rayleigh).  The interactions are then run in
+    // one converged pass per type once enough lanes wait, and finished lanes are
+    // refilled together once enough are idle, so the expensive branches run with
+    // many lanes active instead of one or two.
+    enum : int { EV_NONE = 0, EV_PHOTO = 1, EV_COMPTON = 2, EV_RAYLEIGH = 3 };
+
+    template <bool PALETTE>
+    __device__ __forceinline__ void gather_voxel(const WorldParams& w, const PaletteEntry* pal, uint64_t vidx, float& density, int& mat, bool& measured)
+    {
+        if constexpr (PALETTE) {
+            const PaletteEntry e = pal[__ldg(w.palette_index + vidx)];
+            density = e.density;
+            mat = static_cast<int>(e.code & 0xffu);
+            measured = (e.code >> 8) != 0u;
+        } else {
+            const uint2 raw = __ldg(reinterpret_cast<const uint2*>(w.voxels) + vidx);
+            density = __uint_as_float(raw.x);
+            mat = static_cast<int>(raw.y & 0xffu);
+            measured = ((raw.y >> 8) & 0xffu) != 0u;
+        }
+    }
+
+    template <int MODEL, bool PALETTE>
     __global__ void __launch_bounds__(256) transport_kernel(const __grid_constant__ TransportParams p)
     {
         extern __shared__ float4 smem_f4[];
         const float* L = p.lut;
+        size_t smem_off = 0;
         if (p.lut_in_smem) {
             float4* dst = smem_f4;
             const float4* src = reinterpret_cast<const float4*>(p.lut);
             const int n4 = (p.lut_meta.total_floats + 3) / 4;
             for (int i = threadIdx.x; i < n4; i += blockDim.x)
                 dst[i] = __ldg(src + i);
-            __syncthreads();
             L = reinterpret_cast<const float*>(smem_f4);
+            smem_off = static_cast<size_t>(n4);
         }
+        const PaletteEntry* pal = nullptr;
+        if constexpr (PALETTE) {
+            PaletteEntry* spal = reinterpret_cast<PaletteEntry*>(smem_f4 + smem_off);
+            for (int i = threadIdx.x; i < PALETTE_MAX; i += blockDim.x)
+                spal[i] = i < p.world.palette_n ? p.world.palette[i] : PaletteEntry { 0.0f, 0u };
+            pal = spal;
+        }
+        __syncthreads();
         const LutMeta& m = p.lut_meta;
         const WorldParams& w = p.world;
         const int lane = threadIdx.x & 31;
         const unsigned lanemask_lt = (1u << lane) - 1u;
+        const int regen_t = p.regen_threshold;
+        const int interact_t = p.interact_threshold;
 
         Photon ph {};
         Rng rng;
         bool alive = false;
+        int pending = EV_NONE;
         float maxInv = 0.0f, logE = 0.0f;
         int seg = 0;
         bool updateMax = true;
         int cached_mat = -1;
         uint32_t hist_steps = 0;
         float att0 = 0.0f, att1 = 0.0f, att2 = 0.0f;
+        uint64_t vidx = 0;
         unsigned long long my_steps = 0, my_deposits = 0, my_overflows = 0, my_histories = 0;
 
         // warp-uniform pool of history ids [pool_next, pool_end)
@@ -479,52 +517,60 @@ namespace {
         bool exhausted = false;
 
         while (true) {
-            // ---- regenerate finished lanes from the warp pool ------------------------
-            const unsigned need = __ballot_sync(FULL_MASK, !alive && !exhausted);
-            if (need) {
-                if (pool_next >= pool_end) {
-                    unsigned long long base = 0;
-                    if (lane == 0) {
-                        const bool cancelled = p.cancel && *p.cancel;
-                        base = cancelled ? static_cast<unsigned long long>(p.total_histories) : atomicAdd(&p.counters->next_history, (unsigned long long)WARP_POOL_CHUNK);
+            // ---- refill idle lanes together ------------------------------------------------
+            {
+                unsigned need = __ballot_sync(FULL_MASK, !alive && !exhausted);
+                const unsigned live = __ballot_sync(FULL_MASK, alive);
+                if (need && (__popc(need) >= regen_t || live == 0u)) {
+                    while (need && !exhausted) {
+                        if (pool_next >= pool_end) {
+                            unsigned long long base = 0;
+                            if (lane == 0) {
+                                const bool cancelled = p.cancel && *p.cancel;
+                                base = cancelled ? static_cast<unsigned long long>(p.total_histories)
+                                                 : atomicAdd(&p.counters->next_history, (unsigned long long)WARP_POOL_CHUNK);
+                            }
+                            base = __shfl_sync(FULL_MASK, base, 0);
+                            if (base >= p.total_histories) {
+                                exhausted = true;
+                                break;
+                            }
+                            pool_next = base;
+                            pool_end = min(static_cast<uint64_t>(base + WARP_POOL_CHUNK), p.total_histories);
+                        }
+                        const uint64_t avail = pool_end - pool_next;
+                        const unsigned rank = __popc(need & lanemask_lt);
+                        const bool mine = ((need >> lane) & 1u) && rank < avail;
+                        const unsigned taken = __ballot_sync(FULL_MASK, mine);
+                        if (mine) {
+                            const uint64_t h = pool_next + rank;
+                            rng.init(p.seed, h);
+                            const uint32_t ei = p.uniform_hpe ? static_cast<uint32_t>(h / p.uniform_hpe) : find_exposure(p.source, h);
+                            DevExposure ex;
+                            load_exposure(p.source.exposures + ei, ex);
+                            sample_particle(p.source, ex, rng, ph);
+                            ++my_histories;
+                            alive = transport_to_world(w, ph);
+                            pending = EV_NONE;
+                            updateMax = true;
+                            cached_mat = -1;
+                            hist_steps = 0;
+                        }
+                        pool_next += __popc(taken);
+                        need &= ~taken;
                     }
-                    base = __shfl_sync(FULL_MASK, base, 0);
-                    if (base >= p.total_histories) {
-                        exhausted = true;
-                    } else {
-                        pool_next = base;
-                        pool_end = min(static_cast<uint64_t>(base + WARP_POOL_CHUNK), p.total_histories);
-                    }
-                }
-                if (!exhausted) {
-                    const uint64_t avail = pool_end - pool_next;
-                    const unsigned rank = __popc(need & lanemask_lt);
-                    const bool mine = (need >> lane) & 1u;
-                    if (mine && rank < avail) {
-                        const uint64_t h = pool_next + rank;
-                        rng.init(p.seed, h);
-                        const uint32_t ei = find_exposure(p.source, h);
-                        DevExposure ex;
-                        load_exposure(p.source.exposures + ei, ex);
-                        sample_particle(p.source, ex, rng, ph);
-                        ++my_histories;
-                        alive = transport_to_world(w, ph);
-                        updateMax = true;
-                        cached_mat = -1;
-                        hist_steps = 0;
-                    }
-                    pool_next += min(static_cast<uint64_t>(__popc(need)), avail);
                 }
             }
-            const unsigned stepping = __ballot_sync(FULL_MASK, alive);
-            if (exhausted && stepping == 0u)
+            const unsigned live = __ballot_sync(FULL_MASK, alive);
+            if (exhausted && live == 0u)
                 break;
 
             bool do_score = false;
             float deposit = 0.0f; // energy imparted x weight to score
-            uint64_t vidx = 0;
-            if (alive) {
-                // ---- one Woodcock step (transport.hpp:650-699) ---------------------------
+            bool check_roulette = false;
+
+            // ---- one Woodcock step for lanes without a pending interaction (transport.hpp:650-699)
+            if (alive && pending == EV_NONE) {
                 if (updateMax) {
                     logE = __log10f(ph.energy);
                     seg = lut_segment(L, m, logE);
@@ -547,10 +593,10 @@ namespace {
                     const uint32_t iy = min(static_cast<uint32_t>((ph.py - w.lo[1]) * w.inv_spacing[1]), w.dims[1] - 1);
                     const uint32_t iz = min(static_cast<uint32_t>((ph.pz - w.lo[2]) * w.inv_spacing[2]), w.dims[2] - 1);
                     vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
-                    const uint2 raw = __ldg(reinterpret_cast<const uint2*>(w.voxels) + vidx);
-                    const float density = __uint_as_float(raw.x);
-                    const int mat = static_cast<int>(raw.y & 0xffu);
-                    const bool measured = ((raw.y >> 8) & 0xffu) != 0u;
+                    float density;
+                    int mat;
+                    bool measured;
+                    gather_voxel<PALETTE>(w, pal, vidx, density, mat, measured);
                     ++my_steps;
                     if (mat != cached_mat) {
                         lut_attenuation(L, m, mat, logE, seg, att0, att1, att2);
@@ -558,48 +604,18 @@ namespace {
                     }
                     const float attTot = att0 + att1 + att2;
                     const float eventProb = attTot * density * maxInv;
-
-                    bool cont = true;
                     if (!measured) {
-                        // naive sampling (computeInteractions, transport.hpp:583-638)
+                        // naive sampling (computeInteractions, transport.hpp:583-638): decide
+                        // the event type now, run it in the interaction pass
                         if (rng.uniform() < eventProb) {
                             const float r3 = rng.uniform() * attTot;
-                            if (r3 < att0) {
-                                const float e = photo_absorption<MODEL>(L, m, ph, mat, rng);
-                                do_score = true;
-                                if (ph.energy < ENERGY_CUTOFF) {
-                                    deposit = (e + ph.energy) * ph.weight;
-                                    ph.energy = 0.0f;
-                                    cont = false;
-                                } else {
-                                    deposit = e * ph.weight;
-                                    updateMax = true;
-                                }
-                            } else if (r3 < att0 + att1) {
-                                float e = 0.0f;
-                                if (!compton_scatter<MODEL>(L, m, ph, mat, rng, e)) {
-                                    ++my_overflows;
-                                    cont = false;
-                                } else {
-                                    do_score = true;
-                                    if (ph.energy < ENERGY_CUTOFF) {
-                                        deposit = (e + ph.energy) * ph.weight;
-                                        ph.energy = 0.0f;
-                                        cont = false;
-                                    } else {
-                                        deposit = e * ph.weight;
-                                        updateMax = true;
-                                    }
-                                }
-                            } else {
-                                if (!rayleigh_scatter<MODEL>(L, m, ph, mat, rng)) {
-                                    ++my_overflows;
-                                    cont = false;
-                                }
-                            }
+                            pending = r3 < att0 ? EV_PHOTO : (r3 < att0 + att1 ? EV_COMPTON : EV_RAYLEIGH);
+                        } else {
+                            check_roulette = true;
                         }
                     } else {
                         // forced photoelectric scoring (computeInteractionsForced, transport.hpp:523-581)
+                        bool cont = true;
                         const float photoProb = att0 / attTot;
                         const float wc = eventProb * photoProb;
                         {
@@ -617,8 +633,12 @@ namespace {
                                     cont = false;
                                 } else {
                                     // the forced photoelectric deposit and the Compton deposit are two events
-                                    score(p, vidx, deposit);
-                                    ++my_deposits;
+                                    if (isfinite(deposit)) {
+                                        score(p, vidx, deposit);
+                                        ++my_deposits;
+                                    } else {
+                                        ++my_overflows;
+                                    }
                                     if (ph.energy < ENERGY_CUTOFF) {
                                         deposit = (e + ph.energy) * ph.weight;
                                         ph.energy = 0.0f;
@@ -637,17 +657,66 @@ namespace {
                         }
                         if (cont)
                             ph.weight *= (1.0f - wc);
+                        alive = cont;
+                        check_roulette = cont;
                     }
-                    if (cont) {
-                        // Russian roulette (transport.hpp:684-694)
-                        if (ph.energy * ph.weight < ROULETTE_THRESHOLD) {
-                            if (rng.uniform() < ROULETTE_PROBABILITY)
-                                cont = false;
-                            else
-                                ph.weight *= 1.0f / (1.0f - ROULETTE_PROBABILITY);
+                }
+            }
+
+            // ---- interaction passes, one converged pass per event type ---------------------
+            {
+                const unsigned waiting = __ballot_sync(FULL_MASK, pending != EV_NONE);
+                const unsigned can_step = __ballot_sync(FULL_MASK, alive && pending == EV_NONE);
+                if (waiting && (__popc(waiting) >= interact_t || can_step == 0u || exhausted)) {
+                    const int mat = cached_mat;
+                    if (__any_sync(FULL_MASK, pending == EV_PHOTO) && pending == EV_PHOTO) {
+                        const float e = photo_absorption<MODEL>(L, m, ph, mat, rng);
+                        do_score = true;
+                        if (ph.energy < ENERGY_CUTOFF) {
+                            deposit = (e + ph.energy) * ph.weight;
+                            ph.energy = 0.0f;
+                            alive = false;
+                        } else {
+                            deposit = e * ph.weight;
+                            updateMax = true;
                         }
                     }
-                    alive = cont;
+                    if (__any_sync(FULL_MASK, pending == EV_COMPTON) && pending == EV_COMPTON) {
+                        float e = 0.0f;
+                        if (!compton_scatter<MODEL>(L, m, ph, mat, rng, e)) {
+                            ++my_overflows;
+                            alive = false;
+                        } else {
+                            do_score = true;
+                            if (ph.energy < ENERGY_CUTOFF) {
+                                deposit = (e + ph.energy) * ph.weight;
+                                ph.energy = 0.0f;
+                                alive = false;
+                            } else {
+                                deposit = e * ph.weight;
+                                updateMax = true;
+                            }
+                        }
+                    }
+                    if (__any_sync(FULL_MASK, pending == EV_RAYLEIGH) && pending == EV_RAYLEIGH) {
+                        if (!rayleigh_scatter<MODEL>(L, m, ph, mat, rng)) {
+                            ++my_overflows;
+                            alive = false;
+                        }
+                    }
+                    if (pending != EV_NONE) {
+                        check_roulette = alive;
+                        pending = EV_NONE;
+                    }
+                }
+            }
+            if (check_roulette) {
+                // Russian roulette (transport.hpp:684-694)
+                if (ph.energy * ph.weight < ROULETTE_THRESHOLD) {
+                    if (rng.uniform() < ROULETTE_PROBABILITY)
+                        alive = false;
+                    else
+                        ph.weight *= 1.0f / (1.0f - ROULETTE_PROBABILITY);
                 }
             }
             if (do_score && !isfinite(deposit)) {
@@ -777,31 +846,38 @@ namespace {
 
 } // namespace
 
-cudaError_t launch_transport(const TransportParams& p, int model, int grid, int block, size_t smem, cudaStream_t stream)
+template <int MODEL, bool PALETTE>
+static void* transport_entry() { return reinterpret_cast<void*>(&transport_kernel<MODEL, PALETTE>); }
+
+static void* transport_function(int model, bool palette)
 {
-    if (model == 0)
-        transport_kernel<0><<<grid, block, smem, stream>>>(p);
-    else if (model == 1)
-        transport_kernel<1><<<grid, block, smem, stream>>>(p);
-    else
-        transport_kernel<2><<<grid, block, smem, stream>>>(p);
-    return cudaGetLastError();
+    if (palette)
+        return model == 0 ? transport_entry<0, true>() : (model == 1 ? transport_entry<1, true>() : transport_entry<2, true>());
+    return model == 0 ? transport_entry<0, false>() : (model == 1 ? transport_entry<1, false>() : transport_entry<2, false>());
 }
 
-int transport_max_blocks_per_sm(int model, int block, size_t smem)
+size_t transport_smem_bytes(size_t lut_bytes, bool lut_in_smem, bool palette)
 {
+    size_t b = lut_in_smem ? (lut_bytes + 15) / 16 * 16 : 0;
+    if (palette)
+        b += PALETTE_MAX * sizeof(PaletteEntry);
+    return b;
+}
+
+cudaError_t launch_transport(const TransportParams& p, int model, int grid, int block, size_t smem, cudaStream_t stream)
+{
+    const bool palette = p.world.palette_index != nullptr;
+    void* fn = transport_function(model, palette);
+    void* args[] = { const_cast<TransportParams*>(&p) };
+    return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, stream);
+}
+
+int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem)
+{
+    void* fn = transport_function(model, palette);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     int n = 0;
-    cudaError_t e;
-    if (model == 0) {
-        cudaFuncSetAttribute(transport_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transport_kernel<0>, block, smem);
-    } else if (model == 1) {
-        cudaFuncSetAttribute(transport_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transport_kernel<1>, block, smem);
-    } else {
-        cudaFuncSetAttribute(transport_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, transport_kernel<2>, block, smem);
-    }
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, smem);
     return e == cudaSuccess ? n : 0;
 }
 

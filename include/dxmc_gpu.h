@@ -188,6 +188,8 @@ typedef struct dxmc_gpu_options {
     int32_t blocks_per_sm;   /* resident blocks per SM, 0 = occupancy-derived */
     int32_t tally_mode;      /* DXMC_TALLY_* */
     uint64_t memory_budget;  /* admission budget in bytes, 0 = 90% of free memory */
+    int32_t regen_threshold; /* refill finished lanes of a warp once this many are idle; 0 = default */
+    int32_t interact_threshold; /* run the per-type interaction passes once this many lanes wait; 0 = default */
 } dxmc_gpu_options;
 
 int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out);
@@ -206,7 +208,9 @@ typedef struct dxmc_world_desc {
     const uint8_t* material;      /* material index, host pointer */
     const uint8_t* measurement;   /* forced-interaction map, may be NULL */
     int32_t n_materials;          /* material indices must be < n_materials */
-    int32_t pad;
+    int32_t layout;               /* 0: compact 1-byte palette layout when the world has at most 256
+                                     distinct (material, density, measurement) voxels, else 8-byte;
+                                     1: always the 8-byte layout */
 } dxmc_world_desc;
 
 /* Validates like World::validate (world.hpp:182-227) and copies the arrays to

@@ -10,7 +10,19 @@ from __future__ import annotations
 import numpy as np
 
 # Acceptance thresholds.
-THREE_SIGMA_FRACTION = 0.99   # voxels above 1 % of max within 3 combined standard errors (expect 0.997)
+# Voxels above 1 % of max beyond 3 combined standard errors: a Gaussian tally has
+# 0.27 % of them; the count may exceed that by 4 binomial standard deviations
+# (false-alarm rate about 1e-4 per comparison), and no voxel may be beyond 6.
+P_BEYOND_3SIGMA = 0.0027
+MAX_ABS_Z = 6.0
+# The variance field sums squared deposits per event, not per history
+# (transport.hpp:601, 609, 621, 629), so it under-estimates the variance of the
+# mean when one history deposits more than once in a voxel; the reference
+# restated on the CPU shows chi2/dof = 1.03 against the reference itself on the
+# forced-interaction case.  z is therefore rescaled by the observed
+# overdispersion (chi2/dof, at least 1) before counting, and chi2/dof itself is
+# bounded so that real per-voxel disagreements still fail.
+MAX_CHI2 = 1.2
 TOTAL_ENERGY_RTOL = 0.005     # total energy imparted within 0.5 %
 MEAN_BIAS_RTOL = 0.01         # dose-weighted mean per-voxel relative difference within 1 %
 
@@ -30,19 +42,24 @@ def compare_sparse(ref: dict, dose: np.ndarray, var: np.ndarray, min_frac: float
         n_voxels=int(sel.sum()),
         frac_3sigma=float(np.mean(np.abs(z) <= 3.0)),
         chi2=float(np.mean(z * z)),
+        beyond_3sigma=int(np.sum(np.abs(z) / np.sqrt(max(1.0, float(np.mean(z * z)))) > 3.0)),
         total_ratio=float(dose.sum() / ref["total"][0]),
         # dose-weighted mean relative difference: sum(d2 - d1) / sum(d1); the unweighted
         # mean of ratios is biased by noise in the denominator when voxels are noisy
         mean_bias=float(np.sum(d2 - d1) / np.sum(d1)),
         mean_rel_unweighted=float(np.mean((d2 - d1) / d1)),
         mean_abs_rel=float(np.mean(np.abs(d2 - d1) / d1)),
-        max_abs_z=float(np.max(np.abs(z))) if len(z) else 0.0,
+        max_abs_z=float(np.max(np.abs(z)) / np.sqrt(max(1.0, float(np.mean(z * z))))) if len(z) else 0.0,
     )
 
 
 def assert_parity(stats: dict, label: str = "") -> None:
     msg = f"{label}: {stats}"
     assert stats["n_voxels"] > 10, msg
-    assert stats["frac_3sigma"] >= THREE_SIGMA_FRACTION, msg
+    n = stats["n_voxels"]
+    allowed = int(P_BEYOND_3SIGMA * n + 4.0 * np.sqrt(P_BEYOND_3SIGMA * (1 - P_BEYOND_3SIGMA) * n)) + 1
+    assert stats["beyond_3sigma"] <= allowed, msg + f" (allowed {allowed} beyond 3 sigma)"
+    assert stats["max_abs_z"] <= MAX_ABS_Z, msg
+    assert stats["chi2"] <= MAX_CHI2, msg
     assert abs(stats["total_ratio"] - 1.0) <= TOTAL_ENERGY_RTOL, msg
     assert abs(stats["mean_bias"]) <= MEAN_BIAS_RTOL, msg
