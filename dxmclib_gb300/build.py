@@ -55,9 +55,17 @@ def _headers():
 
 
 def build(verbose: bool = False, force: bool = False) -> Path:
-    """Compile everything that is out of date; returns the path of libdxmc_gpu.so."""
+    """Compile everything that is out of date; returns the path of libdxmc_gpu.so.
+
+    DXMC_NVCC_DEFINES (e.g. "-DDXMC_MIN_BLOCKS_PER_SM=3") adds preprocessor
+    definitions to the CUDA translation units; a change of it forces a rebuild."""
     BUILD.mkdir(exist_ok=True)
     LIB.mkdir(exist_ok=True)
+    defines = os.environ.get("DXMC_NVCC_DEFINES", "").split()
+    stamp = BUILD / "nvcc_defines.txt"
+    if not stamp.exists() or stamp.read_text() != " ".join(defines):
+        force = True
+        stamp.write_text(" ".join(defines))
     headers = _headers()
     jobs = []
     objects = []
@@ -70,7 +78,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         obj = BUILD / (src.stem + ".o")
         objects.append(obj)
         if force or _stale(obj, [src, *headers]):
-            jobs.append([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-c", str(src), "-o", str(obj), *INCLUDES])
+            jobs.append([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", *defines, "-c", str(src), "-o", str(obj),
+                         *INCLUDES])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for r in ex.map(_run, jobs):
             if verbose and (r.stdout or r.stderr):

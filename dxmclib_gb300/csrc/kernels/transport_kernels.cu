@@ -469,8 +469,11 @@ namespace {
         }
     }
 
+#ifndef DXMC_MIN_BLOCKS_PER_SM
+#define DXMC_MIN_BLOCKS_PER_SM 4 // resident 256-thread blocks per SM the register budget must allow (64 registers)
+#endif
     template <int MODEL, bool PALETTE>
-    __global__ void __launch_bounds__(256) transport_kernel(const __grid_constant__ TransportParams p)
+    __global__ void __launch_bounds__(256, DXMC_MIN_BLOCKS_PER_SM) transport_kernel(const __grid_constant__ TransportParams p)
     {
         extern __shared__ float4 smem_f4[];
         const float* L = p.lut;
