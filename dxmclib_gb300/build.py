@@ -78,8 +78,11 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         obj = BUILD / (src.stem + ".o")
         objects.append(obj)
         if force or _stale(obj, [src, *headers]):
-            jobs.append([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", *defines, "-c", str(src), "-o", str(obj),
-                         *INCLUDES])
+            # the transport kernels use the fast single-precision intrinsics (Monte Carlo
+            # sampling tolerates their ulp-level error; tallies stay FP64)
+            fast = ["-use_fast_math"] if src.name == "transport_kernels.cu" else []
+            jobs.append([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", *fast, "-Xcompiler", "-fPIC", *defines, "-c", str(src), "-o",
+                         str(obj), *INCLUDES])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for r in ex.map(_run, jobs):
             if verbose and (r.stdout or r.stderr):

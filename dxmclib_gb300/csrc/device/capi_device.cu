@@ -21,8 +21,8 @@ using namespace dxmc_gb300;
 
 // Warp scheduling of the transport kernel: refill idle lanes once this many
 // are idle; run the per-type interaction passes once this many lanes wait.
-constexpr int DEFAULT_REGEN_THRESHOLD = 16;
-constexpr int DEFAULT_INTERACT_THRESHOLD = 8;
+constexpr int DEFAULT_REGEN_THRESHOLD = 12;
+constexpr int DEFAULT_INTERACT_THRESHOLD = 6;
 
 struct dxmc_gpu_ctx {
     int device = 0;
@@ -539,6 +539,7 @@ int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* b, dxmc_lut** ou
         sp[60] = static_cast<float>(b->spline[mat][76]);
         sp[61] = static_cast<float>(b->spline[mat][77]);
         sp[62] = static_cast<float>(b->spline[mat][78]);
+        sp[63] = static_cast<float>(1.0 / b->spline[mat][77]);
         for (int s = 0; s < dev::N_SHELLS; ++s) {
             const auto& c = b->shells[mat][s];
             float* o = img.data() + m.off_shells + (mat * dev::N_SHELLS + s) * dev::SHELL_FLOATS;

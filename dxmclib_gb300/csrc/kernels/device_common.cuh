@@ -82,34 +82,30 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1
     return c;
 }
 
+// Per-history random stream: a PCG32 (XSH-RR, O'Neill 2014) generator whose
+// 64-bit state and odd increment are drawn from Philox4x32-10 keyed by the job
+// seed with the history id as counter, so every history has its own stream
+// and a job can be split or resumed at any history id.  PCG32 is also the
+// generator of the reference (dxmcrandom.hpp:156-165).
 struct Rng {
-    uint4 buf;
-    uint32_t k0, k1;
-    uint32_t hist_lo, hist_hi;
-    uint32_t block;
-    uint32_t left;
+    uint64_t state;
+    uint64_t inc;
 
     __device__ void init(uint64_t seed, uint64_t history)
     {
-        k0 = static_cast<uint32_t>(seed);
-        k1 = static_cast<uint32_t>(seed >> 32);
-        hist_lo = static_cast<uint32_t>(history);
-        hist_hi = static_cast<uint32_t>(history >> 32);
-        block = 0;
-        left = 0;
+        const uint4 r = philox4x32_10(make_uint4(static_cast<uint32_t>(history), static_cast<uint32_t>(history >> 32), 0x44584d43u, 0u),
+            static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
+        state = (static_cast<uint64_t>(r.y) << 32) | r.x;
+        inc = (((static_cast<uint64_t>(r.w) << 32) | r.z) << 1) | 1u;
+        next();
     }
     __device__ __forceinline__ uint32_t next()
     {
-        if (left == 0) {
-            buf = philox4x32_10(make_uint4(block++, hist_lo, hist_hi, 0x44584d43u), k0, k1);
-            left = 4;
-        }
-        const uint32_t r = buf.x;
-        buf.x = buf.y;
-        buf.y = buf.z;
-        buf.z = buf.w;
-        --left;
-        return r;
+        const uint64_t old = state;
+        state = old * 6364136223846793005ull + inc;
+        const uint32_t xorshifted = static_cast<uint32_t>(((old >> 18u) ^ old) >> 27u);
+        const uint32_t rot = static_cast<uint32_t>(old >> 59u);
+        return __funnelshift_r(xorshifted, xorshifted, rot);
     }
     // [0, 1) with 24 random bits
     __device__ __forceinline__ float uniform() { return static_cast<float>(next() >> 8) * 0x1p-24f; }
@@ -117,6 +113,8 @@ struct Rng {
     __device__ __forceinline__ float uniform_open() { return static_cast<float>((next() >> 8) + 1u) * 0x1p-24f; }
     // integer in [0, n) by the multiply-high method (Lemire)
     __device__ __forceinline__ uint32_t below(uint32_t n) { return __umulhi(next(), n); }
+    // azimuth uniform in [-pi, pi)
+    __device__ __forceinline__ float azimuth() { return fmaf(uniform(), 6.28318530717959f, -3.14159265358979f); }
 };
 
 // ---------------------------------------------------------------------------
@@ -215,9 +213,9 @@ __device__ __forceinline__ float lut_max_inverse(const float* L, const LutMeta& 
 __device__ __forceinline__ float lut_scatter_factor(const float* L, const LutMeta& m, int material, float q)
 {
     const float* s = L + m.off_spline + material * SPLINE_FLOATS;
-    const float start = s[60], step = s[61], stop = s[62];
+    const float start = s[60], stop = s[62], inv_step = s[63];
     const float x = fminf(fmaxf(q, start), stop);
-    const int index = x > start ? static_cast<int>((x - start) / step) : 0;
+    const int index = x > start ? static_cast<int>((x - start) * inv_step) : 0;
     const int off = index < SPLINE_N - 1 ? index * 4 : (SPLINE_N - 2) * 4;
     return s[off] + s[off + 1] * x + s[off + 2] * x * x + s[off + 3] * x * x * x;
 }

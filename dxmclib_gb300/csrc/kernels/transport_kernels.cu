@@ -105,7 +105,7 @@ namespace {
                 }
                 ph.energy = sh[8 + line];
                 const float theta = rng.uniform() * PI_F;
-                const float phi = rng.uniform() * (2.0f * PI_F);
+                const float phi = rng.azimuth();
                 peturb(ph.dx, ph.dy, ph.dz, cosf(theta), phi);
                 return E - ph.energy;
             }
@@ -125,7 +125,7 @@ namespace {
                 float s, c;
                 sincosf(theta, &s, &c);
                 if (!(r1 > (2.0f - s * s) * s)) {
-                    const float phi = rng.uniform() * (2.0f * PI_F);
+                    const float phi = rng.azimuth();
                     peturb(ph.dx, ph.dy, ph.dz, c, phi);
                     return true;
                 }
@@ -141,7 +141,7 @@ namespace {
                     return false;
                 const float cosA = 1.0f - 2.0f * q2 * invE * invE;
                 if (!((1.0f + cosA * cosA) * 0.5f < rng.uniform())) {
-                    const float phi = rng.uniform() * (2.0f * PI_F);
+                    const float phi = rng.azimuth();
                     peturb(ph.dx, ph.dy, ph.dz, cosA, phi);
                     return true;
                 }
@@ -260,7 +260,7 @@ namespace {
         }
         if (!accepted)
             return false;
-        const float phi = rng.uniform() * (2.0f * PI_F);
+        const float phi = rng.azimuth();
         peturb(ph.dx, ph.dy, ph.dz, cosA, phi);
         const float E = ph.energy;
         ph.energy *= e;
@@ -297,7 +297,7 @@ namespace {
                     rejected = r2 > g;
                 }
                 if (!rejected) {
-                    const float phi = rng.uniform() * (2.0f * PI_F);
+                    const float phi = rng.azimuth();
                     peturb(ph.dx, ph.dy, ph.dz, cosA, phi);
                     ph.energy = E * e;
                     deposit = E - ph.energy;
@@ -405,8 +405,9 @@ namespace {
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             if (fabsf(dir[i]) > N_ERROR) {
-                const float a0 = (w.lo[i] - pos[i]) / dir[i];
-                const float an = (w.hi[i] - pos[i]) / dir[i];
+                const float inv = __frcp_rn(dir[i]);
+                const float a0 = (w.lo[i] - pos[i]) * inv;
+                const float an = (w.hi[i] - pos[i]) * inv;
                 amin = fmaxf(amin, fminf(a0, an));
                 amax = fminf(amax, fmaxf(a0, an));
             }
@@ -513,6 +514,7 @@ namespace {
         uint32_t hist_steps = 0;
         float att0 = 0.0f, att1 = 0.0f, att2 = 0.0f;
         uint64_t vidx = 0;
+        float forced_wc = 0.0f; // weight correction waiting for a forced-voxel interaction pass
         unsigned long long my_steps = 0, my_deposits = 0, my_overflows = 0, my_histories = 0;
 
         // warp-uniform pool of history ids [pool_next, pool_end)
@@ -548,7 +550,11 @@ namespace {
                         if (mine) {
                             const uint64_t h = pool_next + rank;
                             rng.init(p.seed, h);
-                            const uint32_t ei = p.uniform_hpe ? static_cast<uint32_t>(h / p.uniform_hpe) : find_exposure(p.source, h);
+                            uint32_t ei;
+                            if (p.uniform_hpe && p.total_histories <= 0xffffffffull)
+                                ei = static_cast<uint32_t>(h) / static_cast<uint32_t>(p.uniform_hpe);
+                            else
+                                ei = p.uniform_hpe ? static_cast<uint32_t>(h / p.uniform_hpe) : find_exposure(p.source, h);
                             DevExposure ex;
                             load_exposure(p.source.exposures + ei, ex);
                             sample_particle(p.source, ex, rng, ph);
@@ -617,53 +623,40 @@ namespace {
                             check_roulette = true;
                         }
                     } else {
-                        // forced photoelectric scoring (computeInteractionsForced, transport.hpp:523-581)
-                        bool cont = true;
+                        // forced photoelectric scoring (computeInteractionsForced, transport.hpp:523-581):
+                        // score the forced photoelectric share now; a real Compton or Rayleigh
+                        // event goes through the interaction passes and the weight correction
+                        // (1 - wc) is applied after it
                         const float photoProb = att0 / attTot;
-                        const float wc = eventProb * photoProb;
+                        forced_wc = eventProb * photoProb;
                         {
                             Photon forced = ph;
                             const float ef = photo_absorption<MODEL>(L, m, forced, mat, rng);
-                            deposit = (forced.energy < ENERGY_CUTOFF ? (ef + forced.energy) : ef) * forced.weight * wc;
+                            deposit = (forced.energy < ENERGY_CUTOFF ? (ef + forced.energy) : ef) * forced.weight * forced_wc;
                             do_score = true;
                         }
                         if (rng.uniform() < eventProb * (1.0f - photoProb)) {
-                            const float r2 = rng.uniform() * (att1 + att2);
-                            if (r2 < att1) {
-                                float e = 0.0f;
-                                if (!compton_scatter<MODEL>(L, m, ph, mat, rng, e)) {
-                                    ++my_overflows;
-                                    cont = false;
-                                } else {
-                                    // the forced photoelectric deposit and the Compton deposit are two events
-                                    if (isfinite(deposit)) {
-                                        score(p, vidx, deposit);
-                                        ++my_deposits;
-                                    } else {
-                                        ++my_overflows;
-                                    }
-                                    if (ph.energy < ENERGY_CUTOFF) {
-                                        deposit = (e + ph.energy) * ph.weight;
-                                        ph.energy = 0.0f;
-                                        cont = false;
-                                    } else {
-                                        deposit = e * ph.weight;
-                                        updateMax = true;
-                                    }
-                                }
-                            } else {
-                                if (!rayleigh_scatter<MODEL>(L, m, ph, mat, rng)) {
-                                    ++my_overflows;
-                                    cont = false;
-                                }
-                            }
+                            pending = rng.uniform() * (att1 + att2) < att1 ? EV_COMPTON : EV_RAYLEIGH;
+                        } else {
+                            ph.weight *= (1.0f - forced_wc);
+                            forced_wc = 0.0f;
+                            check_roulette = true;
                         }
-                        if (cont)
-                            ph.weight *= (1.0f - wc);
-                        alive = cont;
-                        check_roulette = cont;
                     }
                 }
+            }
+            if (do_score) {
+                // the forced photoelectric deposit is scored before this lane's
+                // interaction pass can add a second deposit in the same iteration
+                if (isfinite(deposit)) {
+                    score(p, vidx, deposit);
+                    ++my_deposits;
+                } else {
+                    ++my_overflows;
+                    alive = false;
+                    pending = EV_NONE;
+                }
+                do_score = false;
             }
 
             // ---- interaction passes, one converged pass per event type ---------------------
@@ -708,6 +701,9 @@ namespace {
                         }
                     }
                     if (pending != EV_NONE) {
+                        if (alive && forced_wc != 0.0f)
+                            ph.weight *= (1.0f - forced_wc);
+                        forced_wc = 0.0f;
                         check_roulette = alive;
                         pending = EV_NONE;
                     }

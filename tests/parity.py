@@ -53,11 +53,17 @@ def compare_sparse(ref: dict, dose: np.ndarray, var: np.ndarray, min_frac: float
     )
 
 
-def assert_parity(stats: dict, label: str = "") -> None:
+def assert_parity(stats: dict, label: str = "", correlated: bool = False) -> None:
+    """correlated=True for forced-interaction scoring, where every Woodcock step in a
+    measured voxel scores a deposit: the per-event variance field is then far from
+    Gaussian voxel to voxel (the reference restated on the CPU exceeds the plain
+    Gaussian count against the reference itself), so twice the Gaussian rate of
+    3-sigma exceedances is allowed."""
     msg = f"{label}: {stats}"
     assert stats["n_voxels"] > 10, msg
     n = stats["n_voxels"]
-    allowed = int(P_BEYOND_3SIGMA * n + 4.0 * np.sqrt(P_BEYOND_3SIGMA * (1 - P_BEYOND_3SIGMA) * n)) + 1
+    p_beyond = P_BEYOND_3SIGMA * (2.0 if correlated else 1.0)
+    allowed = int(p_beyond * n + 4.0 * np.sqrt(p_beyond * (1 - p_beyond) * n)) + 1
     assert stats["beyond_3sigma"] <= allowed, msg + f" (allowed {allowed} beyond 3 sigma)"
     assert stats["max_abs_z"] <= MAX_ABS_Z, msg
     # chi2/dof of n standard normals has standard deviation sqrt(2 / n)

@@ -132,7 +132,7 @@ def test_forced_interactions_match_reference(gpu_ctx, golden):
     dose, var, nev, stats = _run(gpu_ctx, world, src.exposures(), src.maxPhotonEnergyProduced(), src.spectrum(),
                                  model=1)
     s = compare_sparse(g, dose, var)
-    assert_parity(s, "forced")
+    assert_parity(s, "forced", correlated=True)
 
 
 def test_warp_aggregated_tally_matches_reference(gpu_ctx, golden):

@@ -101,4 +101,4 @@ def test_port_forced_matches_reference(lib, golden):
     e, e2, nev, secs, steps = port.transport(info, dims, tuple(g["spacing"]), dens, mat, src.exposures().as_matrix(),
                                              model=1, seed=3, spectrum=([50.0], [1.0]), measurement=g["measurement"])
     d, v = port.ev_per_history(e, e2, N)
-    assert_parity(compare_sparse(g, d, v), "port forced")
+    assert_parity(compare_sparse(g, d, v), "port forced", correlated=True)
