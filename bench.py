@@ -285,14 +285,13 @@ def main():
 
     def e2e_step(seed):
         dw = dx.DeviceWorld(ctx, e2e_world, layout=args.layout)
-        bl = dx.LutBlob(e2e_world.materialMap(), dw.max_density(), src.maxPhotonEnergyProduced())
+        bl = dx.LutBlob.cached(e2e_world.materialMap(), dw.max_density(), src.maxPhotonEnergyProduced())
         dl = dx.DeviceLut(ctx, bl)
         ex = src.exposures(e2e_world.directionCosines())
         job = dx.Job(ctx, dw, dl, ex, src.spectrum(), src.heel(), None, seed=seed, model=args.model)
         job.result(A.OUTPUT_EV_PER_HISTORY, out=(out_d, out_v, out_n))
         job.close()
         dl.close()
-        bl.close()
         dw.close()
 
     if args.no_e2e:

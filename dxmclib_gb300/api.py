@@ -284,19 +284,19 @@ class ExposureTable:
     def __len__(self):
         return len(self.weight)
 
-    def to_c(self):
+    def to_c(self) -> np.ndarray:
+        """Packs the table in the layout of dxmc_exposure (19 eight-byte fields per record)."""
         n = len(self)
-        arr = (A.Exposure * n)()
-        for i in range(n):
-            e = arr[i]
-            e.position[:] = self.position[i].tolist()
-            e.direction_cosines[:] = self.cosines[i].tolist()
-            e.beam_direction[:] = self.beam_direction[i].tolist()
-            e.collimation[:] = self.collimation[i].tolist()
-            e.weight = float(self.weight[i])
-            e.n_histories = int(self.n_histories[i])
-            e.mono_energy = float(self.mono_energy[i])
-        return arr
+        buf = np.empty((n, 19), np.float64)
+        buf[:, 0:3] = self.position
+        buf[:, 3:9] = self.cosines
+        buf[:, 9:12] = self.beam_direction
+        buf[:, 12:16] = self.collimation
+        buf[:, 16] = self.weight
+        buf.view(np.uint64)[:, 17] = self.n_histories.astype(np.uint64)
+        buf[:, 18] = self.mono_energy
+        assert C.sizeof(A.Exposure) == 19 * 8
+        return buf
 
     def as_matrix(self) -> np.ndarray:
         """(n, 19) rows: pos[3], cos[6], beam[3], coll[4], weight, n_histories, 0."""
@@ -798,6 +798,27 @@ class LutBlob:
                                                     C.byref(self.handle)), None, "dxmc_lut_build_max_density")
         self.n_materials = len(materials)
 
+    _cache = {}
+    _cache_order: list = []
+    CACHE_SIZE = 16
+
+    @classmethod
+    def cached(cls, materials: Sequence[Material], max_density: Sequence[float], max_energy: float) -> "LutBlob":
+        """LUT for a material set, per-material maximum density and maximum energy, built
+        once and reused: the table depends on nothing else (attenuationlut.hpp:64-96)."""
+        key = (tuple((m.name(), m.standardDensity()) for m in materials),
+               tuple(float(d) for d in max_density), float(max_energy))
+        blob = cls._cache.get(key)
+        if blob is None:
+            blob = cls(materials, max_density, max_energy)
+            blob._materials_ref = list(materials)
+            cls._cache[key] = blob
+            cls._cache_order.append(key)
+            if len(cls._cache_order) > cls.CACHE_SIZE:
+                old = cls._cache_order.pop(0)
+                cls._cache.pop(old).close()
+        return blob
+
     @staticmethod
     def from_world(world: World, max_energy: float) -> "LutBlob":
         mats = world.materialMap()
@@ -897,7 +918,7 @@ class Job:
         jd = A.JobDesc()
         ex = exposures.to_c()
         self._keep.append(ex)
-        jd.exposures = C.cast(ex, C.POINTER(A.Exposure))
+        jd.exposures = ex.ctypes.data_as(C.POINTER(A.Exposure))
         jd.n_exposures = len(exposures)
         if spectrum is not None:
             se = np.ascontiguousarray(spectrum.energies, np.float64)
@@ -1012,7 +1033,7 @@ class Transport:
         exposures = source.exposures(world.directionCosines())
         histories = int(np.sum(exposures.n_histories))
         dworld = DeviceWorld(self._ctx, world)
-        blob = LutBlob(world.materialMap(), dworld.max_density(), source.maxPhotonEnergyProduced())
+        blob = LutBlob.cached(world.materialMap(), dworld.max_density(), source.maxPhotonEnergyProduced())
         dlut = DeviceLut(self._ctx, blob)
         t0 = time.perf_counter()
         job = Job(self._ctx, dworld, dlut, exposures, source.spectrum(), source.heel(), source.bowtie(), self._seed,
@@ -1029,5 +1050,4 @@ class Transport:
         job.close()
         dlut.close()
         dworld.close()
-        blob.close()
         return Result(dose, nev, var, histories, sim_time, units, stats)

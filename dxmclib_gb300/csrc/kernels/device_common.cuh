@@ -82,30 +82,34 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1
     return c;
 }
 
-// Per-history random stream: a PCG32 (XSH-RR, O'Neill 2014) generator whose
-// 64-bit state and odd increment are drawn from Philox4x32-10 keyed by the job
-// seed with the history id as counter, so every history has its own stream
-// and a job can be split or resumed at any history id.  PCG32 is also the
-// generator of the reference (dxmcrandom.hpp:156-165).
+// Per-history random stream: xoshiro128** (Blackman and Vigna, "Scrambled
+// linear pseudorandom number generators", 2021), a 32-bit-native generator,
+// with its 128-bit state drawn from Philox4x32-10 keyed by the job seed with
+// the history id as counter.  Every history has its own stream, so a job can be
+// split or resumed at any history id and results do not depend on scheduling.
 struct Rng {
-    uint64_t state;
-    uint64_t inc;
+    uint32_t s0, s1, s2, s3;
 
     __device__ void init(uint64_t seed, uint64_t history)
     {
         const uint4 r = philox4x32_10(make_uint4(static_cast<uint32_t>(history), static_cast<uint32_t>(history >> 32), 0x44584d43u, 0u),
             static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
-        state = (static_cast<uint64_t>(r.y) << 32) | r.x;
-        inc = (((static_cast<uint64_t>(r.w) << 32) | r.z) << 1) | 1u;
-        next();
+        s0 = r.x;
+        s1 = r.y;
+        s2 = r.z;
+        s3 = r.w | 1u; // the all-zero state is excluded
     }
     __device__ __forceinline__ uint32_t next()
     {
-        const uint64_t old = state;
-        state = old * 6364136223846793005ull + inc;
-        const uint32_t xorshifted = static_cast<uint32_t>(((old >> 18u) ^ old) >> 27u);
-        const uint32_t rot = static_cast<uint32_t>(old >> 59u);
-        return __funnelshift_r(xorshifted, xorshifted, rot);
+        const uint32_t result = __funnelshift_l(s1 * 5u, s1 * 5u, 7) * 9u;
+        const uint32_t t = s1 << 9;
+        s2 ^= s0;
+        s3 ^= s1;
+        s1 ^= s2;
+        s0 ^= s3;
+        s2 ^= t;
+        s3 = __funnelshift_l(s3, s3, 11);
+        return result;
     }
     // [0, 1) with 24 random bits
     __device__ __forceinline__ float uniform() { return static_cast<float>(next() >> 8) * 0x1p-24f; }

@@ -512,10 +512,10 @@ namespace {
         bool updateMax = true;
         int cached_mat = -1;
         uint32_t hist_steps = 0;
+        uint32_t lane_steps = 0, lane_deposits = 0, lane_overflows = 0, lane_histories = 0;
         float att0 = 0.0f, att1 = 0.0f, att2 = 0.0f;
         uint64_t vidx = 0;
         float forced_wc = 0.0f; // weight correction waiting for a forced-voxel interaction pass
-        unsigned long long my_steps = 0, my_deposits = 0, my_overflows = 0, my_histories = 0;
 
         // warp-uniform pool of history ids [pool_next, pool_end)
         uint64_t pool_next = 0, pool_end = 0;
@@ -558,7 +558,7 @@ namespace {
                             DevExposure ex;
                             load_exposure(p.source.exposures + ei, ex);
                             sample_particle(p.source, ex, rng, ph);
-                            ++my_histories;
+                            ++lane_histories;
                             alive = transport_to_world(w, ph);
                             pending = EV_NONE;
                             updateMax = true;
@@ -595,7 +595,7 @@ namespace {
                     alive = false;
                 } else if (++hist_steps > MAX_STEPS_PER_HISTORY) {
                     // bounded work per history: end it and report the overflow
-                    ++my_overflows;
+                    ++lane_overflows;
                     alive = false;
                 } else {
                     const uint32_t ix = min(static_cast<uint32_t>((ph.px - w.lo[0]) * w.inv_spacing[0]), w.dims[0] - 1);
@@ -606,7 +606,7 @@ namespace {
                     int mat;
                     bool measured;
                     gather_voxel<PALETTE>(w, pal, vidx, density, mat, measured);
-                    ++my_steps;
+                    ++lane_steps;
                     if (mat != cached_mat) {
                         lut_attenuation(L, m, mat, logE, seg, att0, att1, att2);
                         cached_mat = mat;
@@ -650,9 +650,9 @@ namespace {
                 // interaction pass can add a second deposit in the same iteration
                 if (isfinite(deposit)) {
                     score(p, vidx, deposit);
-                    ++my_deposits;
+                    ++lane_deposits;
                 } else {
-                    ++my_overflows;
+                    ++lane_overflows;
                     alive = false;
                     pending = EV_NONE;
                 }
@@ -680,7 +680,7 @@ namespace {
                     if (__any_sync(FULL_MASK, pending == EV_COMPTON) && pending == EV_COMPTON) {
                         float e = 0.0f;
                         if (!compton_scatter<MODEL>(L, m, ph, mat, rng, e)) {
-                            ++my_overflows;
+                            ++lane_overflows;
                             alive = false;
                         } else {
                             do_score = true;
@@ -696,7 +696,7 @@ namespace {
                     }
                     if (__any_sync(FULL_MASK, pending == EV_RAYLEIGH) && pending == EV_RAYLEIGH) {
                         if (!rayleigh_scatter<MODEL>(L, m, ph, mat, rng)) {
-                            ++my_overflows;
+                            ++lane_overflows;
                             alive = false;
                         }
                     }
@@ -723,7 +723,7 @@ namespace {
                 // history and report it through the overflow counter
                 do_score = false;
                 alive = false;
-                ++my_overflows;
+                ++lane_overflows;
             }
             // ---- scoring; the warp is converged here ----------------------------------------
             if (p.tally_mode == 2) {
@@ -734,10 +734,11 @@ namespace {
                 score(p, vidx, deposit);
             }
             if (do_score)
-                ++my_deposits;
+                ++lane_deposits;
         }
 
         // ---- per-warp counter flush ------------------------------------------------------
+        unsigned long long my_steps = lane_steps, my_deposits = lane_deposits, my_overflows = lane_overflows, my_histories = lane_histories;
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
             my_steps += __shfl_down_sync(FULL_MASK, my_steps, off);

@@ -155,9 +155,23 @@ class Tube:
                 out[idx] += total * p * math.exp(-mu * 19.3 * 3e-4 / sin_a)
         return out
 
+    def _state(self):
+        return (self._voltage, self._anode, self._res, tuple((m.name(), m.standardDensity(), t) for m, t in self._filters))
+
     def getSpecter(self, energies=None, anode_angle=None, normalize: bool = True) -> np.ndarray:
         e = self.getEnergy() if energies is None else np.asarray(energies, np.float64)
         a = self._anode if anode_angle is None else anode_angle
+        # spectra are deterministic in the tube settings: memoise them
+        key = (self._state(), e.tobytes(), float(a), bool(normalize))
+        cache = self._w_cache.setdefault("spectra", {})
+        hit = cache.get(key)
+        if hit is not None:
+            return hit.copy()
+        spec = self._compute_specter(e, a, normalize)
+        cache[key] = spec.copy()
+        return spec
+
+    def _compute_specter(self, e: np.ndarray, a: float, normalize: bool) -> np.ndarray:
         spec = self._kramers_self_absorbed(e, a)
         spec = self._characteristic(e, a, spec)
         for m, mm in self._filters:
