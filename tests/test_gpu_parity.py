@@ -69,12 +69,16 @@ def test_pencil_beam_matches_reference(gpu_ctx, golden, model):
     g, (dose, var, nev, stats) = _pencil(gpu_ctx, golden, model)
     s = compare_sparse(g, dose, var)
     assert_parity(s, f"pencil m{model}")
-    # depth-dose profile (energy summed over each slice): within 3 %, the statistical
-    # spread of the reference's own 2e6-history slices
+    # depth-dose profile (energy summed over each slice): per-slice z-scores with the slice
+    # variance summed from the voxel variances; the reference side's variance is the GPU's
+    # scaled by the history ratio (same physics, variance of the mean ~ 1/N)
     d3 = dose.reshape(64, 64, 64).sum(axis=(1, 2))
+    v3 = var.reshape(64, 64, 64).sum(axis=(1, 2))
     ref = g["depth"]
     sel = ref > 0.05 * ref.max()
-    np.testing.assert_allclose(d3[sel], ref[sel], rtol=0.03)
+    v_ref = v3 * stats["histories"] / float(g["histories"])
+    z = (d3[sel] - ref[sel]) / np.sqrt(v3[sel] + v_ref[sel])
+    assert np.max(np.abs(z)) <= 5.0, z
     assert abs(d3[sel].sum() / ref[sel].sum() - 1) < 0.005
 
 

@@ -25,7 +25,7 @@ def _job_desc(exposures, spectrum, heel, bowtie, seed, keep):
     jd = A.JobDesc()
     ex = exposures.to_c()
     keep.append(ex)
-    jd.exposures = C.cast(ex, C.POINTER(A.Exposure))
+    jd.exposures = ex.ctypes.data_as(C.POINTER(A.Exposure))
     jd.n_exposures = len(exposures)
     se = np.ascontiguousarray(spectrum.energies, np.float64)
     sw = np.ascontiguousarray(spectrum.weights, np.float64)
