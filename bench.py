@@ -172,6 +172,7 @@ def main():
     ap.add_argument("--layout", type=int, default=0, help="0 = compact palette when possible, 1 = 8-byte voxels")
     ap.add_argument("--block-size", type=int, default=0)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
+    ap.add_argument("--queue-log2", type=int, default=0, help="photon queue chunk 2^n (0 = default, -1 = in-kernel generation)")
     args = ap.parse_args()
     ws, rank, local = _dist()
     metric = "histories/s"
@@ -220,7 +221,7 @@ def main():
     wl = build_workload(histories)
     world, src = wl.world, wl.source
     ctx = dx.GpuContext(device=device, block_size=args.block_size, blocks_per_sm=args.blocks_per_sm,
-                        regen_threshold=args.regen, interact_threshold=args.interact)
+                        regen_threshold=args.regen, interact_threshold=args.interact, queue_log2_chunk=args.queue_log2)
     dworld = dx.DeviceWorld(ctx, world, layout=args.layout)
     md = dworld.max_density()
     blob = dx.LutBlob(world.materialMap(), md, src.maxPhotonEnergyProduced())
@@ -339,7 +340,8 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "histories/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps},
-            "gpu_launches": args.steps,
+            # per step: one generation pass and one transport launch per queue chunk
+            "gpu_launches": args.steps * (1 if args.queue_log2 < 0 else 2 * max(1, -(-n_hist // (1 << (args.queue_log2 or 25))))),
             "clocks": clocks.summary(),
         }
         print(json.dumps(line), flush=True)

@@ -102,6 +102,7 @@ class GpuOptions(C.Structure):
         ("device", C.c_int32), ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32),
         ("tally_mode", C.c_int32), ("memory_budget", C.c_uint64),
         ("regen_threshold", C.c_int32), ("interact_threshold", C.c_int32),
+        ("queue_log2_chunk", C.c_int32), ("pad", C.c_int32),
     ]
 
 

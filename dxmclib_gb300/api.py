@@ -726,10 +726,11 @@ class GpuContext:
     """Owns a dxmc_gpu_ctx; one per device per process is enough."""
 
     def __init__(self, device: int = 0, block_size: int = 0, blocks_per_sm: int = 0, tally_mode: int = A.TALLY_F64,
-                 memory_budget: int = 0, regen_threshold: int = 0, interact_threshold: int = 0):
+                 memory_budget: int = 0, regen_threshold: int = 0, interact_threshold: int = 0,
+                 queue_log2_chunk: int = 0):
         self.lib = A.load()
         opts = A.GpuOptions(device, block_size, blocks_per_sm, tally_mode, memory_budget, regen_threshold,
-                            interact_threshold)
+                            interact_threshold, queue_log2_chunk, 0)
         self.handle = C.c_void_p()
         A.check(self.lib.dxmc_gpu_ctx_create(C.byref(opts), C.byref(self.handle)), None, "dxmc_gpu_ctx_create")
 

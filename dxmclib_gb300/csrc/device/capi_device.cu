@@ -66,6 +66,7 @@ struct dxmc_job {
     uint32_t* n_events = nullptr;
     dev::JobCounters* counters = nullptr;
     unsigned char* tables = nullptr;
+    unsigned char* queue = nullptr; // pre-generated photons (SoA)
     int* cancel_host = nullptr;  // pinned, mapped
     int* cancel_dev = nullptr;
     cudaEvent_t begin = nullptr, start = nullptr, stop = nullptr; // job begin, kernel start, kernel end
@@ -602,6 +603,9 @@ void free_job_device(dxmc_job* j)
         cudaFreeAsync(j->counters, s);
     if (j->tables)
         cudaFreeAsync(j->tables, s);
+    if (j->queue)
+        cudaFreeAsync(j->queue, s);
+    j->queue = nullptr;
     j->tally = nullptr;
     j->tally_f32 = nullptr;
     j->n_events = nullptr;
@@ -725,7 +729,11 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
 
     const uint64_t nv = world->params.n_voxels;
     const uint64_t tally_bytes = tally_mode == 1 ? nv * 2 * sizeof(float) : nv * 2 * sizeof(double);
-    const uint64_t job_bytes = tally_bytes + nv * sizeof(uint32_t) + table_bytes + sizeof(dev::JobCounters);
+    // photon queue: chunks of 2^k histories, 48 bytes per queued photon
+    const int log2_chunk = ctx->options.queue_log2_chunk == 0 ? 25 : ctx->options.queue_log2_chunk;
+    const uint64_t chunk = log2_chunk < 0 ? 0 : std::min<uint64_t>(total, 1ull << std::min(log2_chunk, 34));
+    const uint64_t queue_bytes = chunk * 48;
+    const uint64_t job_bytes = tally_bytes + nv * sizeof(uint32_t) + table_bytes + sizeof(dev::JobCounters) + queue_bytes;
     if (ctx->in_use + job_bytes > ctx->budget)
         return fail(ctx, DXMC_ERR_OOM, "job exceeds the device memory budget");
 
@@ -750,6 +758,8 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
         e = cudaMallocAsync(&j->counters, sizeof(dev::JobCounters), s);
     if (e == cudaSuccess)
         e = cudaMallocAsync(&j->tables, table_bytes, s);
+    if (e == cudaSuccess && queue_bytes)
+        e = cudaMallocAsync(&j->queue, queue_bytes, s);
     if (e == cudaSuccess)
         e = cudaEventCreate(&j->begin);
     if (e == cudaSuccess)
@@ -837,11 +847,33 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
     if (per_sm <= 0)
         per_sm = 1;
     const int grid = ctx->sm_count * per_sm;
-    e = cudaEventRecord(j->start, s);
-    if (e == cudaSuccess)
-        e = dev::launch_transport(p, jd->model, grid, block, smem, s);
-    if (e == cudaSuccess)
-        e = cudaEventRecord(j->stop, s);
+    if (chunk == 0) {
+        // photons generated inside the transport kernel
+        e = cudaEventRecord(j->start, s);
+        if (e == cudaSuccess)
+            e = dev::launch_transport(p, jd->model, grid, block, smem, s);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(j->stop, s);
+    } else {
+        p.queue.pos_energy = reinterpret_cast<float4*>(j->queue);
+        p.queue.dir_weight = reinterpret_cast<float4*>(j->queue + chunk * 16);
+        p.queue.rng = reinterpret_cast<uint4*>(j->queue + chunk * 32);
+        p.queue.capacity = chunk;
+        const int gen_grid = ctx->sm_count * 8;
+        for (uint64_t first = 0; first < total && e == cudaSuccess; first += chunk) {
+            const uint64_t count = std::min(chunk, total - first);
+            // queue_count and next_photon restart for every chunk
+            e = cudaMemsetAsync(&j->counters->queue_count, 0, 2 * sizeof(unsigned long long), s);
+            if (e == cudaSuccess)
+                e = dev::launch_generate(p, first, count, gen_grid, s);
+            if (e == cudaSuccess && first == 0)
+                e = cudaEventRecord(j->start, s);
+            if (e == cudaSuccess)
+                e = dev::launch_transport(p, jd->model, grid, block, smem, s);
+        }
+        if (e == cudaSuccess)
+            e = cudaEventRecord(j->stop, s);
+    }
     if (e != cudaSuccess) {
         cudaStreamSynchronize(s);
         free_job_device(j);

@@ -48,12 +48,23 @@ struct SourceParams {
 
 // Counters shared by all blocks of one job (device scratch).
 struct JobCounters {
-    unsigned long long next_history;   // work queue head
+    unsigned long long next_history;   // work queue head (in-kernel photon generation)
     unsigned long long histories_done;
     unsigned long long steps;          // Woodcock steps inside the grid
     unsigned long long deposits;       // depositing events
     unsigned long long overflows;      // rejection-cap hits
-    unsigned long long pad[3];
+    unsigned long long queue_count;    // photons in the pre-generated queue
+    unsigned long long next_photon;    // pre-generated queue head
+    unsigned long long pad;
+};
+
+// Pre-generated photons (structure of arrays): position + energy, direction +
+// weight, and the history's random-stream state after generation.
+struct PhotonQueue {
+    float4* pos_energy;
+    float4* dir_weight;
+    uint4* rng;
+    uint64_t capacity;
 };
 
 struct TransportParams {
@@ -66,6 +77,7 @@ struct TransportParams {
     uint32_t* n_events;
     JobCounters* counters;
     const volatile int* cancel; // host-mapped flag, may be null
+    PhotonQueue queue;          // pos_energy == nullptr: photons are generated inside the transport kernel
     uint64_t total_histories;
     uint64_t seed;
     uint64_t uniform_hpe;   // histories per exposure when every exposure has the same count, else 0
@@ -76,6 +88,9 @@ struct TransportParams {
 };
 
 // Launchers (defined in transport_kernels.cu).
+// Samples histories [first, first + count) into p.queue (compacted: photons that
+// miss the world are counted but not queued).
+cudaError_t launch_generate(const TransportParams& p, uint64_t first, uint64_t count, int grid, cudaStream_t stream);
 cudaError_t launch_transport(const TransportParams& p, int model, int grid, int block, size_t smem, cudaStream_t stream);
 // blocks per SM for this configuration; also raises the kernel's dynamic shared-memory limit
 int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem);

@@ -502,6 +502,8 @@ namespace {
         const unsigned lanemask_lt = (1u << lane) - 1u;
         const int regen_t = p.regen_threshold;
         const int interact_t = p.interact_threshold;
+        const bool use_queue = p.queue.pos_energy != nullptr;
+        const unsigned long long queue_total = use_queue ? p.counters->queue_count : 0ull;
 
         Photon ph {};
         Rng rng;
@@ -523,7 +525,50 @@ namespace {
 
         while (true) {
             // ---- refill idle lanes together ------------------------------------------------
-            {
+            if (use_queue) {
+                unsigned need = __ballot_sync(FULL_MASK, !alive && !exhausted);
+                const unsigned live = __ballot_sync(FULL_MASK, alive);
+                if (need && (__popc(need) >= regen_t || live == 0u)) {
+                    while (need && !exhausted) {
+                        if (pool_next >= pool_end) {
+                            unsigned long long base = 0;
+                            if (lane == 0) {
+                                const bool cancelled = p.cancel && *p.cancel;
+                                base = cancelled ? queue_total : atomicAdd(&p.counters->next_photon, (unsigned long long)WARP_POOL_CHUNK);
+                            }
+                            base = __shfl_sync(FULL_MASK, base, 0);
+                            if (base >= queue_total) {
+                                exhausted = true;
+                                break;
+                            }
+                            pool_next = base;
+                            pool_end = min(static_cast<uint64_t>(base + WARP_POOL_CHUNK), static_cast<uint64_t>(queue_total));
+                        }
+                        const uint64_t avail = pool_end - pool_next;
+                        const unsigned rank = __popc(need & lanemask_lt);
+                        const bool mine = ((need >> lane) & 1u) && rank < avail;
+                        const unsigned taken = __ballot_sync(FULL_MASK, mine);
+                        if (mine) {
+                            const uint64_t q = pool_next + rank;
+                            const float4 pe = __ldg(p.queue.pos_energy + q);
+                            const float4 dw = __ldg(p.queue.dir_weight + q);
+                            const uint4 rs = __ldg(p.queue.rng + q);
+                            ph = Photon { pe.x, pe.y, pe.z, dw.x, dw.y, dw.z, pe.w, dw.w };
+                            rng.s0 = rs.x;
+                            rng.s1 = rs.y;
+                            rng.s2 = rs.z;
+                            rng.s3 = rs.w;
+                            alive = true;
+                            pending = EV_NONE;
+                            updateMax = true;
+                            cached_mat = -1;
+                            hist_steps = 0;
+                        }
+                        pool_next += __popc(taken);
+                        need &= ~taken;
+                    }
+                }
+            } else {
                 unsigned need = __ballot_sync(FULL_MASK, !alive && !exhausted);
                 const unsigned live = __ballot_sync(FULL_MASK, alive);
                 if (need && (__popc(need) >= regen_t || live == 0u)) {
@@ -755,6 +800,52 @@ namespace {
         }
     }
 
+    // ---- photon generation pass ---------------------------------------------------------
+    // One thread per history: Exposure::sampleParticle + transportParticleToWorld with
+    // every lane of the warp busy; photons inside the world are appended to the queue
+    // together with the state of their random stream.
+    __global__ void __launch_bounds__(256) generate_kernel(const __grid_constant__ TransportParams p, uint64_t first, uint64_t count)
+    {
+        const int lane = threadIdx.x & 31;
+        unsigned long long generated = 0;
+        for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x); base < count; base += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+            const uint64_t i = base + threadIdx.x;
+            bool inworld = false;
+            Photon ph {};
+            Rng rng;
+            if (i < count) {
+                const uint64_t h = first + i;
+                rng.init(p.seed, h);
+                uint32_t ei;
+                if (p.uniform_hpe && p.total_histories <= 0xffffffffull)
+                    ei = static_cast<uint32_t>(h) / static_cast<uint32_t>(p.uniform_hpe);
+                else
+                    ei = p.uniform_hpe ? static_cast<uint32_t>(h / p.uniform_hpe) : find_exposure(p.source, h);
+                DevExposure ex;
+                load_exposure(p.source.exposures + ei, ex);
+                sample_particle(p.source, ex, rng, ph);
+                inworld = transport_to_world(p.world, ph);
+                ++generated;
+            }
+            const unsigned mask = __ballot_sync(FULL_MASK, inworld);
+            unsigned long long slot0 = 0;
+            if (lane == 0 && mask)
+                slot0 = atomicAdd(&p.counters->queue_count, static_cast<unsigned long long>(__popc(mask)));
+            slot0 = __shfl_sync(FULL_MASK, slot0, 0);
+            if (inworld) {
+                const uint64_t q = slot0 + __popc(mask & ((1u << lane) - 1u));
+                p.queue.pos_energy[q] = make_float4(ph.px, ph.py, ph.pz, ph.energy);
+                p.queue.dir_weight[q] = make_float4(ph.dx, ph.dy, ph.dz, ph.weight);
+                p.queue.rng[q] = make_uint4(rng.s0, rng.s1, rng.s2, rng.s3);
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+            generated += __shfl_down_sync(FULL_MASK, generated, off);
+        if (lane == 0 && generated)
+            atomicAdd(&p.counters->histories_done, generated);
+    }
+
     // ---- post-processing (transport.hpp:780-816) -------------------------------------
     template <typename TallyT>
     __global__ void postprocess_kernel(const TallyT* __restrict__ tally, const Voxel* __restrict__ voxels, uint64_t n, int mode,
@@ -854,6 +945,12 @@ static void* transport_function(int model, bool palette)
     if (palette)
         return model == 0 ? transport_entry<0, true>() : (model == 1 ? transport_entry<1, true>() : transport_entry<2, true>());
     return model == 0 ? transport_entry<0, false>() : (model == 1 ? transport_entry<1, false>() : transport_entry<2, false>());
+}
+
+cudaError_t launch_generate(const TransportParams& p, uint64_t first, uint64_t count, int grid, cudaStream_t stream)
+{
+    generate_kernel<<<grid, 256, 0, stream>>>(p, first, count);
+    return cudaGetLastError();
 }
 
 size_t transport_smem_bytes(size_t lut_bytes, bool lut_in_smem, bool palette)

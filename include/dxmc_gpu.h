@@ -190,6 +190,9 @@ typedef struct dxmc_gpu_options {
     uint64_t memory_budget;  /* admission budget in bytes, 0 = 90% of free memory */
     int32_t regen_threshold; /* refill finished lanes of a warp once this many are idle; 0 = default */
     int32_t interact_threshold; /* run the per-type interaction passes once this many lanes wait; 0 = default */
+    int32_t queue_log2_chunk;   /* photons are pre-generated in chunks of 2^n histories (48 B per photon);
+                                   0 = default (2^25), -1 = generate inside the transport kernel */
+    int32_t pad;
 } dxmc_gpu_options;
 
 int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out);
