@@ -21,8 +21,10 @@ using namespace dxmc_gb300;
 
 // Warp scheduling of the transport kernel: refill idle lanes once this many
 // are idle; run the per-type interaction passes once this many lanes wait.
-constexpr int DEFAULT_REGEN_THRESHOLD = 12;
+constexpr int DEFAULT_REGEN_THRESHOLD = 12;       // photons generated in the transport kernel
 constexpr int DEFAULT_INTERACT_THRESHOLD = 6;
+constexpr int DEFAULT_QUEUE_REGEN_THRESHOLD = 4;  // photons taken from the pre-generated queue
+constexpr int DEFAULT_QUEUE_INTERACT_THRESHOLD = 8;
 
 struct dxmc_gpu_ctx {
     int device = 0;
@@ -832,8 +834,13 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
         if (uniform)
             p.uniform_hpe = jd->exposures[0].n_histories;
     }
-    p.regen_threshold = ctx->options.regen_threshold > 0 ? std::min(ctx->options.regen_threshold, 32) : DEFAULT_REGEN_THRESHOLD;
-    p.interact_threshold = ctx->options.interact_threshold > 0 ? std::min(ctx->options.interact_threshold, 32) : DEFAULT_INTERACT_THRESHOLD;
+    {
+        const bool queued = ctx->options.queue_log2_chunk >= 0;
+        p.regen_threshold = ctx->options.regen_threshold > 0 ? std::min(ctx->options.regen_threshold, 32)
+                                                           : (queued ? DEFAULT_QUEUE_REGEN_THRESHOLD : DEFAULT_REGEN_THRESHOLD);
+        p.interact_threshold = ctx->options.interact_threshold > 0 ? std::min(ctx->options.interact_threshold, 32)
+                                                                   : (queued ? DEFAULT_QUEUE_INTERACT_THRESHOLD : DEFAULT_INTERACT_THRESHOLD);
+    }
 
     const size_t lut_bytes = static_cast<size_t>(lut->meta.total_floats) * sizeof(float);
     const size_t smem_limit = std::min<size_t>(ctx->max_smem_optin, 96 * 1024);
