@@ -128,6 +128,10 @@ class JobStats(C.Structure):
     ]
 
 
+class BatchEntry(C.Structure):
+    _fields_ = [("world", VP), ("lut", VP), ("job", C.POINTER(JobDesc))]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "dxmc_gpu_abi_version": (C.c_int, []),
@@ -158,6 +162,11 @@ SIGNATURES = {
     "dxmc_gpu_job_result": (C.c_int, [VP, C.c_int, D, DP, DP, U32P, C.POINTER(JobStats)]),
     "dxmc_gpu_job_free": (None, [VP]),
     "dxmc_gpu_probe_lut": (C.c_int, [VP, VP, C.c_int, DP, C.c_int, DP, DP]),
+    "dxmc_gpu_batch_submit": (C.c_int, [VP, C.POINTER(BatchEntry), C.c_int, C.POINTER(VP)]),
+    "dxmc_gpu_batch_wait": (C.c_int, [VP, C.c_int64]),
+    "dxmc_gpu_batch_job": (C.c_int, [VP, C.c_int, C.POINTER(VP)]),
+    "dxmc_gpu_batch_kernel_ms": (D, [VP]),
+    "dxmc_gpu_batch_free": (None, [VP]),
     "dxmc_gpu_transport_noalloc": (C.c_int, [VP, VP, VP, C.POINTER(JobDesc), VP, VP, C.POINTER(JobStats)]),
     "dxmc_gpu_probe_interactions": (C.c_int, [VP, VP, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_uint64, FP, FP, FP]),
 }

@@ -915,6 +915,20 @@ class Job:
                  seed: int = 1, model: int = LOWENERGYCORRECTION.LIVERMORE, tally_mode: int = -1):
         self.ctx = ctx
         self.dworld = dworld
+        self._owned = True
+        jd = self._describe(exposures, spectrum, heel, bowtie, seed, model, tally_mode)
+        self.handle = C.c_void_p()
+        A.check(ctx.lib.dxmc_gpu_job_submit(ctx.handle, dworld.handle, dlut.handle, C.byref(jd), C.byref(self.handle)),
+                ctx.handle, "dxmc_gpu_job_submit")
+
+    @classmethod
+    def _member(cls, ctx: GpuContext, dworld: DeviceWorld, handle: C.c_void_p) -> "Job":
+        """Job handle owned by a Batch."""
+        j = cls.__new__(cls)
+        j.ctx, j.dworld, j.handle, j._owned = ctx, dworld, handle, False
+        return j
+
+    def _describe(self, exposures: ExposureTable, spectrum, heel, bowtie, seed, model, tally_mode) -> A.JobDesc:
         self._keep = []
         jd = A.JobDesc()
         ex = exposures.to_c()
@@ -942,9 +956,8 @@ class Job:
         jd.seed = int(seed)
         jd.model = int(model)
         jd.tally_mode = int(tally_mode)
-        self.handle = C.c_void_p()
-        A.check(ctx.lib.dxmc_gpu_job_submit(ctx.handle, dworld.handle, dlut.handle, C.byref(jd), C.byref(self.handle)),
-                ctx.handle, "dxmc_gpu_job_submit")
+        self._keep.append(jd)
+        return jd
 
     def wait(self, timeout_ms: int = -1) -> int:
         return self.ctx.lib.dxmc_gpu_job_wait(self.handle, timeout_ms)
@@ -974,8 +987,61 @@ class Job:
         return dose, var, nev, stats
 
     def close(self):
-        if self.handle:
+        if self.handle and self._owned:
             self.ctx.lib.dxmc_gpu_job_free(self.handle)
+        self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BatchEntry:
+    """One job of a Batch: the arguments of Job without the context."""
+
+    def __init__(self, dworld: DeviceWorld, dlut: DeviceLut, exposures: ExposureTable, spectrum: Optional[Spectrum] = None,
+                 heel: Optional[HeelTable] = None, bowtie=None, seed: int = 1, model: int = LOWENERGYCORRECTION.LIVERMORE,
+                 tally_mode: int = -1):
+        self.dworld, self.dlut = dworld, dlut
+        self.args = (exposures, spectrum, heel, bowtie, seed, model, tally_mode)
+
+
+class Batch:
+    """Many jobs in one persistent launch (dxmc_gpu_batch_*); ``jobs[i]`` gives entry i's results."""
+
+    def __init__(self, ctx: GpuContext, entries: Sequence[BatchEntry]):
+        self.ctx = ctx
+        self._descs = []
+        arr = (A.BatchEntry * len(entries))()
+        for i, e in enumerate(entries):
+            holder = Job.__new__(Job)
+            jd = holder._describe(*e.args)
+            self._descs.append(holder)
+            arr[i].world = e.dworld.handle
+            arr[i].lut = e.dlut.handle
+            arr[i].job = C.pointer(jd)
+        self.handle = C.c_void_p()
+        A.check(ctx.lib.dxmc_gpu_batch_submit(ctx.handle, arr, len(entries), C.byref(self.handle)), ctx.handle,
+                "dxmc_gpu_batch_submit")
+        self.jobs = []
+        for i, e in enumerate(entries):
+            h = C.c_void_p()
+            A.check(ctx.lib.dxmc_gpu_batch_job(self.handle, i, C.byref(h)), ctx.handle, "dxmc_gpu_batch_job")
+            self.jobs.append(Job._member(ctx, e.dworld, h))
+
+    def wait(self, timeout_ms: int = -1) -> int:
+        return self.ctx.lib.dxmc_gpu_batch_wait(self.handle, timeout_ms)
+
+    def kernel_ms(self) -> float:
+        return self.ctx.lib.dxmc_gpu_batch_kernel_ms(self.handle)
+
+    def close(self):
+        if self.handle:
+            for j in self.jobs:
+                j.handle = C.c_void_p()
+            self.ctx.lib.dxmc_gpu_batch_free(self.handle)
             self.handle = C.c_void_p()
 
     def __del__(self):

@@ -617,11 +617,14 @@ void free_job_device(dxmc_job* j)
 
 } // namespace
 
-int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_job_desc* jd, dxmc_job** out)
+namespace {
+
+// Validates a job, builds its host tables, allocates and clears its device
+// buffers on the context stream and fills its kernel parameters.  Batched jobs
+// get no photon queue.  Caller holds the context mutex.
+int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_job_desc* jd, bool batched, dxmc_job** out,
+    dev::TransportParams& p, uint64_t& chunk_out)
 {
-    if (!ctx || !world || !lut || !jd || !out)
-        return DXMC_ERR_INVALID;
-    std::lock_guard<std::mutex> lock(ctx->mutex);
     *out = nullptr;
     if (world->ctx != ctx || lut->ctx != ctx)
         return fail(ctx, DXMC_ERR_INVALID, "world or lut belongs to another context");
@@ -733,7 +736,7 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
     const uint64_t tally_bytes = tally_mode == 1 ? nv * 2 * sizeof(float) : nv * 2 * sizeof(double);
     // photon queue: chunks of 2^k histories, 48 bytes per queued photon
     const int log2_chunk = ctx->options.queue_log2_chunk == 0 ? 25 : ctx->options.queue_log2_chunk;
-    const uint64_t chunk = log2_chunk < 0 ? 0 : std::min<uint64_t>(total, 1ull << std::min(log2_chunk, 34));
+    const uint64_t chunk = (log2_chunk < 0 || batched) ? 0 : std::min<uint64_t>(total, 1ull << std::min(log2_chunk, 34));
     const uint64_t queue_bytes = chunk * 48;
     const uint64_t job_bytes = tally_bytes + nv * sizeof(uint32_t) + table_bytes + sizeof(dev::JobCounters) + queue_bytes;
     if (ctx->in_use + job_bytes > ctx->budget)
@@ -792,7 +795,7 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
         return cuda_fail(ctx, e, "job allocation");
     }
 
-    dev::TransportParams p {};
+    p = dev::TransportParams {};
     p.world = world->params;
     auto& S = p.source;
     S.exposures = reinterpret_cast<const dev::DevExposure*>(j->tables + off_ex);
@@ -835,13 +838,51 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
             p.uniform_hpe = jd->exposures[0].n_histories;
     }
     {
-        const bool queued = ctx->options.queue_log2_chunk >= 0;
+        const bool queued = ctx->options.queue_log2_chunk >= 0 && !batched;
         p.regen_threshold = ctx->options.regen_threshold > 0 ? std::min(ctx->options.regen_threshold, 32)
                                                            : (queued ? DEFAULT_QUEUE_REGEN_THRESHOLD : DEFAULT_REGEN_THRESHOLD);
         p.interact_threshold = ctx->options.interact_threshold > 0 ? std::min(ctx->options.interact_threshold, 32)
                                                                    : (queued ? DEFAULT_QUEUE_INTERACT_THRESHOLD : DEFAULT_INTERACT_THRESHOLD);
     }
 
+
+    chunk_out = chunk;
+    *out = j;
+    return DXMC_OK;
+}
+
+void discard_job(dxmc_job* j)
+{
+    free_job_device(j);
+    if (j->cancel_host)
+        cudaFreeHost(j->cancel_host);
+    if (j->begin)
+        cudaEventDestroy(j->begin);
+    if (j->start)
+        cudaEventDestroy(j->start);
+    if (j->stop)
+        cudaEventDestroy(j->stop);
+    delete j;
+}
+
+} // namespace
+
+
+int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_job_desc* jd, dxmc_job** out)
+{
+    if (!ctx || !world || !lut || !jd || !out)
+        return DXMC_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    dev::TransportParams p {};
+    uint64_t chunk = 0;
+    dxmc_job* j = nullptr;
+    const int rc = prepare_job(ctx, world, lut, jd, false, &j, p, chunk);
+    if (rc != DXMC_OK)
+        return rc;
+    const uint64_t total = j->histories;
+    const uint64_t job_bytes = j->bytes;
+    cudaStream_t s = ctx->stream;
+    cudaError_t e = cudaSuccess;
     const size_t lut_bytes = static_cast<size_t>(lut->meta.total_floats) * sizeof(float);
     const size_t smem_limit = std::min<size_t>(ctx->max_smem_optin, 96 * 1024);
     p.lut_in_smem = lut_bytes <= smem_limit ? 1 : 0;
@@ -883,14 +924,170 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
     }
     if (e != cudaSuccess) {
         cudaStreamSynchronize(s);
-        free_job_device(j);
-        cudaFreeHost(j->cancel_host);
-        delete j;
+        discard_job(j);
         return cuda_fail(ctx, e, "transport launch");
     }
     ctx->in_use += job_bytes;
     *out = j;
     return DXMC_OK;
+}
+
+struct dxmc_batch {
+    dxmc_gpu_ctx* ctx = nullptr;
+    std::vector<dxmc_job*> jobs;
+    dev::TransportParams* d_params = nullptr;
+    dev::BatchItem* d_items = nullptr;
+    unsigned long long* d_next = nullptr; // one item counter per model group
+    cudaEvent_t start = nullptr, stop = nullptr;
+    uint64_t bytes = 0;
+};
+
+int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, int n, dxmc_batch** out)
+{
+    if (!ctx || !entries || n <= 0 || !out)
+        return DXMC_ERR_INVALID;
+    *out = nullptr;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    cudaSetDevice(ctx->device);
+    auto* b = new (std::nothrow) dxmc_batch;
+    if (!b)
+        return DXMC_ERR_OOM;
+    b->ctx = ctx;
+    cudaStream_t s = ctx->stream;
+    std::vector<dev::TransportParams> params(n);
+    std::vector<int> models(n);
+    uint64_t all = 0;
+    auto abort = [&](int rc) {
+        cudaStreamSynchronize(s);
+        for (auto* j : b->jobs) {
+            ctx->in_use -= j->bytes;
+            discard_job(j);
+        }
+        if (b->d_params)
+            cudaFree(b->d_params);
+        if (b->d_items)
+            cudaFree(b->d_items);
+        if (b->d_next)
+            cudaFree(b->d_next);
+        if (b->start)
+            cudaEventDestroy(b->start);
+        if (b->stop)
+            cudaEventDestroy(b->stop);
+        delete b;
+        return rc;
+    };
+    for (int i = 0; i < n; ++i) {
+        const dxmc_batch_entry& en = entries[i];
+        if (!en.world || !en.lut || !en.job)
+            return abort(fail(ctx, DXMC_ERR_INVALID, "batch entry " + std::to_string(i) + " is incomplete"));
+        dxmc_job* j = nullptr;
+        uint64_t chunk = 0;
+        const int rc = prepare_job(ctx, en.world, en.lut, en.job, true, &j, params[i], chunk);
+        if (rc != DXMC_OK)
+            return abort(rc);
+        ctx->in_use += j->bytes; // later entries see the earlier ones in the admission check
+        b->jobs.push_back(j);
+        models[i] = en.job->model;
+        all += j->histories;
+    }
+    // work items: about four per resident warp, 256 to 8192 histories each
+    const int per_sm = std::max(1, dev::batch_max_blocks_per_sm(1));
+    const uint64_t warps = static_cast<uint64_t>(ctx->sm_count) * per_sm * 8;
+    uint64_t item = std::clamp<uint64_t>(all / (warps * 4), 256, 8192);
+    item = (item + 31) / 32 * 32;
+    std::vector<dev::BatchItem> items;
+    std::vector<uint64_t> group_start(4, 0), group_count(4, 0);
+    for (int model = 0; model < 3; ++model) {
+        group_start[model] = items.size();
+        for (int i = 0; i < n; ++i) {
+            if (models[i] != model)
+                continue;
+            const uint64_t total = b->jobs[i]->histories;
+            for (uint64_t first = 0; first < total; first += item)
+                items.push_back(dev::BatchItem { static_cast<uint32_t>(i), static_cast<uint32_t>(std::min(item, total - first)), first });
+        }
+        group_count[model] = items.size() - group_start[model];
+    }
+    cudaError_t e = cudaMalloc(&b->d_params, n * sizeof(dev::TransportParams));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&b->d_items, items.size() * sizeof(dev::BatchItem));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&b->d_next, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->d_params, params.data(), n * sizeof(dev::TransportParams), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(dev::BatchItem), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(b->d_next, 0, 4 * sizeof(unsigned long long), s);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&b->start);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&b->stop);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(b->start, s);
+    for (auto* j : b->jobs) // every job's kernel time is the batch's
+        if (e == cudaSuccess)
+            e = cudaEventRecord(j->start, s);
+    for (int model = 0; model < 3 && e == cudaSuccess; ++model) {
+        if (!group_count[model])
+            continue;
+        const int grid = ctx->sm_count * std::max(1, dev::batch_max_blocks_per_sm(model));
+        const int regen = ctx->options.regen_threshold > 0 ? std::min(ctx->options.regen_threshold, 32) : DEFAULT_REGEN_THRESHOLD;
+        const int inter = ctx->options.interact_threshold > 0 ? std::min(ctx->options.interact_threshold, 32) : DEFAULT_INTERACT_THRESHOLD;
+        e = dev::launch_batch(b->d_params, b->d_items + group_start[model], group_count[model], b->d_next + model, model, regen, inter, grid, s);
+    }
+    if (e == cudaSuccess)
+        e = cudaEventRecord(b->stop, s);
+    for (auto* j : b->jobs)
+        if (e == cudaSuccess)
+            e = cudaEventRecord(j->stop, s);
+    if (e != cudaSuccess)
+        return abort(cuda_fail(ctx, e, "batch launch"));
+    b->bytes = n * sizeof(dev::TransportParams) + items.size() * sizeof(dev::BatchItem);
+    *out = b;
+    return DXMC_OK;
+}
+
+int dxmc_gpu_batch_wait(dxmc_batch* b, int64_t timeout_ms)
+{
+    if (!b || b->jobs.empty())
+        return DXMC_ERR_INVALID;
+    return dxmc_gpu_job_wait(b->jobs.back(), timeout_ms);
+}
+
+int dxmc_gpu_batch_job(dxmc_batch* b, int index, dxmc_job** job)
+{
+    if (!b || !job || index < 0 || index >= static_cast<int>(b->jobs.size()))
+        return DXMC_ERR_INVALID;
+    *job = b->jobs[index];
+    return DXMC_OK;
+}
+
+double dxmc_gpu_batch_kernel_ms(dxmc_batch* b)
+{
+    if (!b)
+        return 0.0;
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, b->start, b->stop) != cudaSuccess)
+        return 0.0;
+    return ms;
+}
+
+void dxmc_gpu_batch_free(dxmc_batch* b)
+{
+    if (!b)
+        return;
+    for (auto* j : b->jobs)
+        dxmc_gpu_job_free(j);
+    std::lock_guard<std::mutex> lock(b->ctx->mutex);
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    cudaFree(b->d_params);
+    cudaFree(b->d_items);
+    cudaFree(b->d_next);
+    cudaEventDestroy(b->start);
+    cudaEventDestroy(b->stop);
+    delete b;
 }
 
 int dxmc_gpu_job_wait(dxmc_job* j, int64_t timeout_ms)

@@ -88,6 +88,15 @@ struct TransportParams {
 };
 
 // Launchers (defined in transport_kernels.cu).
+// Work item of the batched kernel: histories [first, first + count) of job `job`.
+struct BatchItem {
+    uint32_t job;
+    uint32_t count;
+    uint64_t first;
+};
+cudaError_t launch_batch(const TransportParams* jobs, const void* items, uint64_t n_items, unsigned long long* next_item, int model,
+    int regen_threshold, int interact_threshold, int grid, cudaStream_t stream);
+int batch_max_blocks_per_sm(int model);
 // Samples histories [first, first + count) into p.queue (compacted: photons that
 // miss the world are counted but not queued).
 cudaError_t launch_generate(const TransportParams& p, uint64_t first, uint64_t count, int grid, cudaStream_t stream);

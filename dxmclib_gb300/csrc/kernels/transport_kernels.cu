@@ -473,6 +473,267 @@ namespace {
 #ifndef DXMC_MIN_BLOCKS_PER_SM
 #define DXMC_MIN_BLOCKS_PER_SM 4 // resident 256-thread blocks per SM the register budget must allow (64 registers)
 #endif
+
+    // State of one lane: its photon, random stream, cached lookups and counters.
+    struct Lane {
+        Photon ph;
+        Rng rng;
+        bool alive;
+        int pending;
+        float maxInv, logE;
+        int seg;
+        bool updateMax;
+        int cached_mat;
+        uint32_t hist_steps;
+        float att0, att1, att2;
+        uint64_t vidx;
+        float forced_wc; // weight correction waiting for a forced-voxel interaction pass
+        uint32_t steps, deposits, overflows, histories;
+
+        __device__ void reset_counters() { steps = deposits = overflows = histories = 0; }
+        __device__ void start_photon()
+        {
+            pending = EV_NONE;
+            updateMax = true;
+            cached_mat = -1;
+            hist_steps = 0;
+            forced_wc = 0.0f;
+        }
+    };
+
+    // Loads photon + stream state from the pre-generated queue.
+    __device__ __forceinline__ void take_queued(Lane& s, const PhotonQueue& q, uint64_t i)
+    {
+        const float4 pe = __ldg(q.pos_energy + i);
+        const float4 dw = __ldg(q.dir_weight + i);
+        const uint4 rs = __ldg(q.rng + i);
+        s.ph = Photon { pe.x, pe.y, pe.z, dw.x, dw.y, dw.z, pe.w, dw.w };
+        s.rng.s0 = rs.x;
+        s.rng.s1 = rs.y;
+        s.rng.s2 = rs.z;
+        s.rng.s3 = rs.w;
+        s.alive = true;
+        s.start_photon();
+    }
+
+    // Samples history h of the job in place (Exposure::sampleParticle + transportParticleToWorld).
+    __device__ __forceinline__ void take_history(Lane& s, const TransportParams& p, uint64_t h)
+    {
+        s.rng.init(p.seed, h);
+        uint32_t ei;
+        if (p.uniform_hpe && p.total_histories <= 0xffffffffull)
+            ei = static_cast<uint32_t>(h) / static_cast<uint32_t>(p.uniform_hpe);
+        else
+            ei = p.uniform_hpe ? static_cast<uint32_t>(h / p.uniform_hpe) : find_exposure(p.source, h);
+        DevExposure ex;
+        load_exposure(p.source.exposures + ei, ex);
+        sample_particle(p.source, ex, s.rng, s.ph);
+        ++s.histories;
+        s.alive = transport_to_world(p.world, s.ph);
+        s.start_photon();
+    }
+
+    // One iteration of the warp-synchronous loop for every lane of the warp: a
+    // Woodcock step for lanes without a pending interaction (transport.hpp:650-699),
+    // the per-type interaction passes once enough lanes wait (transport.hpp:523-638),
+    // Russian roulette and scoring.  Must be called by all 32 lanes.
+    template <int MODEL, bool PALETTE>
+    __device__ __forceinline__ void advance(Lane& s, const TransportParams& p, const float* L, const PaletteEntry* pal,
+        bool drain, int interact_t)
+    {
+        const LutMeta& m = p.lut_meta;
+        const WorldParams& w = p.world;
+        bool do_score = false;
+        float deposit = 0.0f; // energy imparted x weight to score
+        bool check_roulette = false;
+
+        if (s.alive && s.pending == EV_NONE) {
+            if (s.updateMax) {
+                s.logE = __log10f(s.ph.energy);
+                s.seg = lut_segment(L, m, s.logE);
+                s.maxInv = lut_max_inverse(L, m, s.logE, s.seg);
+                s.updateMax = false;
+                s.cached_mat = -1;
+            }
+            const float step = -__logf(s.rng.uniform_open()) * s.maxInv * 10.0f; // cm -> mm
+            s.ph.px = fmaf(s.ph.dx, step, s.ph.px);
+            s.ph.py = fmaf(s.ph.dy, step, s.ph.py);
+            s.ph.pz = fmaf(s.ph.dz, step, s.ph.pz);
+            if (!inside(w, s.ph.px, s.ph.py, s.ph.pz)) {
+                s.alive = false;
+            } else if (++s.hist_steps > MAX_STEPS_PER_HISTORY) {
+                // bounded work per history: end it and report the overflow
+                ++s.overflows;
+                s.alive = false;
+            } else {
+                const uint32_t ix = min(static_cast<uint32_t>((s.ph.px - w.lo[0]) * w.inv_spacing[0]), w.dims[0] - 1);
+                const uint32_t iy = min(static_cast<uint32_t>((s.ph.py - w.lo[1]) * w.inv_spacing[1]), w.dims[1] - 1);
+                const uint32_t iz = min(static_cast<uint32_t>((s.ph.pz - w.lo[2]) * w.inv_spacing[2]), w.dims[2] - 1);
+                s.vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
+                float density;
+                int mat;
+                bool measured;
+                gather_voxel<PALETTE>(w, pal, s.vidx, density, mat, measured);
+                ++s.steps;
+                if (mat != s.cached_mat) {
+                    lut_attenuation(L, m, mat, s.logE, s.seg, s.att0, s.att1, s.att2);
+                    s.cached_mat = mat;
+                }
+                const float attTot = s.att0 + s.att1 + s.att2;
+                const float eventProb = attTot * density * s.maxInv;
+                if (!measured) {
+                    // naive sampling (computeInteractions): decide the event type now,
+                    // run it in the interaction pass
+                    if (s.rng.uniform() < eventProb) {
+                        const float r3 = s.rng.uniform() * attTot;
+                        s.pending = r3 < s.att0 ? EV_PHOTO : (r3 < s.att0 + s.att1 ? EV_COMPTON : EV_RAYLEIGH);
+                    } else {
+                        check_roulette = true;
+                    }
+                } else {
+                    // forced photoelectric scoring (computeInteractionsForced): score the forced
+                    // photoelectric share now; a real Compton or Rayleigh event goes through the
+                    // interaction passes and the weight correction (1 - wc) is applied after it
+                    const float photoProb = s.att0 / attTot;
+                    s.forced_wc = eventProb * photoProb;
+                    {
+                        Photon forced = s.ph;
+                        const float ef = photo_absorption<MODEL>(L, m, forced, mat, s.rng);
+                        deposit = (forced.energy < ENERGY_CUTOFF ? (ef + forced.energy) : ef) * forced.weight * s.forced_wc;
+                        do_score = true;
+                    }
+                    if (s.rng.uniform() < eventProb * (1.0f - photoProb)) {
+                        s.pending = s.rng.uniform() * (s.att1 + s.att2) < s.att1 ? EV_COMPTON : EV_RAYLEIGH;
+                    } else {
+                        s.ph.weight *= (1.0f - s.forced_wc);
+                        s.forced_wc = 0.0f;
+                        check_roulette = true;
+                    }
+                }
+            }
+        }
+        if (do_score) {
+            // the forced photoelectric deposit is scored before this lane's
+            // interaction pass can add a second deposit in the same iteration
+            if (isfinite(deposit)) {
+                score(p, s.vidx, deposit);
+                ++s.deposits;
+            } else {
+                ++s.overflows;
+                s.alive = false;
+                s.pending = EV_NONE;
+            }
+            do_score = false;
+        }
+
+        // ---- interaction passes, one converged pass per event type ---------------------
+        {
+            const unsigned waiting = __ballot_sync(FULL_MASK, s.pending != EV_NONE);
+            const unsigned can_step = __ballot_sync(FULL_MASK, s.alive && s.pending == EV_NONE);
+            if (waiting && (__popc(waiting) >= interact_t || can_step == 0u || drain)) {
+                const int mat = s.cached_mat;
+                if (__any_sync(FULL_MASK, s.pending == EV_PHOTO) && s.pending == EV_PHOTO) {
+                    const float e = photo_absorption<MODEL>(L, m, s.ph, mat, s.rng);
+                    do_score = true;
+                    if (s.ph.energy < ENERGY_CUTOFF) {
+                        deposit = (e + s.ph.energy) * s.ph.weight;
+                        s.ph.energy = 0.0f;
+                        s.alive = false;
+                    } else {
+                        deposit = e * s.ph.weight;
+                        s.updateMax = true;
+                    }
+                }
+                if (__any_sync(FULL_MASK, s.pending == EV_COMPTON) && s.pending == EV_COMPTON) {
+                    float e = 0.0f;
+                    if (!compton_scatter<MODEL>(L, m, s.ph, mat, s.rng, e)) {
+                        ++s.overflows;
+                        s.alive = false;
+                    } else {
+                        do_score = true;
+                        if (s.ph.energy < ENERGY_CUTOFF) {
+                            deposit = (e + s.ph.energy) * s.ph.weight;
+                            s.ph.energy = 0.0f;
+                            s.alive = false;
+                        } else {
+                            deposit = e * s.ph.weight;
+                            s.updateMax = true;
+                        }
+                    }
+                }
+                if (__any_sync(FULL_MASK, s.pending == EV_RAYLEIGH) && s.pending == EV_RAYLEIGH) {
+                    if (!rayleigh_scatter<MODEL>(L, m, s.ph, mat, s.rng)) {
+                        ++s.overflows;
+                        s.alive = false;
+                    }
+                }
+                if (s.pending != EV_NONE) {
+                    if (s.alive && s.forced_wc != 0.0f)
+                        s.ph.weight *= (1.0f - s.forced_wc);
+                    s.forced_wc = 0.0f;
+                    check_roulette = s.alive;
+                    s.pending = EV_NONE;
+                }
+            }
+        }
+        if (check_roulette) {
+            // Russian roulette (transport.hpp:684-694)
+            if (s.ph.energy * s.ph.weight < ROULETTE_THRESHOLD) {
+                if (s.rng.uniform() < ROULETTE_PROBABILITY)
+                    s.alive = false;
+                else
+                    s.ph.weight *= 1.0f / (1.0f - ROULETTE_PROBABILITY);
+            }
+        }
+        if (do_score && !isfinite(deposit)) {
+            // never let a non-finite value into the FP64 accumulators: end the
+            // history and report it through the overflow counter
+            do_score = false;
+            s.alive = false;
+            ++s.overflows;
+        }
+        // ---- scoring; the warp is converged here ----------------------------------------
+        if (p.tally_mode == 2) {
+            const unsigned scoring = __ballot_sync(FULL_MASK, do_score);
+            if (do_score)
+                score_aggregated(p, scoring, s.vidx, deposit);
+        } else if (do_score) {
+            score(p, s.vidx, deposit);
+        }
+        if (do_score)
+            ++s.deposits;
+    }
+
+    // Adds the warp's lane counters to a job's counters and clears them.
+    __device__ __forceinline__ void flush_counters(Lane& s, JobCounters* c)
+    {
+        unsigned long long v[4] = { s.steps, s.deposits, s.overflows, s.histories };
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1)
+                v[k] += __shfl_down_sync(FULL_MASK, v[k], off);
+        if ((threadIdx.x & 31) == 0) {
+            if (v[0])
+                atomicAdd(&c->steps, v[0]);
+            if (v[1])
+                atomicAdd(&c->deposits, v[1]);
+            if (v[2])
+                atomicAdd(&c->overflows, v[2]);
+            if (v[3])
+                atomicAdd(&c->histories_done, v[3]);
+        }
+        s.reset_counters();
+    }
+
+    // ---- single-job transport kernel ----------------------------------------------------
+    //
+    // Warp-synchronous loop.  Each iteration every lane with a live photon and no
+    // pending interaction takes one Woodcock step; a real event only records its
+    // type (photoelectric / Compton / Rayleigh).  The interactions are then run in
+    // one converged pass per type once enough lanes wait, and finished lanes are
+    // refilled together once enough are idle, so the expensive branches run with
+    // many lanes active instead of one or two.
     template <int MODEL, bool PALETTE>
     __global__ void __launch_bounds__(256, DXMC_MIN_BLOCKS_PER_SM) transport_kernel(const __grid_constant__ TransportParams p)
     {
@@ -496,308 +757,170 @@ namespace {
             pal = spal;
         }
         __syncthreads();
-        const LutMeta& m = p.lut_meta;
-        const WorldParams& w = p.world;
         const int lane = threadIdx.x & 31;
         const unsigned lanemask_lt = (1u << lane) - 1u;
         const int regen_t = p.regen_threshold;
         const int interact_t = p.interact_threshold;
         const bool use_queue = p.queue.pos_energy != nullptr;
-        const unsigned long long queue_total = use_queue ? p.counters->queue_count : 0ull;
+        const unsigned long long source_total = use_queue ? p.counters->queue_count : p.total_histories;
+        unsigned long long* source_head = use_queue ? &p.counters->next_photon : &p.counters->next_history;
 
-        Photon ph {};
-        Rng rng;
-        bool alive = false;
-        int pending = EV_NONE;
-        float maxInv = 0.0f, logE = 0.0f;
-        int seg = 0;
-        bool updateMax = true;
-        int cached_mat = -1;
-        uint32_t hist_steps = 0;
-        uint32_t lane_steps = 0, lane_deposits = 0, lane_overflows = 0, lane_histories = 0;
-        float att0 = 0.0f, att1 = 0.0f, att2 = 0.0f;
-        uint64_t vidx = 0;
-        float forced_wc = 0.0f; // weight correction waiting for a forced-voxel interaction pass
-
-        // warp-uniform pool of history ids [pool_next, pool_end)
+        Lane s {};
+        s.alive = false;
+        s.reset_counters();
+        // warp-uniform pool of ids (queue slots or history ids) [pool_next, pool_end)
         uint64_t pool_next = 0, pool_end = 0;
         bool exhausted = false;
 
         while (true) {
             // ---- refill idle lanes together ------------------------------------------------
-            if (use_queue) {
-                unsigned need = __ballot_sync(FULL_MASK, !alive && !exhausted);
-                const unsigned live = __ballot_sync(FULL_MASK, alive);
-                if (need && (__popc(need) >= regen_t || live == 0u)) {
-                    while (need && !exhausted) {
-                        if (pool_next >= pool_end) {
-                            unsigned long long base = 0;
-                            if (lane == 0) {
-                                const bool cancelled = p.cancel && *p.cancel;
-                                base = cancelled ? queue_total : atomicAdd(&p.counters->next_photon, (unsigned long long)WARP_POOL_CHUNK);
-                            }
-                            base = __shfl_sync(FULL_MASK, base, 0);
-                            if (base >= queue_total) {
-                                exhausted = true;
-                                break;
-                            }
-                            pool_next = base;
-                            pool_end = min(static_cast<uint64_t>(base + WARP_POOL_CHUNK), static_cast<uint64_t>(queue_total));
+            unsigned need = __ballot_sync(FULL_MASK, !s.alive && !exhausted);
+            const unsigned live = __ballot_sync(FULL_MASK, s.alive);
+            if (need && (__popc(need) >= regen_t || live == 0u)) {
+                while (need && !exhausted) {
+                    if (pool_next >= pool_end) {
+                        unsigned long long base = 0;
+                        if (lane == 0) {
+                            const bool cancelled = p.cancel && *p.cancel;
+                            base = cancelled ? source_total : atomicAdd(source_head, (unsigned long long)WARP_POOL_CHUNK);
                         }
-                        const uint64_t avail = pool_end - pool_next;
-                        const unsigned rank = __popc(need & lanemask_lt);
-                        const bool mine = ((need >> lane) & 1u) && rank < avail;
-                        const unsigned taken = __ballot_sync(FULL_MASK, mine);
-                        if (mine) {
-                            const uint64_t q = pool_next + rank;
-                            const float4 pe = __ldg(p.queue.pos_energy + q);
-                            const float4 dw = __ldg(p.queue.dir_weight + q);
-                            const uint4 rs = __ldg(p.queue.rng + q);
-                            ph = Photon { pe.x, pe.y, pe.z, dw.x, dw.y, dw.z, pe.w, dw.w };
-                            rng.s0 = rs.x;
-                            rng.s1 = rs.y;
-                            rng.s2 = rs.z;
-                            rng.s3 = rs.w;
-                            alive = true;
-                            pending = EV_NONE;
-                            updateMax = true;
-                            cached_mat = -1;
-                            hist_steps = 0;
+                        base = __shfl_sync(FULL_MASK, base, 0);
+                        if (base >= source_total) {
+                            exhausted = true;
+                            break;
                         }
-                        pool_next += __popc(taken);
-                        need &= ~taken;
+                        pool_next = base;
+                        pool_end = min(static_cast<uint64_t>(base + WARP_POOL_CHUNK), static_cast<uint64_t>(source_total));
                     }
-                }
-            } else {
-                unsigned need = __ballot_sync(FULL_MASK, !alive && !exhausted);
-                const unsigned live = __ballot_sync(FULL_MASK, alive);
-                if (need && (__popc(need) >= regen_t || live == 0u)) {
-                    while (need && !exhausted) {
-                        if (pool_next >= pool_end) {
-                            unsigned long long base = 0;
-                            if (lane == 0) {
-                                const bool cancelled = p.cancel && *p.cancel;
-                                base = cancelled ? static_cast<unsigned long long>(p.total_histories)
-                                                 : atomicAdd(&p.counters->next_history, (unsigned long long)WARP_POOL_CHUNK);
-                            }
-                            base = __shfl_sync(FULL_MASK, base, 0);
-                            if (base >= p.total_histories) {
-                                exhausted = true;
-                                break;
-                            }
-                            pool_next = base;
-                            pool_end = min(static_cast<uint64_t>(base + WARP_POOL_CHUNK), p.total_histories);
-                        }
-                        const uint64_t avail = pool_end - pool_next;
-                        const unsigned rank = __popc(need & lanemask_lt);
-                        const bool mine = ((need >> lane) & 1u) && rank < avail;
-                        const unsigned taken = __ballot_sync(FULL_MASK, mine);
-                        if (mine) {
-                            const uint64_t h = pool_next + rank;
-                            rng.init(p.seed, h);
-                            uint32_t ei;
-                            if (p.uniform_hpe && p.total_histories <= 0xffffffffull)
-                                ei = static_cast<uint32_t>(h) / static_cast<uint32_t>(p.uniform_hpe);
-                            else
-                                ei = p.uniform_hpe ? static_cast<uint32_t>(h / p.uniform_hpe) : find_exposure(p.source, h);
-                            DevExposure ex;
-                            load_exposure(p.source.exposures + ei, ex);
-                            sample_particle(p.source, ex, rng, ph);
-                            ++lane_histories;
-                            alive = transport_to_world(w, ph);
-                            pending = EV_NONE;
-                            updateMax = true;
-                            cached_mat = -1;
-                            hist_steps = 0;
-                        }
-                        pool_next += __popc(taken);
-                        need &= ~taken;
+                    const uint64_t avail = pool_end - pool_next;
+                    const unsigned rank = __popc(need & lanemask_lt);
+                    const bool mine = ((need >> lane) & 1u) && rank < avail;
+                    const unsigned taken = __ballot_sync(FULL_MASK, mine);
+                    if (mine) {
+                        if (use_queue)
+                            take_queued(s, p.queue, pool_next + rank);
+                        else
+                            take_history(s, p, pool_next + rank);
                     }
+                    pool_next += __popc(taken);
+                    need &= ~taken;
                 }
             }
-            const unsigned live = __ballot_sync(FULL_MASK, alive);
-            if (exhausted && live == 0u)
+            if (exhausted && __ballot_sync(FULL_MASK, s.alive) == 0u)
                 break;
+            advance<MODEL, PALETTE>(s, p, L, pal, exhausted, interact_t);
+        }
+        flush_counters(s, p.counters);
+    }
 
-            bool do_score = false;
-            float deposit = 0.0f; // energy imparted x weight to score
-            bool check_roulette = false;
+    // ---- batched transport kernel ------------------------------------------------------
+    //
+    // Many jobs (worlds, LUTs, sources, tallies of their own) in one persistent launch.
+    // Work items (job, first history, count) are taken from a device-side queue by whole
+    // warps; a warp keeps its current job's parameters in shared memory and switches to
+    // another job only once all its lanes have finished, so every lane of a warp always
+    // works on the same job.  LUTs and palettes are read through the L1 (__ldg) since the
+    // warps of one block may serve different jobs.  Each history keeps its own random
+    // stream, so a job's tallies do not depend on what else runs in the batch.
+    struct WorkItem {
+        uint32_t job;
+        uint32_t count;
+        uint64_t first;
+    };
 
-            // ---- one Woodcock step for lanes without a pending interaction (transport.hpp:650-699)
-            if (alive && pending == EV_NONE) {
-                if (updateMax) {
-                    logE = __log10f(ph.energy);
-                    seg = lut_segment(L, m, logE);
-                    maxInv = lut_max_inverse(L, m, logE, seg);
-                    updateMax = false;
-                    cached_mat = -1;
-                }
-                const float step = -__logf(rng.uniform_open()) * maxInv * 10.0f; // cm -> mm
-                ph.px = fmaf(ph.dx, step, ph.px);
-                ph.py = fmaf(ph.dy, step, ph.py);
-                ph.pz = fmaf(ph.dz, step, ph.pz);
-                if (!inside(w, ph.px, ph.py, ph.pz)) {
-                    alive = false;
-                } else if (++hist_steps > MAX_STEPS_PER_HISTORY) {
-                    // bounded work per history: end it and report the overflow
-                    ++lane_overflows;
-                    alive = false;
-                } else {
-                    const uint32_t ix = min(static_cast<uint32_t>((ph.px - w.lo[0]) * w.inv_spacing[0]), w.dims[0] - 1);
-                    const uint32_t iy = min(static_cast<uint32_t>((ph.py - w.lo[1]) * w.inv_spacing[1]), w.dims[1] - 1);
-                    const uint32_t iz = min(static_cast<uint32_t>((ph.pz - w.lo[2]) * w.inv_spacing[2]), w.dims[2] - 1);
-                    vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
-                    float density;
-                    int mat;
-                    bool measured;
-                    gather_voxel<PALETTE>(w, pal, vidx, density, mat, measured);
-                    ++lane_steps;
-                    if (mat != cached_mat) {
-                        lut_attenuation(L, m, mat, logE, seg, att0, att1, att2);
-                        cached_mat = mat;
-                    }
-                    const float attTot = att0 + att1 + att2;
-                    const float eventProb = attTot * density * maxInv;
-                    if (!measured) {
-                        // naive sampling (computeInteractions, transport.hpp:583-638): decide
-                        // the event type now, run it in the interaction pass
-                        if (rng.uniform() < eventProb) {
-                            const float r3 = rng.uniform() * attTot;
-                            pending = r3 < att0 ? EV_PHOTO : (r3 < att0 + att1 ? EV_COMPTON : EV_RAYLEIGH);
-                        } else {
-                            check_roulette = true;
-                        }
-                    } else {
-                        // forced photoelectric scoring (computeInteractionsForced, transport.hpp:523-581):
-                        // score the forced photoelectric share now; a real Compton or Rayleigh
-                        // event goes through the interaction passes and the weight correction
-                        // (1 - wc) is applied after it
-                        const float photoProb = att0 / attTot;
-                        forced_wc = eventProb * photoProb;
-                        {
-                            Photon forced = ph;
-                            const float ef = photo_absorption<MODEL>(L, m, forced, mat, rng);
-                            deposit = (forced.energy < ENERGY_CUTOFF ? (ef + forced.energy) : ef) * forced.weight * forced_wc;
-                            do_score = true;
-                        }
-                        if (rng.uniform() < eventProb * (1.0f - photoProb)) {
-                            pending = rng.uniform() * (att1 + att2) < att1 ? EV_COMPTON : EV_RAYLEIGH;
-                        } else {
-                            ph.weight *= (1.0f - forced_wc);
-                            forced_wc = 0.0f;
-                            check_roulette = true;
-                        }
-                    }
-                }
-            }
-            if (do_score) {
-                // the forced photoelectric deposit is scored before this lane's
-                // interaction pass can add a second deposit in the same iteration
-                if (isfinite(deposit)) {
-                    score(p, vidx, deposit);
-                    ++lane_deposits;
-                } else {
-                    ++lane_overflows;
-                    alive = false;
-                    pending = EV_NONE;
-                }
-                do_score = false;
-            }
+    struct BatchParams {
+        const TransportParams* jobs;
+        const WorkItem* items;
+        uint64_t n_items;
+        unsigned long long* next_item;
+        int regen_threshold;
+        int interact_threshold;
+    };
 
-            // ---- interaction passes, one converged pass per event type ---------------------
-            {
-                const unsigned waiting = __ballot_sync(FULL_MASK, pending != EV_NONE);
-                const unsigned can_step = __ballot_sync(FULL_MASK, alive && pending == EV_NONE);
-                if (waiting && (__popc(waiting) >= interact_t || can_step == 0u || exhausted)) {
-                    const int mat = cached_mat;
-                    if (__any_sync(FULL_MASK, pending == EV_PHOTO) && pending == EV_PHOTO) {
-                        const float e = photo_absorption<MODEL>(L, m, ph, mat, rng);
-                        do_score = true;
-                        if (ph.energy < ENERGY_CUTOFF) {
-                            deposit = (e + ph.energy) * ph.weight;
-                            ph.energy = 0.0f;
-                            alive = false;
-                        } else {
-                            deposit = e * ph.weight;
-                            updateMax = true;
-                        }
-                    }
-                    if (__any_sync(FULL_MASK, pending == EV_COMPTON) && pending == EV_COMPTON) {
-                        float e = 0.0f;
-                        if (!compton_scatter<MODEL>(L, m, ph, mat, rng, e)) {
-                            ++lane_overflows;
-                            alive = false;
-                        } else {
-                            do_score = true;
-                            if (ph.energy < ENERGY_CUTOFF) {
-                                deposit = (e + ph.energy) * ph.weight;
-                                ph.energy = 0.0f;
-                                alive = false;
-                            } else {
-                                deposit = e * ph.weight;
-                                updateMax = true;
+    constexpr int BATCH_WARPS = 8; // 256-thread blocks
+
+    template <int MODEL>
+    __global__ void __launch_bounds__(256, DXMC_MIN_BLOCKS_PER_SM) batch_transport_kernel(const __grid_constant__ BatchParams b)
+    {
+        __shared__ TransportParams sjob[BATCH_WARPS];
+        __shared__ PaletteEntry spal[BATCH_WARPS][PALETTE_MAX];
+        const int lane = threadIdx.x & 31;
+        const int warp = threadIdx.x >> 5;
+        const unsigned lanemask_lt = (1u << lane) - 1u;
+        TransportParams& p = sjob[warp];
+        PaletteEntry* pal = spal[warp];
+
+        Lane s {};
+        s.alive = false;
+        s.reset_counters();
+        int job = -1;
+        uint64_t pool_next = 0, pool_end = 0;
+        WorkItem next {};
+        bool have_next = false;
+        bool exhausted = false;
+
+        while (true) {
+            unsigned need = __ballot_sync(FULL_MASK, !s.alive && !exhausted);
+            const unsigned live = __ballot_sync(FULL_MASK, s.alive);
+            if (need && (__popc(need) >= b.regen_threshold || live == 0u)) {
+                while (need && !exhausted) {
+                    if (pool_next >= pool_end) {
+                        if (!have_next) {
+                            unsigned long long it = 0;
+                            if (lane == 0)
+                                it = atomicAdd(b.next_item, 1ull);
+                            it = __shfl_sync(FULL_MASK, it, 0);
+                            if (it >= b.n_items) {
+                                exhausted = true;
+                                break;
                             }
+                            next = b.items[it];
+                            have_next = true;
                         }
-                    }
-                    if (__any_sync(FULL_MASK, pending == EV_RAYLEIGH) && pending == EV_RAYLEIGH) {
-                        if (!rayleigh_scatter<MODEL>(L, m, ph, mat, rng)) {
-                            ++lane_overflows;
-                            alive = false;
+                        if (static_cast<int>(next.job) != job) {
+                            // switch jobs only when every lane is idle
+                            if (__ballot_sync(FULL_MASK, s.alive) != 0u)
+                                break;
+                            if (job >= 0)
+                                flush_counters(s, p.counters);
+                            job = static_cast<int>(next.job);
+                            __syncwarp();
+                            const int* src = reinterpret_cast<const int*>(b.jobs + job);
+                            int* dst = reinterpret_cast<int*>(&p);
+                            for (int k = lane; k < static_cast<int>(sizeof(TransportParams) / sizeof(int)); k += 32)
+                                dst[k] = __ldg(src + k);
+                            __syncwarp();
+                            const int np = p.world.palette_index ? p.world.palette_n : 0;
+                            for (int k = lane; k < PALETTE_MAX; k += 32)
+                                pal[k] = k < np ? p.world.palette[k] : PaletteEntry { 0.0f, 0u };
+                            __syncwarp();
                         }
+                        pool_next = next.first;
+                        pool_end = next.first + next.count;
+                        have_next = false;
                     }
-                    if (pending != EV_NONE) {
-                        if (alive && forced_wc != 0.0f)
-                            ph.weight *= (1.0f - forced_wc);
-                        forced_wc = 0.0f;
-                        check_roulette = alive;
-                        pending = EV_NONE;
-                    }
+                    const uint64_t avail = pool_end - pool_next;
+                    const unsigned rank = __popc(need & lanemask_lt);
+                    const bool mine = ((need >> lane) & 1u) && rank < avail;
+                    const unsigned taken = __ballot_sync(FULL_MASK, mine);
+                    if (mine)
+                        take_history(s, p, pool_next + rank);
+                    pool_next += __popc(taken);
+                    need &= ~taken;
                 }
             }
-            if (check_roulette) {
-                // Russian roulette (transport.hpp:684-694)
-                if (ph.energy * ph.weight < ROULETTE_THRESHOLD) {
-                    if (rng.uniform() < ROULETTE_PROBABILITY)
-                        alive = false;
-                    else
-                        ph.weight *= 1.0f / (1.0f - ROULETTE_PROBABILITY);
-                }
-            }
-            if (do_score && !isfinite(deposit)) {
-                // never let a non-finite value into the FP64 accumulators: end the
-                // history and report it through the overflow counter
-                do_score = false;
-                alive = false;
-                ++lane_overflows;
-            }
-            // ---- scoring; the warp is converged here ----------------------------------------
-            if (p.tally_mode == 2) {
-                const unsigned scoring = __ballot_sync(FULL_MASK, do_score);
-                if (do_score)
-                    score_aggregated(p, scoring, vidx, deposit);
-            } else if (do_score) {
-                score(p, vidx, deposit);
-            }
-            if (do_score)
-                ++lane_deposits;
+            const unsigned live2 = __ballot_sync(FULL_MASK, s.alive);
+            if (exhausted && live2 == 0u)
+                break;
+            if (live2 == 0u)
+                continue; // waiting to switch jobs with nothing in flight: refill again
+            if (p.world.palette_index)
+                advance<MODEL, true>(s, p, p.lut, pal, exhausted || have_next, b.interact_threshold);
+            else
+                advance<MODEL, false>(s, p, p.lut, pal, exhausted || have_next, b.interact_threshold);
         }
-
-        // ---- per-warp counter flush ------------------------------------------------------
-        unsigned long long my_steps = lane_steps, my_deposits = lane_deposits, my_overflows = lane_overflows, my_histories = lane_histories;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            my_steps += __shfl_down_sync(FULL_MASK, my_steps, off);
-            my_deposits += __shfl_down_sync(FULL_MASK, my_deposits, off);
-            my_overflows += __shfl_down_sync(FULL_MASK, my_overflows, off);
-            my_histories += __shfl_down_sync(FULL_MASK, my_histories, off);
-        }
-        if (lane == 0) {
-            atomicAdd(&p.counters->steps, my_steps);
-            atomicAdd(&p.counters->deposits, my_deposits);
-            if (my_overflows)
-                atomicAdd(&p.counters->overflows, my_overflows);
-            atomicAdd(&p.counters->histories_done, my_histories);
-        }
+        if (job >= 0)
+            flush_counters(s, p.counters);
     }
 
     // ---- photon generation pass ---------------------------------------------------------
@@ -945,6 +1068,32 @@ static void* transport_function(int model, bool palette)
     if (palette)
         return model == 0 ? transport_entry<0, true>() : (model == 1 ? transport_entry<1, true>() : transport_entry<2, true>());
     return model == 0 ? transport_entry<0, false>() : (model == 1 ? transport_entry<1, false>() : transport_entry<2, false>());
+}
+
+cudaError_t launch_batch(const TransportParams* jobs, const void* items, uint64_t n_items, unsigned long long* next_item, int model,
+    int regen_threshold, int interact_threshold, int grid, cudaStream_t stream)
+{
+    BatchParams b { jobs, static_cast<const WorkItem*>(items), n_items, next_item, regen_threshold, interact_threshold };
+    if (model == 0)
+        batch_transport_kernel<0><<<grid, 256, 0, stream>>>(b);
+    else if (model == 1)
+        batch_transport_kernel<1><<<grid, 256, 0, stream>>>(b);
+    else
+        batch_transport_kernel<2><<<grid, 256, 0, stream>>>(b);
+    return cudaGetLastError();
+}
+
+int batch_max_blocks_per_sm(int model)
+{
+    int n = 0;
+    cudaError_t e;
+    if (model == 0)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_transport_kernel<0>, 256, 0);
+    else if (model == 1)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_transport_kernel<1>, 256, 0);
+    else
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_transport_kernel<2>, 256, 0);
+    return e == cudaSuccess ? n : 0;
 }
 
 cudaError_t launch_generate(const TransportParams& p, uint64_t first, uint64_t count, int grid, cudaStream_t stream)

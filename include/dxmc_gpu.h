@@ -262,6 +262,26 @@ int dxmc_gpu_job_result(dxmc_job* job, int output_mode, double calibration,
     double* dose, double* variance, uint32_t* n_events, dxmc_job_stats* stats);
 void dxmc_gpu_job_free(dxmc_job* job);
 
+/* ---- batches: many jobs in one persistent launch ---------------------------- */
+/* No counterpart in the reference (which runs one source at a time).  Every
+ * job keeps its own world, LUT, source tables and tallies; the jobs are cut
+ * into work items on a device-side queue that one persistent kernel launch
+ * (per correction model) drains.  A job's tallies are the same whether it runs
+ * alone or in a batch (each history has its own random stream). */
+typedef struct dxmc_batch dxmc_batch;
+typedef struct dxmc_batch_entry {
+    dxmc_world* world;
+    dxmc_lut* lut;
+    const dxmc_job_desc* job;
+} dxmc_batch_entry;
+int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, int n_entries, dxmc_batch** out);
+int dxmc_gpu_batch_wait(dxmc_batch* batch, int64_t timeout_ms);
+/* Job handle of entry `index`, for dxmc_gpu_job_result; owned by the batch. */
+int dxmc_gpu_batch_job(dxmc_batch* batch, int index, dxmc_job** job);
+/* Device time of the batch's kernels (ms). */
+double dxmc_gpu_batch_kernel_ms(dxmc_batch* batch);
+void dxmc_gpu_batch_free(dxmc_batch* batch);
+
 /* ---- transport without allocation ------------------------------------------ */
 /* No counterpart in the reference.  Runs the same transport as
  * dxmc_gpu_job_submit + dxmc_gpu_job_result(DXMC_OUTPUT_RAW) for callers that
