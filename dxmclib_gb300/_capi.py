@@ -132,6 +132,14 @@ class BatchEntry(C.Structure):
     _fields_ = [("world", VP), ("lut", VP), ("job", C.POINTER(JobDesc))]
 
 
+BATCH_AUTO, BATCH_CONCURRENT, BATCH_PERSISTENT = 0, 1, 2
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("chains", C.c_int32), ("regen_threshold", C.c_int32),
+                ("interact_threshold", C.c_int32), ("item_histories", C.c_int32), ("pad", C.c_int32)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "dxmc_gpu_abi_version": (C.c_int, []),
@@ -162,7 +170,7 @@ SIGNATURES = {
     "dxmc_gpu_job_result": (C.c_int, [VP, C.c_int, D, DP, DP, U32P, C.POINTER(JobStats)]),
     "dxmc_gpu_job_free": (None, [VP]),
     "dxmc_gpu_probe_lut": (C.c_int, [VP, VP, C.c_int, DP, C.c_int, DP, DP]),
-    "dxmc_gpu_batch_submit": (C.c_int, [VP, C.POINTER(BatchEntry), C.c_int, C.POINTER(VP)]),
+    "dxmc_gpu_batch_submit": (C.c_int, [VP, C.POINTER(BatchEntry), C.c_int, C.POINTER(BatchOptions), C.POINTER(VP)]),
     "dxmc_gpu_batch_wait": (C.c_int, [VP, C.c_int64]),
     "dxmc_gpu_batch_job": (C.c_int, [VP, C.c_int, C.POINTER(VP)]),
     "dxmc_gpu_batch_kernel_ms": (D, [VP]),

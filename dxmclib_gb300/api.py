@@ -11,9 +11,11 @@ and ``Transport()`` raises if the library or a device is unavailable.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import math
 import time
+import weakref
 from dataclasses import dataclass, field
 from typing import List, Optional, Sequence
 
@@ -722,8 +724,22 @@ class Result:
             return np.where(self.dose > 0, np.sqrt(np.maximum(self.variance, 0)) / self.dose, 0.0)
 
 
+_live_contexts: "weakref.WeakSet[GpuContext]" = weakref.WeakSet()
+
+
+@atexit.register
+def _close_contexts():
+    """Releases every device object before interpreter teardown, children first,
+    so that no world, LUT or job outlives the context it belongs to."""
+    for ctx in list(_live_contexts):
+        ctx.close()
+
+
 class GpuContext:
-    """Owns a dxmc_gpu_ctx; one per device per process is enough."""
+    """Owns a dxmc_gpu_ctx; one per device per process is enough.  Closing it
+    closes the batches, jobs, LUTs and worlds created on it first."""
+
+    _CLOSE_ORDER = ("Batch", "Job", "DeviceLut", "DeviceWorld")
 
     def __init__(self, device: int = 0, block_size: int = 0, blocks_per_sm: int = 0, tally_mode: int = A.TALLY_F64,
                  memory_budget: int = 0, regen_threshold: int = 0, interact_threshold: int = 0,
@@ -732,10 +748,20 @@ class GpuContext:
         opts = A.GpuOptions(device, block_size, blocks_per_sm, tally_mode, memory_budget, regen_threshold,
                             interact_threshold, queue_log2_chunk, 0)
         self.handle = C.c_void_p()
+        self._children = weakref.WeakSet()
         A.check(self.lib.dxmc_gpu_ctx_create(C.byref(opts), C.byref(self.handle)), None, "dxmc_gpu_ctx_create")
+        _live_contexts.add(self)
+
+    def _register(self, obj):
+        self._children.add(obj)
 
     def close(self):
         if self.handle:
+            children = list(self._children)
+            for kind in self._CLOSE_ORDER:
+                for obj in children:
+                    if type(obj).__name__ == kind:
+                        obj.close()
             self.lib.dxmc_gpu_ctx_destroy(self.handle)
             self.handle = C.c_void_p()
 
@@ -767,6 +793,7 @@ class DeviceWorld:
         d.layout = int(layout)
         self.handle = C.c_void_p()
         A.check(ctx.lib.dxmc_gpu_world_upload(ctx.handle, C.byref(d), C.byref(self.handle)), ctx.handle, "dxmc_gpu_world_upload")
+        ctx._register(self)
 
     def max_density(self) -> np.ndarray:
         n = len(self.world.materialMap())
@@ -776,9 +803,9 @@ class DeviceWorld:
         return out
 
     def close(self):
-        if self.handle:
+        if self.handle and self.ctx.handle:
             self.ctx.lib.dxmc_gpu_world_free(self.handle)
-            self.handle = C.c_void_p()
+        self.handle = C.c_void_p()
 
     def __del__(self):
         try:
@@ -877,6 +904,7 @@ class DeviceLut:
         self.ctx = ctx
         self.handle = C.c_void_p()
         A.check(ctx.lib.dxmc_gpu_lut_upload(ctx.handle, blob.handle, C.byref(self.handle)), ctx.handle, "dxmc_gpu_lut_upload")
+        ctx._register(self)
 
     def probe(self, material: int, energies) -> tuple:
         e = np.ascontiguousarray(energies, np.float64)
@@ -896,9 +924,9 @@ class DeviceLut:
         return c, e, d
 
     def close(self):
-        if self.handle:
+        if self.handle and self.ctx.handle:
             self.ctx.lib.dxmc_gpu_lut_free(self.handle)
-            self.handle = C.c_void_p()
+        self.handle = C.c_void_p()
 
     def __del__(self):
         try:
@@ -920,6 +948,7 @@ class Job:
         self.handle = C.c_void_p()
         A.check(ctx.lib.dxmc_gpu_job_submit(ctx.handle, dworld.handle, dlut.handle, C.byref(jd), C.byref(self.handle)),
                 ctx.handle, "dxmc_gpu_job_submit")
+        ctx._register(self)
 
     @classmethod
     def _member(cls, ctx: GpuContext, dworld: DeviceWorld, handle: C.c_void_p) -> "Job":
@@ -987,7 +1016,7 @@ class Job:
         return dose, var, nev, stats
 
     def close(self):
-        if self.handle and self._owned:
+        if self.handle and self._owned and self.ctx.handle:
             self.ctx.lib.dxmc_gpu_job_free(self.handle)
         self.handle = C.c_void_p()
 
@@ -1011,20 +1040,27 @@ class BatchEntry:
 class Batch:
     """Many jobs in one persistent launch (dxmc_gpu_batch_*); ``jobs[i]`` gives entry i's results."""
 
-    def __init__(self, ctx: GpuContext, entries: Sequence[BatchEntry]):
+    CONCURRENT = A.BATCH_CONCURRENT
+    PERSISTENT = A.BATCH_PERSISTENT
+
+    def __init__(self, ctx: GpuContext, entries: Sequence[BatchEntry], mode: int = A.BATCH_AUTO, chains: int = 0,
+                 regen_threshold: int = 0, interact_threshold: int = 0, item_histories: int = 0):
         self.ctx = ctx
+        self._entries = list(entries)  # worlds and LUTs stay referenced while the batch runs
         self._descs = []
         arr = (A.BatchEntry * len(entries))()
         for i, e in enumerate(entries):
-            holder = Job.__new__(Job)
+            holder = Job._member(ctx, e.dworld, C.c_void_p())
             jd = holder._describe(*e.args)
             self._descs.append(holder)
             arr[i].world = e.dworld.handle
             arr[i].lut = e.dlut.handle
             arr[i].job = C.pointer(jd)
         self.handle = C.c_void_p()
-        A.check(ctx.lib.dxmc_gpu_batch_submit(ctx.handle, arr, len(entries), C.byref(self.handle)), ctx.handle,
-                "dxmc_gpu_batch_submit")
+        opts = A.BatchOptions(int(mode), int(chains), int(regen_threshold), int(interact_threshold), int(item_histories), 0)
+        A.check(ctx.lib.dxmc_gpu_batch_submit(ctx.handle, arr, len(entries), C.byref(opts), C.byref(self.handle)),
+                ctx.handle, "dxmc_gpu_batch_submit")
+        ctx._register(self)
         self.jobs = []
         for i, e in enumerate(entries):
             h = C.c_void_p()
@@ -1041,8 +1077,9 @@ class Batch:
         if self.handle:
             for j in self.jobs:
                 j.handle = C.c_void_p()
-            self.ctx.lib.dxmc_gpu_batch_free(self.handle)
-            self.handle = C.c_void_p()
+            if self.ctx.handle:
+                self.ctx.lib.dxmc_gpu_batch_free(self.handle)
+        self.handle = C.c_void_p()
 
     def __del__(self):
         try:

@@ -26,7 +26,10 @@ constexpr int DEFAULT_INTERACT_THRESHOLD = 6;
 constexpr int DEFAULT_QUEUE_REGEN_THRESHOLD = 4;  // photons taken from the pre-generated queue
 constexpr int DEFAULT_QUEUE_INTERACT_THRESHOLD = 8;
 
+struct BatchEngines;
+
 struct dxmc_gpu_ctx {
+    BatchEngines* engines = nullptr; // created by the first batch
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
@@ -218,6 +221,12 @@ size_t dev_palette_table_bytes() { return PALETTE_TABLE * sizeof(unsigned long l
 
 extern "C" {
 
+namespace {
+void sync_ctx_streams(dxmc_gpu_ctx* ctx);
+void release_engines(dxmc_gpu_ctx* ctx);
+int wait_event(dxmc_gpu_ctx* ctx, cudaEvent_t ev, int64_t timeout_ms, const char* what);
+} // namespace
+
 int dxmc_gpu_device_count(void)
 {
     int n = 0;
@@ -268,7 +277,8 @@ void dxmc_gpu_ctx_destroy(dxmc_gpu_ctx* ctx)
     if (!ctx)
         return;
     cudaSetDevice(ctx->device);
-    cudaStreamSynchronize(ctx->stream);
+    sync_ctx_streams(ctx);
+    release_engines(ctx);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -486,7 +496,7 @@ void dxmc_gpu_world_free(dxmc_world* w)
         return;
     std::lock_guard<std::mutex> lock(w->ctx->mutex);
     cudaSetDevice(w->ctx->device);
-    cudaStreamSynchronize(w->ctx->stream);
+    sync_ctx_streams(w->ctx);
     cudaFree(w->voxels);
     if (w->palette_index)
         cudaFree(w->palette_index);
@@ -584,7 +594,7 @@ void dxmc_gpu_lut_free(dxmc_lut* lut)
         return;
     std::lock_guard<std::mutex> lock(lut->ctx->mutex);
     cudaSetDevice(lut->ctx->device);
-    cudaStreamSynchronize(lut->ctx->stream);
+    sync_ctx_streams(lut->ctx);
     cudaFree(lut->image);
     lut->ctx->in_use -= lut->bytes;
     delete lut;
@@ -622,8 +632,13 @@ namespace {
 // Validates a job, builds its host tables, allocates and clears its device
 // buffers on the context stream and fills its kernel parameters.  Batched jobs
 // get no photon queue.  Caller holds the context mutex.
-int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_job_desc* jd, bool batched, dxmc_job** out,
-    dev::TransportParams& p, uint64_t& chunk_out)
+// Photon queue of a job: its own buffer (single jobs), none (photons generated in
+// the persistent multi-job kernel) or a buffer shared by the jobs of one batch
+// chain, which run one after another on the chain's stream.
+enum class QueueMode { own, none, shared };
+
+int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_job_desc* jd, QueueMode qmode,
+    uint64_t shared_capacity, dxmc_job** out, dev::TransportParams& p, uint64_t& chunk_out)
 {
     *out = nullptr;
     if (world->ctx != ctx || lut->ctx != ctx)
@@ -736,8 +751,12 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     const uint64_t tally_bytes = tally_mode == 1 ? nv * 2 * sizeof(float) : nv * 2 * sizeof(double);
     // photon queue: chunks of 2^k histories, 48 bytes per queued photon
     const int log2_chunk = ctx->options.queue_log2_chunk == 0 ? 25 : ctx->options.queue_log2_chunk;
-    const uint64_t chunk = (log2_chunk < 0 || batched) ? 0 : std::min<uint64_t>(total, 1ull << std::min(log2_chunk, 34));
-    const uint64_t queue_bytes = chunk * 48;
+    uint64_t chunk = 0;
+    if (log2_chunk >= 0 && qmode == QueueMode::own)
+        chunk = std::min<uint64_t>(total, 1ull << std::min(log2_chunk, 34));
+    else if (log2_chunk >= 0 && qmode == QueueMode::shared)
+        chunk = std::min<uint64_t>(total, shared_capacity);
+    const uint64_t queue_bytes = qmode == QueueMode::own ? chunk * 48 : 0;
     const uint64_t job_bytes = tally_bytes + nv * sizeof(uint32_t) + table_bytes + sizeof(dev::JobCounters) + queue_bytes;
     if (ctx->in_use + job_bytes > ctx->budget)
         return fail(ctx, DXMC_ERR_OOM, "job exceeds the device memory budget");
@@ -838,7 +857,7 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
             p.uniform_hpe = jd->exposures[0].n_histories;
     }
     {
-        const bool queued = ctx->options.queue_log2_chunk >= 0 && !batched;
+        const bool queued = chunk > 0;
         p.regen_threshold = ctx->options.regen_threshold > 0 ? std::min(ctx->options.regen_threshold, 32)
                                                            : (queued ? DEFAULT_QUEUE_REGEN_THRESHOLD : DEFAULT_REGEN_THRESHOLD);
         p.interact_threshold = ctx->options.interact_threshold > 0 ? std::min(ctx->options.interact_threshold, 32)
@@ -865,8 +884,71 @@ void discard_job(dxmc_job* j)
     delete j;
 }
 
-} // namespace
+struct LaunchPlan {
+    int grid = 0, block = 256, gen_grid = 0;
+    size_t smem = 0;
+};
 
+// Grid, block and shared memory of a job's transport kernel; sets p.lut_in_smem.
+LaunchPlan plan_launch(dxmc_gpu_ctx* ctx, const dxmc_world* world, const dxmc_lut* lut, int model, dev::TransportParams& p)
+{
+    LaunchPlan L;
+    const size_t lut_bytes = static_cast<size_t>(lut->meta.total_floats) * sizeof(float);
+    const size_t smem_limit = std::min<size_t>(ctx->max_smem_optin, 96 * 1024);
+    p.lut_in_smem = lut_bytes <= smem_limit ? 1 : 0;
+    const bool palette = world->palette_index != nullptr;
+    L.smem = dev::transport_smem_bytes(lut_bytes, p.lut_in_smem != 0, palette);
+    L.block = ctx->options.block_size > 0 ? ctx->options.block_size : 256;
+    // also sets the kernel's dynamic shared-memory limit for this launch
+    const int occ = dev::transport_max_blocks_per_sm(model, palette, L.block, L.smem);
+    int per_sm = ctx->options.blocks_per_sm > 0 ? ctx->options.blocks_per_sm : occ;
+    if (per_sm <= 0)
+        per_sm = 1;
+    L.grid = ctx->sm_count * per_sm;
+    L.gen_grid = ctx->sm_count * 8;
+    return L;
+}
+
+cudaError_t record(cudaEvent_t ev, cudaStream_t s, bool capturing)
+{
+    return capturing ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal) : cudaEventRecord(ev, s);
+}
+
+// Queues one job on stream s: the transport kernel alone (photons generated in
+// the kernel) or, per chunk of the photon queue, a counter reset, the generation
+// pass and the transport kernel.  Records the job's start and stop events.
+cudaError_t enqueue_job(dxmc_job* j, dev::TransportParams p, int model, uint64_t chunk, unsigned char* queue,
+    const LaunchPlan& L, cudaStream_t s, bool capturing)
+{
+    cudaError_t e = cudaSuccess;
+    if (chunk == 0) {
+        e = record(j->start, s, capturing);
+        if (e == cudaSuccess)
+            e = dev::launch_transport(p, model, L.grid, L.block, L.smem, s);
+    } else {
+        p.queue.pos_energy = reinterpret_cast<float4*>(queue);
+        p.queue.dir_weight = reinterpret_cast<float4*>(queue + chunk * 16);
+        p.queue.rng = reinterpret_cast<uint4*>(queue + chunk * 32);
+        p.queue.capacity = chunk;
+        const uint64_t total = j->histories;
+        for (uint64_t first = 0; first < total && e == cudaSuccess; first += chunk) {
+            const uint64_t count = std::min(chunk, total - first);
+            // queue_count and next_photon restart for every chunk
+            e = cudaMemsetAsync(&j->counters->queue_count, 0, 2 * sizeof(unsigned long long), s);
+            if (e == cudaSuccess)
+                e = dev::launch_generate(p, first, count, L.gen_grid, s);
+            if (e == cudaSuccess && first == 0)
+                e = record(j->start, s, capturing);
+            if (e == cudaSuccess)
+                e = dev::launch_transport(p, model, L.grid, L.block, L.smem, s);
+        }
+    }
+    if (e == cudaSuccess)
+        e = record(j->stop, s, capturing);
+    return e;
+}
+
+} // namespace
 
 int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_job_desc* jd, dxmc_job** out)
 {
@@ -876,86 +958,261 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
     dev::TransportParams p {};
     uint64_t chunk = 0;
     dxmc_job* j = nullptr;
-    const int rc = prepare_job(ctx, world, lut, jd, false, &j, p, chunk);
+    const int rc = prepare_job(ctx, world, lut, jd, QueueMode::own, 0, &j, p, chunk);
     if (rc != DXMC_OK)
         return rc;
-    const uint64_t total = j->histories;
-    const uint64_t job_bytes = j->bytes;
-    cudaStream_t s = ctx->stream;
-    cudaError_t e = cudaSuccess;
-    const size_t lut_bytes = static_cast<size_t>(lut->meta.total_floats) * sizeof(float);
-    const size_t smem_limit = std::min<size_t>(ctx->max_smem_optin, 96 * 1024);
-    p.lut_in_smem = lut_bytes <= smem_limit ? 1 : 0;
-    const bool palette = world->palette_index != nullptr;
-    const size_t smem = dev::transport_smem_bytes(lut_bytes, p.lut_in_smem != 0, palette);
-    const int block = ctx->options.block_size > 0 ? ctx->options.block_size : 256;
-    // also sets the kernel's dynamic shared-memory limit for this launch
-    const int occ = dev::transport_max_blocks_per_sm(jd->model, palette, block, smem);
-    int per_sm = ctx->options.blocks_per_sm > 0 ? ctx->options.blocks_per_sm : occ;
-    if (per_sm <= 0)
-        per_sm = 1;
-    const int grid = ctx->sm_count * per_sm;
-    if (chunk == 0) {
-        // photons generated inside the transport kernel
-        e = cudaEventRecord(j->start, s);
-        if (e == cudaSuccess)
-            e = dev::launch_transport(p, jd->model, grid, block, smem, s);
-        if (e == cudaSuccess)
-            e = cudaEventRecord(j->stop, s);
-    } else {
-        p.queue.pos_energy = reinterpret_cast<float4*>(j->queue);
-        p.queue.dir_weight = reinterpret_cast<float4*>(j->queue + chunk * 16);
-        p.queue.rng = reinterpret_cast<uint4*>(j->queue + chunk * 32);
-        p.queue.capacity = chunk;
-        const int gen_grid = ctx->sm_count * 8;
-        for (uint64_t first = 0; first < total && e == cudaSuccess; first += chunk) {
-            const uint64_t count = std::min(chunk, total - first);
-            // queue_count and next_photon restart for every chunk
-            e = cudaMemsetAsync(&j->counters->queue_count, 0, 2 * sizeof(unsigned long long), s);
-            if (e == cudaSuccess)
-                e = dev::launch_generate(p, first, count, gen_grid, s);
-            if (e == cudaSuccess && first == 0)
-                e = cudaEventRecord(j->start, s);
-            if (e == cudaSuccess)
-                e = dev::launch_transport(p, jd->model, grid, block, smem, s);
-        }
-        if (e == cudaSuccess)
-            e = cudaEventRecord(j->stop, s);
-    }
+    const LaunchPlan L = plan_launch(ctx, world, lut, jd->model, p);
+    const cudaError_t e = enqueue_job(j, p, jd->model, chunk, j->queue, L, ctx->stream, false);
     if (e != cudaSuccess) {
-        cudaStreamSynchronize(s);
+        cudaStreamSynchronize(ctx->stream);
         discard_job(j);
         return cuda_fail(ctx, e, "transport launch");
     }
-    ctx->in_use += job_bytes;
+    ctx->in_use += j->bytes;
     *out = j;
     return DXMC_OK;
 }
 
-struct dxmc_batch {
-    dxmc_gpu_ctx* ctx = nullptr;
-    std::vector<dxmc_job*> jobs;
+// ---- batches --------------------------------------------------------------------------
+//
+// Two ways to run a batch, both launched as one CUDA graph on an engine stream:
+//
+// * concurrent (default): every job keeps the single-job kernels (parameters in
+//   the kernel's constant bank, LUT staged in shared memory, photon queue).  The
+//   jobs are dealt longest-first onto a few chains; a chain's jobs run one after
+//   another and share one photon-queue buffer, the chains run side by side, so a
+//   job's blocks fill the SMs as the previous job of another chain drains.
+// * persistent: one multi-job kernel per correction model drains work items
+//   (job, first history, count) of all jobs from a device-side queue.  The graph
+//   is instantiated once per engine: three host-to-device copies (job
+//   parameters, items, control block) and the three kernels as independent
+//   nodes; only the copy sizes change between batches.
+//
+// The context has two engines used in turn, so a batch can be prepared and queued
+// while the previous one still runs.
+constexpr int MAX_BATCH_JOBS = 4096;
+constexpr uint64_t MAX_BATCH_ITEMS = 1ull << 20;
+constexpr int MAX_CHAINS = 8;
+constexpr int DEFAULT_CHAINS = 2;
+
+struct BatchEngine {
+    bool ready = false;
+    cudaStream_t stream = nullptr;
     dev::TransportParams* d_params = nullptr;
     dev::BatchItem* d_items = nullptr;
-    unsigned long long* d_next = nullptr; // one item counter per model group
-    cudaEvent_t start = nullptr, stop = nullptr;
-    uint64_t bytes = 0;
+    dev::BatchControl* d_control = nullptr;
+    dev::TransportParams* h_params = nullptr; // pinned staging
+    dev::BatchItem* h_items = nullptr;
+    dev::BatchControl* h_control = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t copy_params = nullptr, copy_items = nullptr;
+    cudaEvent_t done = nullptr;   // staging may be rewritten once this has completed
+    cudaEvent_t inputs = nullptr; // orders the context stream's job preparation before the graph
+    dev::BatchParams kparams {};
+    // concurrent mode
+    cudaStream_t chain[MAX_CHAINS] {};
+    cudaEvent_t fork = nullptr, join[MAX_CHAINS] {};
+    unsigned char* queue[MAX_CHAINS] {}; // photon-queue buffer per chain (lazily allocated)
+    uint64_t queue_capacity = 0;         // photons per chain buffer
+    uint64_t bytes = 0;                  // device bytes held (budget)
 };
 
-int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, int n, dxmc_batch** out)
+struct BatchEngines {
+    BatchEngine e[2];
+    int next = 0;
+};
+
+namespace {
+
+BatchEngines* engines_of(dxmc_gpu_ctx* ctx, bool create)
+{
+    if (!ctx->engines && create)
+        ctx->engines = new (std::nothrow) BatchEngines;
+    return ctx->engines;
+}
+
+void release_engine(dxmc_gpu_ctx* ctx, BatchEngine& g)
+{
+    if (g.stream)
+        cudaStreamSynchronize(g.stream);
+    for (int c = 0; c < MAX_CHAINS; ++c) {
+        if (g.chain[c]) {
+            cudaStreamSynchronize(g.chain[c]);
+            cudaStreamDestroy(g.chain[c]);
+        }
+        if (g.join[c])
+            cudaEventDestroy(g.join[c]);
+        cudaFree(g.queue[c]);
+    }
+    if (g.fork)
+        cudaEventDestroy(g.fork);
+    if (g.exec)
+        cudaGraphExecDestroy(g.exec);
+    if (g.graph)
+        cudaGraphDestroy(g.graph);
+    cudaFree(g.d_params);
+    cudaFree(g.d_items);
+    cudaFree(g.d_control);
+    cudaFreeHost(g.h_params);
+    cudaFreeHost(g.h_items);
+    cudaFreeHost(g.h_control);
+    if (g.done)
+        cudaEventDestroy(g.done);
+    if (g.inputs)
+        cudaEventDestroy(g.inputs);
+    if (g.stream)
+        cudaStreamDestroy(g.stream);
+    ctx->in_use -= g.bytes;
+    g = BatchEngine {};
+}
+
+cudaError_t build_engine(dxmc_gpu_ctx* ctx, BatchEngine& g)
+{
+    cudaError_t e = cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&g.d_params, MAX_BATCH_JOBS * sizeof(dev::TransportParams));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&g.d_items, MAX_BATCH_ITEMS * sizeof(dev::BatchItem));
+    if (e == cudaSuccess)
+        e = cudaMalloc(&g.d_control, sizeof(dev::BatchControl));
+    if (e == cudaSuccess)
+        e = cudaHostAlloc(&g.h_params, MAX_BATCH_JOBS * sizeof(dev::TransportParams), cudaHostAllocDefault);
+    if (e == cudaSuccess)
+        e = cudaHostAlloc(&g.h_items, MAX_BATCH_ITEMS * sizeof(dev::BatchItem), cudaHostAllocDefault);
+    if (e == cudaSuccess)
+        e = cudaHostAlloc(&g.h_control, sizeof(dev::BatchControl), cudaHostAllocDefault);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&g.inputs, cudaEventDisableTiming);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&g.fork, cudaEventDisableTiming);
+    for (int c = 0; c < MAX_CHAINS && e == cudaSuccess; ++c) {
+        e = cudaStreamCreateWithFlags(&g.chain[c], cudaStreamNonBlocking);
+        if (e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&g.join[c], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess)
+        e = cudaGraphCreate(&g.graph, 0);
+    if (e != cudaSuccess)
+        return e;
+    g.bytes = MAX_BATCH_JOBS * sizeof(dev::TransportParams) + MAX_BATCH_ITEMS * sizeof(dev::BatchItem) + sizeof(dev::BatchControl);
+    ctx->in_use += g.bytes;
+    std::memset(g.h_control, 0, sizeof(dev::BatchControl));
+    // copies (sizes are updated per batch; instantiate with one job and one item)
+    cudaGraphNode_t copy_control = nullptr;
+    e = cudaGraphAddMemcpyNode1D(&g.copy_params, g.graph, nullptr, 0, g.d_params, g.h_params, sizeof(dev::TransportParams), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaGraphAddMemcpyNode1D(&g.copy_items, g.graph, nullptr, 0, g.d_items, g.h_items, sizeof(dev::BatchItem), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaGraphAddMemcpyNode1D(&copy_control, g.graph, nullptr, 0, g.d_control, g.h_control, sizeof(dev::BatchControl), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess)
+        return e;
+    g.kparams = dev::BatchParams { g.d_params, g.d_items, g.d_control };
+    const cudaGraphNode_t deps[3] = { g.copy_params, g.copy_items, copy_control };
+    for (int model = 0; model < 3 && e == cudaSuccess; ++model) {
+        cudaKernelNodeParams kp {};
+        kp.func = const_cast<void*>(dev::batch_kernel_function(model));
+        kp.gridDim = dim3(ctx->sm_count * std::max(1, dev::batch_max_blocks_per_sm(model)));
+        kp.blockDim = dim3(256);
+        kp.sharedMemBytes = 0;
+        void* args[1] = { &g.kparams };
+        kp.kernelParams = args;
+        cudaGraphNode_t node;
+        e = cudaGraphAddKernelNode(&node, g.graph, deps, 3, &kp);
+    }
+    if (e == cudaSuccess)
+        e = cudaGraphInstantiate(&g.exec, g.graph, 0);
+    if (e == cudaSuccess)
+        g.ready = true;
+    return e;
+}
+
+// Photon-queue buffers of the first `chains` chains, `capacity` photons each.
+int ensure_chain_queues(dxmc_gpu_ctx* ctx, BatchEngine& g, int chains, uint64_t capacity)
+{
+    if (g.queue_capacity < capacity) {
+        for (int c = 0; c < MAX_CHAINS; ++c) {
+            if (g.queue[c]) {
+                cudaFree(g.queue[c]);
+                g.queue[c] = nullptr;
+                g.bytes -= g.queue_capacity * 48;
+                ctx->in_use -= g.queue_capacity * 48;
+            }
+        }
+        g.queue_capacity = capacity;
+    }
+    for (int c = 0; c < chains; ++c) {
+        if (g.queue[c])
+            continue;
+        const uint64_t bytes = g.queue_capacity * 48;
+        if (ctx->in_use + bytes > ctx->budget)
+            return fail(ctx, DXMC_ERR_OOM, "batch photon queues exceed the device memory budget");
+        const cudaError_t e = cudaMalloc(&g.queue[c], bytes);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "batch photon queue");
+        g.bytes += bytes;
+        ctx->in_use += bytes;
+    }
+    return DXMC_OK;
+}
+
+} // namespace
+
+struct dxmc_batch {
+    dxmc_gpu_ctx* ctx = nullptr;
+    BatchEngine* engine = nullptr;
+    std::vector<dxmc_job*> jobs;
+    cudaGraphExec_t exec = nullptr; // concurrent mode: this batch's graph
+    cudaEvent_t start = nullptr, stop = nullptr;
+};
+
+int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, int n, const dxmc_batch_options* opt,
+    dxmc_batch** out)
 {
     if (!ctx || !entries || n <= 0 || !out)
         return DXMC_ERR_INVALID;
     *out = nullptr;
+    if (n > MAX_BATCH_JOBS)
+        return fail(ctx, DXMC_ERR_INVALID, "a batch holds at most " + std::to_string(MAX_BATCH_JOBS) + " jobs");
+    const int mode = opt ? opt->mode : DXMC_BATCH_AUTO;
+    if (mode < DXMC_BATCH_AUTO || mode > DXMC_BATCH_PERSISTENT)
+        return fail(ctx, DXMC_ERR_INVALID, "unknown batch mode");
+    const bool persistent = mode == DXMC_BATCH_PERSISTENT;
+    const int chains = std::clamp(opt && opt->chains > 0 ? opt->chains : DEFAULT_CHAINS, 1, MAX_CHAINS);
     std::lock_guard<std::mutex> lock(ctx->mutex);
     cudaSetDevice(ctx->device);
+    BatchEngines* engines = engines_of(ctx, true);
+    if (!engines)
+        return DXMC_ERR_OOM;
+    BatchEngine& g = engines->e[engines->next];
+    if (!g.ready) {
+        const cudaError_t e = build_engine(ctx, g);
+        if (e != cudaSuccess) {
+            release_engine(ctx, g);
+            return cuda_fail(ctx, e, "batch engine");
+        }
+    }
+    // the engine's staging buffers and chain queues are free once its previous batch has finished
+    if (cudaEventSynchronize(g.done) != cudaSuccess)
+        return fail(ctx, DXMC_ERR_DEVICE, "previous batch of the engine failed");
+    const int log2_chunk = ctx->options.queue_log2_chunk == 0 ? 25 : ctx->options.queue_log2_chunk;
+    if (!persistent && log2_chunk >= 0) {
+        const int rc = ensure_chain_queues(ctx, g, chains, 1ull << std::min(log2_chunk, 34));
+        if (rc != DXMC_OK)
+            return rc;
+    }
     auto* b = new (std::nothrow) dxmc_batch;
     if (!b)
         return DXMC_ERR_OOM;
     b->ctx = ctx;
+    b->engine = &g;
     cudaStream_t s = ctx->stream;
-    std::vector<dev::TransportParams> params(n);
     std::vector<int> models(n);
+    std::vector<uint64_t> chunks(n, 0);
+    std::vector<dev::TransportParams> params(persistent ? 0 : n);
+    std::vector<int> chain_of(n, 0);
     uint64_t all = 0;
     auto abort = [&](int rc) {
         cudaStreamSynchronize(s);
@@ -963,12 +1220,8 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
             ctx->in_use -= j->bytes;
             discard_job(j);
         }
-        if (b->d_params)
-            cudaFree(b->d_params);
-        if (b->d_items)
-            cudaFree(b->d_items);
-        if (b->d_next)
-            cudaFree(b->d_next);
+        if (b->exec)
+            cudaGraphExecDestroy(b->exec);
         if (b->start)
             cudaEventDestroy(b->start);
         if (b->stop)
@@ -981,8 +1234,8 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
         if (!en.world || !en.lut || !en.job)
             return abort(fail(ctx, DXMC_ERR_INVALID, "batch entry " + std::to_string(i) + " is incomplete"));
         dxmc_job* j = nullptr;
-        uint64_t chunk = 0;
-        const int rc = prepare_job(ctx, en.world, en.lut, en.job, true, &j, params[i], chunk);
+        const int rc = persistent ? prepare_job(ctx, en.world, en.lut, en.job, QueueMode::none, 0, &j, g.h_params[i], chunks[i])
+                                  : prepare_job(ctx, en.world, en.lut, en.job, QueueMode::shared, g.queue_capacity, &j, params[i], chunks[i]);
         if (rc != DXMC_OK)
             return abort(rc);
         ctx->in_use += j->bytes; // later entries see the earlier ones in the admission check
@@ -990,69 +1243,135 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
         models[i] = en.job->model;
         all += j->histories;
     }
-    // work items: about four per resident warp, 256 to 8192 histories each
-    const int per_sm = std::max(1, dev::batch_max_blocks_per_sm(1));
-    const uint64_t warps = static_cast<uint64_t>(ctx->sm_count) * per_sm * 8;
-    uint64_t item = std::clamp<uint64_t>(all / (warps * 4), 256, 8192);
-    item = (item + 31) / 32 * 32;
-    std::vector<dev::BatchItem> items;
-    std::vector<uint64_t> group_start(4, 0), group_count(4, 0);
-    for (int model = 0; model < 3; ++model) {
-        group_start[model] = items.size();
-        for (int i = 0; i < n; ++i) {
-            if (models[i] != model)
-                continue;
-            const uint64_t total = b->jobs[i]->histories;
-            for (uint64_t first = 0; first < total; first += item)
-                items.push_back(dev::BatchItem { static_cast<uint32_t>(i), static_cast<uint32_t>(std::min(item, total - first)), first });
-        }
-        group_count[model] = items.size() - group_start[model];
-    }
-    cudaError_t e = cudaMalloc(&b->d_params, n * sizeof(dev::TransportParams));
-    if (e == cudaSuccess)
-        e = cudaMalloc(&b->d_items, items.size() * sizeof(dev::BatchItem));
-    if (e == cudaSuccess)
-        e = cudaMalloc(&b->d_next, 4 * sizeof(unsigned long long));
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(b->d_params, params.data(), n * sizeof(dev::TransportParams), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(dev::BatchItem), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-        e = cudaMemsetAsync(b->d_next, 0, 4 * sizeof(unsigned long long), s);
-    if (e == cudaSuccess)
-        e = cudaEventCreate(&b->start);
+    cudaError_t e = cudaEventCreate(&b->start);
     if (e == cudaSuccess)
         e = cudaEventCreate(&b->stop);
+    // job preparation (allocations, clears, source tables) on the context stream comes first
     if (e == cudaSuccess)
-        e = cudaEventRecord(b->start, s);
-    for (auto* j : b->jobs) // every job's kernel time is the batch's
+        e = cudaEventRecord(g.inputs, s);
+    if (e == cudaSuccess)
+        e = cudaStreamWaitEvent(g.stream, g.inputs, 0);
+    if (e != cudaSuccess)
+        return abort(cuda_fail(ctx, e, "batch setup"));
+
+    const char* step = "batch launch";
+    if (persistent) {
+        // work items: about four per resident warp, 256 to 8192 histories each unless set
+        const int per_sm = std::max(1, dev::batch_max_blocks_per_sm(1));
+        const uint64_t warps = static_cast<uint64_t>(ctx->sm_count) * per_sm * 8;
+        uint64_t item = opt && opt->item_histories > 0 ? static_cast<uint64_t>(opt->item_histories)
+                                                       : std::clamp<uint64_t>(all / (warps * 4), 256, 8192);
+        item = std::max<uint64_t>(32, (item + 31) / 32 * 32);
+        auto count_items = [&](uint64_t it) {
+            uint64_t c = 0;
+            for (auto* j : b->jobs)
+                c += (j->histories + it - 1) / it;
+            return c;
+        };
+        while (count_items(item) > MAX_BATCH_ITEMS)
+            item *= 2;
+        if (item > 0xffffffffull)
+            return abort(fail(ctx, DXMC_ERR_INVALID, "batch too large"));
+        dev::BatchControl& c = *g.h_control;
+        std::memset(&c, 0, sizeof(c));
+        uint64_t n_items = 0;
+        for (int model = 0; model < 3; ++model) {
+            c.item_base[model] = n_items;
+            for (int i = 0; i < n; ++i) {
+                if (models[i] != model)
+                    continue;
+                const uint64_t total = b->jobs[i]->histories;
+                for (uint64_t first = 0; first < total; first += item)
+                    g.h_items[n_items++] = dev::BatchItem { static_cast<uint32_t>(i), static_cast<uint32_t>(std::min(item, total - first)), first };
+            }
+            c.n_items[model] = n_items - c.item_base[model];
+        }
+        const int regen = opt && opt->regen_threshold > 0 ? opt->regen_threshold
+                                                          : (ctx->options.regen_threshold > 0 ? ctx->options.regen_threshold : DEFAULT_REGEN_THRESHOLD);
+        const int inter = opt && opt->interact_threshold > 0 ? opt->interact_threshold
+                                                             : (ctx->options.interact_threshold > 0 ? ctx->options.interact_threshold : DEFAULT_INTERACT_THRESHOLD);
+        c.regen_threshold = std::clamp(regen, 1, 32);
+        c.interact_threshold = std::clamp(inter, 1, 32);
+        e = cudaGraphExecMemcpyNodeSetParams1D(g.exec, g.copy_params, g.d_params, g.h_params, n * sizeof(dev::TransportParams), cudaMemcpyHostToDevice);
         if (e == cudaSuccess)
-            e = cudaEventRecord(j->start, s);
-    for (int model = 0; model < 3 && e == cudaSuccess; ++model) {
-        if (!group_count[model])
-            continue;
-        const int grid = ctx->sm_count * std::max(1, dev::batch_max_blocks_per_sm(model));
-        const int regen = ctx->options.regen_threshold > 0 ? std::min(ctx->options.regen_threshold, 32) : DEFAULT_REGEN_THRESHOLD;
-        const int inter = ctx->options.interact_threshold > 0 ? std::min(ctx->options.interact_threshold, 32) : DEFAULT_INTERACT_THRESHOLD;
-        e = dev::launch_batch(b->d_params, b->d_items + group_start[model], group_count[model], b->d_next + model, model, regen, inter, grid, s);
+            e = cudaGraphExecMemcpyNodeSetParams1D(g.exec, g.copy_items, g.d_items, g.h_items, n_items * sizeof(dev::BatchItem), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(b->start, g.stream);
+        for (auto* j : b->jobs) // every job's kernel time is the batch's
+            if (e == cudaSuccess)
+                e = cudaEventRecord(j->start, g.stream);
+        if (e == cudaSuccess)
+            e = cudaGraphLaunch(g.exec, g.stream);
+        for (auto* j : b->jobs)
+            if (e == cudaSuccess)
+                e = cudaEventRecord(j->stop, g.stream);
+    } else {
+        // longest job first onto the chain with the least work
+        std::vector<int> order(n);
+        for (int i = 0; i < n; ++i)
+            order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->jobs[x]->histories > b->jobs[y]->histories; });
+        std::vector<uint64_t> load(chains, 0);
+        std::vector<std::vector<int>> lists(chains);
+        for (int i : order) {
+            const int c = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
+            load[c] += b->jobs[i]->histories;
+            lists[c].push_back(i);
+        }
+        std::vector<LaunchPlan> plans(n);
+        for (int i = 0; i < n; ++i) // occupancy queries and attributes stay outside the capture
+            plans[i] = plan_launch(ctx, entries[i].world, entries[i].lut, models[i], params[i]);
+        cudaGraph_t graph = nullptr;
+        step = "batch capture";
+        e = cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t ce = cudaEventRecord(g.fork, g.stream);
+            for (int c = 0; c < chains && ce == cudaSuccess; ++c) {
+                ce = cudaStreamWaitEvent(g.chain[c], g.fork, 0);
+                for (size_t k = 0; k < lists[c].size() && ce == cudaSuccess; ++k) {
+                    const int i = lists[c][k];
+                    ce = enqueue_job(b->jobs[i], params[i], models[i], chunks[i], g.queue[c], plans[i], g.chain[c], true);
+                }
+                if (ce == cudaSuccess)
+                    ce = cudaEventRecord(g.join[c], g.chain[c]);
+                if (ce == cudaSuccess)
+                    ce = cudaStreamWaitEvent(g.stream, g.join[c], 0);
+            }
+            e = cudaStreamEndCapture(g.stream, &graph);
+            if (ce != cudaSuccess)
+                e = ce;
+        }
+        if (e == cudaSuccess) {
+            step = "batch graph instantiation";
+            e = cudaGraphInstantiate(&b->exec, graph, 0);
+        }
+        if (graph)
+            cudaGraphDestroy(graph);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(b->start, g.stream);
+        if (e == cudaSuccess) {
+            step = "batch graph launch";
+            e = cudaGraphLaunch(b->exec, g.stream);
+        }
     }
     if (e == cudaSuccess)
-        e = cudaEventRecord(b->stop, s);
-    for (auto* j : b->jobs)
-        if (e == cudaSuccess)
-            e = cudaEventRecord(j->stop, s);
-    if (e != cudaSuccess)
-        return abort(cuda_fail(ctx, e, "batch launch"));
-    b->bytes = n * sizeof(dev::TransportParams) + items.size() * sizeof(dev::BatchItem);
+        e = cudaEventRecord(b->stop, g.stream);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(g.done, g.stream);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(g.stream);
+        return abort(cuda_fail(ctx, e, step));
+    }
+    engines->next ^= 1;
     *out = b;
     return DXMC_OK;
 }
 
 int dxmc_gpu_batch_wait(dxmc_batch* b, int64_t timeout_ms)
 {
-    if (!b || b->jobs.empty())
+    if (!b)
         return DXMC_ERR_INVALID;
-    return dxmc_gpu_job_wait(b->jobs.back(), timeout_ms);
+    return wait_event(b->ctx, b->stop, timeout_ms, "batch wait");
 }
 
 int dxmc_gpu_batch_job(dxmc_batch* b, int index, dxmc_job** job)
@@ -1077,39 +1396,71 @@ void dxmc_gpu_batch_free(dxmc_batch* b)
 {
     if (!b)
         return;
+    cudaSetDevice(b->ctx->device);
+    cudaEventSynchronize(b->stop);
     for (auto* j : b->jobs)
         dxmc_gpu_job_free(j);
-    std::lock_guard<std::mutex> lock(b->ctx->mutex);
-    cudaSetDevice(b->ctx->device);
-    cudaStreamSynchronize(b->ctx->stream);
-    cudaFree(b->d_params);
-    cudaFree(b->d_items);
-    cudaFree(b->d_next);
+    if (b->exec)
+        cudaGraphExecDestroy(b->exec);
     cudaEventDestroy(b->start);
     cudaEventDestroy(b->stop);
     delete b;
 }
 
+namespace {
+
+// Waits for the batch engines' streams as well as the context stream (before
+// freeing resources that a queued batch may still read).
+void sync_ctx_streams(dxmc_gpu_ctx* ctx)
+{
+    cudaStreamSynchronize(ctx->stream);
+    if (BatchEngines* en = engines_of(ctx, false))
+        for (auto& g : en->e)
+            if (g.stream)
+                cudaStreamSynchronize(g.stream);
+}
+
+void release_engines(dxmc_gpu_ctx* ctx)
+{
+    if (!ctx->engines)
+        return;
+    for (auto& g : ctx->engines->e)
+        release_engine(ctx, g);
+    delete ctx->engines;
+    ctx->engines = nullptr;
+}
+
+} // namespace
+
+namespace {
+
+// Polls an event until it completes or timeout_ms (< 0: no limit) has passed.
+int wait_event(dxmc_gpu_ctx* ctx, cudaEvent_t ev, int64_t timeout_ms, const char* what)
+{
+    cudaSetDevice(ctx->device);
+    const auto t0 = std::chrono::steady_clock::now();
+    while (true) {
+        const cudaError_t e = cudaEventQuery(ev);
+        if (e == cudaSuccess)
+            return DXMC_OK;
+        if (e != cudaErrorNotReady)
+            return cuda_fail(ctx, e, what);
+        if (timeout_ms >= 0) {
+            const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+            if (ms >= timeout_ms)
+                return fail(ctx, DXMC_ERR_TIMEOUT, std::string(what) + " timed out");
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(100));
+    }
+}
+
+} // namespace
+
 int dxmc_gpu_job_wait(dxmc_job* j, int64_t timeout_ms)
 {
     if (!j)
         return DXMC_ERR_INVALID;
-    dxmc_gpu_ctx* ctx = j->ctx;
-    cudaSetDevice(ctx->device);
-    const auto t0 = std::chrono::steady_clock::now();
-    while (true) {
-        const cudaError_t e = cudaEventQuery(j->stop);
-        if (e == cudaSuccess)
-            return DXMC_OK;
-        if (e != cudaErrorNotReady)
-            return cuda_fail(ctx, e, "job wait");
-        if (timeout_ms >= 0) {
-            const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
-            if (ms >= timeout_ms)
-                return fail(ctx, DXMC_ERR_TIMEOUT, "job wait timed out");
-        }
-        std::this_thread::sleep_for(std::chrono::microseconds(200));
-    }
+    return wait_event(j->ctx, j->stop, timeout_ms, "job wait");
 }
 
 int dxmc_gpu_job_cancel(dxmc_job* j)
@@ -1194,6 +1545,8 @@ void dxmc_gpu_job_free(dxmc_job* j)
     dxmc_gpu_ctx* ctx = j->ctx;
     std::lock_guard<std::mutex> lock(ctx->mutex);
     cudaSetDevice(ctx->device);
+    if (j->stop)
+        cudaEventSynchronize(j->stop); // a batched job runs on its engine's stream
     cudaStreamSynchronize(ctx->stream);
     free_job_device(j);
     cudaStreamSynchronize(ctx->stream);

@@ -87,15 +87,34 @@ struct TransportParams {
     int interact_threshold; // run the interaction passes once at least this many lanes wait (1..32)
 };
 
-// Launchers (defined in transport_kernels.cu).
 // Work item of the batched kernel: histories [first, first + count) of job `job`.
 struct BatchItem {
     uint32_t job;
     uint32_t count;
     uint64_t first;
 };
-cudaError_t launch_batch(const TransportParams* jobs, const void* items, uint64_t n_items, unsigned long long* next_item, int model,
-    int regen_threshold, int interact_threshold, int grid, cudaStream_t stream);
+
+// Per-batch control block in device memory, written by one host-to-device copy
+// before the batch kernels start: the kernels' own arguments never change, so
+// one instantiated CUDA graph serves every batch of an engine.
+struct BatchControl {
+    unsigned long long next_item[4]; // work-queue heads, one per correction model (start at zero)
+    uint64_t item_base[4];           // first item of each model in the item array
+    uint64_t n_items[4];             // items of each model
+    int regen_threshold;
+    int interact_threshold;
+    int pad[2];
+};
+
+struct BatchParams {
+    const TransportParams* jobs;
+    const BatchItem* items;
+    BatchControl* control;
+};
+
+// Launchers (defined in transport_kernels.cu).
+// Entry function of the batched kernel for a correction model (for graph kernel nodes).
+const void* batch_kernel_function(int model);
 int batch_max_blocks_per_sm(int model);
 // Samples histories [first, first + count) into p.queue (compacted: photons that
 // miss the world are counted but not queued).

@@ -9,6 +9,8 @@
 // device function names the reference lines it restates.
 #include "transport.cuh"
 
+#include <mutex>
+
 #include <algorithm>
 
 namespace dxmc_gb300::dev {
@@ -822,21 +824,6 @@ namespace {
     // works on the same job.  LUTs and palettes are read through the L1 (__ldg) since the
     // warps of one block may serve different jobs.  Each history keeps its own random
     // stream, so a job's tallies do not depend on what else runs in the batch.
-    struct WorkItem {
-        uint32_t job;
-        uint32_t count;
-        uint64_t first;
-    };
-
-    struct BatchParams {
-        const TransportParams* jobs;
-        const WorkItem* items;
-        uint64_t n_items;
-        unsigned long long* next_item;
-        int regen_threshold;
-        int interact_threshold;
-    };
-
     constexpr int BATCH_WARPS = 8; // 256-thread blocks
 
     template <int MODEL>
@@ -849,32 +836,38 @@ namespace {
         const unsigned lanemask_lt = (1u << lane) - 1u;
         TransportParams& p = sjob[warp];
         PaletteEntry* pal = spal[warp];
+        BatchControl* ctl = b.control;
+        const BatchItem* items = b.items + ctl->item_base[MODEL];
+        const uint64_t n_items = ctl->n_items[MODEL];
+        unsigned long long* next_item = &ctl->next_item[MODEL];
+        const int regen_t = ctl->regen_threshold;
+        const int interact_t = ctl->interact_threshold;
 
         Lane s {};
         s.alive = false;
         s.reset_counters();
         int job = -1;
         uint64_t pool_next = 0, pool_end = 0;
-        WorkItem next {};
+        BatchItem next {};
         bool have_next = false;
         bool exhausted = false;
 
         while (true) {
             unsigned need = __ballot_sync(FULL_MASK, !s.alive && !exhausted);
             const unsigned live = __ballot_sync(FULL_MASK, s.alive);
-            if (need && (__popc(need) >= b.regen_threshold || live == 0u)) {
+            if (need && (__popc(need) >= regen_t || live == 0u)) {
                 while (need && !exhausted) {
                     if (pool_next >= pool_end) {
                         if (!have_next) {
                             unsigned long long it = 0;
                             if (lane == 0)
-                                it = atomicAdd(b.next_item, 1ull);
+                                it = atomicAdd(next_item, 1ull);
                             it = __shfl_sync(FULL_MASK, it, 0);
-                            if (it >= b.n_items) {
+                            if (it >= n_items) {
                                 exhausted = true;
                                 break;
                             }
-                            next = b.items[it];
+                            next = items[it];
                             have_next = true;
                         }
                         if (static_cast<int>(next.job) != job) {
@@ -915,9 +908,9 @@ namespace {
             if (live2 == 0u)
                 continue; // waiting to switch jobs with nothing in flight: refill again
             if (p.world.palette_index)
-                advance<MODEL, true>(s, p, p.lut, pal, exhausted || have_next, b.interact_threshold);
+                advance<MODEL, true>(s, p, p.lut, pal, exhausted || have_next, interact_t);
             else
-                advance<MODEL, false>(s, p, p.lut, pal, exhausted || have_next, b.interact_threshold);
+                advance<MODEL, false>(s, p, p.lut, pal, exhausted || have_next, interact_t);
         }
         if (job >= 0)
             flush_counters(s, p.counters);
@@ -1070,17 +1063,13 @@ static void* transport_function(int model, bool palette)
     return model == 0 ? transport_entry<0, false>() : (model == 1 ? transport_entry<1, false>() : transport_entry<2, false>());
 }
 
-cudaError_t launch_batch(const TransportParams* jobs, const void* items, uint64_t n_items, unsigned long long* next_item, int model,
-    int regen_threshold, int interact_threshold, int grid, cudaStream_t stream)
+const void* batch_kernel_function(int model)
 {
-    BatchParams b { jobs, static_cast<const WorkItem*>(items), n_items, next_item, regen_threshold, interact_threshold };
     if (model == 0)
-        batch_transport_kernel<0><<<grid, 256, 0, stream>>>(b);
-    else if (model == 1)
-        batch_transport_kernel<1><<<grid, 256, 0, stream>>>(b);
-    else
-        batch_transport_kernel<2><<<grid, 256, 0, stream>>>(b);
-    return cudaGetLastError();
+        return reinterpret_cast<const void*>(&batch_transport_kernel<0>);
+    if (model == 1)
+        return reinterpret_cast<const void*>(&batch_transport_kernel<1>);
+    return reinterpret_cast<const void*>(&batch_transport_kernel<2>);
 }
 
 int batch_max_blocks_per_sm(int model)
@@ -1121,7 +1110,19 @@ cudaError_t launch_transport(const TransportParams& p, int model, int grid, int 
 int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem)
 {
     void* fn = transport_function(model, palette);
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    // The dynamic shared-memory limit is a property of the function, read when a
+    // launch (or a graph holding it) is made: it only ever grows, so launches
+    // queued or captured earlier with larger LUTs stay valid.
+    static std::mutex m;
+    static int limit[6] = {};
+    {
+        std::lock_guard<std::mutex> lock(m);
+        int& cur = limit[model * 2 + (palette ? 1 : 0)];
+        if (static_cast<int>(smem) > cur) {
+            if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) == cudaSuccess)
+                cur = static_cast<int>(smem);
+        }
+    }
     int n = 0;
     const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, block, smem);
     return e == cudaSuccess ? n : 0;

@@ -274,7 +274,26 @@ typedef struct dxmc_batch_entry {
     dxmc_lut* lut;
     const dxmc_job_desc* job;
 } dxmc_batch_entry;
-int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, int n_entries, dxmc_batch** out);
+enum {
+    DXMC_BATCH_AUTO = 0,       /* currently the concurrent mode */
+    DXMC_BATCH_CONCURRENT = 1, /* single-job kernels, jobs dealt onto parallel chains of one graph */
+    DXMC_BATCH_PERSISTENT = 2  /* one multi-job kernel per model over a device-side work queue */
+};
+typedef struct dxmc_batch_options {
+    int32_t mode;               /* DXMC_BATCH_* */
+    int32_t chains;             /* concurrent mode: parallel chains (1..8); 0: 2 */
+    int32_t regen_threshold;    /* persistent mode: refill idle lanes once this many are idle (1..32); 0: default */
+    int32_t interact_threshold; /* persistent mode: interaction passes once this many lanes wait (1..32); 0: default */
+    int32_t item_histories;     /* persistent mode: histories per work item; 0: automatic (256..8192) */
+    int32_t pad;
+} dxmc_batch_options;
+/* Non-blocking.  At most 4096 jobs per batch; `options` may be NULL.  Batches
+ * alternate between two engines (streams + CUDA graphs), so two can be in
+ * flight; a third submit waits until the engine's previous batch has finished.
+ * The concurrent mode holds one photon-queue buffer (48 B x 2^queue_log2_chunk)
+ * per chain and engine. */
+int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, int n_entries,
+                          const dxmc_batch_options* options, dxmc_batch** out);
 int dxmc_gpu_batch_wait(dxmc_batch* batch, int64_t timeout_ms);
 /* Job handle of entry `index`, for dxmc_gpu_job_result; owned by the batch. */
 int dxmc_gpu_batch_job(dxmc_batch* batch, int index, dxmc_job** job);

@@ -1,6 +1,7 @@
 """GPU tests of the batched entry point (dxmc_gpu_batch_*): many jobs with
-worlds, LUTs, sources and correction models of their own drained by one
-persistent launch per model.
+worlds, LUTs, sources and correction models of their own run as one graph,
+either as single-job kernels on parallel chains (concurrent mode) or drained
+by one persistent multi-job kernel per model (persistent mode).
 
 Every history draws its own random stream (seeded from the job seed and the
 history id), so a job's tallies must not depend on whether it ran alone or in
@@ -73,15 +74,18 @@ def test_batch_matches_single_jobs(gpu_ctx, golden):
         job.close()
         assert alone[-1][0].sum() > 0
 
-    for rep in range(2):  # the batch runs twice: item order between warps differs, results must not
+    # each mode twice, in two job orders: work distribution differs between runs, results must not
+    runs = [(mode, rep) for mode in (dx.Batch.CONCURRENT, dx.Batch.PERSISTENT) for rep in range(2)]
+    for mode, rep in runs:
         order = list(range(len(entries)))[::-1] if rep else list(range(len(entries)))
-        batch = dx.Batch(ctx, [dx.BatchEntry(entries[i]["dworld"], entries[i]["dlut"], *_args(entries[i])) for i in order])
+        batch = dx.Batch(ctx, [dx.BatchEntry(entries[i]["dworld"], entries[i]["dlut"], *_args(entries[i])) for i in order],
+                         mode=mode, chains=2 + rep)
         assert batch.wait() == A.DXMC_OK
         assert batch.kernel_ms() > 0
         for pos, i in enumerate(order):
             e_b, e2_b, nev_b, st_b = batch.jobs[pos].result(A.OUTPUT_RAW)
             e_a, e2_a, nev_a, st_a = alone[i]
-            tag = f"rep {rep} job {i}"
+            tag = f"mode {mode} rep {rep} job {i}"
             assert st_b["histories"] == st_a["histories"] == int(np.sum(entries[i]["exposures"].n_histories)), tag
             assert st_b["steps"] == st_a["steps"] and st_b["deposits"] == st_a["deposits"], tag
             assert st_b["rejection_overflows"] == st_a["rejection_overflows"], tag
@@ -99,6 +103,6 @@ def test_batch_rejects_incomplete_entries(gpu_ctx):
     ctx = gpu_ctx
     arr = (A.BatchEntry * 1)()
     out = C.c_void_p()
-    rc = ctx.lib.dxmc_gpu_batch_submit(ctx.handle, arr, 1, C.byref(out))
+    rc = ctx.lib.dxmc_gpu_batch_submit(ctx.handle, arr, 1, None, C.byref(out))
     assert rc == A.DXMC_ERR_INVALID and not out.value
     assert b"incomplete" in ctx.lib.dxmc_gpu_last_error(ctx.handle)
