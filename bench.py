@@ -156,6 +156,101 @@ def cpu_sample(wl, lut_info, target_seconds: float, n_threads: int, model: int):
     return n, secs, f"{n_exp} of {len(ex)} exposures evenly spaced x {hpe} histories ({n} histories)"
 
 
+def serving_measurement(ctx, n_jobs: int, rates, chains: int, seed: int = 20261205) -> dict:
+    """Mixed-stream serving (pencil / DX / CT jobs, Poisson arrivals at each rate)
+    through DoseServer against the plain one-job-per-call path (Transport: upload
+    the world, run one job, copy the result back) on the same jobs and seeds."""
+    import queue as _queue
+    import threading
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300.serve import DoseServer
+    from dxmclib_gb300.workloads import serving_stream
+
+    probe = np.arange(0, 1 << 40, 4099)
+
+    def sample(dose):
+        return dose[probe[probe < dose.size]].copy(), float(np.sum(dose))
+
+    server = DoseServer(ctx, chains=chains)
+    base = serving_stream(n_jobs=n_jobs, rate_per_s=max(rates), seed=seed)
+    # warm-up: one small job per phantom makes every world and LUT resident
+    warm = {}
+    for j in base:
+        warm.setdefault(j.world_key, j)
+    for j in warm.values():
+        hpe = j.source.historiesPerExposure()
+        j.source.setHistoriesPerExposure(max(1, 100_000 // max(1, len(j.source.exposures(j.world.directionCosines())))))
+        server.submit(j.world, j.source, seed=1, world_key=j.world_key).result().release()
+        j.source.setHistoriesPerExposure(hpe)
+
+    def run_stream(rate):
+        # the same jobs at another arrival rate (the job draws do not depend on the rate)
+        arrivals = np.cumsum(np.random.default_rng(seed).exponential(1.0 / rate, len(base)))
+        server.reset_metrics()
+        served = [None] * len(base)
+        done_q = _queue.Queue()
+
+        def consumer():  # the client reads a sample of every result, then hands the buffers back
+            while True:
+                item = done_q.get()
+                if item is None:
+                    return
+                i, fut = item
+                r = fut.result()
+                served[i] = sample(r.dose)
+                r.release()
+
+        reader = threading.Thread(target=consumer, daemon=True)
+        reader.start()
+        t0 = time.perf_counter()
+        for i, j in enumerate(base):
+            delay = arrivals[i] - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            fut = server.submit(j.world, j.source, seed=j.seed, world_key=j.world_key)
+            fut.add_done_callback(lambda f, i=i: done_q.put((i, f)))
+        server.drain()
+        m = server.metrics()
+        done_q.put(None)
+        reader.join()
+        return m, served
+
+    sweep = []
+    served = None
+    for rate in sorted(rates):
+        m, served = run_stream(rate)
+        sweep.append({"rate_jobs_per_s": rate, "served_histories_per_s": m["histories_per_s"], "p50_ms": m["p50_ms"],
+                      "p99_ms": m["p99_ms"], "mean_queue_ms": m["mean_queue_ms"], "batches": m["batches"],
+                      "mean_batch_jobs": m["mean_batch_jobs"]})
+    server.close()
+
+    # plain: one Transport call per job, back to back (no arrival gaps)
+    tr = dx.Transport(ctx)
+    tr.setOutputMode(dx.Transport.EV_PER_HISTORY)
+    plain_s = 0.0
+    worst = 0.0
+    for i, j in enumerate(base):
+        tr.setSeed(j.seed)
+        t = time.perf_counter()
+        res = tr(j.world, j.source)
+        plain_s += time.perf_counter() - t
+        ps, ptot = sample(res.dose)
+        ss, stot = served[i]
+        scale = max(float(np.abs(ps).max()), 1e-300)
+        worst = max(worst, float(np.abs(ss - ps).max()) / scale, abs(stot - ptot) / max(abs(ptot), 1e-300))
+    hist = int(sum(j.histories for j in base))
+    kinds = {k: sum(1 for j in base if j.kind == k) for k in ("pencil", "dx", "ct")}
+    top = sweep[-1]
+    return {"workload": "mixed stream: 40% pencil 64^3, 40% DX 128^3-256^3, 20% CT 512x512x(100-400); "
+                        "histories log-uniform 1e6-1e8; seeded phantom pool",
+            "jobs": len(base), "kinds": kinds, "histories": hist, "chains": chains,
+            "rate_jobs_per_s": top["rate_jobs_per_s"],
+            "served_histories_per_s": top["served_histories_per_s"], "plain_histories_per_s": hist / plain_s,
+            "served_over_plain": top["served_histories_per_s"] / (hist / plain_s),
+            "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"], "sweep": sweep,
+            "max_rel_dose_diff_vs_plain": worst}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -173,6 +268,10 @@ def main():
     ap.add_argument("--block-size", type=int, default=0)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--queue-log2", type=int, default=0, help="photon queue chunk 2^n (0 = default, -1 = in-kernel generation)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served-vs-plain mixed-stream leg")
+    ap.add_argument("--serve-jobs", type=int, default=48)
+    ap.add_argument("--serve-rates", default="25,100,200", help="Poisson arrival rates of the mixed stream (jobs/s)")
+    ap.add_argument("--serve-chains", type=int, default=4)
     args = ap.parse_args()
     ws, rank, local = _dist()
     metric = "histories/s"
@@ -314,6 +413,11 @@ def main():
     h2d = n_vox * 5 + len(exposures) * 80
     d2h = n_vox * (8 + 8 + 4)
 
+    serving = None
+    if rank == 0 and not args.no_serve:
+        serving = serving_measurement(ctx, args.serve_jobs, [float(r) for r in args.serve_rates.split(",")],
+                                      args.serve_chains)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -343,6 +447,7 @@ def main():
             # per step: one generation pass and one transport launch per queue chunk
             "gpu_launches": args.steps * (1 if args.queue_log2 < 0 else 2 * max(1, -(-n_hist // (1 << (args.queue_log2 or 25))))),
             "clocks": clocks.summary(),
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     dlut.close()

@@ -170,6 +170,10 @@ SIGNATURES = {
     "dxmc_gpu_job_result": (C.c_int, [VP, C.c_int, D, DP, DP, U32P, C.POINTER(JobStats)]),
     "dxmc_gpu_job_free": (None, [VP]),
     "dxmc_gpu_probe_lut": (C.c_int, [VP, VP, C.c_int, DP, C.c_int, DP, DP]),
+    "dxmc_gpu_job_release": (C.c_int, [VP]),
+    "dxmc_gpu_ctx_memory": (C.c_int, [VP, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "dxmc_gpu_host_alloc": (C.c_int, [C.c_uint64, C.POINTER(VP)]),
+    "dxmc_gpu_host_free": (None, [VP]),
     "dxmc_gpu_batch_submit": (C.c_int, [VP, C.POINTER(BatchEntry), C.c_int, C.POINTER(BatchOptions), C.POINTER(VP)]),
     "dxmc_gpu_batch_wait": (C.c_int, [VP, C.c_int64]),
     "dxmc_gpu_batch_job": (C.c_int, [VP, C.c_int, C.POINTER(VP)]),

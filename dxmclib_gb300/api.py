@@ -755,6 +755,12 @@ class GpuContext:
     def _register(self, obj):
         self._children.add(obj)
 
+    def memory(self) -> tuple:
+        """(budget, in_use) device bytes of the context's admission check."""
+        b, u = C.c_uint64(), C.c_uint64()
+        A.check(self.lib.dxmc_gpu_ctx_memory(self.handle, C.byref(b), C.byref(u)), self.handle, "dxmc_gpu_ctx_memory")
+        return b.value, u.value
+
     def close(self):
         if self.handle:
             children = list(self._children)
@@ -1014,6 +1020,11 @@ class Job:
         if check and rc not in (A.DXMC_OK,):
             A.check(rc, self.ctx.handle, "dxmc_gpu_job_result")
         return dose, var, nev, stats
+
+    def release(self):
+        """Frees the device buffers of a finished job (its results are gone)."""
+        if self.handle and self.ctx.handle:
+            A.check(self.ctx.lib.dxmc_gpu_job_release(self.handle), self.ctx.handle, "dxmc_gpu_job_release")
 
     def close(self):
         if self.handle and self._owned and self.ctx.handle:

@@ -33,6 +33,7 @@ struct dxmc_gpu_ctx {
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t result_stream = nullptr; // post-processing and result copies
     dxmc_gpu_options options {};
     std::mutex mutex;
     std::string last_error;
@@ -72,7 +73,7 @@ struct dxmc_job {
     dev::JobCounters* counters = nullptr;
     unsigned char* tables = nullptr;
     unsigned char* queue = nullptr; // pre-generated photons (SoA)
-    int* cancel_host = nullptr;  // pinned, mapped
+    int* cancel_host = nullptr;  // pinned, mapped; the counters' host copy follows at byte 16
     int* cancel_dev = nullptr;
     cudaEvent_t begin = nullptr, start = nullptr, stop = nullptr; // job begin, kernel start, kernel end
     uint64_t histories = 0;
@@ -235,6 +236,32 @@ int dxmc_gpu_device_count(void)
     return n;
 }
 
+int dxmc_gpu_ctx_memory(const dxmc_gpu_ctx* ctx, uint64_t* budget, uint64_t* in_use)
+{
+    if (!ctx)
+        return DXMC_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(const_cast<dxmc_gpu_ctx*>(ctx)->mutex);
+    if (budget)
+        *budget = ctx->budget;
+    if (in_use)
+        *in_use = ctx->in_use;
+    return DXMC_OK;
+}
+
+int dxmc_gpu_host_alloc(uint64_t bytes, void** out)
+{
+    if (!out || bytes == 0)
+        return DXMC_ERR_INVALID;
+    *out = nullptr;
+    return cudaHostAlloc(out, bytes, cudaHostAllocDefault) == cudaSuccess ? DXMC_OK : DXMC_ERR_OOM;
+}
+
+void dxmc_gpu_host_free(void* ptr)
+{
+    if (ptr)
+        cudaFreeHost(ptr);
+}
+
 int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out)
 {
     if (!out)
@@ -265,6 +292,11 @@ int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out)
         delete ctx;
         return DXMC_ERR_DEVICE;
     }
+    if (cudaStreamCreateWithFlags(&ctx->result_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return DXMC_ERR_DEVICE;
+    }
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     ctx->budget = ctx->options.memory_budget ? ctx->options.memory_budget : static_cast<uint64_t>(free_b * 0.9);
@@ -279,6 +311,7 @@ void dxmc_gpu_ctx_destroy(dxmc_gpu_ctx* ctx)
     cudaSetDevice(ctx->device);
     sync_ctx_streams(ctx);
     release_engines(ctx);
+    cudaStreamDestroy(ctx->result_stream);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -789,7 +822,7 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     if (e == cudaSuccess)
         e = cudaEventRecord(j->begin, s);
     if (e == cudaSuccess)
-        e = cudaHostAlloc(&j->cancel_host, sizeof(int), cudaHostAllocMapped);
+        e = cudaHostAlloc(&j->cancel_host, 16 + sizeof(dev::JobCounters), cudaHostAllocMapped);
     if (e == cudaSuccess) {
         *j->cancel_host = 0;
         e = cudaHostGetDevicePointer(&j->cancel_dev, j->cancel_host, 0);
@@ -975,21 +1008,22 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
 
 // ---- batches --------------------------------------------------------------------------
 //
-// Two ways to run a batch, both launched as one CUDA graph on an engine stream:
+// Two ways to run a batch:
 //
 // * concurrent (default): every job keeps the single-job kernels (parameters in
 //   the kernel's constant bank, LUT staged in shared memory, photon queue).  The
-//   jobs are dealt longest-first onto a few chains; a chain's jobs run one after
-//   another and share one photon-queue buffer, the chains run side by side, so a
-//   job's blocks fill the SMs as the previous job of another chain drains.
+//   context owns a few chains (a stream and a photon-queue buffer each); a batch
+//   deals its jobs longest-first onto the chains with the least outstanding work,
+//   shortest-first within a chain, captures each chain's share as one CUDA graph
+//   and launches it on the chain's stream.  Chains run side by side, so one job's
+//   blocks fill the SMs as another chain's job drains, and a batch submitted while
+//   others run queues behind them chain by chain (continuous batching); jobs on a
+//   chain run one after another, which is what lets them share its queue buffer.
 // * persistent: one multi-job kernel per correction model drains work items
-//   (job, first history, count) of all jobs from a device-side queue.  The graph
-//   is instantiated once per engine: three host-to-device copies (job
-//   parameters, items, control block) and the three kernels as independent
-//   nodes; only the copy sizes change between batches.
-//
-// The context has two engines used in turn, so a batch can be prepared and queued
-// while the previous one still runs.
+//   (job, first history, count) of all jobs from a device-side queue.  Its graph
+//   is instantiated once per engine: three host-to-device copies (job parameters,
+//   items, control block) and the three kernels as independent nodes; only the
+//   copy sizes change between batches.  Two engines are used in turn.
 constexpr int MAX_BATCH_JOBS = 4096;
 constexpr uint64_t MAX_BATCH_ITEMS = 1ull << 20;
 constexpr int MAX_CHAINS = 8;
@@ -1007,20 +1041,25 @@ struct BatchEngine {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t copy_params = nullptr, copy_items = nullptr;
-    cudaEvent_t done = nullptr;   // staging may be rewritten once this has completed
-    cudaEvent_t inputs = nullptr; // orders the context stream's job preparation before the graph
+    cudaEvent_t done = nullptr; // staging may be rewritten once this has completed
     dev::BatchParams kparams {};
-    // concurrent mode
-    cudaStream_t chain[MAX_CHAINS] {};
-    cudaEvent_t fork = nullptr, join[MAX_CHAINS] {};
-    unsigned char* queue[MAX_CHAINS] {}; // photon-queue buffer per chain (lazily allocated)
-    uint64_t queue_capacity = 0;         // photons per chain buffer
-    uint64_t bytes = 0;                  // device bytes held (budget)
+    uint64_t bytes = 0;
+};
+
+struct Chain {
+    cudaStream_t stream = nullptr;
+    unsigned char* queue = nullptr;
+    std::vector<std::pair<cudaEvent_t, uint64_t>> pending; // (end of a queued share, its histories)
 };
 
 struct BatchEngines {
     BatchEngine e[2];
     int next = 0;
+    Chain chain[MAX_CHAINS];
+    cudaStream_t collector = nullptr; // records batch completion after all its chains
+    uint64_t queue_capacity = 0;      // photons per chain queue buffer
+    uint64_t chain_bytes = 0;
+    std::vector<cudaEvent_t> spare_events;
 };
 
 namespace {
@@ -1036,17 +1075,6 @@ void release_engine(dxmc_gpu_ctx* ctx, BatchEngine& g)
 {
     if (g.stream)
         cudaStreamSynchronize(g.stream);
-    for (int c = 0; c < MAX_CHAINS; ++c) {
-        if (g.chain[c]) {
-            cudaStreamSynchronize(g.chain[c]);
-            cudaStreamDestroy(g.chain[c]);
-        }
-        if (g.join[c])
-            cudaEventDestroy(g.join[c]);
-        cudaFree(g.queue[c]);
-    }
-    if (g.fork)
-        cudaEventDestroy(g.fork);
     if (g.exec)
         cudaGraphExecDestroy(g.exec);
     if (g.graph)
@@ -1059,12 +1087,35 @@ void release_engine(dxmc_gpu_ctx* ctx, BatchEngine& g)
     cudaFreeHost(g.h_control);
     if (g.done)
         cudaEventDestroy(g.done);
-    if (g.inputs)
-        cudaEventDestroy(g.inputs);
     if (g.stream)
         cudaStreamDestroy(g.stream);
     ctx->in_use -= g.bytes;
     g = BatchEngine {};
+}
+
+void release_chains(dxmc_gpu_ctx* ctx, BatchEngines& en)
+{
+    for (auto& c : en.chain) {
+        if (c.stream) {
+            cudaStreamSynchronize(c.stream);
+            cudaStreamDestroy(c.stream);
+        }
+        cudaFree(c.queue);
+        for (auto& pr : c.pending)
+            cudaEventDestroy(pr.first);
+        c = Chain {};
+    }
+    if (en.collector) {
+        cudaStreamSynchronize(en.collector);
+        cudaStreamDestroy(en.collector);
+        en.collector = nullptr;
+    }
+    for (auto ev : en.spare_events)
+        cudaEventDestroy(ev);
+    en.spare_events.clear();
+    ctx->in_use -= en.chain_bytes;
+    en.chain_bytes = 0;
+    en.queue_capacity = 0;
 }
 
 cudaError_t build_engine(dxmc_gpu_ctx* ctx, BatchEngine& g)
@@ -1084,15 +1135,6 @@ cudaError_t build_engine(dxmc_gpu_ctx* ctx, BatchEngine& g)
         e = cudaHostAlloc(&g.h_control, sizeof(dev::BatchControl), cudaHostAllocDefault);
     if (e == cudaSuccess)
         e = cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
-    if (e == cudaSuccess)
-        e = cudaEventCreateWithFlags(&g.inputs, cudaEventDisableTiming);
-    if (e == cudaSuccess)
-        e = cudaEventCreateWithFlags(&g.fork, cudaEventDisableTiming);
-    for (int c = 0; c < MAX_CHAINS && e == cudaSuccess; ++c) {
-        e = cudaStreamCreateWithFlags(&g.chain[c], cudaStreamNonBlocking);
-        if (e == cudaSuccess)
-            e = cudaEventCreateWithFlags(&g.join[c], cudaEventDisableTiming);
-    }
     if (e == cudaSuccess)
         e = cudaGraphCreate(&g.graph, 0);
     if (e != cudaSuccess)
@@ -1129,42 +1171,76 @@ cudaError_t build_engine(dxmc_gpu_ctx* ctx, BatchEngine& g)
     return e;
 }
 
-// Photon-queue buffers of the first `chains` chains, `capacity` photons each.
-int ensure_chain_queues(dxmc_gpu_ctx* ctx, BatchEngine& g, int chains, uint64_t capacity)
+// Streams and photon-queue buffers (`capacity` photons) of the first `chains` chains.
+int ensure_chains(dxmc_gpu_ctx* ctx, BatchEngines& en, int chains, uint64_t capacity)
 {
-    if (g.queue_capacity < capacity) {
-        for (int c = 0; c < MAX_CHAINS; ++c) {
-            if (g.queue[c]) {
-                cudaFree(g.queue[c]);
-                g.queue[c] = nullptr;
-                g.bytes -= g.queue_capacity * 48;
-                ctx->in_use -= g.queue_capacity * 48;
+    if (!en.collector && cudaStreamCreateWithFlags(&en.collector, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(ctx, DXMC_ERR_DEVICE, "batch collector stream");
+    if (capacity > en.queue_capacity) {
+        // larger buffers: wait for every chain, then drop the old ones
+        for (auto& c : en.chain) {
+            if (c.stream)
+                cudaStreamSynchronize(c.stream);
+            if (c.queue) {
+                cudaFree(c.queue);
+                c.queue = nullptr;
+                en.chain_bytes -= en.queue_capacity * 48;
+                ctx->in_use -= en.queue_capacity * 48;
             }
         }
-        g.queue_capacity = capacity;
+        en.queue_capacity = capacity;
     }
-    for (int c = 0; c < chains; ++c) {
-        if (g.queue[c])
+    for (int k = 0; k < chains; ++k) {
+        Chain& c = en.chain[k];
+        if (!c.stream && cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
+            return fail(ctx, DXMC_ERR_DEVICE, "batch chain stream");
+        if (c.queue || capacity == 0)
             continue;
-        const uint64_t bytes = g.queue_capacity * 48;
+        const uint64_t bytes = en.queue_capacity * 48;
         if (ctx->in_use + bytes > ctx->budget)
             return fail(ctx, DXMC_ERR_OOM, "batch photon queues exceed the device memory budget");
-        const cudaError_t e = cudaMalloc(&g.queue[c], bytes);
+        const cudaError_t e = cudaMalloc(&c.queue, bytes);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "batch photon queue");
-        g.bytes += bytes;
+        en.chain_bytes += bytes;
         ctx->in_use += bytes;
     }
     return DXMC_OK;
+}
+
+// Histories still queued or running on a chain (its completed shares are dropped).
+uint64_t chain_outstanding(BatchEngines& en, Chain& c)
+{
+    uint64_t left = 0;
+    std::vector<std::pair<cudaEvent_t, uint64_t>> keep;
+    for (auto& pr : c.pending) {
+        if (cudaEventQuery(pr.first) == cudaSuccess) {
+            en.spare_events.push_back(pr.first);
+        } else {
+            left += pr.second;
+            keep.push_back(pr);
+        }
+    }
+    c.pending.swap(keep);
+    return left;
+}
+
+cudaError_t take_event(BatchEngines& en, cudaEvent_t* ev)
+{
+    if (!en.spare_events.empty()) {
+        *ev = en.spare_events.back();
+        en.spare_events.pop_back();
+        return cudaSuccess;
+    }
+    return cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
 }
 
 } // namespace
 
 struct dxmc_batch {
     dxmc_gpu_ctx* ctx = nullptr;
-    BatchEngine* engine = nullptr;
     std::vector<dxmc_job*> jobs;
-    cudaGraphExec_t exec = nullptr; // concurrent mode: this batch's graph
+    std::vector<cudaGraphExec_t> execs; // concurrent mode: one graph per chain used
     cudaEvent_t start = nullptr, stop = nullptr;
 };
 
@@ -1183,23 +1259,25 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
     const int chains = std::clamp(opt && opt->chains > 0 ? opt->chains : DEFAULT_CHAINS, 1, MAX_CHAINS);
     std::lock_guard<std::mutex> lock(ctx->mutex);
     cudaSetDevice(ctx->device);
-    BatchEngines* engines = engines_of(ctx, true);
-    if (!engines)
+    BatchEngines* en = engines_of(ctx, true);
+    if (!en)
         return DXMC_ERR_OOM;
-    BatchEngine& g = engines->e[engines->next];
-    if (!g.ready) {
-        const cudaError_t e = build_engine(ctx, g);
-        if (e != cudaSuccess) {
-            release_engine(ctx, g);
-            return cuda_fail(ctx, e, "batch engine");
+    BatchEngine* g = nullptr;
+    if (persistent) {
+        g = &en->e[en->next];
+        if (!g->ready) {
+            const cudaError_t e = build_engine(ctx, *g);
+            if (e != cudaSuccess) {
+                release_engine(ctx, *g);
+                return cuda_fail(ctx, e, "batch engine");
+            }
         }
-    }
-    // the engine's staging buffers and chain queues are free once its previous batch has finished
-    if (cudaEventSynchronize(g.done) != cudaSuccess)
-        return fail(ctx, DXMC_ERR_DEVICE, "previous batch of the engine failed");
-    const int log2_chunk = ctx->options.queue_log2_chunk == 0 ? 25 : ctx->options.queue_log2_chunk;
-    if (!persistent && log2_chunk >= 0) {
-        const int rc = ensure_chain_queues(ctx, g, chains, 1ull << std::min(log2_chunk, 34));
+        // the engine's staging buffers are free once its previous batch has finished
+        if (cudaEventSynchronize(g->done) != cudaSuccess)
+            return fail(ctx, DXMC_ERR_DEVICE, "previous batch of the engine failed");
+    } else {
+        const int log2_chunk = ctx->options.queue_log2_chunk == 0 ? 25 : ctx->options.queue_log2_chunk;
+        const int rc = ensure_chains(ctx, *en, chains, log2_chunk >= 0 ? 1ull << std::min(log2_chunk, 34) : 0);
         if (rc != DXMC_OK)
             return rc;
     }
@@ -1207,12 +1285,10 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
     if (!b)
         return DXMC_ERR_OOM;
     b->ctx = ctx;
-    b->engine = &g;
     cudaStream_t s = ctx->stream;
     std::vector<int> models(n);
     std::vector<uint64_t> chunks(n, 0);
     std::vector<dev::TransportParams> params(persistent ? 0 : n);
-    std::vector<int> chain_of(n, 0);
     uint64_t all = 0;
     auto abort = [&](int rc) {
         cudaStreamSynchronize(s);
@@ -1220,8 +1296,8 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
             ctx->in_use -= j->bytes;
             discard_job(j);
         }
-        if (b->exec)
-            cudaGraphExecDestroy(b->exec);
+        for (auto x : b->execs)
+            cudaGraphExecDestroy(x);
         if (b->start)
             cudaEventDestroy(b->start);
         if (b->stop)
@@ -1230,17 +1306,18 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
         return rc;
     };
     for (int i = 0; i < n; ++i) {
-        const dxmc_batch_entry& en = entries[i];
-        if (!en.world || !en.lut || !en.job)
+        const dxmc_batch_entry& entry = entries[i];
+        if (!entry.world || !entry.lut || !entry.job)
             return abort(fail(ctx, DXMC_ERR_INVALID, "batch entry " + std::to_string(i) + " is incomplete"));
         dxmc_job* j = nullptr;
-        const int rc = persistent ? prepare_job(ctx, en.world, en.lut, en.job, QueueMode::none, 0, &j, g.h_params[i], chunks[i])
-                                  : prepare_job(ctx, en.world, en.lut, en.job, QueueMode::shared, g.queue_capacity, &j, params[i], chunks[i]);
+        const int rc = persistent
+            ? prepare_job(ctx, entry.world, entry.lut, entry.job, QueueMode::none, 0, &j, g->h_params[i], chunks[i])
+            : prepare_job(ctx, entry.world, entry.lut, entry.job, QueueMode::shared, en->queue_capacity, &j, params[i], chunks[i]);
         if (rc != DXMC_OK)
             return abort(rc);
         ctx->in_use += j->bytes; // later entries see the earlier ones in the admission check
         b->jobs.push_back(j);
-        models[i] = en.job->model;
+        models[i] = entry.job->model;
         all += j->histories;
     }
     cudaError_t e = cudaEventCreate(&b->start);
@@ -1248,9 +1325,7 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
         e = cudaEventCreate(&b->stop);
     // job preparation (allocations, clears, source tables) on the context stream comes first
     if (e == cudaSuccess)
-        e = cudaEventRecord(g.inputs, s);
-    if (e == cudaSuccess)
-        e = cudaStreamWaitEvent(g.stream, g.inputs, 0);
+        e = cudaEventRecord(b->start, s);
     if (e != cudaSuccess)
         return abort(cuda_fail(ctx, e, "batch setup"));
 
@@ -1272,7 +1347,7 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
             item *= 2;
         if (item > 0xffffffffull)
             return abort(fail(ctx, DXMC_ERR_INVALID, "batch too large"));
-        dev::BatchControl& c = *g.h_control;
+        dev::BatchControl& c = *g->h_control;
         std::memset(&c, 0, sizeof(c));
         uint64_t n_items = 0;
         for (int model = 0; model < 3; ++model) {
@@ -1282,7 +1357,7 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
                     continue;
                 const uint64_t total = b->jobs[i]->histories;
                 for (uint64_t first = 0; first < total; first += item)
-                    g.h_items[n_items++] = dev::BatchItem { static_cast<uint32_t>(i), static_cast<uint32_t>(std::min(item, total - first)), first };
+                    g->h_items[n_items++] = dev::BatchItem { static_cast<uint32_t>(i), static_cast<uint32_t>(std::min(item, total - first)), first };
             }
             c.n_items[model] = n_items - c.item_base[model];
         }
@@ -1292,26 +1367,34 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
                                                              : (ctx->options.interact_threshold > 0 ? ctx->options.interact_threshold : DEFAULT_INTERACT_THRESHOLD);
         c.regen_threshold = std::clamp(regen, 1, 32);
         c.interact_threshold = std::clamp(inter, 1, 32);
-        e = cudaGraphExecMemcpyNodeSetParams1D(g.exec, g.copy_params, g.d_params, g.h_params, n * sizeof(dev::TransportParams), cudaMemcpyHostToDevice);
+        e = cudaGraphExecMemcpyNodeSetParams1D(g->exec, g->copy_params, g->d_params, g->h_params, n * sizeof(dev::TransportParams), cudaMemcpyHostToDevice);
         if (e == cudaSuccess)
-            e = cudaGraphExecMemcpyNodeSetParams1D(g.exec, g.copy_items, g.d_items, g.h_items, n_items * sizeof(dev::BatchItem), cudaMemcpyHostToDevice);
+            e = cudaGraphExecMemcpyNodeSetParams1D(g->exec, g->copy_items, g->d_items, g->h_items, n_items * sizeof(dev::BatchItem), cudaMemcpyHostToDevice);
         if (e == cudaSuccess)
-            e = cudaEventRecord(b->start, g.stream);
+            e = cudaStreamWaitEvent(g->stream, b->start, 0);
         for (auto* j : b->jobs) // every job's kernel time is the batch's
             if (e == cudaSuccess)
-                e = cudaEventRecord(j->start, g.stream);
+                e = cudaEventRecord(j->start, g->stream);
         if (e == cudaSuccess)
-            e = cudaGraphLaunch(g.exec, g.stream);
+            e = cudaGraphLaunch(g->exec, g->stream);
         for (auto* j : b->jobs)
             if (e == cudaSuccess)
-                e = cudaEventRecord(j->stop, g.stream);
+                e = cudaEventRecord(j->stop, g->stream);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(b->stop, g->stream);
+        if (e == cudaSuccess)
+            e = cudaEventRecord(g->done, g->stream);
+        if (e == cudaSuccess)
+            en->next ^= 1;
     } else {
-        // longest job first onto the chain with the least work
+        // longest job first onto the chain with the least outstanding work
+        std::vector<uint64_t> load(chains);
+        for (int c = 0; c < chains; ++c)
+            load[c] = chain_outstanding(*en, en->chain[c]);
         std::vector<int> order(n);
         for (int i = 0; i < n; ++i)
             order[i] = i;
         std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->jobs[x]->histories > b->jobs[y]->histories; });
-        std::vector<uint64_t> load(chains, 0);
         std::vector<std::vector<int>> lists(chains);
         for (int i : order) {
             const int c = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
@@ -1321,48 +1404,64 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
         std::vector<LaunchPlan> plans(n);
         for (int i = 0; i < n; ++i) // occupancy queries and attributes stay outside the capture
             plans[i] = plan_launch(ctx, entries[i].world, entries[i].lut, models[i], params[i]);
-        cudaGraph_t graph = nullptr;
-        step = "batch capture";
-        e = cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal);
-        if (e == cudaSuccess) {
-            cudaError_t ce = cudaEventRecord(g.fork, g.stream);
-            for (int c = 0; c < chains && ce == cudaSuccess; ++c) {
-                ce = cudaStreamWaitEvent(g.chain[c], g.fork, 0);
+        for (int c = 0; c < chains && e == cudaSuccess; ++c) {
+            if (lists[c].empty())
+                continue;
+            std::reverse(lists[c].begin(), lists[c].end()); // shortest first within the chain
+            Chain& ch = en->chain[c];
+            e = cudaStreamWaitEvent(ch.stream, b->start, 0);
+            cudaGraph_t graph = nullptr;
+            uint64_t share = 0;
+            if (e == cudaSuccess) {
+                step = "batch capture";
+                e = cudaStreamBeginCapture(ch.stream, cudaStreamCaptureModeThreadLocal);
+            }
+            if (e == cudaSuccess) {
+                cudaError_t ce = cudaSuccess;
                 for (size_t k = 0; k < lists[c].size() && ce == cudaSuccess; ++k) {
                     const int i = lists[c][k];
-                    ce = enqueue_job(b->jobs[i], params[i], models[i], chunks[i], g.queue[c], plans[i], g.chain[c], true);
+                    ce = enqueue_job(b->jobs[i], params[i], models[i], chunks[i], ch.queue, plans[i], ch.stream, true);
+                    share += b->jobs[i]->histories;
                 }
-                if (ce == cudaSuccess)
-                    ce = cudaEventRecord(g.join[c], g.chain[c]);
-                if (ce == cudaSuccess)
-                    ce = cudaStreamWaitEvent(g.stream, g.join[c], 0);
+                e = cudaStreamEndCapture(ch.stream, &graph);
+                if (ce != cudaSuccess)
+                    e = ce;
             }
-            e = cudaStreamEndCapture(g.stream, &graph);
-            if (ce != cudaSuccess)
-                e = ce;
+            cudaGraphExec_t exec = nullptr;
+            if (e == cudaSuccess) {
+                step = "batch graph instantiation";
+                e = cudaGraphInstantiate(&exec, graph, 0);
+            }
+            if (graph)
+                cudaGraphDestroy(graph);
+            if (e == cudaSuccess) {
+                b->execs.push_back(exec);
+                step = "batch graph launch";
+                e = cudaGraphLaunch(exec, ch.stream);
+            }
+            cudaEvent_t end = nullptr;
+            if (e == cudaSuccess)
+                e = take_event(*en, &end);
+            if (e == cudaSuccess)
+                e = cudaEventRecord(end, ch.stream);
+            if (e == cudaSuccess) {
+                ch.pending.emplace_back(end, share);
+                e = cudaStreamWaitEvent(en->collector, end, 0);
+            } else if (end) {
+                en->spare_events.push_back(end);
+            }
         }
-        if (e == cudaSuccess) {
-            step = "batch graph instantiation";
-            e = cudaGraphInstantiate(&b->exec, graph, 0);
-        }
-        if (graph)
-            cudaGraphDestroy(graph);
         if (e == cudaSuccess)
-            e = cudaEventRecord(b->start, g.stream);
-        if (e == cudaSuccess) {
-            step = "batch graph launch";
-            e = cudaGraphLaunch(b->exec, g.stream);
-        }
+            e = cudaEventRecord(b->stop, en->collector);
     }
-    if (e == cudaSuccess)
-        e = cudaEventRecord(b->stop, g.stream);
-    if (e == cudaSuccess)
-        e = cudaEventRecord(g.done, g.stream);
     if (e != cudaSuccess) {
-        cudaStreamSynchronize(g.stream);
+        if (g)
+            cudaStreamSynchronize(g->stream);
+        for (int c = 0; c < chains; ++c)
+            if (en->chain[c].stream)
+                cudaStreamSynchronize(en->chain[c].stream);
         return abort(cuda_fail(ctx, e, step));
     }
-    engines->next ^= 1;
     *out = b;
     return DXMC_OK;
 }
@@ -1398,10 +1497,10 @@ void dxmc_gpu_batch_free(dxmc_batch* b)
         return;
     cudaSetDevice(b->ctx->device);
     cudaEventSynchronize(b->stop);
+    for (auto x : b->execs) // the graphs record the jobs' events: destroy them first
+        cudaGraphExecDestroy(x);
     for (auto* j : b->jobs)
         dxmc_gpu_job_free(j);
-    if (b->exec)
-        cudaGraphExecDestroy(b->exec);
     cudaEventDestroy(b->start);
     cudaEventDestroy(b->stop);
     delete b;
@@ -1414,10 +1513,15 @@ namespace {
 void sync_ctx_streams(dxmc_gpu_ctx* ctx)
 {
     cudaStreamSynchronize(ctx->stream);
-    if (BatchEngines* en = engines_of(ctx, false))
+    cudaStreamSynchronize(ctx->result_stream);
+    if (BatchEngines* en = engines_of(ctx, false)) {
         for (auto& g : en->e)
             if (g.stream)
                 cudaStreamSynchronize(g.stream);
+        for (auto& c : en->chain)
+            if (c.stream)
+                cudaStreamSynchronize(c.stream);
+    }
 }
 
 void release_engines(dxmc_gpu_ctx* ctx)
@@ -1426,6 +1530,7 @@ void release_engines(dxmc_gpu_ctx* ctx)
         return;
     for (auto& g : ctx->engines->e)
         release_engine(ctx, g);
+    release_chains(ctx, *ctx->engines);
     delete ctx->engines;
     ctx->engines = nullptr;
 }
@@ -1480,15 +1585,52 @@ int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double
     const int wrc = dxmc_gpu_job_wait(j, -1);
     if (wrc != DXMC_OK)
         return wrc;
-    std::lock_guard<std::mutex> lock(ctx->mutex);
-    cudaSetDevice(ctx->device);
-    cudaStream_t s = ctx->stream;
-    if (!j->tally && !j->tally_f32)
-        return fail(ctx, DXMC_ERR_STATE, "job results were already released");
-    dev::JobCounters c {};
-    DXMC_CUDA(ctx, cudaMemcpyAsync(&c, j->counters, sizeof(c), cudaMemcpyDeviceToHost, s));
-    DXMC_CUDA(ctx, cudaStreamSynchronize(s));
     const uint64_t nv = j->world->params.n_voxels;
+    auto* hc = reinterpret_cast<dev::JobCounters*>(reinterpret_cast<unsigned char*>(j->cancel_host) + 16);
+    cudaEvent_t done = nullptr;
+    {
+        // queue post-processing and copies on the result stream under the lock, wait without it
+        std::lock_guard<std::mutex> lock(ctx->mutex);
+        cudaSetDevice(ctx->device);
+        cudaStream_t s = ctx->result_stream;
+        if (!j->tally && !j->tally_f32)
+            return fail(ctx, DXMC_ERR_STATE, "job results were already released");
+        DXMC_CUDA(ctx, cudaMemcpyAsync(hc, j->counters, sizeof(dev::JobCounters), cudaMemcpyDeviceToHost, s));
+        if (!j->cancelled && (dose || variance)) {
+            double* d_out = nullptr;
+            const uint64_t out_elems = (dose ? nv : 0) + (variance ? nv : 0);
+            DXMC_CUDA(ctx, cudaMallocAsync(&d_out, out_elems * sizeof(double), s));
+            double* d_dose = dose ? d_out : nullptr;
+            double* d_var = variance ? d_out + (dose ? nv : 0) : nullptr;
+            const double vv = j->world->spacing[0] * j->world->spacing[1] * j->world->spacing[2] / 1000.0;
+            cudaError_t e;
+            if (j->tally_mode == 1)
+                e = dev::launch_postprocess_f32(j->tally_f32, j->n_events, j->world->voxels, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, s);
+            else
+                e = dev::launch_postprocess(j->tally, j->n_events, j->world->voxels, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, s);
+            if (e == cudaSuccess && dose)
+                e = cudaMemcpyAsync(dose, d_dose, nv * sizeof(double), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess && variance)
+                e = cudaMemcpyAsync(variance, d_var, nv * sizeof(double), cudaMemcpyDeviceToHost, s);
+            cudaFreeAsync(d_out, s);
+            if (e != cudaSuccess)
+                return cuda_fail(ctx, e, "result post-processing");
+        }
+        if (!j->cancelled && n_events)
+            DXMC_CUDA(ctx, cudaMemcpyAsync(n_events, j->n_events, nv * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        DXMC_CUDA(ctx, cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+        const cudaError_t e = cudaEventRecord(done, s);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(done);
+            return cuda_fail(ctx, e, "result copy");
+        }
+    }
+    const cudaError_t e = cudaEventSynchronize(done);
+    cudaEventDestroy(done);
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "result copy");
+    const dev::JobCounters c = *hc;
     if (stats) {
         stats->histories = c.histories_done;
         stats->steps = c.steps;
@@ -1510,31 +1652,23 @@ int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double
             std::memset(n_events, 0, nv * sizeof(uint32_t));
         return fail(ctx, DXMC_ERR_CANCELLED, "job was cancelled");
     }
-    if (dose || variance) {
-        double* d_out = nullptr;
-        const uint64_t out_elems = (dose ? nv : 0) + (variance ? nv : 0);
-        DXMC_CUDA(ctx, cudaMallocAsync(&d_out, out_elems * sizeof(double), s));
-        double* d_dose = dose ? d_out : nullptr;
-        double* d_var = variance ? d_out + (dose ? nv : 0) : nullptr;
-        const double vv = j->world->spacing[0] * j->world->spacing[1] * j->world->spacing[2] / 1000.0;
-        cudaError_t e;
-        if (j->tally_mode == 1)
-            e = dev::launch_postprocess_f32(j->tally_f32, j->n_events, j->world->voxels, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, s);
-        else
-            e = dev::launch_postprocess(j->tally, j->n_events, j->world->voxels, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, s);
-        if (e == cudaSuccess && dose)
-            e = cudaMemcpyAsync(dose, d_dose, nv * sizeof(double), cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess && variance)
-            e = cudaMemcpyAsync(variance, d_var, nv * sizeof(double), cudaMemcpyDeviceToHost, s);
-        cudaFreeAsync(d_out, s);
-        if (e != cudaSuccess)
-            return cuda_fail(ctx, e, "result post-processing");
-    }
-    if (n_events)
-        DXMC_CUDA(ctx, cudaMemcpyAsync(n_events, j->n_events, nv * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    DXMC_CUDA(ctx, cudaStreamSynchronize(s));
     if (c.overflows)
         return fail(ctx, DXMC_ERR_REJECTION_CAP, "sampling loops hit the rejection cap in " + std::to_string(c.overflows) + " events");
+    return DXMC_OK;
+}
+
+int dxmc_gpu_job_release(dxmc_job* j)
+{
+    if (!j)
+        return DXMC_ERR_INVALID;
+    dxmc_gpu_ctx* ctx = j->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    cudaSetDevice(ctx->device);
+    if (j->stop)
+        cudaEventSynchronize(j->stop);
+    free_job_device(j);
+    ctx->in_use -= j->bytes;
+    j->bytes = 0;
     return DXMC_OK;
 }
 

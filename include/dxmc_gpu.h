@@ -200,6 +200,12 @@ void dxmc_gpu_ctx_destroy(dxmc_gpu_ctx* ctx);
 const char* dxmc_gpu_last_error(const dxmc_gpu_ctx* ctx);
 int dxmc_gpu_device_count(void);
 int dxmc_gpu_abi_version(void);
+/* Device-memory budget of the context and the bytes its worlds, LUTs, jobs and
+ * batch buffers hold (the admission check of every upload and submit). */
+int dxmc_gpu_ctx_memory(const dxmc_gpu_ctx* ctx, uint64_t* budget, uint64_t* in_use);
+/* Page-locked host memory for result buffers (cudaHostAlloc / cudaFreeHost). */
+int dxmc_gpu_host_alloc(uint64_t bytes, void** out);
+void dxmc_gpu_host_free(void* ptr);
 
 /* ---- world (World<T>, world.hpp:37-227) ---------------------------------- */
 typedef struct dxmc_world_desc {
@@ -260,6 +266,10 @@ int dxmc_gpu_job_cancel(dxmc_job* job);
  * world size; any output pointer may be NULL.  calibration multiplies DOSE. */
 int dxmc_gpu_job_result(dxmc_job* job, int output_mode, double calibration,
     double* dose, double* variance, uint32_t* n_events, dxmc_job_stats* stats);
+/* Frees a finished job's device buffers (tallies, tables) and returns them to
+ * the memory budget; the handle stays valid for dxmc_gpu_job_free, results are
+ * gone.  For batched jobs, whose handles the batch owns. */
+int dxmc_gpu_job_release(dxmc_job* job);
 void dxmc_gpu_job_free(dxmc_job* job);
 
 /* ---- batches: many jobs in one persistent launch ---------------------------- */
@@ -287,17 +297,18 @@ typedef struct dxmc_batch_options {
     int32_t item_histories;     /* persistent mode: histories per work item; 0: automatic (256..8192) */
     int32_t pad;
 } dxmc_batch_options;
-/* Non-blocking.  At most 4096 jobs per batch; `options` may be NULL.  Batches
- * alternate between two engines (streams + CUDA graphs), so two can be in
- * flight; a third submit waits until the engine's previous batch has finished.
- * The concurrent mode holds one photon-queue buffer (48 B x 2^queue_log2_chunk)
- * per chain and engine. */
+/* Non-blocking.  At most 4096 jobs per batch; `options` may be NULL.
+ * Concurrent mode: the context keeps up to 8 chains (stream + photon-queue buffer
+ * of 48 B x 2^queue_log2_chunk each); a batch's jobs queue behind the work
+ * already on those chains, so batches can be submitted while others run.
+ * Persistent mode: two engines (stream + instantiated graph) are used in turn;
+ * a third submit waits until the engine's previous batch has finished. */
 int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, int n_entries,
                           const dxmc_batch_options* options, dxmc_batch** out);
 int dxmc_gpu_batch_wait(dxmc_batch* batch, int64_t timeout_ms);
 /* Job handle of entry `index`, for dxmc_gpu_job_result; owned by the batch. */
 int dxmc_gpu_batch_job(dxmc_batch* batch, int index, dxmc_job** job);
-/* Device time of the batch's kernels (ms). */
+/* Device time from the batch's submission being ready to its last job's end (ms). */
 double dxmc_gpu_batch_kernel_ms(dxmc_batch* batch);
 void dxmc_gpu_batch_free(dxmc_batch* batch);
 
