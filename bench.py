@@ -251,6 +251,77 @@ def serving_measurement(ctx, n_jobs: int, rates, chains: int, seed: int = 202612
             "max_rel_dose_diff_vs_plain": worst}
 
 
+def batch_measurement(ctx, n_jobs: int = 64, seed: int = 20261204) -> dict:
+    """Batched projection radiography: the uneven DX jobs one job per launch
+    (resident worlds and LUTs, default launch parameters) against one batch with
+    per-class launch parameters and the chain count chosen by the autotuner."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    from dxmclib_gb300.autotune import Autotuner
+    from dxmclib_gb300.workloads import dx_batch
+
+    jobs = dx_batch(n_jobs=n_jobs, seed=seed)
+    prepared = []
+    for k, wl in enumerate(jobs):
+        src = wl.source
+        src.updateFromWorld(wl.world)
+        src.validate()
+        dw = dx.DeviceWorld(ctx, wl.world)
+        dl = dx.DeviceLut(ctx, dx.LutBlob.cached(wl.world.materialMap(), dw.max_density(), src.maxPhotonEnergyProduced()))
+        prepared.append((wl, dw, dl, src.exposures(wl.world.directionCosines()), src.spectrum(), src.heel(), 100 + k))
+    hist = int(sum(np.sum(p[3].n_histories) for p in prepared))
+    tuner = Autotuner(ctx, sample_histories=2_000_000, repeats=1, rounds=1)
+    launches = []
+    for wl, dw, dl, ex, spec, heel, sd in prepared:
+        r = tuner.tune_job(wl.world, dw, dl, ex, spec, heel, None, 1, wl.source.maxPhotonEnergyProduced())
+        launches.append(r["launch"])
+
+    def plain():
+        ms = 0.0
+        t = time.perf_counter()
+        for wl, dw, dl, ex, spec, heel, sd in prepared:
+            job = dx.Job(ctx, dw, dl, ex, spec, heel, None, seed=sd, model=1)
+            job.wait()
+            st = A.JobStats()
+            A.check(ctx.lib.dxmc_gpu_job_result(job.handle, A.OUTPUT_RAW, 1.0, None, None, None, dx.api.C.byref(st)),
+                    ctx.handle, "job_result")
+            ms += st.job_ms
+            job.close()
+        return ms, (time.perf_counter() - t) * 1e3
+
+    def entries():
+        return [dx.BatchEntry(dw, dl, ex, spec, heel, None, sd, 1, -1, launch)
+                for (wl, dw, dl, ex, spec, heel, sd), launch in zip(prepared, launches)]
+
+    chains = tuner.tune_chains(entries(), f"dx_batch_{n_jobs}")
+
+    def batched(mode, c):
+        t = time.perf_counter()
+        b = dx.Batch(ctx, entries(), mode=mode, chains=c)
+        b.wait()
+        ms = b.kernel_ms()
+        b.close()
+        return ms, (time.perf_counter() - t) * 1e3
+
+    plain()
+    batched(A.BATCH_CONCURRENT, chains["chains"])
+    p_ms, p_wall = plain()
+    b_ms, b_wall = batched(A.BATCH_CONCURRENT, chains["chains"])
+    batched(A.BATCH_PERSISTENT, 0)
+    pers_ms, _ = batched(A.BATCH_PERSISTENT, 0)
+    for wl, dw, dl, *_ in prepared:
+        dl.close()
+        dw.close()
+    classes = {k: v for k, v in tuner.cache.items() if k.startswith("job|")}
+    return {"workload": f"{n_jobs} DX jobs, grids 64^3-256^3, 70-90 kVp, 1e6-1e7 histories (seed {seed})",
+            "histories": hist,
+            "plain_histories_per_s": hist / (p_ms / 1e3), "plain_wall_histories_per_s": hist / (p_wall / 1e3),
+            "batched_histories_per_s": hist / (b_ms / 1e3), "batched_wall_histories_per_s": hist / (b_wall / 1e3),
+            "persistent_histories_per_s": hist / (pers_ms / 1e3),
+            "chains": chains["chains"], "chain_ms": chains["ms"],
+            "tuned_classes": {k: {"launch": v["launch"], "speedup": round(v["speedup"], 3)} for k, v in classes.items()}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -269,6 +340,8 @@ def main():
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--queue-log2", type=int, default=0, help="photon queue chunk 2^n (0 = default, -1 = in-kernel generation)")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-vs-plain mixed-stream leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched DX leg")
+    ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--serve-jobs", type=int, default=48)
     ap.add_argument("--serve-rates", default="25,100,200", help="Poisson arrival rates of the mixed stream (jobs/s)")
     ap.add_argument("--serve-chains", type=int, default=4)
@@ -413,6 +486,10 @@ def main():
     h2d = n_vox * 5 + len(exposures) * 80
     d2h = n_vox * (8 + 8 + 4)
 
+    batching = None
+    if rank == 0 and not args.no_batch:
+        batching = batch_measurement(ctx, args.batch_jobs)
+
     serving = None
     if rank == 0 and not args.no_serve:
         serving = serving_measurement(ctx, args.serve_jobs, [float(r) for r in args.serve_rates.split(",")],
@@ -447,6 +524,7 @@ def main():
             # per step: one generation pass and one transport launch per queue chunk
             "gpu_launches": args.steps * (1 if args.queue_log2 < 0 else 2 * max(1, -(-n_hist // (1 << (args.queue_log2 or 25))))),
             "clocks": clocks.summary(),
+            "batching": batching,
             "serving": serving,
         }
         print(json.dumps(line), flush=True)

@@ -118,6 +118,8 @@ class JobDesc(C.Structure):
         ("exposures", C.POINTER(Exposure)), ("n_exposures", C.c_uint64),
         ("spectrum", C.POINTER(SpectrumDesc)), ("heel", C.POINTER(HeelDesc)), ("bowtie", C.POINTER(BowtieDesc)),
         ("seed", C.c_uint64), ("model", C.c_int32), ("tally_mode", C.c_int32),
+        ("regen_threshold", C.c_int32), ("interact_threshold", C.c_int32), ("blocks_per_sm", C.c_int32),
+        ("queue_log2_chunk", C.c_int32),
     ]
 
 

@@ -946,11 +946,14 @@ class Job:
 
     def __init__(self, ctx: GpuContext, dworld: DeviceWorld, dlut: DeviceLut, exposures: ExposureTable,
                  spectrum: Optional[Spectrum] = None, heel: Optional[HeelTable] = None, bowtie=None,
-                 seed: int = 1, model: int = LOWENERGYCORRECTION.LIVERMORE, tally_mode: int = -1):
+                 seed: int = 1, model: int = LOWENERGYCORRECTION.LIVERMORE, tally_mode: int = -1,
+                 launch: Optional[dict] = None):
+        """``launch`` may set regen_threshold, interact_threshold, blocks_per_sm and
+        queue_log2_chunk for this job (an autotuner's choice); unset keys use the context's."""
         self.ctx = ctx
         self.dworld = dworld
         self._owned = True
-        jd = self._describe(exposures, spectrum, heel, bowtie, seed, model, tally_mode)
+        jd = self._describe(exposures, spectrum, heel, bowtie, seed, model, tally_mode, launch)
         self.handle = C.c_void_p()
         A.check(ctx.lib.dxmc_gpu_job_submit(ctx.handle, dworld.handle, dlut.handle, C.byref(jd), C.byref(self.handle)),
                 ctx.handle, "dxmc_gpu_job_submit")
@@ -963,7 +966,10 @@ class Job:
         j.ctx, j.dworld, j.handle, j._owned = ctx, dworld, handle, False
         return j
 
-    def _describe(self, exposures: ExposureTable, spectrum, heel, bowtie, seed, model, tally_mode) -> A.JobDesc:
+    LAUNCH_KEYS = ("regen_threshold", "interact_threshold", "blocks_per_sm", "queue_log2_chunk")
+
+    def _describe(self, exposures: ExposureTable, spectrum, heel, bowtie, seed, model, tally_mode,
+                  launch: Optional[dict] = None) -> A.JobDesc:
         self._keep = []
         jd = A.JobDesc()
         ex = exposures.to_c()
@@ -991,6 +997,10 @@ class Job:
         jd.seed = int(seed)
         jd.model = int(model)
         jd.tally_mode = int(tally_mode)
+        for k, v in (launch or {}).items():
+            if k not in self.LAUNCH_KEYS:
+                raise ValueError(f"unknown launch parameter {k}")
+            setattr(jd, k, int(v))
         self._keep.append(jd)
         return jd
 
@@ -1043,9 +1053,9 @@ class BatchEntry:
 
     def __init__(self, dworld: DeviceWorld, dlut: DeviceLut, exposures: ExposureTable, spectrum: Optional[Spectrum] = None,
                  heel: Optional[HeelTable] = None, bowtie=None, seed: int = 1, model: int = LOWENERGYCORRECTION.LIVERMORE,
-                 tally_mode: int = -1):
+                 tally_mode: int = -1, launch: Optional[dict] = None):
         self.dworld, self.dlut = dworld, dlut
-        self.args = (exposures, spectrum, heel, bowtie, seed, model, tally_mode)
+        self.args = (exposures, spectrum, heel, bowtie, seed, model, tally_mode, launch)
 
 
 class Batch:

@@ -783,12 +783,13 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     const uint64_t nv = world->params.n_voxels;
     const uint64_t tally_bytes = tally_mode == 1 ? nv * 2 * sizeof(float) : nv * 2 * sizeof(double);
     // photon queue: chunks of 2^k histories, 48 bytes per queued photon
-    const int log2_chunk = ctx->options.queue_log2_chunk == 0 ? 25 : ctx->options.queue_log2_chunk;
+    const int log2_option = jd->queue_log2_chunk != 0 ? jd->queue_log2_chunk : ctx->options.queue_log2_chunk;
+    const int log2_chunk = log2_option == 0 ? 25 : log2_option;
     uint64_t chunk = 0;
     if (log2_chunk >= 0 && qmode == QueueMode::own)
         chunk = std::min<uint64_t>(total, 1ull << std::min(log2_chunk, 34));
     else if (log2_chunk >= 0 && qmode == QueueMode::shared)
-        chunk = std::min<uint64_t>(total, shared_capacity);
+        chunk = std::min<uint64_t>({ total, shared_capacity, 1ull << std::min(log2_chunk, 34) });
     const uint64_t queue_bytes = qmode == QueueMode::own ? chunk * 48 : 0;
     const uint64_t job_bytes = tally_bytes + nv * sizeof(uint32_t) + table_bytes + sizeof(dev::JobCounters) + queue_bytes;
     if (ctx->in_use + job_bytes > ctx->budget)
@@ -890,11 +891,12 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
             p.uniform_hpe = jd->exposures[0].n_histories;
     }
     {
+        // job value, else context option, else the default for the generation mode
         const bool queued = chunk > 0;
-        p.regen_threshold = ctx->options.regen_threshold > 0 ? std::min(ctx->options.regen_threshold, 32)
-                                                           : (queued ? DEFAULT_QUEUE_REGEN_THRESHOLD : DEFAULT_REGEN_THRESHOLD);
-        p.interact_threshold = ctx->options.interact_threshold > 0 ? std::min(ctx->options.interact_threshold, 32)
-                                                                   : (queued ? DEFAULT_QUEUE_INTERACT_THRESHOLD : DEFAULT_INTERACT_THRESHOLD);
+        const int regen = jd->regen_threshold > 0 ? jd->regen_threshold : ctx->options.regen_threshold;
+        const int inter = jd->interact_threshold > 0 ? jd->interact_threshold : ctx->options.interact_threshold;
+        p.regen_threshold = regen > 0 ? std::min(regen, 32) : (queued ? DEFAULT_QUEUE_REGEN_THRESHOLD : DEFAULT_REGEN_THRESHOLD);
+        p.interact_threshold = inter > 0 ? std::min(inter, 32) : (queued ? DEFAULT_QUEUE_INTERACT_THRESHOLD : DEFAULT_INTERACT_THRESHOLD);
     }
 
 
@@ -923,8 +925,9 @@ struct LaunchPlan {
 };
 
 // Grid, block and shared memory of a job's transport kernel; sets p.lut_in_smem.
-LaunchPlan plan_launch(dxmc_gpu_ctx* ctx, const dxmc_world* world, const dxmc_lut* lut, int model, dev::TransportParams& p)
+LaunchPlan plan_launch(dxmc_gpu_ctx* ctx, const dxmc_world* world, const dxmc_lut* lut, const dxmc_job_desc* jd, dev::TransportParams& p)
 {
+    const int model = jd->model;
     LaunchPlan L;
     const size_t lut_bytes = static_cast<size_t>(lut->meta.total_floats) * sizeof(float);
     const size_t smem_limit = std::min<size_t>(ctx->max_smem_optin, 96 * 1024);
@@ -934,7 +937,8 @@ LaunchPlan plan_launch(dxmc_gpu_ctx* ctx, const dxmc_world* world, const dxmc_lu
     L.block = ctx->options.block_size > 0 ? ctx->options.block_size : 256;
     // also sets the kernel's dynamic shared-memory limit for this launch
     const int occ = dev::transport_max_blocks_per_sm(model, palette, L.block, L.smem);
-    int per_sm = ctx->options.blocks_per_sm > 0 ? ctx->options.blocks_per_sm : occ;
+    int per_sm = jd->blocks_per_sm > 0 ? std::min(jd->blocks_per_sm, std::max(occ, 1))
+                                        : (ctx->options.blocks_per_sm > 0 ? ctx->options.blocks_per_sm : occ);
     if (per_sm <= 0)
         per_sm = 1;
     L.grid = ctx->sm_count * per_sm;
@@ -994,7 +998,7 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
     const int rc = prepare_job(ctx, world, lut, jd, QueueMode::own, 0, &j, p, chunk);
     if (rc != DXMC_OK)
         return rc;
-    const LaunchPlan L = plan_launch(ctx, world, lut, jd->model, p);
+    const LaunchPlan L = plan_launch(ctx, world, lut, jd, p);
     const cudaError_t e = enqueue_job(j, p, jd->model, chunk, j->queue, L, ctx->stream, false);
     if (e != cudaSuccess) {
         cudaStreamSynchronize(ctx->stream);
@@ -1403,7 +1407,7 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
         }
         std::vector<LaunchPlan> plans(n);
         for (int i = 0; i < n; ++i) // occupancy queries and attributes stay outside the capture
-            plans[i] = plan_launch(ctx, entries[i].world, entries[i].lut, models[i], params[i]);
+            plans[i] = plan_launch(ctx, entries[i].world, entries[i].lut, entries[i].job, params[i]);
         for (int c = 0; c < chains && e == cudaSuccess; ++c) {
             if (lists[c].empty())
                 continue;

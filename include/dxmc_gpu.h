@@ -243,6 +243,11 @@ typedef struct dxmc_job_desc {
     uint64_t seed;                      /* counter-based RNG key */
     int32_t model;                      /* DXMC_MODEL_* */
     int32_t tally_mode;                 /* DXMC_TALLY_*; -1 = context default */
+    /* launch parameters of this job (0 = the context's; set by an autotuner) */
+    int32_t regen_threshold;            /* refill idle lanes once this many are idle (1..32) */
+    int32_t interact_threshold;         /* interaction passes once this many lanes wait (1..32) */
+    int32_t blocks_per_sm;              /* resident blocks per SM (1..occupancy limit) */
+    int32_t queue_log2_chunk;           /* photon queue chunk 2^n; -1 = photons generated in the kernel */
 } dxmc_job_desc;
 
 typedef struct dxmc_job_stats {

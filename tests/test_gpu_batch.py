@@ -106,3 +106,42 @@ def test_batch_rejects_incomplete_entries(gpu_ctx):
     rc = ctx.lib.dxmc_gpu_batch_submit(ctx.handle, arr, 1, None, C.byref(out))
     assert rc == A.DXMC_ERR_INVALID and not out.value
     assert b"incomplete" in ctx.lib.dxmc_gpu_last_error(ctx.handle)
+
+
+def test_autotuned_launch_gives_identical_results(gpu_ctx, tmp_path):
+    """Launch parameters change how the histories are scheduled, not which random
+    numbers they draw: a tuned job equals the default one, and the tuner's cache
+    file serves the second request."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    from dxmclib_gb300.autotune import Autotuner
+    from dxmclib_gb300.workloads import dx_batch
+
+    ctx = gpu_ctx
+    wl = dx_batch(n_jobs=1, seed=4321, histories_range=(400_000, 400_001))[0]
+    src = wl.source
+    src.updateFromWorld(wl.world)
+    src.validate()
+    dworld = dx.DeviceWorld(ctx, wl.world)
+    dlut = dx.DeviceLut(ctx, dx.LutBlob(wl.world.materialMap(), dworld.max_density(), src.maxPhotonEnergyProduced()))
+    ex = src.exposures(wl.world.directionCosines())
+    tuner = Autotuner(ctx, cache_file=str(tmp_path / "tune.json"), sample_histories=300_000, repeats=1, rounds=1)
+    res = tuner.tune_job(wl.world, dworld, dlut, ex, src.spectrum(), src.heel(), src.bowtie(), 1,
+                         src.maxPhotonEnergyProduced())
+    assert res["tuned_ms"] <= res["default_ms"] and res["trials"] >= 10
+    for k, v in res["launch"].items():
+        assert k in A.JobDesc.__dict__ or k in dict(A.JobDesc._fields_), k
+    again = Autotuner(ctx, cache_file=str(tmp_path / "tune.json"))
+    assert again.tune_job(wl.world, dworld, dlut, ex, None, None, None, 1, src.maxPhotonEnergyProduced()) == res
+    outs = []
+    for launch in (None, res["launch"], {"queue_log2_chunk": -1, "regen_threshold": 16, "interact_threshold": 4,
+                                          "blocks_per_sm": 2}):
+        job = dx.Job(ctx, dworld, dlut, ex, src.spectrum(), src.heel(), src.bowtie(), seed=5, model=1, launch=launch)
+        outs.append(job.result(A.OUTPUT_RAW))
+        job.close()
+    for o in outs[1:]:
+        np.testing.assert_allclose(o[0], outs[0][0], rtol=1e-9, atol=1e-12 * outs[0][0].max())
+        np.testing.assert_array_equal(o[2], outs[0][2])
+        assert o[3]["steps"] == outs[0][3]["steps"]
+    dlut.close()
+    dworld.close()
