@@ -341,6 +341,9 @@ def main():
     ap.add_argument("--queue-log2", type=int, default=0, help="photon queue chunk 2^n (0 = default, -1 = in-kernel generation)")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-vs-plain mixed-stream leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched DX leg")
+    ap.add_argument("--no-precision", action="store_true", help="skip the tally-precision study")
+    ap.add_argument("--precision-histories", type=float, default=1e9)
+    ap.add_argument("--precision-slices", type=int, default=400)
     ap.add_argument("--batch-jobs", type=int, default=64)
     ap.add_argument("--serve-jobs", type=int, default=48)
     ap.add_argument("--serve-rates", default="25,100,200", help="Poisson arrival rates of the mixed stream (jobs/s)")
@@ -486,6 +489,13 @@ def main():
     h2d = n_vox * 5 + len(exposures) * 80
     d2h = n_vox * (8 + 8 + 4)
 
+    precision = None
+    if rank == 0 and not args.no_precision:
+        from dxmclib_gb300 import precision as prec
+        from dxmclib_gb300.workloads import ct_helical
+        pw = ct_helical(nz=args.precision_slices, histories=int(args.precision_histories))
+        precision = {"workload": pw.name, **prec.study(ctx, pw.world, pw.source, repeats=1)}
+
     batching = None
     if rank == 0 and not args.no_batch:
         batching = batch_measurement(ctx, args.batch_jobs)
@@ -525,6 +535,7 @@ def main():
             "gpu_launches": args.steps * (1 if args.queue_log2 < 0 else 2 * max(1, -(-n_hist // (1 << (args.queue_log2 or 25))))),
             "clocks": clocks.summary(),
             "batching": batching,
+            "precision": precision,
             "serving": serving,
         }
         print(json.dumps(line), flush=True)

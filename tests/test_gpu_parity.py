@@ -222,3 +222,20 @@ def test_interaction_samplers_match_reference(gpu_ctx, golden, model):
             assert abs(d.astype(np.float64).mean() - ref_mean_dep) <= 0.002 * energy + 5 * d.std() / np.sqrt(N), key
     dlut.close()
     dworld.close()
+
+
+def test_tally_modes_against_fp64(gpu_ctx):
+    """FP32 atomics and warp FP32 partials flushed to FP64 against FP64 atomics on
+    identical per-history streams: only the summation differs, so the energy
+    imparted agrees to FP32 rounding (per voxel within 1e-3 above 1 % of the
+    maximum; total within 1e-5)."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import precision
+    from dxmclib_gb300.workloads import pencil_water
+    wl = pencil_water(n=32, histories=400_000)
+    res = precision.study(gpu_ctx, wl.world, wl.source, repeats=0)
+    for name in ("warp_fp32_to_fp64", "fp32"):
+        m = res["modes"][name]
+        assert m["voxels"] > 50, name
+        assert m["max_rel_err"] < 1e-3, (name, m)
+        assert m["total_energy_rel_err"] < 1e-5, (name, m)
