@@ -339,6 +339,7 @@ def main():
     ap.add_argument("--block-size", type=int, default=0)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--queue-log2", type=int, default=0, help="photon queue chunk 2^n (0 = default, -1 = in-kernel generation)")
+    ap.add_argument("--burst", type=int, default=0, help="Woodcock steps per loop iteration (0 = library default)")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-vs-plain mixed-stream leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched DX leg")
     ap.add_argument("--no-precision", action="store_true", help="skip the tally-precision study")
@@ -411,7 +412,8 @@ def main():
             dist.barrier()
 
     def run_job(seed):
-        job = dx.Job(ctx, dworld, dlut, exposures, spec, heel, None, seed=seed, model=args.model)
+        job = dx.Job(ctx, dworld, dlut, exposures, spec, heel, None, seed=seed, model=args.model,
+                     launch={"woodcock_burst": args.burst} if args.burst else None)
         job.wait()
         st = dx.api.A.JobStats()
         A.check(ctx.lib.dxmc_gpu_job_result(job.handle, A.OUTPUT_RAW, 1.0, None, None, None, dx.api.C.byref(st)),
@@ -520,7 +522,8 @@ def main():
                        "model": ["NONE", "LIVERMORE", "IA"][args.model], "tally": "fp64",
                        "l2": "inputs larger than L2 (420 MB voxels + 1 GB tallies)", "parallelism": f"replicas{ws}",
                        "voxel_layout": "palette-u8" if args.layout == 0 else "8-byte",
-                       "regen_threshold": args.regen or "default", "interact_threshold": args.interact or "default"},
+                       "regen_threshold": args.regen or "default", "interact_threshold": args.interact or "default",
+                       "woodcock_burst": args.burst or "default"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind,
                          # DRAM bytes per launch from the committed ncu capture of a 1e7-history

@@ -966,7 +966,7 @@ class Job:
         j.ctx, j.dworld, j.handle, j._owned = ctx, dworld, handle, False
         return j
 
-    LAUNCH_KEYS = ("regen_threshold", "interact_threshold", "blocks_per_sm", "queue_log2_chunk")
+    LAUNCH_KEYS = ("regen_threshold", "interact_threshold", "blocks_per_sm", "queue_log2_chunk", "woodcock_burst")
 
     def _describe(self, exposures: ExposureTable, spectrum, heel, bowtie, seed, model, tally_mode,
                   launch: Optional[dict] = None) -> A.JobDesc:

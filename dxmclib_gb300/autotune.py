@@ -11,7 +11,9 @@ model):
   refilled together (the refill cadence);
 * ``interact_threshold`` -- how many lanes must wait for an interaction before
   the per-type interaction passes run (the event-sorting cadence);
-* ``blocks_per_sm`` -- resident 256-thread blocks per SM (occupancy).
+* ``blocks_per_sm`` -- resident 256-thread blocks per SM (occupancy);
+* ``woodcock_burst`` -- Woodcock steps a lane may take per loop iteration before
+  the warp checks for refills and interactions again.
 
 For a job class (correction model, grid size in factors of 8, number of
 materials, maximum energy in 20 keV bins) the tuner times a sample of the job -- an even
@@ -41,8 +43,10 @@ SPACE: Dict[str, List[int]] = {
     "regen_threshold": [2, 4, 8, 12, 16],
     "interact_threshold": [4, 6, 8, 12],
     "blocks_per_sm": [2, 3, 4],
+    "woodcock_burst": [1, 2, 4, 8],
 }
-DEFAULTS = {"queue_log2_chunk": 25, "regen_threshold": 4, "interact_threshold": 8, "blocks_per_sm": 0}
+DEFAULTS = {"queue_log2_chunk": 25, "regen_threshold": 4, "interact_threshold": 8, "blocks_per_sm": 0,
+            "woodcock_burst": 0}
 CHAINS = [1, 2, 3, 4, 6]
 
 

@@ -25,6 +25,10 @@ constexpr int DEFAULT_REGEN_THRESHOLD = 12;       // photons generated in the tr
 constexpr int DEFAULT_INTERACT_THRESHOLD = 6;
 constexpr int DEFAULT_QUEUE_REGEN_THRESHOLD = 4;  // photons taken from the pre-generated queue
 constexpr int DEFAULT_QUEUE_INTERACT_THRESHOLD = 8;
+#ifndef DXMC_DEFAULT_WOODCOCK_BURST
+#define DXMC_DEFAULT_WOODCOCK_BURST 8
+#endif
+constexpr int DEFAULT_WOODCOCK_BURST = DXMC_DEFAULT_WOODCOCK_BURST; // Woodcock steps per loop iteration
 
 struct BatchEngines;
 
@@ -897,6 +901,7 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
         const int inter = jd->interact_threshold > 0 ? jd->interact_threshold : ctx->options.interact_threshold;
         p.regen_threshold = regen > 0 ? std::min(regen, 32) : (queued ? DEFAULT_QUEUE_REGEN_THRESHOLD : DEFAULT_REGEN_THRESHOLD);
         p.interact_threshold = inter > 0 ? std::min(inter, 32) : (queued ? DEFAULT_QUEUE_INTERACT_THRESHOLD : DEFAULT_INTERACT_THRESHOLD);
+        p.woodcock_burst = jd->woodcock_burst > 0 ? std::min(jd->woodcock_burst, 64) : DEFAULT_WOODCOCK_BURST;
     }
 
 
@@ -1751,6 +1756,8 @@ int ctx_regen_threshold(const dxmc_gpu_ctx* ctx)
 {
     return ctx->options.regen_threshold > 0 ? std::min(ctx->options.regen_threshold, 32) : DEFAULT_REGEN_THRESHOLD;
 }
+int default_woodcock_burst() { return DEFAULT_WOODCOCK_BURST; }
+
 int ctx_interact_threshold(const dxmc_gpu_ctx* ctx)
 {
     return ctx->options.interact_threshold > 0 ? std::min(ctx->options.interact_threshold, 32) : DEFAULT_INTERACT_THRESHOLD;

@@ -211,6 +211,7 @@ void ctx_set_error(dxmc_gpu_ctx* ctx, const std::string& msg);
 std::mutex& ctx_mutex(dxmc_gpu_ctx* ctx);
 int ctx_regen_threshold(const dxmc_gpu_ctx* ctx);
 int ctx_interact_threshold(const dxmc_gpu_ctx* ctx);
+int default_woodcock_burst();
 const dev::WorldParams* world_params(const dxmc_world* w, const dxmc_gpu_ctx** owner, int* n_materials);
 const float* lut_image(const dxmc_lut* l, dev::LutMeta* meta, const dxmc_gpu_ctx** owner);
 }
@@ -335,6 +336,7 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         p.uniform_hpe = 0; // exposure found by binary search over the prefix sums
         p.regen_threshold = capi::ctx_regen_threshold(ctx);
         p.interact_threshold = capi::ctx_interact_threshold(ctx);
+        p.woodcock_burst = jd->woodcock_burst > 0 ? std::min(jd->woodcock_burst, 64) : capi::default_woodcock_burst();
         const size_t lut_bytes = static_cast<size_t>(meta.total_floats) * sizeof(float);
         const size_t smem_limit = std::min<size_t>(capi::ctx_max_smem(ctx), 96 * 1024);
         p.lut_in_smem = lut_bytes <= smem_limit ? 1 : 0;

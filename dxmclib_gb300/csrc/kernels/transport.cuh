@@ -85,6 +85,8 @@ struct TransportParams {
     int lut_in_smem;
     int regen_threshold;    // refill finished lanes once at least this many are idle (1..32)
     int interact_threshold; // run the interaction passes once at least this many lanes wait (1..32)
+    int woodcock_burst;     // Woodcock steps a lane may take per loop iteration (1..64)
+    int pad_params;
 };
 
 // Work item of the batched kernel: histories [first, first + count) of job `job`.

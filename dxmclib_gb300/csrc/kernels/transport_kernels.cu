@@ -557,17 +557,26 @@ namespace {
                 s.updateMax = false;
                 s.cached_mat = -1;
             }
-            const float step = -__logf(s.rng.uniform_open()) * s.maxInv * 10.0f; // cm -> mm
-            s.ph.px = fmaf(s.ph.dx, step, s.ph.px);
-            s.ph.py = fmaf(s.ph.dy, step, s.ph.py);
-            s.ph.pz = fmaf(s.ph.dz, step, s.ph.pz);
-            if (!inside(w, s.ph.px, s.ph.py, s.ph.pz)) {
-                s.alive = false;
-            } else if (++s.hist_steps > MAX_STEPS_PER_HISTORY) {
-                // bounded work per history: end it and report the overflow
-                ++s.overflows;
-                s.alive = false;
-            } else {
+            // Up to p.woodcock_burst Woodcock steps per iteration: a lane keeps stepping
+            // through virtual collisions and stops at a real event, the grid boundary or a
+            // forced-scoring voxel.  Each lane draws its own stream in the reference's
+            // order, so the burst length changes the schedule, not the histories.
+            const int burst = max(p.woodcock_burst, 1); // at least one step: every iteration makes progress
+            for (int k = 0; k < burst; ++k) {
+                const float step = -__logf(s.rng.uniform_open()) * s.maxInv * 10.0f; // cm -> mm
+                s.ph.px = fmaf(s.ph.dx, step, s.ph.px);
+                s.ph.py = fmaf(s.ph.dy, step, s.ph.py);
+                s.ph.pz = fmaf(s.ph.dz, step, s.ph.pz);
+                if (!inside(w, s.ph.px, s.ph.py, s.ph.pz)) {
+                    s.alive = false;
+                    break;
+                }
+                if (++s.hist_steps > MAX_STEPS_PER_HISTORY) {
+                    // bounded work per history: end it and report the overflow
+                    ++s.overflows;
+                    s.alive = false;
+                    break;
+                }
                 const uint32_t ix = min(static_cast<uint32_t>((s.ph.px - w.lo[0]) * w.inv_spacing[0]), w.dims[0] - 1);
                 const uint32_t iy = min(static_cast<uint32_t>((s.ph.py - w.lo[1]) * w.inv_spacing[1]), w.dims[1] - 1);
                 const uint32_t iz = min(static_cast<uint32_t>((s.ph.pz - w.lo[2]) * w.inv_spacing[2]), w.dims[2] - 1);
@@ -589,8 +598,15 @@ namespace {
                     if (s.rng.uniform() < eventProb) {
                         const float r3 = s.rng.uniform() * attTot;
                         s.pending = r3 < s.att0 ? EV_PHOTO : (r3 < s.att0 + s.att1 ? EV_COMPTON : EV_RAYLEIGH);
-                    } else {
-                        check_roulette = true;
+                        break;
+                    }
+                    // virtual collision: Russian roulette (transport.hpp:684-694)
+                    if (s.ph.energy * s.ph.weight < ROULETTE_THRESHOLD) {
+                        if (s.rng.uniform() < ROULETTE_PROBABILITY) {
+                            s.alive = false;
+                            break;
+                        }
+                        s.ph.weight *= 1.0f / (1.0f - ROULETTE_PROBABILITY);
                     }
                 } else {
                     // forced photoelectric scoring (computeInteractionsForced): score the forced
@@ -611,6 +627,7 @@ namespace {
                         s.forced_wc = 0.0f;
                         check_roulette = true;
                     }
+                    break; // the forced deposit is scored before the next step
                 }
             }
         }
