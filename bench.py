@@ -338,7 +338,7 @@ def main():
     ap.add_argument("--layout", type=int, default=0, help="0 = compact palette when possible, 1 = 8-byte voxels")
     ap.add_argument("--block-size", type=int, default=0)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
-    ap.add_argument("--queue-log2", type=int, default=0, help="photon queue chunk 2^n (0 = default, -1 = in-kernel generation)")
+    ap.add_argument("--queue-log2", type=int, default=0, help="photon queue chunk 2^n (0 = default: in-kernel generation)")
     ap.add_argument("--burst", type=int, default=0, help="Woodcock steps per loop iteration (0 = library default)")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-vs-plain mixed-stream leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched DX leg")
@@ -534,8 +534,8 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "histories/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps},
-            # per step: one generation pass and one transport launch per queue chunk
-            "gpu_launches": args.steps * (1 if args.queue_log2 < 0 else 2 * max(1, -(-n_hist // (1 << (args.queue_log2 or 25))))),
+            # per step: the transport kernel, or one generation pass and one transport launch per queue chunk
+            "gpu_launches": args.steps * (1 if args.queue_log2 <= 0 else 2 * max(1, -(-n_hist // (1 << args.queue_log2)))),
             "clocks": clocks.summary(),
             "batching": batching,
             "precision": precision,

@@ -747,6 +747,9 @@ class GpuContext:
         self.lib = A.load()
         opts = A.GpuOptions(device, block_size, blocks_per_sm, tally_mode, memory_budget, regen_threshold,
                             interact_threshold, queue_log2_chunk, 0)
+        self.options = dict(device=device, block_size=block_size, blocks_per_sm=blocks_per_sm, tally_mode=tally_mode,
+                            memory_budget=memory_budget, regen_threshold=regen_threshold,
+                            interact_threshold=interact_threshold, queue_log2_chunk=queue_log2_chunk)
         self.handle = C.c_void_p()
         self._children = weakref.WeakSet()
         A.check(self.lib.dxmc_gpu_ctx_create(C.byref(opts), C.byref(self.handle)), None, "dxmc_gpu_ctx_create")

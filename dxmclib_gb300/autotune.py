@@ -39,14 +39,14 @@ import numpy as np
 from . import _capi as A
 
 SPACE: Dict[str, List[int]] = {
-    "queue_log2_chunk": [-1, 23, 25],
-    "regen_threshold": [2, 4, 8, 12, 16],
+    "queue_log2_chunk": [23, 25, 0],
+    "regen_threshold": [4, 8, 12, 16],
     "interact_threshold": [4, 6, 8, 12],
     "blocks_per_sm": [2, 3, 4],
     "woodcock_burst": [1, 2, 4, 8],
 }
-DEFAULTS = {"queue_log2_chunk": 25, "regen_threshold": 4, "interact_threshold": 8, "blocks_per_sm": 0,
-            "woodcock_burst": 0}
+DEFAULTS = {"queue_log2_chunk": 0, "regen_threshold": 0, "interact_threshold": 0, "blocks_per_sm": 0,
+            "woodcock_burst": 0}  # 0: the library's default
 CHAINS = [1, 2, 3, 4, 6]
 
 

@@ -21,14 +21,18 @@ using namespace dxmc_gb300;
 
 // Warp scheduling of the transport kernel: refill idle lanes once this many
 // are idle; run the per-type interaction passes once this many lanes wait.
-constexpr int DEFAULT_REGEN_THRESHOLD = 12;       // photons generated in the transport kernel
-constexpr int DEFAULT_INTERACT_THRESHOLD = 6;
+constexpr int DEFAULT_REGEN_THRESHOLD = 8;        // photons generated in the transport kernel
+constexpr int DEFAULT_INTERACT_THRESHOLD = 8;
 constexpr int DEFAULT_QUEUE_REGEN_THRESHOLD = 4;  // photons taken from the pre-generated queue
 constexpr int DEFAULT_QUEUE_INTERACT_THRESHOLD = 8;
 #ifndef DXMC_DEFAULT_WOODCOCK_BURST
 #define DXMC_DEFAULT_WOODCOCK_BURST 8
 #endif
 constexpr int DEFAULT_WOODCOCK_BURST = DXMC_DEFAULT_WOODCOCK_BURST; // Woodcock steps per loop iteration
+// Photons are generated inside the transport kernel unless a job or the context
+// asks for a pre-generated queue (2^n photons per generation pass): with the
+// Woodcock burst the in-kernel generation is as fast and needs no queue memory.
+constexpr int DEFAULT_QUEUE_LOG2 = -1;
 
 struct BatchEngines;
 
@@ -788,7 +792,7 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     const uint64_t tally_bytes = tally_mode == 1 ? nv * 2 * sizeof(float) : nv * 2 * sizeof(double);
     // photon queue: chunks of 2^k histories, 48 bytes per queued photon
     const int log2_option = jd->queue_log2_chunk != 0 ? jd->queue_log2_chunk : ctx->options.queue_log2_chunk;
-    const int log2_chunk = log2_option == 0 ? 25 : log2_option;
+    const int log2_chunk = log2_option == 0 ? DEFAULT_QUEUE_LOG2 : log2_option;
     uint64_t chunk = 0;
     if (log2_chunk >= 0 && qmode == QueueMode::own)
         chunk = std::min<uint64_t>(total, 1ull << std::min(log2_chunk, 34));
@@ -1285,7 +1289,7 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
         if (cudaEventSynchronize(g->done) != cudaSuccess)
             return fail(ctx, DXMC_ERR_DEVICE, "previous batch of the engine failed");
     } else {
-        const int log2_chunk = ctx->options.queue_log2_chunk == 0 ? 25 : ctx->options.queue_log2_chunk;
+        const int log2_chunk = ctx->options.queue_log2_chunk == 0 ? DEFAULT_QUEUE_LOG2 : ctx->options.queue_log2_chunk;
         const int rc = ensure_chains(ctx, *en, chains, log2_chunk >= 0 ? 1ull << std::min(log2_chunk, 34) : 0);
         if (rc != DXMC_OK)
             return rc;

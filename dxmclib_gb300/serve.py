@@ -172,8 +172,10 @@ class GpuBackend:
         self.pool = _PinnedPool(ctx.lib)
         self.luts: "collections.OrderedDict[Hashable, Any]" = collections.OrderedDict()
         self.max_luts = 256
-        # the chains' photon-queue buffers (allocated by the first batch) are kept out of admission
-        self.chain_reserve = chains * 48 * (1 << 25)
+        # the chains' photon-queue buffers (allocated by the first batch, only when the context
+        # pre-generates photons) are kept out of admission
+        log2 = getattr(ctx, "options", {}).get("queue_log2_chunk", 0)
+        self.chain_reserve = chains * 48 * (1 << log2) if log2 > 0 else 0
 
     def memory(self):
         return self.ctx.memory()

@@ -190,8 +190,8 @@ typedef struct dxmc_gpu_options {
     uint64_t memory_budget;  /* admission budget in bytes, 0 = 90% of free memory */
     int32_t regen_threshold; /* refill finished lanes of a warp once this many are idle; 0 = default */
     int32_t interact_threshold; /* run the per-type interaction passes once this many lanes wait; 0 = default */
-    int32_t queue_log2_chunk;   /* photons are pre-generated in chunks of 2^n histories (48 B per photon);
-                                   0 = default (2^25), -1 = generate inside the transport kernel */
+    int32_t queue_log2_chunk;   /* n > 0: photons are pre-generated in chunks of 2^n histories (48 B per
+                                   photon); 0 = default (generated inside the transport kernel); -1 = inside */
     int32_t pad;
 } dxmc_gpu_options;
 
