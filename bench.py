@@ -50,6 +50,22 @@ def _dist():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, dist=None, device: str = "cuda") -> float:
+    """The largest value over the ranks (the slowest replica's time)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(ws: int, histories_per_step: int, steps: int, seconds_max: float) -> float:
+    """Whole-job throughput of N independent replicas: all ranks' histories over the
+    slowest rank's time (weak scaling)."""
+    return ws * histories_per_step * steps / seconds_max
+
+
 class ClockSampler:
     """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
 
@@ -429,12 +445,8 @@ def main():
         barrier()
     job_ms = np.array([s.job_ms for s in stats])
     kern_ms = np.array([s.kernel_ms for s in stats])
-    total_ms = float(job_ms.sum())
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = ws * n_hist * args.steps / (total_ms / 1e3)
+    total_ms = max_over_ranks(float(job_ms.sum()), dist)
+    value = replica_throughput(ws, n_hist, args.steps, total_ms / 1e3)
     steps_per_hist = float(np.mean([s.steps for s in stats])) / n_hist
     deps_per_hist = float(np.mean([s.deposits for s in stats])) / n_hist
     alg_bytes = 5.0 * np.mean([s.steps for s in stats]) + 20.0 * np.mean([s.deposits for s in stats])
@@ -483,11 +495,8 @@ def main():
             e2e_step(3000 + s)
         barrier()
         e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = ws * n_hist * e2e_steps / e2e_s if e2e_steps else None
+    e2e_s = max_over_ranks(e2e_s, dist)
+    e2e_value = replica_throughput(ws, n_hist, e2e_steps, e2e_s) if e2e_steps else None
     h2d = n_vox * 5 + len(exposures) * 80
     d2h = n_vox * (8 + 8 + 4)
 
