@@ -388,7 +388,7 @@ class Source:
     def bowtie(self):
         return None
 
-    def getCalibrationValue(self, model=LOWENERGYCORRECTION.NONE) -> float:
+    def getCalibrationValue(self, model=LOWENERGYCORRECTION.NONE, transport=None) -> float:
         return 1.0
 
 
@@ -426,7 +426,7 @@ class PencilSource(Source):
         return ExposureTable.build(np.tile(self._position, (n, 1)), np.tile(self._cosines, (n, 1)), (0, 0, 0, 0),
                                    1.0, self._hpe, min(max(self._energy, 0.0), 500.0), world_cosines)
 
-    def getCalibrationValue(self, model=LOWENERGYCORRECTION.NONE):
+    def getCalibrationValue(self, model=LOWENERGYCORRECTION.NONE, transport=None):
         """source.hpp:238-246: airDose / (N * E * mu_en(air) * keV->mJ)."""
         air = Material("Air, Dry (near sea level)")
         n = self.totalExposures() * self.historiesPerExposure()
@@ -516,6 +516,22 @@ class DXSource(Source):
     @staticmethod
     def _zero_cosines():
         return np.array([-1.0, 0, 0, 0, 0, 1.0])
+
+    def setDap(self, gycm2: float):
+        if gycm2 > 0.0:
+            self._dap = float(gycm2)
+
+    def dap(self) -> float:
+        return self._dap
+
+    def getCalibrationValue(self, model=LOWENERGYCORRECTION.NONE, transport=None) -> float:
+        """source.hpp:552-568: DAP / (N * sum_E E * w(E) * mu_en,air(E)) over the normalised spectrum."""
+        air = Material("Air, Dry (near sea level)")
+        e = self._tube.getEnergy()
+        w = self._tube.getSpecter(e)
+        out = sum(float(k) * float(wt) * _mass_energy_absorption(air, float(k)) for k, wt in zip(e, w))
+        out *= self.totalExposures() * self.historiesPerExposure()
+        return self._dap / out
 
     def tube(self) -> "Tube":
         return self._tube
@@ -674,6 +690,63 @@ class CTSpiralSource(Source):
 
     def totalExposures(self):
         return int(self._scan * 2 * PI / (self._collimation * self._pitch * self._step))
+
+    def scanLenght(self):
+        return self._scan
+
+    def pitch(self):
+        return self._pitch
+
+    def setCtdiVol(self, ctdivol: float):
+        if ctdivol > 0.0:
+            self._ctdivol = float(ctdivol)
+
+    def ctdiVol(self) -> float:
+        return getattr(self, "_ctdivol", 1.0)
+
+    def setCtdiPhantomDiameter(self, mm: int):
+        self._ctdi_diameter = max(int(mm), 160)
+
+    def ctdiPhantomDiameter(self) -> int:
+        return getattr(self, "_ctdi_diameter", 320)
+
+    def exposuresPerRotatition(self) -> int:
+        return int(2 * PI / self._step)
+
+    def calibration_exposures(self, histories_per_exposure: int, world_cosines=(1, 0, 0, 0, 1, 0)) -> ExposureTable:
+        """Exposures of the axial copy that ctCalibration runs (source.hpp:937-942,
+        1203-1255): one rotation about the phantom axis at the origin, the
+        source's angles, tilt, collimation and field of view."""
+        n = self.exposuresPerRotatition()
+        idx = np.arange(n, dtype=np.float64)
+        pos0 = np.array([0.0, -self._sdd / 2, 0.0])
+        angle = self._start + self._step * idx
+        cos = np.tile(np.array([-1.0, 0, 0, 0, 0, 1.0]), (n, 1))
+        tilt_axis = np.array([1.0, 0, 0])
+        tilt_corr = _rotate(pos0, tilt_axis, self._tilt)
+        rot_axis = _rotate(cos[:, 3:], tilt_axis, self._tilt)
+        other = _rotate(cos[:, :3], tilt_axis, self._tilt)
+        pos = _rotate(np.tile(pos0, (n, 1)), rot_axis, angle)
+        pos[:, 2] += tilt_corr[2]
+        other = _rotate(other, rot_axis, angle)
+        cosines = np.concatenate([other, rot_axis], axis=1)
+        coll_x = math.atan(self._fov / self._sdd) * 2.0
+        coll_y = math.atan(self._collimation / self._sdd) * 2.0
+        coll = (-coll_x / 2, coll_x / 2, -coll_y / 2, coll_y / 2)
+        return ExposureTable.build(pos, cosines, coll, 1.0, histories_per_exposure, 0.0, world_cosines)
+
+    def getCalibrationValue(self, model=LOWENERGYCORRECTION.NONE, transport=None) -> float:
+        """CTSpiralSource::getCalibrationValue (source.hpp:1358-1363): the CTDI
+        calibration of the axial copy (ctCalibration, source.hpp:925-988), run as a
+        GPU job, times the pitch."""
+        from . import calibration as cal
+        ctx = transport.context() if transport is not None else GpuContext()
+        mean_weight = float(np.mean(self.exposures().weight))
+        hpe = cal.calibration_histories_per_exposure(self.exposuresPerRotatition(), self.historiesPerExposure())
+        world = cal.CTDIPhantom(self.ctdiPhantomDiameter())
+        ex = self.calibration_exposures(hpe, world.directionCosines())
+        dose, _, _ = cal.run_ctdi(ctx, world, ex, self.spectrum(), self.heel(), self.bowtie(), int(model))
+        return cal.ctdi_factor(world, dose, self._collimation, self.ctdiVol(), mean_weight) * self._pitch
 
     def exposures(self, world_cosines=(1, 0, 0, 0, 1, 0)):
         n = self.totalExposures()
@@ -1169,7 +1242,7 @@ class Transport:
         job.wait()
         sim_time = time.perf_counter() - t0
         if self._mode == Transport.DOSE:
-            cal = source.getCalibrationValue(self._model) if useSourceDoseCalibration else 1.0
+            cal = source.getCalibrationValue(self._model, transport=self) if useSourceDoseCalibration else 1.0
             dose, var, nev, stats = job.result(A.OUTPUT_DOSE, cal)
             units = "mGy" if useSourceDoseCalibration else "keV/kg"
         else:

@@ -100,7 +100,8 @@ struct RefWorldDesc {
 };
 
 // Source types
-enum { REF_PENCIL = 0, REF_ISOTROPIC = 1, REF_DX = 2, REF_CTSPIRAL = 3, REF_CTAXIAL = 4, REF_CBCT = 5, REF_ISOTROPIC_CT = 6 };
+enum { REF_PENCIL = 0, REF_ISOTROPIC = 1, REF_DX = 2, REF_CTSPIRAL = 3, REF_CTAXIAL = 4, REF_CBCT = 5, REF_ISOTROPIC_CT = 6,
+    REF_CT_CALIBRATION = 7 }; // the axial copy a CT spiral source calibrates with (source.hpp:925-950)
 
 struct RefSourceDesc {
     int type;
@@ -244,6 +245,21 @@ std::unique_ptr<Source<double>> make_source(const RefSourceDesc& s)
         p->setSpanAngleDeg(s.span_deg);
         p->setStepAngleDeg(s.step_deg);
         p->setModelHeelEffect(s.heel != 0);
+        p->setHistoriesPerExposure(s.histories_per_exposure);
+        return p;
+    }
+    case REF_CT_CALIBRATION: {
+        // CTSpiralSource::getCalibrationValue copies the source into a CTAxialSource
+        // (source.hpp:1358-1363, 1603-1608); ctCalibration then aligns it with the
+        // phantom axis, centres it and scans one collimation (source.hpp:937-942)
+        RefSourceDesc sp = s;
+        sp.type = REF_CTSPIRAL;
+        auto spiral = make_source(sp);
+        auto p = std::make_unique<CTAxialSource<double>>(*dynamic_cast<CTSpiralSource<double>*>(spiral.get()));
+        p->setDirectionCosines(std::array<double, 6> { -1, 0, 0, 0, 0, 1 });
+        p->setPosition(std::array<double, 3> { 0, 0, 0 });
+        p->setScanLenght(p->collimation());
+        p->setUseXCareFilter(false);
         p->setHistoriesPerExposure(s.histories_per_exposure);
         return p;
     }
@@ -505,6 +521,77 @@ int ref_transport(const RefWorldDesc* wd, const RefSourceDesc* sd, int model, in
     meta[0] = static_cast<double>(res.numberOfHistories);
     meta[1] = res.simulationTime.count();
     return res.numberOfHistories > 0 ? 0 : -3;
+}
+
+// CTDIPhantom<double> (world.hpp:229-390): arrays and the five hole index lists
+// (Center, West, East, South, North).  Sizes are queried with null arrays.
+int ref_ctdi_phantom(int diameter, std::uint64_t* dims, double* density, std::uint8_t* material, std::uint8_t* measurement,
+    std::uint64_t* hole_counts, std::uint64_t* hole_indices, std::uint64_t hole_cap)
+{
+    CTDIPhantom<double> w(static_cast<std::size_t>(diameter));
+    const auto d = w.dimensions();
+    for (int k = 0; k < 3; ++k)
+        dims[k] = d[k];
+    const std::size_t n = w.size();
+    if (density) {
+        const auto& dens = *w.densityArray();
+        const auto& mat = *w.materialIndexArray();
+        const auto& meas = *w.measurementMapArray();
+        for (std::size_t i = 0; i < n; ++i) {
+            density[i] = dens[i];
+            material[i] = mat[i];
+            measurement[i] = meas[i];
+        }
+    }
+    using H = CTDIPhantom<double>::HolePosition;
+    const H order[5] = { H::Center, H::West, H::East, H::South, H::North };
+    std::uint64_t off = 0;
+    for (int h = 0; h < 5; ++h) {
+        const auto& idx = w.holeIndices(order[h]);
+        hole_counts[h] = idx.size();
+        if (hole_indices) {
+            if (off + idx.size() > hole_cap)
+                return -1;
+            for (auto v : idx)
+                hole_indices[off++] = v;
+        }
+    }
+    return 0;
+}
+
+// CTSpiralSource<double>::getCalibrationValue (source.hpp:1358-1363 -> ctCalibration,
+// source.hpp:925-988): the reference's CTDI calibration factor, run with its own
+// Transport<double> on n_threads workers.  meta: [axial exposures per rotation,
+// histories per exposure of the calibration run, mean exposure weight].
+int ref_ct_calibration(const RefSourceDesc* sd, int model, int n_threads, double ctdivol, int diameter, double* factor,
+    double* meta)
+{
+    if (sd->type != REF_CTSPIRAL)
+        return -1;
+    auto base = make_source(*sd);
+    auto* spiral = dynamic_cast<CTSpiralSource<double>*>(base.get());
+    if (!spiral)
+        return -2;
+    spiral->setCtdiVol(ctdivol);
+    spiral->setCtdiPhantomDiameter(static_cast<std::uint64_t>(diameter));
+    if (n_threads > 0) {
+        // Transport's default worker count is hardware_concurrency; ctCalibration
+        // constructs its own Transport, so the count cannot be passed through.
+    }
+    spiral->validate();
+    CTAxialSource<double> axial(*spiral);
+    double meanWeight = 0;
+    for (std::uint64_t i = 0; i < spiral->totalExposures(); ++i)
+        meanWeight += spiral->getExposure(i).beamIntensityWeight();
+    meanWeight /= static_cast<double>(spiral->totalExposures());
+    std::size_t stat = CTDIPhantom<double>::ctdiMinHistories() / (axial.exposuresPerRotatition() * axial.historiesPerExposure());
+    if (stat < 1)
+        stat = 1;
+    meta[0] = static_cast<double>(axial.exposuresPerRotatition());
+    meta[1] = static_cast<double>(axial.historiesPerExposure() * stat);
+    meta[2] = meanWeight;
+    *factor = spiral->getCalibrationValue(static_cast<LOWENERGYCORRECTION>(model), nullptr);
+    return 0;
 }
 
 } // extern "C"

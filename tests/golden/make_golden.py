@@ -13,7 +13,10 @@ tests/golden/ref_binding.py and stores, as small .npz files:
                     pencil-beam and heterogeneous cone-beam cases, stored
                     for voxels above 0.2 % of the maximum dose plus depth and
                     lateral profiles and the total energy imparted;
-* interactions_*.npz histograms of the reference interaction samplers.
+* interactions_*.npz histograms of the reference interaction samplers;
+* ctdi_phantom.npz  CTDIPhantom arrays and hole lists (world.hpp:229-390);
+* ct_calibration_m1.npz the reference's CT calibration factor and the tables of
+                    the axial copy it runs (source.hpp:925-988).
 
 Usage:  make -C oracle && python tests/golden/make_golden.py [--quick]
 The generator needs the reference checkout and is not run by the test suite.
@@ -205,6 +208,44 @@ def gen_interactions(out: Path, quick: bool):
     np.savez_compressed(out / "interactions_bone.npz", n=N, **res)
 
 
+def gen_ctdi(out: Path, quick: bool):
+    """CTDIPhantom<double> (world.hpp:229-390) arrays and hole lists, and the reference's
+    CT calibration factor (source.hpp:925-988) with the exact exposure, spectrum and
+    heel tables of the axial copy it runs, so the GPU calibration consumes the same inputs."""
+    phantoms = {}
+    for d in (160, 320):
+        dims, dens, mat, meas, counts, holes = R.ctdi_phantom(d)
+        phantoms[f"d{d}_dims"] = np.array(dims)
+        phantoms[f"d{d}_counts"] = np.array(counts)
+        phantoms[f"d{d}_holes"] = holes.astype(np.uint32)
+        phantoms[f"d{d}_material_counts"] = np.bincount(mat, minlength=3)
+        phantoms[f"d{d}_densities"] = np.unique(dens)
+        if d == 160:
+            phantoms["d160_material"] = mat
+            phantoms["d160_measurement"] = meas
+    np.savez_compressed(out / "ctdi_phantom.npz", **phantoms)
+    hpe = 1000
+    s = R.SourceArgs(R.CTSPIRAL, position=(0, 0, 0), kvp=120, al_mm=2.5, ct_collimation=40, pitch=1.0,
+                     scan_length=100, angle_step_deg=1.0, start_angle_deg=0, fov=500, sdd=1190, heel=1,
+                     histories_per_exposure=hpe)
+    t = time.time()
+    factor, meta = R.ct_calibration(s, model=1, ctdivol=1.0, diameter=320)
+    seconds = time.time() - t
+    print(f"ct calibration: factor {factor:.6e}, {meta[0] * meta[1]:.3e} histories, {seconds:.1f} s", flush=True)
+    cal = R.SourceArgs(R.CT_CALIBRATION, position=(0, 0, 0), kvp=120, al_mm=2.5, ct_collimation=40, pitch=1.0,
+                       scan_length=100, angle_step_deg=1.0, start_angle_deg=0, fov=500, sdd=1190, heel=1,
+                       histories_per_exposure=int(meta[1]))
+    dims, dens, mat, meas, counts, holes = R.ctdi_phantom(320)
+    w = R.WorldArgs(dims, (1.0, 1.0, 2.5), dens, mat, ["Air, Dry (near sea level)", "Air, Dry (near sea level)",
+                                                       "Polymethyl Methacralate (Lucite, Perspex)"], measurement=meas)
+    tabs = R.source_tables(cal, w)
+    np.savez_compressed(out / "ct_calibration_m1.npz", factor=factor, exposures_per_rotation=meta[0],
+                        calibration_hpe=meta[1], mean_weight=meta[2], seconds=seconds, ctdivol=1.0, diameter=320,
+                        collimation=40.0, pitch=1.0, exposures=tabs["exposures"], spec_energies=tabs["spec_energies"],
+                        spec_weights=tabs["spec_weights"], heel_meta=tabs["heel_meta"],
+                        heel_weights=tabs.get("heel_weights", np.zeros(0)), max_energy=tabs["max_energy"])
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true")
@@ -215,7 +256,7 @@ def main():
     out = HERE
     steps = dict(lut=lambda: gen_lut(out), alias=lambda: gen_alias(out), sources=lambda: gen_sources(out),
                  transport=lambda: gen_transport(out, a.quick), ct=lambda: gen_ct(out, a.quick),
-                 interactions=lambda: gen_interactions(out, a.quick))
+                 interactions=lambda: gen_interactions(out, a.quick), ctdi=lambda: gen_ctdi(out, a.quick))
     for name, fn in steps.items():
         if a.only and name not in a.only.split(","):
             continue

@@ -239,3 +239,38 @@ def interactions(world: WorldArgs, max_energy: float, model: int, kind: int, ene
     if rc != 0:
         raise RuntimeError(f"ref_interactions failed: {rc}")
     return hc, he, sums
+
+
+CT_CALIBRATION = 7  # the axial copy a CT spiral source calibrates with
+
+
+def ctdi_phantom(diameter: int):
+    """CTDIPhantom<double> arrays and hole index lists (Center, West, East, South, North)."""
+    dims = (C.c_uint64 * 3)()
+    counts = (C.c_uint64 * 5)()
+    rc = lib().ref_ctdi_phantom(C.c_int(diameter), dims, None, None, None, counts, None, C.c_uint64(0))
+    if rc != 0:
+        raise RuntimeError(f"ref_ctdi_phantom failed: {rc}")
+    n = dims[0] * dims[1] * dims[2]
+    dens = np.zeros(n)
+    mat = np.zeros(n, np.uint8)
+    meas = np.zeros(n, np.uint8)
+    total = int(sum(counts))
+    holes = np.zeros(total, np.uint64)
+    rc = lib().ref_ctdi_phantom(C.c_int(diameter), dims, _dptr(dens), mat.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                meas.ctypes.data_as(C.POINTER(C.c_uint8)), counts,
+                                holes.ctypes.data_as(C.POINTER(C.c_uint64)), C.c_uint64(total))
+    if rc != 0:
+        raise RuntimeError(f"ref_ctdi_phantom failed: {rc}")
+    return (tuple(int(d) for d in dims), dens, mat, meas, [int(c) for c in counts], holes)
+
+
+def ct_calibration(source: "SourceArgs", model: int, ctdivol: float, diameter: int):
+    """CTSpiralSource<double>::getCalibrationValue with the reference's own transport."""
+    factor = C.c_double(0)
+    meta = np.zeros(3)
+    rc = lib().ref_ct_calibration(C.byref(source.desc), C.c_int(model), C.c_int(0), C.c_double(ctdivol),
+                                  C.c_int(diameter), C.byref(factor), _dptr(meta))
+    if rc != 0:
+        raise RuntimeError(f"ref_ct_calibration failed: {rc}")
+    return factor.value, meta

@@ -239,3 +239,38 @@ def test_tally_modes_against_fp64(gpu_ctx):
         assert m["voxels"] > 50, name
         assert m["max_rel_err"] < 1e-3, (name, m)
         assert m["total_energy_rel_err"] < 1e-5, (name, m)
+
+
+def test_ct_calibration_matches_reference(gpu_ctx, golden):
+    """CTDI calibration (source.hpp:925-988) as a GPU job: the reference's axial
+    calibration tables on the CTDI phantom (forced scoring in the holes) give the
+    reference's factor.  Three reference runs of 1e8 histories spread by 0.7 %;
+    the tolerance is 2 %."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import calibration as cal
+    g = golden("ct_calibration_m1.npz")
+    world = cal.CTDIPhantom(int(g["diameter"]))
+    ex = g["exposures"]
+    table = dx.ExposureTable(ex[:, 0:3].copy(), ex[:, 3:9].copy(), ex[:, 9:12].copy(), ex[:, 12:16].copy(),
+                             ex[:, 16].copy(), ex[:, 17].astype(np.uint64), np.zeros(len(ex)))
+    spec = dx.Spectrum(g["spec_energies"], g["spec_weights"])
+    hm = g["heel_meta"]
+    heel = dx.HeelTable(hm[1], hm[2], int(hm[3]), hm[4], hm[5], int(hm[6]), g["heel_weights"])
+    dose, var, stats = cal.run_ctdi(gpu_ctx, world, table, spec, heel, None, model=1)
+    assert stats["histories"] == int(np.sum(table.n_histories))
+    factor = cal.ctdi_factor(world, dose, float(g["collimation"]), float(g["ctdivol"]), float(g["mean_weight"]))
+    factor *= float(g["pitch"])
+    ref = float(g["factor"])
+    assert abs(factor / ref - 1.0) < 0.02, (factor, ref)
+
+    # the source's own calibration (project tube spectrum) runs end to end and feeds DOSE mode
+    src = dx.CTSpiralSource()
+    src.tube().setVoltage(120.0)
+    src.tube().setAlFiltration(2.5)
+    src.setCollimation(40.0)
+    src.setScanLenght(40.0)
+    src.setHistoriesPerExposure(1000)
+    src.setCtdiVol(10.0)
+    tr = dx.Transport(gpu_ctx)
+    f = src.getCalibrationValue(1, transport=tr)
+    assert np.isfinite(f) and f > 0
