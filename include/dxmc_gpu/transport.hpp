@@ -313,7 +313,7 @@ public:
             double cal = 1.0;
             if (m_mode == OUTPUTMODE::DOSE) {
                 mode = DXMC_OUTPUT_DOSE;
-                cal = useSourceDoseCalibration ? static_cast<double>(source->getCalibrationValue(m_model, progressbar)) : 1.0;
+                cal = useSourceDoseCalibration ? static_cast<double>(calibrationValue(source, progressbar)) : 1.0;
             }
             ok = check(dxmc_gpu_job_result(job, mode, cal, dose.data(), var.data(), result.nEvents.data(), nullptr), "job result");
             if (ok) {
@@ -343,7 +343,59 @@ public:
         return result;
     }
 
+    // Source::getCalibrationValue, with the CTDI calibration run of CT spiral and axial
+    // sources (CTBaseSource::ctCalibration, source.hpp:925-988) done by this GPU transport
+    // instead of a second CPU transport; other sources keep their own (closed-form) value.
+    T calibrationValue(Source<T>* source, ProgressBar<T>* progressbar = nullptr)
+    {
+        if (auto* spiral = dynamic_cast<CTSpiralSource<T>*>(source)) {
+            CTAxialSource<T> copy(*spiral); // source.hpp:1358-1363
+            return ctCalibration(copy) * spiral->pitch();
+        }
+        if (auto* axial = dynamic_cast<CTAxialSource<T>*>(source)) {
+            CTAxialSource<T> copy(*axial); // source.hpp:1277-1281
+            return ctCalibration(copy);
+        }
+        return source->getCalibrationValue(m_model, progressbar);
+    }
+
 private:
+    T ctCalibration(CTAxialSource<T>& copy)
+    {
+        T meanWeight = 0;
+        for (std::uint64_t i = 0; i < copy.totalExposures(); ++i)
+            meanWeight += copy.getExposure(i).beamIntensityWeight();
+        meanWeight /= copy.totalExposures();
+        copy.setDirectionCosines(std::array<T, 6> { -1, 0, 0, 0, 0, 1 });
+        copy.setPosition(std::array<T, 3> { 0, 0, 0 });
+        copy.setScanLenght(copy.collimation());
+        copy.setUseXCareFilter(false);
+        std::size_t stat = CTDIPhantom<T>::ctdiMinHistories() / (copy.exposuresPerRotatition() * copy.historiesPerExposure());
+        stat = std::max<std::size_t>(stat, 1);
+        CTDIPhantom<T> world(copy.ctdiPhantomDiameter());
+        copy.updateFromWorld(world);
+        copy.setHistoriesPerExposure(copy.historiesPerExposure() * stat);
+        copy.validate();
+        const OUTPUTMODE mode = m_mode;
+        m_mode = OUTPUTMODE::DOSE;
+        auto result = (*this)(world, &copy, nullptr, false);
+        m_mode = mode;
+        if (result.numberOfHistories == 0)
+            return T { 0 };
+        using H = typename CTDIPhantom<T>::HolePosition;
+        const H order[5] = { H::Center, H::West, H::East, H::South, H::North };
+        T measured[5] {};
+        for (int i = 0; i < 5; ++i) {
+            const auto& idx = world.holeIndices(order[i]);
+            for (auto v : idx)
+                measured[i] += result.dose[v];
+            measured[i] /= static_cast<T>(idx.size());
+        }
+        const T periphery = (measured[1] + measured[2] + measured[3] + measured[4]) / T { 4 };
+        const T ctdiw = (measured[0] + 2 * periphery) / 3 * T { 100 } / copy.collimation();
+        return copy.ctdiVol() / ctdiw / meanWeight;
+    }
+
     bool ensure_context()
     {
         if (m_ctx)
