@@ -267,6 +267,24 @@ def serving_measurement(ctx, n_jobs: int, rates, chains: int, seed: int = 202612
             "max_rel_dose_diff_vs_plain": worst}
 
 
+def siddon_measurement(ctx, dworld, dlut, world, n_rays: int = 1 << 20, seed: int = 5) -> dict:
+    """Siddon traversal throughput: rays from the 1 m source circle through random
+    points of the resident CT grid (a projection-like pattern), 40-120 keV."""
+    rng = np.random.default_rng(seed)
+    ext = np.array(world.matrixExtent()).reshape(3, 2)
+    lo, hi = ext[:, 0], ext[:, 1]
+    ang = rng.uniform(0, 2 * np.pi, n_rays)
+    src = np.stack([500 * np.cos(ang), 500 * np.sin(ang), rng.uniform(lo[2], hi[2], n_rays)], 1)
+    tgt = rng.uniform(lo, hi, (n_rays, 3))
+    rays = np.concatenate([src, tgt - src, rng.uniform(40, 120, (n_rays, 1))], 1).astype(np.float32)
+    dworld.radiological_path(dlut, rays[:1024])
+    t = time.perf_counter()
+    out = dworld.radiological_path(dlut, rays)
+    wall = time.perf_counter() - t
+    return {"rays": n_rays, "rays_per_s_e2e": n_rays / wall, "mean_path": float(out.mean()),
+            "note": "host rays in, host results out (28 B + 8 B per ray over the link)"}
+
+
 def batch_measurement(ctx, n_jobs: int = 64, seed: int = 20261204) -> dict:
     """Batched projection radiography: the uneven DX jobs one job per launch
     (resident worlds and LUTs, default launch parameters) against one batch with
@@ -359,6 +377,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the served-vs-plain mixed-stream leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched DX leg")
     ap.add_argument("--no-precision", action="store_true", help="skip the tally-precision study")
+    ap.add_argument("--no-siddon", action="store_true", help="skip the Siddon traversal leg")
     ap.add_argument("--precision-histories", type=float, default=1e9)
     ap.add_argument("--precision-slices", type=int, default=400)
     ap.add_argument("--batch-jobs", type=int, default=64)
@@ -500,6 +519,10 @@ def main():
     h2d = n_vox * 5 + len(exposures) * 80
     d2h = n_vox * (8 + 8 + 4)
 
+    siddon = None
+    if rank == 0 and not args.no_siddon:
+        siddon = siddon_measurement(ctx, dworld, dlut, world)
+
     precision = None
     if rank == 0 and not args.no_precision:
         from dxmclib_gb300 import precision as prec
@@ -548,6 +571,7 @@ def main():
             "clocks": clocks.summary(),
             "batching": batching,
             "precision": precision,
+            "siddon": siddon,
             "serving": serving,
         }
         print(json.dumps(line), flush=True)

@@ -877,6 +877,16 @@ class DeviceWorld:
         A.check(ctx.lib.dxmc_gpu_world_upload(ctx.handle, C.byref(d), C.byref(self.handle)), ctx.handle, "dxmc_gpu_world_upload")
         ctx._register(self)
 
+    def radiological_path(self, dlut: "DeviceLut", rays) -> np.ndarray:
+        """Siddon traversal (dxmc_gpu_radiological_path): ``rays`` (n, 7) origin (mm, grid
+        frame), direction, energy (keV); returns sum mu/rho * density * length (cm)."""
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 7)
+        out = np.zeros(len(r))
+        A.check(self.ctx.lib.dxmc_gpu_radiological_path(self.ctx.handle, self.handle, dlut.handle,
+                                                        r.ctypes.data_as(A.FP), len(r), out.ctypes.data_as(A.DP)),
+                self.ctx.handle, "dxmc_gpu_radiological_path")
+        return out
+
     def max_density(self) -> np.ndarray:
         n = len(self.world.materialMap())
         out = np.zeros(n)

@@ -32,6 +32,7 @@ CUDA_SOURCES = [
     CSRC / "kernels" / "transport_kernels.cu",
     CSRC / "device" / "capi_device.cu",
     CSRC / "device" / "noalloc.cu",
+    CSRC / "kernels" / "siddon_kernels.cu",
 ]
 INCLUDES = [f"-I{REPO / 'include'}", f"-I{CSRC}"]
 

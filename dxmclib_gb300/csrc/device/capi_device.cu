@@ -500,6 +500,8 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     for (int i = 0; i < 3; ++i) {
         P.dims[i] = static_cast<uint32_t>(d->dims[i]);
         P.inv_spacing[i] = static_cast<float>(1.0 / static_cast<double>(static_cast<float>(d->spacing[i])));
+        P.spacing[i] = static_cast<float>(d->spacing[i]);
+        P.lower[i] = static_cast<float>(d->origin[i] - 0.5 * static_cast<double>(d->dims[i]) * d->spacing[i]);
     }
     world_extents(d->dims, d->spacing, d->origin, P.lo, P.hi);
     P.nxy = d->dims[0] * d->dims[1];
@@ -1707,6 +1709,39 @@ void dxmc_gpu_job_free(dxmc_job* j)
         cudaEventDestroy(j->stop);
     ctx->in_use -= j->bytes;
     delete j;
+}
+
+int dxmc_gpu_radiological_path(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const float* rays, uint64_t n_rays,
+    double* out)
+{
+    if (!ctx || !world || !lut || !rays || !out || n_rays == 0)
+        return DXMC_ERR_INVALID;
+    if (world->ctx != ctx || lut->ctx != ctx)
+        return fail(ctx, DXMC_ERR_INVALID, "world or lut belongs to another context");
+    if (lut->meta.n_materials < world->n_materials)
+        return fail(ctx, DXMC_ERR_INVALID, "lut has fewer materials than the world");
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    float* d_rays = nullptr;
+    double* d_out = nullptr;
+    cudaError_t e = cudaMallocAsync(&d_rays, n_rays * 7 * sizeof(float), s);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&d_out, n_rays * sizeof(double), s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_rays, rays, n_rays * 7 * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = dev::launch_radiological_path(world->params, lut->image, lut->meta, d_rays, n_rays, d_out, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out, d_out, n_rays * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (d_rays)
+        cudaFreeAsync(d_rays, s);
+    if (d_out)
+        cudaFreeAsync(d_out, s);
+    const cudaError_t se = cudaStreamSynchronize(s);
+    if (e == cudaSuccess)
+        e = se;
+    return e == cudaSuccess ? DXMC_OK : cuda_fail(ctx, e, "radiological path");
 }
 
 int dxmc_gpu_probe_lut(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, const double* energies, int n, double* out_att, double* out_maxinv)

@@ -24,6 +24,8 @@ struct WorldParams {
     float lo[3];          // nextafter-safe lower extent (world.hpp:55-68)
     float hi[3];          // nextafter-safe upper extent
     float inv_spacing[3]; // 1 / spacing (mm)
+    float spacing[3];     // voxel size (mm)
+    float lower[3];       // lower grid corner (mm), the plane of voxel boundary 0
     uint64_t nxy;
     uint64_t n_voxels;
 };
@@ -130,6 +132,10 @@ cudaError_t launch_postprocess(const double* tally, const uint32_t* n_events, co
     int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream);
 cudaError_t launch_postprocess_f32(const float* tally, const uint32_t* n_events, const Voxel* voxels, uint64_t n,
     int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream);
+// Radiological path of n rays (Siddon traversal): rays are 7 floats each
+// (origin mm, direction, energy keV); out[i] = sum of mu * density * length (cm).
+cudaError_t launch_radiological_path(const WorldParams& w, const float* lut, LutMeta meta, const float* rays, uint64_t n,
+    double* out, cudaStream_t stream);
 cudaError_t launch_max_density(const Voxel* voxels, uint64_t n, unsigned int* out_bits, int n_materials, cudaStream_t stream);
 cudaError_t launch_probe_lut(const float* lut, LutMeta meta, int material, const double* energies, int n, double* out_att, double* out_maxinv, cudaStream_t stream);
 cudaError_t launch_probe_interactions(const float* lut, LutMeta meta, int material, int model, int kind, float energy,

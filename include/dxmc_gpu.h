@@ -319,6 +319,17 @@ int dxmc_gpu_batch_job(dxmc_batch* batch, int index, dxmc_job** job);
 double dxmc_gpu_batch_kernel_ms(dxmc_batch* batch);
 void dxmc_gpu_batch_free(dxmc_batch* batch);
 
+/* ---- Siddon traversal --------------------------------------------------------- */
+/* No counterpart in the reference (which tracks photons with Woodcock steps only;
+ * docs/sphinx/physicsmodel.rst:27).  Radiological path of straight rays through
+ * the world: `rays` holds n_rays records of 7 floats (origin x, y, z in mm in the
+ * world's grid frame, direction x, y, z (normalised here), energy in keV); the
+ * part of each ray from its origin onwards is traversed voxel by voxel and
+ * out[i] = sum over crossed voxels of mu_total(E, material) / rho * density *
+ * length (cm), so exp(-out[i]) is the primary transmission.  Host buffers; blocks. */
+int dxmc_gpu_radiological_path(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const float* rays, uint64_t n_rays,
+                               double* out);
+
 /* ---- transport without allocation ------------------------------------------ */
 /* No counterpart in the reference.  Runs the same transport as
  * dxmc_gpu_job_submit + dxmc_gpu_job_result(DXMC_OUTPUT_RAW) for callers that
