@@ -82,7 +82,7 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1
     return c;
 }
 
-// Per-history random stream: xoshiro128** (Blackman and Vigna, "Scrambled
+// Per-history random stream: xoshiro128+ (Blackman and Vigna, "Scrambled
 // linear pseudorandom number generators", 2021), a 32-bit-native generator,
 // with its 128-bit state drawn from Philox4x32-10 keyed by the job seed with
 // the history id as counter.  Every history has its own stream, so a job can be
@@ -99,9 +99,11 @@ struct Rng {
         s2 = r.z;
         s3 = r.w | 1u; // the all-zero state is excluded
     }
+    // the sum output of xoshiro128+: its lowest bits are weak, and every use
+    // takes the high bits (24-bit floats, multiply-high integers)
     __device__ __forceinline__ uint32_t next()
     {
-        const uint32_t result = __funnelshift_l(s1 * 5u, s1 * 5u, 7) * 9u;
+        const uint32_t result = s0 + s3;
         const uint32_t t = s1 << 9;
         s2 ^= s0;
         s3 ^= s1;

@@ -482,12 +482,13 @@ namespace {
         Rng rng;
         bool alive;
         int pending;
-        float maxInv, logE;
+        float stepK, logE; // Woodcock step = -log2(u) * stepK (mm): 10 * ln 2 / majorant
         int seg;
         bool updateMax;
         int cached_mat;
         uint32_t hist_steps;
-        float att0, att1, att2;
+        float probInv;  // attenuation of the current material / majorant (event probability per unit density)
+        float p0, p01;  // photoelectric and photoelectric + Compton shares of the attenuation
         uint64_t vidx;
         float forced_wc; // weight correction waiting for a forced-voxel interaction pass
         uint32_t steps, deposits, overflows, histories;
@@ -553,7 +554,7 @@ namespace {
             if (s.updateMax) {
                 s.logE = __log10f(s.ph.energy);
                 s.seg = lut_segment(L, m, s.logE);
-                s.maxInv = lut_max_inverse(L, m, s.logE, s.seg);
+                s.stepK = lut_max_inverse(L, m, s.logE, s.seg) * (10.0f * 0.693147180559945f); // cm -> mm, log2 -> ln
                 s.updateMax = false;
                 s.cached_mat = -1;
             }
@@ -563,7 +564,7 @@ namespace {
             // order, so the burst length changes the schedule, not the histories.
             const int burst = max(p.woodcock_burst, 1); // at least one step: every iteration makes progress
             for (int k = 0; k < burst; ++k) {
-                const float step = -__logf(s.rng.uniform_open()) * s.maxInv * 10.0f; // cm -> mm
+                const float step = -__log2f(s.rng.uniform_open()) * s.stepK;
                 s.ph.px = fmaf(s.ph.dx, step, s.ph.px);
                 s.ph.py = fmaf(s.ph.dy, step, s.ph.py);
                 s.ph.pz = fmaf(s.ph.dz, step, s.ph.pz);
@@ -577,27 +578,36 @@ namespace {
                     s.alive = false;
                     break;
                 }
-                const uint32_t ix = min(static_cast<uint32_t>((s.ph.px - w.lo[0]) * w.inv_spacing[0]), w.dims[0] - 1);
-                const uint32_t iy = min(static_cast<uint32_t>((s.ph.py - w.lo[1]) * w.inv_spacing[1]), w.dims[1] - 1);
-                const uint32_t iz = min(static_cast<uint32_t>((s.ph.pz - w.lo[2]) * w.inv_spacing[2]), w.dims[2] - 1);
-                s.vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
+                // (p - lo) / spacing as one FMA; a tiny negative value converts to 0
+                const uint32_t ix = min(static_cast<uint32_t>(fmaf(s.ph.px, w.inv_spacing[0], -w.lo_inv[0])), w.dims[0] - 1);
+                const uint32_t iy = min(static_cast<uint32_t>(fmaf(s.ph.py, w.inv_spacing[1], -w.lo_inv[1])), w.dims[1] - 1);
+                const uint32_t iz = min(static_cast<uint32_t>(fmaf(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2])), w.dims[2] - 1);
+                if (w.n_voxels <= 0xffffffffull)
+                    s.vidx = iz * static_cast<uint32_t>(w.nxy) + (iy * w.dims[0] + ix);
+                else
+                    s.vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
                 float density;
                 int mat;
                 bool measured;
                 gather_voxel<PALETTE>(w, pal, s.vidx, density, mat, measured);
                 ++s.steps;
                 if (mat != s.cached_mat) {
-                    lut_attenuation(L, m, mat, s.logE, s.seg, s.att0, s.att1, s.att2);
+                    float a0, a1, a2;
+                    lut_attenuation(L, m, mat, s.logE, s.seg, a0, a1, a2);
+                    const float attTot = a0 + a1 + a2;
+                    const float inv = 1.0f / attTot;
+                    s.probInv = attTot * s.stepK * (1.0f / (10.0f * 0.693147180559945f));
+                    s.p0 = a0 * inv;
+                    s.p01 = (a0 + a1) * inv;
                     s.cached_mat = mat;
                 }
-                const float attTot = s.att0 + s.att1 + s.att2;
-                const float eventProb = attTot * density * s.maxInv;
+                const float eventProb = s.probInv * density;
                 if (!measured) {
                     // naive sampling (computeInteractions): decide the event type now,
                     // run it in the interaction pass
                     if (s.rng.uniform() < eventProb) {
-                        const float r3 = s.rng.uniform() * attTot;
-                        s.pending = r3 < s.att0 ? EV_PHOTO : (r3 < s.att0 + s.att1 ? EV_COMPTON : EV_RAYLEIGH);
+                        const float r3 = s.rng.uniform();
+                        s.pending = r3 < s.p0 ? EV_PHOTO : (r3 < s.p01 ? EV_COMPTON : EV_RAYLEIGH);
                         break;
                     }
                     // virtual collision: Russian roulette (transport.hpp:684-694)
@@ -612,7 +622,7 @@ namespace {
                     // forced photoelectric scoring (computeInteractionsForced): score the forced
                     // photoelectric share now; a real Compton or Rayleigh event goes through the
                     // interaction passes and the weight correction (1 - wc) is applied after it
-                    const float photoProb = s.att0 / attTot;
+                    const float photoProb = s.p0;
                     s.forced_wc = eventProb * photoProb;
                     {
                         Photon forced = s.ph;
@@ -621,7 +631,7 @@ namespace {
                         do_score = true;
                     }
                     if (s.rng.uniform() < eventProb * (1.0f - photoProb)) {
-                        s.pending = s.rng.uniform() * (s.att1 + s.att2) < s.att1 ? EV_COMPTON : EV_RAYLEIGH;
+                        s.pending = s.rng.uniform() * (1.0f - s.p0) < s.p01 - s.p0 ? EV_COMPTON : EV_RAYLEIGH;
                     } else {
                         s.ph.weight *= (1.0f - s.forced_wc);
                         s.forced_wc = 0.0f;
