@@ -75,7 +75,7 @@ def test_invalid_input_and_budget_are_refused(gpu_ctx):
         dx.Job(ctx, dworld, dlut, wl.source.exposures(), None, None, None, model=7)
     assert e.value.status == A.DXMC_ERR_INVALID
     # a context whose budget is smaller than the world
-    tiny = dx.GpuContext(memory_budget=1 << 16)
+    tiny = dx.GpuContext(memory_budget=1 << 12)  # 4 KB: less than the 32 KB of voxels
     with pytest.raises(A.DxmcError) as e:
         dx.DeviceWorld(tiny, wl.world)
     assert e.value.status == A.DXMC_ERR_OOM
