@@ -472,6 +472,11 @@ namespace {
         }
     }
 
+#ifndef DXMC_RAYLEIGH_THRESHOLD
+#define DXMC_RAYLEIGH_THRESHOLD 2 // lanes waiting for a Rayleigh event before its pass runs alone
+#endif
+    constexpr int RAYLEIGH_THRESHOLD = DXMC_RAYLEIGH_THRESHOLD;
+
 #ifndef DXMC_MIN_BLOCKS_PER_SM
 #define DXMC_MIN_BLOCKS_PER_SM 4 // resident 256-thread blocks per SM the register budget must allow (64 registers)
 #endif
@@ -657,9 +662,15 @@ namespace {
 
         // ---- interaction passes, one converged pass per event type ---------------------
         {
+            // Rayleigh events are rare (about one in ten interactions here), so their pass
+            // waits until RAYLEIGH_THRESHOLD lanes have one, or until nothing else can run
+            const unsigned ray = __ballot_sync(FULL_MASK, s.pending == EV_RAYLEIGH);
             const unsigned waiting = __ballot_sync(FULL_MASK, s.pending != EV_NONE);
             const unsigned can_step = __ballot_sync(FULL_MASK, s.alive && s.pending == EV_NONE);
-            if (waiting && (__popc(waiting) >= interact_t || can_step == 0u || drain)) {
+            const unsigned waiting_other = waiting & ~ray;
+            const bool stuck = can_step == 0u || drain;
+            const bool run_ray = ray && (__popc(ray) >= RAYLEIGH_THRESHOLD || stuck);
+            if ((waiting_other && (__popc(waiting_other) >= interact_t || stuck)) || run_ray) {
                 const int mat = s.cached_mat;
                 if (__any_sync(FULL_MASK, s.pending == EV_PHOTO) && s.pending == EV_PHOTO) {
                     const float e = photo_absorption<MODEL>(L, m, s.ph, mat, s.rng);
@@ -690,13 +701,13 @@ namespace {
                         }
                     }
                 }
-                if (__any_sync(FULL_MASK, s.pending == EV_RAYLEIGH) && s.pending == EV_RAYLEIGH) {
+                if (run_ray && s.pending == EV_RAYLEIGH) {
                     if (!rayleigh_scatter<MODEL>(L, m, s.ph, mat, s.rng)) {
                         ++s.overflows;
                         s.alive = false;
                     }
                 }
-                if (s.pending != EV_NONE) {
+                if (s.pending != EV_NONE && (s.pending != EV_RAYLEIGH || run_ray)) {
                     if (s.alive && s.forced_wc != 0.0f)
                         s.ph.weight *= (1.0f - s.forced_wc);
                     s.forced_wc = 0.0f;
