@@ -55,6 +55,7 @@ struct dxmc_world {
     dev::Voxel* voxels = nullptr;
     uint8_t* palette_index = nullptr;      // compact layout, null if not used
     dev::PaletteEntry* palette = nullptr;
+    std::vector<dev::PaletteEntry> host_palette; // compact layout: the distinct voxels
     uint64_t dims[3] {};
     double spacing[3] {};
     double origin[3] {};
@@ -367,9 +368,7 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     uint8_t* d_material = nullptr;
     uint8_t* d_meas = nullptr;
     unsigned int* d_bad = nullptr;
-    cudaError_t e = cudaMalloc(&w->voxels, bytes);
-    if (e == cudaSuccess)
-        e = cudaMallocAsync(&d_density, n * sizeof(float), ctx->stream);
+    cudaError_t e = cudaMallocAsync(&d_density, n * sizeof(float), ctx->stream);
     if (e == cudaSuccess)
         e = cudaMallocAsync(&d_material, n, ctx->stream);
     if (e == cudaSuccess && d->measurement)
@@ -388,7 +387,6 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     if (e == cudaSuccess) {
         const int grid = ctx->sm_count * 8;
         check_materials_kernel<<<grid, 256, 0, ctx->stream>>>(d_material, n, d->n_materials, d_bad);
-        pack_voxels_kernel<<<grid, 256, 0, ctx->stream>>>(d_density, d_material, d_meas, n, w->voxels);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)
@@ -436,9 +434,9 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(d_slots, slot_index.data(), PALETTE_TABLE, cudaMemcpyHostToDevice, ctx->stream);
             if (e == cudaSuccess)
-                e = cudaMalloc(&w->palette_index, n);
+                e = cudaMallocAsync(&w->palette_index, n, ctx->stream);
             if (e == cudaSuccess)
-                e = cudaMalloc(&w->palette, dev::PALETTE_MAX * sizeof(dev::PaletteEntry));
+                e = cudaMallocAsync(&w->palette, dev::PALETTE_MAX * sizeof(dev::PaletteEntry), ctx->stream);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(w->palette, palette.data(), palette.size() * sizeof(dev::PaletteEntry), cudaMemcpyHostToDevice, ctx->stream);
             if (e == cudaSuccess) {
@@ -447,6 +445,15 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
             }
             if (d_slots)
                 cudaFreeAsync(d_slots, ctx->stream);
+        }
+    }
+    // the 8-byte layout only when the compact one is not used (too many distinct voxels, or asked for)
+    if (e == cudaSuccess && !w->palette_index) {
+        palette.clear();
+        e = cudaMallocAsync(&w->voxels, bytes, ctx->stream);
+        if (e == cudaSuccess) {
+            pack_voxels_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(d_density, d_material, d_meas, n, w->voxels);
+            e = cudaGetLastError();
         }
     }
     if (d_table)
@@ -463,23 +470,17 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
         cudaFreeAsync(d_bad, ctx->stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) {
+    if (e != cudaSuccess || bad) {
         if (w->voxels)
-            cudaFree(w->voxels);
+            cudaFreeAsync(w->voxels, ctx->stream);
         if (w->palette_index)
-            cudaFree(w->palette_index);
+            cudaFreeAsync(w->palette_index, ctx->stream);
         if (w->palette)
-            cudaFree(w->palette);
+            cudaFreeAsync(w->palette, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
         delete w;
-        return cuda_fail(ctx, e, "world upload");
-    }
-    if (bad) {
-        cudaFree(w->voxels);
-        if (w->palette_index)
-            cudaFree(w->palette_index);
-        if (w->palette)
-            cudaFree(w->palette);
-        delete w;
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "world upload");
         return fail(ctx, DXMC_ERR_INVALID, "invalid world: material index >= n_materials");
     }
     for (int i = 0; i < 3; ++i) {
@@ -490,7 +491,8 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     std::memcpy(w->cosines, d->direction_cosines, sizeof(w->cosines));
     w->n_materials = d->n_materials;
     w->has_measurement = d->measurement != nullptr;
-    w->bytes = bytes + (w->palette_index ? n + dev::PALETTE_MAX * sizeof(dev::PaletteEntry) : 0);
+    w->bytes = w->palette_index ? n + dev::PALETTE_MAX * sizeof(dev::PaletteEntry) : bytes;
+    w->host_palette = palette;
     ctx->in_use += w->bytes;
     auto& P = w->params;
     P.voxels = w->voxels;
@@ -518,6 +520,17 @@ int dxmc_gpu_world_max_density(dxmc_world* w, double* out, int n_materials)
         return DXMC_ERR_INVALID;
     dxmc_gpu_ctx* ctx = w->ctx;
     std::lock_guard<std::mutex> lock(ctx->mutex);
+    if (w->palette_index) {
+        // the palette holds every distinct (density, material) pair of the grid
+        for (int i = 0; i < n_materials; ++i)
+            out[i] = 0.0;
+        for (const auto& pe : w->host_palette) {
+            const int mat = static_cast<int>(pe.code & 0xffu);
+            if (mat < n_materials)
+                out[mat] = std::max(out[mat], static_cast<double>(std::max(pe.density, 0.0f)));
+        }
+        return DXMC_OK;
+    }
     cudaSetDevice(ctx->device);
     unsigned int* d_bits = nullptr;
     DXMC_CUDA(ctx, cudaMallocAsync(&d_bits, n_materials * sizeof(unsigned int), ctx->stream));
@@ -541,12 +554,14 @@ void dxmc_gpu_world_free(dxmc_world* w)
         return;
     std::lock_guard<std::mutex> lock(w->ctx->mutex);
     cudaSetDevice(w->ctx->device);
-    sync_ctx_streams(w->ctx);
-    cudaFree(w->voxels);
+    sync_ctx_streams(w->ctx); // no queued batch or job still reads the grid
+    if (w->voxels)
+        cudaFreeAsync(w->voxels, w->ctx->stream);
     if (w->palette_index)
-        cudaFree(w->palette_index);
+        cudaFreeAsync(w->palette_index, w->ctx->stream);
     if (w->palette)
-        cudaFree(w->palette);
+        cudaFreeAsync(w->palette, w->ctx->stream);
+    cudaStreamSynchronize(w->ctx->stream);
     w->ctx->in_use -= w->bytes;
     delete w;
 }
@@ -619,12 +634,17 @@ int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* b, dxmc_lut** ou
     lut->ctx = ctx;
     lut->meta = m;
     lut->bytes = img.size() * sizeof(float);
-    cudaError_t e = cudaMalloc(&lut->image, lut->bytes);
+    cudaError_t e = cudaMallocAsync(&lut->image, lut->bytes, ctx->stream);
     if (e == cudaSuccess)
-        e = cudaMemcpy(lut->image, img.data(), lut->bytes, cudaMemcpyHostToDevice);
+        e = cudaMemcpyAsync(lut->image, img.data(), lut->bytes, cudaMemcpyHostToDevice, ctx->stream);
+    const cudaError_t se = cudaStreamSynchronize(ctx->stream); // img is a local buffer
+    if (e == cudaSuccess)
+        e = se;
     if (e != cudaSuccess) {
-        if (lut->image)
-            cudaFree(lut->image);
+        if (lut->image) {
+            cudaFreeAsync(lut->image, ctx->stream);
+            cudaStreamSynchronize(ctx->stream);
+        }
         delete lut;
         return cuda_fail(ctx, e, "lut upload");
     }
@@ -639,8 +659,9 @@ void dxmc_gpu_lut_free(dxmc_lut* lut)
         return;
     std::lock_guard<std::mutex> lock(lut->ctx->mutex);
     cudaSetDevice(lut->ctx->device);
-    sync_ctx_streams(lut->ctx);
-    cudaFree(lut->image);
+    sync_ctx_streams(lut->ctx); // no queued batch or job still reads the table
+    cudaFreeAsync(lut->image, lut->ctx->stream);
+    cudaStreamSynchronize(lut->ctx->stream);
     lut->ctx->in_use -= lut->bytes;
     delete lut;
 }
@@ -1622,9 +1643,9 @@ int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double
             const double vv = j->world->spacing[0] * j->world->spacing[1] * j->world->spacing[2] / 1000.0;
             cudaError_t e;
             if (j->tally_mode == 1)
-                e = dev::launch_postprocess_f32(j->tally_f32, j->n_events, j->world->voxels, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, s);
+                e = dev::launch_postprocess_f32(j->tally_f32, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, s);
             else
-                e = dev::launch_postprocess(j->tally, j->n_events, j->world->voxels, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, s);
+                e = dev::launch_postprocess(j->tally, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, s);
             if (e == cudaSuccess && dose)
                 e = cudaMemcpyAsync(dose, d_dose, nv * sizeof(double), cudaMemcpyDeviceToHost, s);
             if (e == cudaSuccess && variance)

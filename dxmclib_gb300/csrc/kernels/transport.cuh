@@ -129,9 +129,10 @@ cudaError_t launch_transport(const TransportParams& p, int model, int grid, int 
 int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem);
 // dynamic shared memory the transport kernel needs for a LUT image of lut_bytes
 size_t transport_smem_bytes(size_t lut_bytes, bool lut_in_smem, bool palette);
-cudaError_t launch_postprocess(const double* tally, const uint32_t* n_events, const Voxel* voxels, uint64_t n,
+// Post-processing of the tallies into dose / variance (densities from the world's layout).
+cudaError_t launch_postprocess(const double* tally, const WorldParams& w, uint64_t n,
     int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream);
-cudaError_t launch_postprocess_f32(const float* tally, const uint32_t* n_events, const Voxel* voxels, uint64_t n,
+cudaError_t launch_postprocess_f32(const float* tally, const WorldParams& w, uint64_t n,
     int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream);
 // Radiological path of n rays (Siddon traversal): rays are 7 floats each
 // (origin mm, direction, energy keV); out[i] = sum of mu * density * length (cm).

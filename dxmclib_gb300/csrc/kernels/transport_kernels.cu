@@ -1002,7 +1002,8 @@ namespace {
 
     // ---- post-processing (transport.hpp:780-816) -------------------------------------
     template <typename TallyT>
-    __global__ void postprocess_kernel(const TallyT* __restrict__ tally, const Voxel* __restrict__ voxels, uint64_t n, int mode,
+    __global__ void postprocess_kernel(const TallyT* __restrict__ tally, const Voxel* __restrict__ voxels,
+        const uint8_t* __restrict__ palette_index, const PaletteEntry* __restrict__ palette, uint64_t n, int mode,
         double histories, double voxel_volume_cm3, double calibration, double* __restrict__ dose, double* __restrict__ variance)
     {
         const double h_inv = 1.0 / (histories - 1.0);
@@ -1016,7 +1017,7 @@ namespace {
                 d = e * h_d;
                 v = (ee * h_v - d * d) * h_inv;
             } else if (mode == 2) { // DOSE: energyImpartedToDose
-                const double de = static_cast<double>(voxels[i].density);
+                const double de = static_cast<double>(voxels ? voxels[i].density : palette[palette_index[i]].density);
                 const double mass = de * voxel_volume_cm3 * 0.001;
                 const double f = calibration / mass;
                 d = de > 0.0 ? e * f : 0.0;
@@ -1166,21 +1167,23 @@ int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem)
     return e == cudaSuccess ? n : 0;
 }
 
-cudaError_t launch_postprocess(const double* tally, const uint32_t*, const Voxel* voxels, uint64_t n, int mode, double histories,
+cudaError_t launch_postprocess(const double* tally, const WorldParams& w, uint64_t n, int mode, double histories,
     double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream)
 {
     const int block = 256;
     const int grid = static_cast<int>(std::min<uint64_t>((n + block - 1) / block, 152ull * 16));
-    postprocess_kernel<double><<<grid, block, 0, stream>>>(tally, voxels, n, mode, histories, voxel_volume_cm3, calibration, dose, variance);
+    postprocess_kernel<double><<<grid, block, 0, stream>>>(tally, w.palette_index ? nullptr : w.voxels, w.palette_index, w.palette, n, mode,
+        histories, voxel_volume_cm3, calibration, dose, variance);
     return cudaGetLastError();
 }
 
-cudaError_t launch_postprocess_f32(const float* tally, const uint32_t*, const Voxel* voxels, uint64_t n, int mode, double histories,
+cudaError_t launch_postprocess_f32(const float* tally, const WorldParams& w, uint64_t n, int mode, double histories,
     double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream)
 {
     const int block = 256;
     const int grid = static_cast<int>(std::min<uint64_t>((n + block - 1) / block, 152ull * 16));
-    postprocess_kernel<float><<<grid, block, 0, stream>>>(tally, voxels, n, mode, histories, voxel_volume_cm3, calibration, dose, variance);
+    postprocess_kernel<float><<<grid, block, 0, stream>>>(tally, w.palette_index ? nullptr : w.voxels, w.palette_index, w.palette, n, mode,
+        histories, voxel_volume_cm3, calibration, dose, variance);
     return cudaGetLastError();
 }
 
