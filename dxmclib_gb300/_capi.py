@@ -173,6 +173,8 @@ SIGNATURES = {
     "dxmc_gpu_job_free": (None, [VP]),
     "dxmc_gpu_probe_lut": (C.c_int, [VP, VP, C.c_int, DP, C.c_int, DP, DP]),
     "dxmc_gpu_job_release": (C.c_int, [VP]),
+    "dxmc_gpu_job_progress": (C.c_int, [VP, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "dxmc_gpu_job_preview": (C.c_int, [VP, DP]),
     "dxmc_gpu_radiological_path": (C.c_int, [VP, VP, VP, FP, C.c_uint64, DP]),
     "dxmc_gpu_ctx_memory": (C.c_int, [VP, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     "dxmc_gpu_host_alloc": (C.c_int, [C.c_uint64, C.POINTER(VP)]),

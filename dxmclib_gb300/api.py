@@ -1117,6 +1117,21 @@ class Job:
             A.check(rc, self.ctx.handle, "dxmc_gpu_job_result")
         return dose, var, nev, stats
 
+    def progress(self) -> tuple:
+        """(histories started, total) of a running job."""
+        a, b = C.c_uint64(), C.c_uint64()
+        A.check(self.ctx.lib.dxmc_gpu_job_progress(self.handle, C.byref(a), C.byref(b)), self.ctx.handle,
+                "dxmc_gpu_job_progress")
+        return a.value, b.value
+
+    def preview(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """Energy imparted scored so far (keV per voxel) while the job runs."""
+        n = self.dworld.world.size()
+        out = np.zeros(n) if out is None else out
+        A.check(self.ctx.lib.dxmc_gpu_job_preview(self.handle, out.ctypes.data_as(A.DP)), self.ctx.handle,
+                "dxmc_gpu_job_preview")
+        return out
+
     def release(self):
         """Frees the device buffers of a finished job (its results are gone)."""
         if self.handle and self.ctx.handle:

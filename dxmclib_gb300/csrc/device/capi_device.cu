@@ -1695,6 +1695,44 @@ int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double
     return DXMC_OK;
 }
 
+int dxmc_gpu_job_progress(dxmc_job* j, uint64_t* started, uint64_t* total)
+{
+    if (!j || !started)
+        return DXMC_ERR_INVALID;
+    dxmc_gpu_ctx* ctx = j->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    if (!j->counters)
+        return fail(ctx, DXMC_ERR_STATE, "job results were already released");
+    cudaSetDevice(ctx->device);
+    auto* hc = reinterpret_cast<dev::JobCounters*>(reinterpret_cast<unsigned char*>(j->cancel_host) + 16);
+    // a racy snapshot of a counter the kernels only increase
+    DXMC_CUDA(ctx, cudaMemcpyAsync(&hc->next_history, &j->counters->next_history, 3 * sizeof(unsigned long long),
+        cudaMemcpyDeviceToHost, ctx->result_stream));
+    DXMC_CUDA(ctx, cudaStreamSynchronize(ctx->result_stream));
+    const bool done = cudaEventQuery(j->stop) == cudaSuccess;
+    *started = done ? j->histories : std::min<uint64_t>(std::max(hc->next_history, hc->histories_done), j->histories);
+    if (total)
+        *total = j->histories;
+    return DXMC_OK;
+}
+
+int dxmc_gpu_job_preview(dxmc_job* j, double* energy)
+{
+    if (!j || !energy)
+        return DXMC_ERR_INVALID;
+    dxmc_gpu_ctx* ctx = j->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    if (!j->tally)
+        return fail(ctx, DXMC_ERR_STATE, j->tally_f32 ? "dose preview needs the FP64 tally" : "job results were already released");
+    cudaSetDevice(ctx->device);
+    const uint64_t nv = j->world->params.n_voxels;
+    // every other double of the interleaved (energy, energy^2) tally
+    DXMC_CUDA(ctx, cudaMemcpy2DAsync(energy, sizeof(double), j->tally, 2 * sizeof(double), sizeof(double), nv,
+        cudaMemcpyDeviceToHost, ctx->result_stream));
+    DXMC_CUDA(ctx, cudaStreamSynchronize(ctx->result_stream));
+    return DXMC_OK;
+}
+
 int dxmc_gpu_job_release(dxmc_job* j)
 {
     if (!j)

@@ -273,6 +273,14 @@ int dxmc_gpu_job_cancel(dxmc_job* job);
  * world size; any output pointer may be NULL.  calibration multiplies DOSE. */
 int dxmc_gpu_job_result(dxmc_job* job, int output_mode, double calibration,
     double* dose, double* variance, uint32_t* n_events, dxmc_job_stats* stats);
+/* Live progress of a running job (ProgressBar, progressbar.hpp:42-80): the
+ * histories its kernels have taken so far (photons generated in the kernel) or
+ * queued (pre-generated photons); reads a device counter, does not wait. */
+int dxmc_gpu_job_progress(dxmc_job* job, uint64_t* histories_started, uint64_t* histories_total);
+/* Dose preview while the job runs (ProgressBar::setDoseData, progressbar.hpp:94-101):
+ * copies the energy imparted scored so far (keV per voxel, FP64 tally mode)
+ * into energy[n_voxels]; the values grow until the job ends. */
+int dxmc_gpu_job_preview(dxmc_job* job, double* energy);
 /* Frees a finished job's device buffers (tallies, tables) and returns them to
  * the memory budget; the handle stays valid for dxmc_gpu_job_free, results are
  * gone.  For batched jobs, whose handles the batch owns. */

@@ -289,6 +289,10 @@ public:
         }
         ok = ok && check(dxmc_gpu_job_submit(m_ctx, dworld, lut, &jd, &job), "job submit");
         bool cancelled = false;
+        std::uint64_t reported = 0; // exposures reported to the progress bar
+        std::vector<double> preview;
+        auto last_preview = std::chrono::steady_clock::now();
+        const std::uint64_t per_exposure = std::max<std::uint64_t>(1, flat.exposures.empty() ? 1 : flat.exposures[0].n_histories);
         while (ok) {
             const int rc = dxmc_gpu_job_wait(job, 50);
             if (rc == DXMC_OK)
@@ -300,6 +304,26 @@ public:
             if (progressbar && progressbar->cancel() && !cancelled) {
                 dxmc_gpu_job_cancel(job);
                 cancelled = true;
+            }
+            if (progressbar && !cancelled) {
+                // ProgressBar::exposureCompleted per exposure's worth of histories taken, and
+                // a dose preview from the live tally about once a second (progressbar.hpp:54-101)
+                std::uint64_t started = 0;
+                if (dxmc_gpu_job_progress(job, &started, nullptr) == DXMC_OK) {
+                    const std::uint64_t done = std::min<std::uint64_t>(started / per_exposure, flat.exposures.size());
+                    for (; reported < done; ++reported)
+                        progressbar->exposureCompleted();
+                }
+                const auto now = std::chrono::steady_clock::now();
+                if (now - last_preview > std::chrono::seconds(1)) {
+                    last_preview = now;
+                    preview.resize(n);
+                    if (dxmc_gpu_job_preview(job, preview.data()) == DXMC_OK) {
+                        for (std::size_t i = 0; i < n; ++i)
+                            result.dose[i] = static_cast<T>(preview[i]);
+                        progressbar->setDoseData(result.dose.data(), world.dimensions(), world.spacing());
+                    }
+                }
             }
         }
         result.simulationTime = std::chrono::system_clock::now() - start;

@@ -87,3 +87,37 @@ def test_invalid_input_and_budget_are_refused(gpu_ctx):
     job.close()
     dlut.close()
     dworld.close()
+
+
+def test_progress_and_dose_preview(gpu_ctx):
+    """A running job reports the histories its kernels have taken and a preview of
+    the energy scored so far (what a ProgressBar shows); once it has finished the
+    preview equals the raw energy tally of the result."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    from dxmclib_gb300.workloads import ct_helical
+    ctx = gpu_ctx
+    wl = ct_helical(nz=64, histories=1_500_000_000)
+    src = wl.source
+    dworld = dx.DeviceWorld(ctx, wl.world)
+    dlut = dx.DeviceLut(ctx, dx.LutBlob(wl.world.materialMap(), dworld.max_density(), src.maxPhotonEnergyProduced()))
+    job = dx.Job(ctx, dworld, dlut, src.exposures(wl.world.directionCosines()), src.spectrum(), src.heel(), None,
+                 seed=5, model=1)
+    seen, sums = [], []
+    while job.wait(0) == A.DXMC_ERR_TIMEOUT and len(seen) < 50:
+        started, total = job.progress()
+        seen.append(started)
+        sums.append(job.preview().sum())
+        time.sleep(0.01)
+    assert job.wait() == A.DXMC_OK
+    assert len(seen) >= 2, "the job finished before it could be observed"
+    assert seen == sorted(seen) and seen[-1] <= total
+    assert sums == sorted(sums) and sums[-1] > 0
+    final_preview = job.preview()
+    started, total = job.progress()
+    assert started == total
+    e, _, _, stats = job.result(A.OUTPUT_RAW, want_events=False)
+    np.testing.assert_array_equal(final_preview, e)
+    job.close()
+    dlut.close()
+    dworld.close()
