@@ -274,3 +274,42 @@ def test_ct_calibration_matches_reference(gpu_ctx, golden):
     tr = dx.Transport(gpu_ctx)
     f = src.getCalibrationValue(1, transport=tr)
     assert np.isfinite(f) and f > 0
+
+
+@pytest.mark.parametrize("model", [0, 1, 2])
+def test_forced_scoring_equals_naive(gpu_ctx, model):
+    """The reference's check that forced photoelectric scoring is unbiased
+    (testtransport.cpp:59-115, there per interaction): the same job with a
+    measurement map everywhere and with none imparts the same total energy, here
+    over whole histories (2e7 each, 3 sigma of the difference about 0.1 %)."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    n = 32
+    results = []
+    for forced in (False, True):
+        world = dx.World()
+        world.setDimensions((n, n, n))
+        world.setSpacing((2.0, 2.0, 2.0))
+        world.setDensityArray(np.ones(n ** 3, np.float32))
+        world.setMaterialIndexArray(np.zeros(n ** 3, np.uint8))
+        if forced:
+            world.setMeasurementMapArray(np.ones(n ** 3, np.uint8))
+        world.addMaterialToMap(dx.Material("Water, Liquid"))
+        src = dx.IsotropicSource()
+        src.setPosition((0, 0, -200))
+        src.setCollimationAngles(-0.08, 0.08, -0.08, 0.08)
+        src.setSpecter([1.0], [60.0])
+        src.setTotalExposures(20)
+        src.setHistoriesPerExposure(1_000_000)
+        dworld = dx.DeviceWorld(gpu_ctx, world)
+        dlut = dx.DeviceLut(gpu_ctx, dx.LutBlob(world.materialMap(), dworld.max_density(), 60.0))
+        job = dx.Job(gpu_ctx, dworld, dlut, src.exposures(), src.spectrum(), None, None, seed=21 + forced, model=model)
+        e, e2, _, stats = job.result(A.OUTPUT_RAW, want_events=False)
+        job.close()
+        dlut.close()
+        dworld.close()
+        results.append((e.sum(), e2.sum()))
+    (naive, naive2), (forced_e, forced2) = results
+    # per-history variance bound from the per-event squares (an overestimate for independent events)
+    sigma = np.sqrt(naive2 + forced2)
+    assert abs(forced_e - naive) < max(4 * sigma, 2e-3 * naive), (model, naive, forced_e, sigma)
