@@ -1,7 +1,7 @@
 // Photon-transport kernels for sm_103a.
 //
 // One persistent launch per job: every lane owns one photon history at a
-// time and, inside a warp-synchronous loop, performs one Woodcock step per
+// time and, inside a warp-synchronous loop, takes a burst of Woodcock steps per
 // iteration.  Lanes whose history ended take the next history id from a
 // warp-local pool that one lane refills from a global work queue, so warps
 // stay full until the job runs dry.  Physics follows DXMClib's
@@ -449,8 +449,9 @@ namespace {
     // ---- the transport kernel ----------------------------------------------------
     //
     // Warp-synchronous loop.  Each iteration every lane with a live photon and no
-    // pending interaction takes one Woodcock step; a real event only records its
-    // type (photoelectric / Compton / Rayleigh).  The interactions are then run in
+    // pending interaction takes up to woodcock_burst Woodcock steps; a real event
+    // only records its type (photoelectric / Compton / Rayleigh) and ends the lane's
+    // burst.  The interactions are then run in
     // one converged pass per type once enough lanes wait, and finished lanes are
     // refilled together once enough are idle, so the expensive branches run with
     // many lanes active instead of one or two.
@@ -769,8 +770,9 @@ namespace {
     // ---- single-job transport kernel ----------------------------------------------------
     //
     // Warp-synchronous loop.  Each iteration every lane with a live photon and no
-    // pending interaction takes one Woodcock step; a real event only records its
-    // type (photoelectric / Compton / Rayleigh).  The interactions are then run in
+    // pending interaction takes up to woodcock_burst Woodcock steps; a real event
+    // only records its type (photoelectric / Compton / Rayleigh) and ends the lane's
+    // burst.  The interactions are then run in
     // one converged pass per type once enough lanes wait, and finished lanes are
     // refilled together once enough are idle, so the expensive branches run with
     // many lanes active instead of one or two.
