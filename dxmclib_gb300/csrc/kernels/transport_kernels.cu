@@ -502,6 +502,7 @@ namespace {
         __device__ void reset_counters() { steps = deposits = overflows = histories = 0; }
         __device__ void start_photon()
         {
+            steps += hist_steps; // the previous photon's in-grid steps
             pending = EV_NONE;
             updateMax = true;
             cached_mat = -1;
@@ -596,7 +597,6 @@ namespace {
                 int mat;
                 bool measured;
                 gather_voxel<PALETTE>(w, pal, s.vidx, density, mat, measured);
-                ++s.steps;
                 if (mat != s.cached_mat) {
                     float a0, a1, a2;
                     lut_attenuation(L, m, mat, s.logE, s.seg, a0, a1, a2);
@@ -748,6 +748,8 @@ namespace {
     // Adds the warp's lane counters to a job's counters and clears them.
     __device__ __forceinline__ void flush_counters(Lane& s, JobCounters* c)
     {
+        s.steps += s.hist_steps; // counted once: the photon's steps so far
+        s.hist_steps = 0;
         unsigned long long v[4] = { s.steps, s.deposits, s.overflows, s.histories };
 #pragma unroll
         for (int k = 0; k < 4; ++k)

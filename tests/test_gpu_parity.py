@@ -277,23 +277,34 @@ def test_ct_calibration_matches_reference(gpu_ctx, golden):
 
 
 @pytest.mark.parametrize("model", [0, 1, 2])
-def test_forced_scoring_equals_naive(gpu_ctx, model):
-    """The reference's check that forced photoelectric scoring is unbiased
-    (testtransport.cpp:59-115, there per interaction): the same job with a
-    measurement map everywhere and with none imparts the same total energy, here
-    over whole histories (2e7 each, 3 sigma of the difference about 0.1 %)."""
+def test_forced_scoring_against_naive_as_the_reference(gpu_ctx, model):
+    """Forced photoelectric scoring against naive sampling over whole histories.
+    DXMClib checks the two per interaction (testtransport.cpp:59-115); over whole
+    histories its scheme (computeInteractionsForced, transport.hpp:523-581) is not
+    exactly unbiased: the weight correction (1 - p_photo) also multiplies photons
+    that just scattered, which moves a second-order share of weight from scattered
+    to unscattered photons, and a water cube imparts about 1 % less energy with a
+    measurement map everywhere than without.  The GPU must reproduce that
+    deficit: it is compared with the oracle port's on the same setup (GPU 2e7
+    histories per run, port 2e6)."""
+    import sys
+    from pathlib import Path
     import dxmclib_gb300 as dx
     from dxmclib_gb300 import _capi as A
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1] / "oracle" / "port"))
+    import binding as port
+    port.build()
     n = 32
-    results = []
+    gpu, cpu = [], []
     for forced in (False, True):
         world = dx.World()
         world.setDimensions((n, n, n))
         world.setSpacing((2.0, 2.0, 2.0))
         world.setDensityArray(np.ones(n ** 3, np.float32))
         world.setMaterialIndexArray(np.zeros(n ** 3, np.uint8))
+        meas = np.ones(n ** 3, np.uint8) if forced else None
         if forced:
-            world.setMeasurementMapArray(np.ones(n ** 3, np.uint8))
+            world.setMeasurementMapArray(meas)
         world.addMaterialToMap(dx.Material("Water, Liquid"))
         src = dx.IsotropicSource()
         src.setPosition((0, 0, -200))
@@ -302,14 +313,21 @@ def test_forced_scoring_equals_naive(gpu_ctx, model):
         src.setTotalExposures(20)
         src.setHistoriesPerExposure(1_000_000)
         dworld = dx.DeviceWorld(gpu_ctx, world)
-        dlut = dx.DeviceLut(gpu_ctx, dx.LutBlob(world.materialMap(), dworld.max_density(), 60.0))
+        blob = dx.LutBlob(world.materialMap(), dworld.max_density(), 60.0)
+        dlut = dx.DeviceLut(gpu_ctx, blob)
         job = dx.Job(gpu_ctx, dworld, dlut, src.exposures(), src.spectrum(), None, None, seed=21 + forced, model=model)
-        e, e2, _, stats = job.result(A.OUTPUT_RAW, want_events=False)
+        e, _, _, _ = job.result(A.OUTPUT_RAW, want_events=False)
         job.close()
         dlut.close()
         dworld.close()
-        results.append((e.sum(), e2.sum()))
-    (naive, naive2), (forced_e, forced2) = results
-    # per-history variance bound from the per-event squares (an overestimate for independent events)
-    sigma = np.sqrt(naive2 + forced2)
-    assert abs(forced_e - naive) < max(4 * sigma, 2e-3 * naive), (model, naive, forced_e, sigma)
+        gpu.append(e.sum() / 2e7)
+        src.setHistoriesPerExposure(100_000)
+        sp = src.spectrum()
+        ec, _, _, _, _ = port.transport(blob.info(), (n, n, n), (2.0,) * 3, np.ones(n ** 3), np.zeros(n ** 3, np.uint8),
+                                        src.exposures().as_matrix(), model=model, seed=5 + forced,
+                                        spectrum=(sp.energies, sp.weights), measurement=meas)
+        cpu.append(ec.sum() / 2e6)
+    d_gpu = gpu[1] / gpu[0] - 1.0
+    d_cpu = cpu[1] / cpu[0] - 1.0
+    assert -0.03 < d_gpu < -0.003, (model, d_gpu)  # the scheme's deficit, about 1 %
+    assert abs(d_gpu - d_cpu) < 0.005, (model, d_gpu, d_cpu)
