@@ -330,4 +330,4 @@ def test_forced_scoring_against_naive_as_the_reference(gpu_ctx, model):
     d_gpu = gpu[1] / gpu[0] - 1.0
     d_cpu = cpu[1] / cpu[0] - 1.0
     assert -0.03 < d_gpu < -0.003, (model, d_gpu)  # the scheme's deficit, about 1 %
-    assert abs(d_gpu - d_cpu) < 0.005, (model, d_gpu, d_cpu)
+    assert abs(d_gpu - d_cpu) < 0.006, (model, d_gpu, d_cpu)  # about 3 sigma of the port run
