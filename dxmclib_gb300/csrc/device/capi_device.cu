@@ -33,6 +33,9 @@ constexpr int DEFAULT_WOODCOCK_BURST = DXMC_DEFAULT_WOODCOCK_BURST; // Woodcock 
 // asks for a pre-generated queue (2^n photons per generation pass): with the
 // Woodcock burst the in-kernel generation is as fast and needs no queue memory.
 constexpr int DEFAULT_QUEUE_LOG2 = -1;
+// Sampling tables: energies (log-spaced over the LUT range) and quantile levels per row.
+constexpr int SAMPLING_ENERGIES = 128;
+constexpr int SAMPLING_LEVELS = 512;
 
 struct BatchEngines;
 
@@ -626,6 +629,22 @@ int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* b, dxmc_lut** ou
                 o[8 + k] = static_cast<float>(c.line_energies[k]);
             }
         }
+    }
+    // inverse-CDF sampling tables for the Compton and Rayleigh samplers, after the
+    // part of the image that the kernels stage in shared memory
+    {
+        const auto tp = dxmc_gb300::host::sampling_tables(*b, SAMPLING_ENERGIES, SAMPLING_LEVELS);
+        const auto& t = *tp;
+        m.tab_ne = t.ne;
+        m.tab_nu = t.nu;
+        m.tab_le0 = static_cast<float>(t.le0);
+        m.tab_inv_dle = static_cast<float>(1.0 / t.dle);
+        m.off_ckn = static_cast<int>(img.size());
+        m.off_csf = m.off_ckn + static_cast<int>(t.compton_kn.size());
+        m.off_ray = m.off_csf + static_cast<int>(t.compton_sf.size());
+        img.insert(img.end(), t.compton_kn.begin(), t.compton_kn.end());
+        img.insert(img.end(), t.compton_sf.begin(), t.compton_sf.end());
+        img.insert(img.end(), t.rayleigh.begin(), t.rayleigh.end());
     }
     cudaSetDevice(ctx->device);
     auto* lut = new (std::nothrow) dxmc_lut;

@@ -3,7 +3,9 @@
 #include "lut_builder.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <thread>
 #include <limits>
 #include <numeric>
 
@@ -247,6 +249,133 @@ double lut_scatter_factor(const dxmc_lut_blob& b, int material, double q)
     const std::size_t index = x > start ? static_cast<std::size_t>((x - start) / step) : 0;
     const std::size_t off = index < SPLINE_N - 1 ? index * 4 : (SPLINE_N - 2) * 4;
     return sp[off] + sp[off + 1] * x + sp[off + 2] * x * x + sp[off + 3] * x * x * x;
+}
+
+double rita_value(const dxmc_lut_blob& b, int material, double xi)
+{
+    const auto& r = b.rita[material];
+    const double* x = r.data();
+    const double* e = x + RITA_N;
+    const double* a = e + RITA_N;
+    const double* bb = a + RITA_N;
+    int i = static_cast<int>(std::upper_bound(e, e + RITA_N, xi) - e) - 1;
+    i = std::clamp(i, 0, RITA_N - 2);
+    const double v = xi - e[i];
+    const double d = e[i + 1] - e[i];
+    return x[i] + (1.0 + a[i] + bb[i]) * d * v / (d * d + a[i] * d * v + bb[i] * v * v) * (x[i + 1] - x[i]);
+}
+
+namespace {
+
+// Quantiles at levels k / nu (k = 0..nu) of the density w on [lo, hi] (trapezoid
+// cumulative on M intervals, linear inversion); returns them mapped by `store`.
+void quantiles(double lo, double hi, const std::function<double(double)>& w, int nu, const std::function<double(double)>& store,
+    float* out)
+{
+    constexpr int M = 2048;
+    std::vector<double> G(M + 1, 0.0);
+    const double h = (hi - lo) / M;
+    double prev = std::max(w(lo), 0.0);
+    for (int j = 1; j <= M; ++j) {
+        const double cur = std::max(w(lo + j * h), 0.0);
+        G[j] = G[j - 1] + 0.5 * (prev + cur) * h;
+        prev = cur;
+    }
+    const double total = G[M];
+    int j = 0;
+    for (int k = 0; k <= nu; ++k) {
+        double x;
+        if (!(total > 0)) {
+            x = lo + (hi - lo) * k / nu; // flat: uniform
+        } else {
+            const double target = total * k / nu;
+            while (j < M - 1 && G[j + 1] < target)
+                ++j;
+            const double dg = G[j + 1] - G[j];
+            const double f = dg > 0 ? std::clamp((target - G[j]) / dg, 0.0, 1.0) : 0.0;
+            x = lo + (j + f) * h;
+        }
+        out[k] = static_cast<float>(store(std::clamp(x, lo, hi)));
+    }
+}
+
+} // namespace
+
+void build_sampling_tables(const dxmc_lut_blob& b, int ne, int nu, SamplingTables& out)
+{
+    const int nm = b.n_materials;
+    out.ne = ne;
+    out.nu = nu;
+    out.le0 = std::log(b.min_energy);
+    out.dle = (std::log(b.max_energy) - out.le0) / (ne - 1);
+    const size_t row = static_cast<size_t>(nu) + 1;
+    out.compton_kn.assign(static_cast<size_t>(ne) * row, 0.0f);
+    out.compton_sf.assign(static_cast<size_t>(nm) * ne * row, 0.0f);
+    out.rayleigh.assign(static_cast<size_t>(nm) * ne * row, 0.0f);
+    // rows are independent: spread the energies over the host cores
+    auto build_row = [&](int i) {
+        const double E = std::exp(out.le0 + i * out.dle);
+        const double k = E / ELECTRON_REST_MASS;
+        const double emin = 1.0 / (1.0 + 2.0 * k);
+        const double qscale = E / KEV_TO_ANGSTROM; // q = qscale * sqrt((1 - cos) / 2)
+        auto kn = [=](double e) {
+            const double t = (1.0 - e) / (k * e);
+            return 1.0 / e + e - t * (2.0 - t);
+        };
+        auto q_of = [=](double e) {
+            const double cos = 1.0 - (1.0 - e) / (k * e);
+            return qscale * std::sqrt(std::max(0.5 - 0.5 * cos, 0.0));
+        };
+        auto to_x = [=](double e) { return (e - emin) / (1.0 - emin); };
+        quantiles(emin, 1.0, kn, nu, to_x, out.compton_kn.data() + i * row);
+        const double qmax2 = qscale * qscale;
+        for (int m = 0; m < nm; ++m) {
+            quantiles(emin, 1.0, [&](double e) { return kn(e) * lut_scatter_factor(b, m, q_of(e)); }, nu, to_x,
+                out.compton_sf.data() + (static_cast<size_t>(m) * ne + i) * row);
+            // RITA restricted to q^2 <= qmax^2 (rita_sample: the proposal stops at e[ub] and
+            // draws above qmax^2 are rejected): find xi* with x(xi*) = qmax^2
+            const double* xs = b.rita[m].data();
+            const double* es = xs + RITA_N;
+            const int ub = static_cast<int>(std::upper_bound(xs, xs + RITA_N, qmax2) - xs);
+            double hi = ub < RITA_N ? es[ub] : 1.0;
+            if (rita_value(b, m, hi) > qmax2) {
+                double lo = 0.0;
+                for (int it = 0; it < 80; ++it) {
+                    const double mid = 0.5 * (lo + hi);
+                    (rita_value(b, m, mid) > qmax2 ? hi : lo) = mid;
+                }
+                hi = lo;
+            }
+            auto w = [&](double xi) {
+                const double cos = 1.0 - 2.0 * rita_value(b, m, xi) / qmax2;
+                return 0.5 * (1.0 + cos * cos);
+            };
+            auto to_y = [&](double xi) { return std::clamp(rita_value(b, m, xi) / qmax2, 0.0, 1.0); };
+            quantiles(0.0, hi, w, nu, to_y, out.rayleigh.data() + (static_cast<size_t>(m) * ne + i) * row);
+        }
+    };
+    const int workers = std::clamp(static_cast<int>(std::thread::hardware_concurrency()), 1, 32);
+    std::atomic<int> next { 0 };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < workers; ++t)
+        pool.emplace_back([&] {
+            for (int i = next++; i < ne; i = next++)
+                build_row(i);
+        });
+    for (auto& th : pool)
+        th.join();
+}
+
+std::shared_ptr<const SamplingTables> sampling_tables(const dxmc_lut_blob& b, int ne, int nu)
+{
+    std::lock_guard<std::mutex> lock(*b.tables_mutex);
+    auto cached = std::static_pointer_cast<const SamplingTables>(b.tables);
+    if (cached && cached->ne == ne && cached->nu == nu)
+        return cached;
+    auto t = std::make_shared<SamplingTables>();
+    build_sampling_tables(b, ne, nu, *t);
+    b.tables = t;
+    return t;
 }
 
 int build_lut(const std::vector<MaterialData>& materials, const std::vector<double>& max_density, double max_energy, dxmc_lut_blob& out)

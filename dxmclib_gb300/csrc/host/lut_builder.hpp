@@ -18,6 +18,8 @@
 #include <array>
 #include <cstdint>
 #include <functional>
+#include <memory>
+#include <mutex>
 #include <vector>
 
 struct dxmc_lut_blob {
@@ -37,6 +39,9 @@ struct dxmc_lut_blob {
     std::vector<std::array<double, 79>> spline;
     std::vector<std::array<dxmc_shell_config, 12>> shells;
     std::vector<double> max_density;
+    // inverse-CDF sampling tables, built on first upload and kept with the blob
+    std::shared_ptr<std::mutex> tables_mutex = std::make_shared<std::mutex>();
+    mutable std::shared_ptr<const void> tables;
 
     std::size_t resolution() const { return log_energy.size(); }
 };
@@ -75,6 +80,28 @@ void build_rita(double min, double max, const std::function<double(double)>& pdf
 
 // Natural cubic spline on N knots spaced (stop-start)/(N-2), interpolation.hpp:127-167.
 void build_spline(double start, double stop, const std::function<double(double)>& f, int N, double* coef, double* knots, double& step, double& stop_out);
+
+// Inverse-CDF tables for divergence-free interaction sampling on the GPU.  For
+// ne log-spaced energies between the LUT's minimum and maximum energy, each row
+// holds nu + 1 quantiles (levels k / nu) of the density the reference's rejection
+// samplers draw from:
+//   compton_kn[E]      Compton energy fraction e in [e_min, 1], density
+//                      (1/e + e - sin^2) (transport.hpp:300-340, NONE model),
+//                      stored as (e - e_min) / (1 - e_min);
+//   compton_sf[m][E]   the same times the scatter factor S(q) (LIVERMORE model);
+//   rayleigh[m][E]     momentum transfer q^2 from the RITA form-factor table
+//                      truncated at q_max^2, times (1 + cos^2) / 2
+//                      (transport.hpp:264-298), stored as q^2 / q_max^2.
+struct SamplingTables {
+    int ne = 0, nu = 0;
+    double le0 = 0, dle = 0; // natural log of the first energy, log step
+    std::vector<float> compton_kn, compton_sf, rayleigh;
+};
+void build_sampling_tables(const dxmc_lut_blob& b, int ne, int nu, SamplingTables& out);
+// The blob's tables for (ne, nu), built once and shared by every upload of the blob.
+std::shared_ptr<const SamplingTables> sampling_tables(const dxmc_lut_blob& b, int ne, int nu);
+// RITA inverse transform of xi in [0, 1] for material m (dxmcrandom.hpp:483-500).
+double rita_value(const dxmc_lut_blob& b, int material, double xi);
 
 // Alias table by the squaring-the-histogram method, dxmcrandom.hpp:229-274.
 void build_alias_table(const std::vector<double>& weights, std::vector<double>& probs, std::vector<std::uint64_t>& alias);

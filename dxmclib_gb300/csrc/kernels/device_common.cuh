@@ -54,8 +54,49 @@ struct LutMeta {
     int off_rita;    // n_materials * 4 * 56 (x, e, a, b)
     int off_spline;  // n_materials * 64 (60 coefficients, start, step, stop, pad)
     int off_shells;  // n_materials * 12 * SHELL_FLOATS
-    int pad0, pad1;
+    // inverse-CDF sampling tables, after total_floats (read from global memory,
+    // not staged in shared memory): rows of tab_nu + 1 quantiles
+    int off_ckn;     // Compton energy fraction, no scatter factor: tab_ne rows
+    int off_csf;     // Compton with scatter factor: n_materials * tab_ne rows
+    int off_ray;     // Rayleigh q^2 / q_max^2: n_materials * tab_ne rows
+    int tab_ne, tab_nu;
+    float tab_le0;     // ln of the first table energy
+    float tab_inv_dle; // 1 / ln step
+    int pad0;
 };
+
+// Rows of the sampling tables around energy E: row i and i + 1 with weight f of
+// the upper one.  Draws interpolate the two rows' quantiles at the same level
+// (quantile interpolation), which follows distributions that stretch with
+// energy far more closely than a mixture of the rows would.
+__device__ __forceinline__ int table_row(const LutMeta& m, float E, float& f)
+{
+    const float t = (__logf(E) - m.tab_le0) * m.tab_inv_dle;
+    int i = static_cast<int>(floorf(t));
+    f = t - static_cast<float>(i);
+    if (i < 0) {
+        i = 0;
+        f = 0.0f;
+    } else if (i > m.tab_ne - 2) {
+        i = m.tab_ne - 2;
+        f = 1.0f;
+    }
+    return i;
+}
+
+// Quantile at level u of the energy rows `row` and `row + 1` (stride nu + 1),
+// linear between the stored levels k / nu and between the two rows (weight fe).
+__device__ __forceinline__ float table_quantile(const float* row, int nu, float u, float fe)
+{
+    const float pos = u * static_cast<float>(nu);
+    const int j = min(static_cast<int>(pos), nu - 1);
+    const float f = pos - static_cast<float>(j);
+    const float a0 = __ldg(row + j), b0 = __ldg(row + j + 1);
+    const float a1 = __ldg(row + nu + 1 + j), b1 = __ldg(row + nu + 1 + j + 1);
+    const float q0 = fmaf(f, b0 - a0, a0);
+    const float q1 = fmaf(f, b1 - a1, a1);
+    return fmaf(fe, q1 - q0, q0);
+}
 
 constexpr int RITA_N = 56;
 constexpr int SPLINE_N = 16;

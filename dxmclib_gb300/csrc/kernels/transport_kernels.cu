@@ -117,7 +117,7 @@ namespace {
 
     // ---- Rayleigh (transport.hpp:264-298) ---------------------------------------
     template <int MODEL>
-    __device__ __forceinline__ bool rayleigh_scatter(const float* L, const LutMeta& m, Photon& ph, int material, Rng& rng)
+    __device__ __forceinline__ bool rayleigh_scatter(const float* L, const float* G, const LutMeta& m, Photon& ph, int material, Rng& rng)
     {
         if constexpr (MODEL == 0) {
             constexpr float extreme = 1.08866210790363f; // 4 sqrt(2) / (3 sqrt(3))
@@ -134,21 +134,15 @@ namespace {
             }
             return false;
         } else {
-            const float qmax = ph.energy * (1.0f / KEV_TO_ANGSTROM);
-            const float qmax2 = qmax * qmax;
-            const float invE = KEV_TO_ANGSTROM / ph.energy;
-            for (int it = 0; it < REJECTION_CAP; ++it) {
-                float q2;
-                if (!rita_sample(L, m, material, qmax2, rng, q2))
-                    return false;
-                const float cosA = 1.0f - 2.0f * q2 * invE * invE;
-                if (!((1.0f + cosA * cosA) * 0.5f < rng.uniform())) {
-                    const float phi = rng.azimuth();
-                    peturb(ph.dx, ph.dy, ph.dz, cosA, phi);
-                    return true;
-                }
-            }
-            return false;
+            // the density of the reference's RITA draw of q^2 <= q_max^2 followed by the
+            // (1 + cos^2) / 2 rejection, drawn by inverse CDF: no loop, no divergence
+            float fe;
+            const int row = table_row(m, ph.energy, fe);
+            const float y = table_quantile(G + m.off_ray + (material * m.tab_ne + row) * (m.tab_nu + 1), m.tab_nu, rng.uniform(), fe);
+            const float cosA = 1.0f - 2.0f * y; // q^2 / q_max^2 = (1 - cos) / 2
+            const float phi = rng.azimuth();
+            peturb(ph.dx, ph.dy, ph.dz, cosA, phi);
+            return true;
         }
     }
 
@@ -272,41 +266,29 @@ namespace {
 
     // ---- Compton, Klein-Nishina with optional scatter factor (transport.hpp:300-340)
     template <int MODEL>
-    __device__ __forceinline__ bool compton_scatter(const float* L, const LutMeta& m, Photon& ph, int material, Rng& rng, float& deposit)
+    __device__ __forceinline__ bool compton_scatter(const float* L, const float* G, const LutMeta& m, Photon& ph, int material, Rng& rng, float& deposit)
     {
         if constexpr (MODEL == 2) {
             return compton_ia(L, m, ph, material, rng, deposit);
         } else {
+            // the density of the reference's Klein-Nishina rejection (times the scatter
+            // factor S(q) for LIVERMORE), drawn by inverse CDF: no loop, no divergence
             const float E = ph.energy;
             const float k = E / ELECTRON_REST_MASS;
             const float emin = 1.0f / (1.0f + 2.0f * k);
-            const float gmax_inv = 1.0f / (1.0f / emin + emin);
-            for (int it = 0; it < REJECTION_CAP; ++it) {
-                const float r1 = rng.uniform();
-                const float one_minus_e = (1.0f - r1) * (1.0f - emin);
-                const float e = 1.0f - one_minus_e;
-                const float t = one_minus_e / (k * e);
-                const float sin2 = t * (2.0f - t);
-                const float cosA = 1.0f - t;
-                const float g = (1.0f / e + e - sin2) * gmax_inv;
-                const float r2 = rng.uniform();
-                bool rejected;
-                if constexpr (MODEL == 1) {
-                    // momentumTransferFromCos (attenuationlut.hpp:175-179)
-                    const float q = E * (1.0f / KEV_TO_ANGSTROM) * sqrtf(fmaxf(0.5f - cosA * 0.5f, 0.0f));
-                    rejected = r2 > g * lut_scatter_factor(L, m, material, q);
-                } else {
-                    rejected = r2 > g;
-                }
-                if (!rejected) {
-                    const float phi = rng.azimuth();
-                    peturb(ph.dx, ph.dy, ph.dz, cosA, phi);
-                    ph.energy = E * e;
-                    deposit = E - ph.energy;
-                    return true;
-                }
-            }
-            return false;
+            float fe;
+            const int row = table_row(m, E, fe);
+            const float* tab = MODEL == 1 ? G + m.off_csf + (material * m.tab_ne + row) * (m.tab_nu + 1)
+                                          : G + m.off_ckn + row * (m.tab_nu + 1);
+            const float x = table_quantile(tab, m.tab_nu, rng.uniform(), fe); // (e - e_min) / (1 - e_min)
+            const float one_minus_e = (1.0f - x) * (1.0f - emin);
+            const float e = 1.0f - one_minus_e;
+            const float cosA = 1.0f - one_minus_e / (k * e);
+            const float phi = rng.azimuth();
+            peturb(ph.dx, ph.dy, ph.dz, fmaxf(cosA, -1.0f), phi);
+            ph.energy = E * e;
+            deposit = E - ph.energy;
+            return true;
         }
     }
 
@@ -687,7 +669,7 @@ namespace {
                 }
                 if (__any_sync(FULL_MASK, s.pending == EV_COMPTON) && s.pending == EV_COMPTON) {
                     float e = 0.0f;
-                    if (!compton_scatter<MODEL>(L, m, s.ph, mat, s.rng, e)) {
+                    if (!compton_scatter<MODEL>(L, p.lut, m, s.ph, mat, s.rng, e)) {
                         ++s.overflows;
                         s.alive = false;
                     } else {
@@ -703,7 +685,7 @@ namespace {
                     }
                 }
                 if (run_ray && s.pending == EV_RAYLEIGH) {
-                    if (!rayleigh_scatter<MODEL>(L, m, s.ph, mat, s.rng)) {
+                    if (!rayleigh_scatter<MODEL>(L, p.lut, m, s.ph, mat, s.rng)) {
                         ++s.overflows;
                         s.alive = false;
                     }
@@ -1084,9 +1066,9 @@ namespace {
             if (kind == 0)
                 dep = photo_absorption<MODEL>(L, m, ph, material, rng);
             else if (kind == 1)
-                ok = compton_scatter<MODEL>(L, m, ph, material, rng, dep);
+                ok = compton_scatter<MODEL>(L, L, m, ph, material, rng, dep);
             else
-                ok = rayleigh_scatter<MODEL>(L, m, ph, material, rng);
+                ok = rayleigh_scatter<MODEL>(L, L, m, ph, material, rng);
             const float len = sqrtf(ph.dx * ph.dx + ph.dy * ph.dy + ph.dz * ph.dz);
             out_cos[i] = ok ? (len > 0 ? ph.dz / len : 1.0f) : 2.0f;
             out_energy[i] = ph.energy;
