@@ -257,40 +257,4 @@ __device__ __forceinline__ float lut_max_inverse(const float* L, const LutMeta& 
     return exp10_fast(fmaf(c.y, logE, c.x));
 }
 
-__device__ __forceinline__ float lut_scatter_factor(const float* L, const LutMeta& m, int material, float q)
-{
-    const float* s = L + m.off_spline + material * SPLINE_FLOATS;
-    const float start = s[60], stop = s[62], inv_step = s[63];
-    const float x = fminf(fmaxf(q, start), stop);
-    const int index = x > start ? static_cast<int>((x - start) * inv_step) : 0;
-    const int off = index < SPLINE_N - 1 ? index * 4 : (SPLINE_N - 2) * 4;
-    return s[off] + s[off + 1] * x + s[off + 2] * x * x + s[off + 3] * x * x * x;
-}
-
-// RITA::operator()(state, maxValue): truncated rational inverse transform.
-// Returns false if the rejection cap is hit.
-__device__ __forceinline__ bool rita_sample(const float* L, const LutMeta& m, int material, float max_value, Rng& rng, float& out)
-{
-    const float* x = L + m.off_rita + material * 4 * RITA_N;
-    const float* e = x + RITA_N;
-    const float* a = e + RITA_N;
-    const float* b = a + RITA_N;
-    const int ub = upper_bound_f(x, RITA_N, max_value);
-    const float modifier = ub < RITA_N ? e[ub] : 1.0f;
-    for (int it = 0; it < REJECTION_CAP; ++it) {
-        const float r1 = rng.uniform() * modifier;
-        int i = upper_bound_f(e, RITA_N, r1) - 1;
-        i = min(max(i, 0), RITA_N - 2);
-        const float v = r1 - e[i];
-        const float d = e[i + 1] - e[i];
-        const float res = x[i] + (1.0f + a[i] + b[i]) * d * v / (d * d + a[i] * d * v + b[i] * v * v) * (x[i + 1] - x[i]);
-        if (!(res > max_value)) {
-            out = res;
-            return true;
-        }
-    }
-    out = 0.0f;
-    return false;
-}
-
 } // namespace dxmc_gb300::dev
