@@ -119,7 +119,7 @@ class JobDesc(C.Structure):
         ("spectrum", C.POINTER(SpectrumDesc)), ("heel", C.POINTER(HeelDesc)), ("bowtie", C.POINTER(BowtieDesc)),
         ("seed", C.c_uint64), ("model", C.c_int32), ("tally_mode", C.c_int32),
         ("regen_threshold", C.c_int32), ("interact_threshold", C.c_int32), ("blocks_per_sm", C.c_int32),
-        ("queue_log2_chunk", C.c_int32), ("woodcock_burst", C.c_int32), ("pad", C.c_int32),
+        ("queue_log2_chunk", C.c_int32), ("woodcock_burst", C.c_int32), ("block_size", C.c_int32),
     ]
 
 

@@ -1052,7 +1052,8 @@ class Job:
         j.ctx, j.dworld, j.handle, j._owned = ctx, dworld, handle, False
         return j
 
-    LAUNCH_KEYS = ("regen_threshold", "interact_threshold", "blocks_per_sm", "queue_log2_chunk", "woodcock_burst")
+    LAUNCH_KEYS = ("regen_threshold", "interact_threshold", "blocks_per_sm", "queue_log2_chunk", "woodcock_burst",
+                   "block_size")
 
     def _describe(self, exposures: ExposureTable, spectrum, heel, bowtie, seed, model, tally_mode,
                   launch: Optional[dict] = None) -> A.JobDesc:

@@ -11,7 +11,8 @@ model):
   refilled together (the refill cadence);
 * ``interact_threshold`` -- how many lanes must wait for an interaction before
   the per-type interaction passes run (the event-sorting cadence);
-* ``blocks_per_sm`` -- resident 256-thread blocks per SM (occupancy);
+* ``blocks_per_sm`` -- resident blocks per SM (occupancy);
+* ``block_size`` -- threads per block (128 or 256);
 * ``woodcock_burst`` -- Woodcock steps a lane may take per loop iteration before
   the warp checks for refills and interactions again.
 
@@ -42,11 +43,12 @@ SPACE: Dict[str, List[int]] = {
     "queue_log2_chunk": [23, 25, 0],
     "regen_threshold": [4, 8, 12, 16],
     "interact_threshold": [4, 6, 8, 12],
-    "blocks_per_sm": [2, 3, 4],
-    "woodcock_burst": [1, 2, 4, 8],
+    "blocks_per_sm": [2, 3, 4, 8],
+    "woodcock_burst": [4, 8, 12],
+    "block_size": [128, 256],
 }
 DEFAULTS = {"queue_log2_chunk": 0, "regen_threshold": 0, "interact_threshold": 0, "blocks_per_sm": 0,
-            "woodcock_burst": 0}  # 0: the library's default
+            "woodcock_burst": 0, "block_size": 0}  # 0: the library's default
 CHAINS = [1, 2, 3, 4, 6]
 
 

@@ -987,7 +987,8 @@ LaunchPlan plan_launch(dxmc_gpu_ctx* ctx, const dxmc_world* world, const dxmc_lu
     p.lut_in_smem = lut_bytes <= smem_limit ? 1 : 0;
     const bool palette = world->palette_index != nullptr;
     L.smem = dev::transport_smem_bytes(lut_bytes, p.lut_in_smem != 0, palette);
-    L.block = ctx->options.block_size > 0 ? ctx->options.block_size : 256;
+    L.block = jd->block_size == 128 || jd->block_size == 256 ? jd->block_size
+                                                              : (ctx->options.block_size > 0 ? ctx->options.block_size : 256);
     // also sets the kernel's dynamic shared-memory limit for this launch
     const int occ = dev::transport_max_blocks_per_sm(model, palette, L.block, L.smem);
     int per_sm = jd->blocks_per_sm > 0 ? std::min(jd->blocks_per_sm, std::max(occ, 1))

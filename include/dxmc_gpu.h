@@ -249,7 +249,7 @@ typedef struct dxmc_job_desc {
     int32_t blocks_per_sm;              /* resident blocks per SM (1..occupancy limit) */
     int32_t queue_log2_chunk;           /* photon queue chunk 2^n; -1 = photons generated in the kernel */
     int32_t woodcock_burst;             /* Woodcock steps a lane may take per loop iteration (1..64) */
-    int32_t pad;
+    int32_t block_size;                 /* threads per block of the transport kernel: 128 or 256 */
 } dxmc_job_desc;
 
 typedef struct dxmc_job_stats {
