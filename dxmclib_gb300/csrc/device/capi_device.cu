@@ -509,8 +509,10 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
         P.lower[i] = static_cast<float>(d->origin[i] - 0.5 * static_cast<double>(d->dims[i]) * d->spacing[i]);
     }
     world_extents(d->dims, d->spacing, d->origin, P.lo, P.hi);
-    for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i) {
         P.lo_inv[i] = P.lo[i] * P.inv_spacing[i];
+        P.dims_f[i] = static_cast<float>(d->dims[i]);
+    }
     P.nxy = d->dims[0] * d->dims[1];
     P.n_voxels = n;
     *out = w;

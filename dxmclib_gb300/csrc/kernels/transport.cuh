@@ -25,6 +25,7 @@ struct WorldParams {
     float hi[3];          // nextafter-safe upper extent
     float inv_spacing[3]; // 1 / spacing (mm)
     float lo_inv[3];      // lo * inv_spacing (voxel index as one FMA)
+    float dims_f[3];      // dims as floats (grid coordinates are inside in [0, dims))
     float spacing[3];     // voxel size (mm)
     float lower[3];       // lower grid corner (mm), the plane of voxel boundary 0
     uint64_t nxy;

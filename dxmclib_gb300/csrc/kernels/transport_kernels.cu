@@ -552,25 +552,29 @@ namespace {
             // forced-scoring voxel.  Each lane draws its own stream in the reference's
             // order, so the burst length changes the schedule, not the histories.
             const int burst = max(p.woodcock_burst, 1); // at least one step: every iteration makes progress
-            for (int k = 0; k < burst; ++k) {
+            if (s.hist_steps > MAX_STEPS_PER_HISTORY) {
+                // bounded work per history (checked per burst: at most burst - 1 steps over)
+                ++s.overflows;
+                s.alive = false;
+            }
+            for (int k = 0; k < burst && s.alive; ++k) {
                 const float step = -__log2f(s.rng.uniform_open()) * s.stepK;
                 s.ph.px = fmaf(s.ph.dx, step, s.ph.px);
                 s.ph.py = fmaf(s.ph.dy, step, s.ph.py);
                 s.ph.pz = fmaf(s.ph.dz, step, s.ph.pz);
-                if (!inside(w, s.ph.px, s.ph.py, s.ph.pz)) {
+                // grid coordinates (p - lo) / spacing as one FMA each; the photon is inside
+                // while all three lie in [0, dims), which also bounds the voxel index
+                const float fx = fmaf(s.ph.px, w.inv_spacing[0], -w.lo_inv[0]);
+                const float fy = fmaf(s.ph.py, w.inv_spacing[1], -w.lo_inv[1]);
+                const float fz = fmaf(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2]);
+                if (!(fx >= 0.0f && fx < w.dims_f[0] && fy >= 0.0f && fy < w.dims_f[1] && fz >= 0.0f && fz < w.dims_f[2])) {
                     s.alive = false;
                     break;
                 }
-                if (++s.hist_steps > MAX_STEPS_PER_HISTORY) {
-                    // bounded work per history: end it and report the overflow
-                    ++s.overflows;
-                    s.alive = false;
-                    break;
-                }
-                // (p - lo) / spacing as one FMA; a tiny negative value converts to 0
-                const uint32_t ix = min(static_cast<uint32_t>(fmaf(s.ph.px, w.inv_spacing[0], -w.lo_inv[0])), w.dims[0] - 1);
-                const uint32_t iy = min(static_cast<uint32_t>(fmaf(s.ph.py, w.inv_spacing[1], -w.lo_inv[1])), w.dims[1] - 1);
-                const uint32_t iz = min(static_cast<uint32_t>(fmaf(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2])), w.dims[2] - 1);
+                ++s.hist_steps;
+                const uint32_t ix = static_cast<uint32_t>(fx);
+                const uint32_t iy = static_cast<uint32_t>(fy);
+                const uint32_t iz = static_cast<uint32_t>(fz);
                 if (w.n_voxels <= 0xffffffffull)
                     s.vidx = iz * static_cast<uint32_t>(w.nxy) + (iy * w.dims[0] + ix);
                 else
