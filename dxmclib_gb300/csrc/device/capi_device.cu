@@ -399,7 +399,7 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     unsigned int* d_count = nullptr;
     unsigned int distinct = 0;
     std::vector<dev::PaletteEntry> palette;
-    if (e == cudaSuccess && d->layout == 0) {
+    if (e == cudaSuccess && d->layout == 0 && n <= 0xffffffffull) { // the compact layout indexes voxels in 32 bits
         e = cudaMallocAsync(&d_table, dev_palette_table_bytes(), ctx->stream);
         if (e == cudaSuccess)
             e = cudaMallocAsync(&d_count, sizeof(unsigned int), ctx->stream);

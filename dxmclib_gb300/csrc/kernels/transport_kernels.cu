@@ -479,6 +479,7 @@ namespace {
         float p0, p01;  // photoelectric and photoelectric + Compton shares of the attenuation
         uint64_t vidx;
         float forced_wc; // weight correction waiting for a forced-voxel interaction pass
+        bool armed;      // energy x weight is below the Russian-roulette threshold
         uint32_t steps, deposits, overflows, histories;
 
         __device__ void reset_counters() { steps = deposits = overflows = histories = 0; }
@@ -490,7 +491,11 @@ namespace {
             cached_mat = -1;
             hist_steps = 0;
             forced_wc = 0.0f;
+            arm();
         }
+        // energy and weight change only at interactions and roulette: the roulette
+        // test of a virtual step reads this flag
+        __device__ void arm() { armed = ph.energy * ph.weight < ROULETTE_THRESHOLD; }
     };
 
     // Loads photon + stream state from the pre-generated queue.
@@ -575,7 +580,7 @@ namespace {
                 const uint32_t ix = static_cast<uint32_t>(fx);
                 const uint32_t iy = static_cast<uint32_t>(fy);
                 const uint32_t iz = static_cast<uint32_t>(fz);
-                if (w.n_voxels <= 0xffffffffull)
+                if constexpr (PALETTE) // compact worlds have fewer than 2^32 voxels (world upload)
                     s.vidx = iz * static_cast<uint32_t>(w.nxy) + (iy * w.dims[0] + ix);
                 else
                     s.vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
@@ -603,12 +608,13 @@ namespace {
                         break;
                     }
                     // virtual collision: Russian roulette (transport.hpp:684-694)
-                    if (s.ph.energy * s.ph.weight < ROULETTE_THRESHOLD) {
+                    if (s.armed) {
                         if (s.rng.uniform() < ROULETTE_PROBABILITY) {
                             s.alive = false;
                             break;
                         }
                         s.ph.weight *= 1.0f / (1.0f - ROULETTE_PROBABILITY);
+                        s.arm();
                     }
                 } else {
                     // forced photoelectric scoring (computeInteractionsForced): score the forced
@@ -704,13 +710,14 @@ namespace {
             }
         }
         if (check_roulette) {
-            // Russian roulette (transport.hpp:684-694)
+            // Russian roulette (transport.hpp:684-694) after an interaction or a forced step
             if (s.ph.energy * s.ph.weight < ROULETTE_THRESHOLD) {
                 if (s.rng.uniform() < ROULETTE_PROBABILITY)
                     s.alive = false;
                 else
                     s.ph.weight *= 1.0f / (1.0f - ROULETTE_PROBABILITY);
             }
+            s.arm();
         }
         if (do_score && !isfinite(deposit)) {
             // never let a non-finite value into the FP64 accumulators: end the
