@@ -16,9 +16,10 @@ FP32 transport with FP64 tallies.
   device post-processing and D2H of dose, variance and event counts.
 * roofline: algorithmic bytes of the transport kernel per launch,
   5 B per Woodcock step (u8 material + f32 density) + 20 B per deposit
-  (FP64 energy + FP64 energy^2 + u32 count), from the kernel's own step and
-  deposit counters, over the kernel's CUDA-event duration, against the
-  measured HBM copy bandwidth.
+  (FP64 energy + FP64 energy^2 + u32 count), plus 8 B per step for the cell of
+  the local-majorant grid when the job tracks with local majorants, from the
+  kernel's own step and deposit counters, over the kernel's CUDA-event
+  duration, against the measured HBM copy bandwidth.
 * cpu_baseline / --impl reference: the oracle port (a C++ restatement of the
   reference transport, oracle/port) on the host cores, on a bounded sample of
   the same workload (a subset of the exposures).
@@ -402,6 +403,8 @@ def main():
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--queue-log2", type=int, default=0, help="photon queue chunk 2^n (0 = default: in-kernel generation)")
     ap.add_argument("--burst", type=int, default=0, help="Woodcock steps per loop iteration (0 = library default)")
+    ap.add_argument("--tracking", choices=("local", "global"), default="local",
+                    help="Woodcock majorant: local grid (default) or the reference's global majorant")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-vs-plain mixed-stream leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched DX leg")
     ap.add_argument("--no-precision", action="store_true", help="skip the tally-precision study")
@@ -459,8 +462,10 @@ def main():
 
     wl = build_workload(histories)
     world, src = wl.world, wl.source
+    tracking = A.TRACKING_LOCAL if args.tracking == "local" else A.TRACKING_GLOBAL
     ctx = dx.GpuContext(device=device, block_size=args.block_size, blocks_per_sm=args.blocks_per_sm,
-                        regen_threshold=args.regen, interact_threshold=args.interact, queue_log2_chunk=args.queue_log2)
+                        regen_threshold=args.regen, interact_threshold=args.interact, queue_log2_chunk=args.queue_log2,
+                        tracking=tracking)
     dworld = dx.DeviceWorld(ctx, world, layout=args.layout)
     md = dworld.max_density()
     blob = dx.LutBlob(world.materialMap(), md, src.maxPhotonEnergyProduced())
@@ -508,7 +513,8 @@ def main():
     value = replica_throughput(ws, n_hist, args.steps, total_ms / 1e3)
     steps_per_hist = float(np.mean([s.steps for s in stats])) / n_hist
     deps_per_hist = float(np.mean([s.deposits for s in stats])) / n_hist
-    alg_bytes = 5.0 * np.mean([s.steps for s in stats]) + 20.0 * np.mean([s.deposits for s in stats])
+    step_bytes = 13.0 if tracking == A.TRACKING_LOCAL else 5.0
+    alg_bytes = step_bytes * np.mean([s.steps for s in stats]) + 20.0 * np.mean([s.deposits for s in stats])
     achieved = alg_bytes / (float(kern_ms.mean()) / 1e3) / 1e9
     peak, peak_kind = measured_peaks()
     traffic = committed_traffic()
@@ -596,7 +602,7 @@ def main():
                        "parallelism": f"replicas{ws}",
                        "voxel_layout": "palette-u8" if args.layout == 0 else "8-byte",
                        "regen_threshold": args.regen or "default", "interact_threshold": args.interact or "default",
-                       "woodcock_burst": args.burst or "default"},
+                       "woodcock_burst": args.burst or "default", "tracking": args.tracking},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind,
                          # DRAM bytes per launch from the committed ncu capture of a 1e7-history

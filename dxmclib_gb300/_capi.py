@@ -33,6 +33,7 @@ STATUS_NAMES = {
 MODEL_NONE, MODEL_LIVERMORE, MODEL_IA = 0, 1, 2
 OUTPUT_RAW, OUTPUT_EV_PER_HISTORY, OUTPUT_DOSE = 0, 1, 2
 TALLY_F64, TALLY_F32, TALLY_WARP_F64 = 0, 1, 2
+TRACKING_DEFAULT, TRACKING_GLOBAL, TRACKING_LOCAL = 0, 1, 2
 
 D = C.c_double
 DP = C.POINTER(C.c_double)
@@ -102,7 +103,7 @@ class GpuOptions(C.Structure):
         ("device", C.c_int32), ("block_size", C.c_int32), ("blocks_per_sm", C.c_int32),
         ("tally_mode", C.c_int32), ("memory_budget", C.c_uint64),
         ("regen_threshold", C.c_int32), ("interact_threshold", C.c_int32),
-        ("queue_log2_chunk", C.c_int32), ("pad", C.c_int32),
+        ("queue_log2_chunk", C.c_int32), ("tracking", C.c_int32),
     ]
 
 
@@ -120,6 +121,7 @@ class JobDesc(C.Structure):
         ("seed", C.c_uint64), ("model", C.c_int32), ("tally_mode", C.c_int32),
         ("regen_threshold", C.c_int32), ("interact_threshold", C.c_int32), ("blocks_per_sm", C.c_int32),
         ("queue_log2_chunk", C.c_int32), ("woodcock_burst", C.c_int32), ("block_size", C.c_int32),
+        ("tracking", C.c_int32), ("pad", C.c_int32),
     ]
 
 
@@ -164,6 +166,8 @@ SIGNATURES = {
     "dxmc_gpu_world_upload": (C.c_int, [VP, C.POINTER(WorldDesc), C.POINTER(VP)]),
     "dxmc_gpu_world_max_density": (C.c_int, [VP, DP, C.c_int]),
     "dxmc_gpu_world_free": (None, [VP]),
+    "dxmc_gpu_world_prepare": (C.c_int, [VP, VP, VP]),
+    "dxmc_gpu_world_majorant": (C.c_int, [VP, VP, VP, C.POINTER(C.c_uint32), C.POINTER(C.c_int32), FP]),
     "dxmc_gpu_lut_upload": (C.c_int, [VP, VP, C.POINTER(VP)]),
     "dxmc_gpu_lut_free": (None, [VP]),
     "dxmc_gpu_job_submit": (C.c_int, [VP, VP, VP, C.POINTER(JobDesc), C.POINTER(VP)]),

@@ -816,13 +816,17 @@ class GpuContext:
 
     def __init__(self, device: int = 0, block_size: int = 0, blocks_per_sm: int = 0, tally_mode: int = A.TALLY_F64,
                  memory_budget: int = 0, regen_threshold: int = 0, interact_threshold: int = 0,
-                 queue_log2_chunk: int = 0):
+                 queue_log2_chunk: int = 0, tracking: int = A.TRACKING_DEFAULT):
+        """``tracking``: A.TRACKING_LOCAL (default) draws Woodcock flights with the
+        local-majorant grid of each (world, LUT) pair, A.TRACKING_GLOBAL with the
+        reference's single global majorant; both sample the same process."""
         self.lib = A.load()
         opts = A.GpuOptions(device, block_size, blocks_per_sm, tally_mode, memory_budget, regen_threshold,
-                            interact_threshold, queue_log2_chunk, 0)
+                            interact_threshold, queue_log2_chunk, tracking)
         self.options = dict(device=device, block_size=block_size, blocks_per_sm=blocks_per_sm, tally_mode=tally_mode,
                             memory_budget=memory_budget, regen_threshold=regen_threshold,
-                            interact_threshold=interact_threshold, queue_log2_chunk=queue_log2_chunk)
+                            interact_threshold=interact_threshold, queue_log2_chunk=queue_log2_chunk,
+                            tracking=tracking)
         self.handle = C.c_void_p()
         self._children = weakref.WeakSet()
         A.check(self.lib.dxmc_gpu_ctx_create(C.byref(opts), C.byref(self.handle)), None, "dxmc_gpu_ctx_create")
@@ -886,6 +890,25 @@ class DeviceWorld:
                                                         r.ctypes.data_as(A.FP), len(r), out.ctypes.data_as(A.DP)),
                 self.ctx.handle, "dxmc_gpu_radiological_path")
         return out
+
+    def prepare(self, dlut: "DeviceLut"):
+        """Builds the local-majorant grid for ``dlut`` ahead of the first job
+        (dxmc_gpu_world_prepare); jobs with local tracking otherwise build it on first use."""
+        A.check(self.ctx.lib.dxmc_gpu_world_prepare(self.ctx.handle, self.handle, dlut.handle), self.ctx.handle,
+                "dxmc_gpu_world_prepare")
+
+    def majorant(self, dlut: "DeviceLut"):
+        """The local-majorant grid built for ``dlut``: (shift (3,), cells (nz, ny, nx, 2)
+        holding 1 / scale and R in mm)."""
+        n = (C.c_uint32 * 3)()
+        sh = (C.c_int32 * 3)()
+        A.check(self.ctx.lib.dxmc_gpu_world_majorant(self.ctx.handle, self.handle, dlut.handle, n, sh, None),
+                self.ctx.handle, "dxmc_gpu_world_majorant")
+        cells = np.zeros((n[2], n[1], n[0], 2), np.float32)
+        A.check(self.ctx.lib.dxmc_gpu_world_majorant(self.ctx.handle, self.handle, dlut.handle, n, sh,
+                                                     cells.ctypes.data_as(A.FP)), self.ctx.handle,
+                "dxmc_gpu_world_majorant")
+        return np.array(sh[:], np.int64), cells
 
     def max_density(self) -> np.ndarray:
         n = len(self.world.materialMap())
@@ -1033,12 +1056,15 @@ class Job:
     def __init__(self, ctx: GpuContext, dworld: DeviceWorld, dlut: DeviceLut, exposures: ExposureTable,
                  spectrum: Optional[Spectrum] = None, heel: Optional[HeelTable] = None, bowtie=None,
                  seed: int = 1, model: int = LOWENERGYCORRECTION.LIVERMORE, tally_mode: int = -1,
-                 launch: Optional[dict] = None):
-        """``launch`` may set regen_threshold, interact_threshold, blocks_per_sm and
-        queue_log2_chunk for this job (an autotuner's choice); unset keys use the context's."""
+                 launch: Optional[dict] = None, tracking: int = A.TRACKING_DEFAULT):
+        """``launch`` may set the keys of LAUNCH_KEYS for this job (an autotuner's
+        choice); unset keys use the context's.  ``tracking``: A.TRACKING_* (the
+        context's when DEFAULT)."""
         self.ctx = ctx
         self.dworld = dworld
         self._owned = True
+        if tracking != A.TRACKING_DEFAULT:
+            launch = dict(launch or {}, tracking=tracking)
         jd = self._describe(exposures, spectrum, heel, bowtie, seed, model, tally_mode, launch)
         self.handle = C.c_void_p()
         A.check(ctx.lib.dxmc_gpu_job_submit(ctx.handle, dworld.handle, dlut.handle, C.byref(jd), C.byref(self.handle)),
@@ -1053,7 +1079,7 @@ class Job:
         return j
 
     LAUNCH_KEYS = ("regen_threshold", "interact_threshold", "blocks_per_sm", "queue_log2_chunk", "woodcock_burst",
-                   "block_size")
+                   "block_size", "tracking")
 
     def _describe(self, exposures: ExposureTable, spectrum, heel, bowtie, seed, model, tally_mode,
                   launch: Optional[dict] = None) -> A.JobDesc:

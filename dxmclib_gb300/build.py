@@ -33,6 +33,7 @@ CUDA_SOURCES = [
     CSRC / "device" / "capi_device.cu",
     CSRC / "device" / "noalloc.cu",
     CSRC / "kernels" / "siddon_kernels.cu",
+    CSRC / "kernels" / "majorant_kernels.cu",
 ]
 INCLUDES = [f"-I{REPO / 'include'}", f"-I{CSRC}"]
 

@@ -8,6 +8,7 @@
 #include "../kernels/transport.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -53,8 +54,20 @@ struct dxmc_gpu_ctx {
     size_t max_smem_optin = 0;
 };
 
+// Local-majorant grid of the world for one LUT (built on first use, kept until
+// the world is freed; see MajorantGrid).
+struct MajorantCache {
+    uint64_t lut_serial = 0;
+    float2* cells = nullptr;
+    uint64_t bytes = 0;
+    uint64_t last_use = 0;
+    dev::MajorantGrid grid {};
+};
+
 struct dxmc_world {
     dxmc_gpu_ctx* ctx = nullptr;
+    std::vector<MajorantCache> majorants;
+    uint64_t majorant_clock = 0;
     dev::Voxel* voxels = nullptr;
     uint8_t* palette_index = nullptr;      // compact layout, null if not used
     dev::PaletteEntry* palette = nullptr;
@@ -74,6 +87,9 @@ struct dxmc_lut {
     float* image = nullptr;
     dev::LutMeta meta {};
     uint64_t bytes = 0;
+    uint64_t serial = 0;              // unique per upload: key of the worlds' majorant grids
+    std::vector<float> majorant_ratio; // r_m: max over energies of mu_m(E) / global majorant (per g/cm3)
+    float mu_ref = 0.0f;              // global majorant (1/mm) at half the LUT's maximum energy
 };
 
 struct dxmc_job {
@@ -117,6 +133,43 @@ int cuda_fail(dxmc_gpu_ctx* ctx, cudaError_t e, const char* what)
     } while (0)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Per material m, the largest ratio of its attenuation (per g/cm3) to the global
+// majorant over the LUT's energies, from the float image the kernels read: in
+// each log-log segment both are exponentials of log E, so the ratio of their sum
+// to the majorant is convex in log E and peaks at a segment end.  Each segment is
+// evaluated at its own nodes and both neighbours', which covers either convention
+// of which node interval a segment index serves.  A 0.2 % margin covers the
+// device's exponential and the rounding of the level arithmetic.  mu_ref: the
+// global majorant (1/mm) at half the maximum energy, the reference point of the
+// grid's cost model.
+void majorant_ratios(const std::vector<float>& img, const dev::LutMeta& m, std::vector<float>& ratio, float& mu_ref)
+{
+    const int R = m.R;
+    const float* x = img.data() + m.off_x;
+    const float* maxc = img.data() + m.off_maxcoef;
+    ratio.assign(m.n_materials, 0.0f);
+    for (int mat = 0; mat < m.n_materials; ++mat) {
+        double r = 0.0;
+        for (int seg = 0; seg < R; ++seg) {
+            const float* c = img.data() + m.off_coef + (static_cast<size_t>(mat) * R + seg) * 6;
+            for (int k = std::max(seg - 1, 0); k <= std::min(seg + 1, R - 1); ++k) {
+                const double lx = x[k];
+                double tot = 0.0;
+                for (int t = 0; t < 3; ++t)
+                    tot += std::pow(10.0, c[2 * t] + c[2 * t + 1] * lx);
+                const double inv = std::pow(10.0, maxc[2 * seg] + maxc[2 * seg + 1] * lx);
+                r = std::max(r, tot * inv);
+            }
+        }
+        ratio[mat] = static_cast<float>(r * 1.002);
+    }
+    const double le = std::log10(std::max(static_cast<double>(m.max_energy) * 0.5, 1.0));
+    int seg = static_cast<int>(std::upper_bound(x, x + R, static_cast<float>(le)) - x);
+    seg = std::min(std::max(seg, 0), R - 1);
+    const double inv_cm = std::pow(10.0, maxc[2 * seg] + maxc[2 * seg + 1] * le);
+    mu_ref = static_cast<float>(inv_cm > 0 ? 0.1 / inv_cm : 0.01);
+}
 
 size_t dev_palette_table_bytes();
 
@@ -238,6 +291,7 @@ namespace {
 void sync_ctx_streams(dxmc_gpu_ctx* ctx);
 void release_engines(dxmc_gpu_ctx* ctx);
 int wait_event(dxmc_gpu_ctx* ctx, cudaEvent_t ev, int64_t timeout_ms, const char* what);
+int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool build, const dev::MajorantGrid** out);
 } // namespace
 
 int dxmc_gpu_device_count(void)
@@ -288,7 +342,8 @@ int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out)
     if (options)
         ctx->options = *options;
     ctx->device = ctx->options.device;
-    if (ctx->device < 0 || ctx->device >= count) {
+    if (ctx->device < 0 || ctx->device >= count || ctx->options.tracking < DXMC_TRACKING_DEFAULT
+        || ctx->options.tracking > DXMC_TRACKING_LOCAL) {
         delete ctx;
         return DXMC_ERR_INVALID;
     }
@@ -566,9 +621,55 @@ void dxmc_gpu_world_free(dxmc_world* w)
         cudaFreeAsync(w->palette_index, w->ctx->stream);
     if (w->palette)
         cudaFreeAsync(w->palette, w->ctx->stream);
+    for (auto& m : w->majorants) {
+        cudaFreeAsync(m.cells, w->ctx->stream);
+        w->ctx->in_use -= m.bytes;
+    }
     cudaStreamSynchronize(w->ctx->stream);
     w->ctx->in_use -= w->bytes;
     delete w;
+}
+
+int dxmc_gpu_world_prepare(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut)
+{
+    if (!ctx || !world || !lut)
+        return DXMC_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    if (world->ctx != ctx || lut->ctx != ctx)
+        return fail(ctx, DXMC_ERR_INVALID, "world or lut belongs to another context");
+    cudaSetDevice(ctx->device);
+    const dev::MajorantGrid* grid = nullptr;
+    const int rc = world_majorant(ctx, world, lut, true, &grid);
+    if (rc != DXMC_OK)
+        return rc;
+    const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? DXMC_OK : cuda_fail(ctx, e, "local-majorant grid");
+}
+
+int dxmc_gpu_world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut, uint32_t* cells_per_axis,
+    int32_t* shift, float* cells)
+{
+    if (!ctx || !world || !lut || !cells_per_axis || !shift)
+        return DXMC_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    const dev::MajorantGrid* g = nullptr;
+    world_majorant(ctx, world, lut, false, &g);
+    if (!g)
+        return fail(ctx, DXMC_ERR_STATE, "no local-majorant grid for this world and lut");
+    for (int a = 0; a < 3; ++a) {
+        shift[a] = g->shift[a];
+        cells_per_axis[a] = static_cast<uint32_t>((world->dims[a] + (1ull << g->shift[a]) - 1) >> g->shift[a]);
+    }
+    if (cells) {
+        cudaSetDevice(ctx->device);
+        const uint64_t n = static_cast<uint64_t>(cells_per_axis[0]) * cells_per_axis[1] * cells_per_axis[2];
+        cudaError_t e = cudaMemcpyAsync(cells, g->cells, n * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "local-majorant grid read");
+    }
+    return DXMC_OK;
 }
 
 int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* b, dxmc_lut** out)
@@ -654,6 +755,9 @@ int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* b, dxmc_lut** ou
         return DXMC_ERR_OOM;
     lut->ctx = ctx;
     lut->meta = m;
+    static std::atomic<uint64_t> lut_serials { 0 };
+    lut->serial = ++lut_serials;
+    majorant_ratios(img, m, lut->majorant_ratio, lut->mu_ref);
     lut->bytes = img.size() * sizeof(float);
     cudaError_t e = cudaMallocAsync(&lut->image, lut->bytes, ctx->stream);
     if (e == cudaSuccess)
@@ -722,6 +826,135 @@ namespace {
 // Photon queue of a job: its own buffer (single jobs), none (photons generated in
 // the persistent multi-job kernel) or a buffer shared by the jobs of one batch
 // chain, which run one after another on the chain's stream.
+// ---- local-majorant grids ------------------------------------------------------------
+constexpr int MAJORANT_LEVELS_PER_OCTAVE = 4;
+constexpr int MAJORANT_MAX_LEVEL = 48;            // scale 2^-12: empty and air cells
+constexpr double MAJORANT_CELL_MM = 6.0;          // target cell edge
+constexpr uint64_t MAJORANT_MAX_CELLS_PER_AXIS = 1024;
+constexpr size_t MAJORANT_GRIDS_PER_WORLD = 4;    // one per LUT used with the world, least recently used evicted
+
+int majorant_level(float m)
+{
+    if (m >= 1.0f)
+        return 0;
+    if (!(m > 0.0f))
+        return MAJORANT_MAX_LEVEL;
+    int lv = std::min(MAJORANT_MAX_LEVEL, static_cast<int>(std::floor(-MAJORANT_LEVELS_PER_OCTAVE * std::log2(m))));
+    while (lv > 0 && std::exp2(-static_cast<double>(lv) / MAJORANT_LEVELS_PER_OCTAVE) < m)
+        --lv;
+    return lv;
+}
+
+// The local-majorant grid of (world, lut): found in the world's cache, else (if
+// build) built on the context stream and cached.  Caller holds the context mutex.
+int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool build, const dev::MajorantGrid** out)
+{
+    *out = nullptr;
+    for (auto& m : w->majorants) {
+        if (m.lut_serial == lut->serial) {
+            m.last_use = ++w->majorant_clock;
+            *out = &m.grid;
+            return DXMC_OK;
+        }
+    }
+    if (!build)
+        return DXMC_OK;
+    if (lut->meta.n_materials < w->n_materials)
+        return fail(ctx, DXMC_ERR_INVALID, "lut has fewer materials than the world");
+    dev::MajorantBuild b {};
+    uint64_t ncell = 1;
+    for (int a = 0; a < 3; ++a) {
+        int sh = static_cast<int>(std::lround(std::log2(std::max(MAJORANT_CELL_MM / w->spacing[a], 1.0))));
+        sh = std::min(std::max(sh, 0), 6);
+        while (((w->dims[a] + (1ull << sh) - 1) >> sh) > MAJORANT_MAX_CELLS_PER_AXIS)
+            ++sh;
+        b.shift[a] = sh;
+        b.n[a] = static_cast<uint32_t>((w->dims[a] + (1ull << sh) - 1) >> sh);
+        b.edge[a] = static_cast<float>(w->spacing[a] * static_cast<double>(1ull << sh));
+        ncell *= b.n[a];
+    }
+    b.mu_ref = lut->mu_ref;
+    b.levels_per_octave = MAJORANT_LEVELS_PER_OCTAVE;
+    b.max_level = MAJORANT_MAX_LEVEL;
+    // voxel scales and the levels worth trying: the palette's own levels, or every
+    // second level for the 8-byte layout
+    dev::MajorantScales scales {};
+    uint64_t levels = 0;
+    if (w->palette_index) {
+        for (size_t i = 0; i < w->host_palette.size() && i < static_cast<size_t>(dev::PALETTE_MAX); ++i) {
+            const auto& pe = w->host_palette[i];
+            const int mat = static_cast<int>(pe.code & 0xffu);
+            const bool meas = ((pe.code >> 8) & 0xffu) != 0;
+            const float sc = meas ? 1.0f : pe.density * lut->majorant_ratio[mat];
+            scales.v[i] = sc;
+            levels |= 1ull << majorant_level(sc);
+        }
+    } else {
+        for (int m = 0; m < lut->meta.n_materials && m < dev::PALETTE_MAX; ++m)
+            scales.v[m] = lut->majorant_ratio[m];
+        for (int lv = 2; lv <= MAJORANT_MAX_LEVEL; lv += 2)
+            levels |= 1ull << lv;
+    }
+    const uint64_t cell_bytes = ncell * sizeof(float2);
+    if (ctx->in_use + cell_bytes > ctx->budget)
+        return fail(ctx, DXMC_ERR_OOM, "local-majorant grid exceeds the device memory budget");
+    if (w->majorants.size() >= MAJORANT_GRIDS_PER_WORLD) {
+        auto victim = std::min_element(w->majorants.begin(), w->majorants.end(),
+            [](const MajorantCache& a, const MajorantCache& c) { return a.last_use < c.last_use; });
+        sync_ctx_streams(ctx); // no queued job still reads the grid
+        cudaFreeAsync(victim->cells, ctx->stream);
+        ctx->in_use -= victim->bytes;
+        w->majorants.erase(victim);
+    }
+    cudaStream_t s = ctx->stream;
+    float2* cells = nullptr;
+    uint8_t* level = nullptr;
+    float *d0 = nullptr, *d1 = nullptr, *cost = nullptr;
+    cudaError_t e = cudaMallocAsync(&cells, cell_bytes, s);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&level, ncell, s);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&d0, ncell * sizeof(float), s);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&d1, ncell * sizeof(float), s);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&cost, ncell * sizeof(float), s);
+    if (e == cudaSuccess)
+        e = dev::launch_majorant_levels(w->params, scales, b, level, cells, cost, s);
+    for (int lv = 1; lv <= MAJORANT_MAX_LEVEL && e == cudaSuccess; ++lv)
+        if (levels >> lv & 1ull)
+            e = dev::launch_majorant_level_pass(b, level, lv, d0, d1, cells, cost, s);
+    for (void* ptr : { static_cast<void*>(level), static_cast<void*>(d0), static_cast<void*>(d1), static_cast<void*>(cost) })
+        if (ptr)
+            cudaFreeAsync(ptr, s);
+    if (e != cudaSuccess) {
+        if (cells)
+            cudaFreeAsync(cells, s);
+        cudaStreamSynchronize(s);
+        return cuda_fail(ctx, e, "local-majorant grid");
+    }
+    MajorantCache m;
+    m.lut_serial = lut->serial;
+    m.cells = cells;
+    m.bytes = cell_bytes;
+    m.last_use = ++w->majorant_clock;
+    m.grid.cells = cells;
+    m.grid.nx = b.n[0];
+    m.grid.nxy = b.n[0] * b.n[1];
+    for (int a = 0; a < 3; ++a)
+        m.grid.shift[a] = b.shift[a];
+    ctx->in_use += cell_bytes;
+    w->majorants.push_back(m);
+    *out = &w->majorants.back().grid;
+    return DXMC_OK;
+}
+
+int job_tracking(const dxmc_gpu_ctx* ctx, const dxmc_job_desc* jd)
+{
+    const int t = jd->tracking != DXMC_TRACKING_DEFAULT ? jd->tracking : ctx->options.tracking;
+    return t == DXMC_TRACKING_GLOBAL ? DXMC_TRACKING_GLOBAL : DXMC_TRACKING_LOCAL;
+}
+
 enum class QueueMode { own, none, shared };
 
 int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_job_desc* jd, QueueMode qmode,
@@ -739,6 +972,8 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     const int tally_mode = jd->tally_mode >= 0 ? jd->tally_mode : ctx->options.tally_mode;
     if (tally_mode < 0 || tally_mode > 2)
         return fail(ctx, DXMC_ERR_INVALID, "unknown tally mode");
+    if (jd->tracking < DXMC_TRACKING_DEFAULT || jd->tracking > DXMC_TRACKING_LOCAL)
+        return fail(ctx, DXMC_ERR_INVALID, "unknown tracking mode");
 
     // ---- host-side tables: exposures, prefix offsets, spectrum, heel, bow-tie ----
     const uint64_t ne = jd->n_exposures;
@@ -850,6 +1085,14 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
         return fail(ctx, DXMC_ERR_OOM, "job exceeds the device memory budget");
 
     cudaSetDevice(ctx->device);
+    const dev::MajorantGrid* grid = nullptr;
+    if (job_tracking(ctx, jd) == DXMC_TRACKING_LOCAL) {
+        const int rc = world_majorant(ctx, world, lut, true, &grid);
+        if (rc != DXMC_OK)
+            return rc;
+        if (ctx->in_use + job_bytes > ctx->budget)
+            return fail(ctx, DXMC_ERR_OOM, "job exceeds the device memory budget");
+    }
     auto* j = new (std::nothrow) dxmc_job;
     if (!j)
         return DXMC_ERR_OOM;
@@ -953,6 +1196,8 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
         p.interact_threshold = inter > 0 ? std::min(inter, 32) : (queued ? DEFAULT_QUEUE_INTERACT_THRESHOLD : DEFAULT_INTERACT_THRESHOLD);
         p.woodcock_burst = jd->woodcock_burst > 0 ? std::min(jd->woodcock_burst, 64) : DEFAULT_WOODCOCK_BURST;
     }
+    if (grid)
+        p.majorant = *grid;
 
 
     chunk_out = chunk;
@@ -1895,5 +2140,14 @@ const float* lut_image(const dxmc_lut* l, dev::LutMeta* meta, const dxmc_gpu_ctx
     *owner = l->ctx;
     *meta = l->meta;
     return l->image;
+}
+// The local-majorant grid of (world, lut) if the job tracks with local majorants
+// and the grid was built before (no allocation here); else nullptr.
+const dev::MajorantGrid* built_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* l, const dxmc_job_desc* jd)
+{
+    const dev::MajorantGrid* g = nullptr;
+    if (job_tracking(ctx, jd) == DXMC_TRACKING_LOCAL)
+        world_majorant(ctx, w, l, false, &g);
+    return g;
 }
 } // namespace dxmc_gb300::capi

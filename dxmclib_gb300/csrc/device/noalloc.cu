@@ -19,7 +19,10 @@
 // until the process exits.  All calls share it: calls that overlap on the GPU
 // race with each other, so issue them one at a time.  The first call on each
 // device looks up the array's device address (cudaGetSymbolAddress) with that
-// device current; make that first call before any stream capture.
+// device current; make that first call before any stream capture.  Local-majorant
+// tracking uses the (world, LUT) grid only if it was built before
+// (dxmc_gpu_world_prepare, or an earlier job on the pair); otherwise the call
+// tracks with the global majorant.
 #include "dxmc_gpu.h"
 
 #include "../kernels/transport.cuh"
@@ -214,6 +217,7 @@ int ctx_interact_threshold(const dxmc_gpu_ctx* ctx);
 int default_woodcock_burst();
 const dev::WorldParams* world_params(const dxmc_world* w, const dxmc_gpu_ctx** owner, int* n_materials);
 const float* lut_image(const dxmc_lut* l, dev::LutMeta* meta, const dxmc_gpu_ctx** owner);
+const dev::MajorantGrid* built_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* l, const dxmc_job_desc* jd);
 }
 
 namespace {
@@ -257,6 +261,8 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         return reject(ctx, "invalid bow-tie table");
     if (bowtie_n > NOALLOC_MAX_BOWTIE)
         return reject(ctx, "dxmc_gpu_transport_noalloc: " + std::to_string(bowtie_n) + " bow-tie points exceed the maximum of " + std::to_string(NOALLOC_MAX_BOWTIE));
+    if (jd->tracking < DXMC_TRACKING_DEFAULT || jd->tracking > DXMC_TRACKING_LOCAL)
+        return reject(ctx, "dxmc_gpu_transport_noalloc: unknown tracking mode");
     if (jd->model < 0 || jd->model > 2)
         return reject(ctx, "unknown low-energy correction model");
     if (meta.n_materials < world_materials)
@@ -337,6 +343,9 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         p.regen_threshold = capi::ctx_regen_threshold(ctx);
         p.interact_threshold = capi::ctx_interact_threshold(ctx);
         p.woodcock_burst = jd->woodcock_burst > 0 ? std::min(jd->woodcock_burst, 64) : capi::default_woodcock_burst();
+        // local majorants only from a grid built earlier (dxmc_gpu_world_prepare or a job)
+        if (const dev::MajorantGrid* g = capi::built_majorant(ctx, world, lut, jd))
+            p.majorant = *g;
         const size_t lut_bytes = static_cast<size_t>(meta.total_floats) * sizeof(float);
         const size_t smem_limit = std::min<size_t>(capi::ctx_max_smem(ctx), 96 * 1024);
         p.lut_in_smem = lut_bytes <= smem_limit ? 1 : 0;

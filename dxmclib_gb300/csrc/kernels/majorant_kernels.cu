@@ -1,0 +1,202 @@
+// Construction of the local-majorant grid of a (world, LUT) pair.
+//
+// The reference tracks every photon with one global majorant: the largest
+// attenuation of any material at its largest density (woodcockParticleTracking,
+// transport.hpp:640-700, with AttenuationLut::maxMassTotalAttenuation).  In a CT
+// body phantom that bound is set by cortical bone, so in air, lung and soft
+// tissue nearly every Woodcock step is a virtual collision.  The grid built here
+// lets the transport kernel use a smaller majorant where the neighbourhood of a
+// photon allows it (see MajorantGrid in transport.cuh):
+//
+//   1. every voxel gets a scale s_v = density * r_m, with r_m the largest ratio
+//      of material m's attenuation to the global majorant over the LUT's energy
+//      range (1 for voxels of forced-interaction scoring, which keep the
+//      reference's majorant); each cell takes the maximum over its voxels,
+//      rounded up to a level 2^(-level / levels_per_octave);
+//   2. for each level present, the cells above it are dilated by one cell and a
+//      Euclidean distance transform (three separable passes over the cell grid,
+//      cell sizes in mm) gives every other cell the distance R to the nearest
+//      point of a cell above the level: a flight of length at most R from
+//      anywhere in the cell stays where the level's scale bounds the attenuation;
+//   3. each cell keeps the (level, R) of smallest expected steps per mm,
+//      mu / (1 - exp(-mu R)) with mu = scale * global majorant at a reference
+//      energy, or the global majorant itself (R infinite).
+#include <cmath>
+
+#include "transport.cuh"
+
+namespace dxmc_gb300::dev {
+
+namespace {
+
+__device__ __forceinline__ void cell_coords(uint64_t c, const MajorantBuild& b, uint32_t& cx, uint32_t& cy, uint32_t& cz)
+{
+    cx = static_cast<uint32_t>(c % b.n[0]);
+    const uint64_t t = c / b.n[0];
+    cy = static_cast<uint32_t>(t % b.n[1]);
+    cz = static_cast<uint32_t>(t / b.n[1]);
+}
+
+__device__ __forceinline__ float level_scale(int level, int per_octave)
+{
+    return exp2f(-static_cast<float>(level) / static_cast<float>(per_octave));
+}
+
+__global__ void majorant_level_kernel(WorldParams w, const __grid_constant__ MajorantScales scales, MajorantBuild b,
+    uint8_t* __restrict__ level, float2* __restrict__ cells, float* __restrict__ cost)
+{
+    __shared__ float scale_table[PALETTE_MAX];
+    for (int i = threadIdx.x; i < PALETTE_MAX; i += blockDim.x)
+        scale_table[i] = scales.v[i];
+    __syncthreads();
+    const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
+    for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < ncell;
+         c += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        uint32_t cx, cy, cz;
+        cell_coords(c, b, cx, cy, cz);
+        const uint32_t x0 = cx << b.shift[0], x1 = min(w.dims[0], (cx + 1) << b.shift[0]);
+        const uint32_t y0 = cy << b.shift[1], y1 = min(w.dims[1], (cy + 1) << b.shift[1]);
+        const uint32_t z0 = cz << b.shift[2], z1 = min(w.dims[2], (cz + 1) << b.shift[2]);
+        float m = 0.0f;
+        for (uint32_t z = z0; z < z1; ++z) {
+            for (uint32_t y = y0; y < y1; ++y) {
+                const uint64_t row = static_cast<uint64_t>(z) * w.nxy + static_cast<uint64_t>(y) * w.dims[0];
+                if (w.palette_index) {
+                    for (uint32_t x = x0; x < x1; ++x)
+                        m = fmaxf(m, scale_table[w.palette_index[row + x]]);
+                } else {
+                    for (uint32_t x = x0; x < x1; ++x) {
+                        const Voxel v = w.voxels[row + x];
+                        m = fmaxf(m, v.measurement ? 1.0f : v.density * scale_table[v.material]);
+                    }
+                }
+            }
+        }
+        int lv = b.max_level;
+        if (m >= 1.0f) {
+            lv = 0;
+        } else if (m > 0.0f) {
+            lv = min(b.max_level, static_cast<int>(floorf(-static_cast<float>(b.levels_per_octave) * log2f(m))));
+            // the level's scale must not fall below the cell's maximum, whatever the rounding of log2f
+            while (lv > 0 && level_scale(lv, b.levels_per_octave) < m)
+                --lv;
+        }
+        level[c] = static_cast<uint8_t>(lv);
+        cells[c] = make_float2(1.0f, INFINITY); // the global majorant until a level does better
+        cost[c] = b.mu_ref;
+    }
+}
+
+// d[c] = 0 where a cell of the 27-neighbourhood lies above level lv, else infinity
+__global__ void majorant_dilate_kernel(MajorantBuild b, const uint8_t* __restrict__ level, int lv, float* __restrict__ d)
+{
+    const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
+    for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < ncell;
+         c += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        uint32_t cx, cy, cz;
+        cell_coords(c, b, cx, cy, cz);
+        bool above = false;
+        for (int dz = -1; dz <= 1 && !above; ++dz) {
+            const int z = static_cast<int>(cz) + dz;
+            if (z < 0 || z >= static_cast<int>(b.n[2]))
+                continue;
+            for (int dy = -1; dy <= 1 && !above; ++dy) {
+                const int y = static_cast<int>(cy) + dy;
+                if (y < 0 || y >= static_cast<int>(b.n[1]))
+                    continue;
+                const uint64_t row = (static_cast<uint64_t>(z) * b.n[1] + y) * b.n[0];
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int x = static_cast<int>(cx) + dx;
+                    if (x >= 0 && x < static_cast<int>(b.n[0]) && level[row + x] < lv) {
+                        above = true;
+                        break;
+                    }
+                }
+            }
+        }
+        d[c] = above ? 0.0f : INFINITY;
+    }
+}
+
+// One pass of the separable squared distance transform along AXIS:
+// out[c] = min over the line through c of in[t] + ((pos - t) * edge)^2, scanned
+// outward from pos until the distance alone exceeds the best value.  The last
+// pass (CHOOSE) turns the squared distance into R and keeps the better of the
+// cell's current choice and level lv.
+template <int AXIS, bool CHOOSE>
+__global__ void majorant_axis_kernel(MajorantBuild b, const float* __restrict__ in, float* __restrict__ out, int lv,
+    float2* __restrict__ cells, float* __restrict__ cost)
+{
+    const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
+    const int n = static_cast<int>(b.n[AXIS]);
+    const uint64_t stride = AXIS == 0 ? 1 : (AXIS == 1 ? b.n[0] : static_cast<uint64_t>(b.n[0]) * b.n[1]);
+    const float e = b.edge[AXIS];
+    for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < ncell;
+         c += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        uint32_t coord[3];
+        cell_coords(c, b, coord[0], coord[1], coord[2]);
+        const int pos = static_cast<int>(coord[AXIS]);
+        const uint64_t base = c - static_cast<uint64_t>(pos) * stride;
+        float best = in[c];
+        for (int k = 1; k < n; ++k) {
+            const float dk = static_cast<float>(k) * e;
+            const float d2 = dk * dk;
+            if (d2 >= best)
+                break;
+            const bool lo = pos - k >= 0, hi = pos + k < n;
+            if (!lo && !hi)
+                break;
+            if (lo)
+                best = fminf(best, in[base + static_cast<uint64_t>(pos - k) * stride] + d2);
+            if (hi)
+                best = fminf(best, in[base + static_cast<uint64_t>(pos + k) * stride] + d2);
+        }
+        if constexpr (!CHOOSE) {
+            out[c] = best;
+        } else {
+            if (best <= 0.0f)
+                continue; // the cell itself lies in the dilated set
+            // a small margin keeps rounding of the photon's position on the safe side
+            const float R = fmaf(sqrtf(best), 0.999f, -1.0e-3f);
+            if (!(R > 0.0f))
+                continue;
+            const float s = level_scale(lv, b.levels_per_octave);
+            const float mu = b.mu_ref * s;
+            const float c_new = mu / (1.0f - expf(-mu * R)); // R infinite: mu
+            if (c_new < cost[c]) {
+                cost[c] = c_new;
+                cells[c] = make_float2(1.0f / s, R);
+            }
+        }
+    }
+}
+
+int grid_for(uint64_t n)
+{
+    const uint64_t blocks = (n + 255) / 256;
+    return static_cast<int>(blocks < 4096 ? (blocks > 0 ? blocks : 1) : 4096);
+}
+
+} // namespace
+
+cudaError_t launch_majorant_levels(const WorldParams& w, const MajorantScales& scales, const MajorantBuild& b,
+    uint8_t* level, float2* cells, float* cost, cudaStream_t stream)
+{
+    const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
+    majorant_level_kernel<<<grid_for(ncell), 256, 0, stream>>>(w, scales, b, level, cells, cost);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_majorant_level_pass(const MajorantBuild& b, const uint8_t* level, int lv, float* d0, float* d1,
+    float2* cells, float* cost, cudaStream_t stream)
+{
+    const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
+    const int g = grid_for(ncell);
+    majorant_dilate_kernel<<<g, 256, 0, stream>>>(b, level, lv, d0);
+    majorant_axis_kernel<0, false><<<g, 256, 0, stream>>>(b, d0, d1, lv, cells, cost);
+    majorant_axis_kernel<1, false><<<g, 256, 0, stream>>>(b, d1, d0, lv, cells, cost);
+    majorant_axis_kernel<2, true><<<g, 256, 0, stream>>>(b, d0, nullptr, lv, cells, cost);
+    return cudaGetLastError();
+}
+
+} // namespace dxmc_gb300::dev

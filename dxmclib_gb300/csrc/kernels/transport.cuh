@@ -32,6 +32,21 @@ struct WorldParams {
     uint64_t n_voxels;
 };
 
+// Local majorants for Woodcock tracking: the voxel grid is cut into cells of
+// 2^shift voxels per axis, and cell c holds (1 / s, R): every voxel within the
+// distance R (mm) of any point of the cell attenuates less than s times the
+// global majorant at every energy.  A flight drawn with the majorant s * M(E)
+// stops after R without a collision test and is drawn again from there (the
+// exponential distribution has no memory), so the tracking stays exact while
+// it takes far fewer steps through air, lung and soft tissue.  cells == nullptr
+// selects the global majorant of the reference (s = 1, R infinite).
+struct MajorantGrid {
+    const float2* cells;
+    uint32_t nx, nxy;    // cells along x, cells per z slab
+    int shift[3];        // log2 of the cell size in voxels
+    int pad;
+};
+
 struct SourceParams {
     const DevExposure* exposures;
     const uint64_t* history_offsets; // n_exposures + 1 prefix sums
@@ -91,6 +106,7 @@ struct TransportParams {
     int interact_threshold; // run the interaction passes once at least this many lanes wait (1..32)
     int woodcock_burst;     // Woodcock steps a lane may take per loop iteration (1..64)
     int pad_params;
+    MajorantGrid majorant;
 };
 
 // Work item of the batched kernel: histories [first, first + count) of job `job`.
@@ -139,6 +155,27 @@ cudaError_t launch_postprocess_f32(const float* tally, const WorldParams& w, uin
 // (origin mm, direction, energy keV); out[i] = sum of mu * density * length (cm).
 cudaError_t launch_radiological_path(const WorldParams& w, const float* lut, LutMeta meta, const float* rays, uint64_t n,
     double* out, cudaStream_t stream);
+// Local-majorant grid construction (majorant_kernels.cu).  MajorantScales holds
+// the scale of each palette entry (compact layout) or the ratio r_m of each
+// material (8-byte layout: scale = density * r_m, 1 for measurement voxels).
+struct MajorantBuild {
+    uint32_t n[3];       // cells per axis
+    int shift[3];
+    float edge[3];       // cell size (mm)
+    float mu_ref;        // global majorant (1/mm) at the reference energy of the cost model
+    int levels_per_octave;
+    int max_level;
+};
+struct MajorantScales {
+    float v[PALETTE_MAX];
+};
+cudaError_t launch_majorant_levels(const WorldParams& w, const MajorantScales& scales, const MajorantBuild& b,
+    uint8_t* level, float2* cells, float* cost, cudaStream_t stream);
+// Adds the candidate majorant level lv: cells whose 27-neighbourhood holds no
+// cell above the level get (level scale, distance to the nearest such cell) if
+// that lowers the expected number of steps per mm.  d0 and d1 are scratch grids.
+cudaError_t launch_majorant_level_pass(const MajorantBuild& b, const uint8_t* level, int lv, float* d0, float* d1,
+    float2* cells, float* cost, cudaStream_t stream);
 cudaError_t launch_max_density(const Voxel* voxels, uint64_t n, unsigned int* out_bits, int n_materials, cudaStream_t stream);
 cudaError_t launch_probe_lut(const float* lut, LutMeta meta, int material, const double* energies, int n, double* out_att, double* out_maxinv, cudaStream_t stream);
 cudaError_t launch_probe_interactions(const float* lut, LutMeta meta, int material, int model, int kind, float energy,

@@ -480,6 +480,7 @@ namespace {
         uint64_t vidx;
         float forced_wc; // weight correction waiting for a forced-voxel interaction pass
         bool armed;      // energy x weight is below the Russian-roulette threshold
+        float cinv, cR;  // local majorant: 1 / scale and the flight length it holds for (MajorantGrid)
         uint32_t steps, deposits, overflows, histories;
 
         __device__ void reset_counters() { steps = deposits = overflows = histories = 0; }
@@ -491,12 +492,31 @@ namespace {
             cached_mat = -1;
             hist_steps = 0;
             forced_wc = 0.0f;
+            cinv = 1.0f; // the first flight from the grid boundary uses the global majorant
+            cR = INFINITY;
             arm();
         }
         // energy and weight change only at interactions and roulette: the roulette
         // test of a virtual step reads this flag
         __device__ void arm() { armed = ph.energy * ph.weight < ROULETTE_THRESHOLD; }
     };
+
+    // Local majorant of the cell a photon starts in (it enters the grid on its
+    // boundary, so the coordinates are clamped onto the grid).
+    __device__ __forceinline__ void enter_cell(Lane& s, const TransportParams& p)
+    {
+        const MajorantGrid& g = p.majorant;
+        if (!g.cells || !s.alive)
+            return;
+        const WorldParams& w = p.world;
+        const float fx = fminf(fmaxf(fmaf(s.ph.px, w.inv_spacing[0], -w.lo_inv[0]), 0.0f), w.dims_f[0] - 1.0f);
+        const float fy = fminf(fmaxf(fmaf(s.ph.py, w.inv_spacing[1], -w.lo_inv[1]), 0.0f), w.dims_f[1] - 1.0f);
+        const float fz = fminf(fmaxf(fmaf(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2]), 0.0f), w.dims_f[2] - 1.0f);
+        const uint32_t ix = static_cast<uint32_t>(fx), iy = static_cast<uint32_t>(fy), iz = static_cast<uint32_t>(fz);
+        const float2 cell = __ldg(g.cells + ((iz >> g.shift[2]) * g.nxy + (iy >> g.shift[1]) * g.nx + (ix >> g.shift[0])));
+        s.cinv = cell.x;
+        s.cR = cell.y;
+    }
 
     // Loads photon + stream state from the pre-generated queue.
     __device__ __forceinline__ void take_queued(Lane& s, const PhotonQueue& q, uint64_t i)
@@ -528,6 +548,7 @@ namespace {
         ++s.histories;
         s.alive = transport_to_world(p.world, s.ph);
         s.start_photon();
+        enter_cell(s, p);
     }
 
     // One iteration of the warp-synchronous loop for every lane of the warp: a
@@ -563,7 +584,11 @@ namespace {
                 s.alive = false;
             }
             for (int k = 0; k < burst && s.alive; ++k) {
-                const float step = -__log2f(s.rng.uniform_open()) * s.stepK;
+                // a flight drawn with the local majorant ends without a collision test
+                // where that majorant stops holding (truncated: drawn again from there)
+                const float flight = -__log2f(s.rng.uniform_open()) * (s.stepK * s.cinv);
+                const bool truncated = flight > s.cR;
+                const float step = fminf(flight, s.cR);
                 s.ph.px = fmaf(s.ph.dx, step, s.ph.px);
                 s.ph.py = fmaf(s.ph.dy, step, s.ph.py);
                 s.ph.pz = fmaf(s.ph.dz, step, s.ph.pz);
@@ -580,6 +605,15 @@ namespace {
                 const uint32_t ix = static_cast<uint32_t>(fx);
                 const uint32_t iy = static_cast<uint32_t>(fy);
                 const uint32_t iz = static_cast<uint32_t>(fz);
+                const float cinv = s.cinv; // the majorant this flight was drawn with
+                if (p.majorant.cells) {
+                    const MajorantGrid& g = p.majorant;
+                    const float2 cell = __ldg(g.cells + ((iz >> g.shift[2]) * g.nxy + (iy >> g.shift[1]) * g.nx + (ix >> g.shift[0])));
+                    s.cinv = cell.x;
+                    s.cR = cell.y;
+                }
+                if (truncated)
+                    continue;
                 if constexpr (PALETTE) // compact worlds have fewer than 2^32 voxels (world upload)
                     s.vidx = iz * static_cast<uint32_t>(w.nxy) + (iy * w.dims[0] + ix);
                 else
@@ -598,7 +632,7 @@ namespace {
                     s.p01 = (a0 + a1) * inv;
                     s.cached_mat = mat;
                 }
-                const float eventProb = s.probInv * density;
+                const float eventProb = s.probInv * density * cinv;
                 if (!measured) {
                     // naive sampling (computeInteractions): decide the event type now,
                     // run it in the interaction pass
@@ -834,9 +868,10 @@ namespace {
                     const bool mine = ((need >> lane) & 1u) && rank < avail;
                     const unsigned taken = __ballot_sync(FULL_MASK, mine);
                     if (mine) {
-                        if (use_queue)
+                        if (use_queue) {
                             take_queued(s, p.queue, pool_next + rank);
-                        else
+                            enter_cell(s, p);
+                        } else
                             take_history(s, p, pool_next + rank);
                     }
                     pool_next += __popc(taken);

@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define DXMC_GPU_ABI_VERSION 1
+#define DXMC_GPU_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------- */
 enum {
@@ -54,6 +54,18 @@ enum {
     DXMC_TALLY_F64 = 0,         /* FP64 atomics for every deposit (reference semantics) */
     DXMC_TALLY_F32 = 1,         /* FP32 atomics only (precision study) */
     DXMC_TALLY_WARP_F64 = 2     /* FP32 warp-aggregated partials flushed to FP64 */
+};
+
+/* Woodcock tracking majorant.  GLOBAL is the reference's delta tracking
+ * (woodcockParticleTracking, transport.hpp:640-700): every flight is drawn with
+ * the largest attenuation in the world.  LOCAL draws each flight with a bound of
+ * the photon's neighbourhood from a grid built per (world, LUT) pair, and ends a
+ * flight without a collision test where that bound stops holding; both sample
+ * the same transport process, LOCAL with fewer virtual collisions. */
+enum {
+    DXMC_TRACKING_DEFAULT = 0,  /* the context's choice (LOCAL unless set) */
+    DXMC_TRACKING_GLOBAL = 1,
+    DXMC_TRACKING_LOCAL = 2
 };
 
 /* ---- physics data for the host LUT build -------------------------------- */
@@ -192,7 +204,7 @@ typedef struct dxmc_gpu_options {
     int32_t interact_threshold; /* run the per-type interaction passes once this many lanes wait; 0 = default */
     int32_t queue_log2_chunk;   /* n > 0: photons are pre-generated in chunks of 2^n histories (48 B per
                                    photon); 0 = default (generated inside the transport kernel); -1 = inside */
-    int32_t pad;
+    int32_t tracking;           /* DXMC_TRACKING_* of jobs that leave theirs at DEFAULT */
 } dxmc_gpu_options;
 
 int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out);
@@ -228,6 +240,15 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* desc, dxmc_w
 /* Per-material maximum density of a resident world, computed on the device. */
 int dxmc_gpu_world_max_density(dxmc_world* world, double* out, int n_materials);
 void dxmc_gpu_world_free(dxmc_world* world);
+/* Builds the local-majorant grid of a (world, LUT) pair ahead of its first job
+ * (jobs with LOCAL tracking build it on first use; dxmc_gpu_transport_noalloc
+ * uses it only if it exists).  The world keeps the grid until it is freed. */
+int dxmc_gpu_world_prepare(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut);
+/* Reads back a built local-majorant grid: cells per axis, log2 of the cell size
+ * in voxels per axis and, if cells is not NULL, (1 / scale, R mm) per cell, x
+ * fastest.  DXMC_ERR_STATE if the pair has no grid. */
+int dxmc_gpu_world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut, uint32_t* cells_per_axis,
+    int32_t* shift, float* cells);
 
 /* ---- LUT on the device --------------------------------------------------- */
 int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* blob, dxmc_lut** out);
@@ -250,6 +271,8 @@ typedef struct dxmc_job_desc {
     int32_t queue_log2_chunk;           /* photon queue chunk 2^n; -1 = photons generated in the kernel */
     int32_t woodcock_burst;             /* Woodcock steps a lane may take per loop iteration (1..64) */
     int32_t block_size;                 /* threads per block of the transport kernel: 128 or 256 */
+    int32_t tracking;                   /* DXMC_TRACKING_*; 0 = the context's */
+    int32_t pad;
 } dxmc_job_desc;
 
 typedef struct dxmc_job_stats {

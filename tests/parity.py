@@ -53,12 +53,13 @@ def compare_sparse(ref: dict, dose: np.ndarray, var: np.ndarray, min_frac: float
     )
 
 
-def assert_parity(stats: dict, label: str = "", correlated: bool = False) -> None:
+def assert_parity(stats: dict, label: str = "", correlated: bool = False, max_chi2: float = MAX_CHI2) -> None:
     """correlated=True for forced-interaction scoring, where every Woodcock step in a
     measured voxel scores a deposit: the per-event variance field is then far from
     Gaussian voxel to voxel (the reference restated on the CPU exceeds the plain
     Gaussian count against the reference itself), so twice the Gaussian rate of
-    3-sigma exceedances is allowed."""
+    3-sigma exceedances is allowed.  max_chi2 replaces the chi2/dof bound where a
+    same-method comparison measured the overdispersion of the pair."""
     msg = f"{label}: {stats}"
     assert stats["n_voxels"] > 10, msg
     n = stats["n_voxels"]
@@ -67,6 +68,6 @@ def assert_parity(stats: dict, label: str = "", correlated: bool = False) -> Non
     assert stats["beyond_3sigma"] <= allowed, msg + f" (allowed {allowed} beyond 3 sigma)"
     assert stats["max_abs_z"] <= MAX_ABS_Z, msg
     # chi2/dof of n standard normals has standard deviation sqrt(2 / n)
-    assert stats["chi2"] <= MAX_CHI2 + 4.0 * np.sqrt(2.0 / n), msg
+    assert stats["chi2"] <= max_chi2 + 4.0 * np.sqrt(2.0 / n), msg
     assert abs(stats["total_ratio"] - 1.0) <= TOTAL_ENERGY_RTOL, msg
     assert abs(stats["mean_bias"]) <= MEAN_BIAS_RTOL, msg

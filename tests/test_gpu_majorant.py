@@ -1,0 +1,155 @@
+"""GPU tests of local-majorant Woodcock tracking.
+
+The grid of a (world, LUT) pair must bound the attenuation: for every cell
+holding (1 / s, R), each voxel within the distance R of the cell attenuates less
+than s times the global majorant at every energy of the LUT.  The check below
+recomputes that from the host LUT (double precision) with an exact distance
+transform at voxel resolution.  Tracking with the grid must then sample the
+same process as the reference's global majorant: dose, variance and totals of
+both modes agree within the statistical criteria of tests/parity.py, with far
+fewer Woodcock steps per history.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from parity import assert_parity, compare_sparse
+
+pytestmark = pytest.mark.gpu
+
+
+def _phantom():
+    from dxmclib_gb300.workloads import ct_world
+    # the CT body phantom at 4 x 4 x 5 mm voxels (air, soft tissue, lung, bone)
+    return ct_world(nz=24, nx=104, ny=104, spacing=(4.0, 4.0, 5.0), seed=7)
+
+
+def _voxel_scales(world, blob):
+    """Per voxel, the largest ratio of its attenuation to the global majorant over
+    the LUT's energies (measurement voxels count as 1)."""
+    info = blob.info()
+    energies = np.exp(np.linspace(np.log(info["min_energy"] * 1.0001), np.log(info["max_energy"] * 0.9999), 600))
+    inv = np.array([blob.max_attenuation_inverse(e) for e in energies])
+    r = np.array([max(blob.attenuation(m, e).sum() * i for e, i in zip(energies, inv))
+                  for m in range(len(world.materialMap()))])
+    s = world.densityArray().astype(np.float64) * r[world.materialIndexArray()]
+    if world.measurementMapArray() is not None:
+        s[world.measurementMapArray() != 0] = 1.0
+    d = world.dimensions()
+    return s.reshape(d[2], d[1], d[0])
+
+
+def test_majorant_grid_bounds_attenuation(gpu_ctx):
+    from scipy import ndimage
+    import dxmclib_gb300 as dx
+    world = _phantom()
+    dworld = dx.DeviceWorld(gpu_ctx, world)
+    dlut = dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, 120.0))
+    dworld.prepare(dlut)
+    shift, cells = dworld.majorant(dlut)
+    blob = dx.LutBlob.from_world(world, 120.0)
+    scale = _voxel_scales(world, blob)
+    sp = np.array(world.spacing())[::-1]  # (z, y, x) mm
+    b = [1 << int(shift[2]), 1 << int(shift[1]), 1 << int(shift[0])]
+    s_cell = 1.0 / cells[..., 0].astype(np.float64)
+    R_cell = cells[..., 1].astype(np.float64)
+    assert np.all(s_cell <= 1.0 + 1e-6)
+    # the grid is worth having: air cells far from the body get small scales and long flights
+    assert (s_cell < 0.01).mean() > 0.05, np.unique(s_cell)
+    assert np.nanmax(np.where(s_cell < 0.01, R_cell, np.nan)) > 30.0
+    checked = 0
+    for s in np.unique(s_cell[np.isfinite(R_cell)]):
+        hot = scale > s * (1.0 + 1e-4)
+        if not hot.any():
+            continue
+        # exact gap between voxel boxes: distance transform to the hot set dilated by one voxel
+        near = ndimage.binary_dilation(hot, structure=np.ones((3, 3, 3), bool))
+        gap = np.where(near, 0.0, ndimage.distance_transform_edt(~near, sampling=sp))
+        pad = [(0, (-gap.shape[i]) % b[i]) for i in range(3)]
+        g = np.pad(gap, pad, constant_values=np.inf)
+        cell_gap = g.reshape(g.shape[0] // b[0], b[0], g.shape[1] // b[1], b[1], g.shape[2] // b[2], b[2]).min(axis=(1, 3, 5))
+        sel = (s_cell == s) & np.isfinite(R_cell)
+        bad = sel & (R_cell > cell_gap + 1e-3)
+        assert not bad.any(), (s, int(bad.sum()), R_cell[bad][:5], cell_gap[bad][:5])
+        checked += int(sel.sum())
+    assert checked > 0
+    dlut.close()
+    dworld.close()
+
+
+@pytest.mark.parametrize("model", [1, 2])
+def test_local_tracking_matches_global(gpu_ctx, model):
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    from dxmclib_gb300.workloads import ct_source
+    world = _phantom()
+    src = ct_source(world, 4_000_000)
+    dworld = dx.DeviceWorld(gpu_ctx, world)
+    dlut = dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, src.maxPhotonEnergyProduced()))
+    ex = src.exposures(world.directionCosines())
+    out = {}
+    for mode in (A.TRACKING_GLOBAL, A.TRACKING_LOCAL):
+        job = dx.Job(gpu_ctx, dworld, dlut, ex, src.spectrum(), src.heel(), None, seed=11 + mode, model=model,
+                     tracking=mode)
+        out[mode] = job.result(A.OUTPUT_EV_PER_HISTORY)
+        job.close()
+    dg, vg, _, sg = out[A.TRACKING_GLOBAL]
+    dl, vl, _, sl = out[A.TRACKING_LOCAL]
+    assert sg["histories"] == sl["histories"]
+    ref = dict(idx=np.arange(dg.size), dose=dg, var=vg, total=np.array([dg.sum()]))
+    assert_parity(compare_sparse(ref, dl, vl), f"local vs global tracking, model {model}")
+    # the same process with fewer steps
+    assert sl["steps"] < 0.75 * sg["steps"], (sl["steps"], sg["steps"])
+    dlut.close()
+    dworld.close()
+
+
+def test_forced_scoring_keeps_global_majorant(gpu_ctx):
+    """Measurement voxels (forced photoelectric scoring) count as scale 1, so the
+    cells around them keep the global majorant and the forced estimator sees the
+    reference's step density: both tracking modes give the same scored dose."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    from dxmclib_gb300.workloads import ct_source
+    world = _phantom()
+    d = world.dimensions()
+    meas = np.zeros((d[2], d[1], d[0]), np.uint8)
+    meas[8:16, 40:64, 40:64] = 1
+    world.setMeasurementMapArray(meas.ravel())
+    assert world.isValid()
+    # the measured region's total must agree within 0.5 %: 2e7 histories put its
+    # standard error near 0.15 %
+    src = ct_source(world, 20_000_000)
+    dworld = dx.DeviceWorld(gpu_ctx, world)
+    dlut = dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, src.maxPhotonEnergyProduced()))
+    dworld.prepare(dlut)
+    shift, cells = dworld.majorant(dlut)
+    b = [1 << int(shift[2]), 1 << int(shift[1]), 1 << int(shift[0])]
+    # cells holding a measurement voxel track with the global majorant
+    m = np.pad(meas, [(0, (-meas.shape[i]) % b[i]) for i in range(3)])
+    mc = m.reshape(m.shape[0] // b[0], b[0], m.shape[1] // b[1], b[1], m.shape[2] // b[2], b[2]).max(axis=(1, 3, 5))
+    assert np.all(cells[..., 0][mc > 0] == 1.0) and np.all(np.isinf(cells[..., 1][mc > 0]))
+    ex = src.exposures(world.directionCosines())
+    runs = []
+    for seed, mode in ((21, A.TRACKING_GLOBAL), (22, A.TRACKING_GLOBAL), (23, A.TRACKING_LOCAL)):
+        job = dx.Job(gpu_ctx, dworld, dlut, ex, src.spectrum(), src.heel(), None, seed=seed, model=1, tracking=mode)
+        runs.append(job.result(A.OUTPUT_EV_PER_HISTORY)[:2])
+        job.close()
+    sel = meas.ravel() > 0
+    ref = dict(idx=np.flatnonzero(sel), dose=runs[0][0][sel], var=runs[0][1][sel], total=np.array([runs[0][0][sel].sum()]))
+
+    def against_ref(d, v):
+        d_in = np.zeros_like(d)
+        d_in[sel] = d[sel]
+        return compare_sparse(ref, d_in, v)
+
+    # forced scoring deposits at every step in a measured voxel, so the per-event
+    # variance field under-states the spread even between two global runs: that
+    # pair's chi2/dof sets the bound for the local run
+    same = against_ref(*runs[1])
+    assert_parity(same, "forced scoring, global vs global", correlated=True, max_chi2=1.6)
+    assert_parity(against_ref(*runs[2]), "forced scoring, local vs global", correlated=True,
+                  max_chi2=max(1.2, same["chi2"]) * 1.1)
+    dlut.close()
+    dworld.close()
