@@ -898,17 +898,20 @@ class DeviceWorld:
                 "dxmc_gpu_world_prepare")
 
     def majorant(self, dlut: "DeviceLut"):
-        """The local-majorant grid built for ``dlut``: (shift (3,), cells (nz, ny, nx, 2)
-        holding 1 / scale and R in mm)."""
+        """The local-majorant grid built for ``dlut``: (shift (3,), band edges in keV
+        (bands - 1,), cells (nz, ny, nx, bands, 2) holding 1 / scale and R in mm)."""
         n = (C.c_uint32 * 3)()
         sh = (C.c_int32 * 3)()
-        A.check(self.ctx.lib.dxmc_gpu_world_majorant(self.ctx.handle, self.handle, dlut.handle, n, sh, None),
+        nb = C.c_int32()
+        edges = np.zeros(8, np.float32)
+        A.check(self.ctx.lib.dxmc_gpu_world_majorant(self.ctx.handle, self.handle, dlut.handle, n, sh, C.byref(nb),
+                                                     edges.ctypes.data_as(A.FP), None),
                 self.ctx.handle, "dxmc_gpu_world_majorant")
-        cells = np.zeros((n[2], n[1], n[0], 2), np.float32)
-        A.check(self.ctx.lib.dxmc_gpu_world_majorant(self.ctx.handle, self.handle, dlut.handle, n, sh,
-                                                     cells.ctypes.data_as(A.FP)), self.ctx.handle,
+        cells = np.zeros((n[2], n[1], n[0], nb.value, 2), np.float32)
+        A.check(self.ctx.lib.dxmc_gpu_world_majorant(self.ctx.handle, self.handle, dlut.handle, n, sh, C.byref(nb),
+                                                     None, cells.ctypes.data_as(A.FP)), self.ctx.handle,
                 "dxmc_gpu_world_majorant")
-        return np.array(sh[:], np.int64), cells
+        return np.array(sh[:], np.int64), edges[:nb.value - 1].astype(np.float64), cells
 
     def max_density(self) -> np.ndarray:
         n = len(self.world.materialMap())

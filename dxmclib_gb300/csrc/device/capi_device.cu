@@ -30,6 +30,10 @@ constexpr int DEFAULT_QUEUE_INTERACT_THRESHOLD = 8;
 #define DXMC_DEFAULT_WOODCOCK_BURST 8
 #endif
 constexpr int DEFAULT_WOODCOCK_BURST = DXMC_DEFAULT_WOODCOCK_BURST; // Woodcock steps per loop iteration
+// With local majorants a history takes fewer, more varied steps: shorter bursts
+// and a later refill keep more lanes of a warp stepping together.
+constexpr int DEFAULT_LOCAL_REGEN_THRESHOLD = 10;
+constexpr int DEFAULT_LOCAL_WOODCOCK_BURST = 5;
 // Photons are generated inside the transport kernel unless a job or the context
 // asks for a pre-generated queue (2^n photons per generation pass): with the
 // Woodcock burst the in-kernel generation is as fast and needs no queue memory.
@@ -88,8 +92,13 @@ struct dxmc_lut {
     dev::LutMeta meta {};
     uint64_t bytes = 0;
     uint64_t serial = 0;              // unique per upload: key of the worlds' majorant grids
-    std::vector<float> majorant_ratio; // r_m: max over energies of mu_m(E) / global majorant (per g/cm3)
-    float mu_ref = 0.0f;              // global majorant (1/mm) at half the LUT's maximum energy
+    // local-majorant energy bands: r_m of each band (max over the band's energies of
+    // mu_m(E) / global majorant, per g/cm3; bands x n_materials), the band edges
+    // (keV) and the global majorant (1/mm) at each band's reference energy
+    int majorant_bands = 1;
+    float band_edge[dev::MAJORANT_MAX_BANDS - 1] {};
+    std::vector<float> majorant_ratio;
+    float mu_ref[dev::MAJORANT_MAX_BANDS] {};
 };
 
 struct dxmc_job {
@@ -134,41 +143,81 @@ int cuda_fail(dxmc_gpu_ctx* ctx, cudaError_t e, const char* what)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-// Per material m, the largest ratio of its attenuation (per g/cm3) to the global
-// majorant over the LUT's energies, from the float image the kernels read: in
-// each log-log segment both are exponentials of log E, so the ratio of their sum
-// to the majorant is convex in log E and peaks at a segment end.  Each segment is
-// evaluated at its own nodes and both neighbours', which covers either convention
-// of which node interval a segment index serves.  A 0.2 % margin covers the
-// device's exponential and the rounding of the level arithmetic.  mu_ref: the
-// global majorant (1/mm) at half the maximum energy, the reference point of the
-// grid's cost model.
-void majorant_ratios(const std::vector<float>& img, const dev::LutMeta& m, std::vector<float>& ratio, float& mu_ref)
+// Per energy band and material m, the largest ratio of m's attenuation (per
+// g/cm3) to the global majorant over the band's energies, from the float image
+// the kernels read.  Photons are tracked from 1 keV (the transport cutoff) to
+// the LUT's maximum energy; above 15 keV that range is cut into four bands with
+// edges log-spaced from 10 keV, since soft tissue's share of a bone-set
+// majorant varies five-fold over a diagnostic spectrum.  In each log-log
+// segment both attenuations are exponentials of log E, so the ratio of their
+// sum to the majorant is convex in log E and peaks at an end of the interval of
+// log E that the kernels' segment lookup (lut_segment) maps to that segment.
+// Those ends are nodes of the table, steps of its linear part, band edges or
+// the range limits: every segment is evaluated at each such point where the
+// lookup selects it on either side.  A band's interval is widened by 0.1 % so
+// that rounding of the band choice stays covered, and a 0.2 % margin covers the
+// device's exponential and the level arithmetic.  mu_ref: the global majorant
+// (1/mm) at each band's geometric mid-energy, the cost model's reference.
+void majorant_ratios(const std::vector<float>& img, const dev::LutMeta& m, dxmc_lut& lut)
 {
     const int R = m.R;
     const float* x = img.data() + m.off_x;
     const float* maxc = img.data() + m.off_maxcoef;
-    ratio.assign(m.n_materials, 0.0f);
-    for (int mat = 0; mat < m.n_materials; ++mat) {
-        double r = 0.0;
-        for (int seg = 0; seg < R; ++seg) {
-            const float* c = img.data() + m.off_coef + (static_cast<size_t>(mat) * R + seg) * 6;
-            for (int k = std::max(seg - 1, 0); k <= std::min(seg + 1, R - 1); ++k) {
-                const double lx = x[k];
-                double tot = 0.0;
-                for (int t = 0; t < 3; ++t)
-                    tot += std::pow(10.0, c[2 * t] + c[2 * t + 1] * lx);
-                const double inv = std::pow(10.0, maxc[2 * seg] + maxc[2 * seg + 1] * lx);
-                r = std::max(r, tot * inv);
-            }
+    // the kernels' segment lookup, in the same float arithmetic
+    auto segment = [&](float le) {
+        if (le > m.linear_energy) {
+            const int idx = static_cast<int>((le - m.linear_energy) * m.inv_linear_step) + m.linear_index;
+            return std::min(idx, R - 1);
         }
-        ratio[mat] = static_cast<float>(r * 1.002);
+        const int pos = static_cast<int>(std::upper_bound(x, x + R, le) - x);
+        return pos < R ? pos : R - 1;
+    };
+    auto max_inverse = [&](float le) {
+        const int seg = segment(le);
+        return std::pow(10.0, static_cast<double>(maxc[2 * seg]) + maxc[2 * seg + 1] * static_cast<double>(le));
+    };
+    const double e_max = std::max(static_cast<double>(m.max_energy), 1.0);
+    lut.majorant_bands = e_max > 15.0 ? dev::MAJORANT_MAX_BANDS : 1;
+    const int nb = lut.majorant_bands;
+    std::vector<double> edges { 1.0 };
+    for (int k = 1; k < nb; ++k)
+        edges.push_back(10.0 * std::pow(e_max / 10.0, static_cast<double>(k) / nb));
+    edges.push_back(e_max);
+    for (int k = 0; k < dev::MAJORANT_MAX_BANDS - 1; ++k)
+        lut.band_edge[k] = k + 1 < nb ? static_cast<float>(edges[k + 1]) : INFINITY;
+    std::vector<float> points;
+    for (int k = 0; k < R; ++k)
+        points.push_back(x[k]);
+    for (int k = 0; k <= R; ++k)
+        points.push_back(m.linear_energy + static_cast<float>(k) / m.inv_linear_step);
+    lut.majorant_ratio.assign(static_cast<size_t>(nb) * m.n_materials, 0.0f);
+    for (int b = 0; b < nb; ++b) {
+        const float le_lo = static_cast<float>(std::log10(edges[b]) - (b > 0 ? 4.34e-4 : 0.0));
+        const float le_hi = static_cast<float>(std::log10(edges[b + 1]) + (b + 1 < nb ? 4.34e-4 : 0.0));
+        std::vector<float> pts { le_lo, le_hi };
+        for (const float t : points)
+            if (t > le_lo && t < le_hi)
+                pts.push_back(t);
+        for (int mat = 0; mat < m.n_materials; ++mat) {
+            double r = 0.0;
+            for (const float t : pts) {
+                for (const float le : { std::nextafter(t, -1e30f), t, std::nextafter(t, 1e30f) }) {
+                    if (!(le >= le_lo && le <= le_hi))
+                        continue;
+                    const int seg = segment(le);
+                    const float* c = img.data() + m.off_coef + (static_cast<size_t>(mat) * R + seg) * 6;
+                    double tot = 0.0;
+                    for (int k = 0; k < 3; ++k)
+                        tot += std::pow(10.0, static_cast<double>(c[2 * k]) + c[2 * k + 1] * static_cast<double>(t));
+                    const double inv = std::pow(10.0, static_cast<double>(maxc[2 * seg]) + maxc[2 * seg + 1] * static_cast<double>(t));
+                    r = std::max(r, tot * inv);
+                }
+            }
+            lut.majorant_ratio[static_cast<size_t>(b) * m.n_materials + mat] = static_cast<float>(r * 1.002);
+        }
+        const double inv_cm = max_inverse(static_cast<float>(0.5 * (std::log10(edges[b]) + std::log10(edges[b + 1]))));
+        lut.mu_ref[b] = static_cast<float>(inv_cm > 0 ? 0.1 / inv_cm : 0.01);
     }
-    const double le = std::log10(std::max(static_cast<double>(m.max_energy) * 0.5, 1.0));
-    int seg = static_cast<int>(std::upper_bound(x, x + R, static_cast<float>(le)) - x);
-    seg = std::min(std::max(seg, 0), R - 1);
-    const double inv_cm = std::pow(10.0, maxc[2 * seg] + maxc[2 * seg + 1] * le);
-    mu_ref = static_cast<float>(inv_cm > 0 ? 0.1 / inv_cm : 0.01);
 }
 
 size_t dev_palette_table_bytes();
@@ -647,9 +696,9 @@ int dxmc_gpu_world_prepare(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut*
 }
 
 int dxmc_gpu_world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut, uint32_t* cells_per_axis,
-    int32_t* shift, float* cells)
+    int32_t* shift, int32_t* bands, float* band_edges, float* cells)
 {
-    if (!ctx || !world || !lut || !cells_per_axis || !shift)
+    if (!ctx || !world || !lut || !cells_per_axis || !shift || !bands)
         return DXMC_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mutex);
     const dev::MajorantGrid* g = nullptr;
@@ -660,9 +709,12 @@ int dxmc_gpu_world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut
         shift[a] = g->shift[a];
         cells_per_axis[a] = static_cast<uint32_t>((world->dims[a] + (1ull << g->shift[a]) - 1) >> g->shift[a]);
     }
+    *bands = g->bands;
+    for (int k = 0; band_edges && k + 1 < g->bands; ++k)
+        band_edges[k] = g->band_edge[k];
     if (cells) {
         cudaSetDevice(ctx->device);
-        const uint64_t n = static_cast<uint64_t>(cells_per_axis[0]) * cells_per_axis[1] * cells_per_axis[2];
+        const uint64_t n = static_cast<uint64_t>(cells_per_axis[0]) * cells_per_axis[1] * cells_per_axis[2] * g->bands;
         cudaError_t e = cudaMemcpyAsync(cells, g->cells, n * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess)
             e = cudaStreamSynchronize(ctx->stream);
@@ -757,7 +809,7 @@ int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* b, dxmc_lut** ou
     lut->meta = m;
     static std::atomic<uint64_t> lut_serials { 0 };
     lut->serial = ++lut_serials;
-    majorant_ratios(img, m, lut->majorant_ratio, lut->mu_ref);
+    majorant_ratios(img, m, *lut);
     lut->bytes = img.size() * sizeof(float);
     cudaError_t e = cudaMallocAsync(&lut->image, lut->bytes, ctx->stream);
     if (e == cudaSuccess)
@@ -873,29 +925,33 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
         b.edge[a] = static_cast<float>(w->spacing[a] * static_cast<double>(1ull << sh));
         ncell *= b.n[a];
     }
-    b.mu_ref = lut->mu_ref;
     b.levels_per_octave = MAJORANT_LEVELS_PER_OCTAVE;
     b.max_level = MAJORANT_MAX_LEVEL;
-    // voxel scales and the levels worth trying: the palette's own levels, or every
-    // second level for the 8-byte layout
-    dev::MajorantScales scales {};
-    uint64_t levels = 0;
-    if (w->palette_index) {
-        for (size_t i = 0; i < w->host_palette.size() && i < static_cast<size_t>(dev::PALETTE_MAX); ++i) {
-            const auto& pe = w->host_palette[i];
-            const int mat = static_cast<int>(pe.code & 0xffu);
-            const bool meas = ((pe.code >> 8) & 0xffu) != 0;
-            const float sc = meas ? 1.0f : pe.density * lut->majorant_ratio[mat];
-            scales.v[i] = sc;
-            levels |= 1ull << majorant_level(sc);
+    b.bands = lut->majorant_bands;
+    // per band, the voxel scales and the levels worth trying: the palette's own
+    // levels, or every second level for the 8-byte layout
+    const int nm = lut->meta.n_materials;
+    std::vector<dev::MajorantScales> scales(b.bands);
+    std::vector<uint64_t> levels(b.bands, 0);
+    for (int band = 0; band < b.bands; ++band) {
+        const float* ratio = lut->majorant_ratio.data() + static_cast<size_t>(band) * nm;
+        if (w->palette_index) {
+            for (size_t i = 0; i < w->host_palette.size() && i < static_cast<size_t>(dev::PALETTE_MAX); ++i) {
+                const auto& pe = w->host_palette[i];
+                const int mat = static_cast<int>(pe.code & 0xffu);
+                const bool meas = ((pe.code >> 8) & 0xffu) != 0;
+                const float sc = meas ? 1.0f : pe.density * ratio[mat];
+                scales[band].v[i] = sc;
+                levels[band] |= 1ull << majorant_level(sc);
+            }
+        } else {
+            for (int m = 0; m < nm && m < dev::PALETTE_MAX; ++m)
+                scales[band].v[m] = ratio[m];
+            for (int lv = 2; lv <= MAJORANT_MAX_LEVEL; lv += 2)
+                levels[band] |= 1ull << lv;
         }
-    } else {
-        for (int m = 0; m < lut->meta.n_materials && m < dev::PALETTE_MAX; ++m)
-            scales.v[m] = lut->majorant_ratio[m];
-        for (int lv = 2; lv <= MAJORANT_MAX_LEVEL; lv += 2)
-            levels |= 1ull << lv;
     }
-    const uint64_t cell_bytes = ncell * sizeof(float2);
+    const uint64_t cell_bytes = ncell * b.bands * sizeof(float2);
     if (ctx->in_use + cell_bytes > ctx->budget)
         return fail(ctx, DXMC_ERR_OOM, "local-majorant grid exceeds the device memory budget");
     if (w->majorants.size() >= MAJORANT_GRIDS_PER_WORLD) {
@@ -919,11 +975,14 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
         e = cudaMallocAsync(&d1, ncell * sizeof(float), s);
     if (e == cudaSuccess)
         e = cudaMallocAsync(&cost, ncell * sizeof(float), s);
-    if (e == cudaSuccess)
-        e = dev::launch_majorant_levels(w->params, scales, b, level, cells, cost, s);
-    for (int lv = 1; lv <= MAJORANT_MAX_LEVEL && e == cudaSuccess; ++lv)
-        if (levels >> lv & 1ull)
-            e = dev::launch_majorant_level_pass(b, level, lv, d0, d1, cells, cost, s);
+    for (int band = 0; band < b.bands && e == cudaSuccess; ++band) {
+        b.band = band;
+        b.mu_ref = lut->mu_ref[band];
+        e = dev::launch_majorant_levels(w->params, scales[band], b, level, cells, cost, s);
+        for (int lv = 1; lv <= MAJORANT_MAX_LEVEL && e == cudaSuccess; ++lv)
+            if (levels[band] >> lv & 1ull)
+                e = dev::launch_majorant_level_pass(b, level, lv, d0, d1, cells, cost, s);
+    }
     for (void* ptr : { static_cast<void*>(level), static_cast<void*>(d0), static_cast<void*>(d1), static_cast<void*>(cost) })
         if (ptr)
             cudaFreeAsync(ptr, s);
@@ -943,6 +1002,9 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     m.grid.nxy = b.n[0] * b.n[1];
     for (int a = 0; a < 3; ++a)
         m.grid.shift[a] = b.shift[a];
+    m.grid.bands = b.bands;
+    for (int k = 0; k < dev::MAJORANT_MAX_BANDS - 1; ++k)
+        m.grid.band_edge[k] = lut->band_edge[k];
     ctx->in_use += cell_bytes;
     w->majorants.push_back(m);
     *out = &w->majorants.back().grid;
@@ -1192,9 +1254,11 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
         const bool queued = chunk > 0;
         const int regen = jd->regen_threshold > 0 ? jd->regen_threshold : ctx->options.regen_threshold;
         const int inter = jd->interact_threshold > 0 ? jd->interact_threshold : ctx->options.interact_threshold;
-        p.regen_threshold = regen > 0 ? std::min(regen, 32) : (queued ? DEFAULT_QUEUE_REGEN_THRESHOLD : DEFAULT_REGEN_THRESHOLD);
+        const int regen_default = queued ? DEFAULT_QUEUE_REGEN_THRESHOLD : (grid ? DEFAULT_LOCAL_REGEN_THRESHOLD : DEFAULT_REGEN_THRESHOLD);
+        p.regen_threshold = regen > 0 ? std::min(regen, 32) : regen_default;
         p.interact_threshold = inter > 0 ? std::min(inter, 32) : (queued ? DEFAULT_QUEUE_INTERACT_THRESHOLD : DEFAULT_INTERACT_THRESHOLD);
-        p.woodcock_burst = jd->woodcock_burst > 0 ? std::min(jd->woodcock_burst, 64) : DEFAULT_WOODCOCK_BURST;
+        p.woodcock_burst = jd->woodcock_burst > 0 ? std::min(jd->woodcock_burst, 64)
+                                                  : (grid ? DEFAULT_LOCAL_WOODCOCK_BURST : DEFAULT_WOODCOCK_BURST);
     }
     if (grid)
         p.majorant = *grid;
@@ -2119,11 +2183,12 @@ int ctx_sm_count(const dxmc_gpu_ctx* ctx) { return ctx->sm_count; }
 size_t ctx_max_smem(const dxmc_gpu_ctx* ctx) { return ctx->max_smem_optin; }
 void ctx_set_error(dxmc_gpu_ctx* ctx, const std::string& msg) { ctx->last_error = msg; }
 std::mutex& ctx_mutex(dxmc_gpu_ctx* ctx) { return ctx->mutex; }
-int ctx_regen_threshold(const dxmc_gpu_ctx* ctx)
+int ctx_regen_threshold(const dxmc_gpu_ctx* ctx, bool local)
 {
-    return ctx->options.regen_threshold > 0 ? std::min(ctx->options.regen_threshold, 32) : DEFAULT_REGEN_THRESHOLD;
+    return ctx->options.regen_threshold > 0 ? std::min(ctx->options.regen_threshold, 32)
+                                            : (local ? DEFAULT_LOCAL_REGEN_THRESHOLD : DEFAULT_REGEN_THRESHOLD);
 }
-int default_woodcock_burst() { return DEFAULT_WOODCOCK_BURST; }
+int default_woodcock_burst(bool local) { return local ? DEFAULT_LOCAL_WOODCOCK_BURST : DEFAULT_WOODCOCK_BURST; }
 
 int ctx_interact_threshold(const dxmc_gpu_ctx* ctx)
 {

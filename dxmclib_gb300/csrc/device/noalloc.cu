@@ -212,9 +212,9 @@ int ctx_sm_count(const dxmc_gpu_ctx* ctx);
 size_t ctx_max_smem(const dxmc_gpu_ctx* ctx);
 void ctx_set_error(dxmc_gpu_ctx* ctx, const std::string& msg);
 std::mutex& ctx_mutex(dxmc_gpu_ctx* ctx);
-int ctx_regen_threshold(const dxmc_gpu_ctx* ctx);
+int ctx_regen_threshold(const dxmc_gpu_ctx* ctx, bool local);
 int ctx_interact_threshold(const dxmc_gpu_ctx* ctx);
-int default_woodcock_burst();
+int default_woodcock_burst(bool local);
 const dev::WorldParams* world_params(const dxmc_world* w, const dxmc_gpu_ctx** owner, int* n_materials);
 const float* lut_image(const dxmc_lut* l, dev::LutMeta* meta, const dxmc_gpu_ctx** owner);
 const dev::MajorantGrid* built_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* l, const dxmc_job_desc* jd);
@@ -340,12 +340,13 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         p.seed = jd->seed;
         p.tally_mode = 0; // FP64 atomics
         p.uniform_hpe = 0; // exposure found by binary search over the prefix sums
-        p.regen_threshold = capi::ctx_regen_threshold(ctx);
-        p.interact_threshold = capi::ctx_interact_threshold(ctx);
-        p.woodcock_burst = jd->woodcock_burst > 0 ? std::min(jd->woodcock_burst, 64) : capi::default_woodcock_burst();
         // local majorants only from a grid built earlier (dxmc_gpu_world_prepare or a job)
-        if (const dev::MajorantGrid* g = capi::built_majorant(ctx, world, lut, jd))
+        const dev::MajorantGrid* g = capi::built_majorant(ctx, world, lut, jd);
+        if (g)
             p.majorant = *g;
+        p.regen_threshold = capi::ctx_regen_threshold(ctx, g != nullptr);
+        p.interact_threshold = capi::ctx_interact_threshold(ctx);
+        p.woodcock_burst = jd->woodcock_burst > 0 ? std::min(jd->woodcock_burst, 64) : capi::default_woodcock_burst(g != nullptr);
         const size_t lut_bytes = static_cast<size_t>(meta.total_floats) * sizeof(float);
         const size_t smem_limit = std::min<size_t>(capi::ctx_max_smem(ctx), 96 * 1024);
         p.lut_in_smem = lut_bytes <= smem_limit ? 1 : 0;

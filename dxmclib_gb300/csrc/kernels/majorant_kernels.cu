@@ -21,6 +21,7 @@
 //   3. each cell keeps the (level, R) of smallest expected steps per mm,
 //      mu / (1 - exp(-mu R)) with mu = scale * global majorant at a reference
 //      energy, or the global majorant itself (R infinite).
+// The three steps run once per energy band, with the ratios r_m of that band.
 #include <cmath>
 
 #include "transport.cuh"
@@ -82,7 +83,7 @@ __global__ void majorant_level_kernel(WorldParams w, const __grid_constant__ Maj
                 --lv;
         }
         level[c] = static_cast<uint8_t>(lv);
-        cells[c] = make_float2(1.0f, INFINITY); // the global majorant until a level does better
+        cells[c * b.bands + b.band] = make_float2(1.0f, INFINITY); // the global majorant until a level does better
         cost[c] = b.mu_ref;
     }
 }
@@ -165,7 +166,7 @@ __global__ void majorant_axis_kernel(MajorantBuild b, const float* __restrict__ 
             const float c_new = mu / (1.0f - expf(-mu * R)); // R infinite: mu
             if (c_new < cost[c]) {
                 cost[c] = c_new;
-                cells[c] = make_float2(1.0f / s, R);
+                cells[c * b.bands + b.band] = make_float2(1.0f / s, R);
             }
         }
     }

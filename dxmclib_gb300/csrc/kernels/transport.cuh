@@ -33,17 +33,22 @@ struct WorldParams {
 };
 
 // Local majorants for Woodcock tracking: the voxel grid is cut into cells of
-// 2^shift voxels per axis, and cell c holds (1 / s, R): every voxel within the
+// 2^shift voxels per axis and the photon energies into bands; cell c holds for
+// band b the pair cells[c * bands + b] = (1 / s, R): every voxel within the
 // distance R (mm) of any point of the cell attenuates less than s times the
-// global majorant at every energy.  A flight drawn with the majorant s * M(E)
-// stops after R without a collision test and is drawn again from there (the
-// exponential distribution has no memory), so the tracking stays exact while
-// it takes far fewer steps through air, lung and soft tissue.  cells == nullptr
-// selects the global majorant of the reference (s = 1, R infinite).
+// global majorant at every energy of the band.  A flight drawn with the
+// majorant s * M(E) stops after R without a collision test and is drawn again
+// from there (the exponential distribution has no memory), so the tracking
+// stays exact while it takes far fewer steps through air, lung and soft tissue.
+// cells == nullptr selects the global majorant of the reference (s = 1, R
+// infinite).
+constexpr int MAJORANT_MAX_BANDS = 4;
 struct MajorantGrid {
     const float2* cells;
     uint32_t nx, nxy;    // cells along x, cells per z slab
     int shift[3];        // log2 of the cell size in voxels
+    int bands;
+    float band_edge[MAJORANT_MAX_BANDS - 1]; // keV, ascending; band = number of edges <= E (unused: infinity)
     int pad;
 };
 
@@ -162,9 +167,10 @@ struct MajorantBuild {
     uint32_t n[3];       // cells per axis
     int shift[3];
     float edge[3];       // cell size (mm)
-    float mu_ref;        // global majorant (1/mm) at the reference energy of the cost model
+    float mu_ref;        // global majorant (1/mm) at the reference energy of the band's cost model
     int levels_per_octave;
     int max_level;
+    int band, bands;     // the band being built; output pairs at cells[c * bands + band]
 };
 struct MajorantScales {
     float v[PALETTE_MAX];

@@ -481,6 +481,7 @@ namespace {
         float forced_wc; // weight correction waiting for a forced-voxel interaction pass
         bool armed;      // energy x weight is below the Russian-roulette threshold
         float cinv, cR;  // local majorant: 1 / scale and the flight length it holds for (MajorantGrid)
+        int band;        // energy band of the local-majorant grid
         uint32_t steps, deposits, overflows, histories;
 
         __device__ void reset_counters() { steps = deposits = overflows = histories = 0; }
@@ -501,19 +502,22 @@ namespace {
         __device__ void arm() { armed = ph.energy * ph.weight < ROULETTE_THRESHOLD; }
     };
 
-    // Local majorant of the cell a photon starts in (it enters the grid on its
-    // boundary, so the coordinates are clamped onto the grid).
-    __device__ __forceinline__ void enter_cell(Lane& s, const TransportParams& p)
+    // Local majorant of the photon's cell for its energy band, after the energy
+    // changed (a new photon, or an interaction): the flight drawn next must be
+    // bounded for the new energy.  A new photon sits on the grid boundary, so the
+    // coordinates are clamped onto the grid.
+    __device__ __forceinline__ void fetch_cell(Lane& s, const TransportParams& p)
     {
         const MajorantGrid& g = p.majorant;
-        if (!g.cells || !s.alive)
-            return;
         const WorldParams& w = p.world;
+        const float E = s.ph.energy;
+        s.band = (E >= g.band_edge[0]) + (E >= g.band_edge[1]) + (E >= g.band_edge[2]);
         const float fx = fminf(fmaxf(fmaf(s.ph.px, w.inv_spacing[0], -w.lo_inv[0]), 0.0f), w.dims_f[0] - 1.0f);
         const float fy = fminf(fmaxf(fmaf(s.ph.py, w.inv_spacing[1], -w.lo_inv[1]), 0.0f), w.dims_f[1] - 1.0f);
         const float fz = fminf(fmaxf(fmaf(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2]), 0.0f), w.dims_f[2] - 1.0f);
         const uint32_t ix = static_cast<uint32_t>(fx), iy = static_cast<uint32_t>(fy), iz = static_cast<uint32_t>(fz);
-        const float2 cell = __ldg(g.cells + ((iz >> g.shift[2]) * g.nxy + (iy >> g.shift[1]) * g.nx + (ix >> g.shift[0])));
+        const uint32_t c = (iz >> g.shift[2]) * g.nxy + (iy >> g.shift[1]) * g.nx + (ix >> g.shift[0]);
+        const float2 cell = __ldg(g.cells + (c * g.bands + s.band));
         s.cinv = cell.x;
         s.cR = cell.y;
     }
@@ -548,7 +552,6 @@ namespace {
         ++s.histories;
         s.alive = transport_to_world(p.world, s.ph);
         s.start_photon();
-        enter_cell(s, p);
     }
 
     // One iteration of the warp-synchronous loop for every lane of the warp: a
@@ -572,6 +575,8 @@ namespace {
                 s.stepK = lut_max_inverse(L, m, s.logE, s.seg) * (10.0f * 0.693147180559945f); // cm -> mm, log2 -> ln
                 s.updateMax = false;
                 s.cached_mat = -1;
+                if (p.majorant.cells)
+                    fetch_cell(s, p);
             }
             // Up to p.woodcock_burst Woodcock steps per iteration: a lane keeps stepping
             // through virtual collisions and stops at a real event, the grid boundary or a
@@ -608,7 +613,8 @@ namespace {
                 const float cinv = s.cinv; // the majorant this flight was drawn with
                 if (p.majorant.cells) {
                     const MajorantGrid& g = p.majorant;
-                    const float2 cell = __ldg(g.cells + ((iz >> g.shift[2]) * g.nxy + (iy >> g.shift[1]) * g.nx + (ix >> g.shift[0])));
+                    const uint32_t c = (iz >> g.shift[2]) * g.nxy + (iy >> g.shift[1]) * g.nx + (ix >> g.shift[0]);
+                    const float2 cell = __ldg(g.cells + (c * g.bands + s.band));
                     s.cinv = cell.x;
                     s.cR = cell.y;
                 }
@@ -870,7 +876,6 @@ namespace {
                     if (mine) {
                         if (use_queue) {
                             take_queued(s, p.queue, pool_next + rank);
-                            enter_cell(s, p);
                         } else
                             take_history(s, p, pool_next + rank);
                     }

@@ -245,10 +245,11 @@ void dxmc_gpu_world_free(dxmc_world* world);
  * uses it only if it exists).  The world keeps the grid until it is freed. */
 int dxmc_gpu_world_prepare(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut);
 /* Reads back a built local-majorant grid: cells per axis, log2 of the cell size
- * in voxels per axis and, if cells is not NULL, (1 / scale, R mm) per cell, x
- * fastest.  DXMC_ERR_STATE if the pair has no grid. */
+ * in voxels per axis, the number of energy bands, the band edges (keV, bands - 1
+ * values; may be NULL) and, if cells is not NULL, (1 / scale, R mm) per cell and
+ * band, band fastest, then x, y, z.  DXMC_ERR_STATE if the pair has no grid. */
 int dxmc_gpu_world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut, uint32_t* cells_per_axis,
-    int32_t* shift, float* cells);
+    int32_t* shift, int32_t* bands, float* band_edges, float* cells);
 
 /* ---- LUT on the device --------------------------------------------------- */
 int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* blob, dxmc_lut** out);

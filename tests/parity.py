@@ -38,6 +38,8 @@ def compare_sparse(ref: dict, dose: np.ndarray, var: np.ndarray, min_frac: float
     d2, v2 = dose[i], var[i]
     sigma = np.sqrt(np.maximum(v1, 0) + np.maximum(v2, 0))
     z = (d2 - d1) / np.where(sigma > 0, sigma, np.inf)
+    with np.errstate(divide="ignore", invalid="ignore"):  # a voxel of one tally may be empty
+        rel = (d2 - d1) / d1
     return dict(
         n_voxels=int(sel.sum()),
         frac_3sigma=float(np.mean(np.abs(z) <= 3.0)),
@@ -47,8 +49,8 @@ def compare_sparse(ref: dict, dose: np.ndarray, var: np.ndarray, min_frac: float
         # dose-weighted mean relative difference: sum(d2 - d1) / sum(d1); the unweighted
         # mean of ratios is biased by noise in the denominator when voxels are noisy
         mean_bias=float(np.sum(d2 - d1) / np.sum(d1)),
-        mean_rel_unweighted=float(np.mean((d2 - d1) / d1)),
-        mean_abs_rel=float(np.mean(np.abs(d2 - d1) / d1)),
+        mean_rel_unweighted=float(np.mean(rel)),
+        mean_abs_rel=float(np.mean(np.abs(rel))),
         max_abs_z=float(np.max(np.abs(z)) / np.sqrt(max(1.0, float(np.mean(z * z))))) if len(z) else 0.0,
     )
 

@@ -25,11 +25,10 @@ def _phantom():
     return ct_world(nz=24, nx=104, ny=104, spacing=(4.0, 4.0, 5.0), seed=7)
 
 
-def _voxel_scales(world, blob):
+def _voxel_scales(world, blob, e_lo, e_hi):
     """Per voxel, the largest ratio of its attenuation to the global majorant over
-    the LUT's energies (measurement voxels count as 1)."""
-    info = blob.info()
-    energies = np.exp(np.linspace(np.log(info["min_energy"] * 1.0001), np.log(info["max_energy"] * 0.9999), 600))
+    the energies [e_lo, e_hi] (measurement voxels count as 1)."""
+    energies = np.exp(np.linspace(np.log(e_lo), np.log(e_hi), 400))
     inv = np.array([blob.max_attenuation_inverse(e) for e in energies])
     r = np.array([max(blob.attenuation(m, e).sum() * i for e, i in zip(energies, inv))
                   for m in range(len(world.materialMap()))])
@@ -47,32 +46,37 @@ def test_majorant_grid_bounds_attenuation(gpu_ctx):
     dworld = dx.DeviceWorld(gpu_ctx, world)
     dlut = dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, 120.0))
     dworld.prepare(dlut)
-    shift, cells = dworld.majorant(dlut)
+    shift, edges, cells = dworld.majorant(dlut)
+    assert cells.shape[3] == 4 and len(edges) == 3 and np.all(np.diff(edges) > 0)
     blob = dx.LutBlob.from_world(world, 120.0)
-    scale = _voxel_scales(world, blob)
+    bounds = [1.0, *edges, 120.0]
     sp = np.array(world.spacing())[::-1]  # (z, y, x) mm
     b = [1 << int(shift[2]), 1 << int(shift[1]), 1 << int(shift[0])]
-    s_cell = 1.0 / cells[..., 0].astype(np.float64)
-    R_cell = cells[..., 1].astype(np.float64)
-    assert np.all(s_cell <= 1.0 + 1e-6)
-    # the grid is worth having: air cells far from the body get small scales and long flights
-    assert (s_cell < 0.01).mean() > 0.05, np.unique(s_cell)
-    assert np.nanmax(np.where(s_cell < 0.01, R_cell, np.nan)) > 30.0
     checked = 0
-    for s in np.unique(s_cell[np.isfinite(R_cell)]):
-        hot = scale > s * (1.0 + 1e-4)
-        if not hot.any():
-            continue
-        # exact gap between voxel boxes: distance transform to the hot set dilated by one voxel
-        near = ndimage.binary_dilation(hot, structure=np.ones((3, 3, 3), bool))
-        gap = np.where(near, 0.0, ndimage.distance_transform_edt(~near, sampling=sp))
-        pad = [(0, (-gap.shape[i]) % b[i]) for i in range(3)]
-        g = np.pad(gap, pad, constant_values=np.inf)
-        cell_gap = g.reshape(g.shape[0] // b[0], b[0], g.shape[1] // b[1], b[1], g.shape[2] // b[2], b[2]).min(axis=(1, 3, 5))
-        sel = (s_cell == s) & np.isfinite(R_cell)
-        bad = sel & (R_cell > cell_gap + 1e-3)
-        assert not bad.any(), (s, int(bad.sum()), R_cell[bad][:5], cell_gap[bad][:5])
-        checked += int(sel.sum())
+    for band in range(cells.shape[3]):
+        scale = _voxel_scales(world, blob, bounds[band] * 1.0001, bounds[band + 1] * 0.9999)
+        s_cell = 1.0 / cells[..., band, 0].astype(np.float64)
+        R_cell = cells[..., band, 1].astype(np.float64)
+        assert np.all(s_cell <= 1.0 + 1e-6)
+        # the grid is worth having: air cells far from the body get small scales and long flights
+        assert (s_cell < 0.01).mean() > 0.05, np.unique(s_cell)
+        assert np.nanmax(np.where(s_cell < 0.01, R_cell, np.nan)) > 30.0
+        # soft tissue gets a level well below the bone-set majorant
+        assert np.any((s_cell > 0.05) & (s_cell < 0.7)), np.unique(s_cell)
+        for s in np.unique(s_cell[np.isfinite(R_cell)]):
+            hot = scale > s * (1.0 + 1e-4)
+            if not hot.any():
+                continue
+            # exact gap between voxel boxes: distance transform to the hot set dilated by one voxel
+            near = ndimage.binary_dilation(hot, structure=np.ones((3, 3, 3), bool))
+            gap = np.where(near, 0.0, ndimage.distance_transform_edt(~near, sampling=sp))
+            pad = [(0, (-gap.shape[i]) % b[i]) for i in range(3)]
+            g = np.pad(gap, pad, constant_values=np.inf)
+            cell_gap = g.reshape(g.shape[0] // b[0], b[0], g.shape[1] // b[1], b[1], g.shape[2] // b[2], b[2]).min(axis=(1, 3, 5))
+            sel = (s_cell == s) & np.isfinite(R_cell)
+            bad = sel & (R_cell > cell_gap + 1e-3)
+            assert not bad.any(), (band, s, int(bad.sum()), R_cell[bad][:5], cell_gap[bad][:5])
+            checked += int(sel.sum())
     assert checked > 0
     dlut.close()
     dworld.close()
@@ -124,12 +128,12 @@ def test_forced_scoring_keeps_global_majorant(gpu_ctx):
     dworld = dx.DeviceWorld(gpu_ctx, world)
     dlut = dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, src.maxPhotonEnergyProduced()))
     dworld.prepare(dlut)
-    shift, cells = dworld.majorant(dlut)
+    shift, _, cells = dworld.majorant(dlut)
     b = [1 << int(shift[2]), 1 << int(shift[1]), 1 << int(shift[0])]
-    # cells holding a measurement voxel track with the global majorant
+    # cells holding a measurement voxel track with the global majorant in every band
     m = np.pad(meas, [(0, (-meas.shape[i]) % b[i]) for i in range(3)])
     mc = m.reshape(m.shape[0] // b[0], b[0], m.shape[1] // b[1], b[1], m.shape[2] // b[2], b[2]).max(axis=(1, 3, 5))
-    assert np.all(cells[..., 0][mc > 0] == 1.0) and np.all(np.isinf(cells[..., 1][mc > 0]))
+    assert np.all(cells[mc > 0][..., 0] == 1.0) and np.all(np.isinf(cells[mc > 0][..., 1]))
     ex = src.exposures(world.directionCosines())
     runs = []
     for seed, mode in ((21, A.TRACKING_GLOBAL), (22, A.TRACKING_GLOBAL), (23, A.TRACKING_LOCAL)):
