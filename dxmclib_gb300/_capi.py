@@ -168,7 +168,7 @@ SIGNATURES = {
     "dxmc_gpu_world_free": (None, [VP]),
     "dxmc_gpu_world_prepare": (C.c_int, [VP, VP, VP]),
     "dxmc_gpu_world_majorant": (C.c_int, [VP, VP, VP, C.POINTER(C.c_uint32), C.POINTER(C.c_int32),
-                                          C.POINTER(C.c_int32), FP, FP]),
+                                          C.POINTER(C.c_int32), FP, FP, FP]),
     "dxmc_gpu_lut_upload": (C.c_int, [VP, VP, C.POINTER(VP)]),
     "dxmc_gpu_lut_free": (None, [VP]),
     "dxmc_gpu_job_submit": (C.c_int, [VP, VP, VP, C.POINTER(JobDesc), C.POINTER(VP)]),

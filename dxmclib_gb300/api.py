@@ -899,19 +899,22 @@ class DeviceWorld:
 
     def majorant(self, dlut: "DeviceLut"):
         """The local-majorant grid built for ``dlut``: (shift (3,), band edges in keV
-        (bands - 1,), cells (nz, ny, nx, bands, 2) holding 1 / scale and R in mm)."""
+        (bands - 1,), box (6,) lo / hi in mm of the cells above their band's emptiest
+        level, cells (nz, ny, nx, bands, 2) holding 1 / scale and R in mm, R < 0
+        outside the box)."""
         n = (C.c_uint32 * 3)()
         sh = (C.c_int32 * 3)()
         nb = C.c_int32()
         edges = np.zeros(8, np.float32)
+        box = np.zeros(6, np.float32)
         A.check(self.ctx.lib.dxmc_gpu_world_majorant(self.ctx.handle, self.handle, dlut.handle, n, sh, C.byref(nb),
-                                                     edges.ctypes.data_as(A.FP), None),
+                                                     edges.ctypes.data_as(A.FP), box.ctypes.data_as(A.FP), None),
                 self.ctx.handle, "dxmc_gpu_world_majorant")
         cells = np.zeros((n[2], n[1], n[0], nb.value, 2), np.float32)
         A.check(self.ctx.lib.dxmc_gpu_world_majorant(self.ctx.handle, self.handle, dlut.handle, n, sh, C.byref(nb),
-                                                     None, cells.ctypes.data_as(A.FP)), self.ctx.handle,
+                                                     None, None, cells.ctypes.data_as(A.FP)), self.ctx.handle,
                 "dxmc_gpu_world_majorant")
-        return np.array(sh[:], np.int64), edges[:nb.value - 1].astype(np.float64), cells
+        return (np.array(sh[:], np.int64), edges[:nb.value - 1].astype(np.float64), box.astype(np.float64), cells)
 
     def max_density(self) -> np.ndarray:
         n = len(self.world.materialMap())

@@ -33,7 +33,21 @@ constexpr int DEFAULT_WOODCOCK_BURST = DXMC_DEFAULT_WOODCOCK_BURST; // Woodcock 
 // With local majorants a history takes fewer, more varied steps: shorter bursts
 // and a later refill keep more lanes of a warp stepping together.
 constexpr int DEFAULT_LOCAL_REGEN_THRESHOLD = 10;
-constexpr int DEFAULT_LOCAL_WOODCOCK_BURST = 5;
+constexpr int DEFAULT_LOCAL_WOODCOCK_BURST = 4;
+// Local-majorant grid: target cell edge and energy bands (above 15 keV)
+#ifndef DXMC_MAJORANT_CELL_MM
+#define DXMC_MAJORANT_CELL_MM 6.0
+#endif
+#ifndef DXMC_MAJORANT_BANDS
+#define DXMC_MAJORANT_BANDS 8
+#endif
+#ifndef DXMC_MAJORANT_BOX
+#define DXMC_MAJORANT_BOX 1 // cells outside the box of the denser cells may fly to it
+#endif
+constexpr double MAJORANT_CELL_MM = DXMC_MAJORANT_CELL_MM; // target cell edge
+constexpr int MAJORANT_BANDS = DXMC_MAJORANT_BANDS;         // energy bands above 15 keV
+static_assert(MAJORANT_BANDS >= 1 && MAJORANT_BANDS <= dev::MAJORANT_MAX_BANDS, "band count");
+
 // Photons are generated inside the transport kernel unless a job or the context
 // asks for a pre-generated queue (2^n photons per generation pass): with the
 // Woodcock burst the in-kernel generation is as fast and needs no queue memory.
@@ -146,8 +160,8 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 // Per energy band and material m, the largest ratio of m's attenuation (per
 // g/cm3) to the global majorant over the band's energies, from the float image
 // the kernels read.  Photons are tracked from 1 keV (the transport cutoff) to
-// the LUT's maximum energy; above 15 keV that range is cut into four bands with
-// edges log-spaced from 10 keV, since soft tissue's share of a bone-set
+// the LUT's maximum energy; above 15 keV that range is cut into MAJORANT_BANDS
+// bands with edges log-spaced from 10 keV, since soft tissue's share of a bone-set
 // majorant varies five-fold over a diagnostic spectrum.  In each log-log
 // segment both attenuations are exponentials of log E, so the ratio of their
 // sum to the majorant is convex in log E and peaks at an end of the interval of
@@ -177,7 +191,7 @@ void majorant_ratios(const std::vector<float>& img, const dev::LutMeta& m, dxmc_
         return std::pow(10.0, static_cast<double>(maxc[2 * seg]) + maxc[2 * seg + 1] * static_cast<double>(le));
     };
     const double e_max = std::max(static_cast<double>(m.max_energy), 1.0);
-    lut.majorant_bands = e_max > 15.0 ? dev::MAJORANT_MAX_BANDS : 1;
+    lut.majorant_bands = e_max > 15.0 ? MAJORANT_BANDS : 1;
     const int nb = lut.majorant_bands;
     std::vector<double> edges { 1.0 };
     for (int k = 1; k < nb; ++k)
@@ -696,7 +710,7 @@ int dxmc_gpu_world_prepare(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut*
 }
 
 int dxmc_gpu_world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut, uint32_t* cells_per_axis,
-    int32_t* shift, int32_t* bands, float* band_edges, float* cells)
+    int32_t* shift, int32_t* bands, float* band_edges, float* box, float* cells)
 {
     if (!ctx || !world || !lut || !cells_per_axis || !shift || !bands)
         return DXMC_ERR_INVALID;
@@ -712,10 +726,17 @@ int dxmc_gpu_world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut
     *bands = g->bands;
     for (int k = 0; band_edges && k + 1 < g->bands; ++k)
         band_edges[k] = g->band_edge[k];
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaSuccess;
+    if (box)
+        e = cudaMemcpyAsync(box, g->box, 6 * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess && !cells)
+        e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "local-majorant grid read");
     if (cells) {
-        cudaSetDevice(ctx->device);
         const uint64_t n = static_cast<uint64_t>(cells_per_axis[0]) * cells_per_axis[1] * cells_per_axis[2] * g->bands;
-        cudaError_t e = cudaMemcpyAsync(cells, g->cells, n * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream);
+        e = cudaMemcpyAsync(cells, g->cells, n * sizeof(float2), cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess)
             e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess)
@@ -881,7 +902,6 @@ namespace {
 // ---- local-majorant grids ------------------------------------------------------------
 constexpr int MAJORANT_LEVELS_PER_OCTAVE = 4;
 constexpr int MAJORANT_MAX_LEVEL = 48;            // scale 2^-12: empty and air cells
-constexpr double MAJORANT_CELL_MM = 6.0;          // target cell edge
 constexpr uint64_t MAJORANT_MAX_CELLS_PER_AXIS = 1024;
 constexpr size_t MAJORANT_GRIDS_PER_WORLD = 4;    // one per LUT used with the world, least recently used evicted
 
@@ -951,7 +971,22 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
                 levels[band] |= 1ull << lv;
         }
     }
-    const uint64_t cell_bytes = ncell * b.bands * sizeof(float2);
+    // each band's emptiest level (the palette's highest level); for the 8-byte layout
+    // the levels are not known on the host and the box is not used
+    std::vector<int> floor_level(b.bands, -1);
+    bool use_box = false;
+    if (w->palette_index && DXMC_MAJORANT_BOX) {
+        for (int band = 0; band < b.bands; ++band) {
+            for (int lv = MAJORANT_MAX_LEVEL; lv >= 0; --lv) {
+                if (levels[band] >> lv & 1ull) {
+                    floor_level[band] = lv;
+                    break;
+                }
+            }
+            use_box = use_box || floor_level[band] >= 0;
+        }
+    }
+    const uint64_t cell_bytes = ncell * b.bands * sizeof(float2) + 8 * sizeof(float); // + the box
     if (ctx->in_use + cell_bytes > ctx->budget)
         return fail(ctx, DXMC_ERR_OOM, "local-majorant grid exceeds the device memory budget");
     if (w->majorants.size() >= MAJORANT_GRIDS_PER_WORLD) {
@@ -966,7 +1001,15 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     float2* cells = nullptr;
     uint8_t* level = nullptr;
     float *d0 = nullptr, *d1 = nullptr, *cost = nullptr;
+    int* bounds = nullptr;
     cudaError_t e = cudaMallocAsync(&cells, cell_bytes, s);
+    float* box = cells ? reinterpret_cast<float*>(cells + ncell * b.bands) : nullptr;
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(&bounds, 6 * sizeof(int), s);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(bounds, 0x7f, 3 * sizeof(int), s); // minima start large
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(bounds + 3, 0xff, 3 * sizeof(int), s); // maxima start at -1
     if (e == cudaSuccess)
         e = cudaMallocAsync(&level, ncell, s);
     if (e == cudaSuccess)
@@ -975,15 +1018,21 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
         e = cudaMallocAsync(&d1, ncell * sizeof(float), s);
     if (e == cudaSuccess)
         e = cudaMallocAsync(&cost, ncell * sizeof(float), s);
+    for (int a = 0; a < 3; ++a)
+        b.lower[a] = w->params.lower[a];
     for (int band = 0; band < b.bands && e == cudaSuccess; ++band) {
         b.band = band;
         b.mu_ref = lut->mu_ref[band];
-        e = dev::launch_majorant_levels(w->params, scales[band], b, level, cells, cost, s);
+        b.floor_level = floor_level[band];
+        e = dev::launch_majorant_levels(w->params, scales[band], b, level, cells, cost, bounds, s);
         for (int lv = 1; lv <= MAJORANT_MAX_LEVEL && e == cudaSuccess; ++lv)
             if (levels[band] >> lv & 1ull)
                 e = dev::launch_majorant_level_pass(b, level, lv, d0, d1, cells, cost, s);
     }
-    for (void* ptr : { static_cast<void*>(level), static_cast<void*>(d0), static_cast<void*>(d1), static_cast<void*>(cost) })
+    if (e == cudaSuccess && use_box)
+        e = dev::launch_majorant_box(b, bounds, cells, box, s);
+    for (void* ptr : { static_cast<void*>(level), static_cast<void*>(d0), static_cast<void*>(d1), static_cast<void*>(cost),
+             static_cast<void*>(bounds) })
         if (ptr)
             cudaFreeAsync(ptr, s);
     if (e != cudaSuccess) {
@@ -998,6 +1047,7 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     m.bytes = cell_bytes;
     m.last_use = ++w->majorant_clock;
     m.grid.cells = cells;
+    m.grid.box = box;
     m.grid.nx = b.n[0];
     m.grid.nxy = b.n[0] * b.n[1];
     for (int a = 0; a < 3; ++a)

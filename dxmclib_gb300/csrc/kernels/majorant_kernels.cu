@@ -22,6 +22,8 @@
 //      mu / (1 - exp(-mu R)) with mu = scale * global majorant at a reference
 //      energy, or the global majorant itself (R infinite).
 // The three steps run once per energy band, with the ratios r_m of that band.
+// Last, the cells outside the box of all cells above their band's emptiest
+// level get -R: there a flight may also run to that box (MajorantGrid).
 #include <cmath>
 
 #include "transport.cuh"
@@ -44,7 +46,7 @@ __device__ __forceinline__ float level_scale(int level, int per_octave)
 }
 
 __global__ void majorant_level_kernel(WorldParams w, const __grid_constant__ MajorantScales scales, MajorantBuild b,
-    uint8_t* __restrict__ level, float2* __restrict__ cells, float* __restrict__ cost)
+    uint8_t* __restrict__ level, float2* __restrict__ cells, float* __restrict__ cost, int* __restrict__ bounds)
 {
     __shared__ float scale_table[PALETTE_MAX];
     for (int i = threadIdx.x; i < PALETTE_MAX; i += blockDim.x)
@@ -85,6 +87,51 @@ __global__ void majorant_level_kernel(WorldParams w, const __grid_constant__ Maj
         level[c] = static_cast<uint8_t>(lv);
         cells[c * b.bands + b.band] = make_float2(1.0f, INFINITY); // the global majorant until a level does better
         cost[c] = b.mu_ref;
+        // cells above the band's emptiest level widen the box (warp-reduced atomics)
+        const bool above = b.floor_level >= 0 && lv < b.floor_level;
+        const unsigned mask = __ballot_sync(__activemask(), above);
+        if (mask) {
+            const unsigned active = __activemask();
+            const int big = 0x7fffffff;
+            const int lo[3] = { above ? static_cast<int>(cx) : big, above ? static_cast<int>(cy) : big, above ? static_cast<int>(cz) : big };
+            const int hi[3] = { above ? static_cast<int>(cx) : -1, above ? static_cast<int>(cy) : -1, above ? static_cast<int>(cz) : -1 };
+            const bool leader = (threadIdx.x & 31) == __ffs(active) - 1;
+            for (int a = 0; a < 3; ++a) {
+                const int mn = __reduce_min_sync(active, lo[a]);
+                const int mx = __reduce_max_sync(active, hi[a]);
+                if (leader) {
+                    atomicMin(bounds + a, mn);
+                    atomicMax(bounds + 3 + a, mx);
+                }
+            }
+        }
+    }
+}
+
+__global__ void majorant_box_kernel(MajorantBuild b, const int* __restrict__ bounds, float2* __restrict__ cells, float* __restrict__ box)
+{
+    int lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = bounds[a];
+        hi[a] = bounds[3 + a];
+    }
+    const bool empty = lo[0] > hi[0];
+    if (blockIdx.x == 0 && threadIdx.x < 3) {
+        const int a = threadIdx.x;
+        box[a] = empty ? INFINITY : b.lower[a] + static_cast<float>(lo[a]) * b.edge[a];
+        box[3 + a] = empty ? -INFINITY : b.lower[a] + static_cast<float>(hi[a] + 1) * b.edge[a];
+    }
+    const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
+    for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < ncell;
+         c += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        uint32_t q[3];
+        cell_coords(c, b, q[0], q[1], q[2]);
+        bool outside = empty;
+        for (int a = 0; a < 3; ++a)
+            outside = outside || static_cast<int>(q[a]) < lo[a] || static_cast<int>(q[a]) > hi[a];
+        if (outside)
+            for (int k = 0; k < b.bands; ++k)
+                cells[c * b.bands + k].y = -cells[c * b.bands + k].y;
     }
 }
 
@@ -181,10 +228,17 @@ int grid_for(uint64_t n)
 } // namespace
 
 cudaError_t launch_majorant_levels(const WorldParams& w, const MajorantScales& scales, const MajorantBuild& b,
-    uint8_t* level, float2* cells, float* cost, cudaStream_t stream)
+    uint8_t* level, float2* cells, float* cost, int* bounds, cudaStream_t stream)
 {
     const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
-    majorant_level_kernel<<<grid_for(ncell), 256, 0, stream>>>(w, scales, b, level, cells, cost);
+    majorant_level_kernel<<<grid_for(ncell), 256, 0, stream>>>(w, scales, b, level, cells, cost, bounds);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_majorant_box(const MajorantBuild& b, const int* bounds, float2* cells, float* box, cudaStream_t stream)
+{
+    const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
+    majorant_box_kernel<<<grid_for(ncell), 256, 0, stream>>>(b, bounds, cells, box);
     return cudaGetLastError();
 }
 

@@ -42,9 +42,13 @@ struct WorldParams {
 // stays exact while it takes far fewer steps through air, lung and soft tissue.
 // cells == nullptr selects the global majorant of the reference (s = 1, R
 // infinite).
-constexpr int MAJORANT_MAX_BANDS = 4;
+// Cells outside the box of all cells above the emptiest level (the body of a CT
+// phantom) hold -R: a photon there may also fly straight to that box, since only
+// cells of the emptiest level lie before it on its ray.
+constexpr int MAJORANT_MAX_BANDS = 8;
 struct MajorantGrid {
     const float2* cells;
+    const float* box;    // lo[3], hi[3] in mm (grid frame) of the cells above the emptiest level
     uint32_t nx, nxy;    // cells along x, cells per z slab
     int shift[3];        // log2 of the cell size in voxels
     int bands;
@@ -171,12 +175,18 @@ struct MajorantBuild {
     int levels_per_octave;
     int max_level;
     int band, bands;     // the band being built; output pairs at cells[c * bands + band]
+    int floor_level;     // the band's emptiest level (its cells may be flown through), -1: none
+    float lower[3];      // grid corner (mm)
 };
 struct MajorantScales {
     float v[PALETTE_MAX];
 };
 cudaError_t launch_majorant_levels(const WorldParams& w, const MajorantScales& scales, const MajorantBuild& b,
-    uint8_t* level, float2* cells, float* cost, cudaStream_t stream);
+    uint8_t* level, float2* cells, float* cost, int* bounds, cudaStream_t stream);
+// After all bands: writes the box (mm) of the cells that lay above their band's
+// emptiest level (bounds: cell index min x, y, z, max x, y, z; set up as empty
+// by the caller) and marks every cell outside it by negating its R in all bands.
+cudaError_t launch_majorant_box(const MajorantBuild& b, const int* bounds, float2* cells, float* box, cudaStream_t stream);
 // Adds the candidate majorant level lv: cells whose 27-neighbourhood holds no
 // cell above the level get (level scale, distance to the nearest such cell) if
 // that lowers the expected number of steps per mm.  d0 and d1 are scratch grids.

@@ -465,6 +465,13 @@ namespace {
 #endif
 
     // State of one lane: its photon, random stream, cached lookups and counters.
+    // Per-warp counters of a job in shared memory (lane 0 adds warp totals; rare
+    // events use shared atomics), flushed to the job's counters: they cost the
+    // lanes no registers.
+    struct WarpTally {
+        unsigned long long steps, deposits, overflows, histories;
+    };
+
     struct Lane {
         Photon ph;
         Rng rng;
@@ -482,12 +489,9 @@ namespace {
         bool armed;      // energy x weight is below the Russian-roulette threshold
         float cinv, cR;  // local majorant: 1 / scale and the flight length it holds for (MajorantGrid)
         int band;        // energy band of the local-majorant grid
-        uint32_t steps, deposits, overflows, histories;
 
-        __device__ void reset_counters() { steps = deposits = overflows = histories = 0; }
         __device__ void start_photon()
         {
-            steps += hist_steps; // the previous photon's in-grid steps
             pending = EV_NONE;
             updateMax = true;
             cached_mat = -1;
@@ -511,7 +515,11 @@ namespace {
         const MajorantGrid& g = p.majorant;
         const WorldParams& w = p.world;
         const float E = s.ph.energy;
-        s.band = (E >= g.band_edge[0]) + (E >= g.band_edge[1]) + (E >= g.band_edge[2]);
+        int band = 0;
+#pragma unroll
+        for (int k = 0; k < MAJORANT_MAX_BANDS - 1; ++k)
+            band += E >= g.band_edge[k];
+        s.band = band;
         const float fx = fminf(fmaxf(fmaf(s.ph.px, w.inv_spacing[0], -w.lo_inv[0]), 0.0f), w.dims_f[0] - 1.0f);
         const float fy = fminf(fmaxf(fmaf(s.ph.py, w.inv_spacing[1], -w.lo_inv[1]), 0.0f), w.dims_f[1] - 1.0f);
         const float fz = fminf(fmaxf(fmaf(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2]), 0.0f), w.dims_f[2] - 1.0f);
@@ -520,6 +528,26 @@ namespace {
         const float2 cell = __ldg(g.cells + (c * g.bands + s.band));
         s.cinv = cell.x;
         s.cR = cell.y;
+    }
+
+    // Safe flight length in a cell outside the box of the denser cells (the cell
+    // holds -R): the ball of radius R, or the ray up to where it enters the box
+    // (slab test in flight-parameter units, as the position update), whichever
+    // reaches further.  A ray that misses the box may fly to the grid boundary.
+    __device__ __forceinline__ float reach_to_box(const Photon& ph, const MajorantGrid& g, float R)
+    {
+        const float p[3] = { ph.px, ph.py, ph.pz };
+        const float d[3] = { ph.dx, ph.dy, ph.dz };
+        float tmin = 0.0f, tmax = INFINITY;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float inv = 1.0f / d[a];
+            const float t0 = (__ldg(g.box + a) - p[a]) * inv;
+            const float t1 = (__ldg(g.box + 3 + a) - p[a]) * inv;
+            tmin = fmaxf(tmin, fminf(t0, t1));
+            tmax = fminf(tmax, fmaxf(t0, t1));
+        }
+        return fmaxf(R, tmin <= tmax ? tmin : INFINITY);
     }
 
     // Loads photon + stream state from the pre-generated queue.
@@ -549,7 +577,6 @@ namespace {
         DevExposure ex;
         load_exposure(p.source.exposures + ei, ex);
         sample_particle(p.source, ex, s.rng, s.ph);
-        ++s.histories;
         s.alive = transport_to_world(p.world, s.ph);
         s.start_photon();
     }
@@ -559,7 +586,7 @@ namespace {
     // the per-type interaction passes once enough lanes wait (transport.hpp:523-638),
     // Russian roulette and scoring.  Must be called by all 32 lanes.
     template <int MODEL, bool PALETTE>
-    __device__ __forceinline__ void advance(Lane& s, const TransportParams& p, const float* L, const PaletteEntry* pal,
+    __device__ __forceinline__ void advance(Lane& s, WarpTally& wt, const TransportParams& p, const float* L, const PaletteEntry* pal,
         bool drain, int interact_t)
     {
         const LutMeta& m = p.lut_meta;
@@ -585,15 +612,18 @@ namespace {
             const int burst = max(p.woodcock_burst, 1); // at least one step: every iteration makes progress
             if (s.hist_steps > MAX_STEPS_PER_HISTORY) {
                 // bounded work per history (checked per burst: at most burst - 1 steps over)
-                ++s.overflows;
+                atomicAdd(&wt.overflows, 1ull);
                 s.alive = false;
             }
             for (int k = 0; k < burst && s.alive; ++k) {
                 // a flight drawn with the local majorant ends without a collision test
                 // where that majorant stops holding (truncated: drawn again from there)
+                float R = s.cR;
+                if (R < 0.0f)
+                    R = reach_to_box(s.ph, p.majorant, -R);
                 const float flight = -__log2f(s.rng.uniform_open()) * (s.stepK * s.cinv);
-                const bool truncated = flight > s.cR;
-                const float step = fminf(flight, s.cR);
+                const bool truncated = flight > R;
+                const float step = fminf(flight, R);
                 s.ph.px = fmaf(s.ph.dx, step, s.ph.px);
                 s.ph.py = fmaf(s.ph.dy, step, s.ph.py);
                 s.ph.pz = fmaf(s.ph.dz, step, s.ph.pz);
@@ -684,9 +714,9 @@ namespace {
             // interaction pass can add a second deposit in the same iteration
             if (isfinite(deposit)) {
                 score(p, s.vidx, deposit);
-                ++s.deposits;
+                atomicAdd(&wt.deposits, 1ull);
             } else {
-                ++s.overflows;
+                atomicAdd(&wt.overflows, 1ull);
                 s.alive = false;
                 s.pending = EV_NONE;
             }
@@ -720,7 +750,7 @@ namespace {
                 if (__any_sync(FULL_MASK, s.pending == EV_COMPTON) && s.pending == EV_COMPTON) {
                     float e = 0.0f;
                     if (!compton_scatter<MODEL>(L, p.lut, m, s.ph, mat, s.rng, e)) {
-                        ++s.overflows;
+                        atomicAdd(&wt.overflows, 1ull);
                         s.alive = false;
                     } else {
                         do_score = true;
@@ -736,7 +766,7 @@ namespace {
                 }
                 if (run_ray && s.pending == EV_RAYLEIGH) {
                     if (!rayleigh_scatter<MODEL>(L, p.lut, m, s.ph, mat, s.rng)) {
-                        ++s.overflows;
+                        atomicAdd(&wt.overflows, 1ull);
                         s.alive = false;
                     }
                 }
@@ -764,42 +794,48 @@ namespace {
             // history and report it through the overflow counter
             do_score = false;
             s.alive = false;
-            ++s.overflows;
+            atomicAdd(&wt.overflows, 1ull);
         }
         // ---- scoring; the warp is converged here ----------------------------------------
+        const unsigned scoring = __ballot_sync(FULL_MASK, do_score);
         if (p.tally_mode == 2) {
-            const unsigned scoring = __ballot_sync(FULL_MASK, do_score);
             if (do_score)
                 score_aggregated(p, scoring, s.vidx, deposit);
         } else if (do_score) {
             score(p, s.vidx, deposit);
         }
-        if (do_score)
-            ++s.deposits;
+        if ((threadIdx.x & 31) == 0)
+            wt.deposits += __popc(scoring);
     }
 
-    // Adds the warp's lane counters to a job's counters and clears them.
-    __device__ __forceinline__ void flush_counters(Lane& s, JobCounters* c)
+    // Counts the steps of the photons a warp's lanes finished (before they are
+    // refilled or at a flush).  Called by all 32 lanes.
+    __device__ __forceinline__ void count_steps(Lane& s, WarpTally& wt, bool finished)
     {
-        s.steps += s.hist_steps; // counted once: the photon's steps so far
-        s.hist_steps = 0;
-        unsigned long long v[4] = { s.steps, s.deposits, s.overflows, s.histories };
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1)
-                v[k] += __shfl_down_sync(FULL_MASK, v[k], off);
+        const unsigned n = __reduce_add_sync(FULL_MASK, finished ? s.hist_steps : 0u);
+        if ((threadIdx.x & 31) == 0)
+            wt.steps += n;
+        if (finished)
+            s.hist_steps = 0;
+    }
+
+    // Adds the warp's counters to a job's counters and clears them.  Called by all 32 lanes.
+    __device__ __forceinline__ void flush_counters(Lane& s, WarpTally& wt, JobCounters* c)
+    {
+        count_steps(s, wt, true); // counted once: the photons' steps so far
+        __syncwarp();
         if ((threadIdx.x & 31) == 0) {
-            if (v[0])
-                atomicAdd(&c->steps, v[0]);
-            if (v[1])
-                atomicAdd(&c->deposits, v[1]);
-            if (v[2])
-                atomicAdd(&c->overflows, v[2]);
-            if (v[3])
-                atomicAdd(&c->histories_done, v[3]);
+            if (wt.steps)
+                atomicAdd(&c->steps, wt.steps);
+            if (wt.deposits)
+                atomicAdd(&c->deposits, wt.deposits);
+            if (wt.overflows)
+                atomicAdd(&c->overflows, wt.overflows);
+            if (wt.histories)
+                atomicAdd(&c->histories_done, wt.histories);
+            wt = WarpTally {};
         }
-        s.reset_counters();
+        __syncwarp();
     }
 
     // ---- single-job transport kernel ----------------------------------------------------
@@ -842,9 +878,13 @@ namespace {
         const unsigned long long source_total = use_queue ? p.counters->queue_count : p.total_histories;
         unsigned long long* source_head = use_queue ? &p.counters->next_photon : &p.counters->next_history;
 
+        __shared__ WarpTally tallies[1024 / 32];
+        WarpTally& wt = tallies[threadIdx.x >> 5];
+        if (lane == 0)
+            wt = WarpTally {};
+        __syncwarp();
         Lane s {};
         s.alive = false;
-        s.reset_counters();
         // warp-uniform pool of ids (queue slots or history ids) [pool_next, pool_end)
         uint64_t pool_next = 0, pool_end = 0;
         bool exhausted = false;
@@ -873,6 +913,9 @@ namespace {
                     const unsigned rank = __popc(need & lanemask_lt);
                     const bool mine = ((need >> lane) & 1u) && rank < avail;
                     const unsigned taken = __ballot_sync(FULL_MASK, mine);
+                    count_steps(s, wt, mine);
+                    if (lane == 0 && !use_queue)
+                        wt.histories += __popc(taken);
                     if (mine) {
                         if (use_queue) {
                             take_queued(s, p.queue, pool_next + rank);
@@ -885,9 +928,9 @@ namespace {
             }
             if (exhausted && __ballot_sync(FULL_MASK, s.alive) == 0u)
                 break;
-            advance<MODEL, PALETTE>(s, p, L, pal, exhausted, interact_t);
+            advance<MODEL, PALETTE>(s, wt, p, L, pal, exhausted, interact_t);
         }
-        flush_counters(s, p.counters);
+        flush_counters(s, wt, p.counters);
     }
 
     // ---- batched transport kernel ------------------------------------------------------
@@ -918,9 +961,13 @@ namespace {
         const int regen_t = ctl->regen_threshold;
         const int interact_t = ctl->interact_threshold;
 
+        __shared__ WarpTally tallies[BATCH_WARPS];
+        WarpTally& wt = tallies[warp];
+        if (lane == 0)
+            wt = WarpTally {};
+        __syncwarp();
         Lane s {};
         s.alive = false;
-        s.reset_counters();
         int job = -1;
         uint64_t pool_next = 0, pool_end = 0;
         BatchItem next {};
@@ -950,7 +997,7 @@ namespace {
                             if (__ballot_sync(FULL_MASK, s.alive) != 0u)
                                 break;
                             if (job >= 0)
-                                flush_counters(s, p.counters);
+                                flush_counters(s, wt, p.counters);
                             job = static_cast<int>(next.job);
                             __syncwarp();
                             const int* src = reinterpret_cast<const int*>(b.jobs + job);
@@ -971,6 +1018,9 @@ namespace {
                     const unsigned rank = __popc(need & lanemask_lt);
                     const bool mine = ((need >> lane) & 1u) && rank < avail;
                     const unsigned taken = __ballot_sync(FULL_MASK, mine);
+                    count_steps(s, wt, mine);
+                    if (lane == 0)
+                        wt.histories += __popc(taken);
                     if (mine)
                         take_history(s, p, pool_next + rank);
                     pool_next += __popc(taken);
@@ -983,12 +1033,12 @@ namespace {
             if (live2 == 0u)
                 continue; // waiting to switch jobs with nothing in flight: refill again
             if (p.world.palette_index)
-                advance<MODEL, true>(s, p, p.lut, pal, exhausted || have_next, interact_t);
+                advance<MODEL, true>(s, wt, p, p.lut, pal, exhausted || have_next, interact_t);
             else
-                advance<MODEL, false>(s, p, p.lut, pal, exhausted || have_next, interact_t);
+                advance<MODEL, false>(s, wt, p, p.lut, pal, exhausted || have_next, interact_t);
         }
         if (job >= 0)
-            flush_counters(s, p.counters);
+            flush_counters(s, wt, p.counters);
     }
 
     // ---- photon generation pass ---------------------------------------------------------

@@ -246,10 +246,13 @@ void dxmc_gpu_world_free(dxmc_world* world);
 int dxmc_gpu_world_prepare(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut);
 /* Reads back a built local-majorant grid: cells per axis, log2 of the cell size
  * in voxels per axis, the number of energy bands, the band edges (keV, bands - 1
- * values; may be NULL) and, if cells is not NULL, (1 / scale, R mm) per cell and
- * band, band fastest, then x, y, z.  DXMC_ERR_STATE if the pair has no grid. */
+ * values; may be NULL), the box of the cells above their band's emptiest level
+ * (lo[3], hi[3] in mm from the grid corner's frame; may be NULL) and, if cells
+ * is not NULL, (1 / scale, R mm) per cell and band, band fastest, then x, y, z;
+ * R < 0 marks a cell outside that box (safe length |R|, or up to the box along
+ * the ray).  DXMC_ERR_STATE if the pair has no grid. */
 int dxmc_gpu_world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut, uint32_t* cells_per_axis,
-    int32_t* shift, int32_t* bands, float* band_edges, float* cells);
+    int32_t* shift, int32_t* bands, float* band_edges, float* box, float* cells);
 
 /* ---- LUT on the device --------------------------------------------------- */
 int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* blob, dxmc_lut** out);

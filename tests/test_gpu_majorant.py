@@ -46,8 +46,8 @@ def test_majorant_grid_bounds_attenuation(gpu_ctx):
     dworld = dx.DeviceWorld(gpu_ctx, world)
     dlut = dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, 120.0))
     dworld.prepare(dlut)
-    shift, edges, cells = dworld.majorant(dlut)
-    assert cells.shape[3] == 4 and len(edges) == 3 and np.all(np.diff(edges) > 0)
+    shift, edges, box, cells = dworld.majorant(dlut)
+    assert cells.shape[3] == len(edges) + 1 >= 4 and np.all(np.diff(edges) > 0)
     blob = dx.LutBlob.from_world(world, 120.0)
     bounds = [1.0, *edges, 120.0]
     sp = np.array(world.spacing())[::-1]  # (z, y, x) mm
@@ -56,7 +56,20 @@ def test_majorant_grid_bounds_attenuation(gpu_ctx):
     for band in range(cells.shape[3]):
         scale = _voxel_scales(world, blob, bounds[band] * 1.0001, bounds[band + 1] * 0.9999)
         s_cell = 1.0 / cells[..., band, 0].astype(np.float64)
-        R_cell = cells[..., band, 1].astype(np.float64)
+        R_signed = cells[..., band, 1].astype(np.float64)
+        R_cell = np.abs(R_signed)
+        # cells marked outside the box (R < 0) may fly to the box along their ray: every
+        # voxel outside the box must then lie within the majorant of every marked cell
+        d = world.dimensions()
+        zc, yc, xc = np.meshgrid(*[(np.arange(d[i]) + 0.5) * world.spacing()[i] for i in (2, 1, 0)], indexing="ij")
+        lower = [-0.5 * d[i] * world.spacing()[i] + world.origin()[i] for i in range(3)]
+        pos = [xc + lower[0], yc + lower[1], zc + lower[2]]
+        out_box = np.zeros(scale.shape, bool)
+        for a in range(3):
+            out_box |= (pos[a] < box[a]) | (pos[a] > box[3 + a])
+        marked = R_signed < 0
+        assert marked.any() and (~marked).any()
+        assert scale[out_box].max() <= s_cell[marked].min() * (1.0 + 1e-4), (band, scale[out_box].max(), s_cell[marked].min())
         assert np.all(s_cell <= 1.0 + 1e-6)
         # the grid is worth having: air cells far from the body get small scales and long flights
         assert (s_cell < 0.01).mean() > 0.05, np.unique(s_cell)
@@ -128,12 +141,12 @@ def test_forced_scoring_keeps_global_majorant(gpu_ctx):
     dworld = dx.DeviceWorld(gpu_ctx, world)
     dlut = dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, src.maxPhotonEnergyProduced()))
     dworld.prepare(dlut)
-    shift, _, cells = dworld.majorant(dlut)
+    shift, _, _, cells = dworld.majorant(dlut)
     b = [1 << int(shift[2]), 1 << int(shift[1]), 1 << int(shift[0])]
     # cells holding a measurement voxel track with the global majorant in every band
     m = np.pad(meas, [(0, (-meas.shape[i]) % b[i]) for i in range(3)])
     mc = m.reshape(m.shape[0] // b[0], b[0], m.shape[1] // b[1], b[1], m.shape[2] // b[2], b[2]).max(axis=(1, 3, 5))
-    assert np.all(cells[mc > 0][..., 0] == 1.0) and np.all(np.isinf(cells[mc > 0][..., 1]))
+    assert np.all(cells[mc > 0][..., 0] == 1.0) and np.all(np.isposinf(cells[mc > 0][..., 1]))
     ex = src.exposures(world.directionCosines())
     runs = []
     for seed, mode in ((21, A.TRACKING_GLOBAL), (22, A.TRACKING_GLOBAL), (23, A.TRACKING_LOCAL)):
