@@ -627,19 +627,21 @@ namespace {
                 s.ph.px = fmaf(s.ph.dx, step, s.ph.px);
                 s.ph.py = fmaf(s.ph.dy, step, s.ph.py);
                 s.ph.pz = fmaf(s.ph.dz, step, s.ph.pz);
-                // grid coordinates (p - lo) / spacing as one FMA each; the photon is inside
-                // while all three lie in [0, dims), which also bounds the voxel index
-                const float fx = fmaf(s.ph.px, w.inv_spacing[0], -w.lo_inv[0]);
-                const float fy = fmaf(s.ph.py, w.inv_spacing[1], -w.lo_inv[1]);
-                const float fz = fmaf(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2]);
-                if (!(fx >= 0.0f && fx < w.dims_f[0] && fy >= 0.0f && fy < w.dims_f[1] && fz >= 0.0f && fz < w.dims_f[2])) {
+                // grid coordinates (p - lo) / spacing as one FMA each, rounded down; the photon
+                // is inside while all three lie in [0, dims) (one unsigned compare each: a
+                // negative or saturated conversion falls outside), which bounds the voxel index
+                const int jx = __float2int_rd(fmaf(s.ph.px, w.inv_spacing[0], -w.lo_inv[0]));
+                const int jy = __float2int_rd(fmaf(s.ph.py, w.inv_spacing[1], -w.lo_inv[1]));
+                const int jz = __float2int_rd(fmaf(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2]));
+                if (!(static_cast<uint32_t>(jx) < w.dims[0] && static_cast<uint32_t>(jy) < w.dims[1]
+                        && static_cast<uint32_t>(jz) < w.dims[2])) {
                     s.alive = false;
                     break;
                 }
                 ++s.hist_steps;
-                const uint32_t ix = static_cast<uint32_t>(fx);
-                const uint32_t iy = static_cast<uint32_t>(fy);
-                const uint32_t iz = static_cast<uint32_t>(fz);
+                const uint32_t ix = static_cast<uint32_t>(jx);
+                const uint32_t iy = static_cast<uint32_t>(jy);
+                const uint32_t iz = static_cast<uint32_t>(jz);
                 const float cinv = s.cinv; // the majorant this flight was drawn with
                 if (p.majorant.cells) {
                     const MajorantGrid& g = p.majorant;

@@ -95,14 +95,16 @@ def test_majorant_grid_bounds_attenuation(gpu_ctx):
     dworld.close()
 
 
-@pytest.mark.parametrize("model", [1, 2])
-def test_local_tracking_matches_global(gpu_ctx, model):
+@pytest.mark.parametrize("model,layout", [(1, 0), (2, 0), (1, 1)])
+def test_local_tracking_matches_global(gpu_ctx, model, layout):
+    """Both tracking modes on the compact (palette) and the 8-byte voxel layout;
+    the 8-byte layout has no body box (its levels are not known on the host)."""
     import dxmclib_gb300 as dx
     from dxmclib_gb300 import _capi as A
     from dxmclib_gb300.workloads import ct_source
     world = _phantom()
     src = ct_source(world, 4_000_000)
-    dworld = dx.DeviceWorld(gpu_ctx, world)
+    dworld = dx.DeviceWorld(gpu_ctx, world, layout=layout)
     dlut = dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, src.maxPhotonEnergyProduced()))
     ex = src.exposures(world.directionCosines())
     out = {}
@@ -115,7 +117,7 @@ def test_local_tracking_matches_global(gpu_ctx, model):
     dl, vl, _, sl = out[A.TRACKING_LOCAL]
     assert sg["histories"] == sl["histories"]
     ref = dict(idx=np.arange(dg.size), dose=dg, var=vg, total=np.array([dg.sum()]))
-    assert_parity(compare_sparse(ref, dl, vl), f"local vs global tracking, model {model}")
+    assert_parity(compare_sparse(ref, dl, vl), f"local vs global tracking, model {model}, layout {layout}")
     # the same process with fewer steps
     assert sl["steps"] < 0.75 * sg["steps"], (sl["steps"], sg["steps"])
     dlut.close()
