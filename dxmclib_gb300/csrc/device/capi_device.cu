@@ -157,6 +157,22 @@ int cuda_fail(dxmc_gpu_ctx* ctx, cudaError_t e, const char* what)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// The device address of a page-locked host buffer (cudaHostAlloc or
+// cudaHostRegister), if it is one; false for pageable or device memory.
+template <typename T>
+bool mapped_host(T* ptr, T*& device_ptr)
+{
+    cudaPointerAttributes a {};
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer)
+        return false;
+    device_ptr = static_cast<T*>(a.devicePointer);
+    return true;
+}
+
 // Per energy band and material m, the largest ratio of m's attenuation (per
 // g/cm3) to the global majorant over the band's energies, from the float image
 // the kernels read.  Photons are tracked from 1 keV (the transport cutoff) to
@@ -2015,7 +2031,24 @@ int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double
         if (!j->tally && !j->tally_f32)
             return fail(ctx, DXMC_ERR_STATE, "job results were already released");
         DXMC_CUDA(ctx, cudaMemcpyAsync(hc, j->counters, sizeof(dev::JobCounters), cudaMemcpyDeviceToHost, s));
-        if (!j->cancelled && (dose || variance)) {
+        // page-locked output buffers are written by the post-processing kernel through
+        // their device mapping (one pass over the link, no staging buffer or copies)
+        double* m_dose = nullptr;
+        double* m_var = nullptr;
+        uint32_t* m_events = nullptr;
+        const bool mapped = !j->cancelled && (dose || variance || n_events) && (!dose || mapped_host(dose, m_dose))
+            && (!variance || mapped_host(variance, m_var)) && (!n_events || mapped_host(n_events, m_events));
+        if (mapped) {
+            const double vv = j->world->spacing[0] * j->world->spacing[1] * j->world->spacing[2] / 1000.0;
+            const cudaError_t e = j->tally_mode == 1
+                ? dev::launch_postprocess_f32(j->tally_f32, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv,
+                      calibration, m_dose, m_var, j->n_events, m_events, s)
+                : dev::launch_postprocess(j->tally, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv,
+                      calibration, m_dose, m_var, j->n_events, m_events, s);
+            if (e != cudaSuccess)
+                return cuda_fail(ctx, e, "result post-processing");
+        }
+        if (!mapped && !j->cancelled && (dose || variance)) {
             double* d_out = nullptr;
             const uint64_t out_elems = (dose ? nv : 0) + (variance ? nv : 0);
             DXMC_CUDA(ctx, cudaMallocAsync(&d_out, out_elems * sizeof(double), s));
@@ -2024,9 +2057,9 @@ int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double
             const double vv = j->world->spacing[0] * j->world->spacing[1] * j->world->spacing[2] / 1000.0;
             cudaError_t e;
             if (j->tally_mode == 1)
-                e = dev::launch_postprocess_f32(j->tally_f32, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, s);
+                e = dev::launch_postprocess_f32(j->tally_f32, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, nullptr, nullptr, s);
             else
-                e = dev::launch_postprocess(j->tally, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, s);
+                e = dev::launch_postprocess(j->tally, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, nullptr, nullptr, s);
             if (e == cudaSuccess && dose)
                 e = cudaMemcpyAsync(dose, d_dose, nv * sizeof(double), cudaMemcpyDeviceToHost, s);
             if (e == cudaSuccess && variance)
@@ -2035,7 +2068,7 @@ int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double
             if (e != cudaSuccess)
                 return cuda_fail(ctx, e, "result post-processing");
         }
-        if (!j->cancelled && n_events)
+        if (!mapped && !j->cancelled && n_events)
             DXMC_CUDA(ctx, cudaMemcpyAsync(n_events, j->n_events, nv * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         DXMC_CUDA(ctx, cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
         const cudaError_t e = cudaEventRecord(done, s);

@@ -156,10 +156,14 @@ int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem)
 // dynamic shared memory the transport kernel needs for a LUT image of lut_bytes
 size_t transport_smem_bytes(size_t lut_bytes, bool lut_in_smem, bool palette);
 // Post-processing of the tallies into dose / variance (densities from the world's layout).
+// dose, variance and counts_out may be device memory or page-locked host memory
+// (written through its device mapping); counts_out, if not null, gets a copy of counts.
 cudaError_t launch_postprocess(const double* tally, const WorldParams& w, uint64_t n,
-    int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream);
+    int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance,
+    const uint32_t* counts, uint32_t* counts_out, cudaStream_t stream);
 cudaError_t launch_postprocess_f32(const float* tally, const WorldParams& w, uint64_t n,
-    int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream);
+    int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance,
+    const uint32_t* counts, uint32_t* counts_out, cudaStream_t stream);
 // Radiological path of n rays (Siddon traversal): rays are 7 floats each
 // (origin mm, direction, energy keV); out[i] = sum of mu * density * length (cm).
 cudaError_t launch_radiological_path(const WorldParams& w, const float* lut, LutMeta meta, const float* rays, uint64_t n,

@@ -1093,7 +1093,8 @@ namespace {
     template <typename TallyT>
     __global__ void postprocess_kernel(const TallyT* __restrict__ tally, const Voxel* __restrict__ voxels,
         const uint8_t* __restrict__ palette_index, const PaletteEntry* __restrict__ palette, uint64_t n, int mode,
-        double histories, double voxel_volume_cm3, double calibration, double* __restrict__ dose, double* __restrict__ variance)
+        double histories, double voxel_volume_cm3, double calibration, double* __restrict__ dose, double* __restrict__ variance,
+        const uint32_t* __restrict__ counts, uint32_t* __restrict__ counts_out)
     {
         const double h_inv = 1.0 / (histories - 1.0);
         const double h_d = 1.0e3 / histories;
@@ -1116,6 +1117,8 @@ namespace {
                 dose[i] = d;
             if (variance)
                 variance[i] = v;
+            if (counts_out)
+                counts_out[i] = __ldg(counts + i);
         }
     }
 
@@ -1257,22 +1260,24 @@ int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem)
 }
 
 cudaError_t launch_postprocess(const double* tally, const WorldParams& w, uint64_t n, int mode, double histories,
-    double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream)
+    double voxel_volume_cm3, double calibration, double* dose, double* variance, const uint32_t* counts, uint32_t* counts_out,
+    cudaStream_t stream)
 {
     const int block = 256;
     const int grid = static_cast<int>(std::min<uint64_t>((n + block - 1) / block, 152ull * 16));
     postprocess_kernel<double><<<grid, block, 0, stream>>>(tally, w.palette_index ? nullptr : w.voxels, w.palette_index, w.palette, n, mode,
-        histories, voxel_volume_cm3, calibration, dose, variance);
+        histories, voxel_volume_cm3, calibration, dose, variance, counts, counts_out);
     return cudaGetLastError();
 }
 
 cudaError_t launch_postprocess_f32(const float* tally, const WorldParams& w, uint64_t n, int mode, double histories,
-    double voxel_volume_cm3, double calibration, double* dose, double* variance, cudaStream_t stream)
+    double voxel_volume_cm3, double calibration, double* dose, double* variance, const uint32_t* counts, uint32_t* counts_out,
+    cudaStream_t stream)
 {
     const int block = 256;
     const int grid = static_cast<int>(std::min<uint64_t>((n + block - 1) / block, 152ull * 16));
     postprocess_kernel<float><<<grid, block, 0, stream>>>(tally, w.palette_index ? nullptr : w.voxels, w.palette_index, w.palette, n, mode,
-        histories, voxel_volume_cm3, calibration, dose, variance);
+        histories, voxel_volume_cm3, calibration, dose, variance, counts, counts_out);
     return cudaGetLastError();
 }
 
