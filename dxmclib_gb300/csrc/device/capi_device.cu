@@ -1102,6 +1102,8 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
         return fail(ctx, DXMC_ERR_INVALID, "unknown tally mode");
     if (jd->tracking < DXMC_TRACKING_DEFAULT || jd->tracking > DXMC_TRACKING_LOCAL)
         return fail(ctx, DXMC_ERR_INVALID, "unknown tracking mode");
+    if (jd->direction != DXMC_DIRECTION_REFERENCE && jd->direction != DXMC_DIRECTION_NORMALIZED)
+        return fail(ctx, DXMC_ERR_INVALID, "unknown direction mode");
 
     // ---- host-side tables: exposures, prefix offsets, spectrum, heel, bow-tie ----
     const uint64_t ne = jd->n_exposures;
@@ -1328,6 +1330,7 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     }
     if (grid)
         p.majorant = *grid;
+    p.normalize_direction = jd->direction == DXMC_DIRECTION_NORMALIZED ? 1 : 0;
 
 
     chunk_out = chunk;

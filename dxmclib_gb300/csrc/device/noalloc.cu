@@ -263,6 +263,8 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         return reject(ctx, "dxmc_gpu_transport_noalloc: " + std::to_string(bowtie_n) + " bow-tie points exceed the maximum of " + std::to_string(NOALLOC_MAX_BOWTIE));
     if (jd->tracking < DXMC_TRACKING_DEFAULT || jd->tracking > DXMC_TRACKING_LOCAL)
         return reject(ctx, "dxmc_gpu_transport_noalloc: unknown tracking mode");
+    if (jd->direction != DXMC_DIRECTION_REFERENCE && jd->direction != DXMC_DIRECTION_NORMALIZED)
+        return reject(ctx, "dxmc_gpu_transport_noalloc: unknown direction mode");
     if (jd->model < 0 || jd->model > 2)
         return reject(ctx, "unknown low-energy correction model");
     if (meta.n_materials < world_materials)
@@ -344,6 +346,7 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         const dev::MajorantGrid* g = capi::built_majorant(ctx, world, lut, jd);
         if (g)
             p.majorant = *g;
+        p.normalize_direction = jd->direction == DXMC_DIRECTION_NORMALIZED ? 1 : 0;
         p.regen_threshold = capi::ctx_regen_threshold(ctx, g != nullptr);
         p.interact_threshold = capi::ctx_interact_threshold(ctx);
         p.woodcock_burst = jd->woodcock_burst > 0 ? std::min(jd->woodcock_burst, 64) : capi::default_woodcock_burst(g != nullptr);

@@ -186,8 +186,12 @@ __device__ __forceinline__ void rotate(float& vx, float& vy, float& vz, float ax
 
 // vectormath::peturb (vectormath.hpp:197-221), including its quirk: the
 // orthogonal axis cross(vec, e_k) is never normalised, so |dir| shrinks after
-// every direction change exactly as in the reference.  Takes cos(theta).
-__device__ __forceinline__ void peturb(float& vx, float& vy, float& vz, float cos_theta, float phi)
+// every direction change exactly as in the reference (and the angle between the
+// old and new direction is not theta).  normalize = true scales the axis to unit
+// length first: a unit direction then turns by exactly theta and stays a unit
+// vector (the normalised physics mode; it does not match the reference).  Takes
+// cos(theta).
+__device__ __forceinline__ void peturb(float& vx, float& vy, float& vz, float cos_theta, float phi, bool normalize = false)
 {
     const float ax = fabsf(vx), ay = fabsf(vy), az = fabsf(vz);
     const int k = ax <= ay ? (ax <= az ? 0 : 2) : (ay <= az ? 1 : 2);
@@ -205,6 +209,12 @@ __device__ __forceinline__ void peturb(float& vx, float& vy, float& vz, float co
         ux = vy;
         uy = -vx;
         uz = 0.0f;
+    }
+    if (normalize) {
+        const float inv = rsqrtf(ux * ux + uy * uy + uz * uz);
+        ux *= inv;
+        uy *= inv;
+        uz *= inv;
     }
     rotate(ux, uy, uz, vx, vy, vz, phi);
     const float st = sqrtf(fmaxf(0.0f, 1.0f - cos_theta * cos_theta));

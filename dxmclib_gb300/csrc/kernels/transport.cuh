@@ -114,7 +114,7 @@ struct TransportParams {
     int regen_threshold;    // refill finished lanes once at least this many are idle (1..32)
     int interact_threshold; // run the interaction passes once at least this many lanes wait (1..32)
     int woodcock_burst;     // Woodcock steps a lane may take per loop iteration (1..64)
-    int pad_params;
+    int normalize_direction; // 1: unit scattering axis in peturb (normalised physics), 0: the reference's
     MajorantGrid majorant;
 };
 

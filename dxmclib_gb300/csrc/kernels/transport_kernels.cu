@@ -72,7 +72,7 @@ namespace {
 
     // ---- photoelectric (transport.hpp:216-263) ---------------------------------
     template <int MODEL>
-    __device__ __forceinline__ float photo_absorption(const float* L, const LutMeta& m, Photon& ph, int material, Rng& rng)
+    __device__ __forceinline__ float photo_absorption(const float* L, const LutMeta& m, Photon& ph, int material, Rng& rng, bool norm = false)
     {
         const float E = ph.energy;
         ph.energy = 0.0f;
@@ -108,7 +108,7 @@ namespace {
                 ph.energy = sh[8 + line];
                 const float theta = rng.uniform() * PI_F;
                 const float phi = rng.azimuth();
-                peturb(ph.dx, ph.dy, ph.dz, cosf(theta), phi);
+                peturb(ph.dx, ph.dy, ph.dz, cosf(theta), phi, norm);
                 return E - ph.energy;
             }
             return E;
@@ -117,7 +117,7 @@ namespace {
 
     // ---- Rayleigh (transport.hpp:264-298) ---------------------------------------
     template <int MODEL>
-    __device__ __forceinline__ bool rayleigh_scatter(const float* L, const float* G, const LutMeta& m, Photon& ph, int material, Rng& rng)
+    __device__ __forceinline__ bool rayleigh_scatter(const float* L, const float* G, const LutMeta& m, Photon& ph, int material, Rng& rng, bool norm = false)
     {
         if constexpr (MODEL == 0) {
             constexpr float extreme = 1.08866210790363f; // 4 sqrt(2) / (3 sqrt(3))
@@ -128,7 +128,7 @@ namespace {
                 sincosf(theta, &s, &c);
                 if (!(r1 > (2.0f - s * s) * s)) {
                     const float phi = rng.azimuth();
-                    peturb(ph.dx, ph.dy, ph.dz, c, phi);
+                    peturb(ph.dx, ph.dy, ph.dz, c, phi, norm);
                     return true;
                 }
             }
@@ -141,13 +141,13 @@ namespace {
             const float y = table_quantile(G + m.off_ray + (material * m.tab_ne + row) * (m.tab_nu + 1), m.tab_nu, rng.uniform(), fe);
             const float cosA = 1.0f - 2.0f * y; // q^2 / q_max^2 = (1 - cos) / 2
             const float phi = rng.azimuth();
-            peturb(ph.dx, ph.dy, ph.dz, cosA, phi);
+            peturb(ph.dx, ph.dy, ph.dz, cosA, phi, norm);
             return true;
         }
     }
 
     // ---- Compton, impulse approximation (transport.hpp:342-483) -----------------
-    __device__ __forceinline__ bool compton_ia(const float* L, const LutMeta& m, Photon& ph, int material, Rng& rng, float& deposit)
+    __device__ __forceinline__ bool compton_ia(const float* L, const LutMeta& m, Photon& ph, int material, Rng& rng, float& deposit, bool norm = false)
     {
         const float* shells = L + m.off_shells + material * N_SHELLS * SHELL_FLOATS;
         float total = 0.0f;
@@ -257,7 +257,7 @@ namespace {
         if (!accepted)
             return false;
         const float phi = rng.azimuth();
-        peturb(ph.dx, ph.dy, ph.dz, cosA, phi);
+        peturb(ph.dx, ph.dy, ph.dz, cosA, phi, norm);
         const float E = ph.energy;
         ph.energy *= e;
         deposit = E - ph.energy;
@@ -266,10 +266,10 @@ namespace {
 
     // ---- Compton, Klein-Nishina with optional scatter factor (transport.hpp:300-340)
     template <int MODEL>
-    __device__ __forceinline__ bool compton_scatter(const float* L, const float* G, const LutMeta& m, Photon& ph, int material, Rng& rng, float& deposit)
+    __device__ __forceinline__ bool compton_scatter(const float* L, const float* G, const LutMeta& m, Photon& ph, int material, Rng& rng, float& deposit, bool norm = false)
     {
         if constexpr (MODEL == 2) {
-            return compton_ia(L, m, ph, material, rng, deposit);
+            return compton_ia(L, m, ph, material, rng, deposit, norm);
         } else {
             // the density of the reference's Klein-Nishina rejection (times the scatter
             // factor S(q) for LIVERMORE), drawn by inverse CDF: no loop, no divergence
@@ -285,7 +285,7 @@ namespace {
             const float e = 1.0f - one_minus_e;
             const float cosA = 1.0f - one_minus_e / (k * e);
             const float phi = rng.azimuth();
-            peturb(ph.dx, ph.dy, ph.dz, fmaxf(cosA, -1.0f), phi);
+            peturb(ph.dx, ph.dy, ph.dz, fmaxf(cosA, -1.0f), phi, norm);
             ph.energy = E * e;
             deposit = E - ph.energy;
             return true;
@@ -696,7 +696,7 @@ namespace {
                     s.forced_wc = eventProb * photoProb;
                     {
                         Photon forced = s.ph;
-                        const float ef = photo_absorption<MODEL>(L, m, forced, mat, s.rng);
+                        const float ef = photo_absorption<MODEL>(L, m, forced, mat, s.rng, p.normalize_direction);
                         deposit = (forced.energy < ENERGY_CUTOFF ? (ef + forced.energy) : ef) * forced.weight * s.forced_wc;
                         do_score = true;
                     }
@@ -738,7 +738,7 @@ namespace {
             if ((waiting_other && (__popc(waiting_other) >= interact_t || stuck)) || run_ray) {
                 const int mat = s.cached_mat;
                 if (__any_sync(FULL_MASK, s.pending == EV_PHOTO) && s.pending == EV_PHOTO) {
-                    const float e = photo_absorption<MODEL>(L, m, s.ph, mat, s.rng);
+                    const float e = photo_absorption<MODEL>(L, m, s.ph, mat, s.rng, p.normalize_direction);
                     do_score = true;
                     if (s.ph.energy < ENERGY_CUTOFF) {
                         deposit = (e + s.ph.energy) * s.ph.weight;
@@ -751,7 +751,7 @@ namespace {
                 }
                 if (__any_sync(FULL_MASK, s.pending == EV_COMPTON) && s.pending == EV_COMPTON) {
                     float e = 0.0f;
-                    if (!compton_scatter<MODEL>(L, p.lut, m, s.ph, mat, s.rng, e)) {
+                    if (!compton_scatter<MODEL>(L, p.lut, m, s.ph, mat, s.rng, e, p.normalize_direction)) {
                         atomicAdd(&wt.overflows, 1ull);
                         s.alive = false;
                     } else {
@@ -767,7 +767,7 @@ namespace {
                     }
                 }
                 if (run_ray && s.pending == EV_RAYLEIGH) {
-                    if (!rayleigh_scatter<MODEL>(L, p.lut, m, s.ph, mat, s.rng)) {
+                    if (!rayleigh_scatter<MODEL>(L, p.lut, m, s.ph, mat, s.rng, p.normalize_direction)) {
                         atomicAdd(&wt.overflows, 1ull);
                         s.alive = false;
                     }

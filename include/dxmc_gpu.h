@@ -68,6 +68,13 @@ enum {
     DXMC_TRACKING_LOCAL = 2
 };
 
+/* Direction changes.  REFERENCE keeps vectormath::peturb's unnormalised
+ * orthogonal axis (vectormath.hpp:197-221): |dir| shrinks after each scatter and
+ * the turn is not exactly the sampled angle, as in the reference.  NORMALIZED
+ * scales the axis to unit length (directions stay unit vectors and turn by the
+ * sampled angle); its results do not match the reference's. */
+enum { DXMC_DIRECTION_REFERENCE = 0, DXMC_DIRECTION_NORMALIZED = 1 };
+
 /* ---- physics data for the host LUT build -------------------------------- */
 /* One electron shell, mirrors dxmc::ElectronShellConfiguration (material.hpp:29-58). */
 typedef struct dxmc_shell_config {
@@ -276,7 +283,7 @@ typedef struct dxmc_job_desc {
     int32_t woodcock_burst;             /* Woodcock steps a lane may take per loop iteration (1..64) */
     int32_t block_size;                 /* threads per block of the transport kernel: 128 or 256 */
     int32_t tracking;                   /* DXMC_TRACKING_*; 0 = the context's */
-    int32_t pad;
+    int32_t direction;                  /* DXMC_DIRECTION_* */
 } dxmc_job_desc;
 
 typedef struct dxmc_job_stats {

@@ -51,6 +51,8 @@ def lib():
     if _lib is None:
         build()
         _lib = C.CDLL(str(LIB))
+        _lib.oracle_port_set_direction.argtypes = [C.c_int]
+        _lib.oracle_port_set_direction.restype = None
         _lib.oracle_port_transport.restype = C.c_double
         _lib.oracle_port_transport.argtypes = [C.POINTER(PortLut), C.POINTER(PortWorld), C.POINTER(PortSource), C.c_int,
                                                C.c_int, C.c_uint64, DP, DP, C.POINTER(C.c_uint32),
@@ -63,8 +65,10 @@ def _d(a):
 
 
 def transport(lut_info: dict, dims, spacing, density, material, exposures19, model: int = 1, n_threads: int = 0,
-              seed: int = 1, spectrum=None, heel=None, bowtie=None, measurement=None, origin=(0, 0, 0)):
-    """Runs the CPU restatement; returns (energy, energy^2, nEvents, seconds, steps) raw tallies."""
+              seed: int = 1, spectrum=None, heel=None, bowtie=None, measurement=None, origin=(0, 0, 0),
+              normalized_direction: bool = False):
+    """Runs the CPU restatement; returns (energy, energy^2, nEvents, seconds, steps) raw tallies.
+    normalized_direction selects the normalised physics mode (unit scattering axis)."""
     keep = []
     L = PortLut()
     x = np.ascontiguousarray(lut_info["x"], np.float64)
@@ -120,6 +124,7 @@ def transport(lut_info: dict, dims, spacing, density, material, exposures19, mod
     e2 = np.zeros(n)
     nev = np.zeros(n, np.uint32)
     steps = C.c_uint64(0)
+    lib().oracle_port_set_direction(1 if normalized_direction else 0)
     secs = lib().oracle_port_transport(C.byref(L), C.byref(W), C.byref(S), int(model), int(n_threads), int(seed),
                                        _d(e), _d(e2), nev.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(steps))
     return e, e2, nev, secs, steps.value

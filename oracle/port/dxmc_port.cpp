@@ -88,7 +88,13 @@ void rotate(double v[3], const double a[3], double angle)
     v[2] = o[2];
 }
 
+// Normalised physics mode (no reference counterpart): the orthogonal axis of
+// peturb is scaled to unit length, so directions stay unit vectors.  Set for a
+// whole run through oracle_port_set_direction.
+bool g_normalize_direction = false;
+
 // vectormath::peturb (vectormath.hpp:197-221), orthogonal axis left unnormalised
+// (or normalised in the normalised physics mode)
 void peturb(double v[3], double theta, double phi)
 {
     const double ax = std::abs(v[0]), ay = std::abs(v[1]), az = std::abs(v[2]);
@@ -96,6 +102,11 @@ void peturb(double v[3], double theta, double phi)
     double e[3] = { 0, 0, 0 };
     e[k] = 1;
     double u[3] = { v[1] * e[2] - v[2] * e[1], v[2] * e[0] - v[0] * e[2], v[0] * e[1] - v[1] * e[0] };
+    if (g_normalize_direction) {
+        const double inv = 1.0 / std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+        for (double& c : u)
+            c *= inv;
+    }
     rotate(u, v, phi);
     const double ts = std::sin(theta), tc = std::cos(theta);
     for (int i = 0; i < 3; ++i)
@@ -650,6 +661,9 @@ struct PortSource {
     const double* bowtie_angles;
     const double* bowtie_weights;
 };
+
+// 0: the reference's peturb; 1: the normalised physics mode (for the next runs).
+void oracle_port_set_direction(int normalized) { g_normalize_direction = normalized != 0; }
 
 // Runs the transport and writes energy imparted (keV) and its squared sum per
 // voxel (raw tallies, the reference's Result before normalizeScoring).
