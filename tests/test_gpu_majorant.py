@@ -172,3 +172,48 @@ def test_forced_scoring_keeps_global_majorant(gpu_ctx):
                   max_chi2=max(1.2, same["chi2"]) * 1.1)
     dlut.close()
     dworld.close()
+
+
+def test_majorant_grids_per_world_are_evicted_and_accounted(gpu_ctx):
+    """A world keeps the grids of up to four LUTs; a fifth LUT evicts the least
+    recently used one (after the context's queued work), jobs on any of them stay
+    correct, and freeing the world returns every grid's bytes to the budget."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    from dxmclib_gb300.workloads import ct_source
+    world = _phantom()
+    src = ct_source(world, 200_000)
+    ex = src.exposures(world.directionCosines())
+    _, before = gpu_ctx.memory()
+    dworld = dx.DeviceWorld(gpu_ctx, world)
+    _, with_world = gpu_ctx.memory()
+    luts = [dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, e)) for e in (120.0, 121.0, 122.0, 123.0, 124.0)]
+    _, with_luts = gpu_ctx.memory()
+    totals = []
+    for i, dlut in enumerate(luts):
+        dworld.prepare(dlut)
+        job = dx.Job(gpu_ctx, dworld, dlut, ex, src.spectrum(), src.heel(), None, seed=5, model=1)
+        d, _, _, st = job.result(A.OUTPUT_RAW, want_events=False)
+        assert st["histories"] == int(np.sum(ex.n_histories)) and d.sum() > 0
+        totals.append(d.sum() / st["histories"])
+        job.close()
+    _, with_grids = gpu_ctx.memory()
+    grid_bytes = (with_grids - with_luts) / 4  # four grids stay
+    assert grid_bytes > 0
+    # the first LUT's grid was evicted: reading it back fails, the last one's succeeds
+    with pytest.raises(A.DxmcError) as e:
+        dworld.majorant(luts[0])
+    assert e.value.status == A.DXMC_ERR_STATE
+    dworld.majorant(luts[-1])
+    # a job on the evicted pair rebuilds its grid
+    job = dx.Job(gpu_ctx, dworld, luts[0], ex, src.spectrum(), src.heel(), None, seed=5, model=1)
+    d, _, _, st = job.result(A.OUTPUT_RAW, want_events=False)
+    job.close()
+    np.testing.assert_allclose(d.sum() / st["histories"], totals[0], rtol=1e-9)  # same seed, same grid
+    dworld.close()
+    _, after_world = gpu_ctx.memory()
+    assert after_world == with_luts - (with_world - before)
+    for dlut in luts:
+        dlut.close()
+    _, after = gpu_ctx.memory()
+    assert after == before
