@@ -916,8 +916,13 @@ namespace {
 // the persistent multi-job kernel) or a buffer shared by the jobs of one batch
 // chain, which run one after another on the chain's stream.
 // ---- local-majorant grids ------------------------------------------------------------
-constexpr int MAJORANT_LEVELS_PER_OCTAVE = 4;
-constexpr int MAJORANT_MAX_LEVEL = 48;            // scale 2^-12: empty and air cells
+#ifndef DXMC_MAJORANT_LEVELS_PER_OCTAVE
+#define DXMC_MAJORANT_LEVELS_PER_OCTAVE 6
+#endif
+constexpr int MAJORANT_LEVELS_PER_OCTAVE = DXMC_MAJORANT_LEVELS_PER_OCTAVE;
+// the emptiest level (air and empty cells): scale 2^-12, or 2^-10.5 at six levels per octave;
+// levels index a 64-bit mask
+constexpr int MAJORANT_MAX_LEVEL = MAJORANT_LEVELS_PER_OCTAVE * 12 < 63 ? MAJORANT_LEVELS_PER_OCTAVE * 12 : 63;
 constexpr uint64_t MAJORANT_MAX_CELLS_PER_AXIS = 1024;
 constexpr size_t MAJORANT_GRIDS_PER_WORLD = 4;    // one per LUT used with the world, least recently used evicted
 
