@@ -60,6 +60,7 @@ struct BatchEngines;
 
 struct dxmc_gpu_ctx {
     BatchEngines* engines = nullptr; // created by the first batch
+    cudaMemPool_t pool = nullptr;    // stream-ordered allocations of this context
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
@@ -156,6 +157,16 @@ int cuda_fail(dxmc_gpu_ctx* ctx, cudaError_t e, const char* what)
     } while (0)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Stream-ordered allocation from the context's own memory pool, which keeps
+// freed memory up to the context's budget instead of returning it to the
+// driver at every synchronisation: a world, a job's 1 GB of tallies or a grid
+// allocated again after a free costs no new mapping.
+template <typename T>
+cudaError_t pool_alloc(dxmc_gpu_ctx* ctx, T** ptr, size_t bytes, cudaStream_t stream)
+{
+    return cudaMallocFromPoolAsync(reinterpret_cast<void**>(ptr), bytes, ctx->pool, stream);
+}
 
 // The device address of a page-locked host buffer (cudaHostAlloc or
 // cudaHostRegister), if it is one; false for pageable or device memory.
@@ -446,6 +457,21 @@ int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out)
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     ctx->budget = ctx->options.memory_budget ? ctx->options.memory_budget : static_cast<uint64_t>(free_b * 0.9);
+    cudaMemPoolProps props {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = ctx->device;
+    uint64_t keep = ctx->budget;
+    if (cudaMemPoolCreate(&ctx->pool, &props) != cudaSuccess
+        || cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+        if (ctx->pool)
+            cudaMemPoolDestroy(ctx->pool);
+        cudaStreamDestroy(ctx->result_stream);
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return DXMC_ERR_DEVICE;
+    }
     *out = ctx;
     return DXMC_OK;
 }
@@ -459,6 +485,7 @@ void dxmc_gpu_ctx_destroy(dxmc_gpu_ctx* ctx)
     release_engines(ctx);
     cudaStreamDestroy(ctx->result_stream);
     cudaStreamDestroy(ctx->stream);
+    cudaMemPoolDestroy(ctx->pool); // memory still held by objects not freed is released with them
     delete ctx;
 }
 
@@ -505,13 +532,13 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     uint8_t* d_material = nullptr;
     uint8_t* d_meas = nullptr;
     unsigned int* d_bad = nullptr;
-    cudaError_t e = cudaMallocAsync(&d_density, n * sizeof(float), ctx->stream);
+    cudaError_t e = pool_alloc(ctx, &d_density, n * sizeof(float), ctx->stream);
     if (e == cudaSuccess)
-        e = cudaMallocAsync(&d_material, n, ctx->stream);
+        e = pool_alloc(ctx, &d_material, n, ctx->stream);
     if (e == cudaSuccess && d->measurement)
-        e = cudaMallocAsync(&d_meas, n, ctx->stream);
+        e = pool_alloc(ctx, &d_meas, n, ctx->stream);
     if (e == cudaSuccess)
-        e = cudaMallocAsync(&d_bad, sizeof(unsigned int), ctx->stream);
+        e = pool_alloc(ctx, &d_bad, sizeof(unsigned int), ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_density, d->density, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess)
@@ -534,9 +561,9 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     unsigned int distinct = 0;
     std::vector<dev::PaletteEntry> palette;
     if (e == cudaSuccess && d->layout == 0 && n <= 0xffffffffull) { // the compact layout indexes voxels in 32 bits
-        e = cudaMallocAsync(&d_table, dev_palette_table_bytes(), ctx->stream);
+        e = pool_alloc(ctx, &d_table, dev_palette_table_bytes(), ctx->stream);
         if (e == cudaSuccess)
-            e = cudaMallocAsync(&d_count, sizeof(unsigned int), ctx->stream);
+            e = pool_alloc(ctx, &d_count, sizeof(unsigned int), ctx->stream);
         if (e == cudaSuccess)
             e = cudaMemsetAsync(d_table, 0, dev_palette_table_bytes(), ctx->stream);
         if (e == cudaSuccess)
@@ -567,13 +594,13 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
             }
             uint8_t* d_slots = nullptr;
             if (e == cudaSuccess)
-                e = cudaMallocAsync(&d_slots, PALETTE_TABLE, ctx->stream);
+                e = pool_alloc(ctx, &d_slots, PALETTE_TABLE, ctx->stream);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(d_slots, slot_index.data(), PALETTE_TABLE, cudaMemcpyHostToDevice, ctx->stream);
             if (e == cudaSuccess)
-                e = cudaMallocAsync(&w->palette_index, n, ctx->stream);
+                e = pool_alloc(ctx, &w->palette_index, n, ctx->stream);
             if (e == cudaSuccess)
-                e = cudaMallocAsync(&w->palette, dev::PALETTE_MAX * sizeof(dev::PaletteEntry), ctx->stream);
+                e = pool_alloc(ctx, &w->palette, dev::PALETTE_MAX * sizeof(dev::PaletteEntry), ctx->stream);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(w->palette, palette.data(), palette.size() * sizeof(dev::PaletteEntry), cudaMemcpyHostToDevice, ctx->stream);
             if (e == cudaSuccess) {
@@ -587,7 +614,7 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     // the 8-byte layout only when the compact one is not used (too many distinct voxels, or asked for)
     if (e == cudaSuccess && !w->palette_index) {
         palette.clear();
-        e = cudaMallocAsync(&w->voxels, bytes, ctx->stream);
+        e = pool_alloc(ctx, &w->voxels, bytes, ctx->stream);
         if (e == cudaSuccess) {
             pack_voxels_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(d_density, d_material, d_meas, n, w->voxels);
             e = cudaGetLastError();
@@ -672,7 +699,7 @@ int dxmc_gpu_world_max_density(dxmc_world* w, double* out, int n_materials)
     }
     cudaSetDevice(ctx->device);
     unsigned int* d_bits = nullptr;
-    DXMC_CUDA(ctx, cudaMallocAsync(&d_bits, n_materials * sizeof(unsigned int), ctx->stream));
+    DXMC_CUDA(ctx, pool_alloc(ctx, &d_bits, n_materials * sizeof(unsigned int), ctx->stream));
     DXMC_CUDA(ctx, cudaMemsetAsync(d_bits, 0, n_materials * sizeof(unsigned int), ctx->stream));
     DXMC_CUDA(ctx, dev::launch_max_density(w->voxels, w->params.n_voxels, d_bits, n_materials, ctx->stream));
     std::vector<unsigned int> bits(n_materials);
@@ -848,7 +875,7 @@ int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* b, dxmc_lut** ou
     lut->serial = ++lut_serials;
     majorant_ratios(img, m, *lut);
     lut->bytes = img.size() * sizeof(float);
-    cudaError_t e = cudaMallocAsync(&lut->image, lut->bytes, ctx->stream);
+    cudaError_t e = pool_alloc(ctx, &lut->image, lut->bytes, ctx->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(lut->image, img.data(), lut->bytes, cudaMemcpyHostToDevice, ctx->stream);
     const cudaError_t se = cudaStreamSynchronize(ctx->stream); // img is a local buffer
@@ -1023,22 +1050,22 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     uint8_t* level = nullptr;
     float *d0 = nullptr, *d1 = nullptr, *cost = nullptr;
     int* bounds = nullptr;
-    cudaError_t e = cudaMallocAsync(&cells, cell_bytes, s);
+    cudaError_t e = pool_alloc(ctx, &cells, cell_bytes, s);
     float* box = cells ? reinterpret_cast<float*>(cells + ncell * b.bands) : nullptr;
     if (e == cudaSuccess)
-        e = cudaMallocAsync(&bounds, 6 * sizeof(int), s);
+        e = pool_alloc(ctx, &bounds, 6 * sizeof(int), s);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(bounds, 0x7f, 3 * sizeof(int), s); // minima start large
     if (e == cudaSuccess)
         e = cudaMemsetAsync(bounds + 3, 0xff, 3 * sizeof(int), s); // maxima start at -1
     if (e == cudaSuccess)
-        e = cudaMallocAsync(&level, ncell, s);
+        e = pool_alloc(ctx, &level, ncell, s);
     if (e == cudaSuccess)
-        e = cudaMallocAsync(&d0, ncell * sizeof(float), s);
+        e = pool_alloc(ctx, &d0, ncell * sizeof(float), s);
     if (e == cudaSuccess)
-        e = cudaMallocAsync(&d1, ncell * sizeof(float), s);
+        e = pool_alloc(ctx, &d1, ncell * sizeof(float), s);
     if (e == cudaSuccess)
-        e = cudaMallocAsync(&cost, ncell * sizeof(float), s);
+        e = pool_alloc(ctx, &cost, ncell * sizeof(float), s);
     for (int a = 0; a < 3; ++a)
         b.lower[a] = w->params.lower[a];
     for (int band = 0; band < b.bands && e == cudaSuccess; ++band) {
@@ -1239,17 +1266,17 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     cudaStream_t s = ctx->stream;
     cudaError_t e = cudaSuccess;
     if (tally_mode == 1)
-        e = cudaMallocAsync(&j->tally_f32, tally_bytes, s);
+        e = pool_alloc(ctx, &j->tally_f32, tally_bytes, s);
     else
-        e = cudaMallocAsync(&j->tally, tally_bytes, s);
+        e = pool_alloc(ctx, &j->tally, tally_bytes, s);
     if (e == cudaSuccess)
-        e = cudaMallocAsync(&j->n_events, nv * sizeof(uint32_t), s);
+        e = pool_alloc(ctx, &j->n_events, nv * sizeof(uint32_t), s);
     if (e == cudaSuccess)
-        e = cudaMallocAsync(&j->counters, sizeof(dev::JobCounters), s);
+        e = pool_alloc(ctx, &j->counters, sizeof(dev::JobCounters), s);
     if (e == cudaSuccess)
-        e = cudaMallocAsync(&j->tables, table_bytes, s);
+        e = pool_alloc(ctx, &j->tables, table_bytes, s);
     if (e == cudaSuccess && queue_bytes)
-        e = cudaMallocAsync(&j->queue, queue_bytes, s);
+        e = pool_alloc(ctx, &j->queue, queue_bytes, s);
     if (e == cudaSuccess)
         e = cudaEventCreate(&j->begin);
     if (e == cudaSuccess)
@@ -2059,7 +2086,7 @@ int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double
         if (!mapped && !j->cancelled && (dose || variance)) {
             double* d_out = nullptr;
             const uint64_t out_elems = (dose ? nv : 0) + (variance ? nv : 0);
-            DXMC_CUDA(ctx, cudaMallocAsync(&d_out, out_elems * sizeof(double), s));
+            DXMC_CUDA(ctx, pool_alloc(ctx, &d_out, out_elems * sizeof(double), s));
             double* d_dose = dose ? d_out : nullptr;
             double* d_var = variance ? d_out + (dose ? nv : 0) : nullptr;
             const double vv = j->world->spacing[0] * j->world->spacing[1] * j->world->spacing[2] / 1000.0;
@@ -2208,9 +2235,9 @@ int dxmc_gpu_radiological_path(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* l
     cudaStream_t s = ctx->stream;
     float* d_rays = nullptr;
     double* d_out = nullptr;
-    cudaError_t e = cudaMallocAsync(&d_rays, n_rays * 7 * sizeof(float), s);
+    cudaError_t e = pool_alloc(ctx, &d_rays, n_rays * 7 * sizeof(float), s);
     if (e == cudaSuccess)
-        e = cudaMallocAsync(&d_out, n_rays * sizeof(double), s);
+        e = pool_alloc(ctx, &d_out, n_rays * sizeof(double), s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_rays, rays, n_rays * 7 * sizeof(float), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
@@ -2235,7 +2262,7 @@ int dxmc_gpu_probe_lut(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, const dou
     cudaSetDevice(ctx->device);
     cudaStream_t s = ctx->stream;
     double* buf = nullptr;
-    DXMC_CUDA(ctx, cudaMallocAsync(&buf, static_cast<size_t>(n) * 5 * sizeof(double), s));
+    DXMC_CUDA(ctx, pool_alloc(ctx, &buf, static_cast<size_t>(n) * 5 * sizeof(double), s));
     DXMC_CUDA(ctx, cudaMemcpyAsync(buf, energies, n * sizeof(double), cudaMemcpyHostToDevice, s));
     DXMC_CUDA(ctx, dev::launch_probe_lut(lut->image, lut->meta, material, buf, n, buf + n, buf + 4 * static_cast<size_t>(n), s));
     DXMC_CUDA(ctx, cudaMemcpyAsync(out_att, buf + n, 3 * static_cast<size_t>(n) * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -2254,7 +2281,7 @@ int dxmc_gpu_probe_interactions(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, 
     cudaSetDevice(ctx->device);
     cudaStream_t s = ctx->stream;
     float* buf = nullptr;
-    DXMC_CUDA(ctx, cudaMallocAsync(&buf, n * 3 * sizeof(float), s));
+    DXMC_CUDA(ctx, pool_alloc(ctx, &buf, n * 3 * sizeof(float), s));
     DXMC_CUDA(ctx, dev::launch_probe_interactions(lut->image, lut->meta, material, model, kind, static_cast<float>(energy), n, seed, buf, buf + n, buf + 2 * n, s));
     DXMC_CUDA(ctx, cudaMemcpyAsync(out_cos, buf, n * sizeof(float), cudaMemcpyDeviceToHost, s));
     DXMC_CUDA(ctx, cudaMemcpyAsync(out_energy, buf + n, n * sizeof(float), cudaMemcpyDeviceToHost, s));
