@@ -982,15 +982,25 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     if (lut->meta.n_materials < w->n_materials)
         return fail(ctx, DXMC_ERR_INVALID, "lut has fewer materials than the world");
     dev::MajorantBuild b {};
-    uint64_t ncell = 1;
+    int shift[3];
     for (int a = 0; a < 3; ++a) {
         int sh = static_cast<int>(std::lround(std::log2(std::max(MAJORANT_CELL_MM / w->spacing[a], 1.0))));
         sh = std::min(std::max(sh, 0), 6);
         while (((w->dims[a] + (1ull << sh) - 1) >> sh) > MAJORANT_MAX_CELLS_PER_AXIS)
             ++sh;
-        b.shift[a] = sh;
-        b.n[a] = static_cast<uint32_t>((w->dims[a] + (1ull << sh) - 1) >> sh);
-        b.edge[a] = static_cast<float>(w->spacing[a] * static_cast<double>(1ull << sh));
+        shift[a] = sh;
+    }
+    auto cells_along = [&](int a) { return (w->dims[a] + (1ull << shift[a]) - 1) >> shift[a]; };
+    // the kernels index (cell, band) pairs in 32 bits: coarser cells for huge grids
+    while (cells_along(0) * cells_along(1) * cells_along(2) * static_cast<uint64_t>(lut->majorant_bands) >= (1ull << 31)) {
+        const int a = cells_along(0) >= cells_along(1) ? (cells_along(0) >= cells_along(2) ? 0 : 2) : (cells_along(1) >= cells_along(2) ? 1 : 2);
+        ++shift[a];
+    }
+    uint64_t ncell = 1;
+    for (int a = 0; a < 3; ++a) {
+        b.shift[a] = shift[a];
+        b.n[a] = static_cast<uint32_t>(cells_along(a));
+        b.edge[a] = static_cast<float>(w->spacing[a] * static_cast<double>(1ull << shift[a]));
         ncell *= b.n[a];
     }
     b.levels_per_octave = MAJORANT_LEVELS_PER_OCTAVE;
