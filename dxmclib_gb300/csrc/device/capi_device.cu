@@ -112,6 +112,7 @@ struct dxmc_lut {
     // (keV) and the global majorant (1/mm) at each band's reference energy
     int majorant_bands = 1;
     float band_edge[dev::MAJORANT_MAX_BANDS - 1] {};
+    float band_log0 = 1.0f, band_inv_dlog = 0.0f; // log10 of the first edge's base (10 keV) and 1 / log10 step
     std::vector<float> majorant_ratio;
     float mu_ref[dev::MAJORANT_MAX_BANDS] {};
 };
@@ -226,6 +227,8 @@ void majorant_ratios(const std::vector<float>& img, const dev::LutMeta& m, dxmc_
     edges.push_back(e_max);
     for (int k = 0; k < dev::MAJORANT_MAX_BANDS - 1; ++k)
         lut.band_edge[k] = k + 1 < nb ? static_cast<float>(edges[k + 1]) : INFINITY;
+    lut.band_log0 = 1.0f;
+    lut.band_inv_dlog = nb > 1 ? static_cast<float>(nb / std::log10(e_max / 10.0)) : 0.0f;
     std::vector<float> points;
     for (int k = 0; k < R; ++k)
         points.push_back(x[k]);
@@ -1113,6 +1116,8 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     m.grid.bands = b.bands;
     for (int k = 0; k < dev::MAJORANT_MAX_BANDS - 1; ++k)
         m.grid.band_edge[k] = lut->band_edge[k];
+    m.grid.band_log0 = lut->band_log0;
+    m.grid.band_inv_dlog = lut->band_inv_dlog;
     ctx->in_use += cell_bytes;
     w->majorants.push_back(m);
     *out = &w->majorants.back().grid;

@@ -53,7 +53,9 @@ struct MajorantGrid {
     int shift[3];        // log2 of the cell size in voxels
     int bands;
     float band_edge[MAJORANT_MAX_BANDS - 1]; // keV, ascending; band = number of edges <= E (unused: infinity)
-    int pad;
+    // the edges are log-spaced: band = clamp(floor((log10 E - band_log0) * band_inv_dlog), 0, bands - 1)
+    float band_log0;
+    float band_inv_dlog;
 };
 
 struct SourceParams {

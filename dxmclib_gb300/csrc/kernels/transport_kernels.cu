@@ -389,7 +389,7 @@ namespace {
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             if (fabsf(dir[i]) > N_ERROR) {
-                const float inv = __frcp_rn(dir[i]);
+                const float inv = 1.0f / dir[i];
                 const float a0 = (w.lo[i] - pos[i]) * inv;
                 const float an = (w.hi[i] - pos[i]) * inv;
                 amin = fmaxf(amin, fminf(a0, an));
@@ -514,12 +514,9 @@ namespace {
     {
         const MajorantGrid& g = p.majorant;
         const WorldParams& w = p.world;
-        const float E = s.ph.energy;
-        int band = 0;
-#pragma unroll
-        for (int k = 0; k < MAJORANT_MAX_BANDS - 1; ++k)
-            band += E >= g.band_edge[k];
-        s.band = band;
+        // s.logE = log10 E was just computed; the band intervals of the bounds are
+        // widened by 0.1 % on the host, which covers the rounding here
+        s.band = min(max(__float2int_rd((s.logE - g.band_log0) * g.band_inv_dlog), 0), g.bands - 1);
         const float fx = fminf(fmaxf(fmaf(s.ph.px, w.inv_spacing[0], -w.lo_inv[0]), 0.0f), w.dims_f[0] - 1.0f);
         const float fy = fminf(fmaxf(fmaf(s.ph.py, w.inv_spacing[1], -w.lo_inv[1]), 0.0f), w.dims_f[1] - 1.0f);
         const float fz = fminf(fmaxf(fmaf(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2]), 0.0f), w.dims_f[2] - 1.0f);
