@@ -148,6 +148,7 @@ class BatchOptions(C.Structure):
 # name -> (restype, argtypes)
 SIGNATURES = {
     "dxmc_gpu_abi_version": (C.c_int, []),
+    "dxmc_udiv_invariant": (C.c_int, [C.POINTER(C.c_uint32), C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32)]),
     "dxmc_physics_material": (C.c_int, [C.c_char_p, D, C.POINTER(MaterialProvider)]),
     "dxmc_physics_material_free": (None, [C.POINTER(MaterialProvider)]),
     "dxmc_physics_element_material": (C.c_int, [C.c_int, C.POINTER(MaterialProvider)]),

@@ -1361,8 +1361,14 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
         bool uniform = true;
         for (uint64_t i = 1; i < ne && uniform; ++i)
             uniform = jd->exposures[i].n_histories == jd->exposures[0].n_histories;
-        if (uniform)
+        if (uniform) {
             p.uniform_hpe = jd->exposures[0].n_histories;
+            if (p.uniform_hpe <= 0xffffffffull) {
+                const auto q = udiv_magic(static_cast<uint32_t>(p.uniform_hpe));
+                p.hpe_magic = q.m;
+                p.hpe_shifts = q.shifts;
+            }
+        }
     }
     {
         // job value, else context option, else the default for the generation mode

@@ -200,6 +200,16 @@ int dxmc_lut_get_info(const dxmc_lut_blob* blob, dxmc_lut_info* info)
     return DXMC_OK;
 }
 
+int dxmc_udiv_invariant(const uint32_t* n, uint64_t count, uint32_t d, uint32_t* out)
+{
+    if (!n || !out || d == 0)
+        return DXMC_ERR_INVALID;
+    const auto q = dxmc_gb300::udiv_magic(d);
+    for (uint64_t i = 0; i < count; ++i)
+        out[i] = dxmc_gb300::udiv_apply(n[i], q.m, q.shifts);
+    return DXMC_OK;
+}
+
 int dxmc_philox4x32_10(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4])
 {
     if (!counter || !key || !out)

@@ -44,4 +44,30 @@ DXMC_HD inline void philox4x32_10(std::uint32_t& c0, std::uint32_t& c1, std::uin
     }
 }
 
+// Unsigned 32-bit division by a divisor fixed for a whole job, as a multiply-high
+// and two shifts (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994; the round-up variant for every divisor):
+// n / d = (t + ((n - t) >> s1)) >> s2 with t = mulhi(m, n), for all n < 2^32.
+struct UDivMagic {
+    std::uint32_t m;
+    std::uint32_t shifts; // s1 | s2 << 8
+};
+
+inline UDivMagic udiv_magic(std::uint32_t d)
+{
+    if (d <= 1)
+        return UDivMagic { 0u, 0u }; // n / 1 = n
+    int l = 0;
+    while ((std::uint64_t { 1 } << l) < d)
+        ++l; // l = ceil(log2 d)
+    const std::uint64_t m = ((std::uint64_t { 1 } << 32) * ((std::uint64_t { 1 } << l) - d)) / d + 1;
+    return UDivMagic { static_cast<std::uint32_t>(m), 1u | (static_cast<std::uint32_t>(l - 1) << 8) };
+}
+
+DXMC_HD inline std::uint32_t udiv_apply(std::uint32_t n, std::uint32_t m, std::uint32_t shifts)
+{
+    const std::uint32_t t = mulhi32(m, n);
+    return (t + ((n - t) >> (shifts & 0xffu))) >> (shifts >> 8);
+}
+
 } // namespace dxmc_gb300

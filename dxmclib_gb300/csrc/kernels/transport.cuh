@@ -111,6 +111,8 @@ struct TransportParams {
     uint64_t total_histories;
     uint64_t seed;
     uint64_t uniform_hpe;   // histories per exposure when every exposure has the same count, else 0
+    uint32_t hpe_magic;     // history / uniform_hpe as a multiply-high (udiv_magic), jobs below 2^32 histories
+    uint32_t hpe_shifts;
     int tally_mode;
     int lut_in_smem;
     int regen_threshold;    // refill finished lanes once at least this many are idle (1..32)

@@ -568,7 +568,7 @@ namespace {
         s.rng.init(p.seed, h);
         uint32_t ei;
         if (p.uniform_hpe && p.total_histories <= 0xffffffffull)
-            ei = static_cast<uint32_t>(h) / static_cast<uint32_t>(p.uniform_hpe);
+            ei = udiv_apply(static_cast<uint32_t>(h), p.hpe_magic, p.hpe_shifts);
         else
             ei = p.uniform_hpe ? static_cast<uint32_t>(h / p.uniform_hpe) : find_exposure(p.source, h);
         DevExposure ex;
@@ -1058,7 +1058,7 @@ namespace {
                 rng.init(p.seed, h);
                 uint32_t ei;
                 if (p.uniform_hpe && p.total_histories <= 0xffffffffull)
-                    ei = static_cast<uint32_t>(h) / static_cast<uint32_t>(p.uniform_hpe);
+                    ei = udiv_apply(static_cast<uint32_t>(h), p.hpe_magic, p.hpe_shifts);
                 else
                     ei = p.uniform_hpe ? static_cast<uint32_t>(h / p.uniform_hpe) : find_exposure(p.source, h);
                 DevExposure ex;

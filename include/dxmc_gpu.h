@@ -191,6 +191,9 @@ typedef struct dxmc_bowtie_desc {
 /* Philox4x32-10, the counter-based generator the kernels draw from (one stream
  * per history), exposed for known-answer tests. */
 int dxmc_philox4x32_10(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4]);
+/* The kernels' division of history ids by the histories per exposure (multiply-high
+ * and shifts, magic from the divisor), for host-side checks: out[i] = n[i] / d. */
+int dxmc_udiv_invariant(const uint32_t* n, uint64_t count, uint32_t d, uint32_t* out);
 
 /* Alias table of a spectrum (host), exposed for parity tests. */
 int dxmc_alias_table(const double* weights, int n, double* probs, uint64_t* alias);

@@ -227,3 +227,26 @@ def test_invalid_inputs_are_rejected(lib):
     assert lib.dxmc_lut_build_max_density(C.byref(prov), 0, md.ctypes.data_as(A.DP), 60.0, C.byref(blob)) == A.DXMC_ERR_INVALID
     assert lib.dxmc_lut_build_max_density(C.byref(prov), 1, md.ctypes.data_as(A.DP), -5.0, C.byref(blob)) == A.DXMC_ERR_INVALID
     lib.dxmc_physics_material_free(C.byref(prov))
+
+
+def test_invariant_division_is_exact(lib):
+    """The kernels map a history id to its exposure with a multiply-high and two
+    shifts instead of a division (udiv_magic / udiv_apply); it must equal n / d
+    for every 32-bit n and divisor."""
+    from dxmclib_gb300 import _capi as A
+    rng = np.random.default_rng(11)
+    n = np.concatenate([rng.integers(0, 2 ** 32, 200_000, dtype=np.uint64),
+                        np.array([0, 1, 2, 3, 2 ** 31 - 1, 2 ** 31, 2 ** 32 - 2, 2 ** 32 - 1], np.uint64)]).astype(np.uint32)
+    divisors = [1, 2, 3, 5, 7, 10, 22223, 65535, 65536, 65537, 2 ** 31 - 1, 2 ** 31, 2 ** 31 + 1, 2 ** 32 - 1]
+    divisors += [int(d) for d in rng.integers(2, 2 ** 32, 40, dtype=np.uint64)]
+    out = np.zeros_like(n)
+    for d in divisors:
+        assert lib.dxmc_udiv_invariant(n.ctypes.data_as(A.U32P), len(n), d, out.ctypes.data_as(A.U32P)) == 0
+        np.testing.assert_array_equal(out, n // np.uint32(d), err_msg=str(d))
+        # the multiples of d and their neighbours, where rounding would show
+        k = (n[:1000].astype(np.uint64) % (2 ** 32 // d + 1)) * d
+        m = np.concatenate([k, k + 1, np.where(k > 0, k - 1, 0)])
+        m = m[m < 2 ** 32].astype(np.uint32)
+        o2 = np.zeros_like(m)
+        assert lib.dxmc_udiv_invariant(m.ctypes.data_as(A.U32P), len(m), d, o2.ctypes.data_as(A.U32P)) == 0
+        np.testing.assert_array_equal(o2, m // np.uint32(d), err_msg=str(d))
