@@ -136,6 +136,7 @@ class World:
         self._density: Optional[np.ndarray] = None
         self._material: Optional[np.ndarray] = None
         self._measurement: Optional[np.ndarray] = None
+        self._measurement_given = False  # False: validate() made the all-zero map
         self._materials: List[Material] = []
         self._valid = False
 
@@ -167,6 +168,7 @@ class World:
 
     def setMeasurementMapArray(self, measurement):
         self._measurement = None if measurement is None else np.ascontiguousarray(measurement, dtype=np.uint8).ravel()
+        self._measurement_given = measurement is not None
         self._valid = False
 
     def addMaterialToMap(self, material: Material) -> bool:
@@ -874,7 +876,8 @@ class DeviceWorld:
         meas = world.measurementMapArray()
         d.density = dens.ctypes.data_as(A.FP)
         d.material = mat.ctypes.data_as(A.U8P)
-        d.measurement = meas.ctypes.data_as(A.U8P) if meas is not None and meas.any() else None
+        # the all-zero map that validation creates stays on the host (no forced scoring)
+        d.measurement = meas.ctypes.data_as(A.U8P) if meas is not None and world._measurement_given else None
         d.n_materials = len(world.materialMap())
         d.layout = int(layout)
         self.handle = C.c_void_p()
