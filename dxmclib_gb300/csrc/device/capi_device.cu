@@ -1012,7 +1012,7 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     // per band, the voxel scales and the levels worth trying: the palette's own
     // levels, or every second level for the 8-byte layout
     const int nm = lut->meta.n_materials;
-    std::vector<dev::MajorantScales> scales(b.bands);
+    std::vector<float> scales(static_cast<size_t>(b.bands) * dev::PALETTE_MAX, 0.0f);
     std::vector<uint64_t> levels(b.bands, 0);
     for (int band = 0; band < b.bands; ++band) {
         const float* ratio = lut->majorant_ratio.data() + static_cast<size_t>(band) * nm;
@@ -1022,12 +1022,12 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
                 const int mat = static_cast<int>(pe.code & 0xffu);
                 const bool meas = ((pe.code >> 8) & 0xffu) != 0;
                 const float sc = meas ? 1.0f : pe.density * ratio[mat];
-                scales[band].v[i] = sc;
+                scales[static_cast<size_t>(band) * dev::PALETTE_MAX + i] = sc;
                 levels[band] |= 1ull << majorant_level(sc);
             }
         } else {
             for (int m = 0; m < nm && m < dev::PALETTE_MAX; ++m)
-                scales[band].v[m] = ratio[m];
+                scales[static_cast<size_t>(band) * dev::PALETTE_MAX + m] = ratio[m];
             for (int lv = 2; lv <= MAJORANT_MAX_LEVEL; lv += 2)
                 levels[band] |= 1ull << lv;
         }
@@ -1061,7 +1061,7 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     cudaStream_t s = ctx->stream;
     float2* cells = nullptr;
     uint8_t* level = nullptr;
-    float *d0 = nullptr, *d1 = nullptr, *cost = nullptr;
+    float *d0 = nullptr, *d1 = nullptr, *cost = nullptr, *d_scales = nullptr;
     int* bounds = nullptr;
     cudaError_t e = pool_alloc(ctx, &cells, cell_bytes, s);
     float* box = cells ? reinterpret_cast<float*>(cells + ncell * b.bands) : nullptr;
@@ -1072,28 +1072,39 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     if (e == cudaSuccess)
         e = cudaMemsetAsync(bounds + 3, 0xff, 3 * sizeof(int), s); // maxima start at -1
     if (e == cudaSuccess)
-        e = pool_alloc(ctx, &level, ncell, s);
+        e = pool_alloc(ctx, &level, ncell * b.bands, s);
     if (e == cudaSuccess)
         e = pool_alloc(ctx, &d0, ncell * sizeof(float), s);
     if (e == cudaSuccess)
         e = pool_alloc(ctx, &d1, ncell * sizeof(float), s);
     if (e == cudaSuccess)
-        e = pool_alloc(ctx, &cost, ncell * sizeof(float), s);
+        e = pool_alloc(ctx, &cost, ncell * b.bands * sizeof(float), s);
+    if (e == cudaSuccess)
+        e = pool_alloc(ctx, &d_scales, scales.size() * sizeof(float), s);
+    if (e == cudaSuccess) // pageable source: staged before the call returns
+        e = cudaMemcpyAsync(d_scales, scales.data(), scales.size() * sizeof(float), cudaMemcpyHostToDevice, s);
     for (int a = 0; a < 3; ++a)
         b.lower[a] = w->params.lower[a];
+    for (int band = 0; band < dev::MAJORANT_MAX_BANDS; ++band) {
+        b.floor_levels[band] = band < b.bands ? floor_level[band] : -1;
+        b.mu_refs[band] = band < b.bands ? lut->mu_ref[band] : 0.0f;
+    }
+    // the levels of every band in one pass over the voxels, then the distance
+    // transforms band by band
+    if (e == cudaSuccess)
+        e = dev::launch_majorant_levels(w->params, d_scales, b, level, cells, cost, bounds, s);
     for (int band = 0; band < b.bands && e == cudaSuccess; ++band) {
         b.band = band;
         b.mu_ref = lut->mu_ref[band];
-        b.floor_level = floor_level[band];
-        e = dev::launch_majorant_levels(w->params, scales[band], b, level, cells, cost, bounds, s);
         for (int lv = 1; lv <= MAJORANT_MAX_LEVEL && e == cudaSuccess; ++lv)
             if (levels[band] >> lv & 1ull)
-                e = dev::launch_majorant_level_pass(b, level, lv, d0, d1, cells, cost, s);
+                e = dev::launch_majorant_level_pass(b, level + static_cast<size_t>(band) * ncell, lv, d0, d1, cells,
+                    cost + static_cast<size_t>(band) * ncell, s);
     }
     if (e == cudaSuccess && use_box)
         e = dev::launch_majorant_box(b, bounds, cells, box, s);
     for (void* ptr : { static_cast<void*>(level), static_cast<void*>(d0), static_cast<void*>(d1), static_cast<void*>(cost),
-             static_cast<void*>(bounds) })
+             static_cast<void*>(bounds), static_cast<void*>(d_scales) })
         if (ptr)
             cudaFreeAsync(ptr, s);
     if (e != cudaSuccess) {

@@ -24,6 +24,7 @@
 // The three steps run once per energy band, with the ratios r_m of that band.
 // Last, the cells outside the box of all cells above their band's emptiest
 // level get -R: there a flight may also run to that box (MajorantGrid).
+#include <algorithm>
 #include <cmath>
 
 #include "transport.cuh"
@@ -45,12 +46,15 @@ __device__ __forceinline__ float level_scale(int level, int per_octave)
     return exp2f(-static_cast<float>(level) / static_cast<float>(per_octave));
 }
 
-__global__ void majorant_level_kernel(WorldParams w, const __grid_constant__ MajorantScales scales, MajorantBuild b,
+// Cell levels of every band in one pass over the voxels: scales holds bands x 256
+// scales (per palette entry, or r_m per material for the 8-byte layout); level
+// and cost are bands x ncell, cells ncell x bands.
+__global__ void majorant_level_kernel(WorldParams w, const float* __restrict__ scales, MajorantBuild b,
     uint8_t* __restrict__ level, float2* __restrict__ cells, float* __restrict__ cost, int* __restrict__ bounds)
 {
-    __shared__ float scale_table[PALETTE_MAX];
-    for (int i = threadIdx.x; i < PALETTE_MAX; i += blockDim.x)
-        scale_table[i] = scales.v[i];
+    __shared__ float scale_table[MAJORANT_MAX_BANDS * PALETTE_MAX];
+    for (int i = threadIdx.x; i < b.bands * PALETTE_MAX; i += blockDim.x)
+        scale_table[i] = scales[i];
     __syncthreads();
     const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
     for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < ncell;
@@ -60,35 +64,52 @@ __global__ void majorant_level_kernel(WorldParams w, const __grid_constant__ Maj
         const uint32_t x0 = cx << b.shift[0], x1 = min(w.dims[0], (cx + 1) << b.shift[0]);
         const uint32_t y0 = cy << b.shift[1], y1 = min(w.dims[1], (cy + 1) << b.shift[1]);
         const uint32_t z0 = cz << b.shift[2], z1 = min(w.dims[2], (cz + 1) << b.shift[2]);
-        float m = 0.0f;
+        float m[MAJORANT_MAX_BANDS];
+#pragma unroll
+        for (int k = 0; k < MAJORANT_MAX_BANDS; ++k)
+            m[k] = 0.0f;
         for (uint32_t z = z0; z < z1; ++z) {
             for (uint32_t y = y0; y < y1; ++y) {
                 const uint64_t row = static_cast<uint64_t>(z) * w.nxy + static_cast<uint64_t>(y) * w.dims[0];
-                if (w.palette_index) {
-                    for (uint32_t x = x0; x < x1; ++x)
-                        m = fmaxf(m, scale_table[w.palette_index[row + x]]);
-                } else {
-                    for (uint32_t x = x0; x < x1; ++x) {
+                for (uint32_t x = x0; x < x1; ++x) {
+                    int idx;
+                    float dens = 1.0f;
+                    bool forced = false;
+                    if (w.palette_index) {
+                        idx = w.palette_index[row + x];
+                    } else {
                         const Voxel v = w.voxels[row + x];
-                        m = fmaxf(m, v.measurement ? 1.0f : v.density * scale_table[v.material]);
+                        idx = v.material;
+                        dens = v.density;
+                        forced = v.measurement != 0;
                     }
+#pragma unroll
+                    for (int k = 0; k < MAJORANT_MAX_BANDS; ++k)
+                        if (k < b.bands)
+                            m[k] = fmaxf(m[k], forced ? 1.0f : dens * scale_table[k * PALETTE_MAX + idx]);
                 }
             }
         }
-        int lv = b.max_level;
-        if (m >= 1.0f) {
-            lv = 0;
-        } else if (m > 0.0f) {
-            lv = min(b.max_level, static_cast<int>(floorf(-static_cast<float>(b.levels_per_octave) * log2f(m))));
-            // the level's scale must not fall below the cell's maximum, whatever the rounding of log2f
-            while (lv > 0 && level_scale(lv, b.levels_per_octave) < m)
-                --lv;
+        bool above = false;
+#pragma unroll
+        for (int k = 0; k < MAJORANT_MAX_BANDS; ++k) {
+            if (k >= b.bands)
+                break;
+            int lv = b.max_level;
+            if (m[k] >= 1.0f) {
+                lv = 0;
+            } else if (m[k] > 0.0f) {
+                lv = min(b.max_level, static_cast<int>(floorf(-static_cast<float>(b.levels_per_octave) * log2f(m[k]))));
+                // the level's scale must not fall below the cell's maximum, whatever the rounding of log2f
+                while (lv > 0 && level_scale(lv, b.levels_per_octave) < m[k])
+                    --lv;
+            }
+            level[k * ncell + c] = static_cast<uint8_t>(lv);
+            cells[c * b.bands + k] = make_float2(1.0f, INFINITY); // the global majorant until a level does better
+            cost[k * ncell + c] = b.mu_refs[k];
+            above = above || (b.floor_levels[k] >= 0 && lv < b.floor_levels[k]);
         }
-        level[c] = static_cast<uint8_t>(lv);
-        cells[c * b.bands + b.band] = make_float2(1.0f, INFINITY); // the global majorant until a level does better
-        cost[c] = b.mu_ref;
-        // cells above the band's emptiest level widen the box (warp-reduced atomics)
-        const bool above = b.floor_level >= 0 && lv < b.floor_level;
+        // cells above their band's emptiest level widen the box (warp-reduced atomics)
         const unsigned mask = __ballot_sync(__activemask(), above);
         if (mask) {
             const unsigned active = __activemask();
@@ -219,6 +240,36 @@ __global__ void majorant_axis_kernel(MajorantBuild b, const float* __restrict__ 
     }
 }
 
+// The first (x) pass of the distance transform on the dilated set itself (0 on
+// it, infinity elsewhere): one thread per grid row finds each cell's nearest set
+// cell on the row with a forward and a backward sweep, instead of a scan per cell
+// (rows without a set cell would cost every cell a full scan).
+__global__ void majorant_sweep_x_kernel(MajorantBuild b, const float* __restrict__ in, float* __restrict__ out)
+{
+    const uint64_t rows = static_cast<uint64_t>(b.n[1]) * b.n[2];
+    const int n = static_cast<int>(b.n[0]);
+    const float e = b.edge[0];
+    for (uint64_t r = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; r < rows;
+         r += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const float* row_in = in + r * n;
+        float* row_out = out + r * n;
+        int last = -1; // the nearest set cell at or before x
+        for (int x = 0; x < n; ++x) {
+            if (row_in[x] == 0.0f)
+                last = x;
+            row_out[x] = last >= 0 ? static_cast<float>(x - last) : INFINITY;
+        }
+        int next = -1; // the nearest set cell at or after x
+        for (int x = n - 1; x >= 0; --x) {
+            if (row_in[x] == 0.0f)
+                next = x;
+            const float k = fminf(row_out[x], next >= 0 ? static_cast<float>(next - x) : INFINITY);
+            const float d = k * e;
+            row_out[x] = d * d;
+        }
+    }
+}
+
 int grid_for(uint64_t n)
 {
     const uint64_t blocks = (n + 255) / 256;
@@ -227,7 +278,7 @@ int grid_for(uint64_t n)
 
 } // namespace
 
-cudaError_t launch_majorant_levels(const WorldParams& w, const MajorantScales& scales, const MajorantBuild& b,
+cudaError_t launch_majorant_levels(const WorldParams& w, const float* scales, const MajorantBuild& b,
     uint8_t* level, float2* cells, float* cost, int* bounds, cudaStream_t stream)
 {
     const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
@@ -248,7 +299,8 @@ cudaError_t launch_majorant_level_pass(const MajorantBuild& b, const uint8_t* le
     const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
     const int g = grid_for(ncell);
     majorant_dilate_kernel<<<g, 256, 0, stream>>>(b, level, lv, d0);
-    majorant_axis_kernel<0, false><<<g, 256, 0, stream>>>(b, d0, d1, lv, cells, cost);
+    const uint64_t rows = static_cast<uint64_t>(b.n[1]) * b.n[2];
+    majorant_sweep_x_kernel<<<static_cast<int>(std::min<uint64_t>((rows + 63) / 64, 4096)), 64, 0, stream>>>(b, d0, d1);
     majorant_axis_kernel<1, false><<<g, 256, 0, stream>>>(b, d1, d0, lv, cells, cost);
     majorant_axis_kernel<2, true><<<g, 256, 0, stream>>>(b, d0, nullptr, lv, cells, cost);
     return cudaGetLastError();

@@ -172,7 +172,7 @@ cudaError_t launch_postprocess_f32(const float* tally, const WorldParams& w, uin
 // (origin mm, direction, energy keV); out[i] = sum of mu * density * length (cm).
 cudaError_t launch_radiological_path(const WorldParams& w, const float* lut, LutMeta meta, const float* rays, uint64_t n,
     double* out, cudaStream_t stream);
-// Local-majorant grid construction (majorant_kernels.cu).  MajorantScales holds
+// Local-majorant grid construction (majorant_kernels.cu).  The scale tables hold
 // the scale of each palette entry (compact layout) or the ratio r_m of each
 // material (8-byte layout: scale = density * r_m, 1 for measurement voxels).
 struct MajorantBuild {
@@ -183,13 +183,13 @@ struct MajorantBuild {
     int levels_per_octave;
     int max_level;
     int band, bands;     // the band being built; output pairs at cells[c * bands + band]
-    int floor_level;     // the band's emptiest level (its cells may be flown through), -1: none
+    int floor_levels[MAJORANT_MAX_BANDS]; // each band's emptiest level (its cells may be flown through), -1: none
+    float mu_refs[MAJORANT_MAX_BANDS];    // each band's mu_ref (the level kernel initialises every band)
     float lower[3];      // grid corner (mm)
 };
-struct MajorantScales {
-    float v[PALETTE_MAX];
-};
-cudaError_t launch_majorant_levels(const WorldParams& w, const MajorantScales& scales, const MajorantBuild& b,
+// All bands in one pass: scales is bands x PALETTE_MAX floats in device memory;
+// level and cost are bands x ncell.
+cudaError_t launch_majorant_levels(const WorldParams& w, const float* scales, const MajorantBuild& b,
     uint8_t* level, float2* cells, float* cost, int* bounds, cudaStream_t stream);
 // After all bands: writes the box (mm) of the cells that lay above their band's
 // emptiest level (bounds: cell index min x, y, z, max x, y, z; set up as empty
