@@ -955,6 +955,7 @@ constexpr int MAJORANT_LEVELS_PER_OCTAVE = DXMC_MAJORANT_LEVELS_PER_OCTAVE;
 constexpr int MAJORANT_MAX_LEVEL = MAJORANT_LEVELS_PER_OCTAVE * 12 < 63 ? MAJORANT_LEVELS_PER_OCTAVE * 12 : 63;
 constexpr uint64_t MAJORANT_MAX_CELLS_PER_AXIS = 1024;
 constexpr size_t MAJORANT_GRIDS_PER_WORLD = 4;    // one per LUT used with the world, least recently used evicted
+constexpr int MAJORANT_MAX_CANDIDATES = 12;       // distance transforms per band at most
 
 int majorant_level(float m)
 {
@@ -1009,8 +1010,7 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     b.levels_per_octave = MAJORANT_LEVELS_PER_OCTAVE;
     b.max_level = MAJORANT_MAX_LEVEL;
     b.bands = lut->majorant_bands;
-    // per band, the voxel scales and the levels worth trying: the palette's own
-    // levels, or every second level for the 8-byte layout
+    // per band, the voxel scales and (compact layout) the palette's own levels
     const int nm = lut->meta.n_materials;
     std::vector<float> scales(static_cast<size_t>(b.bands) * dev::PALETTE_MAX, 0.0f);
     std::vector<uint64_t> levels(b.bands, 0);
@@ -1026,10 +1026,9 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
                 levels[band] |= 1ull << majorant_level(sc);
             }
         } else {
+            // the levels come from the device histogram
             for (int m = 0; m < nm && m < dev::PALETTE_MAX; ++m)
                 scales[static_cast<size_t>(band) * dev::PALETTE_MAX + m] = ratio[m];
-            for (int lv = 2; lv <= MAJORANT_MAX_LEVEL; lv += 2)
-                levels[band] |= 1ull << lv;
         }
     }
     // each band's emptiest level (the palette's highest level); for the 8-byte layout
@@ -1063,6 +1062,7 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     uint8_t* level = nullptr;
     float *d0 = nullptr, *d1 = nullptr, *cost = nullptr, *d_scales = nullptr;
     int* bounds = nullptr;
+    unsigned int* d_hist = nullptr;
     cudaError_t e = pool_alloc(ctx, &cells, cell_bytes, s);
     float* box = cells ? reinterpret_cast<float*>(cells + ncell * b.bands) : nullptr;
     if (e == cudaSuccess)
@@ -1083,6 +1083,10 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
         e = pool_alloc(ctx, &d_scales, scales.size() * sizeof(float), s);
     if (e == cudaSuccess) // pageable source: staged before the call returns
         e = cudaMemcpyAsync(d_scales, scales.data(), scales.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        e = pool_alloc(ctx, &d_hist, static_cast<size_t>(b.bands) * 64 * sizeof(unsigned int), s);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(d_hist, 0, static_cast<size_t>(b.bands) * 64 * sizeof(unsigned int), s);
     for (int a = 0; a < 3; ++a)
         b.lower[a] = w->params.lower[a];
     for (int band = 0; band < dev::MAJORANT_MAX_BANDS; ++band) {
@@ -1092,19 +1096,38 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     // the levels of every band in one pass over the voxels, then the distance
     // transforms band by band
     if (e == cudaSuccess)
-        e = dev::launch_majorant_levels(w->params, d_scales, b, level, cells, cost, bounds, s);
+        e = dev::launch_majorant_levels(w->params, d_scales, b, level, cells, cost, bounds, d_hist, s);
+    // the levels worth a distance transform: those the cells actually have, at
+    // most MAJORANT_MAX_CANDIDATES per band (the most populated, and the
+    // emptiest one for the body box); any subset gives a valid grid
+    std::vector<unsigned int> hist(static_cast<size_t>(b.bands) * 64, 0u);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hist.data(), d_hist, hist.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
     for (int band = 0; band < b.bands && e == cudaSuccess; ++band) {
+        std::vector<std::pair<unsigned int, int>> present; // (cells, level)
+        for (int lv = 1; lv <= MAJORANT_MAX_LEVEL; ++lv)
+            if (hist[static_cast<size_t>(band) * 64 + lv])
+                present.emplace_back(hist[static_cast<size_t>(band) * 64 + lv], lv);
+        std::sort(present.begin(), present.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+        uint64_t chosen = 0;
+        if (floor_level[band] >= 1 && hist[static_cast<size_t>(band) * 64 + floor_level[band]])
+            chosen |= 1ull << floor_level[band];
+        for (const auto& pr : present)
+            if (static_cast<int>(__builtin_popcountll(chosen)) < MAJORANT_MAX_CANDIDATES)
+                chosen |= 1ull << pr.second;
         b.band = band;
         b.mu_ref = lut->mu_ref[band];
         for (int lv = 1; lv <= MAJORANT_MAX_LEVEL && e == cudaSuccess; ++lv)
-            if (levels[band] >> lv & 1ull)
+            if (chosen >> lv & 1ull)
                 e = dev::launch_majorant_level_pass(b, level + static_cast<size_t>(band) * ncell, lv, d0, d1, cells,
                     cost + static_cast<size_t>(band) * ncell, s);
     }
     if (e == cudaSuccess && use_box)
         e = dev::launch_majorant_box(b, bounds, cells, box, s);
     for (void* ptr : { static_cast<void*>(level), static_cast<void*>(d0), static_cast<void*>(d1), static_cast<void*>(cost),
-             static_cast<void*>(bounds), static_cast<void*>(d_scales) })
+             static_cast<void*>(bounds), static_cast<void*>(d_scales), static_cast<void*>(d_hist) })
         if (ptr)
             cudaFreeAsync(ptr, s);
     if (e != cudaSuccess) {

@@ -50,11 +50,15 @@ __device__ __forceinline__ float level_scale(int level, int per_octave)
 // scales (per palette entry, or r_m per material for the 8-byte layout); level
 // and cost are bands x ncell, cells ncell x bands.
 __global__ void majorant_level_kernel(WorldParams w, const float* __restrict__ scales, MajorantBuild b,
-    uint8_t* __restrict__ level, float2* __restrict__ cells, float* __restrict__ cost, int* __restrict__ bounds)
+    uint8_t* __restrict__ level, float2* __restrict__ cells, float* __restrict__ cost, int* __restrict__ bounds,
+    unsigned int* __restrict__ hist)
 {
     __shared__ float scale_table[MAJORANT_MAX_BANDS * PALETTE_MAX];
+    __shared__ unsigned int shist[MAJORANT_MAX_BANDS * 64];
     for (int i = threadIdx.x; i < b.bands * PALETTE_MAX; i += blockDim.x)
         scale_table[i] = scales[i];
+    for (int i = threadIdx.x; i < MAJORANT_MAX_BANDS * 64; i += blockDim.x)
+        shist[i] = 0u;
     __syncthreads();
     const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
     for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < ncell;
@@ -105,6 +109,7 @@ __global__ void majorant_level_kernel(WorldParams w, const float* __restrict__ s
                     --lv;
             }
             level[k * ncell + c] = static_cast<uint8_t>(lv);
+            atomicAdd(&shist[k * 64 + lv], 1u);
             cells[c * b.bands + k] = make_float2(1.0f, INFINITY); // the global majorant until a level does better
             cost[k * ncell + c] = b.mu_refs[k];
             above = above || (b.floor_levels[k] >= 0 && lv < b.floor_levels[k]);
@@ -127,6 +132,10 @@ __global__ void majorant_level_kernel(WorldParams w, const float* __restrict__ s
             }
         }
     }
+    __syncthreads();
+    for (int i = threadIdx.x; i < b.bands * 64; i += blockDim.x)
+        if (shist[i])
+            atomicAdd(hist + i, shist[i]);
 }
 
 __global__ void majorant_box_kernel(MajorantBuild b, const int* __restrict__ bounds, float2* __restrict__ cells, float* __restrict__ box)
@@ -279,10 +288,10 @@ int grid_for(uint64_t n)
 } // namespace
 
 cudaError_t launch_majorant_levels(const WorldParams& w, const float* scales, const MajorantBuild& b,
-    uint8_t* level, float2* cells, float* cost, int* bounds, cudaStream_t stream)
+    uint8_t* level, float2* cells, float* cost, int* bounds, unsigned int* hist, cudaStream_t stream)
 {
     const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
-    majorant_level_kernel<<<grid_for(ncell), 256, 0, stream>>>(w, scales, b, level, cells, cost, bounds);
+    majorant_level_kernel<<<grid_for(ncell), 256, 0, stream>>>(w, scales, b, level, cells, cost, bounds, hist);
     return cudaGetLastError();
 }
 

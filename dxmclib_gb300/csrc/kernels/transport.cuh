@@ -188,9 +188,10 @@ struct MajorantBuild {
     float lower[3];      // grid corner (mm)
 };
 // All bands in one pass: scales is bands x PALETTE_MAX floats in device memory;
-// level and cost are bands x ncell.
+// level and cost are bands x ncell; hist (bands x 64, zeroed by the caller)
+// counts the cells of each level.
 cudaError_t launch_majorant_levels(const WorldParams& w, const float* scales, const MajorantBuild& b,
-    uint8_t* level, float2* cells, float* cost, int* bounds, cudaStream_t stream);
+    uint8_t* level, float2* cells, float* cost, int* bounds, unsigned int* hist, cudaStream_t stream);
 // After all bands: writes the box (mm) of the cells that lay above their band's
 // emptiest level (bounds: cell index min x, y, z, max x, y, z; set up as empty
 // by the caller) and marks every cell outside it by negating its R in all bands.
