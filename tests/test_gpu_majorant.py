@@ -39,42 +39,39 @@ def _voxel_scales(world, blob, e_lo, e_hi):
     return s.reshape(d[2], d[1], d[0])
 
 
-def test_majorant_grid_bounds_attenuation(gpu_ctx):
+def _check_grid_bounds(dworld, dlut, world, blob, expect_air=True):
+    """Every cell's (1 / s, R) per band bounds the attenuation of every voxel within
+    R, and every voxel outside the body box lies within the majorant of every cell
+    marked outside it."""
     from scipy import ndimage
-    import dxmclib_gb300 as dx
-    world = _phantom()
-    dworld = dx.DeviceWorld(gpu_ctx, world)
-    dlut = dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, 120.0))
-    dworld.prepare(dlut)
     shift, edges, box, cells = dworld.majorant(dlut)
     assert cells.shape[3] == len(edges) + 1 >= 4 and np.all(np.diff(edges) > 0)
-    blob = dx.LutBlob.from_world(world, 120.0)
-    bounds = [1.0, *edges, 120.0]
+    bounds = [1.0, *edges, blob.info()["max_energy"]]
     sp = np.array(world.spacing())[::-1]  # (z, y, x) mm
     b = [1 << int(shift[2]), 1 << int(shift[1]), 1 << int(shift[0])]
+    d = world.dimensions()
+    zc, yc, xc = np.meshgrid(*[(np.arange(d[i]) + 0.5) * world.spacing()[i] for i in (2, 1, 0)], indexing="ij")
+    lower = [-0.5 * d[i] * world.spacing()[i] + world.origin()[i] for i in range(3)]
+    pos = [xc + lower[0], yc + lower[1], zc + lower[2]]
     checked = 0
     for band in range(cells.shape[3]):
         scale = _voxel_scales(world, blob, bounds[band] * 1.0001, bounds[band + 1] * 0.9999)
         s_cell = 1.0 / cells[..., band, 0].astype(np.float64)
         R_signed = cells[..., band, 1].astype(np.float64)
         R_cell = np.abs(R_signed)
-        # cells marked outside the box (R < 0) may fly to the box along their ray: every
-        # voxel outside the box must then lie within the majorant of every marked cell
-        d = world.dimensions()
-        zc, yc, xc = np.meshgrid(*[(np.arange(d[i]) + 0.5) * world.spacing()[i] for i in (2, 1, 0)], indexing="ij")
-        lower = [-0.5 * d[i] * world.spacing()[i] + world.origin()[i] for i in range(3)]
-        pos = [xc + lower[0], yc + lower[1], zc + lower[2]]
-        out_box = np.zeros(scale.shape, bool)
-        for a in range(3):
-            out_box |= (pos[a] < box[a]) | (pos[a] > box[3 + a])
-        marked = R_signed < 0
-        assert marked.any() and (~marked).any()
-        assert scale[out_box].max() <= s_cell[marked].min() * (1.0 + 1e-4), (band, scale[out_box].max(), s_cell[marked].min())
         assert np.all(s_cell <= 1.0 + 1e-6)
-        # the grid is worth having: air cells far from the body get small scales and long flights
-        assert (s_cell < 0.01).mean() > 0.05, np.unique(s_cell)
-        assert np.nanmax(np.where(s_cell < 0.01, R_cell, np.nan)) > 30.0
-        # soft tissue gets a level well below the bone-set majorant
+        marked = R_signed < 0
+        if marked.any():
+            out_box = np.zeros(scale.shape, bool)
+            for a in range(3):
+                out_box |= (pos[a] < box[a]) | (pos[a] > box[3 + a])
+            assert scale[out_box].max() <= s_cell[marked].min() * (1.0 + 1e-4), (band, scale[out_box].max(), s_cell[marked].min())
+        if expect_air:
+            # air cells far from the body get small scales and long flights
+            assert (s_cell < 0.01).mean() > 0.05, np.unique(s_cell)
+            assert np.nanmax(np.where(s_cell < 0.01, R_cell, np.nan)) > 30.0
+            assert marked.any() and (~marked).any()
+        # some cells get a level well below the global majorant
         assert np.any((s_cell > 0.05) & (s_cell < 0.7)), np.unique(s_cell)
         for s in np.unique(s_cell[np.isfinite(R_cell)]):
             hot = scale > s * (1.0 + 1e-4)
@@ -91,6 +88,71 @@ def test_majorant_grid_bounds_attenuation(gpu_ctx):
             assert not bad.any(), (band, s, int(bad.sum()), R_cell[bad][:5], cell_gap[bad][:5])
             checked += int(sel.sum())
     assert checked > 0
+
+
+def test_majorant_grid_bounds_attenuation(gpu_ctx):
+    import dxmclib_gb300 as dx
+    world = _phantom()
+    dworld = dx.DeviceWorld(gpu_ctx, world)
+    dlut = dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, 120.0))
+    dworld.prepare(dlut)
+    _check_grid_bounds(dworld, dlut, world, dx.LutBlob.from_world(world, 120.0))
+    dlut.close()
+    dworld.close()
+
+
+def _continuous_world(n=48, distinct=None, seed=3):
+    """Soft tissue and bone with densities from a smooth field: ``distinct`` density
+    values (compact layout, many levels per band) or all different (8-byte layout)."""
+    import dxmclib_gb300 as dx
+    rng = np.random.default_rng(seed)
+    z, y, x = np.meshgrid(*[np.linspace(-1, 1, n)] * 3, indexing="ij")
+    field = 0.05 + 1.9 * np.clip(0.5 + 0.5 * np.sin(3 * x + rng.uniform(0, 3)) * np.cos(2 * y) * np.cos(z), 0, 1)
+    if distinct:
+        field = np.round(field * distinct / 2.0) * 2.0 / distinct + 0.001
+    mat = (field > 1.3).astype(np.uint8)
+    w = dx.World()
+    w.setDimensions((n, n, n))
+    w.setSpacing((3.0, 3.0, 3.0))
+    w.setDensityArray(field.astype(np.float32).ravel())
+    w.setMaterialIndexArray(mat.ravel())
+    w.addMaterialToMap(dx.Material("Tissue, Soft (ICRP)"))
+    w.addMaterialToMap(dx.Material("Bone, Cortical (ICRP)"))
+    assert w.isValid()
+    return w
+
+
+@pytest.mark.parametrize("distinct", [120, None])
+def test_many_levels_grid_bounds_and_parity(gpu_ctx, distinct):
+    """Worlds with many density values (120 in the compact layout, all different in
+    the 8-byte layout) have many majorant levels per band; the grid keeps at most
+    12 distance transforms per band and must still bound the attenuation, and both
+    tracking modes must agree."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    world = _continuous_world(distinct=distinct)
+    dworld = dx.DeviceWorld(gpu_ctx, world)
+    blob = dx.LutBlob.from_world(world, 90.0)
+    dlut = dx.DeviceLut(gpu_ctx, blob)
+    dworld.prepare(dlut)
+    _check_grid_bounds(dworld, dlut, world, blob, expect_air=False)
+    src = dx.DXSource()
+    src.tube().setVoltage(90)
+    src.tube().setAlFiltration(3.0)
+    src.setFieldSize((150, 150))
+    src.setHistoriesPerExposure(2_000_000)
+    src.setTotalExposures(2)
+    ex = src.exposures(world.directionCosines())
+    out = {}
+    for mode in (A.TRACKING_GLOBAL, A.TRACKING_LOCAL):
+        job = dx.Job(gpu_ctx, dworld, dlut, ex, src.spectrum(), src.heel(), None, seed=41 + mode, model=1, tracking=mode)
+        out[mode] = job.result(A.OUTPUT_EV_PER_HISTORY)
+        job.close()
+    dg, vg = out[A.TRACKING_GLOBAL][:2]
+    dl, vl, _, sl = out[A.TRACKING_LOCAL]
+    ref = dict(idx=np.arange(dg.size), dose=dg, var=vg, total=np.array([dg.sum()]))
+    assert_parity(compare_sparse(ref, dl, vl), f"many levels ({distinct}), local vs global")
+    assert sl["steps"] < out[A.TRACKING_GLOBAL][3]["steps"]
     dlut.close()
     dworld.close()
 
