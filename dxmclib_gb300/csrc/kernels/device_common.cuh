@@ -154,10 +154,11 @@ struct Rng {
         s3 = __funnelshift_l(s3, s3, 11);
         return result;
     }
-    // [0, 1) with 24 random bits
-    __device__ __forceinline__ float uniform() { return static_cast<float>(next() >> 8) * 0x1p-24f; }
-    // (0, 1] for logarithms
-    __device__ __forceinline__ float uniform_open() { return static_cast<float>((next() >> 8) + 1u) * 0x1p-24f; }
+    // [0, 1) with 23 random bits: the top bits as the mantissa of a float in [1, 2),
+    // minus one (no integer-to-float conversion)
+    __device__ __forceinline__ float uniform() { return __uint_as_float(0x3f800000u | (next() >> 9)) - 1.0f; }
+    // (0, 1] for logarithms: two minus a float in [1, 2)
+    __device__ __forceinline__ float uniform_open() { return 2.0f - __uint_as_float(0x3f800000u | (next() >> 9)); }
     // integer in [0, n) by the multiply-high method (Lemire)
     __device__ __forceinline__ uint32_t below(uint32_t n) { return __umulhi(next(), n); }
     // azimuth uniform in [-pi, pi)
