@@ -141,7 +141,7 @@ struct Rng {
         s3 = r.w | 1u; // the all-zero state is excluded
     }
     // the sum output of xoshiro128+: its lowest bits are weak, and every use
-    // takes the high bits (24-bit floats, multiply-high integers)
+    // takes the high bits (23-bit float mantissas, multiply-high integers)
     __device__ __forceinline__ uint32_t next()
     {
         const uint32_t result = s0 + s3;
