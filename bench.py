@@ -69,20 +69,27 @@ def replica_throughput(ws: int, histories_per_step: int, steps: int, seconds_max
 
 
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+    """Samples nvidia-smi clocks and throttle reasons (every 50 ms, time-stamped by
+    nvidia-smi).  Started before the warm-up so that the sampler is running when
+    the timed region begins; mark() / done() bracket the timed region, and the
+    summary uses the samples inside it (or the nearest one if the region is
+    shorter than the interval)."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device: int):
         self.device = device
         self.samples = []
         self._proc = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
-        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-             "clocks_event_reasons.sw_power_cap")
         try:
-            self._proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200",
-                                           "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                           "-lms", "50", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                          stderr=subprocess.DEVNULL, text=True)
             self._thread = threading.Thread(target=self._read, daemon=True)
             self._thread.start()
         except Exception:
@@ -90,8 +97,21 @@ class ClockSampler:
         return self
 
     def _read(self):
+        import datetime
         for line in self._proc.stdout:
-            self.samples.append([x.strip() for x in line.split(",")])
+            f = [x.strip() for x in line.split(",")]
+            try:
+                t = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                t = None
+            self.samples.append((t, f[1:]))
+
+    def mark(self):
+        self.t0 = time.time()
+
+    def done(self):
+        self.t1 = time.time()
+        time.sleep(0.12)  # let the sample that follows the region arrive
 
     def __exit__(self, *a):
         if self._proc:
@@ -104,17 +124,20 @@ class ClockSampler:
     def summary(self):
         if not self.samples:
             return None
-        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        inside = [f for t, f in self.samples if t is not None and self.t0 is not None and self.t0 - 0.025 <= t <= self.t1 + 0.025]
+        if not inside:  # region shorter than the interval: the sample nearest to it
+            timed = [(abs(t - 0.5 * (self.t0 + self.t1)), f) for t, f in self.samples if t is not None and self.t0 is not None]
+            inside = [min(timed, key=lambda x: x[0])[1]] if timed else [self.samples[-1][1]]
+        sm = [float(s[1]) for s in inside if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in inside if s[2].replace(".", "").isdigit()]
         reasons = set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for s in self.samples:
+        for s in inside:
             for i, n in enumerate(names):
                 if len(s) > 5 + i and s[5 + i].lower() == "active":
                     reasons.add(n)
-        loaded = sorted(sm)[len(sm) // 2:] if sm else []
-        return {"sm_mhz": float(np.median(loaded)) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.samples)}
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(inside)}
 
 
 def measured_peaks():
@@ -497,16 +520,18 @@ def main():
         flush.fill_(1)
         torch.cuda.synchronize()
 
-    for w in range(args.warmup):
-        flush_l2()
-        run_job(1000 + w)
-    barrier()
     with ClockSampler(device) as clocks:
+        for w in range(args.warmup):
+            flush_l2()
+            run_job(1000 + w)
+        barrier()
+        clocks.mark()
         stats = []
         for step in range(args.steps):
             flush_l2()
             stats.append(run_job(2000 + step))
         barrier()
+        clocks.done()
     job_ms = np.array([s.job_ms for s in stats])
     kern_ms = np.array([s.kernel_ms for s in stats])
     total_ms = max_over_ranks(float(job_ms.sum()), dist)
