@@ -14,7 +14,7 @@ struct PaletteEntry {
 constexpr int PALETTE_MAX = 256;
 
 struct WorldParams {
-    const Voxel* voxels;            // 8-byte layout (always present)
+    const Voxel* voxels;            // 8-byte layout, or nullptr when the compact layout is used
     const uint8_t* palette_index;   // 1-byte layout, or nullptr when the world has > 256 distinct voxels
     const PaletteEntry* palette;    // PALETTE_MAX entries
     int palette_n;
