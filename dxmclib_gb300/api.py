@@ -381,6 +381,28 @@ class Source:
     def exposures(self, world_cosines=(1, 0, 0, 0, 1, 0)) -> ExposureTable:
         raise NotImplementedError
 
+    def _memo_exposures(self, world_cosines, build):
+        """The exposure table for the source's current settings: built by ``build()``
+        once and returned as a copy while no setting (or the world's cosines)
+        changes.  Thousands of CT exposures cost about a millisecond to rebuild."""
+        def norm(v):
+            if isinstance(v, np.ndarray):
+                return (v.dtype.str, v.shape, v.tobytes())
+            if isinstance(v, (tuple, list)):
+                return tuple(norm(x) for x in v)
+            if v is None or isinstance(v, (bool, int, float, str, np.generic)):
+                return v
+            return ("object", id(v))
+        key = (norm(tuple(np.asarray(world_cosines, np.float64).ravel())),
+               tuple((k, norm(v)) for k, v in sorted(vars(self).items()) if k not in ("_exposure_memo", "_tube")))
+        memo = getattr(self, "_exposure_memo", None)
+        if memo is None or memo[0] != key:
+            memo = (key, build())
+            self._exposure_memo = memo
+        t = memo[1]
+        return ExposureTable(t.position.copy(), t.cosines.copy(), t.beam_direction.copy(), t.collimation.copy(),
+                             t.weight.copy(), t.n_histories.copy(), t.mono_energy.copy())
+
     def spectrum(self) -> Optional[Spectrum]:
         return None
 
@@ -751,6 +773,9 @@ class CTSpiralSource(Source):
         return cal.ctdi_factor(world, dose, self._collimation, self.ctdiVol(), mean_weight) * self._pitch
 
     def exposures(self, world_cosines=(1, 0, 0, 0, 1, 0)):
+        return self._memo_exposures(world_cosines, lambda: self._build_exposures(world_cosines))
+
+    def _build_exposures(self, world_cosines):
         n = self.totalExposures()
         idx = np.arange(n, dtype=np.float64)
         pos0 = np.array([0.0, -self._sdd / 2, 0.0])
