@@ -134,8 +134,11 @@ def test_autotuned_launch_gives_identical_results(gpu_ctx, tmp_path):
     again = Autotuner(ctx, cache_file=str(tmp_path / "tune.json"))
     assert again.tune_job(wl.world, dworld, dlut, ex, None, None, None, 1, src.maxPhotonEnergyProduced()) == res
     outs = []
+    # in-kernel generation and the pre-generated photon queue (two chunks), other
+    # thresholds, bursts and block sizes: the same histories
     for launch in (None, res["launch"], {"queue_log2_chunk": -1, "regen_threshold": 16, "interact_threshold": 4,
-                                          "blocks_per_sm": 2}):
+                                          "blocks_per_sm": 2},
+                   {"queue_log2_chunk": 18, "woodcock_burst": 9, "block_size": 128}):
         job = dx.Job(ctx, dworld, dlut, ex, src.spectrum(), src.heel(), src.bowtie(), seed=5, model=1, launch=launch)
         outs.append(job.result(A.OUTPUT_RAW))
         job.close()
