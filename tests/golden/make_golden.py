@@ -121,7 +121,7 @@ def gen_sources(out: Path):
 
 def gen_transport(out: Path, quick: bool):
     scale = 0.1 if quick else 1.0
-    # pencil 60 keV in a 64^3 water cube of 2 mm voxels (spec configuration 1)
+    # pencil 60 keV in a 64^3 water cube of 2 mm voxels (the small pencil-beam workload)
     n = 64
     dims = (n, n, n)
     w = R.WorldArgs(dims, (2.0, 2.0, 2.0), np.ones(n ** 3), np.zeros(n ** 3, np.uint8), ["Water, Liquid"])
