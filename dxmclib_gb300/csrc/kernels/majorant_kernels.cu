@@ -8,20 +8,22 @@
 // lets the transport kernel use a smaller majorant where the neighbourhood of a
 // photon allows it (see MajorantGrid in transport.cuh):
 //
-//   1. every voxel gets a scale s_v = density * r_m, with r_m the largest ratio
-//      of material m's attenuation to the global majorant over the LUT's energy
-//      range (1 for voxels of forced-interaction scoring, which keep the
-//      reference's majorant); each cell takes the maximum over its voxels,
-//      rounded up to a level 2^(-level / levels_per_octave);
-//   2. for each level present, the cells above it are dilated by one cell and a
+//   1. per energy band, every voxel gets a scale s_v = density * r_m, with r_m
+//      the largest ratio of material m's attenuation to the global majorant
+//      over the band's energies (1 for voxels of forced-interaction scoring,
+//      which keep the reference's majorant); each cell takes the maximum over
+//      its voxels, rounded up to a level 2^(-level / levels_per_octave) (one
+//      pass over the voxels for all bands, with a histogram of the levels);
+//   2. for each level the cells have (the host picks at most a dozen per band
+//      from the histogram), the cells above it are dilated by one cell and a
 //      Euclidean distance transform (three separable passes over the cell grid,
-//      cell sizes in mm) gives every other cell the distance R to the nearest
-//      point of a cell above the level: a flight of length at most R from
-//      anywhere in the cell stays where the level's scale bounds the attenuation;
+//      cell sizes in mm: row sweeps along x, scans along y and z) gives every
+//      other cell the distance R to the nearest point of a cell above the
+//      level: a flight of length at most R from anywhere in the cell stays
+//      where the level's scale bounds the attenuation;
 //   3. each cell keeps the (level, R) of smallest expected steps per mm,
-//      mu / (1 - exp(-mu R)) with mu = scale * global majorant at a reference
-//      energy, or the global majorant itself (R infinite).
-// The three steps run once per energy band, with the ratios r_m of that band.
+//      mu / (1 - exp(-mu R)) with mu = scale * global majorant at the band's
+//      reference energy, or the global majorant itself (R infinite).
 // Last, the cells outside the box of all cells above their band's emptiest
 // level get -R: there a flight may also run to that box (MajorantGrid).
 #include <algorithm>
