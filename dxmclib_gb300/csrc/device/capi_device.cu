@@ -71,15 +71,17 @@ struct dxmc_gpu_ctx {
     uint64_t budget = 0;
     uint64_t in_use = 0;
     size_t max_smem_optin = 0;
+    uint64_t submission = 0; // counts the calls that may build grids (job, batch, world prepare)
 };
 
-// Local-majorant grid of the world for one LUT (built on first use, kept until
-// the world is freed; see MajorantGrid).
+// Local-majorant grid of the world for one LUT (built on first use; the least
+// recently used one is freed when a world holds too many; see MajorantGrid).
 struct MajorantCache {
     uint64_t lut_serial = 0;
     float2* cells = nullptr;
     uint64_t bytes = 0;
     uint64_t last_use = 0;
+    uint64_t submission = 0; // the last submission whose jobs read it
     dev::MajorantGrid grid {};
 };
 
@@ -747,6 +749,7 @@ int dxmc_gpu_world_prepare(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut*
     if (world->ctx != ctx || lut->ctx != ctx)
         return fail(ctx, DXMC_ERR_INVALID, "world or lut belongs to another context");
     cudaSetDevice(ctx->device);
+    ++ctx->submission; // no job of this call holds a grid: every grid but the new one may go
     const dev::MajorantGrid* grid = nullptr;
     const int rc = world_majorant(ctx, world, lut, true, &grid);
     if (rc != DXMC_OK)
@@ -971,12 +974,15 @@ int majorant_level(float m)
 
 // The local-majorant grid of (world, lut): found in the world's cache, else (if
 // build) built on the context stream and cached.  Caller holds the context mutex.
+// A grid that a job of the current submission (ctx->submission) copied into its
+// parameters is not evicted before that submission has launched.
 int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool build, const dev::MajorantGrid** out)
 {
     *out = nullptr;
     for (auto& m : w->majorants) {
         if (m.lut_serial == lut->serial) {
             m.last_use = ++w->majorant_clock;
+            m.submission = ctx->submission;
             *out = &m.grid;
             return DXMC_OK;
         }
@@ -1049,9 +1055,15 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     const uint64_t cell_bytes = ncell * b.bands * sizeof(float2) + 8 * sizeof(float); // + the box
     if (ctx->in_use + cell_bytes > ctx->budget)
         return fail(ctx, DXMC_ERR_OOM, "local-majorant grid exceeds the device memory budget");
-    if (w->majorants.size() >= MAJORANT_GRIDS_PER_WORLD) {
-        auto victim = std::min_element(w->majorants.begin(), w->majorants.end(),
-            [](const MajorantCache& a, const MajorantCache& c) { return a.last_use < c.last_use; });
+    // least recently used first, never a grid the current submission reads
+    // (the cache may then hold more grids until a later submission)
+    while (w->majorants.size() >= MAJORANT_GRIDS_PER_WORLD) {
+        auto victim = w->majorants.end();
+        for (auto it = w->majorants.begin(); it != w->majorants.end(); ++it)
+            if (it->submission != ctx->submission && (victim == w->majorants.end() || it->last_use < victim->last_use))
+                victim = it;
+        if (victim == w->majorants.end())
+            break;
         sync_ctx_streams(ctx); // no queued job still reads the grid
         cudaFreeAsync(victim->cells, ctx->stream);
         ctx->in_use -= victim->bytes;
@@ -1141,6 +1153,7 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     m.cells = cells;
     m.bytes = cell_bytes;
     m.last_use = ++w->majorant_clock;
+    m.submission = ctx->submission;
     m.grid.cells = cells;
     m.grid.box = box;
     m.grid.nx = b.n[0];
@@ -1513,6 +1526,7 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
     if (!ctx || !world || !lut || !jd || !out)
         return DXMC_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mutex);
+    ++ctx->submission;
     dev::TransportParams p {};
     uint64_t chunk = 0;
     dxmc_job* j = nullptr;
@@ -1783,6 +1797,7 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
     const bool persistent = mode == DXMC_BATCH_PERSISTENT;
     const int chains = std::clamp(opt && opt->chains > 0 ? opt->chains : DEFAULT_CHAINS, 1, MAX_CHAINS);
     std::lock_guard<std::mutex> lock(ctx->mutex);
+    ++ctx->submission; // the grids of every entry stay until the batch has launched
     cudaSetDevice(ctx->device);
     BatchEngines* en = engines_of(ctx, true);
     if (!en)

@@ -161,9 +161,18 @@ __global__ void majorant_box_kernel(MajorantBuild b, const int* __restrict__ bou
         bool outside = empty;
         for (int a = 0; a < 3; ++a)
             outside = outside || static_cast<int>(q[a]) < lo[a] || static_cast<int>(q[a]) > hi[a];
-        if (outside)
-            for (int k = 0; k < b.bands; ++k)
-                cells[c * b.bands + k].y = -cells[c * b.bands + k].y;
+        if (!outside)
+            continue;
+        for (int k = 0; k < b.bands; ++k) {
+            // every cell outside the box lies at or below the band's emptiest level: a
+            // flight may run to the box with the cell's scale only if that scale is at
+            // least the emptiest level's (the host finds that level in double
+            // arithmetic, the cells' levels here in float, which may differ by one)
+            const int fl = b.floor_levels[k];
+            float2& cell = cells[c * b.bands + k];
+            if (fl >= 0 && cell.x <= 1.0f / level_scale(fl, b.levels_per_octave))
+                cell.y = -cell.y;
+        }
     }
 }
 

@@ -279,3 +279,57 @@ def test_majorant_grids_per_world_are_evicted_and_accounted(gpu_ctx):
         dlut.close()
     _, after = gpu_ctx.memory()
     assert after == before
+
+
+@pytest.mark.parametrize("mode", ["concurrent", "persistent"])
+def test_batch_keeps_the_grids_of_all_its_entries(gpu_ctx, mode):
+    """A batch whose entries use one world with more LUTs than a world caches
+    grids for: no entry's grid is evicted before the batch has launched, so every
+    entry equals its job run alone; the next grid built outside the batch trims
+    the cache back to four grids, and freeing the world returns every grid's bytes."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    from dxmclib_gb300.workloads import ct_source
+    world = _phantom()
+    src = ct_source(world, 150_000)
+    ex = src.exposures(world.directionCosines())
+    _, before = gpu_ctx.memory()
+    dworld = dx.DeviceWorld(gpu_ctx, world)
+    _, with_world = gpu_ctx.memory()
+    luts = [dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, e)) for e in (120.0, 121.0, 122.0, 123.0, 124.0, 125.0)]
+    extra = dx.DeviceLut(gpu_ctx, dx.LutBlob.from_world(world, 126.0))
+    _, with_luts = gpu_ctx.memory()
+    alone = []
+    for dlut in luts:  # leaves the grids of the last four LUTs cached
+        job = dx.Job(gpu_ctx, dworld, dlut, ex, src.spectrum(), src.heel(), None, seed=5, model=1)
+        alone.append(job.result(A.OUTPUT_RAW))
+        job.close()
+    _, four = gpu_ctx.memory()
+    grid_bytes = (four - with_luts) // 4
+    assert grid_bytes > 0 and four == with_luts + 4 * grid_bytes
+    batch = dx.Batch(gpu_ctx, [dx.BatchEntry(dworld, dlut, ex, src.spectrum(), src.heel(), None, 5, 1) for dlut in luts],
+                     mode=dx.Batch.CONCURRENT if mode == "concurrent" else dx.Batch.PERSISTENT)
+    assert batch.wait() == A.DXMC_OK
+    for i, (e_a, e2_a, nev_a, st_a) in enumerate(alone):
+        e_b, e2_b, nev_b, st_b = batch.jobs[i].result(A.OUTPUT_RAW)
+        assert st_b["histories"] == st_a["histories"] and st_b["steps"] == st_a["steps"], i
+        np.testing.assert_allclose(e_b, e_a, rtol=1e-9, atol=1e-12 * e_a.max(), err_msg=str(i))
+        np.testing.assert_array_equal(nev_b, nev_a, err_msg=str(i))
+    batch.close()
+    for dlut in luts:  # two grids rebuilt, none evicted inside the batch
+        dworld.majorant(dlut)
+    # (the batch engines' buffers stay allocated: compare differences from here on)
+    _, six = gpu_ctx.memory()
+    dworld.prepare(extra)
+    _, trimmed = gpu_ctx.memory()
+    assert six - trimmed == 2 * grid_bytes  # three evicted, one built
+    with pytest.raises(A.DxmcError):
+        dworld.majorant(luts[0])
+    dworld.majorant(extra)
+    dworld.close()
+    _, after_world = gpu_ctx.memory()
+    assert trimmed - after_world == (with_world - before) + 4 * grid_bytes
+    for dlut in luts + [extra]:
+        dlut.close()
+    _, after = gpu_ctx.memory()
+    assert after_world - after == with_luts - with_world
