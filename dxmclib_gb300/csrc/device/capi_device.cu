@@ -959,6 +959,8 @@ constexpr int MAJORANT_MAX_LEVEL = MAJORANT_LEVELS_PER_OCTAVE * 12 < 63 ? MAJORA
 constexpr uint64_t MAJORANT_MAX_CELLS_PER_AXIS = 1024;
 constexpr size_t MAJORANT_GRIDS_PER_WORLD = 4;    // one per LUT used with the world, least recently used evicted
 constexpr int MAJORANT_MAX_CANDIDATES = 12;       // distance transforms per band at most
+constexpr size_t MAJORANT_SCRATCH_BYTES = 512ull << 20; // distance-transform scratch of one group of levels
+static_assert(MAJORANT_MAX_CANDIDATES * dev::MAJORANT_MAX_BANDS <= dev::MAJORANT_MAX_PAIRS, "pair table too small");
 
 int majorant_level(float m)
 {
@@ -1086,10 +1088,6 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     if (e == cudaSuccess)
         e = pool_alloc(ctx, &level, ncell * b.bands, s);
     if (e == cudaSuccess)
-        e = pool_alloc(ctx, &d0, ncell * sizeof(float), s);
-    if (e == cudaSuccess)
-        e = pool_alloc(ctx, &d1, ncell * sizeof(float), s);
-    if (e == cudaSuccess)
         e = pool_alloc(ctx, &cost, ncell * b.bands * sizeof(float), s);
     if (e == cudaSuccess)
         e = pool_alloc(ctx, &d_scales, scales.size() * sizeof(float), s);
@@ -1117,6 +1115,7 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
         e = cudaMemcpyAsync(hist.data(), d_hist, hist.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(s);
+    std::vector<std::pair<int, int>> pairs; // (band, level), band-major, levels ascending
     for (int band = 0; band < b.bands && e == cudaSuccess; ++band) {
         std::vector<std::pair<unsigned int, int>> present; // (cells, level)
         for (int lv = 1; lv <= MAJORANT_MAX_LEVEL; ++lv)
@@ -1126,15 +1125,37 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
         uint64_t chosen = 0;
         if (floor_level[band] >= 1 && hist[static_cast<size_t>(band) * 64 + floor_level[band]])
             chosen |= 1ull << floor_level[band];
+        int n_chosen = __builtin_popcountll(chosen);
         for (const auto& pr : present)
-            if (static_cast<int>(__builtin_popcountll(chosen)) < MAJORANT_MAX_CANDIDATES)
+            if (n_chosen < MAJORANT_MAX_CANDIDATES && !(chosen >> pr.second & 1ull)) {
                 chosen |= 1ull << pr.second;
-        b.band = band;
-        b.mu_ref = lut->mu_ref[band];
-        for (int lv = 1; lv <= MAJORANT_MAX_LEVEL && e == cudaSuccess; ++lv)
+                ++n_chosen;
+            }
+        for (int lv = 1; lv <= MAJORANT_MAX_LEVEL; ++lv)
             if (chosen >> lv & 1ull)
-                e = dev::launch_majorant_level_pass(b, level + static_cast<size_t>(band) * ncell, lv, d0, d1, cells,
-                    cost + static_cast<size_t>(band) * ncell, s);
+                pairs.emplace_back(band, lv);
+    }
+    // the distance transforms of many pairs run as one launch per pass, in groups
+    // whose two scratch grids stay within MAJORANT_SCRATCH_BYTES
+    const size_t group = std::clamp<size_t>(MAJORANT_SCRATCH_BYTES / (2 * ncell * sizeof(float)), 1,
+        std::min<size_t>(std::max<size_t>(pairs.size(), 1), dev::MAJORANT_MAX_PAIRS));
+    if (e == cudaSuccess && !pairs.empty())
+        e = pool_alloc(ctx, &d0, group * ncell * sizeof(float), s);
+    if (e == cudaSuccess && !pairs.empty())
+        e = pool_alloc(ctx, &d1, group * ncell * sizeof(float), s);
+    for (size_t g0 = 0; g0 < pairs.size() && e == cudaSuccess; g0 += group) {
+        dev::MajorantPairs pg {};
+        pg.count = static_cast<int>(std::min(group, pairs.size() - g0));
+        for (int i = 0; i < pg.count; ++i) {
+            pg.band[i] = static_cast<uint8_t>(pairs[g0 + i].first);
+            pg.level[i] = static_cast<uint8_t>(pairs[g0 + i].second);
+        }
+        for (int band = 0, i = 0; band <= dev::MAJORANT_MAX_BANDS; ++band) {
+            while (i < pg.count && pg.band[i] < band)
+                ++i;
+            pg.first[band] = i;
+        }
+        e = dev::launch_majorant_level_passes(b, pg, level, d0, d1, cells, cost, s);
     }
     if (e == cudaSuccess && use_box)
         e = dev::launch_majorant_box(b, bounds, cells, box, s);

@@ -20,10 +20,13 @@
 //      cell sizes in mm: row sweeps along x, scans along y and z) gives every
 //      other cell the distance R to the nearest point of a cell above the
 //      level: a flight of length at most R from anywhere in the cell stays
-//      where the level's scale bounds the attenuation;
+//      where the level's scale bounds the attenuation.  All (band, level)
+//      pairs of a group run in one launch per pass (blockIdx.y = pair);
 //   3. each cell keeps the (level, R) of smallest expected steps per mm,
 //      mu / (1 - exp(-mu R)) with mu = scale * global majorant at the band's
-//      reference energy, or the global majorant itself (R infinite).
+//      reference energy, or the global majorant itself (R infinite); the z
+//      pass and this choice are one kernel that tries a band's levels in
+//      ascending order, so the grid does not depend on the grouping.
 // Last, the cells outside the box of all cells above their band's emptiest
 // level get -R: there a flight may also run to that box (MajorantGrid).
 #include <algorithm>
@@ -140,7 +143,7 @@ __global__ void majorant_level_kernel(WorldParams w, const float* __restrict__ s
             atomicAdd(hist + i, shist[i]);
 }
 
-__global__ void majorant_box_kernel(MajorantBuild b, const int* __restrict__ bounds, float2* __restrict__ cells, float* __restrict__ box)
+__global__ void majorant_box_kernel(const __grid_constant__ MajorantBuild b, const int* __restrict__ bounds, float2* __restrict__ cells, float* __restrict__ box)
 {
     int lo[3], hi[3];
     for (int a = 0; a < 3; ++a) {
@@ -176,10 +179,16 @@ __global__ void majorant_box_kernel(MajorantBuild b, const int* __restrict__ bou
     }
 }
 
-// d[c] = 0 where a cell of the 27-neighbourhood lies above level lv, else infinity
-__global__ void majorant_dilate_kernel(MajorantBuild b, const uint8_t* __restrict__ level, int lv, float* __restrict__ d)
+// d[p][c] = 0 where a cell of the 27-neighbourhood of c lies above pair p's
+// level in its band, else infinity (blockIdx.y = p)
+__global__ void majorant_dilate_kernel(MajorantBuild b, const __grid_constant__ MajorantPairs pairs,
+    const uint8_t* __restrict__ level, float* __restrict__ d)
 {
     const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
+    const int p = blockIdx.y;
+    const int lv = pairs.level[p];
+    const uint8_t* __restrict__ lvl = level + static_cast<uint64_t>(pairs.band[p]) * ncell;
+    float* __restrict__ out = d + static_cast<uint64_t>(p) * ncell;
     for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < ncell;
          c += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
         uint32_t cx, cy, cz;
@@ -196,66 +205,97 @@ __global__ void majorant_dilate_kernel(MajorantBuild b, const uint8_t* __restric
                 const uint64_t row = (static_cast<uint64_t>(z) * b.n[1] + y) * b.n[0];
                 for (int dx = -1; dx <= 1; ++dx) {
                     const int x = static_cast<int>(cx) + dx;
-                    if (x >= 0 && x < static_cast<int>(b.n[0]) && level[row + x] < lv) {
+                    if (x >= 0 && x < static_cast<int>(b.n[0]) && lvl[row + x] < lv) {
                         above = true;
                         break;
                     }
                 }
             }
         }
-        d[c] = above ? 0.0f : INFINITY;
+        out[c] = above ? 0.0f : INFINITY;
     }
 }
 
-// One pass of the separable squared distance transform along AXIS:
-// out[c] = min over the line through c of in[t] + ((pos - t) * edge)^2, scanned
-// outward from pos until the distance alone exceeds the best value.  The last
-// pass (CHOOSE) turns the squared distance into R and keeps the better of the
-// cell's current choice and level lv.
-template <int AXIS, bool CHOOSE>
-__global__ void majorant_axis_kernel(MajorantBuild b, const float* __restrict__ in, float* __restrict__ out, int lv,
-    float2* __restrict__ cells, float* __restrict__ cost)
+// One step of the separable squared distance transform along AXIS at cell c:
+// min over the line through c of in[t] + ((pos - t) * edge)^2, scanned outward
+// from pos until the distance alone exceeds the best value.
+template <int AXIS>
+__device__ __forceinline__ float axis_min(const MajorantBuild& b, const float* __restrict__ in, uint64_t c, int pos)
 {
-    const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
     const int n = static_cast<int>(b.n[AXIS]);
     const uint64_t stride = AXIS == 0 ? 1 : (AXIS == 1 ? b.n[0] : static_cast<uint64_t>(b.n[0]) * b.n[1]);
     const float e = b.edge[AXIS];
+    const uint64_t base = c - static_cast<uint64_t>(pos) * stride;
+    float best = in[c];
+    for (int k = 1; k < n; ++k) {
+        const float dk = static_cast<float>(k) * e;
+        const float d2 = dk * dk;
+        if (d2 >= best)
+            break;
+        const bool lo = pos - k >= 0, hi = pos + k < n;
+        if (!lo && !hi)
+            break;
+        if (lo)
+            best = fminf(best, in[base + static_cast<uint64_t>(pos - k) * stride] + d2);
+        if (hi)
+            best = fminf(best, in[base + static_cast<uint64_t>(pos + k) * stride] + d2);
+    }
+    return best;
+}
+
+// A middle pass of the distance transform for every pair (blockIdx.y = pair).
+template <int AXIS>
+__global__ void majorant_axis_kernel(MajorantBuild b, const float* __restrict__ in, float* __restrict__ out)
+{
+    const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
+    const uint64_t off = static_cast<uint64_t>(blockIdx.y) * ncell;
     for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < ncell;
          c += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
         uint32_t coord[3];
         cell_coords(c, b, coord[0], coord[1], coord[2]);
-        const int pos = static_cast<int>(coord[AXIS]);
-        const uint64_t base = c - static_cast<uint64_t>(pos) * stride;
-        float best = in[c];
-        for (int k = 1; k < n; ++k) {
-            const float dk = static_cast<float>(k) * e;
-            const float d2 = dk * dk;
-            if (d2 >= best)
-                break;
-            const bool lo = pos - k >= 0, hi = pos + k < n;
-            if (!lo && !hi)
-                break;
-            if (lo)
-                best = fminf(best, in[base + static_cast<uint64_t>(pos - k) * stride] + d2);
-            if (hi)
-                best = fminf(best, in[base + static_cast<uint64_t>(pos + k) * stride] + d2);
-        }
-        if constexpr (!CHOOSE) {
-            out[c] = best;
-        } else {
+        out[off + c] = axis_min<AXIS>(b, in + off, c, static_cast<int>(coord[AXIS]));
+    }
+}
+
+// The last (z) pass of every pair, then the choice (blockIdx.y = band): each
+// cell keeps the best of its current (scale, R) and its band's levels of the
+// group, in ascending order; R is the distance less a small margin that keeps
+// rounding of the photon's position on the safe side.
+__global__ void majorant_choose_kernel(const __grid_constant__ MajorantBuild b, const __grid_constant__ MajorantPairs pairs,
+    const float* __restrict__ d, float2* __restrict__ cells, float* __restrict__ cost)
+{
+    const int band = blockIdx.y;
+    const int p0 = pairs.first[band], p1 = pairs.first[band + 1];
+    if (p0 == p1)
+        return;
+    const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
+    const float mu_ref = b.mu_refs[band];
+    for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < ncell;
+         c += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        uint32_t cx, cy, cz;
+        cell_coords(c, b, cx, cy, cz);
+        float best_cost = cost[static_cast<uint64_t>(band) * ncell + c];
+        float2 choice = make_float2(0.0f, 0.0f);
+        bool changed = false;
+        for (int p = p0; p < p1; ++p) {
+            const float best = axis_min<2>(b, d + static_cast<uint64_t>(p) * ncell, c, static_cast<int>(cz));
             if (best <= 0.0f)
                 continue; // the cell itself lies in the dilated set
-            // a small margin keeps rounding of the photon's position on the safe side
             const float R = fmaf(sqrtf(best), 0.999f, -1.0e-3f);
             if (!(R > 0.0f))
                 continue;
-            const float s = level_scale(lv, b.levels_per_octave);
-            const float mu = b.mu_ref * s;
+            const float s = level_scale(pairs.level[p], b.levels_per_octave);
+            const float mu = mu_ref * s;
             const float c_new = mu / (1.0f - expf(-mu * R)); // R infinite: mu
-            if (c_new < cost[c]) {
-                cost[c] = c_new;
-                cells[c * b.bands + b.band] = make_float2(1.0f / s, R);
+            if (c_new < best_cost) {
+                best_cost = c_new;
+                choice = make_float2(1.0f / s, R);
+                changed = true;
             }
+        }
+        if (changed) {
+            cost[static_cast<uint64_t>(band) * ncell + c] = best_cost;
+            cells[c * b.bands + band] = choice;
         }
     }
 }
@@ -263,16 +303,17 @@ __global__ void majorant_axis_kernel(MajorantBuild b, const float* __restrict__ 
 // The first (x) pass of the distance transform on the dilated set itself (0 on
 // it, infinity elsewhere): one thread per grid row finds each cell's nearest set
 // cell on the row with a forward and a backward sweep, instead of a scan per cell
-// (rows without a set cell would cost every cell a full scan).
+// (rows without a set cell would cost every cell a full scan).  blockIdx.y = pair.
 __global__ void majorant_sweep_x_kernel(MajorantBuild b, const float* __restrict__ in, float* __restrict__ out)
 {
     const uint64_t rows = static_cast<uint64_t>(b.n[1]) * b.n[2];
     const int n = static_cast<int>(b.n[0]);
     const float e = b.edge[0];
+    const uint64_t off = static_cast<uint64_t>(blockIdx.y) * rows * n;
     for (uint64_t r = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; r < rows;
          r += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
-        const float* row_in = in + r * n;
-        float* row_out = out + r * n;
+        const float* row_in = in + off + r * n;
+        float* row_out = out + off + r * n;
         int last = -1; // the nearest set cell at or before x
         for (int x = 0; x < n; ++x) {
             if (row_in[x] == 0.0f)
@@ -313,16 +354,18 @@ cudaError_t launch_majorant_box(const MajorantBuild& b, const int* bounds, float
     return cudaGetLastError();
 }
 
-cudaError_t launch_majorant_level_pass(const MajorantBuild& b, const uint8_t* level, int lv, float* d0, float* d1,
-    float2* cells, float* cost, cudaStream_t stream)
+cudaError_t launch_majorant_level_passes(const MajorantBuild& b, const MajorantPairs& pairs, const uint8_t* level,
+    float* d0, float* d1, float2* cells, float* cost, cudaStream_t stream)
 {
+    if (pairs.count <= 0)
+        return cudaSuccess;
     const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
-    const int g = grid_for(ncell);
-    majorant_dilate_kernel<<<g, 256, 0, stream>>>(b, level, lv, d0);
+    const dim3 per_pair(grid_for(ncell), pairs.count);
+    majorant_dilate_kernel<<<per_pair, 256, 0, stream>>>(b, pairs, level, d0);
     const uint64_t rows = static_cast<uint64_t>(b.n[1]) * b.n[2];
-    majorant_sweep_x_kernel<<<static_cast<int>(std::min<uint64_t>((rows + 63) / 64, 4096)), 64, 0, stream>>>(b, d0, d1);
-    majorant_axis_kernel<1, false><<<g, 256, 0, stream>>>(b, d1, d0, lv, cells, cost);
-    majorant_axis_kernel<2, true><<<g, 256, 0, stream>>>(b, d0, nullptr, lv, cells, cost);
+    majorant_sweep_x_kernel<<<dim3(static_cast<unsigned>(std::min<uint64_t>((rows + 63) / 64, 4096)), pairs.count), 64, 0, stream>>>(b, d0, d1);
+    majorant_axis_kernel<1><<<per_pair, 256, 0, stream>>>(b, d1, d0);
+    majorant_choose_kernel<<<dim3(grid_for(ncell), b.bands), 256, 0, stream>>>(b, pairs, d0, cells, cost);
     return cudaGetLastError();
 }
 

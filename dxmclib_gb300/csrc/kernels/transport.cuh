@@ -179,13 +179,21 @@ struct MajorantBuild {
     uint32_t n[3];       // cells per axis
     int shift[3];
     float edge[3];       // cell size (mm)
-    float mu_ref;        // global majorant (1/mm) at the reference energy of the band's cost model
     int levels_per_octave;
     int max_level;
-    int band, bands;     // the band being built; output pairs at cells[c * bands + band]
+    int bands;           // output pairs at cells[c * bands + band]
     int floor_levels[MAJORANT_MAX_BANDS]; // each band's emptiest level (its cells may be flown through), -1: none
-    float mu_refs[MAJORANT_MAX_BANDS];    // each band's mu_ref (the level kernel initialises every band)
+    float mu_refs[MAJORANT_MAX_BANDS];    // global majorant (1/mm) at each band's reference energy (cost model)
     float lower[3];      // grid corner (mm)
+};
+// Candidate levels whose distance transforms run together: pairs[first[k],
+// first[k + 1]) are band k's levels, in ascending order.
+constexpr int MAJORANT_MAX_PAIRS = MAJORANT_MAX_BANDS * 16;
+struct MajorantPairs {
+    int count;
+    int first[MAJORANT_MAX_BANDS + 1];
+    uint8_t band[MAJORANT_MAX_PAIRS];
+    uint8_t level[MAJORANT_MAX_PAIRS];
 };
 // All bands in one pass: scales is bands x PALETTE_MAX floats in device memory;
 // level and cost are bands x ncell; hist (bands x 64, zeroed by the caller)
@@ -196,11 +204,13 @@ cudaError_t launch_majorant_levels(const WorldParams& w, const float* scales, co
 // emptiest level (bounds: cell index min x, y, z, max x, y, z; set up as empty
 // by the caller) and marks every cell outside it by negating its R in all bands.
 cudaError_t launch_majorant_box(const MajorantBuild& b, const int* bounds, float2* cells, float* box, cudaStream_t stream);
-// Adds the candidate majorant level lv: cells whose 27-neighbourhood holds no
-// cell above the level get (level scale, distance to the nearest such cell) if
-// that lowers the expected number of steps per mm.  d0 and d1 are scratch grids.
-cudaError_t launch_majorant_level_pass(const MajorantBuild& b, const uint8_t* level, int lv, float* d0, float* d1,
-    float2* cells, float* cost, cudaStream_t stream);
+// Adds a group of candidate (band, level) pairs: for each, cells whose
+// 27-neighbourhood holds no cell above the level get (level scale, distance to
+// the nearest such cell) if that lowers the band's expected number of steps per
+// mm, a band's levels tried in ascending order.  d0 and d1 are scratch grids of
+// pairs.count x ncell floats.
+cudaError_t launch_majorant_level_passes(const MajorantBuild& b, const MajorantPairs& pairs, const uint8_t* level,
+    float* d0, float* d1, float2* cells, float* cost, cudaStream_t stream);
 cudaError_t launch_max_density(const Voxel* voxels, uint64_t n, unsigned int* out_bits, int n_materials, cudaStream_t stream);
 cudaError_t launch_probe_lut(const float* lut, LutMeta meta, int material, const double* energies, int n, double* out_att, double* out_maxinv, cudaStream_t stream);
 cudaError_t launch_probe_interactions(const float* lut, LutMeta meta, int material, int model, int kind, float energy,
