@@ -1136,8 +1136,12 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
                 pairs.emplace_back(band, lv);
     }
     // the distance transforms of many pairs run as one launch per pass, in groups
-    // whose two scratch grids stay within MAJORANT_SCRATCH_BYTES
-    const size_t group = std::clamp<size_t>(MAJORANT_SCRATCH_BYTES / (2 * ncell * sizeof(float)), 1,
+    // whose two scratch grids stay within MAJORANT_SCRATCH_BYTES and what the
+    // context's budget leaves beside the grid and the build's other buffers (one
+    // pair at a time if it leaves less)
+    const uint64_t held = ctx->in_use + cell_bytes + ncell * b.bands * (1 + sizeof(float));
+    const uint64_t room = std::min<uint64_t>(MAJORANT_SCRATCH_BYTES, ctx->budget > held ? ctx->budget - held : 0);
+    const size_t group = std::clamp<size_t>(room / (2 * ncell * sizeof(float)), 1,
         std::min<size_t>(std::max<size_t>(pairs.size(), 1), dev::MAJORANT_MAX_PAIRS));
     if (e == cudaSuccess && !pairs.empty())
         e = pool_alloc(ctx, &d0, group * ncell * sizeof(float), s);
@@ -1157,8 +1161,11 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
         }
         e = dev::launch_majorant_level_passes(b, pg, level, d0, d1, cells, cost, s);
     }
+    static const float no_box[6] = { INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY };
     if (e == cudaSuccess && use_box)
         e = dev::launch_majorant_box(b, bounds, cells, box, s);
+    else if (e == cudaSuccess) // an empty box: no cell is marked, the read-back says so
+        e = cudaMemcpyAsync(box, no_box, sizeof(no_box), cudaMemcpyHostToDevice, s);
     for (void* ptr : { static_cast<void*>(level), static_cast<void*>(d0), static_cast<void*>(d1), static_cast<void*>(cost),
              static_cast<void*>(bounds), static_cast<void*>(d_scales), static_cast<void*>(d_hist) })
         if (ptr)

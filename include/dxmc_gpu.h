@@ -259,7 +259,8 @@ int dxmc_gpu_world_prepare(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut*
 /* Reads back a built local-majorant grid: cells per axis, log2 of the cell size
  * in voxels per axis, the number of energy bands, the band edges (keV, bands - 1
  * values; may be NULL), the box of the cells above their band's emptiest level
- * (lo[3], hi[3] in mm from the grid corner's frame; may be NULL) and, if cells
+ * (lo[3], hi[3] in mm from the grid corner's frame, lo = +inf and hi = -inf
+ * where no box is used, as for the 8-byte voxel layout; may be NULL) and, if cells
  * is not NULL, (1 / scale, R mm) per cell and band, band fastest, then x, y, z;
  * R < 0 marks a cell outside that box (safe length |R|, or up to the box along
  * the ray).  DXMC_ERR_STATE if the pair has no grid. */

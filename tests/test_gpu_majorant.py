@@ -157,6 +157,44 @@ def test_many_levels_grid_bounds_and_parity(gpu_ctx, distinct):
     dworld.close()
 
 
+@pytest.mark.parametrize("distinct", [120, None])
+def test_grid_does_not_depend_on_the_grouping_of_levels(gpu_ctx, distinct):
+    """The distance transforms of a build's (band, level) pairs run in groups
+    sized by the scratch memory the context's budget leaves; a context whose
+    budget leaves room for one or three pairs at a time builds the same grid,
+    bit for bit, as one that runs them all together."""
+    import dxmclib_gb300 as dx
+    world = _continuous_world(distinct=distinct)
+    blob = dx.LutBlob.from_world(world, 90.0)
+    _, m0 = gpu_ctx.memory()
+    dworld = dx.DeviceWorld(gpu_ctx, world)
+    dlut = dx.DeviceLut(gpu_ctx, blob)
+    _, m1 = gpu_ctx.memory()
+    dworld.prepare(dlut)
+    _, m2 = gpu_ctx.memory()
+    ref = dworld.majorant(dlut)
+    dlut.close()
+    dworld.close()
+    shift, edges, box, cells = ref
+    ncell, bands = int(np.prod(cells.shape[:3])), cells.shape[3]
+    # the build holds the grid, a level byte and a cost float per cell and band,
+    # and two scratch floats per cell for each pair of a group
+    held = (m1 - m0) + (m2 - m1) + ncell * bands * 5
+    for per_group in (1, 3):
+        ctx = dx.GpuContext(memory_budget=held + 8 * ncell * per_group + 4 * ncell)
+        try:
+            w = dx.DeviceWorld(ctx, world)
+            lut = dx.DeviceLut(ctx, blob)
+            w.prepare(lut)
+            got = w.majorant(lut)
+            for a, b in zip(ref, got):
+                np.testing.assert_array_equal(a, b, err_msg=f"{per_group} pairs per group")
+            lut.close()
+            w.close()
+        finally:
+            ctx.close()
+
+
 @pytest.mark.parametrize("model,layout", [(1, 0), (2, 0), (1, 1)])
 def test_local_tracking_matches_global(gpu_ctx, model, layout):
     """Both tracking modes on the compact (palette) and the 8-byte voxel layout;
