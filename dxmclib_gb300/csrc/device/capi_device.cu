@@ -295,11 +295,29 @@ __global__ void pack_voxels_kernel(const float* __restrict__ density, const uint
     }
 }
 
+// Sets *bad if any material index is >= n_materials (16 indices per load where
+// the array is 16-byte aligned, then the tail).
 __global__ void check_materials_kernel(const uint8_t* __restrict__ material, uint64_t n, int n_materials, unsigned int* bad)
 {
-    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
-        if (material[i] >= n_materials)
-            atomicOr(bad, 1u);
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    const uint64_t t0 = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+    bool found = false;
+    uint64_t first_scalar = 0;
+    if ((reinterpret_cast<uintptr_t>(material) & 15u) == 0) {
+        const uint64_t vecs = n / 16;
+        for (uint64_t v = t0; v < vecs; v += stride) {
+            const uint4 q = reinterpret_cast<const uint4*>(material)[v];
+            const uint32_t words[4] = { q.x, q.y, q.z, q.w };
+#pragma unroll
+            for (int k = 0; k < 16; ++k)
+                found = found || static_cast<int>((words[k >> 2] >> (8 * (k & 3))) & 0xffu) >= n_materials;
+        }
+        first_scalar = vecs * 16;
+    }
+    for (uint64_t i = first_scalar + t0; i < n; i += stride)
+        found = found || material[i] >= n_materials;
+    if (found)
+        atomicOr(bad, 1u);
 }
 
 // ---- compact palette layout ---------------------------------------------------------
@@ -307,6 +325,7 @@ __global__ void check_materials_kernel(const uint8_t* __restrict__ material, uin
 // open-addressing hash table; with at most PALETTE_MAX of them every voxel is
 // stored as a 1-byte palette index (exact: the palette holds the f32 density).
 constexpr int PALETTE_TABLE = 4096; // hash slots (power of two)
+constexpr int PALETTE_SEEN = 512;   // per-block cache of keys already in the table (power of two)
 constexpr uint64_t PALETTE_EMPTY = 0ull;
 
 __device__ __forceinline__ uint64_t palette_key(float density, uint8_t material, uint8_t measurement)
@@ -322,58 +341,121 @@ __device__ __forceinline__ uint32_t palette_hash(uint64_t key)
     return static_cast<uint32_t>(key) & (PALETTE_TABLE - 1);
 }
 
+// The voxels of 4-voxel group g (i = 4g .. 4g + 3) when every array allows vector
+// loads; the caller runs the scalar tail.
+struct VoxelQuad {
+    uint64_t key[4];
+};
+
+__device__ __forceinline__ VoxelQuad load_quad(const float* __restrict__ density, const uint8_t* __restrict__ material,
+    const uint8_t* __restrict__ measurement, uint64_t g)
+{
+    const float4 d = reinterpret_cast<const float4*>(density)[g];
+    const uchar4 m = reinterpret_cast<const uchar4*>(material)[g];
+    const uchar4 f = measurement ? reinterpret_cast<const uchar4*>(measurement)[g] : make_uchar4(0, 0, 0, 0);
+    return VoxelQuad { { palette_key(d.x, m.x, f.x), palette_key(d.y, m.y, f.y), palette_key(d.z, m.z, f.z), palette_key(d.w, m.w, f.w) } };
+}
+
+__device__ __forceinline__ bool quad_loads(const float* density, const uint8_t* material, const uint8_t* measurement)
+{
+    return (reinterpret_cast<uintptr_t>(density) & 15u) == 0 && (reinterpret_cast<uintptr_t>(material) & 3u) == 0
+        && (reinterpret_cast<uintptr_t>(measurement) & 3u) == 0;
+}
+
+// Adds key to the global table unless the block's cache of keys already in the
+// table holds it.  The cache is direct-mapped; concurrent writers of one slot
+// each store a key that is in the table, so any value read is a valid hit.
+__device__ __forceinline__ void palette_insert(uint64_t key, unsigned long long* seen, unsigned long long* table,
+    unsigned int* count)
+{
+    const uint32_t h0 = palette_hash(key);
+    unsigned long long* cached = seen + (h0 & (PALETTE_SEEN - 1));
+    if (*reinterpret_cast<volatile unsigned long long*>(cached) == key)
+        return;
+    if (*reinterpret_cast<volatile unsigned int*>(count) > static_cast<unsigned>(dev::PALETTE_MAX))
+        return; // already too many distinct voxels: the 8-byte layout will be used
+    uint32_t h = h0;
+    for (int probe = 0; probe < PALETTE_TABLE; ++probe) {
+        const unsigned long long cur = table[h];
+        if (cur == key)
+            break;
+        if (cur == PALETTE_EMPTY) {
+            const unsigned long long prev = atomicCAS(table + h, PALETTE_EMPTY, key);
+            if (prev == PALETTE_EMPTY) {
+                atomicAdd(count, 1u);
+                break;
+            }
+            if (prev == key)
+                break;
+        }
+        h = (h + 1) & (PALETTE_TABLE - 1);
+    }
+    *reinterpret_cast<volatile unsigned long long*>(cached) = key;
+}
+
 __global__ void palette_insert_kernel(const float* __restrict__ density, const uint8_t* __restrict__ material,
     const uint8_t* __restrict__ measurement, uint64_t n, unsigned long long* table, unsigned int* count)
 {
+    __shared__ unsigned long long seen[PALETTE_SEEN];
+    for (int i = threadIdx.x; i < PALETTE_SEEN; i += blockDim.x)
+        seen[i] = PALETTE_EMPTY;
+    __syncthreads();
     const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-    for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x); base < n; base += stride) {
-        const uint64_t i = base + threadIdx.x;
-        const bool valid = i < n;
-        const uint64_t key = valid ? palette_key(density[i], material[i], measurement ? measurement[i] : 0) : PALETTE_EMPTY;
-        const unsigned active = __ballot_sync(0xffffffffu, valid);
-        if (!valid)
-            continue;
-        const unsigned peers = __match_any_sync(active, key);
-        if ((threadIdx.x & 31) != __ffs(peers) - 1)
-            continue; // one lane per distinct key of the warp probes the table
-        if (*reinterpret_cast<volatile unsigned int*>(count) > static_cast<unsigned>(dev::PALETTE_MAX))
-            continue; // already too many distinct voxels: the 8-byte layout will be used
-        uint32_t h = palette_hash(key);
-        for (int probe = 0; probe < PALETTE_TABLE; ++probe) {
-            const unsigned long long cur = table[h];
-            if (cur == key)
-                break;
-            if (cur == PALETTE_EMPTY) {
-                const unsigned long long prev = atomicCAS(table + h, PALETTE_EMPTY, key);
-                if (prev == PALETTE_EMPTY) {
-                    atomicAdd(count, 1u);
-                    break;
-                }
-                if (prev == key)
-                    break;
-            }
-            h = (h + 1) & (PALETTE_TABLE - 1);
+    const uint64_t t0 = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+    uint64_t first_scalar = 0;
+    if (quad_loads(density, material, measurement)) {
+        const uint64_t quads = n / 4;
+        for (uint64_t g = t0; g < quads; g += stride) {
+            const VoxelQuad q = load_quad(density, material, measurement, g);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (k == 0 || q.key[k] != q.key[k - 1])
+                    palette_insert(q.key[k], seen, table, count);
         }
+        first_scalar = quads * 4;
     }
+    for (uint64_t i = first_scalar + t0; i < n; i += stride)
+        palette_insert(palette_key(density[i], material[i], measurement ? measurement[i] : 0), seen, table, count);
 }
 
+// The palette index of every voxel, probing a copy of the table in shared memory.
 __global__ void palette_map_kernel(const float* __restrict__ density, const uint8_t* __restrict__ material,
     const uint8_t* __restrict__ measurement, uint64_t n, const unsigned long long* __restrict__ table,
     const uint8_t* __restrict__ slot_index, uint8_t* __restrict__ out)
 {
-    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
-        const uint64_t key = palette_key(density[i], material[i], measurement ? measurement[i] : 0);
+    __shared__ unsigned long long keys[PALETTE_TABLE];
+    __shared__ uint8_t slots[PALETTE_TABLE];
+    for (int i = threadIdx.x; i < PALETTE_TABLE; i += blockDim.x) {
+        keys[i] = table[i];
+        slots[i] = slot_index[i];
+    }
+    __syncthreads();
+    auto lookup = [&](uint64_t key) -> uint8_t {
         uint32_t h = palette_hash(key);
-        uint8_t idx = 0;
         for (int probe = 0; probe < PALETTE_TABLE; ++probe) {
-            if (table[h] == key) {
-                idx = slot_index[h];
-                break;
-            }
+            if (keys[h] == key)
+                return slots[h];
             h = (h + 1) & (PALETTE_TABLE - 1);
         }
-        out[i] = idx;
+        return 0;
+    };
+    const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+    const uint64_t t0 = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x;
+    uint64_t first_scalar = 0;
+    if (quad_loads(density, material, measurement) && (reinterpret_cast<uintptr_t>(out) & 3u) == 0) {
+        const uint64_t quads = n / 4;
+        for (uint64_t g = t0; g < quads; g += stride) {
+            const VoxelQuad q = load_quad(density, material, measurement, g);
+            uint8_t idx[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                idx[k] = (k > 0 && q.key[k] == q.key[k - 1]) ? idx[k - 1] : lookup(q.key[k]);
+            reinterpret_cast<uchar4*>(out)[g] = make_uchar4(idx[0], idx[1], idx[2], idx[3]);
+        }
+        first_scalar = quads * 4;
     }
+    for (uint64_t i = first_scalar + t0; i < n; i += stride)
+        out[i] = lookup(palette_key(density[i], material[i], measurement ? measurement[i] : 0));
 }
 
 size_t dev_palette_table_bytes() { return PALETTE_TABLE * sizeof(unsigned long long); }

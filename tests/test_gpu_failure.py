@@ -56,18 +56,20 @@ def test_invalid_input_and_budget_are_refused(gpu_ctx):
     ctx = gpu_ctx
     wl = pencil_water(n=16, histories=10_000)
     # material index outside the material map: found by the device check at upload
-    bad = dx.World()
-    bad.setDimensions((16, 16, 16))
-    bad.setSpacing((1, 1, 1))
-    bad.setDensityArray(np.ones(16 ** 3, np.float32))
-    mat = np.zeros(16 ** 3, np.uint8)
-    mat[100] = 3
-    bad.setMaterialIndexArray(mat)
-    bad.addMaterialToMap(dx.Material("Water, Liquid"))
-    bad._valid = True  # bypass the host-side check to reach the device-side one
-    with pytest.raises(A.DxmcError) as e:
-        dx.DeviceWorld(ctx, bad)
-    assert e.value.status == A.DXMC_ERR_INVALID and "material index" in str(e.value)
+    # (16 indices per load, then a tail: the last byte of a load, the tail, the first voxel)
+    for side, where in ((16, 100), (16, 15), (5, 124), (5, 0)):
+        bad = dx.World()
+        bad.setDimensions((side, side, side))
+        bad.setSpacing((1, 1, 1))
+        bad.setDensityArray(np.ones(side ** 3, np.float32))
+        mat = np.zeros(side ** 3, np.uint8)
+        mat[where] = 3
+        bad.setMaterialIndexArray(mat)
+        bad.addMaterialToMap(dx.Material("Water, Liquid"))
+        bad._valid = True  # bypass the host-side check to reach the device-side one
+        with pytest.raises(A.DxmcError) as e:
+            dx.DeviceWorld(ctx, bad)
+        assert e.value.status == A.DXMC_ERR_INVALID and "material index" in str(e.value), (side, where)
     # unknown correction model
     dworld = dx.DeviceWorld(ctx, wl.world)
     dlut = dx.DeviceLut(ctx, dx.LutBlob(wl.world.materialMap(), dworld.max_density(), 60.0))
