@@ -187,6 +187,16 @@ bool mapped_host(T* ptr, T*& device_ptr)
     return true;
 }
 
+// Local-majorant bounds of a LUT: band edges, per band and material the ratio
+// bound, per band the cost model's reference majorant.
+struct MajorantRatios {
+    int bands = 1;
+    float band_edge[dev::MAJORANT_MAX_BANDS - 1] {};
+    float band_log0 = 1.0f, band_inv_dlog = 0.0f;
+    std::vector<float> ratio; // bands x materials
+    float mu_ref[dev::MAJORANT_MAX_BANDS] {};
+};
+
 // Per energy band and material m, the largest ratio of m's attenuation (per
 // g/cm3) to the global majorant over the band's energies, from the float image
 // the kernels read.  Photons are tracked from 1 keV (the transport cutoff) to
@@ -202,7 +212,7 @@ bool mapped_host(T* ptr, T*& device_ptr)
 // that rounding of the band choice stays covered, and a 0.2 % margin covers the
 // device's exponential and the level arithmetic.  mu_ref: the global majorant
 // (1/mm) at each band's geometric mid-energy, the cost model's reference.
-void majorant_ratios(const std::vector<float>& img, const dev::LutMeta& m, dxmc_lut& lut)
+void compute_majorant_ratios(const std::vector<float>& img, const dev::LutMeta& m, MajorantRatios& lut)
 {
     const int R = m.R;
     const float* x = img.data() + m.off_x;
@@ -221,8 +231,8 @@ void majorant_ratios(const std::vector<float>& img, const dev::LutMeta& m, dxmc_
         return std::pow(10.0, static_cast<double>(maxc[2 * seg]) + maxc[2 * seg + 1] * static_cast<double>(le));
     };
     const double e_max = std::max(static_cast<double>(m.max_energy), 1.0);
-    lut.majorant_bands = e_max > 15.0 ? MAJORANT_BANDS : 1;
-    const int nb = lut.majorant_bands;
+    lut.bands = e_max > 15.0 ? MAJORANT_BANDS : 1;
+    const int nb = lut.bands;
     std::vector<double> edges { 1.0 };
     for (int k = 1; k < nb; ++k)
         edges.push_back(10.0 * std::pow(e_max / 10.0, static_cast<double>(k) / nb));
@@ -236,7 +246,7 @@ void majorant_ratios(const std::vector<float>& img, const dev::LutMeta& m, dxmc_
         points.push_back(x[k]);
     for (int k = 0; k <= R; ++k)
         points.push_back(m.linear_energy + static_cast<float>(k) / m.inv_linear_step);
-    lut.majorant_ratio.assign(static_cast<size_t>(nb) * m.n_materials, 0.0f);
+    lut.ratio.assign(static_cast<size_t>(nb) * m.n_materials, 0.0f);
     for (int b = 0; b < nb; ++b) {
         const float le_lo = static_cast<float>(std::log10(edges[b]) - (b > 0 ? 4.34e-4 : 0.0));
         const float le_hi = static_cast<float>(std::log10(edges[b + 1]) + (b + 1 < nb ? 4.34e-4 : 0.0));
@@ -259,11 +269,24 @@ void majorant_ratios(const std::vector<float>& img, const dev::LutMeta& m, dxmc_
                     r = std::max(r, tot * inv);
                 }
             }
-            lut.majorant_ratio[static_cast<size_t>(b) * m.n_materials + mat] = static_cast<float>(r * 1.002);
+            lut.ratio[static_cast<size_t>(b) * m.n_materials + mat] = static_cast<float>(r * 1.002);
         }
         const double inv_cm = max_inverse(static_cast<float>(0.5 * (std::log10(edges[b]) + std::log10(edges[b + 1]))));
         lut.mu_ref[b] = static_cast<float>(inv_cm > 0 ? 0.1 / inv_cm : 0.01);
     }
+}
+
+// The ratio bounds of a blob, computed at its first upload and kept with it (the
+// same blob is often uploaded again, to other contexts or after a free).
+std::shared_ptr<const MajorantRatios> majorant_ratios(const dxmc_lut_blob& b, const std::vector<float>& img, const dev::LutMeta& m)
+{
+    std::lock_guard<std::mutex> lock(*b.tables_mutex);
+    if (auto cached = std::static_pointer_cast<const MajorantRatios>(b.majorant))
+        return cached;
+    auto r = std::make_shared<MajorantRatios>();
+    compute_majorant_ratios(img, m, *r);
+    b.majorant = r;
+    return r;
 }
 
 size_t dev_palette_table_bytes();
@@ -961,7 +984,15 @@ int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* b, dxmc_lut** ou
     lut->meta = m;
     static std::atomic<uint64_t> lut_serials { 0 };
     lut->serial = ++lut_serials;
-    majorant_ratios(img, m, *lut);
+    {
+        const auto mr = majorant_ratios(*b, img, m);
+        lut->majorant_bands = mr->bands;
+        std::copy(std::begin(mr->band_edge), std::end(mr->band_edge), lut->band_edge);
+        lut->band_log0 = mr->band_log0;
+        lut->band_inv_dlog = mr->band_inv_dlog;
+        lut->majorant_ratio = mr->ratio;
+        std::copy(std::begin(mr->mu_ref), std::end(mr->mu_ref), lut->mu_ref);
+    }
     lut->bytes = img.size() * sizeof(float);
     cudaError_t e = pool_alloc(ctx, &lut->image, lut->bytes, ctx->stream);
     if (e == cudaSuccess)

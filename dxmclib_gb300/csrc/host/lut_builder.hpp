@@ -39,9 +39,11 @@ struct dxmc_lut_blob {
     std::vector<std::array<double, 79>> spline;
     std::vector<std::array<dxmc_shell_config, 12>> shells;
     std::vector<double> max_density;
-    // inverse-CDF sampling tables, built on first upload and kept with the blob
+    // inverse-CDF sampling tables and the local-majorant ratio bounds, built on
+    // first upload and kept with the blob (both under tables_mutex)
     std::shared_ptr<std::mutex> tables_mutex = std::make_shared<std::mutex>();
     mutable std::shared_ptr<const void> tables;
+    mutable std::shared_ptr<const void> majorant;
 
     std::size_t resolution() const { return log_energy.size(); }
 };
