@@ -1187,6 +1187,7 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     cudaStream_t s = ctx->stream;
     float2* cells = nullptr;
     uint8_t* level = nullptr;
+    uint8_t* minlev = nullptr;
     float *d0 = nullptr, *d1 = nullptr, *cost = nullptr, *d_scales = nullptr;
     int* bounds = nullptr;
     unsigned int* d_hist = nullptr;
@@ -1200,6 +1201,8 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
         e = cudaMemsetAsync(bounds + 3, 0xff, 3 * sizeof(int), s); // maxima start at -1
     if (e == cudaSuccess)
         e = pool_alloc(ctx, &level, ncell * b.bands, s);
+    if (e == cudaSuccess)
+        e = pool_alloc(ctx, &minlev, ncell * b.bands, s);
     if (e == cudaSuccess)
         e = pool_alloc(ctx, &cost, ncell * b.bands * sizeof(float), s);
     if (e == cudaSuccess)
@@ -1228,6 +1231,9 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
         e = cudaMemcpyAsync(hist.data(), d_hist, hist.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(s);
+    // each cell's lowest level over its neighbourhood: the dilated set of every level
+    if (e == cudaSuccess)
+        e = dev::launch_majorant_minfilter(b, level, minlev, s);
     std::vector<std::pair<int, int>> pairs; // (band, level), band-major, levels ascending
     for (int band = 0; band < b.bands && e == cudaSuccess; ++band) {
         std::vector<std::pair<unsigned int, int>> present; // (cells, level)
@@ -1252,7 +1258,7 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     // whose two scratch grids stay within MAJORANT_SCRATCH_BYTES and what the
     // context's budget leaves beside the grid and the build's other buffers (one
     // pair at a time if it leaves less)
-    const uint64_t held = ctx->in_use + cell_bytes + ncell * b.bands * (1 + sizeof(float));
+    const uint64_t held = ctx->in_use + cell_bytes + ncell * b.bands * (2 + sizeof(float));
     const uint64_t room = std::min<uint64_t>(MAJORANT_SCRATCH_BYTES, ctx->budget > held ? ctx->budget - held : 0);
     const size_t group = std::clamp<size_t>(room / (2 * ncell * sizeof(float)), 1,
         std::min<size_t>(std::max<size_t>(pairs.size(), 1), dev::MAJORANT_MAX_PAIRS));
@@ -1272,14 +1278,14 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
                 ++i;
             pg.first[band] = i;
         }
-        e = dev::launch_majorant_level_passes(b, pg, level, d0, d1, cells, cost, s);
+        e = dev::launch_majorant_level_passes(b, pg, minlev, d0, d1, cells, cost, s);
     }
     static const float no_box[6] = { INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY };
     if (e == cudaSuccess && use_box)
         e = dev::launch_majorant_box(b, bounds, cells, box, s);
     else if (e == cudaSuccess) // an empty box: no cell is marked, the read-back says so
         e = cudaMemcpyAsync(box, no_box, sizeof(no_box), cudaMemcpyHostToDevice, s);
-    for (void* ptr : { static_cast<void*>(level), static_cast<void*>(d0), static_cast<void*>(d1), static_cast<void*>(cost),
+    for (void* ptr : { static_cast<void*>(level), static_cast<void*>(minlev), static_cast<void*>(d0), static_cast<void*>(d1), static_cast<void*>(cost),
              static_cast<void*>(bounds), static_cast<void*>(d_scales), static_cast<void*>(d_hist) })
         if (ptr)
             cudaFreeAsync(ptr, s);

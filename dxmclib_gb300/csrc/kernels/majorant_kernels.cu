@@ -15,9 +15,11 @@
 //      its voxels, rounded up to a level 2^(-level / levels_per_octave) (one
 //      pass over the voxels for all bands, with a histogram of the levels);
 //   2. for each level the cells have (the host picks at most a dozen per band
-//      from the histogram), the cells above it are dilated by one cell and a
-//      Euclidean distance transform (three separable passes over the cell grid,
-//      cell sizes in mm: row sweeps along x, scans along y and z) gives every
+//      from the histogram), the cells above it are dilated by one cell (one
+//      min-filter of the levels over the 27-neighbourhood serves every level)
+//      and a Euclidean distance transform (three separable passes over the
+//      cell grid, cell sizes in mm: warp scans along x rows, scans along y and
+//      z) gives every
 //      other cell the distance R to the nearest point of a cell above the
 //      level: a flight of length at most R from anywhere in the cell stays
 //      where the level's scale bounds the attenuation.  All (band, level)
@@ -179,40 +181,36 @@ __global__ void majorant_box_kernel(const __grid_constant__ MajorantBuild b, con
     }
 }
 
-// d[p][c] = 0 where a cell of the 27-neighbourhood of c lies above pair p's
-// level in its band, else infinity (blockIdx.y = p)
-__global__ void majorant_dilate_kernel(MajorantBuild b, const __grid_constant__ MajorantPairs pairs,
-    const uint8_t* __restrict__ level, float* __restrict__ d)
+// minlev[k][c] = the lowest level (largest scale) of band k in the 27-neighbourhood
+// of cell c (blockIdx.y = band): cell c lies in the dilated set of level lv, the
+// cells above lv grown by one cell, exactly when minlev < lv.
+__global__ void majorant_minfilter_kernel(MajorantBuild b, const uint8_t* __restrict__ level, uint8_t* __restrict__ minlev)
 {
     const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
-    const int p = blockIdx.y;
-    const int lv = pairs.level[p];
-    const uint8_t* __restrict__ lvl = level + static_cast<uint64_t>(pairs.band[p]) * ncell;
-    float* __restrict__ out = d + static_cast<uint64_t>(p) * ncell;
+    const uint64_t off = static_cast<uint64_t>(blockIdx.y) * ncell;
+    const uint8_t* __restrict__ lvl = level + off;
     for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < ncell;
          c += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
         uint32_t cx, cy, cz;
         cell_coords(c, b, cx, cy, cz);
-        bool above = false;
-        for (int dz = -1; dz <= 1 && !above; ++dz) {
+        int lo = 255;
+        for (int dz = -1; dz <= 1; ++dz) {
             const int z = static_cast<int>(cz) + dz;
             if (z < 0 || z >= static_cast<int>(b.n[2]))
                 continue;
-            for (int dy = -1; dy <= 1 && !above; ++dy) {
+            for (int dy = -1; dy <= 1; ++dy) {
                 const int y = static_cast<int>(cy) + dy;
                 if (y < 0 || y >= static_cast<int>(b.n[1]))
                     continue;
                 const uint64_t row = (static_cast<uint64_t>(z) * b.n[1] + y) * b.n[0];
                 for (int dx = -1; dx <= 1; ++dx) {
                     const int x = static_cast<int>(cx) + dx;
-                    if (x >= 0 && x < static_cast<int>(b.n[0]) && lvl[row + x] < lv) {
-                        above = true;
-                        break;
-                    }
+                    if (x >= 0 && x < static_cast<int>(b.n[0]))
+                        lo = min(lo, static_cast<int>(lvl[row + x]));
                 }
             }
         }
-        out[c] = above ? 0.0f : INFINITY;
+        minlev[off + c] = static_cast<uint8_t>(lo);
     }
 }
 
@@ -300,33 +298,60 @@ __global__ void majorant_choose_kernel(const __grid_constant__ MajorantBuild b, 
     }
 }
 
-// The first (x) pass of the distance transform on the dilated set itself (0 on
-// it, infinity elsewhere): one thread per grid row finds each cell's nearest set
-// cell on the row with a forward and a backward sweep, instead of a scan per cell
-// (rows without a set cell would cost every cell a full scan).  blockIdx.y = pair.
-__global__ void majorant_sweep_x_kernel(MajorantBuild b, const float* __restrict__ in, float* __restrict__ out)
+// The first (x) pass of the distance transform on the dilated set of pair p
+// (blockIdx.y = p; minlev < the pair's level): one warp per grid row finds each
+// cell's nearest set cell before and after it on the row with a max- and a
+// min-scan over 32-cell chunks, carried from chunk to chunk, and writes the
+// squared distance (cell sizes in mm) to out.
+__global__ void majorant_sweep_x_kernel(MajorantBuild b, const __grid_constant__ MajorantPairs pairs,
+    const uint8_t* __restrict__ minlev, float* __restrict__ out)
 {
     const uint64_t rows = static_cast<uint64_t>(b.n[1]) * b.n[2];
     const int n = static_cast<int>(b.n[0]);
     const float e = b.edge[0];
-    const uint64_t off = static_cast<uint64_t>(blockIdx.y) * rows * n;
-    for (uint64_t r = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; r < rows;
-         r += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
-        const float* row_in = in + off + r * n;
-        float* row_out = out + off + r * n;
-        int last = -1; // the nearest set cell at or before x
-        for (int x = 0; x < n; ++x) {
-            if (row_in[x] == 0.0f)
-                last = x;
-            row_out[x] = last >= 0 ? static_cast<float>(x - last) : INFINITY;
+    const int p = blockIdx.y;
+    const int lv = pairs.level[p];
+    const uint64_t ncell = rows * n;
+    const uint8_t* __restrict__ in = minlev + static_cast<uint64_t>(pairs.band[p]) * ncell;
+    float* __restrict__ dst = out + static_cast<uint64_t>(p) * ncell;
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = static_cast<uint64_t>(gridDim.x) * (blockDim.x >> 5);
+    for (uint64_t r = blockIdx.x * static_cast<uint64_t>(blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
+        const uint8_t* row_in = in + r * n;
+        float* row_out = dst + r * n;
+        int last = -1; // the nearest set cell at or before the chunk's cells
+        for (int x0 = 0; x0 < n; x0 += 32) {
+            const int x = x0 + lane;
+            int v = (x < n && row_in[x] < lv) ? x : -1;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o)
+                    v = max(v, t);
+            }
+            v = max(v, last);
+            if (x < n)
+                row_out[x] = v >= 0 ? static_cast<float>(x - v) : INFINITY;
+            last = __shfl_sync(0xffffffffu, v, 31);
         }
-        int next = -1; // the nearest set cell at or after x
-        for (int x = n - 1; x >= 0; --x) {
-            if (row_in[x] == 0.0f)
-                next = x;
-            const float k = fminf(row_out[x], next >= 0 ? static_cast<float>(next - x) : INFINITY);
-            const float d = k * e;
-            row_out[x] = d * d;
+        constexpr int none = 0x7fffffff;
+        int next = none; // the nearest set cell at or after the chunk's cells
+        for (int x0 = ((n - 1) / 32) * 32; x0 >= 0; x0 -= 32) {
+            const int x = x0 + lane;
+            int v = (x < n && row_in[x] < lv) ? x : none;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_down_sync(0xffffffffu, v, o);
+                if (lane + o < 32)
+                    v = min(v, t);
+            }
+            v = min(v, next);
+            if (x < n) {
+                const float k = fminf(row_out[x], v != none ? static_cast<float>(v - x) : INFINITY);
+                const float d = k * e;
+                row_out[x] = d * d;
+            }
+            next = __shfl_sync(0xffffffffu, v, 0);
         }
     }
 }
@@ -354,16 +379,23 @@ cudaError_t launch_majorant_box(const MajorantBuild& b, const int* bounds, float
     return cudaGetLastError();
 }
 
-cudaError_t launch_majorant_level_passes(const MajorantBuild& b, const MajorantPairs& pairs, const uint8_t* level,
+cudaError_t launch_majorant_minfilter(const MajorantBuild& b, const uint8_t* level, uint8_t* minlev, cudaStream_t stream)
+{
+    const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
+    majorant_minfilter_kernel<<<dim3(grid_for(ncell), b.bands), 256, 0, stream>>>(b, level, minlev);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_majorant_level_passes(const MajorantBuild& b, const MajorantPairs& pairs, const uint8_t* minlev,
     float* d0, float* d1, float2* cells, float* cost, cudaStream_t stream)
 {
     if (pairs.count <= 0)
         return cudaSuccess;
     const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
-    const dim3 per_pair(grid_for(ncell), pairs.count);
-    majorant_dilate_kernel<<<per_pair, 256, 0, stream>>>(b, pairs, level, d0);
     const uint64_t rows = static_cast<uint64_t>(b.n[1]) * b.n[2];
-    majorant_sweep_x_kernel<<<dim3(static_cast<unsigned>(std::min<uint64_t>((rows + 63) / 64, 4096)), pairs.count), 64, 0, stream>>>(b, d0, d1);
+    majorant_sweep_x_kernel<<<dim3(static_cast<unsigned>(std::min<uint64_t>((rows + 7) / 8, 4096)), pairs.count), 256, 0, stream>>>(
+        b, pairs, minlev, d1);
+    const dim3 per_pair(grid_for(ncell), pairs.count);
     majorant_axis_kernel<1><<<per_pair, 256, 0, stream>>>(b, d1, d0);
     majorant_choose_kernel<<<dim3(grid_for(ncell), b.bands), 256, 0, stream>>>(b, pairs, d0, cells, cost);
     return cudaGetLastError();

@@ -204,12 +204,14 @@ cudaError_t launch_majorant_levels(const WorldParams& w, const float* scales, co
 // emptiest level (bounds: cell index min x, y, z, max x, y, z; set up as empty
 // by the caller) and marks every cell outside it by negating its R in all bands.
 cudaError_t launch_majorant_box(const MajorantBuild& b, const int* bounds, float2* cells, float* box, cudaStream_t stream);
+// minlev (bands x ncell): each cell's lowest level over its 27-neighbourhood.
+cudaError_t launch_majorant_minfilter(const MajorantBuild& b, const uint8_t* level, uint8_t* minlev, cudaStream_t stream);
 // Adds a group of candidate (band, level) pairs: for each, cells whose
-// 27-neighbourhood holds no cell above the level get (level scale, distance to
-// the nearest such cell) if that lowers the band's expected number of steps per
-// mm, a band's levels tried in ascending order.  d0 and d1 are scratch grids of
-// pairs.count x ncell floats.
-cudaError_t launch_majorant_level_passes(const MajorantBuild& b, const MajorantPairs& pairs, const uint8_t* level,
+// 27-neighbourhood holds no cell above the level (minlev >= level) get (level
+// scale, distance to the nearest such cell) if that lowers the band's expected
+// number of steps per mm, a band's levels tried in ascending order.  d0 and d1
+// are scratch grids of pairs.count x ncell floats.
+cudaError_t launch_majorant_level_passes(const MajorantBuild& b, const MajorantPairs& pairs, const uint8_t* minlev,
     float* d0, float* d1, float2* cells, float* cost, cudaStream_t stream);
 cudaError_t launch_max_density(const Voxel* voxels, uint64_t n, unsigned int* out_bits, int n_materials, cudaStream_t stream);
 cudaError_t launch_probe_lut(const float* lut, LutMeta meta, int material, const double* energies, int n, double* out_att, double* out_maxinv, cudaStream_t stream);

@@ -177,9 +177,9 @@ def test_grid_does_not_depend_on_the_grouping_of_levels(gpu_ctx, distinct):
     dworld.close()
     shift, edges, box, cells = ref
     ncell, bands = int(np.prod(cells.shape[:3])), cells.shape[3]
-    # the build holds the grid, a level byte and a cost float per cell and band,
+    # the build holds the grid, two level bytes and a cost float per cell and band,
     # and two scratch floats per cell for each pair of a group
-    held = (m1 - m0) + (m2 - m1) + ncell * bands * 5
+    held = (m1 - m0) + (m2 - m1) + ncell * bands * 6
     for per_group in (1, 3):
         ctx = dx.GpuContext(memory_budget=held + 8 * ncell * per_group + 4 * ncell)
         try:
