@@ -203,6 +203,13 @@ public:
     void setDevice(int device) { m_options.device = device; }
     void setSeed(std::uint64_t seed) { m_seed = seed; }
     void setTallyMode(int mode) { m_options.tally_mode = mode; }
+    // GPU-only choices, with the reference's behaviour at REFERENCE direction and
+    // either tracking mode (local majorants sample the same process, faster):
+    // DXMC_TRACKING_DEFAULT / GLOBAL / LOCAL and DXMC_DIRECTION_REFERENCE / NORMALIZED.
+    void setTracking(int tracking) { m_tracking = tracking; }
+    int tracking() const { return m_tracking; }
+    void setDirectionMode(int direction) { m_direction = direction; }
+    int directionMode() const { return m_direction; }
     // Spectrum for IsotropicSource, whose spectrum has no public getter.
     void setIsotropicSpectrum(std::vector<T> energies, std::vector<T> weights) { m_iso = { std::move(energies), std::move(weights) }; }
     const std::string& lastError() const { return m_error; }
@@ -283,6 +290,8 @@ public:
         jd.seed = m_seed++;
         jd.model = static_cast<int32_t>(m_model);
         jd.tally_mode = -1;
+        jd.tracking = m_tracking;
+        jd.direction = m_direction;
         const auto start = std::chrono::system_clock::now();
         if (progressbar) {
             progressbar->setTotalExposures(flat.exposures.size());
@@ -449,6 +458,8 @@ private:
     dxmc_gpu_ctx* m_ctx = nullptr;
     dxmc_gpu_options m_options {};
     std::uint64_t m_seed = 1;
+    int m_tracking = DXMC_TRACKING_DEFAULT;
+    int m_direction = DXMC_DIRECTION_REFERENCE;
     std::pair<std::vector<T>, std::vector<T>> m_iso;
     std::string m_error;
     OUTPUTMODE m_mode = OUTPUTMODE::DOSE;                             // transport.hpp:838

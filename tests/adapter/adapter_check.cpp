@@ -102,5 +102,15 @@ int main()
             static_cast<unsigned long long>(res.numberOfHistories), t.lastError().c_str());
         failures += !nogpu_ok;
     }
+    // 4) the GPU-only choices default to the reference's behaviour and round-trip
+    {
+        gpu::Transport<double> t;
+        bool opt_ok = t.tracking() == DXMC_TRACKING_DEFAULT && t.directionMode() == DXMC_DIRECTION_REFERENCE;
+        t.setTracking(DXMC_TRACKING_GLOBAL);
+        t.setDirectionMode(DXMC_DIRECTION_NORMALIZED);
+        opt_ok = opt_ok && t.tracking() == DXMC_TRACKING_GLOBAL && t.directionMode() == DXMC_DIRECTION_NORMALIZED;
+        std::printf("%s options tracking=%d direction=%d\n", opt_ok ? "OK" : "FAIL", t.tracking(), t.directionMode());
+        failures += !opt_ok;
+    }
     return failures;
 }
