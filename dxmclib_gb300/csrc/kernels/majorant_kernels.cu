@@ -214,17 +214,13 @@ __global__ void majorant_minfilter_kernel(MajorantBuild b, const uint8_t* __rest
     }
 }
 
-// One step of the separable squared distance transform along AXIS at cell c:
-// min over the line through c of in[t] + ((pos - t) * edge)^2, scanned outward
-// from pos until the distance alone exceeds the best value.
-template <int AXIS>
-__device__ __forceinline__ float axis_min(const MajorantBuild& b, const float* __restrict__ in, uint64_t c, int pos)
+// One step of the separable squared distance transform at position pos of a
+// line of n cells of size e: min over t of get(t) + ((pos - t) * e)^2, scanned
+// outward from pos until the distance alone exceeds the best value.
+template <typename Get>
+__device__ __forceinline__ float line_min(Get get, int n, int pos, float e)
 {
-    const int n = static_cast<int>(b.n[AXIS]);
-    const uint64_t stride = AXIS == 0 ? 1 : (AXIS == 1 ? b.n[0] : static_cast<uint64_t>(b.n[0]) * b.n[1]);
-    const float e = b.edge[AXIS];
-    const uint64_t base = c - static_cast<uint64_t>(pos) * stride;
-    float best = in[c];
+    float best = get(pos);
     for (int k = 1; k < n; ++k) {
         const float dk = static_cast<float>(k) * e;
         const float d2 = dk * dk;
@@ -234,11 +230,36 @@ __device__ __forceinline__ float axis_min(const MajorantBuild& b, const float* _
         if (!lo && !hi)
             break;
         if (lo)
-            best = fminf(best, in[base + static_cast<uint64_t>(pos - k) * stride] + d2);
+            best = fminf(best, get(pos - k) + d2);
         if (hi)
-            best = fminf(best, in[base + static_cast<uint64_t>(pos + k) * stride] + d2);
+            best = fminf(best, get(pos + k) + d2);
     }
     return best;
+}
+
+// line_min along AXIS through cell c, reading the grid in global memory
+template <int AXIS>
+__device__ __forceinline__ float axis_min(const MajorantBuild& b, const float* __restrict__ in, uint64_t c, int pos)
+{
+    const uint64_t stride = AXIS == 0 ? 1 : (AXIS == 1 ? b.n[0] : static_cast<uint64_t>(b.n[0]) * b.n[1]);
+    const uint64_t base = c - static_cast<uint64_t>(pos) * stride;
+    return line_min([&](int t) { return in[base + static_cast<uint64_t>(t) * stride]; }, static_cast<int>(b.n[AXIS]), pos,
+        b.edge[AXIS]);
+}
+
+// Shared-memory tiles for the y pass: the lines of 32 adjacent x cells,
+// tile[t * 32 + lane] = the line of x0 + lane at position t (infinity past the
+// grid), so a warp scanning its 32 lines reads 32 consecutive banks.
+constexpr int TILE_W = 32;
+constexpr size_t TILE_SMEM_MAX = 48 * 1024;
+
+__device__ __forceinline__ void load_tile(float* tile, const float* __restrict__ src, uint32_t x0, uint32_t n0, int n,
+    uint64_t base, uint64_t stride)
+{
+    for (uint32_t i = threadIdx.x; i < static_cast<uint32_t>(n) * TILE_W; i += blockDim.x) {
+        const uint32_t t = i / TILE_W, x = x0 + i % TILE_W;
+        tile[i] = x < n0 ? src[base + t * stride + x] : INFINITY;
+    }
 }
 
 // A middle pass of the distance transform for every pair (blockIdx.y = pair).
@@ -294,6 +315,33 @@ __global__ void majorant_choose_kernel(const __grid_constant__ MajorantBuild b, 
         if (changed) {
             cost[static_cast<uint64_t>(band) * ncell + c] = best_cost;
             cells[c * b.bands + band] = choice;
+        }
+    }
+}
+
+// The y pass with tiles in shared memory (blockIdx.y = pair): one tile per x
+// group of 32 cells and z, the block's warps taking y rows in turn.
+__global__ void majorant_axis_y_tiled_kernel(MajorantBuild b, const float* __restrict__ in, float* __restrict__ out)
+{
+    extern __shared__ float tile[];
+    const uint32_t n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
+    const uint64_t ncell = static_cast<uint64_t>(n0) * n1 * n2;
+    const uint64_t off = static_cast<uint64_t>(blockIdx.y) * ncell;
+    const uint32_t xtiles = (n0 + TILE_W - 1) / TILE_W;
+    const uint64_t tiles = static_cast<uint64_t>(xtiles) * n2;
+    const uint32_t lane = threadIdx.x % TILE_W, warps = blockDim.x / TILE_W;
+    for (uint64_t ti = blockIdx.x; ti < tiles; ti += gridDim.x) {
+        const uint32_t z = static_cast<uint32_t>(ti / xtiles), x0 = static_cast<uint32_t>(ti % xtiles) * TILE_W;
+        const uint64_t base = off + static_cast<uint64_t>(z) * n1 * n0;
+        __syncthreads(); // the previous tile is no longer read
+        load_tile(tile, in, x0, n0, static_cast<int>(n1), base, n0);
+        __syncthreads();
+        const uint32_t x = x0 + lane;
+        for (uint32_t y = threadIdx.x / TILE_W; y < n1; y += warps) {
+            const float best = line_min([&](int t) { return tile[t * TILE_W + lane]; }, static_cast<int>(n1),
+                static_cast<int>(y), b.edge[1]);
+            if (x < n0)
+                out[base + static_cast<uint64_t>(y) * n0 + x] = best;
         }
     }
 }
@@ -395,8 +443,17 @@ cudaError_t launch_majorant_level_passes(const MajorantBuild& b, const MajorantP
     const uint64_t rows = static_cast<uint64_t>(b.n[1]) * b.n[2];
     majorant_sweep_x_kernel<<<dim3(static_cast<unsigned>(std::min<uint64_t>((rows + 7) / 8, 4096)), pairs.count), 256, 0, stream>>>(
         b, pairs, minlev, d1);
-    const dim3 per_pair(grid_for(ncell), pairs.count);
-    majorant_axis_kernel<1><<<per_pair, 256, 0, stream>>>(b, d1, d0);
+    // the y pass from shared-memory tiles where a tile's lines fit (the same
+    // arithmetic in the same order as the global-memory kernel); the z pass and
+    // choice read global memory: there one thread per cell hides the latency of
+    // the cost arithmetic better than a tile's threads walking many cells each
+    const size_t smem_y = static_cast<size_t>(b.n[1]) * TILE_W * sizeof(float);
+    const uint64_t xtiles = (b.n[0] + TILE_W - 1) / TILE_W;
+    if (smem_y <= TILE_SMEM_MAX)
+        majorant_axis_y_tiled_kernel<<<dim3(static_cast<unsigned>(std::min<uint64_t>(xtiles * b.n[2], 4096)), pairs.count), 256, smem_y,
+            stream>>>(b, d1, d0);
+    else
+        majorant_axis_kernel<1><<<dim3(grid_for(ncell), pairs.count), 256, 0, stream>>>(b, d1, d0);
     majorant_choose_kernel<<<dim3(grid_for(ncell), b.bands), 256, 0, stream>>>(b, pairs, d0, cells, cost);
     return cudaGetLastError();
 }

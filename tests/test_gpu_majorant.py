@@ -39,7 +39,7 @@ def _voxel_scales(world, blob, e_lo, e_hi):
     return s.reshape(d[2], d[1], d[0])
 
 
-def _check_grid_bounds(dworld, dlut, world, blob, expect_air=True):
+def _check_grid_bounds(dworld, dlut, world, blob, expect_air=True, expect_mid=True):
     """Every cell's (1 / s, R) per band bounds the attenuation of every voxel within
     R, and every voxel outside the body box lies within the majorant of every cell
     marked outside it."""
@@ -71,8 +71,8 @@ def _check_grid_bounds(dworld, dlut, world, blob, expect_air=True):
             assert (s_cell < 0.01).mean() > 0.05, np.unique(s_cell)
             assert np.nanmax(np.where(s_cell < 0.01, R_cell, np.nan)) > 30.0
             assert marked.any() and (~marked).any()
-        # some cells get a level well below the global majorant
-        assert np.any((s_cell > 0.05) & (s_cell < 0.7)), np.unique(s_cell)
+        if expect_mid:  # some cells get a level well below the global majorant
+            assert np.any((s_cell > 0.05) & (s_cell < 0.7)), np.unique(s_cell)
         for s in np.unique(s_cell[np.isfinite(R_cell)]):
             hot = scale > s * (1.0 + 1e-4)
             if not hot.any():
@@ -101,25 +101,64 @@ def test_majorant_grid_bounds_attenuation(gpu_ctx):
     dworld.close()
 
 
-def _continuous_world(n=48, distinct=None, seed=3):
+def _continuous_world(n=48, distinct=None, seed=3, dims=None, spacing=3.0):
     """Soft tissue and bone with densities from a smooth field: ``distinct`` density
-    values (compact layout, many levels per band) or all different (8-byte layout)."""
+    values (compact layout, many levels per band) or all different (8-byte layout);
+    ``dims`` (x, y, z) for a non-cubic grid."""
     import dxmclib_gb300 as dx
     rng = np.random.default_rng(seed)
-    z, y, x = np.meshgrid(*[np.linspace(-1, 1, n)] * 3, indexing="ij")
+    nx, ny, nz = dims or (n, n, n)
+    z, y, x = np.meshgrid(np.linspace(-1, 1, nz), np.linspace(-1, 1, ny), np.linspace(-1, 1, nx), indexing="ij")
     field = 0.05 + 1.9 * np.clip(0.5 + 0.5 * np.sin(3 * x + rng.uniform(0, 3)) * np.cos(2 * y) * np.cos(z), 0, 1)
     if distinct:
         field = np.round(field * distinct / 2.0) * 2.0 / distinct + 0.001
     mat = (field > 1.3).astype(np.uint8)
     w = dx.World()
-    w.setDimensions((n, n, n))
-    w.setSpacing((3.0, 3.0, 3.0))
+    w.setDimensions((nx, ny, nz))
+    w.setSpacing((spacing, spacing, spacing))
     w.setDensityArray(field.astype(np.float32).ravel())
     w.setMaterialIndexArray(mat.ravel())
     w.addMaterialToMap(dx.Material("Tissue, Soft (ICRP)"))
     w.addMaterialToMap(dx.Material("Bone, Cortical (ICRP)"))
     assert w.isValid()
     return w
+
+
+@pytest.mark.parametrize("dims", [(12, 400, 12), (12, 12, 400)])
+def test_grid_bounds_on_long_axes(gpu_ctx, dims):
+    """The y pass of the distance transform reads tiles of the grid from shared
+    memory where a line of cells fits; longer lines (here 400 cells of 6 mm
+    along y) take the global-memory kernel, as the z pass does.  Both must bound
+    the attenuation, with safe lengths of many cells along the long axis."""
+    import dxmclib_gb300 as dx
+    # a rod of low-density tissue with a bone slab across the long axis: cells far
+    # from the slab get low scales with safe lengths of many cells along that axis
+    nx, ny, nz = dims
+    axis = 1 if ny > nz else 0  # axis of the (z, y, x) array along the rod
+    mat = np.zeros((nz, ny, nx), np.uint8)
+    sl = [slice(None)] * 3
+    sl[axis] = slice(180, 200)
+    mat[tuple(sl)] = 1
+    dens = np.where(mat == 1, 1.92, 0.3).astype(np.float32)
+    world = dx.World()
+    world.setDimensions(dims)
+    world.setSpacing((6.0, 6.0, 6.0))
+    world.setDensityArray(dens.ravel())
+    world.setMaterialIndexArray(mat.ravel())
+    world.addMaterialToMap(dx.Material("Tissue, Soft (ICRP)"))
+    world.addMaterialToMap(dx.Material("Bone, Cortical (ICRP)"))
+    assert world.isValid()
+    blob = dx.LutBlob.from_world(world, 90.0)
+    dworld = dx.DeviceWorld(gpu_ctx, world)
+    dlut = dx.DeviceLut(gpu_ctx, blob)
+    dworld.prepare(dlut)
+    shift, _, _, cells = dworld.majorant(dlut)
+    assert max(cells.shape[:3]) == 400 and list(shift) == [0, 0, 0]
+    R = np.abs(cells[..., 1])
+    assert np.nanmax(np.where(np.isfinite(R), R, np.nan)) > 100 * 6.0  # safe lengths of 100+ cells
+    _check_grid_bounds(dworld, dlut, world, blob, expect_air=False, expect_mid=False)
+    dlut.close()
+    dworld.close()
 
 
 @pytest.mark.parametrize("distinct", [120, None])
