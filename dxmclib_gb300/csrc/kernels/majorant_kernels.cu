@@ -26,9 +26,9 @@
 //      pairs of a group run in one launch per pass (blockIdx.y = pair);
 //   3. each cell keeps the (level, R) of smallest expected steps per mm,
 //      mu / (1 - exp(-mu R)) with mu = scale * global majorant at the band's
-//      reference energy, or the global majorant itself (R infinite); the z
-//      pass and this choice are one kernel that tries a band's levels in
-//      ascending order, so the grid does not depend on the grouping.
+//      reference energy, or the global majorant itself (R infinite); one
+//      thread per cell and band tries the band's levels in ascending order,
+//      so the grid does not depend on the grouping.
 // Last, the cells outside the box of all cells above their band's emptiest
 // level get -R: there a flight may also run to that box (MajorantGrid).
 #include <algorithm>
@@ -247,7 +247,7 @@ __device__ __forceinline__ float axis_min(const MajorantBuild& b, const float* _
         b.edge[AXIS]);
 }
 
-// Shared-memory tiles for the y pass: the lines of 32 adjacent x cells,
+// Shared-memory tiles for the y and z passes: the lines of 32 adjacent x cells,
 // tile[t * 32 + lane] = the line of x0 + lane at position t (infinity past the
 // grid), so a warp scanning its 32 lines reads 32 consecutive banks.
 constexpr int TILE_W = 32;
@@ -319,29 +319,74 @@ __global__ void majorant_choose_kernel(const __grid_constant__ MajorantBuild b, 
     }
 }
 
-// The y pass with tiles in shared memory (blockIdx.y = pair): one tile per x
-// group of 32 cells and z, the block's warps taking y rows in turn.
-__global__ void majorant_axis_y_tiled_kernel(MajorantBuild b, const float* __restrict__ in, float* __restrict__ out)
+// The y (AXIS 1) or z (AXIS 2) pass with tiles in shared memory (blockIdx.y =
+// pair): one tile per x group of 32 cells and the other axis' position, the
+// block's warps taking the cells of the lines in turn.
+template <int AXIS>
+__global__ void majorant_axis_tiled_kernel(MajorantBuild b, const float* __restrict__ in, float* __restrict__ out)
 {
     extern __shared__ float tile[];
     const uint32_t n0 = b.n[0], n1 = b.n[1], n2 = b.n[2];
     const uint64_t ncell = static_cast<uint64_t>(n0) * n1 * n2;
     const uint64_t off = static_cast<uint64_t>(blockIdx.y) * ncell;
+    const uint32_t n = AXIS == 1 ? n1 : n2;      // cells along the lines
+    const uint32_t other = AXIS == 1 ? n2 : n1;  // positions of the tiles across them
+    const uint64_t stride = AXIS == 1 ? n0 : static_cast<uint64_t>(n0) * n1;
+    const uint64_t other_stride = AXIS == 1 ? static_cast<uint64_t>(n0) * n1 : n0;
     const uint32_t xtiles = (n0 + TILE_W - 1) / TILE_W;
-    const uint64_t tiles = static_cast<uint64_t>(xtiles) * n2;
+    const uint64_t tiles = static_cast<uint64_t>(xtiles) * other;
     const uint32_t lane = threadIdx.x % TILE_W, warps = blockDim.x / TILE_W;
     for (uint64_t ti = blockIdx.x; ti < tiles; ti += gridDim.x) {
-        const uint32_t z = static_cast<uint32_t>(ti / xtiles), x0 = static_cast<uint32_t>(ti % xtiles) * TILE_W;
-        const uint64_t base = off + static_cast<uint64_t>(z) * n1 * n0;
+        const uint32_t o = static_cast<uint32_t>(ti / xtiles), x0 = static_cast<uint32_t>(ti % xtiles) * TILE_W;
+        const uint64_t base = off + o * other_stride;
         __syncthreads(); // the previous tile is no longer read
-        load_tile(tile, in, x0, n0, static_cast<int>(n1), base, n0);
+        load_tile(tile, in, x0, n0, static_cast<int>(n), base, stride);
         __syncthreads();
         const uint32_t x = x0 + lane;
-        for (uint32_t y = threadIdx.x / TILE_W; y < n1; y += warps) {
-            const float best = line_min([&](int t) { return tile[t * TILE_W + lane]; }, static_cast<int>(n1),
-                static_cast<int>(y), b.edge[1]);
+        for (uint32_t t = threadIdx.x / TILE_W; t < n; t += warps) {
+            const float best = line_min([&](int k) { return tile[k * TILE_W + lane]; }, static_cast<int>(n),
+                static_cast<int>(t), b.edge[AXIS]);
             if (x < n0)
-                out[base + static_cast<uint64_t>(y) * n0 + x] = best;
+                out[base + t * stride + x] = best;
+        }
+    }
+}
+
+// The choice after a tiled z pass (blockIdx.y = band): d holds each pair's
+// squared distances; the arithmetic of majorant_choose_kernel.
+__global__ void majorant_choose_final_kernel(const __grid_constant__ MajorantBuild b, const __grid_constant__ MajorantPairs pairs,
+    const float* __restrict__ d, float2* __restrict__ cells, float* __restrict__ cost)
+{
+    const int band = blockIdx.y;
+    const int p0 = pairs.first[band], p1 = pairs.first[band + 1];
+    if (p0 == p1)
+        return;
+    const uint64_t ncell = static_cast<uint64_t>(b.n[0]) * b.n[1] * b.n[2];
+    const float mu_ref = b.mu_refs[band];
+    for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c < ncell;
+         c += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        float best_cost = cost[static_cast<uint64_t>(band) * ncell + c];
+        float2 choice = make_float2(0.0f, 0.0f);
+        bool changed = false;
+        for (int p = p0; p < p1; ++p) {
+            const float best = d[static_cast<uint64_t>(p) * ncell + c];
+            if (best <= 0.0f)
+                continue; // the cell itself lies in the dilated set
+            const float R = fmaf(sqrtf(best), 0.999f, -1.0e-3f);
+            if (!(R > 0.0f))
+                continue;
+            const float s = level_scale(pairs.level[p], b.levels_per_octave);
+            const float mu = mu_ref * s;
+            const float c_new = mu / (1.0f - expf(-mu * R)); // R infinite: mu
+            if (c_new < best_cost) {
+                best_cost = c_new;
+                choice = make_float2(1.0f / s, R);
+                changed = true;
+            }
+        }
+        if (changed) {
+            cost[static_cast<uint64_t>(band) * ncell + c] = best_cost;
+            cells[c * b.bands + band] = choice;
         }
     }
 }
@@ -443,18 +488,25 @@ cudaError_t launch_majorant_level_passes(const MajorantBuild& b, const MajorantP
     const uint64_t rows = static_cast<uint64_t>(b.n[1]) * b.n[2];
     majorant_sweep_x_kernel<<<dim3(static_cast<unsigned>(std::min<uint64_t>((rows + 7) / 8, 4096)), pairs.count), 256, 0, stream>>>(
         b, pairs, minlev, d1);
-    // the y pass from shared-memory tiles where a tile's lines fit (the same
-    // arithmetic in the same order as the global-memory kernel); the z pass and
-    // choice read global memory: there one thread per cell hides the latency of
-    // the cost arithmetic better than a tile's threads walking many cells each
+    // the y and z passes from shared-memory tiles where a tile's lines fit (the
+    // same arithmetic in the same order as the global-memory kernels), the
+    // choice then one thread per cell and band; otherwise the z pass runs inside
+    // the choice from global memory
     const size_t smem_y = static_cast<size_t>(b.n[1]) * TILE_W * sizeof(float);
+    const size_t smem_z = static_cast<size_t>(b.n[2]) * TILE_W * sizeof(float);
     const uint64_t xtiles = (b.n[0] + TILE_W - 1) / TILE_W;
     if (smem_y <= TILE_SMEM_MAX)
-        majorant_axis_y_tiled_kernel<<<dim3(static_cast<unsigned>(std::min<uint64_t>(xtiles * b.n[2], 4096)), pairs.count), 256, smem_y,
+        majorant_axis_tiled_kernel<1><<<dim3(static_cast<unsigned>(std::min<uint64_t>(xtiles * b.n[2], 4096)), pairs.count), 256, smem_y,
             stream>>>(b, d1, d0);
     else
         majorant_axis_kernel<1><<<dim3(grid_for(ncell), pairs.count), 256, 0, stream>>>(b, d1, d0);
-    majorant_choose_kernel<<<dim3(grid_for(ncell), b.bands), 256, 0, stream>>>(b, pairs, d0, cells, cost);
+    if (smem_z <= TILE_SMEM_MAX) {
+        majorant_axis_tiled_kernel<2><<<dim3(static_cast<unsigned>(std::min<uint64_t>(xtiles * b.n[1], 4096)), pairs.count), 256, smem_z,
+            stream>>>(b, d0, d1);
+        majorant_choose_final_kernel<<<dim3(grid_for(ncell), b.bands), 256, 0, stream>>>(b, pairs, d1, cells, cost);
+    } else {
+        majorant_choose_kernel<<<dim3(grid_for(ncell), b.bands), 256, 0, stream>>>(b, pairs, d0, cells, cost);
+    }
     return cudaGetLastError();
 }
 
