@@ -79,6 +79,9 @@ __global__ void majorant_level_kernel(WorldParams w, const float* __restrict__ s
 #pragma unroll
         for (int k = 0; k < MAJORANT_MAX_BANDS; ++k)
             m[k] = 0.0f;
+        int last_idx = -1; // a voxel equal to the one before adds nothing to the maxima
+        float last_dens = 0.0f;
+        bool last_forced = false;
         for (uint32_t z = z0; z < z1; ++z) {
             for (uint32_t y = y0; y < y1; ++y) {
                 const uint64_t row = static_cast<uint64_t>(z) * w.nxy + static_cast<uint64_t>(y) * w.dims[0];
@@ -94,6 +97,11 @@ __global__ void majorant_level_kernel(WorldParams w, const float* __restrict__ s
                         dens = v.density;
                         forced = v.measurement != 0;
                     }
+                    if (idx == last_idx && dens == last_dens && forced == last_forced)
+                        continue;
+                    last_idx = idx;
+                    last_dens = dens;
+                    last_forced = forced;
 #pragma unroll
                     for (int k = 0; k < MAJORANT_MAX_BANDS; ++k)
                         if (k < b.bands)
