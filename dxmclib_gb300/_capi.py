@@ -193,6 +193,7 @@ SIGNATURES = {
     "dxmc_gpu_batch_free": (None, [VP]),
     "dxmc_gpu_transport_noalloc": (C.c_int, [VP, VP, VP, C.POINTER(JobDesc), VP, VP, C.POINTER(JobStats)]),
     "dxmc_gpu_probe_interactions": (C.c_int, [VP, VP, C.c_int, C.c_int, C.c_int, D, C.c_uint64, C.c_uint64, FP, FP, FP]),
+    "dxmc_gpu_probe_uniform": (C.c_int, [VP, C.c_uint64, C.c_uint64, C.c_uint32, C.c_int, C.c_int32, U64P]),
 }
 
 _lib = None

@@ -20,6 +20,10 @@
 
 using namespace dxmc_gb300;
 
+namespace dxmc_gb300::noalloc {
+cudaError_t preload(int device); // noalloc.cu
+}
+
 // Warp scheduling of the transport kernel: refill idle lanes once this many
 // are idle; run the per-type interaction passes once this many lanes wait.
 constexpr int DEFAULT_REGEN_THRESHOLD = 8;        // photons generated in the transport kernel
@@ -577,6 +581,15 @@ int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out)
         || cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
         if (ctx->pool)
             cudaMemPoolDestroy(ctx->pool);
+        cudaStreamDestroy(ctx->result_stream);
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return DXMC_ERR_DEVICE;
+    }
+    // the no-allocation entry point must not meet a lazy module load (which
+    // allocates) in its first call: load its module and the transport kernels now
+    if (noalloc::preload(ctx->device) != cudaSuccess) {
+        cudaMemPoolDestroy(ctx->pool);
         cudaStreamDestroy(ctx->result_stream);
         cudaStreamDestroy(ctx->stream);
         delete ctx;
@@ -1389,8 +1402,13 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
         const auto* h = jd->heel;
         if (h->energy_size <= 0 || h->angle_size <= 0 || !h->weights || !(h->energy_step > 0) || !(h->angle_step != 0))
             return fail(ctx, DXMC_ERR_INVALID, "invalid heel table");
-        for (int i = 0; i < h->energy_size * h->angle_size; ++i)
-            heel.push_back(static_cast<float>(h->weights[i]));
+        // the table size in 64 bits: a product that wraps in int would leave the kernel
+        // indexing a short table with the caller's (huge) sizes
+        const int64_t heel_n = static_cast<int64_t>(h->energy_size) * h->angle_size;
+        if (heel_n > DXMC_MAX_HEEL_WEIGHTS)
+            return fail(ctx, DXMC_ERR_INVALID, "heel table has " + std::to_string(heel_n) + " weights, more than the maximum of "
+                    + std::to_string(DXMC_MAX_HEEL_WEIGHTS));
+        heel.assign(h->weights, h->weights + heel_n);
     }
     std::vector<float> bt_a, bt_w;
     if (jd->bowtie) {
@@ -2503,6 +2521,25 @@ int dxmc_gpu_probe_interactions(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, 
     DXMC_CUDA(ctx, cudaMemcpyAsync(out_cos, buf, n * sizeof(float), cudaMemcpyDeviceToHost, s));
     DXMC_CUDA(ctx, cudaMemcpyAsync(out_energy, buf + n, n * sizeof(float), cudaMemcpyDeviceToHost, s));
     DXMC_CUDA(ctx, cudaMemcpyAsync(out_dep, buf + 2 * n, n * sizeof(float), cudaMemcpyDeviceToHost, s));
+    cudaFreeAsync(buf, s);
+    DXMC_CUDA(ctx, cudaStreamSynchronize(s));
+    return DXMC_OK;
+}
+
+int dxmc_gpu_probe_uniform(dxmc_gpu_ctx* ctx, uint64_t seed, uint64_t n_streams, uint32_t draws_per_stream, int kind,
+    int32_t n_bins, uint64_t* hist)
+{
+    if (!ctx || !hist || n_streams == 0 || draws_per_stream == 0 || kind < 0 || kind > 2 || n_bins < 1 || n_bins > 4096)
+        return DXMC_ERR_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    unsigned long long* buf = nullptr;
+    const size_t bytes = (static_cast<size_t>(n_bins) + 1) * sizeof(unsigned long long);
+    DXMC_CUDA(ctx, pool_alloc(ctx, &buf, bytes, s));
+    DXMC_CUDA(ctx, cudaMemsetAsync(buf, 0, bytes, s));
+    DXMC_CUDA(ctx, dev::launch_probe_uniform(seed, n_streams, draws_per_stream, kind, n_bins, buf, ctx->sm_count, s));
+    DXMC_CUDA(ctx, cudaMemcpyAsync(hist, buf, bytes, cudaMemcpyDeviceToHost, s));
     cudaFreeAsync(buf, s);
     DXMC_CUDA(ctx, cudaStreamSynchronize(s));
     return DXMC_OK;

@@ -17,9 +17,14 @@
 // points; larger jobs are rejected with DXMC_ERR_INVALID and a message.  The
 // array (about 2.2 MB) stays resident on every device that loads the library
 // until the process exits.  All calls share it: calls that overlap on the GPU
-// race with each other, so issue them one at a time.  The first call on each
-// device looks up the array's device address (cudaGetSymbolAddress) with that
-// device current; make that first call before any stream capture.  Local-majorant
+// race with each other, so issue them one at a time.  dxmc_gpu_ctx_create
+// loads this file's module and the transport kernels' modules on its device
+// (CUDA loads modules lazily, and loading one allocates device memory) and looks
+// up the array's device address (cudaGetSymbolAddress) with that device current,
+// so a caller that creates its context before it fills the device meets no
+// allocation in its first call; a first call on a device whose context skipped
+// that step does the look-up itself and should come before any stream capture.
+// Local-majorant
 // tracking uses the (world, LUT) grid only if it was built before
 // (dxmc_gpu_world_prepare, or an earlier job on the pair); otherwise the call
 // tracks with the global majorant.
@@ -86,6 +91,30 @@ cudaError_t scratch_address(int device, unsigned char** out)
     *out = static_cast<unsigned char*>(g_scratch_address[device]);
     return cudaSuccess;
 }
+
+__global__ void noalloc_setup_kernel(unsigned char* s, uint32_t n_exposures, int spec_n, int heel_n, int bowtie_n);
+
+} // namespace
+
+namespace dxmc_gb300::noalloc {
+// Called by dxmc_gpu_ctx_create with the context's device current: loads the
+// module of the scratch array and of the set-up kernel, and the transport
+// kernels' modules, and records the array's device address, so that the first
+// dxmc_gpu_transport_noalloc call on the device triggers no lazy module load.
+cudaError_t preload(int device)
+{
+    unsigned char* s = nullptr;
+    cudaError_t e = scratch_address(device, &s);
+    cudaFuncAttributes attr {};
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&attr, noalloc_setup_kernel);
+    if (e == cudaSuccess)
+        e = dev::preload_transport_kernels();
+    return e;
+}
+} // namespace dxmc_gb300::noalloc
+
+namespace {
 
 // Builds the job tables inside the scratch array from the raw copies of the
 // caller's host structures: packed exposures, history prefix sums, the
@@ -251,11 +280,14 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         return reject(ctx, "invalid spectrum");
     if (spec_n > NOALLOC_MAX_SPECTRUM)
         return reject(ctx, "dxmc_gpu_transport_noalloc: " + std::to_string(spec_n) + " spectrum bins exceed the maximum of " + std::to_string(NOALLOC_MAX_SPECTRUM));
-    const int heel_n = jd->heel ? jd->heel->energy_size * jd->heel->angle_size : 0;
     if (jd->heel && (jd->heel->energy_size <= 0 || jd->heel->angle_size <= 0 || !jd->heel->weights || !(jd->heel->energy_step > 0) || !(jd->heel->angle_step != 0)))
         return reject(ctx, "invalid heel table");
-    if (heel_n > NOALLOC_MAX_HEEL)
-        return reject(ctx, "dxmc_gpu_transport_noalloc: " + std::to_string(heel_n) + " heel weights exceed the maximum of " + std::to_string(NOALLOC_MAX_HEEL));
+    // the table size in 64 bits, checked before it narrows: a product that wrapped in
+    // int could pass the limit while the kernel indexes with the caller's sizes
+    const int64_t heel_n64 = jd->heel ? static_cast<int64_t>(jd->heel->energy_size) * jd->heel->angle_size : 0;
+    if (heel_n64 > NOALLOC_MAX_HEEL)
+        return reject(ctx, "dxmc_gpu_transport_noalloc: " + std::to_string(heel_n64) + " heel weights exceed the maximum of " + std::to_string(NOALLOC_MAX_HEEL));
+    const int heel_n = static_cast<int>(heel_n64);
     const int bowtie_n = jd->bowtie ? jd->bowtie->n : 0;
     if (jd->bowtie && (bowtie_n <= 0 || !jd->bowtie->angles || !jd->bowtie->weights))
         return reject(ctx, "invalid bow-tie table");
@@ -361,8 +393,10 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
             per_sm = 1;
         e = dev::launch_transport(p, jd->model, capi::ctx_sm_count(ctx) * per_sm, block, smem, stream);
     }
+    // the counters are read back on every call (into this stack copy, no allocation):
+    // a rejection-cap overflow is reported whether or not the caller asked for stats
     dev::JobCounters c {};
-    if (e == cudaSuccess && stats)
+    if (e == cudaSuccess)
         e = cudaMemcpyAsync(&c, s + OFF_COUNTERS, sizeof(c), cudaMemcpyDeviceToHost, stream);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(stream);
@@ -380,7 +414,7 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         capi::ctx_set_error(ctx, std::string("dxmc_gpu_transport_noalloc: ") + cudaGetErrorString(e));
         return DXMC_ERR_DEVICE;
     }
-    if (stats && c.overflows) {
+    if (c.overflows) {
         capi::ctx_set_error(ctx, "sampling loops hit the rejection cap");
         return DXMC_ERR_REJECTION_CAP;
     }

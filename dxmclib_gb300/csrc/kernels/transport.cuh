@@ -155,6 +155,9 @@ int batch_max_blocks_per_sm(int model);
 // miss the world are counted but not queued).
 cudaError_t launch_generate(const TransportParams& p, uint64_t first, uint64_t count, int grid, cudaStream_t stream);
 cudaError_t launch_transport(const TransportParams& p, int model, int grid, int block, size_t smem, cudaStream_t stream);
+// Loads the modules of every single-job transport kernel on the current device
+// (CUDA loads modules lazily, on first use, and a load allocates device memory).
+cudaError_t preload_transport_kernels();
 // blocks per SM for this configuration; also raises the kernel's dynamic shared-memory limit
 int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem);
 // dynamic shared memory the transport kernel needs for a LUT image of lut_bytes
@@ -215,6 +218,9 @@ cudaError_t launch_majorant_level_passes(const MajorantBuild& b, const MajorantP
     float* d0, float* d1, float2* cells, float* cost, cudaStream_t stream);
 cudaError_t launch_max_density(const Voxel* voxels, uint64_t n, unsigned int* out_bits, int n_materials, cudaStream_t stream);
 cudaError_t launch_probe_lut(const float* lut, LutMeta meta, int material, const double* energies, int n, double* out_att, double* out_maxinv, cudaStream_t stream);
+// Histogram of the per-history random streams' output (see dxmc_gpu_probe_uniform).
+cudaError_t launch_probe_uniform(uint64_t seed, uint64_t n_streams, uint32_t draws, int kind, int nbins,
+    unsigned long long* hist, int sm_count, cudaStream_t stream);
 cudaError_t launch_probe_interactions(const float* lut, LutMeta meta, int material, int model, int kind, float energy,
     uint64_t n, uint64_t seed, float* out_cos, float* out_energy, float* out_dep, cudaStream_t stream);
 

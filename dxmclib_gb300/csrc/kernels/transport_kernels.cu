@@ -1179,6 +1179,42 @@ namespace {
         }
     }
 
+    // Histogram of the per-history streams' output (the generator every sampler
+    // draws from): n_streams streams of `draws` values each.  kind 0: uniform()
+    // in [0, 1); kind 1: uniform_open() in (0, 1], binned as 1 - u; kind 2:
+    // below(nbins).  hist[nbins] counts values outside their stated range.
+    __global__ void probe_uniform_kernel(uint64_t seed, uint64_t n_streams, uint32_t draws, int kind, int nbins,
+        unsigned long long* hist)
+    {
+        extern __shared__ unsigned int sbins[];
+        for (int i = threadIdx.x; i <= nbins; i += blockDim.x)
+            sbins[i] = 0u;
+        __syncthreads();
+        for (uint64_t h = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; h < n_streams;
+             h += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+            Rng rng;
+            rng.init(seed, h);
+            for (uint32_t k = 0; k < draws; ++k) {
+                int b;
+                if (kind == 0) {
+                    const float u = rng.uniform();
+                    b = (u >= 0.0f && u < 1.0f) ? min(static_cast<int>(u * nbins), nbins - 1) : nbins;
+                } else if (kind == 1) {
+                    const float u = rng.uniform_open();
+                    b = (u > 0.0f && u <= 1.0f) ? min(static_cast<int>((1.0f - u) * nbins), nbins - 1) : nbins;
+                } else {
+                    const uint32_t v = rng.below(static_cast<uint32_t>(nbins));
+                    b = v < static_cast<uint32_t>(nbins) ? static_cast<int>(v) : nbins;
+                }
+                atomicAdd(&sbins[b], 1u);
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i <= nbins; i += blockDim.x)
+            if (sbins[i])
+                atomicAdd(hist + i, static_cast<unsigned long long>(sbins[i]));
+    }
+
 } // namespace
 
 template <int MODEL, bool PALETTE>
@@ -1233,6 +1269,18 @@ cudaError_t launch_transport(const TransportParams& p, int model, int grid, int 
     void* fn = transport_function(model, palette);
     void* args[] = { const_cast<TransportParams*>(&p) };
     return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, stream);
+}
+
+cudaError_t preload_transport_kernels()
+{
+    for (int model = 0; model < 3; ++model)
+        for (int palette = 0; palette < 2; ++palette) {
+            cudaFuncAttributes attr {};
+            const cudaError_t e = cudaFuncGetAttributes(&attr, transport_function(model, palette != 0));
+            if (e != cudaSuccess)
+                return e;
+        }
+    return cudaSuccess;
 }
 
 int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem)
@@ -1303,6 +1351,15 @@ cudaError_t launch_probe_interactions(const float* lut, LutMeta meta, int materi
         probe_interactions_kernel<1><<<grid, block, 0, stream>>>(lut, meta, material, kind, energy, n, seed, out_cos, out_energy, out_dep);
     else
         probe_interactions_kernel<2><<<grid, block, 0, stream>>>(lut, meta, material, kind, energy, n, seed, out_cos, out_energy, out_dep);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_probe_uniform(uint64_t seed, uint64_t n_streams, uint32_t draws, int kind, int nbins,
+    unsigned long long* hist, int sm_count, cudaStream_t stream)
+{
+    const int block = 256;
+    const int grid = static_cast<int>(std::min<uint64_t>((n_streams + block - 1) / block, static_cast<uint64_t>(sm_count) * 8));
+    probe_uniform_kernel<<<grid, block, (nbins + 1) * sizeof(unsigned int), stream>>>(seed, n_streams, draws, kind, nbins, hist);
     return cudaGetLastError();
 }
 

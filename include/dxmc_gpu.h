@@ -171,7 +171,10 @@ typedef struct dxmc_spectrum_desc {
     const double* weights;
 } dxmc_spectrum_desc;
 
-/* Heel table: HeelFilter (beamfilters.hpp:435-569). */
+/* Heel table: HeelFilter (beamfilters.hpp:435-569).  At most
+ * DXMC_MAX_HEEL_WEIGHTS weights (energy_size * angle_size, counted in 64 bits);
+ * a larger table is rejected with DXMC_ERR_INVALID. */
+#define DXMC_MAX_HEEL_WEIGHTS (1 << 24)
 typedef struct dxmc_heel_desc {
     double energy_start, energy_step;
     int32_t energy_size;
@@ -409,6 +412,17 @@ int dxmc_gpu_probe_lut(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, const dou
  * and the energy imparted for each sample. */
 int dxmc_gpu_probe_interactions(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, int model, int kind,
     double energy, uint64_t n, uint64_t seed, float* out_cos, float* out_energy, float* out_deposit);
+
+/* Histogram of the per-history random streams every device sampler draws
+ * from (xoshiro128+ seeded by Philox4x32-10 of (seed, stream)): n_streams
+ * streams of draws_per_stream values.  kind 0: uniform in [0, 1); kind 1: the
+ * open-at-zero uniform in (0, 1] used for logarithms, binned as 1 - u; kind 2:
+ * an integer below n_bins.  hist gets n_bins + 1 counts, the last one of the
+ * values outside their range.  Replaces RandomState's generator
+ * (dxmcrandom.hpp:37-167) and carries the reference's uniformity check
+ * (tests/testrandom.cpp:21-58) over to the device generator. */
+int dxmc_gpu_probe_uniform(dxmc_gpu_ctx* ctx, uint64_t seed, uint64_t n_streams, uint32_t draws_per_stream, int kind,
+    int32_t n_bins, uint64_t* hist);
 
 #ifdef __cplusplus
 }

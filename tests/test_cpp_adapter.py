@@ -2,7 +2,7 @@
 
 Compiles the adapter together with DXMClib's unmodified headers (and the
 project Material backend that stands in for xraylib) and runs its host-side
-checks.  Needs the reference checkout, so it is skipped where that is absent.
+checks.  Needs the reference checkout, named by DXMC_REFERENCE; skipped without it.
 """
 from __future__ import annotations
 
@@ -13,12 +13,12 @@ from pathlib import Path
 import pytest
 
 REPO = Path(__file__).resolve().parents[1]
-REF = Path(os.environ.get("DXMC_REFERENCE", "/root/reference"))
+REF = Path(os.environ["DXMC_REFERENCE"]) if os.environ.get("DXMC_REFERENCE") else None
 
 
 def test_cpp_adapter_host_checks(lib, tmp_path):
-    if not (REF / "include" / "dxmc").is_dir():
-        pytest.skip("DXMClib headers not available on this machine")
+    if REF is None or not (REF / "include" / "dxmc").is_dir():
+        pytest.skip("DXMClib headers not available (set DXMC_REFERENCE to a reference checkout)")
     exe = tmp_path / "adapter_check"
     cmd = ["g++", "-std=c++20", "-O1", "-pthread", f"-I{REF / 'include'}", f"-I{REPO / 'include'}",
            str(REPO / "tests" / "adapter" / "adapter_check.cpp"), str(REPO / "oracle" / "material_backend.cpp"),

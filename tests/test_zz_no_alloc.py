@@ -90,18 +90,71 @@ def test_noalloc_matches_job_entry_point(gpu_ctx, golden):
     jd = _job_desc(exposures, spectrum, heel, bowtie, seed, keep)
     tally = torch.full((2 * n,), -1.0, dtype=torch.float64, device="cuda")
     nev = torch.full((n,), 7, dtype=torch.int32, device="cuda")
-    for call in range(2):  # two calls in a row share (and must clear) the static scratch
-        st = A.JobStats()
-        rc = ctx.lib.dxmc_gpu_transport_noalloc(ctx.handle, dworld.handle, dlut.handle, C.byref(jd),
-                                                C.c_void_p(tally.data_ptr()), C.c_void_p(nev.data_ptr()), C.byref(st))
+
+    def noalloc(desc, dw, with_stats=True):
+        st = A.JobStats() if with_stats else None
+        rc = ctx.lib.dxmc_gpu_transport_noalloc(ctx.handle, dw.handle, dlut.handle, C.byref(desc),
+                                                C.c_void_p(tally.data_ptr()), C.c_void_p(nev.data_ptr()),
+                                                C.byref(st) if with_stats else None)
         A.check(rc, ctx.handle, "dxmc_gpu_transport_noalloc")
         torch.cuda.synchronize()
-        t = tally.cpu().numpy()
+        return st, tally.cpu().numpy(), nev.cpu().numpy().view(np.uint32)
+
+    def same(t, nv, e, e2, ne, label):
+        np.testing.assert_allclose(t[0::2], e, rtol=1e-9, atol=1e-12 * e.max(), err_msg=label)
+        np.testing.assert_allclose(t[1::2], e2, rtol=1e-9, atol=1e-12 * e2.max(), err_msg=label)
+        np.testing.assert_array_equal(nv, ne, err_msg=label)
+
+    for call in range(2):  # two calls in a row share (and must clear) the static scratch
+        st, t, nv = noalloc(jd, dworld)
         assert st.histories == stats_ref["histories"] == int(np.sum(exposures.n_histories)), call
         assert st.steps == stats_ref["steps"] and st.deposits == stats_ref["deposits"], call
-        np.testing.assert_allclose(t[0::2], e_ref, rtol=1e-9, atol=1e-12 * e_ref.max(), err_msg=f"call {call}")
-        np.testing.assert_allclose(t[1::2], e2_ref, rtol=1e-9, atol=1e-12 * e2_ref.max(), err_msg=f"call {call}")
-        np.testing.assert_array_equal(nev.cpu().numpy().view(np.uint32), nev_ref, err_msg=f"call {call}")
+        same(t, nv, e_ref, e2_ref, nev_ref, f"call {call}")
+
+    # without a stats pointer the call still reads the device counters (a rejection-cap
+    # overflow is reported through the return code) and gives the same tallies
+    _, t, nv = noalloc(jd, dworld, with_stats=False)
+    same(t, nv, e_ref, e2_ref, nev_ref, "stats = NULL")
+
+    # the reference's global majorant, both entry points
+    jd.tracking = A.TRACKING_GLOBAL
+    job = dx.Job(ctx, dworld, dlut, exposures, spectrum, heel, bowtie, seed=seed, model=1, tally_mode=0,
+                 tracking=A.TRACKING_GLOBAL)
+    eg, e2g, neg, stg = job.result(A.OUTPUT_RAW)
+    job.close()
+    st, t, nv = noalloc(jd, dworld)
+    assert st.steps == stg["steps"] and st.deposits == stg["deposits"]
+    same(t, nv, eg, e2g, neg, "global majorant")
+    assert st.steps > stats_ref["steps"]  # the local grid really was in use above
+
+    # local majorants on a world whose grid was built by dxmc_gpu_world_prepare (no job
+    # has run on it): the no-allocation call tracks with that grid, as a regular job does
+    dworld2 = dx.DeviceWorld(ctx, world)
+    dworld2.prepare(dlut)
+    jd.tracking = A.TRACKING_LOCAL
+    st, t, nv = noalloc(jd, dworld2)
+    job = dx.Job(ctx, dworld2, dlut, exposures, spectrum, heel, bowtie, seed=seed, model=1, tally_mode=0,
+                 tracking=A.TRACKING_LOCAL)
+    el, e2l, nel, stl = job.result(A.OUTPUT_RAW)
+    job.close()
+    assert st.steps == stl["steps"] == stats_ref["steps"] and st.deposits == stl["deposits"]
+    same(t, nv, el, e2l, nel, "local majorant after prepare")
+    dworld2.close()
+    jd.tracking = A.TRACKING_DEFAULT
+
+    # a heel table whose size overflows 32 bits is rejected before any device work
+    huge = A.HeelDesc(heel.energy_start, heel.energy_step, 65536, 65536, heel.angle_start, heel.angle_step,
+                      jd.heel.contents.weights)
+    jd_huge = _job_desc(exposures, spectrum, heel, bowtie, seed, keep)
+    jd_huge.heel = C.pointer(huge)
+    rc = ctx.lib.dxmc_gpu_transport_noalloc(ctx.handle, dworld.handle, dlut.handle, C.byref(jd_huge),
+                                            C.c_void_p(tally.data_ptr()), C.c_void_p(nev.data_ptr()), None)
+    assert rc == A.DXMC_ERR_INVALID
+    assert b"maximum" in ctx.lib.dxmc_gpu_last_error(ctx.handle)
+    handle = C.c_void_p()
+    rc = ctx.lib.dxmc_gpu_job_submit(ctx.handle, dworld.handle, dlut.handle, C.byref(jd_huge), C.byref(handle))
+    assert rc == A.DXMC_ERR_INVALID and not handle.value
+    assert b"maximum" in ctx.lib.dxmc_gpu_last_error(ctx.handle)
 
     # jobs beyond the stated maximum are rejected with a clear message, before any device work
     big = dx.ExposureTable.build(np.zeros((8193, 3)), np.tile([1, 0, 0, 0, 1, 0], (8193, 1)), (0, 0, 0, 0), 1.0, 1, 60.0)
