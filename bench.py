@@ -20,9 +20,13 @@ FP32 transport with FP64 tallies.
   the local-majorant grid when the job tracks with local majorants, from the
   kernel's own step and deposit counters, over the kernel's CUDA-event
   duration, against the measured HBM copy bandwidth.
-* cpu_baseline / --impl reference: the oracle port (a C++ restatement of the
-  reference transport, oracle/port) on the host cores, on a bounded sample of
-  the same workload (a subset of the exposures).
+* cpu_baseline / --impl reference: the oracle port (oracle/port, a C++
+  restatement of the reference's Transport<T>, pinned to the reference's own
+  tallies on this configuration) in float precision, as Transport<float>, on
+  all host cores.  Each step is a fixed sample of the workload: every 10th
+  exposure at the workload's histories per exposure (about 1e7 histories),
+  with the reference's own exposure, spectrum, heel and LUT tables from the
+  golden fixture; the reference arm loads no product library.
 
 Multi-GPU (torchrun, N > 1): every rank runs an independent replica of the job
 (histories are independent; no data-path collective), barrier + max over ranks.
@@ -164,37 +168,58 @@ def build_workload(histories: int):
     return workloads.ct_helical(histories=histories)
 
 
-def cpu_sample(wl, lut_info, target_seconds: float, n_threads: int, model: int):
-    """Runs the oracle port on a bounded, evenly spread subset of the workload's exposures."""
-    sys.path.insert(0, str(REPO / "oracle" / "port"))
-    import binding as port
-    world = wl.world
-    src = wl.source
-    ex = src.exposures().as_matrix()
-    spec = src.spectrum()
-    heel = src.heel()
-    heel_d = None if heel is None else dict(energy_start=heel.energy_start, energy_step=heel.energy_step,
-                                             energy_size=heel.energy_size, angle_start=heel.angle_start,
-                                             angle_step=heel.angle_step, angle_size=heel.angle_size, weights=heel.weights)
-    dens = world.densityArray().astype(np.float64)
-    mat = world.materialIndexArray()
+CT_FIXTURE = REPO / "tests" / "golden" / "bench_ct_helical.npz"
+CPU_SAMPLE_STRIDE = 10  # the CPU legs run every 10th exposure of the workload
 
-    def run(n_exp, hpe):
-        idx = np.linspace(0, len(ex) - 1, n_exp).astype(np.int64)
-        sub = ex[idx].copy()
-        sub[:, 17] = hpe
-        e, e2, nev, secs, steps = port.transport(lut_info, world.dimensions(), world.spacing(), dens, mat, sub,
-                                                 model=model, n_threads=n_threads, seed=99,
-                                                 spectrum=(spec.energies, spec.weights), heel=heel_d)
-        return n_exp * hpe, secs
 
-    n_pilot, secs = run(64, 200)
-    rate = n_pilot / max(secs, 1e-3)
-    hist = int(max(rate * target_seconds, 64 * 200))
-    n_exp = min(len(ex), 450)
-    hpe = max(hist // n_exp, 1)
-    n, secs = run(n_exp, hpe)
-    return n, secs, f"{n_exp} of {len(ex)} exposures evenly spaced x {hpe} histories ({n} histories)"
+class CpuWorkload:
+    """The CT helical workload as the CPU legs run it, without the product library:
+    the seeded phantom (numpy), and the reference's own exposure, spectrum, heel and
+    LUT tables for this configuration from the golden fixture the reference
+    produced (tests/golden/make_golden.py).  The sample is every
+    CPU_SAMPLE_STRIDE-th exposure at the workload's histories per exposure."""
+
+    def __init__(self, histories: int):
+        from dxmclib_gb300.workloads import ct_phantom_arrays
+        g = dict(np.load(CT_FIXTURE))
+        self.dims = tuple(int(x) for x in g["dims"])
+        self.spacing = tuple(float(x) for x in g["spacing"])
+        mat, dens = ct_phantom_arrays(*self.dims, spacing=self.spacing, seed=int(g["phantom_seed"]))
+        self.material, self.density = mat, dens.astype(np.float64)
+        ex = g["exposures"].copy()
+        self.n_exposures = len(ex)
+        self.hpe = -(-int(histories) // self.n_exposures)  # as workloads.ct_source: ceil(histories / exposures)
+        ex[:, 17] = self.hpe
+        self.sample = ex[::CPU_SAMPLE_STRIDE].copy()
+        self.sample_histories = int(self.sample[:, 17].sum())
+        self.spectrum = (g["spec_energies"], g["spec_weights"])
+        hm = g["heel_meta"]
+        self.heel = dict(energy_start=hm[1], energy_step=hm[2], energy_size=hm[3], angle_start=hm[4],
+                         angle_step=hm[5], angle_size=hm[6], weights=g["heel_weights"])
+        self.g = g
+        self.describe = (f"{len(self.sample)} of {self.n_exposures} exposures (every {CPU_SAMPLE_STRIDE}th) x "
+                         f"{self.hpe} histories = {self.sample_histories} histories per step; reference exposure, "
+                         f"spectrum, heel and LUT tables from tests/golden/bench_ct_helical.npz")
+
+    def run(self, n_threads: int, model: int, precision: str, seed: int = 99):
+        """One sample step of the oracle port; returns its transport seconds."""
+        sys.path.insert(0, str(REPO / "oracle" / "port"))
+        import binding as port
+        _, _, _, secs, _ = port.transport(port.lut_from_fixture(self.g), self.dims, self.spacing, self.density,
+                                          self.material, self.sample, model=model, n_threads=n_threads, seed=seed,
+                                          spectrum=self.spectrum, heel=self.heel, precision=precision)
+        return secs
+
+
+def bench_config(args, n_hist: int, n_exposures: int) -> dict:
+    """The `config` object of both arms' JSON lines (identical by construction)."""
+    return {"workload": f"ct_helical_512x512x{200}", "histories_per_step": n_hist, "exposures": n_exposures,
+            "model": ["NONE", "LIVERMORE", "IA"][args.model], "tally": "fp64",
+            "l2": "flushed between steps (256 MB write); 1 GB tallies per step, 52 MB palette grid",
+            "parallelism": f"replicas{_dist()[0]}",
+            "voxel_layout": "palette-u8" if args.layout == 0 else "8-byte",
+            "regen_threshold": args.regen or "default", "interact_threshold": args.interact or "default",
+            "woodcock_burst": args.burst or "default", "tracking": args.tracking}
 
 
 def serving_measurement(ctx, n_jobs: int, rates, chains: int, seed: int = 20261205) -> dict:
@@ -418,7 +443,6 @@ def main():
     ap.add_argument("--model", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--regen", type=int, default=0, help="warp refill threshold (0 = library default)")
     ap.add_argument("--interact", type=int, default=0, help="interaction-pass threshold (0 = library default)")
     ap.add_argument("--layout", type=int, default=0, help="0 = compact palette when possible, 1 = 8-byte voxels")
@@ -444,28 +468,26 @@ def main():
     histories = int(args.histories)
 
     if args.impl == "reference":
+        # the reference's CPU transport (the oracle port, a C++ restatement of DXMClib's
+        # Transport<T>, in float as Transport<float>) on all host cores; no product code
         if rank != 0:
             return
-        from dxmclib_gb300 import LutBlob, build as b
-        b.build()
-        wl = build_workload(histories)
-        md = np.zeros(len(wl.world.materialMap()))
-        np.maximum.at(md, wl.world.materialIndexArray(), wl.world.densityArray().astype(np.float64))
-        info = LutBlob(wl.world.materialMap(), md, wl.source.maxPhotonEnergyProduced()).info()
+        cw = CpuWorkload(histories)
         threads = os.cpu_count() or 1
-        rates = []
-        sample = ""
+        secs = []
         for step in range(args.warmup + args.steps):
-            n, secs, sample = cpu_sample(wl, info, args.cpu_seconds / 2, threads, args.model)
+            t = cw.run(threads, args.model, "float", seed=100 + step)
             if step >= args.warmup:
-                rates.append(n / secs)
-        v = float(np.mean(rates))
+                secs.append(t)
+        v = cw.sample_histories * len(secs) / float(np.sum(secs))
+        n_hist = cw.hpe * cw.n_exposures
         line = {"metric": metric, "value": v, "unit": "histories/s", "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1e3 * histories / v, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": wl.name, "histories_per_step": histories, "model": "LIVERMORE"},
-                "impl": "reference",
-                "cpu_baseline": {"value": v, "unit": "histories/s", "cores": threads, "kind": "port", "sample": sample},
+                "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": bench_config(args, n_hist, cw.n_exposures),
+                "impl": "reference", "histories_per_sample_step": cw.sample_histories,
+                "cpu_baseline": {"value": v, "unit": "histories/s", "cores": threads, "kind": "port",
+                                 "precision": "float", "sample": cw.describe},
                 "e2e": {"value": v, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -612,22 +634,20 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
+        # the oracle port on the host cores, one fixed sample step per precision
         threads = os.cpu_count() or 1
-        n, secs, sample = cpu_sample(wl, blob.info(), args.cpu_seconds, threads, args.model)
-        cpu = {"value": n / secs, "unit": "histories/s", "cores": threads, "kind": "port", "sample": sample}
+        cw = CpuWorkload(histories)
+        t32 = cw.run(threads, args.model, "float")
+        t64 = cw.run(threads, args.model, "double")
+        cpu = {"value": cw.sample_histories / t32, "unit": "histories/s", "cores": threads, "kind": "port",
+               "precision": "float", "double_value": cw.sample_histories / t64, "sample": cw.describe}
 
     if rank == 0:
         line = {
             "metric": metric, "value": value, "unit": "histories/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": wl.name, "histories_per_step": n_hist, "exposures": len(exposures),
-                       "model": ["NONE", "LIVERMORE", "IA"][args.model], "tally": "fp64",
-                       "l2": "flushed between steps (256 MB write); 1 GB tallies per step, 52 MB palette grid",
-                       "parallelism": f"replicas{ws}",
-                       "voxel_layout": "palette-u8" if args.layout == 0 else "8-byte",
-                       "regen_threshold": args.regen or "default", "interact_threshold": args.interact or "default",
-                       "woodcock_burst": args.burst or "default", "tracking": args.tracking},
+            "config": bench_config(args, n_hist, len(exposures)),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind,
                          # DRAM bytes per launch from the committed ncu capture of a 1e7-history

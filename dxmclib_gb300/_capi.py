@@ -151,6 +151,7 @@ SIGNATURES = {
     "dxmc_udiv_invariant": (C.c_int, [C.POINTER(C.c_uint32), C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32)]),
     "dxmc_physics_material": (C.c_int, [C.c_char_p, D, C.POINTER(MaterialProvider)]),
     "dxmc_physics_material_free": (None, [C.POINTER(MaterialProvider)]),
+    "dxmc_physics_mass_energy_absorption": (C.c_int, [C.POINTER(MaterialProvider), D, DP]),
     "dxmc_physics_element_material": (C.c_int, [C.c_int, C.POINTER(MaterialProvider)]),
     "dxmc_lut_build": (C.c_int, [C.POINTER(MaterialProvider), C.c_int, FP, U8P, C.c_uint64, D, C.POINTER(VP)]),
     "dxmc_lut_build_max_density": (C.c_int, [C.POINTER(MaterialProvider), C.c_int, DP, D, C.POINTER(VP)]),

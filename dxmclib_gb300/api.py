@@ -107,6 +107,12 @@ class Material:
     def getRayleightAttenuation(self, e: float) -> float:
         return self._provider.rayleigh(self._provider.user, e)
 
+    def getMassEnergyAbsorbtion(self, e: float) -> float:
+        """Mass energy-absorption coefficient, cm2/g (material.hpp:74)."""
+        out = C.c_double(0.0)
+        A.check(A.load().dxmc_physics_mass_energy_absorption(C.byref(self._provider), float(e), C.byref(out)))
+        return out.value
+
     def getTotalAttenuation(self, e: float) -> float:
         return self.getPhotoelectricAttenuation(e) + self.getComptonAttenuation(e) + self.getRayleightAttenuation(e)
 
@@ -459,22 +465,8 @@ class PencilSource(Source):
 
 
 def _mass_energy_absorption(material: Material, energy: float) -> float:
-    # energy absorption from the physics model: photo + compton * transfer fraction
-    # (exposed through the attenuation callbacks; transfer fraction via KN)
-    k = energy / ELECTRON_REST_MASS
-    # Klein-Nishina energy-transfer fraction (Evans) as the Compton weighting
-    def kn_sigma(kk):
-        return ((1 + kk) / kk ** 2 * (2 * (1 + kk) / (1 + 2 * kk) - math.log(1 + 2 * kk) / kk)
-                + math.log(1 + 2 * kk) / (2 * kk) - (1 + 3 * kk) / (1 + 2 * kk) ** 2)
-    def kn_tr(kk):
-        a = 2 * (1 + kk) ** 2 / (kk ** 2 * (1 + 2 * kk))
-        b = (1 + 3 * kk) / (1 + 2 * kk) ** 2
-        c = (1 + kk) * (2 * kk ** 2 - 2 * kk - 1) / (kk ** 2 * (1 + 2 * kk) ** 2)
-        d = 4 * kk ** 2 / (3 * (1 + 2 * kk) ** 3)
-        e = ((1 + kk) / kk ** 3 - 1 / (2 * kk) + 1 / (2 * kk ** 3)) * math.log(1 + 2 * kk)
-        return a - b - c - d - e
-    frac = kn_tr(k) / kn_sigma(k)
-    return material.getPhotoelectricAttenuation(energy) + material.getComptonAttenuation(energy) * frac
+    """Material::getMassEnergyAbsorbtion (material.cpp:56-59) from the physics model."""
+    return material.getMassEnergyAbsorbtion(energy)
 
 
 class IsotropicSource(Source):

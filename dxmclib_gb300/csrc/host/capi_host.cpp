@@ -107,6 +107,15 @@ int dxmc_physics_element_material(int Z, dxmc_material_provider* out)
     return dxmc_physics_material(phys::element(Z).symbol.c_str(), -1, out);
 }
 
+int dxmc_physics_mass_energy_absorption(const dxmc_material_provider* provider, double energy, double* out)
+{
+    // only providers made by dxmc_physics_material carry a composition
+    if (!provider || !out || !provider->user || provider->photoelectric != cb_photo || !(energy > 0))
+        return DXMC_ERR_INVALID;
+    *out = phys::mass_energy_absorption(pm(provider->user)->composition, energy);
+    return DXMC_OK;
+}
+
 void dxmc_physics_material_free(dxmc_material_provider* provider)
 {
     if (provider && provider->user) {

@@ -112,6 +112,11 @@ typedef struct dxmc_material_provider {
  * until dxmc_physics_material_free. */
 int dxmc_physics_material(const char* name, double density, dxmc_material_provider* out);
 void dxmc_physics_material_free(dxmc_material_provider* provider);
+/* Mass energy-absorption coefficient (cm2/g) of a material made by
+ * dxmc_physics_material: Material::getMassEnergyAbsorbtion (material.cpp:56-59),
+ * which the DX dose-area-product calibration weighs the spectrum with
+ * (source.hpp:552-568). */
+int dxmc_physics_mass_energy_absorption(const dxmc_material_provider* provider, double energy_kev, double* out);
 int dxmc_physics_element_material(int atomic_number, dxmc_material_provider* out);
 
 /* ---- host LUT (AttenuationLut<T>::generate, attenuationlut.hpp:64-96) ---- */

@@ -12,6 +12,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle_port.so"
 SRC = HERE / "dxmc_port.cpp"
+CORE = HERE / "port_core.inc"
 
 DP = C.POINTER(C.c_double)
 
@@ -35,7 +36,7 @@ class PortSource(C.Structure):
 
 
 def build(force: bool = False) -> Path:
-    if force or not LIB.exists() or LIB.stat().st_mtime < SRC.stat().st_mtime:
+    if force or not LIB.exists() or LIB.stat().st_mtime < max(SRC.stat().st_mtime, CORE.stat().st_mtime):
         r = subprocess.run(["g++", "-std=c++20", "-O3", "-fPIC", "-shared", "-pthread", "-o", str(LIB), str(SRC)],
                            capture_output=True, text=True)
         if r.returncode != 0:
@@ -53,10 +54,10 @@ def lib():
         _lib = C.CDLL(str(LIB))
         _lib.oracle_port_set_direction.argtypes = [C.c_int]
         _lib.oracle_port_set_direction.restype = None
-        _lib.oracle_port_transport.restype = C.c_double
-        _lib.oracle_port_transport.argtypes = [C.POINTER(PortLut), C.POINTER(PortWorld), C.POINTER(PortSource), C.c_int,
-                                               C.c_int, C.c_uint64, DP, DP, C.POINTER(C.c_uint32),
-                                               C.POINTER(C.c_uint64)]
+        _lib.oracle_port_transport_ex.restype = C.c_double
+        _lib.oracle_port_transport_ex.argtypes = [C.POINTER(PortLut), C.POINTER(PortWorld), C.POINTER(PortSource),
+                                                  C.c_int, C.c_int, C.c_uint64, C.c_int, DP, DP, C.POINTER(C.c_uint32),
+                                                  C.POINTER(C.c_uint64)]
     return _lib
 
 
@@ -64,11 +65,23 @@ def _d(a):
     return a.ctypes.data_as(DP)
 
 
+def lut_from_fixture(g: dict, prefix: str = "lut_") -> dict:
+    """LUT tables in the form transport() takes, from a golden fixture that stores
+    the reference's own AttenuationLut<double> tables (tests/golden/make_golden.py):
+    the port then runs without the product library."""
+    meta = g[prefix + "meta"]
+    return dict(x=g[prefix + "x"], coef=g[prefix + "coef"], maxcoef=g[prefix + "maxcoef"], rita=g[prefix + "rita"],
+                spline=g[prefix + "spline"], shells=g[prefix + "shells"], n_energy=int(meta[0]),
+                linear_index=int(meta[1]), linear_step=float(meta[2]), linear_energy=float(meta[3]),
+                min_energy=float(meta[4]), max_energy=float(meta[5]))
+
+
 def transport(lut_info: dict, dims, spacing, density, material, exposures19, model: int = 1, n_threads: int = 0,
               seed: int = 1, spectrum=None, heel=None, bowtie=None, measurement=None, origin=(0, 0, 0),
-              normalized_direction: bool = False):
+              normalized_direction: bool = False, precision: str = "double"):
     """Runs the CPU restatement; returns (energy, energy^2, nEvents, seconds, steps) raw tallies.
-    normalized_direction selects the normalised physics mode (unit scattering axis)."""
+    normalized_direction selects the normalised physics mode (unit scattering axis);
+    precision "double" or "float" (Transport<double> / Transport<float>)."""
     keep = []
     L = PortLut()
     x = np.ascontiguousarray(lut_info["x"], np.float64)
@@ -125,8 +138,10 @@ def transport(lut_info: dict, dims, spacing, density, material, exposures19, mod
     nev = np.zeros(n, np.uint32)
     steps = C.c_uint64(0)
     lib().oracle_port_set_direction(1 if normalized_direction else 0)
-    secs = lib().oracle_port_transport(C.byref(L), C.byref(W), C.byref(S), int(model), int(n_threads), int(seed),
-                                       _d(e), _d(e2), nev.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(steps))
+    prec = {"double": 0, "float": 1}[precision]
+    secs = lib().oracle_port_transport_ex(C.byref(L), C.byref(W), C.byref(S), int(model), int(n_threads), int(seed),
+                                          prec, _d(e), _d(e2), nev.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                          C.byref(steps))
     return e, e2, nev, secs, steps.value
 
 

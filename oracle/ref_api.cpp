@@ -24,11 +24,13 @@
 #include "dxmc/transport.hpp"
 #include "dxmc/world.hpp"
 
+#include <chrono>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 using namespace dxmc;
@@ -158,14 +160,15 @@ std::vector<Material> make_materials(const RefWorldDesc& w)
     return mats;
 }
 
-bool make_world(const RefWorldDesc& d, World<double>& world)
+template <class T>
+bool make_world(const RefWorldDesc& d, World<T>& world)
 {
     world.setDimensions({ d.dims[0], d.dims[1], d.dims[2] });
-    world.setSpacing({ d.spacing[0], d.spacing[1], d.spacing[2] });
-    world.setOrigin({ d.origin[0], d.origin[1], d.origin[2] });
-    world.setDirectionCosines({ d.direction_cosines[0], d.direction_cosines[1], d.direction_cosines[2], d.direction_cosines[3], d.direction_cosines[4], d.direction_cosines[5] });
+    world.setSpacing({ static_cast<T>(d.spacing[0]), static_cast<T>(d.spacing[1]), static_cast<T>(d.spacing[2]) });
+    world.setOrigin({ static_cast<T>(d.origin[0]), static_cast<T>(d.origin[1]), static_cast<T>(d.origin[2]) });
+    world.setDirectionCosines({ static_cast<T>(d.direction_cosines[0]), static_cast<T>(d.direction_cosines[1]), static_cast<T>(d.direction_cosines[2]), static_cast<T>(d.direction_cosines[3]), static_cast<T>(d.direction_cosines[4]), static_cast<T>(d.direction_cosines[5]) });
     const std::size_t n = d.dims[0] * d.dims[1] * d.dims[2];
-    auto dens = std::make_shared<std::vector<double>>(d.density, d.density + n);
+    auto dens = std::make_shared<std::vector<T>>(d.density, d.density + n);
     auto mat = std::make_shared<std::vector<std::uint8_t>>(d.material, d.material + n);
     world.setDensityArray(dens);
     world.setMaterialIndexArray(mat);
@@ -177,7 +180,8 @@ bool make_world(const RefWorldDesc& d, World<double>& world)
     return world.isValid();
 }
 
-void setup_tube(Tube<double>& tube, const RefSourceDesc& s)
+template <class T>
+void setup_tube(Tube<T>& tube, const RefSourceDesc& s)
 {
     tube.setVoltage(s.kvp);
     if (s.anode_angle_deg > 0)
@@ -187,17 +191,20 @@ void setup_tube(Tube<double>& tube, const RefSourceDesc& s)
         tube.setCuFiltration(s.cu_mm);
 }
 
-std::unique_ptr<Source<double>> make_source(const RefSourceDesc& s)
+template <class T>
+std::unique_ptr<Source<T>> make_source(const RefSourceDesc& s)
 {
-    const std::array<double, 3> pos { s.position[0], s.position[1], s.position[2] };
-    const std::array<double, 6> cos { s.direction_cosines[0], s.direction_cosines[1], s.direction_cosines[2], s.direction_cosines[3], s.direction_cosines[4], s.direction_cosines[5] };
+    const std::array<T, 3> pos { static_cast<T>(s.position[0]), static_cast<T>(s.position[1]), static_cast<T>(s.position[2]) };
+    std::array<T, 6> cos {};
+    for (int k = 0; k < 6; ++k)
+        cos[k] = static_cast<T>(s.direction_cosines[k]);
     // BowTieFilter's constructors (beamfilters.hpp:86-122) call normalizeData,
     // whose std::reduce (beamfilters.hpp:90) does not compile against GCC 13's
     // libstdc++; bow-tie weighting is therefore not exercised through the
     // reference and the bowtie_* fields are ignored here.
     switch (s.type) {
     case REF_PENCIL: {
-        auto p = std::make_unique<PencilSource<double>>();
+        auto p = std::make_unique<PencilSource<T>>();
         p->setPosition(pos);
         p->setDirectionCosines(cos);
         p->setPhotonEnergy(s.energy);
@@ -207,23 +214,23 @@ std::unique_ptr<Source<double>> make_source(const RefSourceDesc& s)
     }
     case REF_ISOTROPIC:
     case REF_ISOTROPIC_CT: {
-        std::unique_ptr<IsotropicSource<double>> p;
+        std::unique_ptr<IsotropicSource<T>> p;
         if (s.type == REF_ISOTROPIC)
-            p = std::make_unique<IsotropicSource<double>>();
+            p = std::make_unique<IsotropicSource<T>>();
         else
-            p = std::make_unique<IsotropicCTSource<double>>();
+            p = std::make_unique<IsotropicCTSource<T>>();
         p->setPosition(pos);
         p->setDirectionCosines(cos);
         p->setCollimationAngles(s.collimation[0], s.collimation[1], s.collimation[2], s.collimation[3]);
-        std::vector<double> e(s.spec_energies, s.spec_energies + s.spec_n);
-        std::vector<double> w(s.spec_weights, s.spec_weights + s.spec_n);
+        std::vector<T> e(s.spec_energies, s.spec_energies + s.spec_n);
+        std::vector<T> w(s.spec_weights, s.spec_weights + s.spec_n);
         p->setSpecter(w, e);
         p->setHistoriesPerExposure(s.histories_per_exposure);
         p->setTotalExposures(s.total_exposures);
         return p;
     }
     case REF_DX: {
-        auto p = std::make_unique<DXSource<double>>();
+        auto p = std::make_unique<DXSource<T>>();
         setup_tube(p->tube(), s);
         p->setPosition(pos);
         p->setSourceDetectorDistance(s.sdd);
@@ -236,7 +243,7 @@ std::unique_ptr<Source<double>> make_source(const RefSourceDesc& s)
         return p;
     }
     case REF_CBCT: {
-        auto p = std::make_unique<CBCTSource<double>>();
+        auto p = std::make_unique<CBCTSource<T>>();
         setup_tube(p->tube(), s);
         p->setPosition(pos);
         p->setSourceDetectorDistance(s.sdd);
@@ -254,10 +261,10 @@ std::unique_ptr<Source<double>> make_source(const RefSourceDesc& s)
         // phantom axis, centres it and scans one collimation (source.hpp:937-942)
         RefSourceDesc sp = s;
         sp.type = REF_CTSPIRAL;
-        auto spiral = make_source(sp);
-        auto p = std::make_unique<CTAxialSource<double>>(*dynamic_cast<CTSpiralSource<double>*>(spiral.get()));
-        p->setDirectionCosines(std::array<double, 6> { -1, 0, 0, 0, 0, 1 });
-        p->setPosition(std::array<double, 3> { 0, 0, 0 });
+        auto spiral = make_source<T>(sp);
+        auto p = std::make_unique<CTAxialSource<T>>(*dynamic_cast<CTSpiralSource<T>*>(spiral.get()));
+        p->setDirectionCosines(std::array<T, 6> { -1, 0, 0, 0, 0, 1 });
+        p->setPosition(std::array<T, 3> { 0, 0, 0 });
         p->setScanLenght(p->collimation());
         p->setUseXCareFilter(false);
         p->setHistoriesPerExposure(s.histories_per_exposure);
@@ -265,13 +272,13 @@ std::unique_ptr<Source<double>> make_source(const RefSourceDesc& s)
     }
     case REF_CTSPIRAL:
     case REF_CTAXIAL: {
-        std::unique_ptr<CTSource<double>> p;
+        std::unique_ptr<CTSource<T>> p;
         if (s.type == REF_CTSPIRAL) {
-            auto sp = std::make_unique<CTSpiralSource<double>>();
+            auto sp = std::make_unique<CTSpiralSource<T>>();
             sp->setPitch(s.pitch);
             p = std::move(sp);
         } else {
-            p = std::make_unique<CTAxialSource<double>>();
+            p = std::make_unique<CTAxialSource<T>>();
         }
         setup_tube(p->tube(), s);
         p->setPosition(pos);
@@ -394,7 +401,7 @@ int ref_source_tables(const RefSourceDesc* sd, const RefWorldDesc* wd,
     World<double> world;
     if (!make_world(*wd, world))
         return -1;
-    auto src = make_source(*sd);
+    auto src = make_source<double>(*sd);
     if (!src)
         return -2;
     src->updateFromWorld(world);
@@ -504,7 +511,7 @@ int ref_transport(const RefWorldDesc* wd, const RefSourceDesc* sd, int model, in
     World<double> world;
     if (!make_world(*wd, world))
         return -1;
-    auto src = make_source(*sd);
+    auto src = make_source<double>(*sd);
     if (!src)
         return -2;
     Transport<double> transport;
@@ -521,6 +528,74 @@ int ref_transport(const RefWorldDesc* wd, const RefSourceDesc* sd, int model, in
     meta[0] = static_cast<double>(res.numberOfHistories);
     meta[1] = res.simulationTime.count();
     return res.numberOfHistories > 0 ? 0 : -3;
+}
+
+} // extern "C"
+
+namespace {
+template <class T>
+int transport_any(const RefWorldDesc* wd, const RefSourceDesc* sd, int model, int n_threads, int output_mode,
+    int use_calibration, double* dose, double* variance, std::uint32_t* n_events, double* meta)
+{
+    World<T> world;
+    if (!make_world(*wd, world))
+        return -1;
+    auto src = make_source<T>(*sd);
+    if (!src)
+        return -2;
+    Transport<T> transport;
+    transport.setNumberOfWorkers(n_threads > 0 ? n_threads : std::thread::hardware_concurrency());
+    transport.setLowEnergyCorrectionModel(static_cast<LOWENERGYCORRECTION>(model));
+    transport.setOutputMode(output_mode == 1 ? Transport<T>::OUTPUTMODE::DOSE : Transport<T>::OUTPUTMODE::EV_PER_HISTORY);
+    auto res = transport(world, src.get(), nullptr, use_calibration != 0);
+    const std::size_t n = world.size();
+    for (std::size_t i = 0; i < n; ++i) {
+        dose[i] = res.dose[i];
+        variance[i] = res.variance[i];
+        n_events[i] = res.nEvents[i];
+    }
+    meta[0] = static_cast<double>(res.numberOfHistories);
+    meta[1] = std::chrono::duration<double>(res.simulationTime).count();
+    meta[2] = 0.0;
+    meta[3] = res.dose_units == "mGy" ? 2 : (res.dose_units == "keV/kg" ? 1 : 0);
+    return res.numberOfHistories > 0 ? 0 : -3;
+}
+} // namespace
+
+extern "C" {
+
+// Transport<T>::operator() (transport.hpp:135-202) in T = double (precision 0) or
+// float (precision 1) on World<T>, in EV_PER_HISTORY (output_mode 0) or DOSE
+// (output_mode 1) mode; with use_calibration the source's calibration factor
+// converts keV/kg to mGy (transport.hpp:187-195).  meta: [histories, seconds of
+// Result::simulationTime (the timed transport, transport.hpp:166-174), 0,
+// units (0 eV/history, 1 keV/kg, 2 mGy)].
+int ref_transport_ex(const RefWorldDesc* wd, const RefSourceDesc* sd, int model, int n_threads, int output_mode,
+    int use_calibration, int precision, double* dose, double* variance, std::uint32_t* n_events, double* meta)
+{
+    if (precision == 1)
+        return transport_any<float>(wd, sd, model, n_threads, output_mode, use_calibration, dose, variance, n_events, meta);
+    return transport_any<double>(wd, sd, model, n_threads, output_mode, use_calibration, dose, variance, n_events, meta);
+}
+
+// Source<double>::getCalibrationValue (source.hpp:196) after updateFromWorld and
+// validate, as Transport::operator() calls it in DOSE mode (transport.hpp:146-190):
+// the factor that turns keV/kg into mGy.  Deterministic for DX (dose-area
+// product, source.hpp:552-568); a Monte Carlo estimate for CT sources.
+int ref_calibration_value(const RefWorldDesc* wd, const RefSourceDesc* sd, int model, double* value)
+{
+    World<double> world;
+    if (!make_world(*wd, world))
+        return -1;
+    auto src = make_source<double>(*sd);
+    if (!src)
+        return -2;
+    src->updateFromWorld(world);
+    src->validate();
+    if (!src->isValid())
+        return -3;
+    *value = src->getCalibrationValue(static_cast<LOWENERGYCORRECTION>(model), nullptr);
+    return 0;
 }
 
 // CTDIPhantom<double> (world.hpp:229-390): arrays and the five hole index lists
@@ -568,7 +643,7 @@ int ref_ct_calibration(const RefSourceDesc* sd, int model, int n_threads, double
 {
     if (sd->type != REF_CTSPIRAL)
         return -1;
-    auto base = make_source(*sd);
+    auto base = make_source<double>(*sd);
     auto* spiral = dynamic_cast<CTSpiralSource<double>*>(base.get());
     if (!spiral)
         return -2;

@@ -16,9 +16,21 @@ tests/golden/ref_binding.py and stores, as small .npz files:
 * interactions_*.npz histograms of the reference interaction samplers;
 * ctdi_phantom.npz  CTDIPhantom arrays and hole lists (world.hpp:229-390);
 * ct_calibration_m1.npz the reference's CT calibration factor and the tables of
-                    the axial copy it runs (source.hpp:925-988).
+                    the axial copy it runs (source.hpp:925-988);
+* bench_ct_helical.npz Transport<double> on the 512 x 512 x 200 CT helical
+                    workload (the benchmark's headline configuration), as block
+                    sums of 8 x 8 x 4 voxels, with the reference's exposure,
+                    spectrum and heel tables, its LUT tables for the phantom and
+                    the statistics of a second, independent reference run
+                    against the first (the per-event variance estimator's
+                    over-dispersion at this block size);
+* bench_dx.npz      the same for a DXSource beam on a 128^3 phantom of the
+                    batched-radiography configuration (4 x 4 x 4 blocks);
+* transport_dose_dx.npz Transport<double> in DOSE mode (mGy through the DX
+                    dose-area-product calibration, and keV/kg without it) on a
+                    64^3 DX phantom, 2 x 2 x 2 block sums, with the factor.
 
-Usage:  make -C oracle && python tests/golden/make_golden.py [--quick]
+Usage:  make -C oracle REF=<reference checkout> && python tests/golden/make_golden.py [--quick]
 The generator needs the reference checkout and is not run by the test suite.
 """
 from __future__ import annotations
@@ -191,6 +203,134 @@ def gen_ct(out: Path, quick: bool):
                         **sparse_tally(dose, var, nev, dims))
 
 
+def block_tally(dose, var, nev, dims, block, frac=0.002):
+    """Block sums (dose, variance, events) of a tally, kept for blocks above frac of
+    the largest block (dims x-fastest as the world, block in voxels per axis)."""
+    nx, ny, nz = dims
+    bx, by, bz = block
+
+    def bs(a):
+        return a.reshape(nz // bz, bz, ny // by, by, nx // bx, bx).sum(axis=(1, 3, 5)).ravel()
+
+    d, v, n = bs(dose), bs(var), bs(nev.astype(np.float64))
+    keep = np.nonzero(d > frac * d.max())[0].astype(np.uint32)
+    return dict(idx=keep, dose=d[keep], var=v[keep], nev=n[keep], total=np.array([dose.sum()]),
+                total_events=np.array([nev.sum()], np.float64)), (d, v)
+
+
+def same_method_stats(a, b):
+    """parity.compare_sparse of two independent reference runs (block sums)."""
+    sys.path.insert(0, str(HERE.parent))
+    from parity import compare_sparse
+    ref = dict(idx=np.arange(len(a[0])), dose=a[0], var=a[1], total=np.array([a[0].sum()]))
+    st = compare_sparse(ref, b[0], b[1])
+    return np.array([st["chi2"], st["n_voxels"], st["beyond_3sigma"], st["max_abs_z"], st["total_ratio"],
+                     st["mean_bias"]])
+
+
+def gen_bench_ct(out: Path, quick: bool):
+    """The headline CT helical workload (512 x 512 x 200, 0.8 x 0.8 x 2.5 mm, seeded body
+    phantom; 120 kVp, 2.5 mm Al, 40 mm collimation, pitch 1, 1 degree steps, heel) run
+    twice by the reference at 2e7 histories each."""
+    sys.path.insert(0, str(HERE.parents[1]))
+    from dxmclib_gb300.workloads import CT_MATERIALS, ct_phantom_arrays
+    dims, spacing, block = (512, 512, 200), (0.8, 0.8, 2.5), (8, 8, 4)
+    mat, dens = ct_phantom_arrays()
+    names = [n for n, _ in CT_MATERIALS]
+    w = R.WorldArgs(dims, spacing, dens.astype(np.float64), mat, names,
+                    material_densities=[d for _, d in CT_MATERIALS])
+    hist = int(2e6 if quick else 2e7)
+    length = dims[2] * spacing[2]
+    s = R.SourceArgs(R.CTSPIRAL, position=(0, 0, -length / 2), kvp=120, al_mm=2.5, ct_collimation=40, pitch=1.0,
+                     scan_length=length, angle_step_deg=1.0, start_angle_deg=0, fov=500, sdd=1190, heel=1,
+                     histories_per_exposure=1)
+    n_exp = len(R.source_tables(s, w)["exposures"])
+    s.desc.histories_per_exposure = -(-hist // n_exp)
+    tabs = R.source_tables(s, w)
+    md = np.zeros(len(names))
+    np.maximum.at(md, mat.astype(np.int64), dens.astype(np.float64))
+    lut = R.lut_dump(R.WorldArgs((4, 1, 1), (1, 1, 1), md, np.arange(4, dtype=np.uint8), names), tabs["max_energy"],
+                     np.array([10.0]), np.array([1.0]))
+    runs = []
+    for k in range(2):
+        dose, var, nev, N, st, _ = R.transport_ex(w, s, model=1)
+        print(f"bench ct run {k}: {N} histories {st:.2f} s ({N / st:.3g} hist/s)", flush=True)
+        runs.append((block_tally(dose, var, nev, dims, block), N, st))
+        del dose, var, nev
+    (tally, full_a), N, st = runs[0]
+    stats = same_method_stats(full_a, runs[1][0][1])
+    print(f"bench ct: reference vs reference chi2/n {stats[0]:.3f} over {int(stats[1])} blocks", flush=True)
+    np.savez_compressed(out / "bench_ct_helical.npz", dims=np.array(dims), spacing=np.array(spacing),
+                        block=np.array(block), phantom_seed=20261203, names=np.array(names),
+                        material_densities=np.array([d for _, d in CT_MATERIALS]), histories=N, seconds=st,
+                        exposures=tabs["exposures"], spec_energies=tabs["spec_energies"],
+                        spec_weights=tabs["spec_weights"], heel_meta=tabs["heel_meta"],
+                        heel_weights=tabs.get("heel_weights", np.zeros(0)), max_energy=tabs["max_energy"],
+                        max_density=md, lut_x=lut["x"], lut_coef=lut["coef"], lut_maxcoef=lut["maxcoef"],
+                        lut_rita=lut["rita"], lut_spline=lut["spline"], lut_shells=lut["shells"], lut_meta=lut["meta"],
+                        same_method=stats, **tally)
+
+
+def gen_bench_dx(out: Path, quick: bool):
+    """A DXSource beam (80 kVp, 3 mm Al, 200 mm field at SDD 1000 mm, angled, heel) on a
+    128^3 phantom of the batched-radiography configuration, two reference runs."""
+    sys.path.insert(0, str(HERE.parents[1]))
+    from dxmclib_gb300.workloads import DX_MATERIALS, dx_phantom_arrays
+    n = 128
+    dims, spacing, block = (n, n, n), (2.0, 2.0, 2.0), (4, 4, 4)
+    mat, dens = dx_phantom_arrays(n, np.random.default_rng(20261204))
+    w = R.WorldArgs(dims, spacing, dens.astype(np.float64), mat, DX_MATERIALS)
+    hist = int(1e6 if quick else 1e7)
+    s = R.SourceArgs(R.DX, position=(0, 0, 0), cosines=(-1, 0, 0, 0, 0, 1), kvp=80, al_mm=3.0, field_size=(200, 200),
+                     sdd=1000, source_angles_deg=(15, -10), tube_rotation_deg=0, heel=1,
+                     histories_per_exposure=hist // 8, total_exposures=8)
+    tabs = R.source_tables(s, w)
+    runs = []
+    for k in range(2):
+        dose, var, nev, N, st, _ = R.transport_ex(w, s, model=1)
+        print(f"bench dx run {k}: {N} histories {st:.2f} s", flush=True)
+        runs.append((block_tally(dose, var, nev, dims, block), N, st))
+    (tally, full_a), N, st = runs[0]
+    stats = same_method_stats(full_a, runs[1][0][1])
+    print(f"bench dx: reference vs reference chi2/n {stats[0]:.3f} over {int(stats[1])} blocks", flush=True)
+    np.savez_compressed(out / "bench_dx.npz", dims=np.array(dims), spacing=np.array(spacing), block=np.array(block),
+                        phantom_seed=20261204, material=mat, density=dens.astype(np.float32),
+                        names=np.array(DX_MATERIALS), histories=N, seconds=st, exposures=tabs["exposures"],
+                        spec_energies=tabs["spec_energies"], spec_weights=tabs["spec_weights"],
+                        heel_meta=tabs["heel_meta"], heel_weights=tabs.get("heel_weights", np.zeros(0)),
+                        max_energy=tabs["max_energy"], same_method=stats, **tally)
+
+
+def gen_dose(out: Path, quick: bool):
+    """DOSE output mode (transport.hpp:186-195, 796-816): a DX beam on a 64^3 phantom,
+    once with the source's dose-area-product calibration (mGy) and once without (keV/kg)."""
+    sys.path.insert(0, str(HERE.parents[1]))
+    from dxmclib_gb300.workloads import DX_MATERIALS, dx_phantom_arrays
+    n = 64
+    dims, spacing, block = (n, n, n), (4.0, 4.0, 4.0), (2, 2, 2)
+    mat, dens = dx_phantom_arrays(n, np.random.default_rng(7))
+    w = R.WorldArgs(dims, spacing, dens.astype(np.float64), mat, DX_MATERIALS)
+    hist = int(4e5 if quick else 4e6)
+    s = R.SourceArgs(R.DX, position=(0, 0, 0), cosines=(-1, 0, 0, 0, 0, 1), kvp=70, al_mm=3.0, field_size=(150, 150),
+                     sdd=1000, source_angles_deg=(0, 0), tube_rotation_deg=0, heel=1,
+                     histories_per_exposure=hist // 8, total_exposures=8)
+    tabs = R.source_tables(s, w)
+    cal = R.calibration_value(w, s, model=1)
+    res = {}
+    for label, use_cal in (("mgy", True), ("kevkg", False)):
+        dose, var, nev, N, st, units = R.transport_ex(w, s, model=1, output_mode=1, use_calibration=use_cal)
+        assert units == (2 if use_cal else 1), units
+        t, _ = block_tally(dose, var, nev, dims, block)
+        res.update({f"{label}_{k}": v for k, v in t.items()})
+        print(f"dose {label}: {N} histories, total {dose.sum():.6g}", flush=True)
+    np.savez_compressed(out / "transport_dose_dx.npz", dims=np.array(dims), spacing=np.array(spacing),
+                        block=np.array(block), material=mat, density=dens.astype(np.float32),
+                        names=np.array(DX_MATERIALS), histories=N, calibration=cal, exposures=tabs["exposures"],
+                        spec_energies=tabs["spec_energies"], spec_weights=tabs["spec_weights"],
+                        heel_meta=tabs["heel_meta"], heel_weights=tabs.get("heel_weights", np.zeros(0)),
+                        max_energy=tabs["max_energy"], **res)
+
+
 def gen_interactions(out: Path, quick: bool):
     n = 8
     w = R.WorldArgs((n, n, n), (1, 1, 1), np.ones(n ** 3) * 1.92, np.zeros(n ** 3, np.uint8),
@@ -252,11 +392,13 @@ def main():
     ap.add_argument("--only", default="")
     a = ap.parse_args()
     if not R.available():
-        raise SystemExit("oracle/_ref/libdxmc_ref.so missing: run `make -C oracle` where the reference checkout exists")
+        raise SystemExit("oracle/_ref/libdxmc_ref.so missing: run `make -C oracle REF=<reference checkout>` first")
     out = HERE
     steps = dict(lut=lambda: gen_lut(out), alias=lambda: gen_alias(out), sources=lambda: gen_sources(out),
                  transport=lambda: gen_transport(out, a.quick), ct=lambda: gen_ct(out, a.quick),
-                 interactions=lambda: gen_interactions(out, a.quick), ctdi=lambda: gen_ctdi(out, a.quick))
+                 interactions=lambda: gen_interactions(out, a.quick), ctdi=lambda: gen_ctdi(out, a.quick),
+                 bench_ct=lambda: gen_bench_ct(out, a.quick), bench_dx=lambda: gen_bench_dx(out, a.quick),
+                 dose=lambda: gen_dose(out, a.quick))
     for name, fn in steps.items():
         if a.only and name not in a.only.split(","):
             continue

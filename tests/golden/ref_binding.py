@@ -274,3 +274,32 @@ def ct_calibration(source: "SourceArgs", model: int, ctdivol: float, diameter: i
     if rc != 0:
         raise RuntimeError(f"ref_ct_calibration failed: {rc}")
     return factor.value, meta
+
+
+def transport_ex(world: WorldArgs, source: SourceArgs, model: int = 1, n_threads: int = 0, output_mode: int = 0,
+                 use_calibration: bool = False, precision: int = 0):
+    """Transport<T>::operator() in T = double (precision 0) or float (1), in
+    EV_PER_HISTORY (output_mode 0) or DOSE (1) mode.  Returns (dose, variance,
+    nEvents, histories, simulation seconds, units) with units 0 eV/history,
+    1 keV/kg, 2 mGy."""
+    n = world.size
+    dose = np.zeros(n, np.float64)
+    var = np.zeros(n, np.float64)
+    nev = np.zeros(n, np.uint32)
+    meta = np.zeros(4, np.float64)
+    rc = lib().ref_transport_ex(C.byref(world.desc), C.byref(source.desc), C.c_int(model), C.c_int(n_threads),
+                                C.c_int(output_mode), C.c_int(1 if use_calibration else 0), C.c_int(precision),
+                                _dptr(dose), _dptr(var), nev.ctypes.data_as(C.POINTER(C.c_uint32)), _dptr(meta))
+    if rc != 0:
+        raise RuntimeError(f"ref_transport_ex failed: {rc}")
+    return dose, var, nev, int(meta[0]), float(meta[1]), int(meta[3])
+
+
+def calibration_value(world: WorldArgs, source: SourceArgs, model: int = 1) -> float:
+    """Source::getCalibrationValue after updateFromWorld / validate (the factor DOSE
+    mode multiplies keV/kg by to give mGy)."""
+    v = C.c_double(0)
+    rc = lib().ref_calibration_value(C.byref(world.desc), C.byref(source.desc), C.c_int(model), C.byref(v))
+    if rc != 0:
+        raise RuntimeError(f"ref_calibration_value failed: {rc}")
+    return v.value

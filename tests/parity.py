@@ -63,6 +63,7 @@ def assert_parity(stats: dict, label: str = "", correlated: bool = False, max_ch
     3-sigma exceedances is allowed.  max_chi2 replaces the chi2/dof bound where a
     same-method comparison measured the overdispersion of the pair."""
     msg = f"{label}: {stats}"
+    report(stats, label)
     assert stats["n_voxels"] > 10, msg
     n = stats["n_voxels"]
     p_beyond = P_BEYOND_3SIGMA * (2.0 if correlated else 1.0)
@@ -73,3 +74,19 @@ def assert_parity(stats: dict, label: str = "", correlated: bool = False, max_ch
     assert stats["chi2"] <= max_chi2 + 4.0 * np.sqrt(2.0 / n), msg
     assert abs(stats["total_ratio"] - 1.0) <= TOTAL_ENERGY_RTOL, msg
     assert abs(stats["mean_bias"]) <= MEAN_BIAS_RTOL, msg
+
+
+def block_sums(values: np.ndarray, dims, block) -> np.ndarray:
+    """Sums of a voxel array (x fastest, dims = (nx, ny, nz)) over blocks of
+    block = (bx, by, bz) voxels, in the block grid's x-fastest order."""
+    nx, ny, nz = (int(d) for d in dims)
+    bx, by, bz = (int(b) for b in block)
+    a = np.asarray(values, np.float64).reshape(nz // bz, bz, ny // by, by, nx // bx, bx)
+    return a.sum(axis=(1, 3, 5)).ravel()
+
+
+def report(stats: dict, label: str) -> None:
+    """One line per parity case with chi2/dof, printed into the test output."""
+    print(f"[parity] {label}: chi2/n {stats['chi2']:.3f} over {stats['n_voxels']} voxels, "
+          f"{stats['beyond_3sigma']} beyond 3 sigma, max |z| {stats['max_abs_z']:.2f}, "
+          f"total ratio {stats['total_ratio']:.5f}, mean bias {stats['mean_bias']:+.5f}")

@@ -61,3 +61,46 @@ def test_calibration_exposures_match_reference(golden):
     assert ours.shape == ref.shape
     np.testing.assert_allclose(ours[:, :17], ref[:, :17], atol=1e-9)
     assert np.array_equal(ours[:, 17], ref[:, 17])
+
+
+class _SpectrumTube:
+    """Stands in for a Tube with a given (energy, normalised weight) table."""
+
+    def __init__(self, energies, weights):
+        self.e, self.w = np.asarray(energies, np.float64), np.asarray(weights, np.float64)
+
+    def getEnergy(self):
+        return list(self.e)
+
+    def getSpecter(self, energies=None, normalize=True):
+        return list(self.w)
+
+    def voltage(self):
+        return float(self.e.max())
+
+
+def test_dx_dap_calibration_matches_reference(golden):
+    """DXSource::getCalibrationValue (source.hpp:552-568) on the reference's own spectrum:
+    DAP / (N * sum_E E w(E) mu_en,air(E)), with mu_en from the physics model as the
+    reference's Material::getMassEnergyAbsorbtion (material.cpp:56-59) gives it."""
+    import dxmclib_gb300 as dx
+    g = golden("transport_dose_dx.npz")
+    src = dx.DXSource()
+    src._tube = _SpectrumTube(g["spec_energies"], g["spec_weights"])
+    src.setTotalExposures(8)
+    src.setHistoriesPerExposure(int(g["histories"]) // 8)
+    assert abs(src.getCalibrationValue(1) / float(g["calibration"]) - 1.0) < 1e-12
+
+
+def test_ct_benchmark_exposures_match_reference(golden):
+    """The exposure table of the benchmark's CT helical workload (workloads.ct_source)
+    is the reference's CTSpiralSource table for the same settings."""
+    from dxmclib_gb300.workloads import ct_source, ct_world
+    g = golden("bench_ct_helical.npz")
+    world = ct_world(int(g["dims"][2]), seed=int(g["phantom_seed"]))
+    src = ct_source(world, int(g["histories"]))
+    ours = src.exposures(world.directionCosines()).as_matrix()
+    ref = g["exposures"]
+    assert ours.shape == ref.shape
+    np.testing.assert_allclose(ours[:, :17], ref[:, :17], atol=1e-9)
+    assert np.array_equal(ours[:, 17], ref[:, 17])

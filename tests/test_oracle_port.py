@@ -138,3 +138,28 @@ def test_port_normalized_direction_mode():
                                        spectrum=(sp.energies, sp.weights), normalized_direction=norm)
         tot[norm] = e.sum() / 1e6
     assert 0.003 < tot[False] / tot[True] - 1.0 < 0.015, tot
+
+
+@pytest.mark.parametrize("precision", ["double", "float"])
+def test_port_ct_benchmark_configuration_matches_reference(golden, precision):
+    """The port on the headline CT helical workload (512 x 512 x 200, the reference's
+    own exposure, spectrum, heel and LUT tables from the fixture; no product code),
+    in both precisions, against Transport<double> as 8 x 8 x 4 block sums.  This is
+    the configuration and the code path bench.py's CPU legs time."""
+    from parity import block_sums
+    from dxmclib_gb300.workloads import ct_phantom_arrays
+    g = golden("bench_ct_helical.npz")
+    dims, block = tuple(int(x) for x in g["dims"]), tuple(int(x) for x in g["block"])
+    mat, dens = ct_phantom_arrays(*dims, spacing=tuple(g["spacing"]), seed=int(g["phantom_seed"]))
+    hm = g["heel_meta"]
+    heel = dict(energy_start=hm[1], energy_step=hm[2], energy_size=hm[3], angle_start=hm[4], angle_step=hm[5],
+                angle_size=hm[6], weights=g["heel_weights"])
+    ex = g["exposures"].copy()
+    ex[:, 17] = ex[:, 17] // 2
+    n = int(ex[:, 17].sum())
+    e, e2, nev, secs, steps = port.transport(port.lut_from_fixture(g), dims, tuple(g["spacing"]), dens, mat, ex,
+                                             model=1, seed=5, spectrum=(g["spec_energies"], g["spec_weights"]),
+                                             heel=heel, precision=precision)
+    d, v = port.ev_per_history(e, e2, n)
+    s = compare_sparse(g, block_sums(d, dims, block), block_sums(v, dims, block))
+    assert_parity(s, f"port {precision} ct helical 512x512x200", max_chi2=max(1.2, float(g["same_method"][0])))
