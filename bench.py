@@ -442,6 +442,8 @@ def main():
     ap.add_argument("--histories", type=float, default=1e8)
     ap.add_argument("--model", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-precision", choices=("float", "both"), default="float",
+                    help="reference arm: time the port in float only, or in float and then double")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--regen", type=int, default=0, help="warp refill threshold (0 = library default)")
     ap.add_argument("--interact", type=int, default=0, help="interaction-pass threshold (0 = library default)")
@@ -474,11 +476,16 @@ def main():
             return
         cw = CpuWorkload(histories)
         threads = os.cpu_count() or 1
-        secs = []
+        secs, secs64 = [], []
         for step in range(args.warmup + args.steps):
             t = cw.run(threads, args.model, "float", seed=100 + step)
             if step >= args.warmup:
                 secs.append(t)
+        if args.cpu_precision == "both":  # Transport<double> beside the fair float baseline
+            for step in range(args.warmup + args.steps):
+                t = cw.run(threads, args.model, "double", seed=200 + step)
+                if step >= args.warmup:
+                    secs64.append(t)
         v = cw.sample_histories * len(secs) / float(np.sum(secs))
         n_hist = cw.hpe * cw.n_exposures
         line = {"metric": metric, "value": v, "unit": "histories/s", "n_gpus": ws, "steps": args.steps,
@@ -487,10 +494,23 @@ def main():
                 "config": bench_config(args, n_hist, cw.n_exposures),
                 "impl": "reference", "histories_per_sample_step": cw.sample_histories,
                 "cpu_baseline": {"value": v, "unit": "histories/s", "cores": threads, "kind": "port",
-                                 "precision": "float", "sample": cw.describe},
+                                 "precision": "float", "sample": cw.describe,
+                                 "double_value": (cw.sample_histories * len(secs64) / float(np.sum(secs64))
+                                                  if secs64 else None)},
                 "e2e": {"value": v, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        # the CPU baseline runs first, in a fresh process of the reference arm's own code
+        # (no CUDA context, no threads of this process competing for the host cores):
+        # one warm-up and one timed fixed-sample step in float, then the same in double
+        r = subprocess.run([sys.executable, str(REPO / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup",
+                            "1", "--cpu-precision", "both", "--model", str(args.model),
+                            "--histories", str(args.histories)], capture_output=True, text=True)
+        lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+        cpu = json.loads(lines[-1])["cpu_baseline"] if r.returncode == 0 and lines else {"error": r.stderr[-500:]}
 
     import torch
     import dxmclib_gb300 as dx
@@ -632,15 +652,6 @@ def main():
         serving = serving_measurement(ctx, args.serve_jobs, [float(r) for r in args.serve_rates.split(",")],
                                       args.serve_chains)
 
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        # the oracle port on the host cores, one fixed sample step per precision
-        threads = os.cpu_count() or 1
-        cw = CpuWorkload(histories)
-        t32 = cw.run(threads, args.model, "float")
-        t64 = cw.run(threads, args.model, "double")
-        cpu = {"value": cw.sample_histories / t32, "unit": "histories/s", "cores": threads, "kind": "port",
-               "precision": "float", "double_value": cw.sample_histories / t64, "sample": cw.describe}
 
     if rank == 0:
         line = {

@@ -126,9 +126,9 @@ struct dxmc_lut {
 struct dxmc_job {
     dxmc_gpu_ctx* ctx = nullptr;
     dxmc_world* world = nullptr;
-    double* tally = nullptr;
-    float* tally_f32 = nullptr;
-    uint32_t* n_events = nullptr;
+    dev::TallyRecord* records = nullptr; // FP64 tallies (modes 0 and 2): one 32-byte record per voxel
+    float* tally_f32 = nullptr;          // FP32 tally mode: interleaved (energy, energy^2) ...
+    uint32_t* n_events = nullptr;        // ... with the event counts beside it
     dev::JobCounters* counters = nullptr;
     unsigned char* tables = nullptr;
     unsigned char* queue = nullptr; // pre-generated photons (SoA)
@@ -1044,8 +1044,8 @@ namespace {
 void free_job_device(dxmc_job* j)
 {
     cudaStream_t s = j->ctx->stream;
-    if (j->tally)
-        cudaFreeAsync(j->tally, s);
+    if (j->records)
+        cudaFreeAsync(j->records, s);
     if (j->tally_f32)
         cudaFreeAsync(j->tally_f32, s);
     if (j->n_events)
@@ -1057,7 +1057,7 @@ void free_job_device(dxmc_job* j)
     if (j->queue)
         cudaFreeAsync(j->queue, s);
     j->queue = nullptr;
-    j->tally = nullptr;
+    j->records = nullptr;
     j->tally_f32 = nullptr;
     j->n_events = nullptr;
     j->counters = nullptr;
@@ -1459,7 +1459,8 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     std::memcpy(tables.data() + off_btw, bt_w.data(), bt_w.size() * 4);
 
     const uint64_t nv = world->params.n_voxels;
-    const uint64_t tally_bytes = tally_mode == 1 ? nv * 2 * sizeof(float) : nv * 2 * sizeof(double);
+    const uint64_t tally_bytes = tally_mode == 1 ? nv * 2 * sizeof(float) : nv * sizeof(dev::TallyRecord);
+    const uint64_t count_bytes = tally_mode == 1 ? nv * sizeof(uint32_t) : 0; // records hold their counts
     // photon queue: chunks of 2^k histories, 48 bytes per queued photon
     const int log2_option = jd->queue_log2_chunk != 0 ? jd->queue_log2_chunk : ctx->options.queue_log2_chunk;
     const int log2_chunk = log2_option == 0 ? DEFAULT_QUEUE_LOG2 : log2_option;
@@ -1469,7 +1470,7 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     else if (log2_chunk >= 0 && qmode == QueueMode::shared)
         chunk = std::min<uint64_t>({ total, shared_capacity, 1ull << std::min(log2_chunk, 34) });
     const uint64_t queue_bytes = qmode == QueueMode::own ? chunk * 48 : 0;
-    const uint64_t job_bytes = tally_bytes + nv * sizeof(uint32_t) + table_bytes + sizeof(dev::JobCounters) + queue_bytes;
+    const uint64_t job_bytes = tally_bytes + count_bytes + table_bytes + sizeof(dev::JobCounters) + queue_bytes;
     if (ctx->in_use + job_bytes > ctx->budget)
         return fail(ctx, DXMC_ERR_OOM, "job exceeds the device memory budget");
 
@@ -1492,12 +1493,13 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     j->bytes = job_bytes;
     cudaStream_t s = ctx->stream;
     cudaError_t e = cudaSuccess;
-    if (tally_mode == 1)
+    if (tally_mode == 1) {
         e = pool_alloc(ctx, &j->tally_f32, tally_bytes, s);
-    else
-        e = pool_alloc(ctx, &j->tally, tally_bytes, s);
-    if (e == cudaSuccess)
-        e = pool_alloc(ctx, &j->n_events, nv * sizeof(uint32_t), s);
+        if (e == cudaSuccess)
+            e = pool_alloc(ctx, &j->n_events, count_bytes, s);
+    } else {
+        e = pool_alloc(ctx, &j->records, tally_bytes, s);
+    }
     if (e == cudaSuccess)
         e = pool_alloc(ctx, &j->counters, sizeof(dev::JobCounters), s);
     if (e == cudaSuccess)
@@ -1515,9 +1517,9 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
         e = cudaHostGetDevicePointer(&j->cancel_dev, j->cancel_host, 0);
     }
     if (e == cudaSuccess)
-        e = cudaMemsetAsync(j->tally ? static_cast<void*>(j->tally) : static_cast<void*>(j->tally_f32), 0, tally_bytes, s);
-    if (e == cudaSuccess)
-        e = cudaMemsetAsync(j->n_events, 0, nv * sizeof(uint32_t), s);
+        e = cudaMemsetAsync(j->records ? static_cast<void*>(j->records) : static_cast<void*>(j->tally_f32), 0, tally_bytes, s);
+    if (e == cudaSuccess && j->n_events)
+        e = cudaMemsetAsync(j->n_events, 0, count_bytes, s);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(j->counters, 0, sizeof(dev::JobCounters), s);
     if (e == cudaSuccess)
@@ -1560,7 +1562,8 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     }
     p.lut = lut->image;
     p.lut_meta = lut->meta;
-    p.tally = j->tally;
+    p.records = j->records;
+    p.tally = nullptr;
     p.tally_f32 = j->tally_f32;
     p.n_events = j->n_events;
     p.counters = j->counters;
@@ -2298,7 +2301,7 @@ int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double
         std::lock_guard<std::mutex> lock(ctx->mutex);
         cudaSetDevice(ctx->device);
         cudaStream_t s = ctx->result_stream;
-        if (!j->tally && !j->tally_f32)
+        if (!j->records && !j->tally_f32)
             return fail(ctx, DXMC_ERR_STATE, "job results were already released");
         DXMC_CUDA(ctx, cudaMemcpyAsync(hc, j->counters, sizeof(dev::JobCounters), cudaMemcpyDeviceToHost, s));
         // page-locked output buffers are written by the post-processing kernel through
@@ -2313,32 +2316,37 @@ int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double
             const cudaError_t e = j->tally_mode == 1
                 ? dev::launch_postprocess_f32(j->tally_f32, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv,
                       calibration, m_dose, m_var, j->n_events, m_events, s)
-                : dev::launch_postprocess(j->tally, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv,
-                      calibration, m_dose, m_var, j->n_events, m_events, s);
+                : dev::launch_postprocess_records(j->records, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv,
+                      calibration, m_dose, m_var, m_events, s);
             if (e != cudaSuccess)
                 return cuda_fail(ctx, e, "result post-processing");
         }
-        if (!mapped && !j->cancelled && (dose || variance)) {
+        // counts of record tallies are unpacked by the post-processing kernel into a staging array
+        const bool unpack_counts = n_events && j->records;
+        if (!mapped && !j->cancelled && (dose || variance || unpack_counts)) {
             double* d_out = nullptr;
-            const uint64_t out_elems = (dose ? nv : 0) + (variance ? nv : 0);
+            const uint64_t out_elems = (dose ? nv : 0) + (variance ? nv : 0) + (unpack_counts ? (nv + 1) / 2 : 0);
             DXMC_CUDA(ctx, pool_alloc(ctx, &d_out, out_elems * sizeof(double), s));
             double* d_dose = dose ? d_out : nullptr;
             double* d_var = variance ? d_out + (dose ? nv : 0) : nullptr;
+            uint32_t* d_counts = unpack_counts ? reinterpret_cast<uint32_t*>(d_out + (dose ? nv : 0) + (variance ? nv : 0)) : nullptr;
             const double vv = j->world->spacing[0] * j->world->spacing[1] * j->world->spacing[2] / 1000.0;
             cudaError_t e;
             if (j->tally_mode == 1)
                 e = dev::launch_postprocess_f32(j->tally_f32, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, nullptr, nullptr, s);
             else
-                e = dev::launch_postprocess(j->tally, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, nullptr, nullptr, s);
+                e = dev::launch_postprocess_records(j->records, j->world->params, nv, output_mode, static_cast<double>(j->histories), vv, calibration, d_dose, d_var, d_counts, s);
             if (e == cudaSuccess && dose)
                 e = cudaMemcpyAsync(dose, d_dose, nv * sizeof(double), cudaMemcpyDeviceToHost, s);
             if (e == cudaSuccess && variance)
                 e = cudaMemcpyAsync(variance, d_var, nv * sizeof(double), cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess && d_counts)
+                e = cudaMemcpyAsync(n_events, d_counts, nv * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
             cudaFreeAsync(d_out, s);
             if (e != cudaSuccess)
                 return cuda_fail(ctx, e, "result post-processing");
         }
-        if (!mapped && !j->cancelled && n_events)
+        if (!mapped && !j->cancelled && n_events && j->n_events)
             DXMC_CUDA(ctx, cudaMemcpyAsync(n_events, j->n_events, nv * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
         DXMC_CUDA(ctx, cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
         const cudaError_t e = cudaEventRecord(done, s);
@@ -2406,12 +2414,12 @@ int dxmc_gpu_job_preview(dxmc_job* j, double* energy)
         return DXMC_ERR_INVALID;
     dxmc_gpu_ctx* ctx = j->ctx;
     std::lock_guard<std::mutex> lock(ctx->mutex);
-    if (!j->tally)
+    if (!j->records)
         return fail(ctx, DXMC_ERR_STATE, j->tally_f32 ? "dose preview needs the FP64 tally" : "job results were already released");
     cudaSetDevice(ctx->device);
     const uint64_t nv = j->world->params.n_voxels;
-    // every other double of the interleaved (energy, energy^2) tally
-    DXMC_CUDA(ctx, cudaMemcpy2DAsync(energy, sizeof(double), j->tally, 2 * sizeof(double), sizeof(double), nv,
+    // the energy sum of each 32-byte tally record
+    DXMC_CUDA(ctx, cudaMemcpy2DAsync(energy, sizeof(double), j->records, sizeof(dev::TallyRecord), sizeof(double), nv,
         cudaMemcpyDeviceToHost, ctx->result_stream));
     DXMC_CUDA(ctx, cudaStreamSynchronize(ctx->result_stream));
     return DXMC_OK;

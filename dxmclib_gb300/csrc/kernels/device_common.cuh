@@ -133,13 +133,33 @@ struct Rng {
 
     __device__ void init(uint64_t seed, uint64_t history)
     {
+#ifdef DXMC_SEED_SPLITMIX
+        // SplitMix64 (Steele, Lea, Flood 2014) of (seed, history): the seeding Vigna
+        // recommends for the xoshiro family
+        uint64_t x = seed ^ (history * 0x9e3779b97f4a7c15ull);
+        uint64_t a = splitmix64(x), b = splitmix64(x);
+        s0 = static_cast<uint32_t>(a);
+        s1 = static_cast<uint32_t>(a >> 32);
+        s2 = static_cast<uint32_t>(b);
+        s3 = static_cast<uint32_t>(b >> 32) | 1u;
+#else
         const uint4 r = philox4x32_10(make_uint4(static_cast<uint32_t>(history), static_cast<uint32_t>(history >> 32), 0x44584d43u, 0u),
             static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
         s0 = r.x;
         s1 = r.y;
         s2 = r.z;
         s3 = r.w | 1u; // the all-zero state is excluded
+#endif
     }
+#ifdef DXMC_SEED_SPLITMIX
+    __device__ __forceinline__ static uint64_t splitmix64(uint64_t& x)
+    {
+        uint64_t z = (x += 0x9e3779b97f4a7c15ull);
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        return z ^ (z >> 31);
+    }
+#endif
     // the sum output of xoshiro128+: its lowest bits are weak, and every use
     // takes the high bits (23-bit float mantissas, multiply-high integers)
     __device__ __forceinline__ uint32_t next()

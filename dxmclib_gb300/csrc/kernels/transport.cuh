@@ -97,12 +97,24 @@ struct PhotonQueue {
     uint64_t capacity;
 };
 
+// FP64 tally of one voxel in one 32-byte sector (the unit of L2 and DRAM
+// transfers): a deposit's three atomic additions touch a single sector.
+struct alignas(32) TallyRecord {
+    double energy;   // sum of energy imparted x weight (keV)
+    double energy2;  // sum of its squares
+    uint32_t events; // deposits
+    uint32_t pad0;
+    uint64_t pad1;
+};
+static_assert(sizeof(TallyRecord) == 32, "one tally record per 32-byte sector");
+
 struct TransportParams {
     WorldParams world;
     SourceParams source;
     const float* lut;   // global LUT image
     LutMeta lut_meta;
-    double* tally;      // interleaved (energy, energy^2) per voxel, FP64
+    TallyRecord* records; // FP64 tallies as one record per voxel (jobs); nullptr: the arrays below
+    double* tally;      // interleaved (energy, energy^2) per voxel, FP64 (with n_events; the no-allocation path)
     float* tally_f32;   // interleaved, FP32 tally mode
     uint32_t* n_events;
     JobCounters* counters;
@@ -168,6 +180,9 @@ size_t transport_smem_bytes(size_t lut_bytes, bool lut_in_smem, bool palette);
 cudaError_t launch_postprocess(const double* tally, const WorldParams& w, uint64_t n,
     int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance,
     const uint32_t* counts, uint32_t* counts_out, cudaStream_t stream);
+cudaError_t launch_postprocess_records(const TallyRecord* records, const WorldParams& w, uint64_t n,
+    int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance,
+    uint32_t* counts_out, cudaStream_t stream);
 cudaError_t launch_postprocess_f32(const float* tally, const WorldParams& w, uint64_t n,
     int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance,
     const uint32_t* counts, uint32_t* counts_out, cudaStream_t stream);

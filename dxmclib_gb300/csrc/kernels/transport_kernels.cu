@@ -29,8 +29,41 @@ namespace {
     };
 
     // ---- scoring (transport.hpp:208-214, 598-609) ------------------------------
+    // Atomic additions to the tally with an L2 evict-first policy: the tally is
+    // read-modify-written at random voxels and would otherwise push the voxel and
+    // majorant grids (gathered on every flight) out of L2.
+    __device__ __forceinline__ void red_add_evict_first(double* a, double v)
+    {
+#ifdef DXMC_TALLY_NO_HINT
+        atomicAdd(a, v);
+        return;
+#endif
+        asm volatile("{\n\t.reg .b64 pol;\n\tcreatepolicy.fractional.L2::evict_first.b64 pol, 1.0;\n\t"
+                     "red.global.add.L2::cache_hint.f64 [%0], %1, pol;\n\t}" ::"l"(a), "d"(v) : "memory");
+    }
+    __device__ __forceinline__ void red_add_evict_first(uint32_t* a, uint32_t v)
+    {
+#ifdef DXMC_TALLY_NO_HINT
+        atomicAdd(a, v);
+        return;
+#endif
+        asm volatile("{\n\t.reg .b64 pol;\n\tcreatepolicy.fractional.L2::evict_first.b64 pol, 1.0;\n\t"
+                     "red.global.add.L2::cache_hint.u32 [%0], %1, pol;\n\t}" ::"l"(a), "r"(v) : "memory");
+    }
+    __device__ __forceinline__ void score_record(TallyRecord* r, double e, double e2, uint32_t n)
+    {
+        red_add_evict_first(&r->energy, e);
+        red_add_evict_first(&r->energy2, e2);
+        red_add_evict_first(&r->events, n);
+    }
+
     __device__ __forceinline__ void score(const TransportParams& p, uint64_t idx, float e)
     {
+        if (p.records) {
+            const double ed = static_cast<double>(e);
+            score_record(p.records + idx, ed, ed * ed, 1u);
+            return;
+        }
         if (p.tally_mode == 1) {
             float* t = p.tally_f32 + 2 * idx;
             atomicAdd(t, e);
@@ -63,10 +96,14 @@ namespace {
             ++count;
         }
         if (lane == leader) {
-            double* t = p.tally + 2 * idx;
-            atomicAdd(t, static_cast<double>(sum));
-            atomicAdd(t + 1, static_cast<double>(sum2));
-            atomicAdd(p.n_events + idx, count);
+            if (p.records) {
+                score_record(p.records + idx, static_cast<double>(sum), static_cast<double>(sum2), count);
+            } else {
+                double* t = p.tally + 2 * idx;
+                atomicAdd(t, static_cast<double>(sum));
+                atomicAdd(t + 1, static_cast<double>(sum2));
+                atomicAdd(p.n_events + idx, count);
+            }
         }
     }
 
@@ -1119,6 +1156,38 @@ namespace {
         }
     }
 
+    // Post-processing from tally records: one 32-byte record read per voxel.
+    __global__ void postprocess_records_kernel(const TallyRecord* __restrict__ rec, const Voxel* __restrict__ voxels,
+        const uint8_t* __restrict__ palette_index, const PaletteEntry* __restrict__ palette, uint64_t n, int mode,
+        double histories, double voxel_volume_cm3, double calibration, double* __restrict__ dose, double* __restrict__ variance,
+        uint32_t* __restrict__ counts_out)
+    {
+        const double h_inv = 1.0 / (histories - 1.0);
+        const double h_d = 1.0e3 / histories;
+        const double h_v = 1.0e6 / histories;
+        for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+            const double2 ee2 = __ldcs(reinterpret_cast<const double2*>(rec + i));
+            const double e = ee2.x, ee = ee2.y;
+            double d = e, v = ee;
+            if (mode == 1) { // EV_PER_HISTORY: normalizeScoring
+                d = e * h_d;
+                v = (ee * h_v - d * d) * h_inv;
+            } else if (mode == 2) { // DOSE: energyImpartedToDose
+                const double de = static_cast<double>(voxels ? voxels[i].density : palette[palette_index[i]].density);
+                const double mass = de * voxel_volume_cm3 * 0.001;
+                const double f = calibration / mass;
+                d = de > 0.0 ? e * f : 0.0;
+                v = de > 0.0 ? ee * f * f : 0.0;
+            }
+            if (dose)
+                dose[i] = d;
+            if (variance)
+                variance[i] = v;
+            if (counts_out)
+                counts_out[i] = __ldcs(&rec[i].events);
+        }
+    }
+
     // ---- per-material maximum density (attenuationinterpolator.hpp:48-60) ------------
     __global__ void max_density_kernel(const Voxel* __restrict__ voxels, uint64_t n, unsigned int* out_bits, int n_materials)
     {
@@ -1312,6 +1381,17 @@ cudaError_t launch_postprocess(const double* tally, const WorldParams& w, uint64
     const int grid = static_cast<int>(std::min<uint64_t>((n + block - 1) / block, 152ull * 16));
     postprocess_kernel<double><<<grid, block, 0, stream>>>(tally, w.palette_index ? nullptr : w.voxels, w.palette_index, w.palette, n, mode,
         histories, voxel_volume_cm3, calibration, dose, variance, counts, counts_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_postprocess_records(const TallyRecord* records, const WorldParams& w, uint64_t n, int mode,
+    double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance, uint32_t* counts_out,
+    cudaStream_t stream)
+{
+    const int block = 256;
+    const int grid = static_cast<int>(std::min<uint64_t>((n + block - 1) / block, 152ull * 16));
+    postprocess_records_kernel<<<grid, block, 0, stream>>>(records, w.palette_index ? nullptr : w.voxels, w.palette_index,
+        w.palette, n, mode, histories, voxel_volume_cm3, calibration, dose, variance, counts_out);
     return cudaGetLastError();
 }
 

@@ -185,7 +185,8 @@ class GpuBackend:
 
     def job_bytes(self, req: ServeRequest) -> int:
         n = int(req.world.size())
-        return n * 20 + 80 * len(req.exposures) + (1 << 20)
+        # one 32-byte FP64 tally record per voxel, the job's tables and counters
+        return n * 32 + 80 * len(req.exposures) + (1 << 20)
 
     def upload_world(self, world):
         dw = self.api.DeviceWorld(self.ctx, world)

@@ -126,7 +126,7 @@ def test_dose_output_mode_matches_reference(gpu_ctx, golden, mode):
     dose, var, nev, stats = _job(gpu_ctx, world, table, spec, heel, float(g["max_energy"]), 2028, A.OUTPUT_DOSE,
                                     calibration=cal)
     n_gpu = float(stats["histories"])
-    ref = {k[len(mode) + 1:]: g[k] for k in g.files if k.startswith(mode + "_")}
+    ref = {k[len(mode) + 1:]: v for k, v in g.items() if k.startswith(mode + "_")}
     if mode == "mgy":  # mGy for the same dose-area product: independent of the history count
         ref_n = ref
         d_gpu, v_gpu = block_sums(dose, dims, block), block_sums(var, dims, block)
