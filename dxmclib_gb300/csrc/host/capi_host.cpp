@@ -4,7 +4,7 @@
 
 #include "../physics/physics_model.hpp"
 #include "lut_builder.hpp"
-#include "../kernels/philox.hpp"
+#include "../kernels/stream_seed.hpp"
 
 #include <algorithm>
 #include <cstring>
@@ -219,16 +219,11 @@ int dxmc_udiv_invariant(const uint32_t* n, uint64_t count, uint32_t d, uint32_t*
     return DXMC_OK;
 }
 
-int dxmc_philox4x32_10(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4])
+int dxmc_stream_seed(uint64_t seed, uint64_t history, uint32_t out[4])
 {
-    if (!counter || !key || !out)
+    if (!out)
         return DXMC_ERR_INVALID;
-    uint32_t c0 = counter[0], c1 = counter[1], c2 = counter[2], c3 = counter[3];
-    dxmc_gb300::philox4x32_10(c0, c1, c2, c3, key[0], key[1]);
-    out[0] = c0;
-    out[1] = c1;
-    out[2] = c2;
-    out[3] = c3;
+    dxmc_gb300::stream_seed(seed, history, out);
     return DXMC_OK;
 }
 

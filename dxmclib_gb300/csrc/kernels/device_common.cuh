@@ -5,7 +5,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include "philox.hpp"
+#include "stream_seed.hpp"
 
 namespace dxmc_gb300::dev {
 
@@ -113,53 +113,23 @@ constexpr float ROULETTE_PROBABILITY = 0.8f;    // transport.hpp:819-822
 constexpr float N_ERROR = 1.0e-9f;              // transport.hpp:831-834
 constexpr int REJECTION_CAP = 4096;             // iteration cap on every sampling loop
 
-// ---------------------------------------------------------------------------
-// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): counter-based, one
-// independent stream per (seed, history) pair.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1)
-{
-    dxmc_gb300::philox4x32_10(c.x, c.y, c.z, c.w, k0, k1);
-    return c;
-}
-
 // Per-history random stream: xoshiro128+ (Blackman and Vigna, "Scrambled
 // linear pseudorandom number generators", 2021), a 32-bit-native generator,
-// with its 128-bit state drawn from Philox4x32-10 keyed by the job seed with
-// the history id as counter.  Every history has its own stream, so a job can be
-// split or resumed at any history id and results do not depend on scheduling.
+// with its 128-bit state from SplitMix64 of (job seed, history id)
+// (stream_seed.hpp).  Every history has its own stream, so a job can be split
+// or resumed at any history id and results do not depend on scheduling.
 struct Rng {
     uint32_t s0, s1, s2, s3;
 
     __device__ void init(uint64_t seed, uint64_t history)
     {
-#ifdef DXMC_SEED_SPLITMIX
-        // SplitMix64 (Steele, Lea, Flood 2014) of (seed, history): the seeding Vigna
-        // recommends for the xoshiro family
-        uint64_t x = seed ^ (history * 0x9e3779b97f4a7c15ull);
-        uint64_t a = splitmix64(x), b = splitmix64(x);
-        s0 = static_cast<uint32_t>(a);
-        s1 = static_cast<uint32_t>(a >> 32);
-        s2 = static_cast<uint32_t>(b);
-        s3 = static_cast<uint32_t>(b >> 32) | 1u;
-#else
-        const uint4 r = philox4x32_10(make_uint4(static_cast<uint32_t>(history), static_cast<uint32_t>(history >> 32), 0x44584d43u, 0u),
-            static_cast<uint32_t>(seed), static_cast<uint32_t>(seed >> 32));
-        s0 = r.x;
-        s1 = r.y;
-        s2 = r.z;
-        s3 = r.w | 1u; // the all-zero state is excluded
-#endif
+        uint32_t st[4];
+        stream_seed(seed, history, st);
+        s0 = st[0];
+        s1 = st[1];
+        s2 = st[2];
+        s3 = st[3];
     }
-#ifdef DXMC_SEED_SPLITMIX
-    __device__ __forceinline__ static uint64_t splitmix64(uint64_t& x)
-    {
-        uint64_t z = (x += 0x9e3779b97f4a7c15ull);
-        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
-        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
-        return z ^ (z >> 31);
-    }
-#endif
     // the sum output of xoshiro128+: its lowest bits are weak, and every use
     // takes the high bits (23-bit float mantissas, multiply-high integers)
     __device__ __forceinline__ uint32_t next()

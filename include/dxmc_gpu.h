@@ -196,9 +196,11 @@ typedef struct dxmc_bowtie_desc {
     const double* weights;
 } dxmc_bowtie_desc;
 
-/* Philox4x32-10, the counter-based generator the kernels draw from (one stream
- * per history), exposed for known-answer tests. */
-int dxmc_philox4x32_10(const uint32_t counter[4], const uint32_t key[2], uint32_t out[4]);
+/* The xoshiro128+ state of the random stream of history `history` of a job
+ * seeded with `seed` (SplitMix64 of (seed, history)), as the kernels seed it;
+ * exposed for known-answer tests.  Replaces RandomState's seeding from
+ * std::random_device (dxmcrandom.hpp:42-48), which is not reproducible. */
+int dxmc_stream_seed(uint64_t seed, uint64_t history, uint32_t out[4]);
 /* The kernels' division of history ids by the histories per exposure (multiply-high
  * and shifts, magic from the divisor), for host-side checks: out[i] = n[i] / d. */
 int dxmc_udiv_invariant(const uint32_t* n, uint64_t count, uint32_t d, uint32_t* out);

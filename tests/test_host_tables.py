@@ -84,21 +84,36 @@ def test_alias_table_distribution(lib):
     np.testing.assert_allclose(implied / 40, w / w.sum(), rtol=1e-12)
 
 
-def test_philox_known_answers(lib):
-    """Philox4x32-10 known-answer vectors from the Random123 distribution (Salmon et al., SC'11)."""
+def _splitmix64(x):
+    """SplitMix64 (Steele, Lea and Flood, OOPSLA 2014), restated in Python: returns
+    (new counter, output)."""
+    m = (1 << 64) - 1
+    x = (x + 0x9E3779B97F4A7C15) & m
+    z = x
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+    return x, z ^ (z >> 31)
+
+
+def test_stream_seed_known_answers(lib):
+    """The per-history stream state (SplitMix64 of seed ^ history * gamma, two
+    outputs, lowest bit of the last word set) against a Python restatement, for
+    seeds and history ids across the 64-bit range."""
     from dxmclib_gb300 import _capi as A
-    cases = [
-        ([0, 0, 0, 0], [0, 0], [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
-        ([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2, [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
-        ([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0],
-         [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]),
-    ]
-    for c, k, want in cases:
-        c = np.array(c, np.uint32)
-        k = np.array(k, np.uint32)
-        o = np.zeros(4, np.uint32)
-        assert lib.dxmc_philox4x32_10(c.ctypes.data_as(A.U32P), k.ctypes.data_as(A.U32P), o.ctypes.data_as(A.U32P)) == 0
-        assert o.tolist() == want
+    m = (1 << 64) - 1
+    # SplitMix64 itself: its first two outputs from counter 0
+    x, a = _splitmix64(0)
+    x, b = _splitmix64(x)
+    assert (a, b) == (0xE220A8397B1DCDAF, 0x6E789E6AA1B965F4)
+    for seed in (0, 1, 2026, 0xFFFFFFFFFFFFFFFF, 0x123456789ABCDEF0):
+        for h in (0, 1, 255, 256, 1 << 32, (1 << 64) - 1):
+            x = seed ^ ((h * 0x9E3779B97F4A7C15) & m)
+            x, a = _splitmix64(x)
+            x, b = _splitmix64(x)
+            want = [a & 0xFFFFFFFF, a >> 32, b & 0xFFFFFFFF, (b >> 32) | 1]
+            o = np.zeros(4, np.uint32)
+            assert lib.dxmc_stream_seed(seed, h, o.ctypes.data_as(A.U32P)) == 0
+            assert o.tolist() == want, (seed, h)
 
 
 def _dx_source():
