@@ -421,7 +421,7 @@ int dxmc_gpu_probe_interactions(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, 
     double energy, uint64_t n, uint64_t seed, float* out_cos, float* out_energy, float* out_deposit);
 
 /* Histogram of the per-history random streams every device sampler draws
- * from (xoshiro128+ seeded by Philox4x32-10 of (seed, stream)): n_streams
+ * from (xoshiro128+ seeded by SplitMix64 of (seed, stream)): n_streams
  * streams of draws_per_stream values.  kind 0: uniform in [0, 1); kind 1: the
  * open-at-zero uniform in (0, 1] used for logarithms, binned as 1 - u; kind 2:
  * an integer below n_bins.  hist gets n_bins + 1 counts, the last one of the

@@ -1,7 +1,7 @@
 """GPU test: uniformity of the device random streams.
 
 Every device sampler draws from per-history xoshiro128+ streams whose state is
-Philox4x32-10 of (seed, history).  DXMClib checks its own generator by
+SplitMix64 of (seed, history).  DXMClib checks its own generator by
 binning 1e8 uniforms into 100 bins and requiring each bin within 5 % of the
 nominal count (tests/testrandom.cpp:21-58).  The same check runs here on the
 device streams through dxmc_gpu_probe_uniform (the C ABI), with a chi-square
