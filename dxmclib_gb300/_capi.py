@@ -35,6 +35,7 @@ OUTPUT_RAW, OUTPUT_EV_PER_HISTORY, OUTPUT_DOSE = 0, 1, 2
 TALLY_F64, TALLY_F32, TALLY_WARP_F64 = 0, 1, 2
 TRACKING_DEFAULT, TRACKING_GLOBAL, TRACKING_LOCAL = 0, 1, 2
 DIRECTION_REFERENCE, DIRECTION_NORMALIZED = 0, 1
+PRECISION_FP32, PRECISION_FP64 = 0, 1
 
 D = C.c_double
 DP = C.POINTER(C.c_double)
@@ -122,7 +123,7 @@ class JobDesc(C.Structure):
         ("seed", C.c_uint64), ("model", C.c_int32), ("tally_mode", C.c_int32),
         ("regen_threshold", C.c_int32), ("interact_threshold", C.c_int32), ("blocks_per_sm", C.c_int32),
         ("queue_log2_chunk", C.c_int32), ("woodcock_burst", C.c_int32), ("block_size", C.c_int32),
-        ("tracking", C.c_int32), ("direction", C.c_int32),
+        ("tracking", C.c_int32), ("direction", C.c_int32), ("precision", C.c_int32),
     ]
 
 

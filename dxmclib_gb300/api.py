@@ -1083,11 +1083,13 @@ class Job:
                  spectrum: Optional[Spectrum] = None, heel: Optional[HeelTable] = None, bowtie=None,
                  seed: int = 1, model: int = LOWENERGYCORRECTION.LIVERMORE, tally_mode: int = -1,
                  launch: Optional[dict] = None, tracking: int = A.TRACKING_DEFAULT,
-                 direction: int = A.DIRECTION_REFERENCE):
+                 direction: int = A.DIRECTION_REFERENCE, precision: int = A.PRECISION_FP32):
         """``launch`` may set the keys of LAUNCH_KEYS for this job (an autotuner's
         choice); unset keys use the context's.  ``tracking``: A.TRACKING_* (the
         context's when DEFAULT).  ``direction``: A.DIRECTION_REFERENCE (the
-        reference's peturb) or A.DIRECTION_NORMALIZED (unit scattering axis)."""
+        reference's peturb) or A.DIRECTION_NORMALIZED (unit scattering axis).
+        ``precision``: A.PRECISION_FP32 (FP32 transport, FP64 tallies) or
+        A.PRECISION_FP64 (FP64 everywhere, as Transport<double>)."""
         self.ctx = ctx
         self.dworld = dworld
         self._owned = True
@@ -1095,6 +1097,8 @@ class Job:
             launch = dict(launch or {}, tracking=tracking)
         if direction != A.DIRECTION_REFERENCE:
             launch = dict(launch or {}, direction=direction)
+        if precision != A.PRECISION_FP32:
+            launch = dict(launch or {}, precision=precision)
         jd = self._describe(exposures, spectrum, heel, bowtie, seed, model, tally_mode, launch)
         self.handle = C.c_void_p()
         A.check(ctx.lib.dxmc_gpu_job_submit(ctx.handle, dworld.handle, dlut.handle, C.byref(jd), C.byref(self.handle)),
@@ -1109,7 +1113,7 @@ class Job:
         return j
 
     LAUNCH_KEYS = ("regen_threshold", "interact_threshold", "blocks_per_sm", "queue_log2_chunk", "woodcock_burst",
-                   "block_size", "tracking", "direction")
+                   "block_size", "tracking", "direction", "precision")
 
     def _describe(self, exposures: ExposureTable, spectrum, heel, bowtie, seed, model, tally_mode,
                   launch: Optional[dict] = None) -> A.JobDesc:

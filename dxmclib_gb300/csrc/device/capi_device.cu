@@ -1358,6 +1358,8 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
         return fail(ctx, DXMC_ERR_INVALID, "unknown tracking mode");
     if (jd->direction != DXMC_DIRECTION_REFERENCE && jd->direction != DXMC_DIRECTION_NORMALIZED)
         return fail(ctx, DXMC_ERR_INVALID, "unknown direction mode");
+    if (jd->precision != DXMC_PRECISION_FP32 && jd->precision != DXMC_PRECISION_FP64)
+        return fail(ctx, DXMC_ERR_INVALID, "unknown precision");
 
     // ---- host-side tables: exposures, prefix offsets, spectrum, heel, bow-tie ----
     const uint64_t ne = jd->n_exposures;
@@ -1463,7 +1465,8 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     const uint64_t count_bytes = tally_mode == 1 ? nv * sizeof(uint32_t) : 0; // records hold their counts
     // photon queue: chunks of 2^k histories, 48 bytes per queued photon
     const int log2_option = jd->queue_log2_chunk != 0 ? jd->queue_log2_chunk : ctx->options.queue_log2_chunk;
-    const int log2_chunk = log2_option == 0 ? DEFAULT_QUEUE_LOG2 : log2_option;
+    // FP64 jobs generate their photons in the kernel (the queue holds FP32 photons)
+    const int log2_chunk = jd->precision == DXMC_PRECISION_FP64 ? -1 : (log2_option == 0 ? DEFAULT_QUEUE_LOG2 : log2_option);
     uint64_t chunk = 0;
     if (log2_chunk >= 0 && qmode == QueueMode::own)
         chunk = std::min<uint64_t>(total, 1ull << std::min(log2_chunk, 34));
@@ -1571,6 +1574,7 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     p.total_histories = total;
     p.seed = jd->seed;
     p.tally_mode = tally_mode;
+    p.precision = jd->precision;
     p.uniform_hpe = 0;
     {
         bool uniform = true;
@@ -1638,7 +1642,7 @@ LaunchPlan plan_launch(dxmc_gpu_ctx* ctx, const dxmc_world* world, const dxmc_lu
     L.block = jd->block_size == 128 || jd->block_size == 256 ? jd->block_size
                                                               : (ctx->options.block_size > 0 ? ctx->options.block_size : 256);
     // also sets the kernel's dynamic shared-memory limit for this launch
-    const int occ = dev::transport_max_blocks_per_sm(model, palette, L.block, L.smem);
+    const int occ = dev::transport_max_blocks_per_sm(model, palette, L.block, L.smem, p.precision);
     int per_sm = jd->blocks_per_sm > 0 ? std::min(jd->blocks_per_sm, std::max(occ, 1))
                                         : (ctx->options.blocks_per_sm > 0 ? ctx->options.blocks_per_sm : occ);
     if (per_sm <= 0)
@@ -1963,6 +1967,10 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
     if (mode < DXMC_BATCH_AUTO || mode > DXMC_BATCH_PERSISTENT)
         return fail(ctx, DXMC_ERR_INVALID, "unknown batch mode");
     const bool persistent = mode == DXMC_BATCH_PERSISTENT;
+    if (persistent)
+        for (int i = 0; i < n; ++i)
+            if (entries[i].job && entries[i].job->precision != DXMC_PRECISION_FP32)
+                return fail(ctx, DXMC_ERR_INVALID, "the persistent multi-job kernel computes in FP32: run FP64 jobs in a concurrent batch");
     const int chains = std::clamp(opt && opt->chains > 0 ? opt->chains : DEFAULT_CHAINS, 1, MAX_CHAINS);
     std::lock_guard<std::mutex> lock(ctx->mutex);
     ++ctx->submission; // the grids of every entry stay until the batch has launched

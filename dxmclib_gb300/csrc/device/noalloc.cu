@@ -297,6 +297,8 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         return reject(ctx, "dxmc_gpu_transport_noalloc: unknown tracking mode");
     if (jd->direction != DXMC_DIRECTION_REFERENCE && jd->direction != DXMC_DIRECTION_NORMALIZED)
         return reject(ctx, "dxmc_gpu_transport_noalloc: unknown direction mode");
+    if (jd->precision != DXMC_PRECISION_FP32 && jd->precision != DXMC_PRECISION_FP64)
+        return reject(ctx, "dxmc_gpu_transport_noalloc: unknown precision");
     if (jd->model < 0 || jd->model > 2)
         return reject(ctx, "unknown low-energy correction model");
     if (meta.n_materials < world_materials)
@@ -379,6 +381,7 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         if (g)
             p.majorant = *g;
         p.normalize_direction = jd->direction == DXMC_DIRECTION_NORMALIZED ? 1 : 0;
+        p.precision = jd->precision;
         p.regen_threshold = capi::ctx_regen_threshold(ctx, g != nullptr);
         p.interact_threshold = capi::ctx_interact_threshold(ctx);
         p.woodcock_burst = jd->woodcock_burst > 0 ? std::min(jd->woodcock_burst, 64) : capi::default_woodcock_burst(g != nullptr);
@@ -388,7 +391,7 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         const bool palette = wp->palette_index != nullptr;
         const size_t smem = dev::transport_smem_bytes(lut_bytes, p.lut_in_smem != 0, palette);
         const int block = 256;
-        int per_sm = dev::transport_max_blocks_per_sm(jd->model, palette, block, smem);
+        int per_sm = dev::transport_max_blocks_per_sm(jd->model, palette, block, smem, jd->precision);
         if (per_sm <= 0)
             per_sm = 1;
         e = dev::launch_transport(p, jd->model, capi::ctx_sm_count(ctx) * per_sm, block, smem, stream);

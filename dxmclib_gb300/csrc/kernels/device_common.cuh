@@ -65,37 +65,76 @@ struct LutMeta {
     int pad0;
 };
 
+__device__ __forceinline__ float exp10_fast(float y) { return exp2f(y * 3.32192809488736f); }
+
+// Arithmetic in the precision a kernel computes in: float (single-precision
+// intrinsics; the transport's translation unit is built with fast math) or
+// double (the FP64-everywhere precision mode, accurate double functions).
+// One source serves both through these overloads.
+__device__ __forceinline__ float m_log(float x) { return __logf(x); }
+__device__ __forceinline__ double m_log(double x) { return log(x); }
+__device__ __forceinline__ float m_log2(float x) { return __log2f(x); }
+__device__ __forceinline__ double m_log2(double x) { return log2(x); }
+__device__ __forceinline__ float m_log10(float x) { return __log10f(x); }
+__device__ __forceinline__ double m_log10(double x) { return log10(x); }
+__device__ __forceinline__ float m_exp10(float y) { return exp10_fast(y); }
+__device__ __forceinline__ double m_exp10(double y) { return exp10(y); }
+__device__ __forceinline__ float m_exp(float y) { return expf(y); }
+__device__ __forceinline__ double m_exp(double y) { return exp(y); }
+__device__ __forceinline__ void m_sincos(float a, float* s, float* c) { sincosf(a, s, c); }
+__device__ __forceinline__ void m_sincos(double a, double* s, double* c) { sincos(a, s, c); }
+__device__ __forceinline__ float m_cos(float a) { return cosf(a); }
+__device__ __forceinline__ double m_cos(double a) { return cos(a); }
+__device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float m_rsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double m_rsqrt(double x) { return rsqrt(x); }
+__device__ __forceinline__ float m_fma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double m_fma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float m_min(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ double m_min(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ float m_max(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ double m_max(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ float m_abs(float a) { return fabsf(a); }
+__device__ __forceinline__ double m_abs(double a) { return fabs(a); }
+__device__ __forceinline__ float m_floor(float a) { return floorf(a); }
+__device__ __forceinline__ double m_floor(double a) { return floor(a); }
+__device__ __forceinline__ int m_floor_int(float a) { return __float2int_rd(a); }
+__device__ __forceinline__ int m_floor_int(double a) { return __double2int_rd(a); }
+
 // Rows of the sampling tables around energy E: row i and i + 1 with weight f of
 // the upper one.  Draws interpolate the two rows' quantiles at the same level
 // (quantile interpolation), which follows distributions that stretch with
 // energy far more closely than a mixture of the rows would.
-__device__ __forceinline__ int table_row(const LutMeta& m, float E, float& f)
+template <class Real>
+__device__ __forceinline__ int table_row(const LutMeta& m, Real E, Real& f)
 {
-    const float t = (__logf(E) - m.tab_le0) * m.tab_inv_dle;
-    int i = static_cast<int>(floorf(t));
-    f = t - static_cast<float>(i);
+    const Real t = (m_log(E) - m.tab_le0) * m.tab_inv_dle;
+    int i = static_cast<int>(m_floor(t));
+    f = t - static_cast<Real>(i);
     if (i < 0) {
         i = 0;
-        f = 0.0f;
+        f = Real(0);
     } else if (i > m.tab_ne - 2) {
         i = m.tab_ne - 2;
-        f = 1.0f;
+        f = Real(1);
     }
     return i;
 }
 
 // Quantile at level u of the energy rows `row` and `row + 1` (stride nu + 1),
 // linear between the stored levels k / nu and between the two rows (weight fe).
-__device__ __forceinline__ float table_quantile(const float* row, int nu, float u, float fe)
+template <class Real>
+__device__ __forceinline__ Real table_quantile(const float* row, int nu, Real u, Real fe)
 {
-    const float pos = u * static_cast<float>(nu);
+    const Real pos = u * static_cast<Real>(nu);
     const int j = min(static_cast<int>(pos), nu - 1);
-    const float f = pos - static_cast<float>(j);
-    const float a0 = __ldg(row + j), b0 = __ldg(row + j + 1);
-    const float a1 = __ldg(row + nu + 1 + j), b1 = __ldg(row + nu + 1 + j + 1);
-    const float q0 = fmaf(f, b0 - a0, a0);
-    const float q1 = fmaf(f, b1 - a1, a1);
-    return fmaf(fe, q1 - q0, q0);
+    const Real f = pos - static_cast<Real>(j);
+    const Real a0 = __ldg(row + j), b0 = __ldg(row + j + 1);
+    const Real a1 = __ldg(row + nu + 1 + j), b1 = __ldg(row + nu + 1 + j + 1);
+    const Real q0 = m_fma(f, b0 - a0, a0);
+    const Real q1 = m_fma(f, b1 - a1, a1);
+    return m_fma(fe, q1 - q0, q0);
 }
 
 constexpr int RITA_N = 56;
@@ -112,6 +151,15 @@ constexpr float ROULETTE_THRESHOLD = 5.0f;      // transport.hpp:823-826
 constexpr float ROULETTE_PROBABILITY = 0.8f;    // transport.hpp:819-822
 constexpr float N_ERROR = 1.0e-9f;              // transport.hpp:831-834
 constexpr int REJECTION_CAP = 4096;             // iteration cap on every sampling loop
+// the same constants in double, for kernels that compute in double (a float
+// kernel rounds them to the float values above)
+constexpr double PI_D = 3.14159265358979323846;
+constexpr double KEV_TO_ANGSTROM_D = 12.398520;
+constexpr double ELECTRON_REST_MASS_D = 510.9989461;
+constexpr double ENERGY_CUTOFF_D = 1.0;
+constexpr double ROULETTE_THRESHOLD_D = 5.0;
+constexpr double ROULETTE_PROBABILITY_D = 0.8;
+constexpr double N_ERROR_D = 1.0e-9;
 
 // Per-history random stream: xoshiro128+ (Blackman and Vigna, "Scrambled
 // linear pseudorandom number generators", 2021), a 32-bit-native generator,
@@ -155,21 +203,28 @@ struct Rng {
     __device__ __forceinline__ float azimuth() { return fmaf(uniform(), 6.28318530717959f, -3.14159265358979f); }
 };
 
+// azimuth uniform in [-pi, pi) in the kernel's precision, from the same 23-bit draw
+template <class Real>
+__device__ __forceinline__ Real rng_azimuth(Rng& r)
+{
+    return m_fma(static_cast<Real>(r.uniform()), Real(2.0 * PI_D), Real(-PI_D));
+}
+
 // ---------------------------------------------------------------------------
 // Math helpers
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float exp10_fast(float y) { return exp2f(y * 3.32192809488736f); }
 
 // vectormath::rotate (vectormath.hpp:83-99): Rodrigues rotation about a (not
 // necessarily unit) axis.
-__device__ __forceinline__ void rotate(float& vx, float& vy, float& vz, float ax, float ay, float az, float angle)
+template <class Real>
+__device__ __forceinline__ void rotate(Real& vx, Real& vy, Real& vz, Real ax, Real ay, Real az, Real angle)
 {
-    float s, c;
-    sincosf(angle, &s, &c);
-    const float midt = (1.0f - c) * (vx * ax + vy * ay + vz * az);
-    const float ox = c * vx + midt * ax + s * (ay * vz - az * vy);
-    const float oy = c * vy + midt * ay + s * (-ax * vz + az * vx);
-    const float oz = c * vz + midt * az + s * (ax * vy - ay * vx);
+    Real s, c;
+    m_sincos(angle, &s, &c);
+    const Real midt = (Real(1) - c) * (vx * ax + vy * ay + vz * az);
+    const Real ox = c * vx + midt * ax + s * (ay * vz - az * vy);
+    const Real oy = c * vy + midt * ay + s * (-ax * vz + az * vx);
+    const Real oz = c * vz + midt * az + s * (ax * vy - ay * vx);
     vx = ox;
     vy = oy;
     vz = oz;
@@ -182,33 +237,34 @@ __device__ __forceinline__ void rotate(float& vx, float& vy, float& vz, float ax
 // length first: a unit direction then turns by exactly theta and stays a unit
 // vector (the normalised physics mode; it does not match the reference).  Takes
 // cos(theta).
-__device__ __forceinline__ void peturb(float& vx, float& vy, float& vz, float cos_theta, float phi, bool normalize = false)
+template <class Real>
+__device__ __forceinline__ void peturb(Real& vx, Real& vy, Real& vz, Real cos_theta, Real phi, bool normalize = false)
 {
-    const float ax = fabsf(vx), ay = fabsf(vy), az = fabsf(vz);
+    const Real ax = m_abs(vx), ay = m_abs(vy), az = m_abs(vz);
     const int k = ax <= ay ? (ax <= az ? 0 : 2) : (ay <= az ? 1 : 2);
     // cross(vec, e_k)
-    float ux, uy, uz;
+    Real ux, uy, uz;
     if (k == 0) {
-        ux = 0.0f;
+        ux = Real(0);
         uy = vz;
         uz = -vy;
     } else if (k == 1) {
         ux = -vz;
-        uy = 0.0f;
+        uy = Real(0);
         uz = vx;
     } else {
         ux = vy;
         uy = -vx;
-        uz = 0.0f;
+        uz = Real(0);
     }
     if (normalize) {
-        const float inv = rsqrtf(ux * ux + uy * uy + uz * uz);
+        const Real inv = m_rsqrt(ux * ux + uy * uy + uz * uz);
         ux *= inv;
         uy *= inv;
         uz *= inv;
     }
     rotate(ux, uy, uz, vx, vy, vz, phi);
-    const float st = sqrtf(fmaxf(0.0f, 1.0f - cos_theta * cos_theta));
+    const Real st = m_sqrt(m_max(Real(0), Real(1) - cos_theta * cos_theta));
     vx = vx * cos_theta + ux * st;
     vy = vy * cos_theta + uy * st;
     vz = vz * cos_theta + uz * st;
@@ -218,7 +274,8 @@ __device__ __forceinline__ void peturb(float& vx, float& vy, float& vz, float co
 // LUT lookups (attenuationinterpolator.hpp:207-248, attenuationlut.hpp:124-204,
 // interpolation.hpp:169-176, dxmcrandom.hpp:483-500)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int upper_bound_f(const float* x, int n, float v)
+template <class Real>
+__device__ __forceinline__ int upper_bound_f(const float* x, int n, Real v)
 {
     int lo = 0, count = n;
     while (count > 0) {
@@ -233,7 +290,8 @@ __device__ __forceinline__ int upper_bound_f(const float* x, int n, float v)
     return lo;
 }
 
-__device__ __forceinline__ int lut_segment(const float* L, const LutMeta& m, float logE)
+template <class Real>
+__device__ __forceinline__ int lut_segment(const float* L, const LutMeta& m, Real logE)
 {
     if (logE > m.linear_energy) {
         const int idx = static_cast<int>((logE - m.linear_energy) * m.inv_linear_step) + m.linear_index;
@@ -243,19 +301,21 @@ __device__ __forceinline__ int lut_segment(const float* L, const LutMeta& m, flo
     return pos < m.R ? pos : m.R - 1;
 }
 
-__device__ __forceinline__ void lut_attenuation(const float* L, const LutMeta& m, int material, float logE, int seg, float& photo, float& compt, float& rayl)
+template <class Real>
+__device__ __forceinline__ void lut_attenuation(const float* L, const LutMeta& m, int material, Real logE, int seg, Real& photo, Real& compt, Real& rayl)
 {
     const float2* c = reinterpret_cast<const float2*>(L + m.off_coef + (material * m.R + seg) * 6);
     const float2 p = c[0], q = c[1], r = c[2];
-    photo = exp10_fast(fmaf(p.y, logE, p.x));
-    compt = exp10_fast(fmaf(q.y, logE, q.x));
-    rayl = exp10_fast(fmaf(r.y, logE, r.x));
+    photo = m_exp10(m_fma(Real(p.y), logE, Real(p.x)));
+    compt = m_exp10(m_fma(Real(q.y), logE, Real(q.x)));
+    rayl = m_exp10(m_fma(Real(r.y), logE, Real(r.x)));
 }
 
-__device__ __forceinline__ float lut_max_inverse(const float* L, const LutMeta& m, float logE, int seg)
+template <class Real>
+__device__ __forceinline__ Real lut_max_inverse(const float* L, const LutMeta& m, Real logE, int seg)
 {
     const float2 c = reinterpret_cast<const float2*>(L + m.off_maxcoef)[seg];
-    return exp10_fast(fmaf(c.y, logE, c.x));
+    return m_exp10(m_fma(Real(c.y), logE, Real(c.x)));
 }
 
 } // namespace dxmc_gb300::dev

@@ -131,6 +131,8 @@ struct TransportParams {
     int interact_threshold; // run the interaction passes once at least this many lanes wait (1..32)
     int woodcock_burst;     // Woodcock steps a lane may take per loop iteration (1..64)
     int normalize_direction; // 1: unit scattering axis in peturb (normalised physics), 0: the reference's
+    int precision;          // 0: FP32 transport; 1: FP64 everywhere (position, direction, energy, LUT, sampling)
+    int pad_precision;
     MajorantGrid majorant;
 };
 
@@ -171,7 +173,7 @@ cudaError_t launch_transport(const TransportParams& p, int model, int grid, int 
 // (CUDA loads modules lazily, on first use, and a load allocates device memory).
 cudaError_t preload_transport_kernels();
 // blocks per SM for this configuration; also raises the kernel's dynamic shared-memory limit
-int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem);
+int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem, int precision = 0);
 // dynamic shared memory the transport kernel needs for a LUT image of lut_bytes
 size_t transport_smem_bytes(size_t lut_bytes, bool lut_in_smem, bool palette);
 // Post-processing of the tallies into dose / variance (densities from the world's layout).

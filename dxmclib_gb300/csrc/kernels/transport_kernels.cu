@@ -21,11 +21,12 @@ namespace {
     constexpr int WARP_POOL_CHUNK = 256; // histories fetched per queue access
     constexpr uint32_t MAX_STEPS_PER_HISTORY = 1u << 20; // guard against unbounded histories
 
-    struct Photon {
-        float px, py, pz;
-        float dx, dy, dz;
-        float energy;
-        float weight;
+    template <class Real>
+    struct PhotonT {
+        Real px, py, pz;
+        Real dx, dy, dz;
+        Real energy;
+        Real weight;
     };
 
     // ---- scoring (transport.hpp:208-214, 598-609) ------------------------------
@@ -57,7 +58,8 @@ namespace {
         red_add_evict_first(&r->events, n);
     }
 
-    __device__ __forceinline__ void score(const TransportParams& p, uint64_t idx, float e)
+    template <class Real>
+    __device__ __forceinline__ void score(const TransportParams& p, uint64_t idx, Real e)
     {
         if (p.records) {
             const double ed = static_cast<double>(e);
@@ -80,17 +82,18 @@ namespace {
     // Warp-aggregated scoring: lanes depositing into the same voxel in the same
     // iteration are combined by __match_any_sync and one leader issues the
     // atomics (FP32 partial sums flushed to the FP64 accumulators).
-    __device__ __forceinline__ void score_aggregated(const TransportParams& p, unsigned active, uint64_t idx, float e)
+    template <class Real>
+    __device__ __forceinline__ void score_aggregated(const TransportParams& p, unsigned active, uint64_t idx, Real e)
     {
         const unsigned peers = __match_any_sync(active, idx);
         const int leader = __ffs(peers) - 1;
         const int lane = threadIdx.x & 31;
-        float sum = 0.0f, sum2 = 0.0f;
+        Real sum = Real(0.0), sum2 = Real(0.0);
         unsigned count = 0;
         // each peer group reduces over its members (group sizes are small)
         for (unsigned m = peers; m; m &= m - 1) {
             const int src = __ffs(m) - 1;
-            const float v = __shfl_sync(peers, e, src);
+            const Real v = __shfl_sync(peers, e, src);
             sum += v;
             sum2 += v * v;
             ++count;
@@ -108,44 +111,44 @@ namespace {
     }
 
     // ---- photoelectric (transport.hpp:216-263) ---------------------------------
-    template <int MODEL>
-    __device__ __forceinline__ float photo_absorption(const float* L, const LutMeta& m, Photon& ph, int material, Rng& rng, bool norm = false)
+    template <int MODEL, class Real>
+    __device__ __forceinline__ Real photo_absorption(const float* L, const LutMeta& m, PhotonT<Real>& ph, int material, Rng& rng, bool norm = false)
     {
-        const float E = ph.energy;
-        ph.energy = 0.0f;
+        const Real E = ph.energy;
+        ph.energy = Real(0.0);
         if constexpr (MODEL < 2) {
             return E;
         } else {
             const float* shells = L + m.off_shells + material * N_SHELLS * SHELL_FLOATS;
-            float total = 0.0f;
+            Real total = Real(0.0);
 #pragma unroll
             for (int s = 0; s < N_SHELLS; ++s)
-                total += E > shells[s * SHELL_FLOATS] ? shells[s * SHELL_FLOATS + 3] : 0.0f;
-            const float sample = total * rng.uniform();
-            float cum = 0.0f;
+                total += E > shells[s * SHELL_FLOATS] ? shells[s * SHELL_FLOATS + 3] : Real(0.0);
+            const Real sample = total * static_cast<Real>(rng.uniform());
+            Real cum = Real(0.0);
             int idx = 0;
             for (int s = 0; s < N_SHELLS; ++s) {
-                cum += E > shells[s * SHELL_FLOATS] ? shells[s * SHELL_FLOATS + 3] : 0.0f;
+                cum += E > shells[s * SHELL_FLOATS] ? shells[s * SHELL_FLOATS + 3] : Real(0.0);
                 idx = s;
                 if (!(cum < sample) || s == N_SHELLS - 1)
                     break;
             }
             const float* sh = shells + idx * SHELL_FLOATS;
-            const float binding = sh[0];
-            if (binding > E || binding < ENERGY_CUTOFF)
+            const Real binding = sh[0];
+            if (binding > E || binding < Real(ENERGY_CUTOFF_D))
                 return E;
-            const float r1 = rng.uniform();
+            const Real r1 = static_cast<Real>(rng.uniform());
             if (r1 <= sh[4]) {
                 int line = 0;
-                float r3 = rng.uniform() - sh[5];
-                while (r3 > 0.0f && line < 2) {
+                Real r3 = static_cast<Real>(rng.uniform()) - sh[5];
+                while (r3 > Real(0.0) && line < 2) {
                     ++line;
                     r3 -= sh[5 + line];
                 }
                 ph.energy = sh[8 + line];
-                const float theta = rng.uniform() * PI_F;
-                const float phi = rng.azimuth();
-                peturb(ph.dx, ph.dy, ph.dz, cosf(theta), phi, norm);
+                const Real theta = static_cast<Real>(rng.uniform()) * Real(PI_D);
+                const Real phi = rng_azimuth<Real>(rng);
+                peturb(ph.dx, ph.dy, ph.dz, m_cos(theta), phi, norm);
                 return E - ph.energy;
             }
             return E;
@@ -153,18 +156,18 @@ namespace {
     }
 
     // ---- Rayleigh (transport.hpp:264-298) ---------------------------------------
-    template <int MODEL>
-    __device__ __forceinline__ bool rayleigh_scatter(const float* L, const float* G, const LutMeta& m, Photon& ph, int material, Rng& rng, bool norm = false)
+    template <int MODEL, class Real>
+    __device__ __forceinline__ bool rayleigh_scatter(const float* L, const float* G, const LutMeta& m, PhotonT<Real>& ph, int material, Rng& rng, bool norm = false)
     {
         if constexpr (MODEL == 0) {
-            constexpr float extreme = 1.08866210790363f; // 4 sqrt(2) / (3 sqrt(3))
+            constexpr Real extreme = Real(1.08866210790363); // 4 sqrt(2) / (3 sqrt(3))
             for (int it = 0; it < REJECTION_CAP; ++it) {
-                const float r1 = rng.uniform() * extreme;
-                const float theta = rng.uniform() * PI_F;
-                float s, c;
-                sincosf(theta, &s, &c);
-                if (!(r1 > (2.0f - s * s) * s)) {
-                    const float phi = rng.azimuth();
+                const Real r1 = static_cast<Real>(rng.uniform()) * extreme;
+                const Real theta = static_cast<Real>(rng.uniform()) * Real(PI_D);
+                Real s, c;
+                m_sincos(theta, &s, &c);
+                if (!(r1 > (Real(2.0) - s * s) * s)) {
+                    const Real phi = rng_azimuth<Real>(rng);
                     peturb(ph.dx, ph.dy, ph.dz, c, phi, norm);
                     return true;
                 }
@@ -173,156 +176,157 @@ namespace {
         } else {
             // the density of the reference's RITA draw of q^2 <= q_max^2 followed by the
             // (1 + cos^2) / 2 rejection, drawn by inverse CDF: no loop, no divergence
-            float fe;
+            Real fe;
             const int row = table_row(m, ph.energy, fe);
-            const float y = table_quantile(G + m.off_ray + (material * m.tab_ne + row) * (m.tab_nu + 1), m.tab_nu, rng.uniform(), fe);
-            const float cosA = 1.0f - 2.0f * y; // q^2 / q_max^2 = (1 - cos) / 2
-            const float phi = rng.azimuth();
+            const Real y = table_quantile(G + m.off_ray + (material * m.tab_ne + row) * (m.tab_nu + 1), m.tab_nu, static_cast<Real>(rng.uniform()), fe);
+            const Real cosA = Real(1.0) - Real(2.0) * y; // q^2 / q_max^2 = (1 - cos) / 2
+            const Real phi = rng_azimuth<Real>(rng);
             peturb(ph.dx, ph.dy, ph.dz, cosA, phi, norm);
             return true;
         }
     }
 
     // ---- Compton, impulse approximation (transport.hpp:342-483) -----------------
-    __device__ __forceinline__ bool compton_ia(const float* L, const LutMeta& m, Photon& ph, int material, Rng& rng, float& deposit, bool norm = false)
+    template <class Real>
+    __device__ __forceinline__ bool compton_ia(const float* L, const LutMeta& m, PhotonT<Real>& ph, int material, Rng& rng, Real& deposit, bool norm = false)
     {
         const float* shells = L + m.off_shells + material * N_SHELLS * SHELL_FLOATS;
-        float total = 0.0f;
+        Real total = Real(0.0);
 #pragma unroll
         for (int s = 0; s < N_SHELLS; ++s)
-            total += (shells[s * SHELL_FLOATS] < ph.energy && shells[s * SHELL_FLOATS + 2] > 0.0f) ? shells[s * SHELL_FLOATS + 1] : 0.0f;
-        const float sample = total * rng.uniform();
-        float cum = 0.0f;
+            total += (shells[s * SHELL_FLOATS] < ph.energy && shells[s * SHELL_FLOATS + 2] > Real(0.0)) ? shells[s * SHELL_FLOATS + 1] : Real(0.0);
+        const Real sample = total * static_cast<Real>(rng.uniform());
+        Real cum = Real(0.0);
         int shell = 0;
         for (int s = 0; s < N_SHELLS; ++s) {
-            cum += (shells[s * SHELL_FLOATS] < ph.energy && shells[s * SHELL_FLOATS + 2] > 0.0f) ? shells[s * SHELL_FLOATS + 1] : 0.0f;
+            cum += (shells[s * SHELL_FLOATS] < ph.energy && shells[s * SHELL_FLOATS + 2] > Real(0.0)) ? shells[s * SHELL_FLOATS + 1] : Real(0.0);
             shell = s;
             if (!(cum < sample) || s == N_SHELLS - 1)
                 break;
         }
-        if (!(total > 0.0f)) {
-            deposit = 0.0f; // no shell can take part: the interaction is rejected
+        if (!(total > Real(0.0))) {
+            deposit = Real(0.0); // no shell can take part: the interaction is rejected
             return true;
         }
         const float* sh = shells + shell * SHELL_FLOATS;
-        const float U = sh[0] / ELECTRON_REST_MASS;
-        const float pU = sqrtf(2.0f * U + U * U);
-        const float J0 = sh[2];
-        const float k = ph.energy / ELECTRON_REST_MASS;
+        const Real U = sh[0] / Real(ELECTRON_REST_MASS_D);
+        const Real pU = m_sqrt(Real(2.0) * U + U * U);
+        const Real J0 = sh[2];
+        const Real k = ph.energy / Real(ELECTRON_REST_MASS_D);
         if (U > k) {
-            deposit = 0.0f; // interaction rejected (corrects the cross section)
+            deposit = Real(0.0); // interaction rejected (corrects the cross section)
             return true;
         }
-        const float emin = 1.0f / (1.0f + 2.0f * k);
-        const float gmax_inv = 1.0f / (1.0f / emin + emin);
-        constexpr float sp2 = 2.50662827463100f; // 1 / (1/sqrt(pi) / sqrt(2)) = sqrt(2 pi)
-        constexpr float a1 = 0.34802f, a2 = -0.0958798f, a3 = 0.7478556f;
-        const float sqrte = 1.64872127070013f;
-        float e = 1.0f, cosA = 1.0f;
+        const Real emin = Real(1.0) / (Real(1.0) + Real(2.0) * k);
+        const Real gmax_inv = Real(1.0) / (Real(1.0) / emin + emin);
+        constexpr Real sp2 = Real(2.50662827463100); // 1 / (1/sqrt(pi) / sqrt(2)) = sqrt(2 pi)
+        constexpr Real a1 = Real(0.34802), a2 = -Real(0.0958798), a3 = Real(0.7478556);
+        const Real sqrte = Real(1.64872127070013);
+        Real e = Real(1.0), cosA = Real(1.0);
         bool accepted = false;
         for (int it = 0; it < REJECTION_CAP && !accepted; ++it) {
-            const float r1 = rng.uniform();
+            const Real r1 = static_cast<Real>(rng.uniform());
             // e = r1 + (1 - r1) emin, with 1 - e = (1 - r1)(1 - emin) formed directly so
             // that t stays positive when e rounds to 1 in single precision
-            const float one_minus_e = (1.0f - r1) * (1.0f - emin);
-            e = 1.0f - one_minus_e;
-            const float t = one_minus_e / (k * e);
-            const float sin2 = t * (2.0f - t);
-            cosA = 1.0f - t;
-            const float g = (1.0f / e + e - sin2) * gmax_inv;
-            const float r2 = rng.uniform();
+            const Real one_minus_e = (Real(1.0) - r1) * (Real(1.0) - emin);
+            e = Real(1.0) - one_minus_e;
+            const Real t = one_minus_e / (k * e);
+            const Real sin2 = t * (Real(2.0) - t);
+            cosA = Real(1.0) - t;
+            const Real g = (Real(1.0) / e + e - sin2) * gmax_inv;
+            const Real r2 = static_cast<Real>(rng.uniform());
             if (r2 > g)
                 continue;
-            const float pi = (k * (k - U) * t - U) / sqrtf(fmaxf(2.0f * k * (k - U) * t + U * U, 1e-30f));
-            const float kc = k * e;
-            const float qc = sqrtf(fmaxf(k * k + kc * kc - 2.0f * k * kc * cosA, 1e-30f));
-            const float alpha = qc * (1.0f + kc * (kc - k * cosA) / (qc * qc)) / k;
-            const float b_part = 1.0f + 2.0f * J0 * fabsf(pi);
-            const float b = (b_part * b_part + 1.0f) * 0.5f;
-            const float expb = expf(-b);
-            float S;
+            const Real pi = (k * (k - U) * t - U) / m_sqrt(m_max(Real(2.0) * k * (k - U) * t + U * U, Real(1e-30)));
+            const Real kc = k * e;
+            const Real qc = m_sqrt(m_max(k * k + kc * kc - Real(2.0) * k * kc * cosA, Real(1e-30)));
+            const Real alpha = qc * (Real(1.0) + kc * (kc - k * cosA) / (qc * qc)) / k;
+            const Real b_part = Real(1.0) + Real(2.0) * J0 * m_abs(pi);
+            const Real b = (b_part * b_part + Real(1.0)) * Real(0.5);
+            const Real expb = m_exp(-b);
+            Real S;
             if (pi <= -pU) {
-                S = (1.0f - alpha * pU) * expb * 0.5f;
+                S = (Real(1.0) - alpha * pU) * expb * Real(0.5);
             } else if (pi < pU) {
-                const float part1 = alpha * sp2 / (4.0f * J0);
-                const float tp = 1.0f / (1.0f + 0.332673f * (1.0f + 2.0f * J0 * fabsf(pU)));
-                const float tpi = 1.0f / (1.0f + 0.332673f * (1.0f + 2.0f * J0 * fabsf(pi)));
-                const float part2p = sqrte - expb * tp * (a1 + a2 * tp + a3 * tp * tp);
-                const float part2pi = sqrte - expb * tpi * (a1 + a2 * tpi + a3 * tpi * tpi);
-                if (pi <= 0.0f)
-                    S = (1.0f - alpha * pi) * expb * 0.5f - part1 * (part2p - part2pi);
+                const Real part1 = alpha * sp2 / (Real(4.0) * J0);
+                const Real tp = Real(1.0) / (Real(1.0) + Real(0.332673) * (Real(1.0) + Real(2.0) * J0 * m_abs(pU)));
+                const Real tpi = Real(1.0) / (Real(1.0) + Real(0.332673) * (Real(1.0) + Real(2.0) * J0 * m_abs(pi)));
+                const Real part2p = sqrte - expb * tp * (a1 + a2 * tp + a3 * tp * tp);
+                const Real part2pi = sqrte - expb * tpi * (a1 + a2 * tpi + a3 * tpi * tpi);
+                if (pi <= Real(0.0))
+                    S = (Real(1.0) - alpha * pi) * expb * Real(0.5) - part1 * (part2p - part2pi);
                 else
-                    S = 1.0f - (1.0f - alpha * pi) * expb * 0.5f - part1 * (part2p - part2pi);
+                    S = Real(1.0) - (Real(1.0) - alpha * pi) * expb * Real(0.5) - part1 * (part2p - part2pi);
             } else {
-                S = 1.0f - (1.0f - alpha * pU) * expb * 0.5f;
+                S = Real(1.0) - (Real(1.0) - alpha * pU) * expb * Real(0.5);
             }
-            const float r3 = rng.uniform();
+            const Real r3 = static_cast<Real>(rng.uniform());
             if (r3 > S)
                 continue;
-            float Fmax;
+            Real Fmax;
             if (pi <= -pU)
-                Fmax = 1.0f - alpha * pU;
+                Fmax = Real(1.0) - alpha * pU;
             else if (pi >= pU)
-                Fmax = 1.0f + alpha * pU;
+                Fmax = Real(1.0) + alpha * pU;
             else
-                Fmax = 1.0f + alpha * pi;
-            const float r4 = rng.uniform_open(); // log(rbar2) below needs rbar2 > 0
-            const float rbar2 = 2.0f * r4 * expb;
-            float pz;
-            if (rbar2 < 1.0f) {
-                const float part = sqrtf(1.0f - 2.0f * logf(rbar2));
-                pz = (1.0f - part) / (2.0f * J0) / ELECTRON_REST_MASS;
+                Fmax = Real(1.0) + alpha * pi;
+            const Real r4 = static_cast<Real>(rng.uniform_open()); // log(rbar2) below needs rbar2 > 0
+            const Real rbar2 = Real(2.0) * r4 * expb;
+            Real pz;
+            if (rbar2 < Real(1.0)) {
+                const Real part = m_sqrt(Real(1.0) - Real(2.0) * m_log(rbar2));
+                pz = (Real(1.0) - part) / (Real(2.0) * J0) / Real(ELECTRON_REST_MASS_D);
             } else {
-                const float part = sqrtf(1.0f - 2.0f * logf(2.0f - rbar2));
-                pz = (part - 1.0f) / (2.0f * J0) / ELECTRON_REST_MASS;
+                const Real part = m_sqrt(Real(1.0) - Real(2.0) * m_log(Real(2.0) - rbar2));
+                pz = (part - Real(1.0)) / (Real(2.0) * J0) / Real(ELECTRON_REST_MASS_D);
             }
-            float Fpz;
+            Real Fpz;
             if (pz <= -pU)
-                Fpz = 1.0f - alpha * pU;
+                Fpz = Real(1.0) - alpha * pU;
             else if (pz >= pU)
-                Fpz = 1.0f + alpha * pU;
+                Fpz = Real(1.0) + alpha * pU;
             else
-                Fpz = 1.0f + alpha * pz;
-            const float r5 = rng.uniform();
+                Fpz = Real(1.0) + alpha * pz;
+            const Real r5 = static_cast<Real>(rng.uniform());
             if (r5 > Fpz / Fmax)
                 continue;
-            const float part = sqrtf(fmaxf(1.0f - 2.0f * e * cosA + e * e * (1.0f - pz * pz * sin2), 0.0f));
-            const float kbar = kc / (1.0f - pz * pz * e * e) * (1.0f - pz * pz * e * cosA + pz * part);
+            const Real part = m_sqrt(m_max(Real(1.0) - Real(2.0) * e * cosA + e * e * (Real(1.0) - pz * pz * sin2), Real(0.0)));
+            const Real kbar = kc / (Real(1.0) - pz * pz * e * e) * (Real(1.0) - pz * pz * e * cosA + pz * part);
             e = kbar / k;
             accepted = true;
         }
         if (!accepted)
             return false;
-        const float phi = rng.azimuth();
+        const Real phi = rng_azimuth<Real>(rng);
         peturb(ph.dx, ph.dy, ph.dz, cosA, phi, norm);
-        const float E = ph.energy;
+        const Real E = ph.energy;
         ph.energy *= e;
         deposit = E - ph.energy;
         return true;
     }
 
     // ---- Compton, Klein-Nishina with optional scatter factor (transport.hpp:300-340)
-    template <int MODEL>
-    __device__ __forceinline__ bool compton_scatter(const float* L, const float* G, const LutMeta& m, Photon& ph, int material, Rng& rng, float& deposit, bool norm = false)
+    template <int MODEL, class Real>
+    __device__ __forceinline__ bool compton_scatter(const float* L, const float* G, const LutMeta& m, PhotonT<Real>& ph, int material, Rng& rng, Real& deposit, bool norm = false)
     {
         if constexpr (MODEL == 2) {
             return compton_ia(L, m, ph, material, rng, deposit, norm);
         } else {
             // the density of the reference's Klein-Nishina rejection (times the scatter
             // factor S(q) for LIVERMORE), drawn by inverse CDF: no loop, no divergence
-            const float E = ph.energy;
-            const float k = E / ELECTRON_REST_MASS;
-            const float emin = 1.0f / (1.0f + 2.0f * k);
-            float fe;
+            const Real E = ph.energy;
+            const Real k = E / Real(ELECTRON_REST_MASS_D);
+            const Real emin = Real(1.0) / (Real(1.0) + Real(2.0) * k);
+            Real fe;
             const int row = table_row(m, E, fe);
             const float* tab = MODEL == 1 ? G + m.off_csf + (material * m.tab_ne + row) * (m.tab_nu + 1)
                                           : G + m.off_ckn + row * (m.tab_nu + 1);
-            const float x = table_quantile(tab, m.tab_nu, rng.uniform(), fe); // (e - e_min) / (1 - e_min)
-            const float one_minus_e = (1.0f - x) * (1.0f - emin);
-            const float e = 1.0f - one_minus_e;
-            const float cosA = 1.0f - one_minus_e / (k * e);
-            const float phi = rng.azimuth();
-            peturb(ph.dx, ph.dy, ph.dz, fmaxf(cosA, -1.0f), phi, norm);
+            const Real x = table_quantile(tab, m.tab_nu, static_cast<Real>(rng.uniform()), fe); // (e - e_min) / (1 - e_min)
+            const Real one_minus_e = (Real(1.0) - x) * (Real(1.0) - emin);
+            const Real e = Real(1.0) - one_minus_e;
+            const Real cosA = Real(1.0) - one_minus_e / (k * e);
+            const Real phi = rng_azimuth<Real>(rng);
+            peturb(ph.dx, ph.dy, ph.dz, m_max(cosA, -Real(1.0)), phi, norm);
             ph.energy = E * e;
             deposit = E - ph.energy;
             return true;
@@ -330,10 +334,11 @@ namespace {
     }
 
     // ---- photon generation: Exposure::sampleParticle (exposure.hpp:280-304) -----
-    __device__ __forceinline__ void sample_particle(const SourceParams& s, const DevExposure& ex, Rng& rng, Photon& ph)
+    template <class Real>
+    __device__ __forceinline__ void sample_particle(const SourceParams& s, const DevExposure& ex, Rng& rng, PhotonT<Real>& ph)
     {
-        const float theta = ex.coll[0] + rng.uniform() * (ex.coll[1] - ex.coll[0]);
-        const float phi = ex.coll[2] + rng.uniform() * (ex.coll[3] - ex.coll[2]);
+        const Real theta = ex.coll[0] + static_cast<Real>(rng.uniform()) * (ex.coll[1] - ex.coll[0]);
+        const Real phi = ex.coll[2] + static_cast<Real>(rng.uniform()) * (ex.coll[3] - ex.coll[2]);
         ph.px = ex.pos[0];
         ph.py = ex.pos[1];
         ph.pz = ex.pos[2];
@@ -341,16 +346,16 @@ namespace {
         ph.dy = ex.beam[1];
         ph.dz = ex.beam[2];
         ph.weight = ex.weight;
-        rotate(ph.dx, ph.dy, ph.dz, ex.cosy[0], ex.cosy[1], ex.cosy[2], theta);
-        rotate(ph.dx, ph.dy, ph.dz, ex.cosx[0], ex.cosx[1], ex.cosx[2], phi);
+        rotate(ph.dx, ph.dy, ph.dz, Real(ex.cosy[0]), Real(ex.cosy[1]), Real(ex.cosy[2]), theta);
+        rotate(ph.dx, ph.dy, ph.dz, Real(ex.cosx[0]), Real(ex.cosx[1]), Real(ex.cosx[2]), phi);
         if (s.spec_n > 0) {
             // SpecterDistribution::sampleValue (dxmcrandom.hpp:322-326)
-            const float r = rng.uniform();
+            const Real r = static_cast<Real>(rng.uniform());
             const uint32_t k = rng.below(static_cast<uint32_t>(s.spec_n));
             const uint32_t idx = r < __ldg(s.spec_prob + k) ? k : __ldg(s.spec_alias + k);
             if (idx + 1 < static_cast<uint32_t>(s.spec_n)) {
-                const float e0 = __ldg(s.spec_energy + idx), e1 = __ldg(s.spec_energy + idx + 1);
-                ph.energy = e0 + rng.uniform() * (e1 - e0);
+                const Real e0 = __ldg(s.spec_energy + idx), e1 = __ldg(s.spec_energy + idx + 1);
+                ph.energy = e0 + static_cast<Real>(rng.uniform()) * (e1 - e0);
             } else {
                 ph.energy = __ldg(s.spec_energy + idx);
             }
@@ -359,7 +364,7 @@ namespace {
         }
         if (s.bowtie_angle) {
             // BowTieFilter::sampleIntensityWeight (beamfilters.hpp:150-190)
-            const float angle = fabsf(theta);
+            const Real angle = m_abs(theta);
             int first = 0, last = s.bowtie_n - 1;
             int it = first + (last - first) / 2;
             while (it != first) {
@@ -371,22 +376,22 @@ namespace {
                 }
                 it += (last - first) / 2;
             }
-            float w;
+            Real w;
             if (angle < __ldg(s.bowtie_angle + first))
                 w = __ldg(s.bowtie_weight);
             else if (angle > __ldg(s.bowtie_angle + last))
                 w = __ldg(s.bowtie_weight + s.bowtie_n - 1);
             else {
-                const float x0 = __ldg(s.bowtie_angle + first), x1 = __ldg(s.bowtie_angle + last);
-                const float y0 = __ldg(s.bowtie_weight + first), y1 = __ldg(s.bowtie_weight + last);
+                const Real x0 = __ldg(s.bowtie_angle + first), x1 = __ldg(s.bowtie_angle + last);
+                const Real y0 = __ldg(s.bowtie_weight + first), y1 = __ldg(s.bowtie_weight + last);
                 w = y0 + (angle - x0) * (y1 - y0) / (x1 - x0);
             }
             ph.weight *= w;
         }
         if (s.heel_weights) {
             // HeelFilter::sampleIntensityWeight (beamfilters.hpp:514-538)
-            const float energy = ph.energy;
-            int e_index = static_cast<int>((energy - s.heel_e_start + 0.5f * s.heel_e_step) / s.heel_e_step);
+            const Real energy = ph.energy;
+            int e_index = static_cast<int>((energy - s.heel_e_start + Real(0.5) * s.heel_e_step) / s.heel_e_step);
             if (e_index >= s.heel_e_size || e_index < 0)
                 e_index = e_index < 0 ? 0 : s.heel_e_size - 1;
             if (energy < s.heel_e_start)
@@ -397,11 +402,11 @@ namespace {
             if (phi < s.heel_a_start)
                 a_index = 0;
             const int w_index = e_index * s.heel_a_size + a_index;
-            float w;
+            Real w;
             if (a_index < s.heel_a_size - 1) {
-                const float a0 = s.heel_a_start + s.heel_a_step * a_index;
-                const float a1 = s.heel_a_start + s.heel_a_step * (a_index + 1);
-                const float w0 = __ldg(s.heel_weights + w_index), w1 = __ldg(s.heel_weights + w_index + 1);
+                const Real a0 = s.heel_a_start + s.heel_a_step * a_index;
+                const Real a1 = s.heel_a_start + s.heel_a_step * (a_index + 1);
+                const Real w0 = __ldg(s.heel_weights + w_index), w1 = __ldg(s.heel_weights + w_index + 1);
                 w = w0 + (w1 - w0) * (phi - a0) / (a1 - a0);
             } else {
                 w = __ldg(s.heel_weights + w_index);
@@ -410,30 +415,32 @@ namespace {
         }
     }
 
-    __device__ __forceinline__ bool inside(const WorldParams& w, float x, float y, float z)
+    template <class Real>
+    __device__ __forceinline__ bool inside(const WorldParams& w, Real x, Real y, Real z)
     {
         return (x > w.lo[0] && x < w.hi[0]) && (y > w.lo[1] && y < w.hi[1]) && (z > w.lo[2] && z < w.hi[2]);
     }
 
     // transportParticleToWorld (transport.hpp:702-728)
-    __device__ __forceinline__ bool transport_to_world(const WorldParams& w, Photon& ph)
+    template <class Real>
+    __device__ __forceinline__ bool transport_to_world(const WorldParams& w, PhotonT<Real>& ph)
     {
         if (inside(w, ph.px, ph.py, ph.pz))
             return true;
-        float amin = -3.402823466e38f, amax = 3.402823466e38f;
-        const float pos[3] = { ph.px, ph.py, ph.pz };
-        const float dir[3] = { ph.dx, ph.dy, ph.dz };
+        Real amin = -Real(3.402823466e38), amax = Real(3.402823466e38);
+        const Real pos[3] = { ph.px, ph.py, ph.pz };
+        const Real dir[3] = { ph.dx, ph.dy, ph.dz };
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            if (fabsf(dir[i]) > N_ERROR) {
-                const float inv = 1.0f / dir[i];
-                const float a0 = (w.lo[i] - pos[i]) * inv;
-                const float an = (w.hi[i] - pos[i]) * inv;
-                amin = fmaxf(amin, fminf(a0, an));
-                amax = fminf(amax, fmaxf(a0, an));
+            if (m_abs(dir[i]) > Real(N_ERROR_D)) {
+                const Real inv = Real(1.0) / dir[i];
+                const Real a0 = (w.lo[i] - pos[i]) * inv;
+                const Real an = (w.hi[i] - pos[i]) * inv;
+                amin = m_max(amin, m_min(a0, an));
+                amax = m_min(amax, m_max(a0, an));
             }
         }
-        if (amin < amax && amin > 0.0f) {
+        if (amin < amax && amin > Real(0.0)) {
             ph.px += amin * ph.dx;
             ph.py += amin * ph.dy;
             ph.pz += amin * ph.dz;
@@ -476,8 +483,8 @@ namespace {
     // many lanes active instead of one or two.
     enum : int { EV_NONE = 0, EV_PHOTO = 1, EV_COMPTON = 2, EV_RAYLEIGH = 3 };
 
-    template <bool PALETTE>
-    __device__ __forceinline__ void gather_voxel(const WorldParams& w, const PaletteEntry* pal, uint64_t vidx, float& density, int& mat, bool& measured)
+    template <bool PALETTE, class Real>
+    __device__ __forceinline__ void gather_voxel(const WorldParams& w, const PaletteEntry* pal, uint64_t vidx, Real& density, int& mat, bool& measured)
     {
         if constexpr (PALETTE) {
             const PaletteEntry e = pal[__ldg(w.palette_index + vidx)];
@@ -509,22 +516,23 @@ namespace {
         unsigned long long steps, deposits, overflows, histories;
     };
 
-    struct Lane {
-        Photon ph;
+    template <class Real>
+    struct LaneT {
+        PhotonT<Real> ph;
         Rng rng;
         bool alive;
         int pending;
-        float stepK, logE; // Woodcock step = -log2(u) * stepK (mm): 10 * ln 2 / majorant
+        Real stepK, logE; // Woodcock step = -log2(u) * stepK (mm): 10 * ln 2 / majorant
         int seg;
         bool updateMax;
         int cached_mat;
         uint32_t hist_steps;
-        float probInv;  // attenuation of the current material / majorant (event probability per unit density)
-        float p0, p01;  // photoelectric and photoelectric + Compton shares of the attenuation
+        Real probInv;  // attenuation of the current material / majorant (event probability per unit density)
+        Real p0, p01;  // photoelectric and photoelectric + Compton shares of the attenuation
         uint64_t vidx;
-        float forced_wc; // weight correction waiting for a forced-voxel interaction pass
+        Real forced_wc; // weight correction waiting for a forced-voxel interaction pass
         bool armed;      // energy x weight is below the Russian-roulette threshold
-        float cinv, cR;  // local majorant: 1 / scale and the flight length it holds for (MajorantGrid)
+        Real cinv, cR;  // local majorant: 1 / scale and the flight length it holds for (MajorantGrid)
         int band;        // energy band of the local-majorant grid
 
         __device__ void start_photon()
@@ -533,30 +541,31 @@ namespace {
             updateMax = true;
             cached_mat = -1;
             hist_steps = 0;
-            forced_wc = 0.0f;
-            cinv = 1.0f; // the first flight from the grid boundary uses the global majorant
+            forced_wc = Real(0.0);
+            cinv = Real(1.0); // the first flight from the grid boundary uses the global majorant
             cR = INFINITY;
             arm();
         }
         // energy and weight change only at interactions and roulette: the roulette
         // test of a virtual step reads this flag
-        __device__ void arm() { armed = ph.energy * ph.weight < ROULETTE_THRESHOLD; }
+        __device__ void arm() { armed = ph.energy * ph.weight < Real(ROULETTE_THRESHOLD_D); }
     };
 
     // Local majorant of the photon's cell for its energy band, after the energy
     // changed (a new photon, or an interaction): the flight drawn next must be
     // bounded for the new energy.  A new photon sits on the grid boundary, so the
     // coordinates are clamped onto the grid.
-    __device__ __forceinline__ void fetch_cell(Lane& s, const TransportParams& p)
+    template <class Real>
+    __device__ __forceinline__ void fetch_cell(LaneT<Real>& s, const TransportParams& p)
     {
         const MajorantGrid& g = p.majorant;
         const WorldParams& w = p.world;
         // s.logE = log10 E was just computed; the band intervals of the bounds are
         // widened by 0.1 % on the host, which covers the rounding here
-        s.band = min(max(__float2int_rd((s.logE - g.band_log0) * g.band_inv_dlog), 0), g.bands - 1);
-        const float fx = fminf(fmaxf(fmaf(s.ph.px, w.inv_spacing[0], -w.lo_inv[0]), 0.0f), w.dims_f[0] - 1.0f);
-        const float fy = fminf(fmaxf(fmaf(s.ph.py, w.inv_spacing[1], -w.lo_inv[1]), 0.0f), w.dims_f[1] - 1.0f);
-        const float fz = fminf(fmaxf(fmaf(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2]), 0.0f), w.dims_f[2] - 1.0f);
+        s.band = min(max(m_floor_int((s.logE - g.band_log0) * g.band_inv_dlog), 0), g.bands - 1);
+        const Real fx = m_min(m_max(m_fma(s.ph.px, w.inv_spacing[0], -w.lo_inv[0]), Real(0.0)), w.dims_f[0] - Real(1.0));
+        const Real fy = m_min(m_max(m_fma(s.ph.py, w.inv_spacing[1], -w.lo_inv[1]), Real(0.0)), w.dims_f[1] - Real(1.0));
+        const Real fz = m_min(m_max(m_fma(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2]), Real(0.0)), w.dims_f[2] - Real(1.0));
         const uint32_t ix = static_cast<uint32_t>(fx), iy = static_cast<uint32_t>(fy), iz = static_cast<uint32_t>(fz);
         const uint32_t c = (iz >> g.shift[2]) * g.nxy + (iy >> g.shift[1]) * g.nx + (ix >> g.shift[0]);
         const float2 cell = __ldg(g.cells + (c * g.bands + s.band));
@@ -568,29 +577,31 @@ namespace {
     // holds -R): the ball of radius R, or the ray up to where it enters the box
     // (slab test in flight-parameter units, as the position update), whichever
     // reaches further.  A ray that misses the box may fly to the grid boundary.
-    __device__ __forceinline__ float reach_to_box(const Photon& ph, const MajorantGrid& g, float R)
+    template <class Real>
+    __device__ __forceinline__ Real reach_to_box(const PhotonT<Real>& ph, const MajorantGrid& g, Real R)
     {
-        const float p[3] = { ph.px, ph.py, ph.pz };
-        const float d[3] = { ph.dx, ph.dy, ph.dz };
-        float tmin = 0.0f, tmax = INFINITY;
+        const Real p[3] = { ph.px, ph.py, ph.pz };
+        const Real d[3] = { ph.dx, ph.dy, ph.dz };
+        Real tmin = Real(0.0), tmax = INFINITY;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            const float inv = 1.0f / d[a];
-            const float t0 = (__ldg(g.box + a) - p[a]) * inv;
-            const float t1 = (__ldg(g.box + 3 + a) - p[a]) * inv;
-            tmin = fmaxf(tmin, fminf(t0, t1));
-            tmax = fminf(tmax, fmaxf(t0, t1));
+            const Real inv = Real(1.0) / d[a];
+            const Real t0 = (__ldg(g.box + a) - p[a]) * inv;
+            const Real t1 = (__ldg(g.box + 3 + a) - p[a]) * inv;
+            tmin = m_max(tmin, m_min(t0, t1));
+            tmax = m_min(tmax, m_max(t0, t1));
         }
-        return fmaxf(R, tmin <= tmax ? tmin : INFINITY);
+        return m_max(R, tmin <= tmax ? tmin : INFINITY);
     }
 
     // Loads photon + stream state from the pre-generated queue.
-    __device__ __forceinline__ void take_queued(Lane& s, const PhotonQueue& q, uint64_t i)
+    template <class Real>
+    __device__ __forceinline__ void take_queued(LaneT<Real>& s, const PhotonQueue& q, uint64_t i)
     {
         const float4 pe = __ldg(q.pos_energy + i);
         const float4 dw = __ldg(q.dir_weight + i);
         const uint4 rs = __ldg(q.rng + i);
-        s.ph = Photon { pe.x, pe.y, pe.z, dw.x, dw.y, dw.z, pe.w, dw.w };
+        s.ph = PhotonT<Real> { pe.x, pe.y, pe.z, dw.x, dw.y, dw.z, pe.w, dw.w };
         s.rng.s0 = rs.x;
         s.rng.s1 = rs.y;
         s.rng.s2 = rs.z;
@@ -600,7 +611,8 @@ namespace {
     }
 
     // Samples history h of the job in place (Exposure::sampleParticle + transportParticleToWorld).
-    __device__ __forceinline__ void take_history(Lane& s, const TransportParams& p, uint64_t h)
+    template <class Real>
+    __device__ __forceinline__ void take_history(LaneT<Real>& s, const TransportParams& p, uint64_t h)
     {
         s.rng.init(p.seed, h);
         uint32_t ei;
@@ -619,21 +631,21 @@ namespace {
     // Woodcock step for lanes without a pending interaction (transport.hpp:650-699),
     // the per-type interaction passes once enough lanes wait (transport.hpp:523-638),
     // Russian roulette and scoring.  Must be called by all 32 lanes.
-    template <int MODEL, bool PALETTE>
-    __device__ __forceinline__ void advance(Lane& s, WarpTally& wt, const TransportParams& p, const float* L, const PaletteEntry* pal,
+    template <int MODEL, bool PALETTE, class Real>
+    __device__ __forceinline__ void advance(LaneT<Real>& s, WarpTally& wt, const TransportParams& p, const float* L, const PaletteEntry* pal,
         bool drain, int interact_t)
     {
         const LutMeta& m = p.lut_meta;
         const WorldParams& w = p.world;
         bool do_score = false;
-        float deposit = 0.0f; // energy imparted x weight to score
+        Real deposit = Real(0.0); // energy imparted x weight to score
         bool check_roulette = false;
 
         if (s.alive && s.pending == EV_NONE) {
             if (s.updateMax) {
-                s.logE = __log10f(s.ph.energy);
+                s.logE = m_log10(s.ph.energy);
                 s.seg = lut_segment(L, m, s.logE);
-                s.stepK = lut_max_inverse(L, m, s.logE, s.seg) * (10.0f * 0.693147180559945f); // cm -> mm, log2 -> ln
+                s.stepK = lut_max_inverse(L, m, s.logE, s.seg) * (Real(10.0) * Real(0.693147180559945)); // cm -> mm, log2 -> ln
                 s.updateMax = false;
                 s.cached_mat = -1;
                 if (p.majorant.cells)
@@ -652,21 +664,21 @@ namespace {
             for (int k = 0; k < burst && s.alive; ++k) {
                 // a flight drawn with the local majorant ends without a collision test
                 // where that majorant stops holding (truncated: drawn again from there)
-                float R = s.cR;
-                if (R < 0.0f)
+                Real R = s.cR;
+                if (R < Real(0.0))
                     R = reach_to_box(s.ph, p.majorant, -R);
-                const float flight = -__log2f(s.rng.uniform_open()) * (s.stepK * s.cinv);
+                const Real flight = -m_log2(static_cast<Real>(s.rng.uniform_open())) * (s.stepK * s.cinv);
                 const bool truncated = flight > R;
-                const float step = fminf(flight, R);
-                s.ph.px = fmaf(s.ph.dx, step, s.ph.px);
-                s.ph.py = fmaf(s.ph.dy, step, s.ph.py);
-                s.ph.pz = fmaf(s.ph.dz, step, s.ph.pz);
+                const Real step = m_min(flight, R);
+                s.ph.px = m_fma(s.ph.dx, step, s.ph.px);
+                s.ph.py = m_fma(s.ph.dy, step, s.ph.py);
+                s.ph.pz = m_fma(s.ph.dz, step, s.ph.pz);
                 // grid coordinates (p - lo) / spacing as one FMA each, rounded down; the photon
                 // is inside while all three lie in [0, dims) (one unsigned compare each: a
                 // negative or saturated conversion falls outside), which bounds the voxel index
-                const int jx = __float2int_rd(fmaf(s.ph.px, w.inv_spacing[0], -w.lo_inv[0]));
-                const int jy = __float2int_rd(fmaf(s.ph.py, w.inv_spacing[1], -w.lo_inv[1]));
-                const int jz = __float2int_rd(fmaf(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2]));
+                const int jx = m_floor_int(m_fma(s.ph.px, w.inv_spacing[0], -w.lo_inv[0]));
+                const int jy = m_floor_int(m_fma(s.ph.py, w.inv_spacing[1], -w.lo_inv[1]));
+                const int jz = m_floor_int(m_fma(s.ph.pz, w.inv_spacing[2], -w.lo_inv[2]));
                 if (!(static_cast<uint32_t>(jx) < w.dims[0] && static_cast<uint32_t>(jy) < w.dims[1]
                         && static_cast<uint32_t>(jz) < w.dims[2])) {
                     s.alive = false;
@@ -676,7 +688,7 @@ namespace {
                 const uint32_t ix = static_cast<uint32_t>(jx);
                 const uint32_t iy = static_cast<uint32_t>(jy);
                 const uint32_t iz = static_cast<uint32_t>(jz);
-                const float cinv = s.cinv; // the majorant this flight was drawn with
+                const Real cinv = s.cinv; // the majorant this flight was drawn with
                 if (p.majorant.cells) {
                     const MajorantGrid& g = p.majorant;
                     const uint32_t c = (iz >> g.shift[2]) * g.nxy + (iy >> g.shift[1]) * g.nx + (ix >> g.shift[0]);
@@ -690,55 +702,55 @@ namespace {
                     s.vidx = iz * static_cast<uint32_t>(w.nxy) + (iy * w.dims[0] + ix);
                 else
                     s.vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
-                float density;
+                Real density;
                 int mat;
                 bool measured;
                 gather_voxel<PALETTE>(w, pal, s.vidx, density, mat, measured);
                 if (mat != s.cached_mat) {
-                    float a0, a1, a2;
+                    Real a0, a1, a2;
                     lut_attenuation(L, m, mat, s.logE, s.seg, a0, a1, a2);
-                    const float attTot = a0 + a1 + a2;
-                    const float inv = 1.0f / attTot;
-                    s.probInv = attTot * s.stepK * (1.0f / (10.0f * 0.693147180559945f));
+                    const Real attTot = a0 + a1 + a2;
+                    const Real inv = Real(1.0) / attTot;
+                    s.probInv = attTot * s.stepK * (Real(1.0) / (Real(10.0) * Real(0.693147180559945)));
                     s.p0 = a0 * inv;
                     s.p01 = (a0 + a1) * inv;
                     s.cached_mat = mat;
                 }
-                const float eventProb = s.probInv * density * cinv;
+                const Real eventProb = s.probInv * density * cinv;
                 if (!measured) {
                     // naive sampling (computeInteractions): decide the event type now,
                     // run it in the interaction pass
-                    if (s.rng.uniform() < eventProb) {
-                        const float r3 = s.rng.uniform();
+                    if (static_cast<Real>(s.rng.uniform()) < eventProb) {
+                        const Real r3 = static_cast<Real>(s.rng.uniform());
                         s.pending = r3 < s.p0 ? EV_PHOTO : (r3 < s.p01 ? EV_COMPTON : EV_RAYLEIGH);
                         break;
                     }
                     // virtual collision: Russian roulette (transport.hpp:684-694)
                     if (s.armed) {
-                        if (s.rng.uniform() < ROULETTE_PROBABILITY) {
+                        if (static_cast<Real>(s.rng.uniform()) < Real(ROULETTE_PROBABILITY_D)) {
                             s.alive = false;
                             break;
                         }
-                        s.ph.weight *= 1.0f / (1.0f - ROULETTE_PROBABILITY);
+                        s.ph.weight *= Real(1.0) / (Real(1.0) - Real(ROULETTE_PROBABILITY_D));
                         s.arm();
                     }
                 } else {
                     // forced photoelectric scoring (computeInteractionsForced): score the forced
                     // photoelectric share now; a real Compton or Rayleigh event goes through the
                     // interaction passes and the weight correction (1 - wc) is applied after it
-                    const float photoProb = s.p0;
+                    const Real photoProb = s.p0;
                     s.forced_wc = eventProb * photoProb;
                     {
-                        Photon forced = s.ph;
-                        const float ef = photo_absorption<MODEL>(L, m, forced, mat, s.rng, p.normalize_direction);
-                        deposit = (forced.energy < ENERGY_CUTOFF ? (ef + forced.energy) : ef) * forced.weight * s.forced_wc;
+                        PhotonT<Real> forced = s.ph;
+                        const Real ef = photo_absorption<MODEL>(L, m, forced, mat, s.rng, p.normalize_direction);
+                        deposit = (forced.energy < Real(ENERGY_CUTOFF_D) ? (ef + forced.energy) : ef) * forced.weight * s.forced_wc;
                         do_score = true;
                     }
-                    if (s.rng.uniform() < eventProb * (1.0f - photoProb)) {
-                        s.pending = s.rng.uniform() * (1.0f - s.p0) < s.p01 - s.p0 ? EV_COMPTON : EV_RAYLEIGH;
+                    if (static_cast<Real>(s.rng.uniform()) < eventProb * (Real(1.0) - photoProb)) {
+                        s.pending = static_cast<Real>(s.rng.uniform()) * (Real(1.0) - s.p0) < s.p01 - s.p0 ? EV_COMPTON : EV_RAYLEIGH;
                     } else {
-                        s.ph.weight *= (1.0f - s.forced_wc);
-                        s.forced_wc = 0.0f;
+                        s.ph.weight *= (Real(1.0) - s.forced_wc);
+                        s.forced_wc = Real(0.0);
                         check_roulette = true;
                     }
                     break; // the forced deposit is scored before the next step
@@ -772,11 +784,11 @@ namespace {
             if ((waiting_other && (__popc(waiting_other) >= interact_t || stuck)) || run_ray) {
                 const int mat = s.cached_mat;
                 if (__any_sync(FULL_MASK, s.pending == EV_PHOTO) && s.pending == EV_PHOTO) {
-                    const float e = photo_absorption<MODEL>(L, m, s.ph, mat, s.rng, p.normalize_direction);
+                    const Real e = photo_absorption<MODEL>(L, m, s.ph, mat, s.rng, p.normalize_direction);
                     do_score = true;
-                    if (s.ph.energy < ENERGY_CUTOFF) {
+                    if (s.ph.energy < Real(ENERGY_CUTOFF_D)) {
                         deposit = (e + s.ph.energy) * s.ph.weight;
-                        s.ph.energy = 0.0f;
+                        s.ph.energy = Real(0.0);
                         s.alive = false;
                     } else {
                         deposit = e * s.ph.weight;
@@ -784,15 +796,15 @@ namespace {
                     }
                 }
                 if (__any_sync(FULL_MASK, s.pending == EV_COMPTON) && s.pending == EV_COMPTON) {
-                    float e = 0.0f;
+                    Real e = Real(0.0);
                     if (!compton_scatter<MODEL>(L, p.lut, m, s.ph, mat, s.rng, e, p.normalize_direction)) {
                         atomicAdd(&wt.overflows, 1ull);
                         s.alive = false;
                     } else {
                         do_score = true;
-                        if (s.ph.energy < ENERGY_CUTOFF) {
+                        if (s.ph.energy < Real(ENERGY_CUTOFF_D)) {
                             deposit = (e + s.ph.energy) * s.ph.weight;
-                            s.ph.energy = 0.0f;
+                            s.ph.energy = Real(0.0);
                             s.alive = false;
                         } else {
                             deposit = e * s.ph.weight;
@@ -807,9 +819,9 @@ namespace {
                     }
                 }
                 if (s.pending != EV_NONE && (s.pending != EV_RAYLEIGH || run_ray)) {
-                    if (s.alive && s.forced_wc != 0.0f)
-                        s.ph.weight *= (1.0f - s.forced_wc);
-                    s.forced_wc = 0.0f;
+                    if (s.alive && s.forced_wc != Real(0.0))
+                        s.ph.weight *= (Real(1.0) - s.forced_wc);
+                    s.forced_wc = Real(0.0);
                     check_roulette = s.alive;
                     s.pending = EV_NONE;
                 }
@@ -817,11 +829,11 @@ namespace {
         }
         if (check_roulette) {
             // Russian roulette (transport.hpp:684-694) after an interaction or a forced step
-            if (s.ph.energy * s.ph.weight < ROULETTE_THRESHOLD) {
-                if (s.rng.uniform() < ROULETTE_PROBABILITY)
+            if (s.ph.energy * s.ph.weight < Real(ROULETTE_THRESHOLD_D)) {
+                if (static_cast<Real>(s.rng.uniform()) < Real(ROULETTE_PROBABILITY_D))
                     s.alive = false;
                 else
-                    s.ph.weight *= 1.0f / (1.0f - ROULETTE_PROBABILITY);
+                    s.ph.weight *= Real(1.0) / (Real(1.0) - Real(ROULETTE_PROBABILITY_D));
             }
             s.arm();
         }
@@ -846,7 +858,8 @@ namespace {
 
     // Counts the steps of the photons a warp's lanes finished (before they are
     // refilled or at a flush).  Called by all 32 lanes.
-    __device__ __forceinline__ void count_steps(Lane& s, WarpTally& wt, bool finished)
+    template <class Real>
+    __device__ __forceinline__ void count_steps(LaneT<Real>& s, WarpTally& wt, bool finished)
     {
         const unsigned n = __reduce_add_sync(FULL_MASK, finished ? s.hist_steps : 0u);
         if ((threadIdx.x & 31) == 0)
@@ -856,7 +869,8 @@ namespace {
     }
 
     // Adds the warp's counters to a job's counters and clears them.  Called by all 32 lanes.
-    __device__ __forceinline__ void flush_counters(Lane& s, WarpTally& wt, JobCounters* c)
+    template <class Real>
+    __device__ __forceinline__ void flush_counters(LaneT<Real>& s, WarpTally& wt, JobCounters* c)
     {
         count_steps(s, wt, true); // counted once: the photons' steps so far
         __syncwarp();
@@ -883,8 +897,9 @@ namespace {
     // one converged pass per type once enough lanes wait, and finished lanes are
     // refilled together once enough are idle, so the expensive branches run with
     // many lanes active instead of one or two.
-    template <int MODEL, bool PALETTE>
-    __global__ void __launch_bounds__(256, DXMC_MIN_BLOCKS_PER_SM) transport_kernel(const __grid_constant__ TransportParams p)
+    // the FP64-everywhere instantiation needs about twice the registers: two blocks per SM
+    template <class Real, int MODEL, bool PALETTE>
+    __global__ void __launch_bounds__(256, sizeof(Real) == 4 ? DXMC_MIN_BLOCKS_PER_SM : 2) transport_kernel(const __grid_constant__ TransportParams p)
     {
         extern __shared__ float4 smem_f4[];
         const float* L = p.lut;
@@ -902,7 +917,7 @@ namespace {
         if constexpr (PALETTE) {
             PaletteEntry* spal = reinterpret_cast<PaletteEntry*>(smem_f4 + smem_off);
             for (int i = threadIdx.x; i < PALETTE_MAX; i += blockDim.x)
-                spal[i] = i < p.world.palette_n ? p.world.palette[i] : PaletteEntry { 0.0f, 0u };
+                spal[i] = i < p.world.palette_n ? p.world.palette[i] : PaletteEntry { Real(0.0), 0u };
             pal = spal;
         }
         __syncthreads();
@@ -919,7 +934,7 @@ namespace {
         if (lane == 0)
             wt = WarpTally {};
         __syncwarp();
-        Lane s {};
+        LaneT<Real> s {};
         s.alive = false;
         // warp-uniform pool of ids (queue slots or history ids) [pool_next, pool_end)
         uint64_t pool_next = 0, pool_end = 0;
@@ -1002,7 +1017,7 @@ namespace {
         if (lane == 0)
             wt = WarpTally {};
         __syncwarp();
-        Lane s {};
+        LaneT<float> s {};
         s.alive = false;
         int job = -1;
         uint64_t pool_next = 0, pool_end = 0;
@@ -1088,7 +1103,7 @@ namespace {
         for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x); base < count; base += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
             const uint64_t i = base + threadIdx.x;
             bool inworld = false;
-            Photon ph {};
+            PhotonT<float> ph {};
             Rng rng;
             if (i < count) {
                 const uint64_t h = first + i;
@@ -1232,7 +1247,7 @@ namespace {
         for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n; i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
             Rng rng;
             rng.init(seed, i);
-            Photon ph { 0, 0, 0, 0, 0, 1, energy, 1 };
+            PhotonT<float> ph { 0, 0, 0, 0, 0, 1, energy, 1 };
             float dep = 0.0f;
             bool ok = true;
             if (kind == 0)
@@ -1286,14 +1301,21 @@ namespace {
 
 } // namespace
 
-template <int MODEL, bool PALETTE>
-static void* transport_entry() { return reinterpret_cast<void*>(&transport_kernel<MODEL, PALETTE>); }
+template <class Real, int MODEL, bool PALETTE>
+static void* transport_entry() { return reinterpret_cast<void*>(&transport_kernel<Real, MODEL, PALETTE>); }
 
-static void* transport_function(int model, bool palette)
+template <class Real>
+static void* transport_function_as(int model, bool palette)
 {
     if (palette)
-        return model == 0 ? transport_entry<0, true>() : (model == 1 ? transport_entry<1, true>() : transport_entry<2, true>());
-    return model == 0 ? transport_entry<0, false>() : (model == 1 ? transport_entry<1, false>() : transport_entry<2, false>());
+        return model == 0 ? transport_entry<Real, 0, true>() : (model == 1 ? transport_entry<Real, 1, true>() : transport_entry<Real, 2, true>());
+    return model == 0 ? transport_entry<Real, 0, false>() : (model == 1 ? transport_entry<Real, 1, false>() : transport_entry<Real, 2, false>());
+}
+
+// precision 0: FP32 transport (the fast path); 1: FP64 everywhere (the precision study)
+static void* transport_function(int model, bool palette, int precision)
+{
+    return precision == 1 ? transport_function_as<double>(model, palette) : transport_function_as<float>(model, palette);
 }
 
 const void* batch_kernel_function(int model)
@@ -1335,34 +1357,35 @@ size_t transport_smem_bytes(size_t lut_bytes, bool lut_in_smem, bool palette)
 cudaError_t launch_transport(const TransportParams& p, int model, int grid, int block, size_t smem, cudaStream_t stream)
 {
     const bool palette = p.world.palette_index != nullptr;
-    void* fn = transport_function(model, palette);
+    void* fn = transport_function(model, palette, p.precision);
     void* args[] = { const_cast<TransportParams*>(&p) };
     return cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, stream);
 }
 
 cudaError_t preload_transport_kernels()
 {
-    for (int model = 0; model < 3; ++model)
-        for (int palette = 0; palette < 2; ++palette) {
-            cudaFuncAttributes attr {};
-            const cudaError_t e = cudaFuncGetAttributes(&attr, transport_function(model, palette != 0));
-            if (e != cudaSuccess)
-                return e;
-        }
+    for (int precision = 0; precision < 2; ++precision)
+        for (int model = 0; model < 3; ++model)
+            for (int palette = 0; palette < 2; ++palette) {
+                cudaFuncAttributes attr {};
+                const cudaError_t e = cudaFuncGetAttributes(&attr, transport_function(model, palette != 0, precision));
+                if (e != cudaSuccess)
+                    return e;
+            }
     return cudaSuccess;
 }
 
-int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem)
+int transport_max_blocks_per_sm(int model, bool palette, int block, size_t smem, int precision)
 {
-    void* fn = transport_function(model, palette);
+    void* fn = transport_function(model, palette, precision);
     // The dynamic shared-memory limit is a property of the function, read when a
     // launch (or a graph holding it) is made: it only ever grows, so launches
     // queued or captured earlier with larger LUTs stay valid.
     static std::mutex m;
-    static int limit[6] = {};
+    static int limit[12] = {};
     {
         std::lock_guard<std::mutex> lock(m);
-        int& cur = limit[model * 2 + (palette ? 1 : 0)];
+        int& cur = limit[(precision == 1 ? 6 : 0) + model * 2 + (palette ? 1 : 0)];
         if (static_cast<int>(smem) > cur) {
             if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) == cudaSuccess)
                 cur = static_cast<int>(smem);

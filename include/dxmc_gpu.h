@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define DXMC_GPU_ABI_VERSION 2
+#define DXMC_GPU_ABI_VERSION 3
 
 /* ---- status codes ------------------------------------------------------- */
 enum {
@@ -300,7 +300,15 @@ typedef struct dxmc_job_desc {
     int32_t block_size;                 /* threads per block of the transport kernel: 128 or 256 */
     int32_t tracking;                   /* DXMC_TRACKING_*; 0 = the context's */
     int32_t direction;                  /* DXMC_DIRECTION_* */
+    /* DXMC_PRECISION_FP32 (0): FP32 transport with FP64 tallies, the default;
+     * DXMC_PRECISION_FP64 (1): FP64 everywhere (position, direction, energy, LUT
+     * evaluation and sampling in double, as Transport<double>, transport.hpp:114-840)
+     * on the same per-history random streams; photons are generated in the kernel */
+    int32_t precision;
 } dxmc_job_desc;
+
+#define DXMC_PRECISION_FP32 0
+#define DXMC_PRECISION_FP64 1
 
 typedef struct dxmc_job_stats {
     uint64_t histories;        /* histories simulated */

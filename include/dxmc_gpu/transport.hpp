@@ -210,6 +210,10 @@ public:
     int tracking() const { return m_tracking; }
     void setDirectionMode(int direction) { m_direction = direction; }
     int directionMode() const { return m_direction; }
+    // DXMC_PRECISION_FP32 (default: FP32 transport, FP64 tallies) or
+    // DXMC_PRECISION_FP64 (everything in double, as Transport<double> computes)
+    void setTransportPrecision(int precision) { m_precision = precision; }
+    int transportPrecision() const { return m_precision; }
     // Spectrum for IsotropicSource, whose spectrum has no public getter.
     void setIsotropicSpectrum(std::vector<T> energies, std::vector<T> weights) { m_iso = { std::move(energies), std::move(weights) }; }
     const std::string& lastError() const { return m_error; }
@@ -292,6 +296,7 @@ public:
         jd.tally_mode = -1;
         jd.tracking = m_tracking;
         jd.direction = m_direction;
+        jd.precision = m_precision;
         const auto start = std::chrono::system_clock::now();
         if (progressbar) {
             progressbar->setTotalExposures(flat.exposures.size());
@@ -460,6 +465,7 @@ private:
     std::uint64_t m_seed = 1;
     int m_tracking = DXMC_TRACKING_DEFAULT;
     int m_direction = DXMC_DIRECTION_REFERENCE;
+    int m_precision = DXMC_PRECISION_FP32;
     std::pair<std::vector<T>, std::vector<T>> m_iso;
     std::string m_error;
     OUTPUTMODE m_mode = OUTPUTMODE::DOSE;                             // transport.hpp:838

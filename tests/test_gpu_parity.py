@@ -32,14 +32,15 @@ def _world(dims, spacing, material, density, names, measurement=None):
     return w
 
 
-def _run(ctx, world, exposures, max_energy, spectrum=None, heel=None, model=1, seed=11, tally_mode=-1):
+def _run(ctx, world, exposures, max_energy, spectrum=None, heel=None, model=1, seed=11, tally_mode=-1, precision=0):
     import dxmclib_gb300 as dx
     from dxmclib_gb300 import _capi as A
     dworld = dx.DeviceWorld(ctx, world)
     md = dworld.max_density()
     blob = dx.LutBlob(world.materialMap(), md, max_energy)
     dlut = dx.DeviceLut(ctx, blob)
-    job = dx.Job(ctx, dworld, dlut, exposures, spectrum, heel, None, seed=seed, model=model, tally_mode=tally_mode)
+    job = dx.Job(ctx, dworld, dlut, exposures, spectrum, heel, None, seed=seed, model=model, tally_mode=tally_mode,
+                 precision=precision)
     dose, var, nev, stats = job.result(A.OUTPUT_EV_PER_HISTORY)
     assert stats["histories"] == int(np.sum(exposures.n_histories))
     assert stats["rejection_overflows"] == 0
@@ -388,3 +389,32 @@ def test_normalized_direction_matches_port(gpu_ctx, model):
                   max_chi2=max(1.2, stats[A.DIRECTION_REFERENCE]["chi2"]) * 1.15)
     gap = gpu[A.DIRECTION_REFERENCE][0].sum() / gpu[A.DIRECTION_NORMALIZED][0].sum() - 1.0
     assert 0.003 < gap < 0.015, gap
+
+
+@pytest.mark.parametrize("model", [1, 2])
+def test_fp64_everywhere_matches_reference(gpu_ctx, golden, model):
+    """The FP64-everywhere kernel (position, direction, energy, LUT evaluation and
+    sampling in double, as Transport<double>) on the heterogeneous cone beam,
+    against the reference; and against the FP32 kernel on the same per-history
+    streams (totals and Woodcock steps agree far closer than independent runs)."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    g = golden(f"transport_cone_m{model}.npz")
+    dims = tuple(int(x) for x in g["dims"])
+    world = _world(dims, tuple(g["spacing"]), g["material"], g["density"], g["names"])
+    src = dx.IsotropicSource()
+    src.setPosition((0, 0, -500))
+    src.setDirectionCosines((1, 0, 0, 0, 1, 0))
+    src.setCollimationAngles(-0.12, 0.12, -0.1, 0.1)
+    src.setSpecter(g["spec_weights"], g["spec_energies"])
+    src.setTotalExposures(8)
+    src.setHistoriesPerExposure(int(g["histories"]) // 8)
+    d64, v64, n64, st64 = _run(gpu_ctx, world, src.exposures(), src.maxPhotonEnergyProduced(), src.spectrum(),
+                               model=model, precision=A.PRECISION_FP64)
+    assert_parity(compare_sparse(g, d64, v64), f"cone m{model} fp64 everywhere")
+    d32, v32, n32, st32 = _run(gpu_ctx, world, src.exposures(), src.maxPhotonEnergyProduced(), src.spectrum(),
+                               model=model)
+    print(f"[fp64] cone m{model}: fp32/fp64 total {d32.sum() / d64.sum():.6f}, steps {st32['steps'] / st64['steps']:.6f}, "
+          f"fp64 kernel {st64['kernel_ms']:.1f} ms, fp32 {st32['kernel_ms']:.2f} ms")
+    assert abs(d32.sum() / d64.sum() - 1) < 2e-3, (d32.sum(), d64.sum())
+    assert abs(st32["steps"] / st64["steps"] - 1) < 2e-3, (st32["steps"], st64["steps"])

@@ -228,7 +228,7 @@ def test_capi_exports_every_declared_symbol(lib):
     assert len(names) >= 25
     missing = [n for n in sorted(names) if not hasattr(lib, n)]
     assert not missing, missing
-    assert lib.dxmc_gpu_abi_version() == 2
+    assert lib.dxmc_gpu_abi_version() == 3
 
 
 def test_invalid_inputs_are_rejected(lib):
