@@ -153,6 +153,7 @@ SIGNATURES = {
     "dxmc_physics_material": (C.c_int, [C.c_char_p, D, C.POINTER(MaterialProvider)]),
     "dxmc_physics_material_free": (None, [C.POINTER(MaterialProvider)]),
     "dxmc_physics_mass_energy_absorption": (C.c_int, [C.POINTER(MaterialProvider), D, DP]),
+    "dxmc_tube_spectrum": (C.c_int, [D, D, D, DP, C.c_int, C.POINTER(MaterialProvider), DP, C.c_int, C.c_int, DP]),
     "dxmc_physics_element_material": (C.c_int, [C.c_int, C.POINTER(MaterialProvider)]),
     "dxmc_lut_build": (C.c_int, [C.POINTER(MaterialProvider), C.c_int, FP, U8P, C.c_uint64, D, C.POINTER(VP)]),
     "dxmc_lut_build_max_density": (C.c_int, [C.POINTER(MaterialProvider), C.c_int, DP, D, C.POINTER(VP)]),

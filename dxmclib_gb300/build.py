@@ -27,6 +27,7 @@ HOST_SOURCES = [
     CSRC / "physics" / "physics_model.cpp",
     CSRC / "host" / "lut_builder.cpp",
     CSRC / "host" / "capi_host.cpp",
+    CSRC / "host" / "tube_spectrum.cpp",
 ]
 CUDA_SOURCES = [
     CSRC / "kernels" / "transport_kernels.cu",

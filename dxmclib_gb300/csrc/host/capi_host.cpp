@@ -5,6 +5,7 @@
 #include "../physics/physics_model.hpp"
 #include "lut_builder.hpp"
 #include "../kernels/stream_seed.hpp"
+#include "tube_spectrum.hpp"
 
 #include <algorithm>
 #include <cstring>
@@ -216,6 +217,31 @@ int dxmc_udiv_invariant(const uint32_t* n, uint64_t count, uint32_t d, uint32_t*
     const auto q = dxmc_gb300::udiv_magic(d);
     for (uint64_t i = 0; i < count; ++i)
         out[i] = dxmc_gb300::udiv_apply(n[i], q.m, q.shifts);
+    return DXMC_OK;
+}
+
+namespace {
+double provider_total_attenuation(const void* user, double e)
+{
+    const auto* p = static_cast<const dxmc_material_provider*>(user);
+    return p->photoelectric(p->user, e) + p->compton(p->user, e) + p->rayleigh(p->user, e);
+}
+} // namespace
+
+int dxmc_tube_spectrum(double voltage, double takeoff_angle, double line_takeoff_angle, const double* energies, int n_energies,
+    const dxmc_material_provider* filters, const double* filter_mm, int n_filters, int normalize, double* out)
+{
+    if (!energies || !out || n_energies <= 0 || !(voltage > 0) || n_filters < 0 || (n_filters > 0 && (!filters || !filter_mm)))
+        return DXMC_ERR_INVALID;
+    std::vector<dxmc_gb300::host::SpectrumFilter> f;
+    for (int i = 0; i < n_filters; ++i) {
+        if (!provider_ok(filters[i]) || !(filters[i].standard_density > 0))
+            return DXMC_ERR_INVALID;
+        f.push_back({ provider_total_attenuation, &filters[i], filters[i].standard_density, std::abs(filter_mm[i]) });
+    }
+    const std::vector<double> e(energies, energies + n_energies);
+    const auto s = dxmc_gb300::host::tube_spectrum(voltage, takeoff_angle, line_takeoff_angle, e, f, normalize != 0);
+    std::copy(s.begin(), s.end(), out);
     return DXMC_OK;
 }
 

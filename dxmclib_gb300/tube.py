@@ -1,18 +1,12 @@
 """X-ray tube spectrum and heel table (host side).
 
 Spectrum generation stays on the host, as in DXMClib (tube.hpp:35-299,
-beamfilters.hpp:435-569).  The project's own tube model is a thick-target
-Kramers spectrum with depth-resolved anode self-absorption:
-
-* electrons slow down in tungsten along the Thomson-Whiddington law
-  T(x)^2 = T0^2 - C x, with C = T0^2 / R(T0) and R the Kanaya-Okayama range;
-* at each depth the Kramers thin-target yield is 1/hv per unit electron
-  energy loss for hv < T;
-* photons emitted at mass depth x leave the anode through x / sin(angle) of
-  tungsten (attenuation from the project physics model);
-* tungsten K-lines (energies from the project shell model) are added with a
-  yield proportional to ((T0 - E_K) / E_K)^1.63 (Green-Cosslett);
-* added filtration is exp(-mu/rho * rho * t) per filter material.
+beamfilters.hpp:435-569).  The spectrum is DXMClib's model, computed by the
+library's host code (dxmc_tube_spectrum, csrc/host/tube_spectrum.cpp):
+thick-target semi-relativistic Bethe-Heitler bremsstrahlung integrated over the
+tabulated electron fluence in tungsten of Poludniowski and Evans (2007), with
+self-absorption in the anode along the take-off direction, the tungsten K lines,
+and added filtration exp(-mu/rho * rho * t) per filter material.
 
 The interface mirrors Tube<T> (voltage, anode angle, energy resolution,
 filtration setters, getEnergy, getSpecter) and HeelFilter<T> (energy grid
@@ -100,61 +94,6 @@ class Tube:
             hv = hv + self._res
         return np.asarray(out, np.float64)
 
-    def _tungsten(self):
-        if "W" not in self._w_cache:
-            from .api import Material
-            self._w_cache["W"] = Material("W")
-        return self._w_cache["W"]
-
-    def _kramers_self_absorbed(self, energies: np.ndarray, anode_angle: float) -> np.ndarray:
-        T0 = self._voltage
-        W = self._tungsten()
-        rho = 19.3
-        # Kanaya-Okayama range (um -> cm) and Whiddington constant
-        R_cm = 0.0276 * 183.84 * T0 ** 1.67 / (74 ** 0.889 * rho) * 1e-4
-        Cw = T0 ** 2 / (rho * R_cm)  # keV^2 per g/cm2
-        sin_a = max(math.sin(anode_angle), 1e-6)
-        nT = 200
-        out = np.zeros(len(energies))
-        for i, hv in enumerate(energies):
-            if hv <= 0 or hv >= T0:
-                continue
-            mu = W.getTotalAttenuation(float(hv))
-            T = np.linspace(hv, T0, nT)
-            x = (T0 ** 2 - T ** 2) / Cw  # g/cm2 depth where the electron has energy T
-            f = np.exp(-mu * x / sin_a) / hv
-            out[i] = np.trapezoid(f, T) if hasattr(np, "trapezoid") else np.trapz(f, T)
-        return out
-
-    def _characteristic(self, energies: np.ndarray, anode_angle: float, spec: np.ndarray) -> np.ndarray:
-        """Tungsten K lines added to the nearest energy bin within 2 keV."""
-        T0 = self._voltage
-        import ctypes as C
-        from . import _capi as A
-        W = self._tungsten()
-        shells = (A.ShellConfig * 12)()
-        W.provider.shells(W.provider.user, shells)
-        k = shells[0]
-        EK = k.binding_energy
-        if T0 <= EK:
-            return spec
-        sin_a = max(math.sin(anode_angle), 1e-6)
-        yield_k = ((T0 - EK) / EK) ** 1.63
-        # normalise against the bremsstrahlung just above the edge energy scale
-        brem_ref = np.interp(EK * 0.8, energies, spec) if len(energies) > 1 else 0.0
-        total = 0.15 * yield_k * brem_ref * len(energies) / 12.0
-        out = spec.copy()
-        for line in range(3):
-            e = k.line_energies[line]
-            p = k.line_probabilities[line]
-            if e <= 0 or p <= 0:
-                continue
-            idx = np.searchsorted(energies, e)
-            if idx < len(energies) and abs(energies[idx] - e) <= 2.0:
-                mu = W.getTotalAttenuation(float(e))
-                out[idx] += total * p * math.exp(-mu * 19.3 * 3e-4 / sin_a)
-        return out
-
     def _state(self):
         return (self._voltage, self._anode, self._res, tuple((m.name(), m.standardDensity(), t) for m, t in self._filters))
 
@@ -172,15 +111,20 @@ class Tube:
         return spec
 
     def _compute_specter(self, e: np.ndarray, a: float, normalize: bool) -> np.ndarray:
-        spec = self._kramers_self_absorbed(e, a)
-        spec = self._characteristic(e, a, spec)
-        for m, mm in self._filters:
-            cm = mm * 0.1
-            mu = np.array([m.getTotalAttenuation(float(x)) for x in e])
-            spec = spec * np.exp(-mu * m.standardDensity() * cm)
-        if normalize and spec.sum() > 0:
-            spec = spec / spec.sum()
-        return spec
+        """Tube<T>::getSpecter(energies, anodeAngle, normalize) (tube.hpp:195-213): the
+        bremsstrahlung at take-off angle ``a``, the K lines at the tube's anode angle."""
+        from . import _capi as A
+        lib = A.load()
+        e = np.ascontiguousarray(e, np.float64)
+        out = np.zeros(len(e))
+        filt = (A.MaterialProvider * max(len(self._filters), 1))()
+        for i, (m, _) in enumerate(self._filters):
+            filt[i] = m.provider
+        mm = np.array([t for _, t in self._filters] or [0.0], np.float64)
+        A.check(lib.dxmc_tube_spectrum(float(self._voltage), float(a), float(self._anode), e.ctypes.data_as(A.DP), len(e),
+                                       filt, mm.ctypes.data_as(A.DP), len(self._filters), 1 if normalize else 0,
+                                       out.ctypes.data_as(A.DP)), None, "dxmc_tube_spectrum")
+        return out
 
 
 class HeelFilter:

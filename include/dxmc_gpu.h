@@ -119,6 +119,21 @@ void dxmc_physics_material_free(dxmc_material_provider* provider);
 int dxmc_physics_mass_energy_absorption(const dxmc_material_provider* provider, double energy_kev, double* out);
 int dxmc_physics_element_material(int atomic_number, dxmc_material_provider* out);
 
+/* ---- tube spectra (host; Tube<T>::getSpecter, tube.hpp:191-261) ----------- */
+/* Photon fluence per energy of an x-ray tube at voltage_kv with a tungsten
+ * anode: thick-target semi-relativistic Bethe-Heitler bremsstrahlung from the
+ * tabulated electron fluence of Poludniowski and Evans (2007), photons leaving
+ * the anode at takeoff_angle (radians), the tungsten K lines computed at
+ * line_takeoff_angle (the tube's own anode angle: DXMClib evaluates the lines
+ * there even for the heel table's other angles, tube.hpp:220-241), then
+ * attenuated by n_filters materials of filter_mm thickness each at their
+ * standard density, and with normalize scaled to sum to one.  energies are in
+ * keV, ascending (Tube::getEnergy: the resolution, twice it, ... up to the
+ * voltage).  Replaces betheHeitlerCrossSection.hpp:326-407 and tube.hpp:191-261. */
+int dxmc_tube_spectrum(double voltage_kv, double takeoff_angle, double line_takeoff_angle, const double* energies,
+    int n_energies, const dxmc_material_provider* filters, const double* filter_mm, int n_filters, int normalize,
+    double* out);
+
 /* ---- host LUT (AttenuationLut<T>::generate, attenuationlut.hpp:64-96) ---- */
 typedef struct dxmc_lut_blob dxmc_lut_blob;
 

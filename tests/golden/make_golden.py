@@ -26,6 +26,8 @@ tests/golden/ref_binding.py and stores, as small .npz files:
                     over-dispersion at this block size);
 * bench_dx.npz      the same for a DXSource beam on a 128^3 phantom of the
                     batched-radiography configuration (4 x 4 x 4 blocks);
+* tube_spectra.npz  Tube::getSpecter spectra and HeelFilter weights at 70-120 kV
+                    with Al / Cu filtration and two anode angles;
 * transport_dose_dx.npz Transport<double> in DOSE mode (mGy through the DX
                     dose-area-product calibration, and keV/kg without it) on a
                     64^3 DX phantom, 2 x 2 x 2 block sums, with the factor.
@@ -331,6 +333,25 @@ def gen_dose(out: Path, quick: bool):
                         max_energy=tabs["max_energy"], **res)
 
 
+def gen_tubes(out: Path):
+    """Tube<double>::getSpecter (tube.hpp:191-261) and HeelFilter<double> weights
+    (beamfilters.hpp:455-505), read through DX sources of the reference, at the
+    voltages and filtrations of the benchmark configurations."""
+    w = R.WorldArgs((8, 8, 8), (1, 1, 1), np.ones(512), np.zeros(512, np.uint8), ["Water, Liquid"])
+    res = {}
+    cases = [(70, 3.0, 0.0, 12.0), (80, 3.0, 0.0, 12.0), (90, 3.0, 0.1, 12.0), (120, 2.5, 0.0, 12.0), (100, 2.0, 0.0, 8.0)]
+    for k, (kvp, al, cu, anode) in enumerate(cases):
+        s = R.SourceArgs(R.DX, kvp=kvp, al_mm=al, cu_mm=cu, anode_angle_deg=anode, field_size=(300, 200), sdd=1000,
+                         heel=1, histories_per_exposure=10, total_exposures=1)
+        t = R.source_tables(s, w)
+        res[f"case{k}"] = np.array([kvp, al, cu, anode])
+        res[f"energies{k}"] = t["spec_energies"]
+        res[f"weights{k}"] = t["spec_weights"]
+        res[f"heel_meta{k}"] = t["heel_meta"]
+        res[f"heel_weights{k}"] = t["heel_weights"]
+    np.savez_compressed(out / "tube_spectra.npz", n=len(cases), **res)
+
+
 def gen_interactions(out: Path, quick: bool):
     n = 8
     w = R.WorldArgs((n, n, n), (1, 1, 1), np.ones(n ** 3) * 1.92, np.zeros(n ** 3, np.uint8),
@@ -398,7 +419,7 @@ def main():
                  transport=lambda: gen_transport(out, a.quick), ct=lambda: gen_ct(out, a.quick),
                  interactions=lambda: gen_interactions(out, a.quick), ctdi=lambda: gen_ctdi(out, a.quick),
                  bench_ct=lambda: gen_bench_ct(out, a.quick), bench_dx=lambda: gen_bench_dx(out, a.quick),
-                 dose=lambda: gen_dose(out, a.quick))
+                 dose=lambda: gen_dose(out, a.quick), tubes=lambda: gen_tubes(out))
     for name, fn in steps.items():
         if a.only and name not in a.only.split(","):
             continue

@@ -104,3 +104,8 @@ def test_ct_benchmark_exposures_match_reference(golden):
     assert ours.shape == ref.shape
     np.testing.assert_allclose(ours[:, :17], ref[:, :17], atol=1e-9)
     assert np.array_equal(ours[:, 17], ref[:, 17])
+    # and the same spectrum and heel table: the benchmark runs the reference's workload
+    spec = src.spectrum()
+    np.testing.assert_array_equal(spec.energies, g["spec_energies"])
+    np.testing.assert_allclose(spec.weights, g["spec_weights"], rtol=1e-12)
+    np.testing.assert_allclose(src.heel().weights, g["heel_weights"], rtol=1e-12, atol=1e-14)

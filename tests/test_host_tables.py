@@ -206,6 +206,33 @@ def test_heel_table_layout_matches_reference(lib, golden):
     np.testing.assert_allclose(gw.mean(axis=1), 1.0, rtol=1e-12)
 
 
+def test_tube_spectra_match_reference(lib, golden):
+    """Tube::getSpecter (tube.hpp:191-261: thick-target Bethe-Heitler bremsstrahlung
+    over the tabulated tungsten electron fluence, K lines, filtration, normalised)
+    and the HeelFilter weight table (beamfilters.hpp:455-505) against the
+    reference's, at 70-120 kV with Al and Cu filtration and two anode angles."""
+    import dxmclib_gb300 as dx
+    g = golden("tube_spectra.npz")
+    for k in range(int(g["n"])):
+        kvp, al, cu, anode = g[f"case{k}"]
+        src = dx.DXSource()
+        src.tube().setVoltage(kvp)
+        src.tube().setAnodeAngleDeg(anode)
+        src.tube().setAlFiltration(al)
+        if cu > 0:
+            src.tube().setCuFiltration(cu)
+        src.setFieldSize((300, 200))
+        src.setSourceDetectorDistance(1000)
+        e = src.tube().getEnergy()
+        np.testing.assert_array_equal(e, g[f"energies{k}"])
+        np.testing.assert_allclose(src.tube().getSpecter(e), g[f"weights{k}"], rtol=1e-12, atol=1e-300, err_msg=str(kvp))
+        h = src.heel()
+        meta = g[f"heel_meta{k}"]
+        assert (h.energy_start, h.energy_step, h.energy_size, h.angle_size) == (meta[1], meta[2], int(meta[3]), int(meta[6]))
+        assert h.angle_start == pytest.approx(meta[4], rel=1e-12) and h.angle_step == pytest.approx(meta[5], rel=1e-12)
+        np.testing.assert_allclose(h.weights, g[f"heel_weights{k}"], rtol=1e-12, atol=1e-14, err_msg=f"heel {kvp}")
+
+
 def test_tube_spectrum_is_physical(lib):
     import dxmclib_gb300 as dx
     t = dx.Tube(120)
