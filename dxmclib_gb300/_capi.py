@@ -36,6 +36,7 @@ TALLY_F64, TALLY_F32, TALLY_WARP_F64 = 0, 1, 2
 TRACKING_DEFAULT, TRACKING_GLOBAL, TRACKING_LOCAL = 0, 1, 2
 DIRECTION_REFERENCE, DIRECTION_NORMALIZED = 0, 1
 PRECISION_FP32, PRECISION_FP64 = 0, 1
+RESULT_F64, RESULT_F32 = 0, 1
 
 D = C.c_double
 DP = C.POINTER(C.c_double)
@@ -181,6 +182,8 @@ SIGNATURES = {
     "dxmc_gpu_job_cancel": (C.c_int, [VP]),
     "dxmc_gpu_job_result": (C.c_int, [VP, C.c_int, D, DP, DP, U32P, C.POINTER(JobStats)]),
     "dxmc_gpu_job_free": (None, [VP]),
+    "dxmc_gpu_job_result_async": (C.c_int, [VP, C.c_int, D, C.c_int, VP, VP, U32P]),
+    "dxmc_gpu_job_result_wait": (C.c_int, [VP, C.POINTER(JobStats)]),
     "dxmc_gpu_probe_lut": (C.c_int, [VP, VP, C.c_int, DP, C.c_int, DP, DP]),
     "dxmc_gpu_job_release": (C.c_int, [VP]),
     "dxmc_gpu_job_progress": (C.c_int, [VP, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),

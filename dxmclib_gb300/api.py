@@ -1178,6 +1178,43 @@ class Job:
             A.check(rc, self.ctx.handle, "dxmc_gpu_job_result")
         return dose, var, nev, stats
 
+    def result_async(self, output_mode: int = A.OUTPUT_EV_PER_HISTORY, calibration: float = 1.0, out=None,
+                     dtype=np.float64, want_events: bool = True):
+        """Queues the post-processing and the copies of the results behind the job
+        and returns at once (dxmc_gpu_job_result_async); ``result_wait`` finishes it.
+        ``out`` may supply (dose, variance, nEvents) buffers of ``dtype`` (float64:
+        Result<double>, float32: Result<float>), page-locked for overlapped copies;
+        they must stay alive until ``result_wait`` returns."""
+        n = self.dworld.world.size()
+        dtype = np.dtype(dtype)
+        if out is not None:
+            dose, var, nev = out
+        else:
+            dose, var = np.zeros(n, dtype), np.zeros(n, dtype)
+            nev = np.zeros(n, np.uint32) if want_events else None
+        for a in (dose, var):
+            if a is not None and (a.dtype != dtype or a.size != n or not a.flags.c_contiguous):
+                raise ValueError(f"result buffers must be contiguous {dtype} arrays of {n} elements")
+        rtype = A.RESULT_F32 if dtype == np.float32 else A.RESULT_F64
+        A.check(self.ctx.lib.dxmc_gpu_job_result_async(self.handle, output_mode, calibration, rtype,
+                                                       dose.ctypes.data_as(A.VP) if dose is not None else None,
+                                                       var.ctypes.data_as(A.VP) if var is not None else None,
+                                                       nev.ctypes.data_as(A.U32P) if nev is not None else None),
+                self.ctx.handle, "dxmc_gpu_job_result_async")
+        self._async_out = (dose, var, nev)
+        return self._async_out
+
+    def result_wait(self, check: bool = True) -> tuple:
+        """Waits for the asynchronous result; returns (dose, variance, nEvents, stats)."""
+        st = A.JobStats()
+        rc = self.ctx.lib.dxmc_gpu_job_result_wait(self.handle, C.byref(st))
+        stats = dict(histories=st.histories, steps=st.steps, deposits=st.deposits,
+                     rejection_overflows=st.rejection_overflows, kernel_ms=st.kernel_ms, job_ms=st.job_ms, status=rc)
+        if check and rc != A.DXMC_OK:
+            A.check(rc, self.ctx.handle, "dxmc_gpu_job_result_wait")
+        out, self._async_out = self._async_out, None
+        return (*out, stats)
+
     def progress(self) -> tuple:
         """(histories started, total) of a running job."""
         a, b = C.c_uint64(), C.c_uint64()

@@ -140,6 +140,13 @@ struct dxmc_job {
     uint64_t bytes = 0;
     bool cancelled = false;
     bool overflowed = false;
+    // an asynchronous result (dxmc_gpu_job_result_async): its completion and the
+    // caller's buffers (zeroed by the wait if the job was cancelled)
+    cudaEvent_t result_done = nullptr;
+    void* result_dose = nullptr;
+    void* result_variance = nullptr;
+    uint32_t* result_events = nullptr;
+    size_t result_elem = 0;
 };
 
 namespace {
@@ -2433,6 +2440,122 @@ int dxmc_gpu_job_preview(dxmc_job* j, double* energy)
     return DXMC_OK;
 }
 
+int dxmc_gpu_job_result_async(dxmc_job* j, int output_mode, double calibration, int result_type, void* dose, void* variance,
+    uint32_t* n_events)
+{
+    if (!j || output_mode < 0 || output_mode > 2 || (result_type != DXMC_RESULT_F64 && result_type != DXMC_RESULT_F32))
+        return DXMC_ERR_INVALID;
+    dxmc_gpu_ctx* ctx = j->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    cudaSetDevice(ctx->device);
+    if (!j->records && !j->tally_f32)
+        return fail(ctx, DXMC_ERR_STATE, "job results were already released");
+    if (j->result_done)
+        return fail(ctx, DXMC_ERR_STATE, "the job already has an asynchronous result pending");
+    if (result_type == DXMC_RESULT_F32 && !j->records)
+        return fail(ctx, DXMC_ERR_INVALID, "float results need an FP64 tally");
+    const uint64_t nv = j->world->params.n_voxels;
+    const size_t elem = result_type == DXMC_RESULT_F32 ? sizeof(float) : sizeof(double);
+    cudaStream_t s = ctx->result_stream;
+    auto* hc = reinterpret_cast<dev::JobCounters*>(reinterpret_cast<unsigned char*>(j->cancel_host) + 16);
+    // everything below runs on the result stream after the job's kernel: the caller may
+    // submit the next job at once, and these copies run on the copy engine beside it
+    DXMC_CUDA(ctx, cudaStreamWaitEvent(s, j->stop, 0));
+    DXMC_CUDA(ctx, cudaMemcpyAsync(hc, j->counters, sizeof(dev::JobCounters), cudaMemcpyDeviceToHost, s));
+    const bool counts_staged = n_events && j->records;
+    const size_t bytes = ((dose ? nv : 0) + (variance ? nv : 0)) * elem + (counts_staged ? nv * sizeof(uint32_t) : 0);
+    unsigned char* stage = nullptr;
+    if (bytes)
+        DXMC_CUDA(ctx, pool_alloc(ctx, &stage, bytes, s));
+    unsigned char* d_dose = dose ? stage : nullptr;
+    unsigned char* d_var = variance ? stage + (dose ? nv * elem : 0) : nullptr;
+    uint32_t* d_counts = counts_staged ? reinterpret_cast<uint32_t*>(stage + ((dose ? nv : 0) + (variance ? nv : 0)) * elem) : nullptr;
+    const double vv = j->world->spacing[0] * j->world->spacing[1] * j->world->spacing[2] / 1000.0;
+    const double hist = static_cast<double>(j->histories);
+    cudaError_t e = cudaSuccess;
+    if (dose || variance || counts_staged) {
+        if (!j->records)
+            e = dev::launch_postprocess_f32(j->tally_f32, j->world->params, nv, output_mode, hist, vv, calibration,
+                reinterpret_cast<double*>(d_dose), reinterpret_cast<double*>(d_var), nullptr, nullptr, s);
+        else if (result_type == DXMC_RESULT_F32)
+            e = dev::launch_postprocess_records_f32(j->records, j->world->params, nv, output_mode, hist, vv, calibration,
+                reinterpret_cast<float*>(d_dose), reinterpret_cast<float*>(d_var), d_counts, s);
+        else
+            e = dev::launch_postprocess_records(j->records, j->world->params, nv, output_mode, hist, vv, calibration,
+                reinterpret_cast<double*>(d_dose), reinterpret_cast<double*>(d_var), d_counts, s);
+    }
+    if (e == cudaSuccess && dose)
+        e = cudaMemcpyAsync(dose, d_dose, nv * elem, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && variance)
+        e = cudaMemcpyAsync(variance, d_var, nv * elem, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && n_events)
+        e = cudaMemcpyAsync(n_events, counts_staged ? d_counts : j->n_events, nv * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    if (stage)
+        cudaFreeAsync(stage, s);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&j->result_done, cudaEventDisableTiming);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(j->result_done, s);
+    if (e != cudaSuccess) {
+        if (j->result_done) {
+            cudaEventDestroy(j->result_done);
+            j->result_done = nullptr;
+        }
+        return cuda_fail(ctx, e, "asynchronous result");
+    }
+    j->result_dose = dose;
+    j->result_variance = variance;
+    j->result_events = n_events;
+    j->result_elem = elem;
+    return DXMC_OK;
+}
+
+int dxmc_gpu_job_result_wait(dxmc_job* j, dxmc_job_stats* stats)
+{
+    if (!j)
+        return DXMC_ERR_INVALID;
+    dxmc_gpu_ctx* ctx = j->ctx;
+    cudaEvent_t done = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(ctx->mutex);
+        done = j->result_done;
+        if (!done)
+            return fail(ctx, DXMC_ERR_STATE, "the job has no asynchronous result pending");
+    }
+    const cudaError_t e = cudaEventSynchronize(done);
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    cudaEventDestroy(done);
+    j->result_done = nullptr;
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "asynchronous result");
+    const dev::JobCounters c = *reinterpret_cast<dev::JobCounters*>(reinterpret_cast<unsigned char*>(j->cancel_host) + 16);
+    const uint64_t nv = j->world->params.n_voxels;
+    if (stats) {
+        stats->histories = c.histories_done;
+        stats->steps = c.steps;
+        stats->deposits = c.deposits;
+        stats->rejection_overflows = c.overflows;
+        float ms = 0, jms = 0;
+        cudaEventElapsedTime(&ms, j->start, j->stop);
+        cudaEventElapsedTime(&jms, j->begin, j->stop);
+        stats->kernel_ms = ms;
+        stats->job_ms = jms;
+    }
+    if (j->cancelled) {
+        // transport.hpp:176-185: a cancelled run reports zeros
+        if (j->result_dose)
+            std::memset(j->result_dose, 0, nv * j->result_elem);
+        if (j->result_variance)
+            std::memset(j->result_variance, 0, nv * j->result_elem);
+        if (j->result_events)
+            std::memset(j->result_events, 0, nv * sizeof(uint32_t));
+        return fail(ctx, DXMC_ERR_CANCELLED, "job was cancelled");
+    }
+    if (c.overflows)
+        return fail(ctx, DXMC_ERR_REJECTION_CAP, "sampling loops hit the rejection cap in " + std::to_string(c.overflows) + " events");
+    return DXMC_OK;
+}
+
 int dxmc_gpu_job_release(dxmc_job* j)
 {
     if (!j)
@@ -2442,6 +2565,8 @@ int dxmc_gpu_job_release(dxmc_job* j)
     cudaSetDevice(ctx->device);
     if (j->stop)
         cudaEventSynchronize(j->stop);
+    if (j->result_done)
+        cudaEventSynchronize(j->result_done); // the asynchronous result still reads the tallies
     free_job_device(j);
     ctx->in_use -= j->bytes;
     j->bytes = 0;
@@ -2457,6 +2582,11 @@ void dxmc_gpu_job_free(dxmc_job* j)
     cudaSetDevice(ctx->device);
     if (j->stop)
         cudaEventSynchronize(j->stop); // a batched job runs on its engine's stream
+    if (j->result_done) {
+        cudaEventSynchronize(j->result_done);
+        cudaEventDestroy(j->result_done);
+        j->result_done = nullptr;
+    }
     cudaStreamSynchronize(ctx->stream);
     free_job_device(j);
     cudaStreamSynchronize(ctx->stream);

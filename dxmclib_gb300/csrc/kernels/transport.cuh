@@ -185,6 +185,10 @@ cudaError_t launch_postprocess(const double* tally, const WorldParams& w, uint64
 cudaError_t launch_postprocess_records(const TallyRecord* records, const WorldParams& w, uint64_t n,
     int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance,
     uint32_t* counts_out, cudaStream_t stream);
+// The same with float results (Result<float>: 12 bytes per voxel with the counts).
+cudaError_t launch_postprocess_records_f32(const TallyRecord* records, const WorldParams& w, uint64_t n,
+    int mode, double histories, double voxel_volume_cm3, double calibration, float* dose, float* variance,
+    uint32_t* counts_out, cudaStream_t stream);
 cudaError_t launch_postprocess_f32(const float* tally, const WorldParams& w, uint64_t n,
     int mode, double histories, double voxel_volume_cm3, double calibration, double* dose, double* variance,
     const uint32_t* counts, uint32_t* counts_out, cudaStream_t stream);

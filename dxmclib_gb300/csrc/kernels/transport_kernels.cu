@@ -1171,10 +1171,12 @@ namespace {
         }
     }
 
-    // Post-processing from tally records: one 32-byte record read per voxel.
+    // Post-processing from tally records: one 32-byte record read per voxel; the
+    // results in double (Result<double>) or float (Result<float>), computed in double.
+    template <typename OutT>
     __global__ void postprocess_records_kernel(const TallyRecord* __restrict__ rec, const Voxel* __restrict__ voxels,
         const uint8_t* __restrict__ palette_index, const PaletteEntry* __restrict__ palette, uint64_t n, int mode,
-        double histories, double voxel_volume_cm3, double calibration, double* __restrict__ dose, double* __restrict__ variance,
+        double histories, double voxel_volume_cm3, double calibration, OutT* __restrict__ dose, OutT* __restrict__ variance,
         uint32_t* __restrict__ counts_out)
     {
         const double h_inv = 1.0 / (histories - 1.0);
@@ -1195,9 +1197,9 @@ namespace {
                 v = de > 0.0 ? ee * f * f : 0.0;
             }
             if (dose)
-                dose[i] = d;
+                dose[i] = static_cast<OutT>(d);
             if (variance)
-                variance[i] = v;
+                variance[i] = static_cast<OutT>(v);
             if (counts_out)
                 counts_out[i] = __ldcs(&rec[i].events);
         }
@@ -1413,7 +1415,18 @@ cudaError_t launch_postprocess_records(const TallyRecord* records, const WorldPa
 {
     const int block = 256;
     const int grid = static_cast<int>(std::min<uint64_t>((n + block - 1) / block, 152ull * 16));
-    postprocess_records_kernel<<<grid, block, 0, stream>>>(records, w.palette_index ? nullptr : w.voxels, w.palette_index,
+    postprocess_records_kernel<double><<<grid, block, 0, stream>>>(records, w.palette_index ? nullptr : w.voxels, w.palette_index,
+        w.palette, n, mode, histories, voxel_volume_cm3, calibration, dose, variance, counts_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_postprocess_records_f32(const TallyRecord* records, const WorldParams& w, uint64_t n, int mode,
+    double histories, double voxel_volume_cm3, double calibration, float* dose, float* variance, uint32_t* counts_out,
+    cudaStream_t stream)
+{
+    const int block = 256;
+    const int grid = static_cast<int>(std::min<uint64_t>((n + block - 1) / block, 152ull * 16));
+    postprocess_records_kernel<float><<<grid, block, 0, stream>>>(records, w.palette_index ? nullptr : w.voxels, w.palette_index,
         w.palette, n, mode, histories, voxel_volume_cm3, calibration, dose, variance, counts_out);
     return cudaGetLastError();
 }

@@ -432,6 +432,26 @@ int dxmc_gpu_radiological_path(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* l
 int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_job_desc* job,
     double* tally, uint32_t* n_events, dxmc_job_stats* stats);
 
+/* Asynchronous results.  dxmc_gpu_job_result_async queues the post-processing
+ * (output_mode and calibration as dxmc_gpu_job_result) and the copies into the
+ * caller's buffers on the context's result stream, ordered after the job's
+ * kernel, and returns at once: the caller may submit the next job meanwhile and
+ * the copies run on the copy engine beside its transport.  result_type
+ * DXMC_RESULT_F64 writes double dose / variance (Result<double>, 20 bytes per
+ * voxel with the counts), DXMC_RESULT_F32 float ones (Result<float>, 12 bytes;
+ * needs an FP64 tally).  Any of dose, variance, n_events may be NULL; page-locked
+ * buffers make the copies asynchronous.  The buffers must stay valid until
+ * dxmc_gpu_job_result_wait returns, which waits, fills stats and returns the
+ * job's status as dxmc_gpu_job_result does (zeroed buffers and
+ * DXMC_ERR_CANCELLED for a cancelled job).  One asynchronous result per job at
+ * a time.  Together they replace the result hand-back of Transport<T>::operator()
+ * (transport.hpp:176-201) for callers that overlap jobs. */
+#define DXMC_RESULT_F64 0
+#define DXMC_RESULT_F32 1
+int dxmc_gpu_job_result_async(dxmc_job* job, int output_mode, double calibration, int result_type, void* dose,
+    void* variance, uint32_t* n_events);
+int dxmc_gpu_job_result_wait(dxmc_job* job, dxmc_job_stats* stats);
+
 /* ---- device probes for component parity tests ----------------------------- */
 /* Runs the device LUT lookup on energies[n]: out_att[n*3], out_maxinv[n]. */
 int dxmc_gpu_probe_lut(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, const double* energies, int n,
