@@ -163,6 +163,22 @@ def committed_traffic():
     return None
 
 
+def issue_roofline(profile, histories_per_s: float, clocks, sms: int = 152):
+    """The instruction-issue roofline of the transport kernel, the one that binds
+    it: warp instructions per history (committed ncu capture) x histories/s
+    against one warp instruction per cycle per SM sub-partition (4 per SM) at the
+    SM clock sampled during the timed region."""
+    if not profile or "warp_instructions_per_history" not in profile:
+        return None
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    peak = sms * 4 * mhz * 1e6
+    achieved = profile["warp_instructions_per_history"] * histories_per_s
+    return {"achieved": achieved, "peak": peak, "unit": "warp instructions/s", "frac": achieved / peak,
+            "warp_instructions_per_history": profile["warp_instructions_per_history"],
+            "active_lanes_per_instruction": profile.get("active_lanes_per_instruction"),
+            "sm_mhz": mhz}
+
+
 def build_workload(histories: int):
     from dxmclib_gb300 import workloads
     return workloads.ct_helical(histories=histories)
@@ -222,10 +238,14 @@ def bench_config(args, n_hist: int, n_exposures: int) -> dict:
             "woodcock_burst": args.burst or "default", "tracking": args.tracking}
 
 
-def serving_measurement(ctx, n_jobs: int, rates, chains: int, seed: int = 20261205) -> dict:
+def serving_measurement(ctx, n_jobs: int, rates, chains: int, seconds_per_rate: float = 30.0,
+                        seed: int = 20261205) -> dict:
     """Mixed-stream serving (pencil / DX / CT jobs, Poisson arrivals at each rate)
     through DoseServer against the plain one-job-per-call path (Transport: upload
-    the world, run one job, copy the result back) on the same jobs and seeds."""
+    the world, run one job, copy the result back) on the same jobs and seeds.
+    Each rate serves the first min(n_jobs, rate x seconds_per_rate) jobs of the
+    stream (at least 20); a saturating burst submits all n_jobs at once, so its
+    served rate is the server's capacity rather than the offered load."""
     import queue as _queue
     import threading
     import dxmclib_gb300 as dx
@@ -249,11 +269,15 @@ def serving_measurement(ctx, n_jobs: int, rates, chains: int, seed: int = 202612
         server.submit(j.world, j.source, seed=1, world_key=j.world_key).result().release()
         j.source.setHistoriesPerExposure(hpe)
 
-    def run_stream(rate):
-        # the same jobs at another arrival rate (the job draws do not depend on the rate)
-        arrivals = np.cumsum(np.random.default_rng(seed).exponential(1.0 / rate, len(base)))
+    def run_stream(rate, jobs):
+        # the same jobs at another arrival rate (the job draws do not depend on the rate);
+        # rate None: every job arrives at once
+        if rate is None:
+            arrivals = np.zeros(len(jobs))
+        else:
+            arrivals = np.cumsum(np.random.default_rng(seed).exponential(1.0 / rate, len(jobs)))
         server.reset_metrics()
-        served = [None] * len(base)
+        served = [None] * len(jobs)
         done_q = _queue.Queue()
 
         def consumer():  # the client reads a sample of every result, then hands the buffers back
@@ -269,7 +293,7 @@ def serving_measurement(ctx, n_jobs: int, rates, chains: int, seed: int = 202612
         reader = threading.Thread(target=consumer, daemon=True)
         reader.start()
         t0 = time.perf_counter()
-        for i, j in enumerate(base):
+        for i, j in enumerate(jobs):
             delay = arrivals[i] - (time.perf_counter() - t0)
             if delay > 0:
                 time.sleep(delay)
@@ -281,13 +305,18 @@ def serving_measurement(ctx, n_jobs: int, rates, chains: int, seed: int = 202612
         reader.join()
         return m, served
 
+    def line(rate, n, m):
+        return {"rate_jobs_per_s": rate, "jobs": n, "served_histories_per_s": m["histories_per_s"],
+                "p50_ms": m["p50_ms"], "p99_ms": m["p99_ms"], "mean_queue_ms": m["mean_queue_ms"],
+                "batches": m["batches"], "mean_batch_jobs": m["mean_batch_jobs"]}
+
     sweep = []
-    served = None
     for rate in sorted(rates):
-        m, served = run_stream(rate)
-        sweep.append({"rate_jobs_per_s": rate, "served_histories_per_s": m["histories_per_s"], "p50_ms": m["p50_ms"],
-                      "p99_ms": m["p99_ms"], "mean_queue_ms": m["mean_queue_ms"], "batches": m["batches"],
-                      "mean_batch_jobs": m["mean_batch_jobs"]})
+        n = min(len(base), max(20, int(math.ceil(rate * seconds_per_rate))))
+        m, _ = run_stream(rate, base[:n])
+        sweep.append(line(rate, n, m))
+    m, served = run_stream(None, base)
+    saturation = line("burst", len(base), m)
     server.close()
 
     # plain: one Transport call per job, back to back (no arrival gaps)
@@ -331,17 +360,54 @@ def serving_measurement(ctx, n_jobs: int, rates, chains: int, seed: int = 202612
         dw.close()
     hist = int(sum(j.histories for j in base))
     kinds = {k: sum(1 for j in base if j.kind == k) for k in ("pencil", "dx", "ct")}
-    top = sweep[-1]
+    plain = hist / plain_s
     return {"workload": "mixed stream: 40% pencil 64^3, 40% DX 128^3-256^3, 20% CT 512x512x(100-400); "
                         "histories log-uniform 1e6-1e8; seeded phantom pool",
             "jobs": len(base), "kinds": kinds, "histories": hist, "chains": chains,
-            "rate_jobs_per_s": top["rate_jobs_per_s"],
-            "served_histories_per_s": top["served_histories_per_s"], "plain_histories_per_s": hist / plain_s,
-            "served_over_plain": top["served_histories_per_s"] / (hist / plain_s),
+            "seconds_per_rate": seconds_per_rate,
+            "saturation": saturation,
+            "served_histories_per_s": saturation["served_histories_per_s"], "plain_histories_per_s": plain,
+            "served_over_plain": saturation["served_histories_per_s"] / plain,
             "plain_resident_histories_per_s": hist / resident_s,
-            "served_over_plain_resident": top["served_histories_per_s"] / (hist / resident_s),
-            "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"], "sweep": sweep,
+            "served_over_plain_resident": saturation["served_histories_per_s"] / (hist / resident_s),
+            "p50_ms": saturation["p50_ms"], "p99_ms": saturation["p99_ms"], "sweep": sweep,
             "max_rel_dose_diff_vs_plain": worst}
+
+
+def layout8_measurement(ctx, src, model: int, steps: int = 3, seed: int = 20261206) -> dict:
+    """The CT helical job on the same phantom with continuous per-voxel densities
+    (each voxel's density times a seeded factor uniform in [0.95, 1.05]), as a
+    CT-derived phantom has them: far more than 256 distinct voxels, so the world
+    takes the 8-byte voxel layout (f32 density, u8 material, u8 measurement)."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    from dxmclib_gb300.workloads import ct_world
+    w = ct_world(200)
+    dens = (w.densityArray() * np.random.default_rng(seed).uniform(0.95, 1.05, w.size())).astype(np.float32)
+    w.setDensityArray(dens)
+    # (the densities alone rule out the palette; layout 1 states it)
+    dw = dx.DeviceWorld(ctx, w, layout=1)
+    dl = dx.DeviceLut(ctx, dx.LutBlob(w.materialMap(), dw.max_density(), src.maxPhotonEnergyProduced()))
+    ex = src.exposures(w.directionCosines())
+    n_hist = int(np.sum(ex.n_histories))
+    ms, st = [], None
+    for k in range(steps + 1):
+        job = dx.Job(ctx, dw, dl, ex, src.spectrum(), src.heel(), None, seed=500 + k, model=model)
+        job.wait()
+        s = A.JobStats()
+        A.check(ctx.lib.dxmc_gpu_job_result(job.handle, A.OUTPUT_RAW, 1.0, None, None, None, dx.api.C.byref(s)),
+                ctx.handle, "job_result")
+        job.close()
+        if k:
+            ms.append(s.kernel_ms)
+            st = s
+    out = {"workload": "ct_helical_512x512x200 with continuous densities (x U[0.95, 1.05] per voxel)",
+           "voxel_layout": "8-byte", "distinct_densities": int(np.unique(dens).size),
+           "histories_per_s": n_hist / (float(np.mean(ms)) / 1e3), "kernel_ms": float(np.mean(ms)),
+           "steps_per_history": st.steps / n_hist, "deposits_per_history": st.deposits / n_hist}
+    dl.close()
+    dw.close()
+    return out
 
 
 def siddon_measurement(ctx, dworld, dlut, world, n_rays: int = 1 << 20, seed: int = 5) -> dict:
@@ -458,11 +524,14 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched DX leg")
     ap.add_argument("--no-precision", action="store_true", help="skip the tally-precision study")
     ap.add_argument("--no-siddon", action="store_true", help="skip the Siddon traversal leg")
+    ap.add_argument("--no-layout8", action="store_true", help="skip the 8-byte voxel layout leg")
     ap.add_argument("--precision-histories", type=float, default=1e9)
     ap.add_argument("--precision-slices", type=int, default=400)
     ap.add_argument("--batch-jobs", type=int, default=64)
-    ap.add_argument("--serve-jobs", type=int, default=48)
-    ap.add_argument("--serve-rates", default="25,100,200", help="Poisson arrival rates of the mixed stream (jobs/s)")
+    ap.add_argument("--serve-jobs", type=int, default=500)
+    ap.add_argument("--serve-rates", default="1,10,25,100,200", help="Poisson arrival rates of the mixed stream (jobs/s)")
+    ap.add_argument("--serve-seconds", type=float, default=30.0,
+                    help="each rate serves at most rate x this many jobs of the stream")
     ap.add_argument("--serve-chains", type=int, default=4)
     args = ap.parse_args()
     ws, rank, local = _dist()
@@ -580,9 +649,15 @@ def main():
     value = replica_throughput(ws, n_hist, args.steps, total_ms / 1e3)
     steps_per_hist = float(np.mean([s.steps for s in stats])) / n_hist
     deps_per_hist = float(np.mean([s.deposits for s in stats])) / n_hist
-    step_bytes = 13.0 if tracking == A.TRACKING_LOCAL else 5.0
-    alg_bytes = step_bytes * np.mean([s.steps for s in stats]) + 20.0 * np.mean([s.deposits for s in stats])
-    achieved = alg_bytes / (float(kern_ms.mean()) / 1e3) / 1e9
+    # algorithmic bytes per launch: 5 B per Woodcock step inside the grid (u8 material +
+    # f32 density) and 20 B per deposit (FP64 energy, FP64 energy^2, u32 count); the
+    # local-majorant grid adds an 8-byte cell per step, reported beside it
+    mean_steps = float(np.mean([s.steps for s in stats]))
+    mean_deps = float(np.mean([s.deposits for s in stats]))
+    alg_bytes = 5.0 * mean_steps + 20.0 * mean_deps
+    alg_bytes_cells = alg_bytes + (8.0 * mean_steps if tracking == A.TRACKING_LOCAL else 0.0)
+    kernel_s = float(kern_ms.mean()) / 1e3
+    achieved = alg_bytes / kernel_s / 1e9
     peak, peak_kind = measured_peaks()
     traffic = committed_traffic()
 
@@ -600,18 +675,28 @@ def main():
     for m in world.materialMap():
         e2e_world.addMaterialToMap(m)
     assert e2e_world.isValid()
-    out_d = torch.empty(n_vox, dtype=torch.float64, pin_memory=True).numpy()
-    out_v = torch.empty(n_vox, dtype=torch.float64, pin_memory=True).numpy()
-    out_n = torch.empty(n_vox, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
-    e2e_steps = max(1, min(args.steps, 3))
+    # results as a Transport<float> caller receives them (Result<float>: float dose and
+    # variance, u32 counts = 12 B per voxel), into two page-locked buffer sets so that
+    # job k's result copies run on the copy engine while job k + 1 is transported
+    def pinned_result():
+        return (torch.empty(n_vox, dtype=torch.float32, pin_memory=True).numpy(),
+                torch.empty(n_vox, dtype=torch.float32, pin_memory=True).numpy(),
+                torch.empty(n_vox, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32))
+    out_bufs = [pinned_result(), pinned_result()]
+    e2e_steps = max(1, min(args.steps, 5))
 
-    def e2e_step(seed):
+    def e2e_submit(seed, buf):
         dw = dx.DeviceWorld(ctx, e2e_world, layout=args.layout)
         bl = dx.LutBlob.cached(e2e_world.materialMap(), dw.max_density(), src.maxPhotonEnergyProduced())
         dl = dx.DeviceLut(ctx, bl)
         ex = src.exposures(e2e_world.directionCosines())
         job = dx.Job(ctx, dw, dl, ex, src.spectrum(), src.heel(), None, seed=seed, model=args.model)
-        job.result(A.OUTPUT_EV_PER_HISTORY, out=(out_d, out_v, out_n))
+        job.result_async(A.OUTPUT_EV_PER_HISTORY, out=buf, dtype=np.float32)
+        return job, dl, dw
+
+    def e2e_finish(handle):
+        job, dl, dw = handle
+        job.result_wait()
         job.close()
         dl.close()
         dw.close()
@@ -620,17 +705,26 @@ def main():
         e2e_steps = 0
         e2e_s = float("nan")
     else:
-        e2e_step(1)
+        e2e_finish(e2e_submit(1, out_bufs[0]))
         barrier()
         t0 = time.perf_counter()
-        for s in range(e2e_steps):
-            e2e_step(3000 + s)
+        pending = None
+        for step in range(e2e_steps):
+            h = e2e_submit(3000 + step, out_bufs[step % 2])
+            if pending is not None:
+                e2e_finish(pending)
+            pending = h
+        e2e_finish(pending)
         barrier()
         e2e_s = time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_s, dist)
     e2e_value = replica_throughput(ws, n_hist, e2e_steps, e2e_s) if e2e_steps else None
     h2d = n_vox * 5 + len(exposures) * 80
-    d2h = n_vox * (8 + 8 + 4)
+    d2h = n_vox * (4 + 4 + 4)
+
+    layout8 = None
+    if rank == 0 and not args.no_layout8:
+        layout8 = layout8_measurement(ctx, src, args.model)
 
     siddon = None
     if rank == 0 and not args.no_siddon:
@@ -650,7 +744,7 @@ def main():
     serving = None
     if rank == 0 and not args.no_serve:
         serving = serving_measurement(ctx, args.serve_jobs, [float(r) for r in args.serve_rates.split(",")],
-                                      args.serve_chains)
+                                      args.serve_chains, args.serve_seconds)
 
 
     if rank == 0:
@@ -665,7 +759,12 @@ def main():
                          # launch, scaled by histories (traffic grows in proportion)
                          "traffic": None if not traffic else traffic["dram_bytes_per_history"] * n_hist,
                          "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": float(kern_ms.mean()),
-                         "steps_per_history": steps_per_hist, "deposits_per_history": deps_per_hist},
+                         "steps_per_history": steps_per_hist, "deposits_per_history": deps_per_hist,
+                         "bytes_formula": "5 B x steps + 20 B x deposits",
+                         "with_majorant_cells": {"bytes_per_launch": alg_bytes_cells,
+                                                 "achieved": alg_bytes_cells / kernel_s / 1e9,
+                                                 "frac": alg_bytes_cells / kernel_s / 1e9 / peak},
+                         "issue": issue_roofline(traffic, n_hist / kernel_s, clocks.summary())},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "histories/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "steps": e2e_steps},
@@ -675,6 +774,7 @@ def main():
             "batching": batching,
             "precision": precision,
             "siddon": siddon,
+            "layout_8byte": layout8,
             "serving": serving,
         }
         print(json.dumps(line), flush=True)
