@@ -20,6 +20,7 @@
 #include <cstring>
 #include <limits>
 #include <mutex>
+#include <utility>
 #include <numeric>
 #include <thread>
 #include <type_traits>
@@ -209,6 +210,7 @@ double run_port(const PortLut* lut, const PortWorld* w, const PortSource* s, int
     job.var = out_v;
     job.nev = n_events;
     const int nt = n_threads > 0 ? n_threads : std::max(1u, std::thread::hardware_concurrency());
+    job.make_pool(job.n_exposures, static_cast<std::uint64_t>(nt));
     std::vector<std::uint64_t> steps(nt, 0);
     const auto t0 = std::chrono::steady_clock::now();
     std::vector<std::thread> threads;
