@@ -3,11 +3,14 @@
 //
 // Every history draws from its own xoshiro128+ generator (Blackman and Vigna,
 // "Scrambled linear pseudorandom number generators", 2021).  Its 128-bit state
-// is two outputs of SplitMix64 (Steele, Lea and Flood, "Fast splittable
-// pseudorandom number generators", OOPSLA 2014) started from the job seed
-// combined with the history id by a Weyl step: the seeding Vigna recommends for
-// the xoshiro family.  A history's stream depends on (seed, history) only, so a
-// job can be split, batched or resumed at any history id.
+// is the next two outputs of SplitMix64 (Steele, Lea and Flood, "Fast
+// splittable pseudorandom number generators", OOPSLA 2014), the seeding Vigna
+// recommends for the xoshiro family, from a starting counter of the mixed job
+// seed XOR the history id.  The counters SplitMix64 visits for two histories
+// (start + 1 and 2 Weyl increments) never coincide: starting counters of
+// histories below 2^62 differ by less than 2^62, a Weyl increment is larger.
+// A history's stream depends on (seed, history) only, so a job can be split,
+// batched or resumed at any history id.
 #pragma once
 
 #include <cstdint>
@@ -35,7 +38,8 @@ DXMC_HD inline std::uint64_t splitmix64(std::uint64_t& x)
 // all-zero state is excluded by setting the lowest bit of the last word.
 DXMC_HD inline void stream_seed(std::uint64_t seed, std::uint64_t history, std::uint32_t out[4])
 {
-    std::uint64_t x = seed ^ (history * SPLITMIX_GAMMA);
+    std::uint64_t k = seed;
+    std::uint64_t x = splitmix64(k) ^ history;
     const std::uint64_t a = splitmix64(x);
     const std::uint64_t b = splitmix64(x);
     out[0] = static_cast<std::uint32_t>(a);

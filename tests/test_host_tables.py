@@ -96,24 +96,29 @@ def _splitmix64(x):
 
 
 def test_stream_seed_known_answers(lib):
-    """The per-history stream state (SplitMix64 of seed ^ history * gamma, two
-    outputs, lowest bit of the last word set) against a Python restatement, for
-    seeds and history ids across the 64-bit range."""
+    """The per-history stream state (SplitMix64 from the counter mix(seed) ^ history,
+    two outputs, lowest bit of the last word set) against a Python restatement, for
+    seeds and history ids across the 64-bit range; and neighbouring histories share
+    no state word (an earlier seeding, seed ^ history * gamma, let history h's
+    second word equal history h + 1's first for many seeds)."""
     from dxmclib_gb300 import _capi as A
-    m = (1 << 64) - 1
     # SplitMix64 itself: its first two outputs from counter 0
     x, a = _splitmix64(0)
     x, b = _splitmix64(x)
     assert (a, b) == (0xE220A8397B1DCDAF, 0x6E789E6AA1B965F4)
-    for seed in (0, 1, 2026, 0xFFFFFFFFFFFFFFFF, 0x123456789ABCDEF0):
-        for h in (0, 1, 255, 256, 1 << 32, (1 << 64) - 1):
-            x = seed ^ ((h * 0x9E3779B97F4A7C15) & m)
+    for seed in (0, 1, 11, 2026, 0xFFFFFFFFFFFFFFFF, 0x123456789ABCDEF0):
+        words = set()
+        for h in (0, 1, 2, 3, 255, 256, 1 << 32, (1 << 64) - 1):
+            _, key = _splitmix64(seed)
+            x = key ^ h
             x, a = _splitmix64(x)
             x, b = _splitmix64(x)
             want = [a & 0xFFFFFFFF, a >> 32, b & 0xFFFFFFFF, (b >> 32) | 1]
             o = np.zeros(4, np.uint32)
             assert lib.dxmc_stream_seed(seed, h, o.ctypes.data_as(A.U32P)) == 0
             assert o.tolist() == want, (seed, h)
+            assert not words & {a, b}, (seed, h)
+            words |= {a, b}
 
 
 def _dx_source():
