@@ -89,6 +89,30 @@ struct MajorantCache {
     dev::MajorantGrid grid {};
 };
 
+// Where in the context's streams an object was last read (see dxmc_world::usage).
+struct Usage {
+    cudaEvent_t on_stream = nullptr; // after the last single job on the context stream
+    cudaEvent_t on_results = nullptr; // after the last result post-processing on the result stream
+    bool batched = false;             // read by a batch: wait for all streams
+    cudaError_t mark(cudaEvent_t& ev, cudaStream_t s)
+    {
+        if (!ev) {
+            const cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+            if (e != cudaSuccess)
+                return e;
+        }
+        return cudaEventRecord(ev, s);
+    }
+    void destroy()
+    {
+        if (on_stream)
+            cudaEventDestroy(on_stream);
+        if (on_results)
+            cudaEventDestroy(on_results);
+        on_stream = on_results = nullptr;
+    }
+};
+
 struct dxmc_world {
     dxmc_gpu_ctx* ctx = nullptr;
     std::vector<MajorantCache> majorants;
@@ -105,6 +129,11 @@ struct dxmc_world {
     bool has_measurement = false;
     uint64_t bytes = 0;
     dev::WorldParams params {};
+    // the last use of the world by single jobs on the context stream and by the
+    // post-processing of asynchronous results on the result stream: freeing the
+    // world waits for these, not for unrelated work; a world used by a batch
+    // (chain or engine streams) waits for every stream of the context
+    Usage usage;
 };
 
 struct dxmc_lut {
@@ -121,6 +150,7 @@ struct dxmc_lut {
     float band_log0 = 1.0f, band_inv_dlog = 0.0f; // log10 of the first edge's base (10 keV) and 1 / log10 step
     std::vector<float> majorant_ratio;
     float mu_ref[dev::MAJORANT_MAX_BANDS] {};
+    Usage usage; // as the world's
 };
 
 struct dxmc_job {
@@ -500,6 +530,7 @@ extern "C" {
 
 namespace {
 void sync_ctx_streams(dxmc_gpu_ctx* ctx);
+void wait_unused(dxmc_gpu_ctx* ctx, const Usage& u);
 void release_engines(dxmc_gpu_ctx* ctx);
 int wait_event(dxmc_gpu_ctx* ctx, cudaEvent_t ev, int64_t timeout_ms, const char* what);
 int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool build, const dev::MajorantGrid** out);
@@ -850,7 +881,7 @@ void dxmc_gpu_world_free(dxmc_world* w)
         return;
     std::lock_guard<std::mutex> lock(w->ctx->mutex);
     cudaSetDevice(w->ctx->device);
-    sync_ctx_streams(w->ctx); // no queued batch or job still reads the grid
+    wait_unused(w->ctx, w->usage); // no queued batch, job or result post-processing still reads the grid
     if (w->voxels)
         cudaFreeAsync(w->voxels, w->ctx->stream);
     if (w->palette_index)
@@ -861,7 +892,7 @@ void dxmc_gpu_world_free(dxmc_world* w)
         cudaFreeAsync(m.cells, w->ctx->stream);
         w->ctx->in_use -= m.bytes;
     }
-    cudaStreamSynchronize(w->ctx->stream);
+    w->usage.destroy();
     w->ctx->in_use -= w->bytes;
     delete w;
 }
@@ -1039,9 +1070,9 @@ void dxmc_gpu_lut_free(dxmc_lut* lut)
         return;
     std::lock_guard<std::mutex> lock(lut->ctx->mutex);
     cudaSetDevice(lut->ctx->device);
-    sync_ctx_streams(lut->ctx); // no queued batch or job still reads the table
+    wait_unused(lut->ctx, lut->usage); // no queued batch or job still reads the table
     cudaFreeAsync(lut->image, lut->ctx->stream);
-    cudaStreamSynchronize(lut->ctx->stream);
+    lut->usage.destroy();
     lut->ctx->in_use -= lut->bytes;
     delete lut;
 }
@@ -1713,7 +1744,11 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
     if (rc != DXMC_OK)
         return rc;
     const LaunchPlan L = plan_launch(ctx, world, lut, jd, p);
-    const cudaError_t e = enqueue_job(j, p, jd->model, chunk, j->queue, L, ctx->stream, false);
+    cudaError_t e = enqueue_job(j, p, jd->model, chunk, j->queue, L, ctx->stream, false);
+    if (e == cudaSuccess)
+        e = world->usage.mark(world->usage.on_stream, ctx->stream);
+    if (e == cudaSuccess)
+        e = lut->usage.mark(lut->usage.on_stream, ctx->stream);
     if (e != cudaSuccess) {
         cudaStreamSynchronize(ctx->stream);
         discard_job(j);
@@ -2032,6 +2067,8 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
         const dxmc_batch_entry& entry = entries[i];
         if (!entry.world || !entry.lut || !entry.job)
             return abort(fail(ctx, DXMC_ERR_INVALID, "batch entry " + std::to_string(i) + " is incomplete"));
+        entry.world->usage.batched = true;
+        entry.lut->usage.batched = true;
         dxmc_job* j = nullptr;
         const int rc = persistent
             ? prepare_job(ctx, entry.world, entry.lut, entry.job, QueueMode::none, 0, &j, g->h_params[i], chunks[i])
@@ -2233,6 +2270,21 @@ namespace {
 
 // Waits for the batch engines' streams as well as the context stream (before
 // freeing resources that a queued batch may still read).
+// Waits until no queued work reads an object: its recorded last uses, or every
+// stream of the context when a batch read it.  Later work on the streams is not
+// waited for, so an object can be freed while the next job runs.
+void wait_unused(dxmc_gpu_ctx* ctx, const Usage& u)
+{
+    if (u.batched) {
+        sync_ctx_streams(ctx);
+        return;
+    }
+    if (u.on_stream)
+        cudaEventSynchronize(u.on_stream);
+    if (u.on_results)
+        cudaEventSynchronize(u.on_results);
+}
+
 void sync_ctx_streams(dxmc_gpu_ctx* ctx)
 {
     cudaStreamSynchronize(ctx->stream);
@@ -2496,6 +2548,8 @@ int dxmc_gpu_job_result_async(dxmc_job* j, int output_mode, double calibration, 
         e = cudaEventCreateWithFlags(&j->result_done, cudaEventDisableTiming);
     if (e == cudaSuccess)
         e = cudaEventRecord(j->result_done, s);
+    if (e == cudaSuccess) // DOSE post-processing reads the world's densities
+        e = j->world->usage.mark(j->world->usage.on_results, s);
     if (e != cudaSuccess) {
         if (j->result_done) {
             cudaEventDestroy(j->result_done);
@@ -2587,9 +2641,9 @@ void dxmc_gpu_job_free(dxmc_job* j)
         cudaEventDestroy(j->result_done);
         j->result_done = nullptr;
     }
-    cudaStreamSynchronize(ctx->stream);
+    // the job's kernels and copies are done: its buffers go back to the pool in the
+    // context stream's order, without waiting for later jobs
     free_job_device(j);
-    cudaStreamSynchronize(ctx->stream);
     if (j->cancel_host)
         cudaFreeHost(j->cancel_host);
     if (j->begin)
