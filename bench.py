@@ -257,7 +257,8 @@ def serving_measurement(ctx, n_jobs: int, rates, chains: int, seconds_per_rate: 
     def sample(dose):
         return dose[probe[probe < dose.size]].copy(), float(np.sum(dose))
 
-    server = DoseServer(ctx, chains=chains)
+    # results as Result<float> (a Transport<float> caller's): 12 bytes per voxel over the link
+    server = DoseServer(ctx, chains=chains, result_dtype=np.float32)
     base = serving_stream(n_jobs=n_jobs, rate_per_s=max(rates), seed=seed)
     # warm-up: one small job per phantom makes every world and LUT resident
     warm = {}
