@@ -62,6 +62,50 @@ constexpr int SAMPLING_LEVELS = 512;
 
 struct BatchEngines;
 
+// Page-locked, mapped host blocks that hold a job's cancel flag (byte 0) and the
+// host copy of its counters (byte 16).  Freeing page-locked memory waits for all
+// work on the device, which would make freeing one job wait for the jobs queued
+// after it: the blocks go back to this list and are released with the context.
+struct PinnedSlots {
+    static constexpr size_t SLOT = 128;
+    static constexpr int PER_CHUNK = 64;
+    static_assert(16 + sizeof(dev::JobCounters) <= SLOT, "a slot holds the flag and the counters");
+    std::vector<void*> chunks;
+    std::vector<std::pair<int*, int*>> free_slots; // (host, device) addresses
+    cudaError_t take(int** host, int** device)
+    {
+        if (free_slots.empty()) {
+            void* chunk = nullptr;
+            cudaError_t e = cudaHostAlloc(&chunk, SLOT * PER_CHUNK, cudaHostAllocMapped);
+            if (e != cudaSuccess)
+                return e;
+            void* dchunk = nullptr;
+            e = cudaHostGetDevicePointer(&dchunk, chunk, 0);
+            if (e != cudaSuccess) {
+                cudaFreeHost(chunk);
+                return e;
+            }
+            chunks.push_back(chunk);
+            for (int i = PER_CHUNK - 1; i >= 0; --i)
+                free_slots.emplace_back(reinterpret_cast<int*>(static_cast<unsigned char*>(chunk) + i * SLOT),
+                    reinterpret_cast<int*>(static_cast<unsigned char*>(dchunk) + i * SLOT));
+        }
+        *host = free_slots.back().first;
+        *device = free_slots.back().second;
+        free_slots.pop_back();
+        std::memset(*host, 0, SLOT);
+        return cudaSuccess;
+    }
+    void give(int* host, int* device) { free_slots.emplace_back(host, device); }
+    void release()
+    {
+        for (void* c : chunks)
+            cudaFreeHost(c);
+        chunks.clear();
+        free_slots.clear();
+    }
+};
+
 struct dxmc_gpu_ctx {
     BatchEngines* engines = nullptr; // created by the first batch
     cudaMemPool_t pool = nullptr;    // stream-ordered allocations of this context
@@ -69,6 +113,9 @@ struct dxmc_gpu_ctx {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t result_stream = nullptr; // post-processing and result copies
+    // world and table uploads: their copies and host waits do not queue behind
+    // the jobs on the context stream (uploading the next world overlaps a job)
+    cudaStream_t upload_stream = nullptr;
     dxmc_gpu_options options {};
     std::mutex mutex;
     std::string last_error;
@@ -76,7 +123,16 @@ struct dxmc_gpu_ctx {
     uint64_t in_use = 0;
     size_t max_smem_optin = 0;
     uint64_t submission = 0; // counts the calls that may build grids (job, batch, world prepare)
+    PinnedSlots pinned;      // the jobs' cancel flags and counter copies
+    // Page-locked, mapped area for the small read-backs a call waits for (palette
+    // size and table, a grid's level histogram, per-material maxima).  A kernel
+    // writes them there: a copy would queue on the copy engine behind an earlier
+    // job's result copies (hundreds of MB) and make the call wait for those.
+    unsigned char* readback_host = nullptr;
+    unsigned char* readback_dev = nullptr;
 };
+
+constexpr size_t READBACK_BYTES = 64 << 10;
 
 // Local-majorant grid of the world for one LUT (built on first use; the least
 // recently used one is freed when a world holds too many; see MajorantGrid).
@@ -202,14 +258,33 @@ int cuda_fail(dxmc_gpu_ctx* ctx, cudaError_t e, const char* what)
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+} // namespace
+extern "C" {
+namespace {
+void sync_ctx_streams(dxmc_gpu_ctx* ctx); // waits for every stream of the context (defined below)
+} // namespace
+} // extern "C"
+namespace {
+
 // Stream-ordered allocation from the context's own memory pool, which keeps
 // freed memory up to the context's budget instead of returning it to the
 // driver at every synchronisation: a world, a job's 1 GB of tallies or a grid
-// allocated again after a free costs no new mapping.
+// allocated again after a free costs no new mapping.  The pool never makes one
+// stream wait for another to reuse a block (a job's tallies would otherwise
+// wait for the previous job's result copies, an upload for the running job):
+// a block freed on another stream is reused once that free has completed, and
+// an allocation that finds no room waits for the context's streams and tries
+// again.
 template <typename T>
 cudaError_t pool_alloc(dxmc_gpu_ctx* ctx, T** ptr, size_t bytes, cudaStream_t stream)
 {
-    return cudaMallocFromPoolAsync(reinterpret_cast<void**>(ptr), bytes, ctx->pool, stream);
+    cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(ptr), bytes, ctx->pool, stream);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        sync_ctx_streams(ctx); // every pending free completes
+        e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(ptr), bytes, ctx->pool, stream);
+    }
+    return e;
 }
 
 // The device address of a page-locked host buffer (cudaHostAlloc or
@@ -361,6 +436,26 @@ __global__ void pack_voxels_kernel(const float* __restrict__ density, const uint
 
 // Sets *bad if any material index is >= n_materials (16 indices per load where
 // the array is 16-byte aligned, then the tail).
+__global__ void readback_kernel(const unsigned int* __restrict__ src, unsigned int* __restrict__ dst, uint32_t n_words)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_words; i += gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+// Enqueues the copy of `bytes` (a multiple of 4) from device memory into the
+// context's read-back area at `offset`; the host reads readback_host + offset
+// after synchronising the stream.  Caller holds the context mutex.
+cudaError_t enqueue_readback(dxmc_gpu_ctx* ctx, const void* src, size_t offset, size_t bytes, cudaStream_t s)
+{
+    if (offset % 4 || bytes % 4 || offset + bytes > READBACK_BYTES)
+        return cudaErrorInvalidValue;
+    const uint32_t words = static_cast<uint32_t>(bytes / 4);
+    const int blocks = static_cast<int>(std::min<uint32_t>((words + 255) / 256, 32));
+    readback_kernel<<<std::max(blocks, 1), 256, 0, s>>>(static_cast<const unsigned int*>(src),
+        reinterpret_cast<unsigned int*>(ctx->readback_dev + offset), words);
+    return cudaGetLastError();
+}
+
 __global__ void check_materials_kernel(const uint8_t* __restrict__ material, uint64_t n, int n_materials, unsigned int* bad)
 {
     const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
@@ -606,6 +701,12 @@ int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out)
         delete ctx;
         return DXMC_ERR_DEVICE;
     }
+    if (cudaStreamCreateWithFlags(&ctx->upload_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamDestroy(ctx->result_stream);
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return DXMC_ERR_DEVICE;
+    }
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     ctx->budget = ctx->options.memory_budget ? ctx->options.memory_budget : static_cast<uint64_t>(free_b * 0.9);
@@ -615,19 +716,38 @@ int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out)
     props.location.type = cudaMemLocationTypeDevice;
     props.location.id = ctx->device;
     uint64_t keep = ctx->budget;
+    int no_cross_stream_waits = 0;
     if (cudaMemPoolCreate(&ctx->pool, &props) != cudaSuccess
-        || cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+        || cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess
+        || cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolReuseAllowInternalDependencies, &no_cross_stream_waits)
+            != cudaSuccess) {
         if (ctx->pool)
             cudaMemPoolDestroy(ctx->pool);
+        cudaStreamDestroy(ctx->upload_stream);
         cudaStreamDestroy(ctx->result_stream);
         cudaStreamDestroy(ctx->stream);
         delete ctx;
         return DXMC_ERR_DEVICE;
     }
+    void* rb_dev = nullptr;
+    if (cudaHostAlloc(reinterpret_cast<void**>(&ctx->readback_host), READBACK_BYTES, cudaHostAllocMapped) != cudaSuccess
+        || cudaHostGetDevicePointer(&rb_dev, ctx->readback_host, 0) != cudaSuccess) {
+        if (ctx->readback_host)
+            cudaFreeHost(ctx->readback_host);
+        cudaMemPoolDestroy(ctx->pool);
+        cudaStreamDestroy(ctx->upload_stream);
+        cudaStreamDestroy(ctx->result_stream);
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return DXMC_ERR_DEVICE;
+    }
+    ctx->readback_dev = static_cast<unsigned char*>(rb_dev);
     // the no-allocation entry point must not meet a lazy module load (which
     // allocates) in its first call: load its module and the transport kernels now
     if (noalloc::preload(ctx->device) != cudaSuccess) {
+        cudaFreeHost(ctx->readback_host);
         cudaMemPoolDestroy(ctx->pool);
+        cudaStreamDestroy(ctx->upload_stream);
         cudaStreamDestroy(ctx->result_stream);
         cudaStreamDestroy(ctx->stream);
         delete ctx;
@@ -644,6 +764,9 @@ void dxmc_gpu_ctx_destroy(dxmc_gpu_ctx* ctx)
     cudaSetDevice(ctx->device);
     sync_ctx_streams(ctx);
     release_engines(ctx);
+    ctx->pinned.release();
+    cudaFreeHost(ctx->readback_host);
+    cudaStreamDestroy(ctx->upload_stream);
     cudaStreamDestroy(ctx->result_stream);
     cudaStreamDestroy(ctx->stream);
     cudaMemPoolDestroy(ctx->pool); // memory still held by objects not freed is released with them
@@ -693,53 +816,58 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     uint8_t* d_material = nullptr;
     uint8_t* d_meas = nullptr;
     unsigned int* d_bad = nullptr;
-    cudaError_t e = pool_alloc(ctx, &d_density, n * sizeof(float), ctx->stream);
+    cudaError_t e = pool_alloc(ctx, &d_density, n * sizeof(float), ctx->upload_stream);
     if (e == cudaSuccess)
-        e = pool_alloc(ctx, &d_material, n, ctx->stream);
+        e = pool_alloc(ctx, &d_material, n, ctx->upload_stream);
     if (e == cudaSuccess && d->measurement)
-        e = pool_alloc(ctx, &d_meas, n, ctx->stream);
+        e = pool_alloc(ctx, &d_meas, n, ctx->upload_stream);
     if (e == cudaSuccess)
-        e = pool_alloc(ctx, &d_bad, sizeof(unsigned int), ctx->stream);
+        e = pool_alloc(ctx, &d_bad, sizeof(unsigned int), ctx->upload_stream);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_density, d->density, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream);
+        e = cudaMemcpyAsync(d_density, d->density, n * sizeof(float), cudaMemcpyHostToDevice, ctx->upload_stream);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_material, d->material, n, cudaMemcpyHostToDevice, ctx->stream);
+        e = cudaMemcpyAsync(d_material, d->material, n, cudaMemcpyHostToDevice, ctx->upload_stream);
     if (e == cudaSuccess && d_meas)
-        e = cudaMemcpyAsync(d_meas, d->measurement, n, cudaMemcpyHostToDevice, ctx->stream);
+        e = cudaMemcpyAsync(d_meas, d->measurement, n, cudaMemcpyHostToDevice, ctx->upload_stream);
     if (e == cudaSuccess)
-        e = cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), ctx->stream);
+        e = cudaMemsetAsync(d_bad, 0, sizeof(unsigned int), ctx->upload_stream);
     unsigned int bad = 0;
     if (e == cudaSuccess) {
         const int grid = ctx->sm_count * 8;
-        check_materials_kernel<<<grid, 256, 0, ctx->stream>>>(d_material, n, d->n_materials, d_bad);
+        check_materials_kernel<<<grid, 256, 0, ctx->upload_stream>>>(d_material, n, d->n_materials, d_bad);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(&bad, d_bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) // read after the upload's last synchronisation
+        e = enqueue_readback(ctx, d_bad, 0, sizeof(unsigned int), ctx->upload_stream);
     // compact palette layout when the world has few distinct voxels
     unsigned long long* d_table = nullptr;
     unsigned int* d_count = nullptr;
     unsigned int distinct = 0;
     std::vector<dev::PaletteEntry> palette;
     if (e == cudaSuccess && d->layout == 0 && n <= 0xffffffffull) { // the compact layout indexes voxels in 32 bits
-        e = pool_alloc(ctx, &d_table, dev_palette_table_bytes(), ctx->stream);
+        e = pool_alloc(ctx, &d_table, dev_palette_table_bytes(), ctx->upload_stream);
         if (e == cudaSuccess)
-            e = pool_alloc(ctx, &d_count, sizeof(unsigned int), ctx->stream);
+            e = pool_alloc(ctx, &d_count, sizeof(unsigned int), ctx->upload_stream);
         if (e == cudaSuccess)
-            e = cudaMemsetAsync(d_table, 0, dev_palette_table_bytes(), ctx->stream);
+            e = cudaMemsetAsync(d_table, 0, dev_palette_table_bytes(), ctx->upload_stream);
         if (e == cudaSuccess)
-            e = cudaMemsetAsync(d_count, 0, sizeof(unsigned int), ctx->stream);
+            e = cudaMemsetAsync(d_count, 0, sizeof(unsigned int), ctx->upload_stream);
         if (e == cudaSuccess) {
-            palette_insert_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(d_density, d_material, d_meas, n, d_table, d_count);
+            palette_insert_kernel<<<ctx->sm_count * 8, 256, 0, ctx->upload_stream>>>(d_density, d_material, d_meas, n, d_table, d_count);
             e = cudaGetLastError();
         }
+        // the count and the table in one read-back (the table is only used when the count fits)
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(&distinct, d_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream);
+            e = enqueue_readback(ctx, d_count, 4, sizeof(unsigned int), ctx->upload_stream);
         if (e == cudaSuccess)
-            e = cudaStreamSynchronize(ctx->stream);
+            e = enqueue_readback(ctx, d_table, 64, dev_palette_table_bytes(), ctx->upload_stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(ctx->upload_stream);
+        if (e == cudaSuccess)
+            std::memcpy(&distinct, ctx->readback_host + 4, sizeof(unsigned int));
         if (e == cudaSuccess && distinct >= 1 && distinct <= static_cast<unsigned>(dev::PALETTE_MAX)) {
             std::vector<unsigned long long> table(PALETTE_TABLE);
-            e = cudaMemcpy(table.data(), d_table, dev_palette_table_bytes(), cudaMemcpyDeviceToHost);
+            std::memcpy(table.data(), ctx->readback_host + 64, dev_palette_table_bytes());
             std::vector<uint8_t> slot_index(PALETTE_TABLE, 0);
             for (int slot = 0; slot < PALETTE_TABLE && e == cudaSuccess; ++slot) {
                 const unsigned long long key = table[slot];
@@ -755,54 +883,56 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
             }
             uint8_t* d_slots = nullptr;
             if (e == cudaSuccess)
-                e = pool_alloc(ctx, &d_slots, PALETTE_TABLE, ctx->stream);
+                e = pool_alloc(ctx, &d_slots, PALETTE_TABLE, ctx->upload_stream);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(d_slots, slot_index.data(), PALETTE_TABLE, cudaMemcpyHostToDevice, ctx->stream);
+                e = cudaMemcpyAsync(d_slots, slot_index.data(), PALETTE_TABLE, cudaMemcpyHostToDevice, ctx->upload_stream);
             if (e == cudaSuccess)
-                e = pool_alloc(ctx, &w->palette_index, n, ctx->stream);
+                e = pool_alloc(ctx, &w->palette_index, n, ctx->upload_stream);
             if (e == cudaSuccess)
-                e = pool_alloc(ctx, &w->palette, dev::PALETTE_MAX * sizeof(dev::PaletteEntry), ctx->stream);
+                e = pool_alloc(ctx, &w->palette, dev::PALETTE_MAX * sizeof(dev::PaletteEntry), ctx->upload_stream);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(w->palette, palette.data(), palette.size() * sizeof(dev::PaletteEntry), cudaMemcpyHostToDevice, ctx->stream);
+                e = cudaMemcpyAsync(w->palette, palette.data(), palette.size() * sizeof(dev::PaletteEntry), cudaMemcpyHostToDevice, ctx->upload_stream);
             if (e == cudaSuccess) {
-                palette_map_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(d_density, d_material, d_meas, n, d_table, d_slots, w->palette_index);
+                palette_map_kernel<<<ctx->sm_count * 8, 256, 0, ctx->upload_stream>>>(d_density, d_material, d_meas, n, d_table, d_slots, w->palette_index);
                 e = cudaGetLastError();
             }
             if (d_slots)
-                cudaFreeAsync(d_slots, ctx->stream);
+                cudaFreeAsync(d_slots, ctx->upload_stream);
         }
     }
     // the 8-byte layout only when the compact one is not used (too many distinct voxels, or asked for)
     if (e == cudaSuccess && !w->palette_index) {
         palette.clear();
-        e = pool_alloc(ctx, &w->voxels, bytes, ctx->stream);
+        e = pool_alloc(ctx, &w->voxels, bytes, ctx->upload_stream);
         if (e == cudaSuccess) {
-            pack_voxels_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(d_density, d_material, d_meas, n, w->voxels);
+            pack_voxels_kernel<<<ctx->sm_count * 8, 256, 0, ctx->upload_stream>>>(d_density, d_material, d_meas, n, w->voxels);
             e = cudaGetLastError();
         }
     }
     if (d_table)
-        cudaFreeAsync(d_table, ctx->stream);
+        cudaFreeAsync(d_table, ctx->upload_stream);
     if (d_count)
-        cudaFreeAsync(d_count, ctx->stream);
+        cudaFreeAsync(d_count, ctx->upload_stream);
     if (d_density)
-        cudaFreeAsync(d_density, ctx->stream);
+        cudaFreeAsync(d_density, ctx->upload_stream);
     if (d_material)
-        cudaFreeAsync(d_material, ctx->stream);
+        cudaFreeAsync(d_material, ctx->upload_stream);
     if (d_meas)
-        cudaFreeAsync(d_meas, ctx->stream);
+        cudaFreeAsync(d_meas, ctx->upload_stream);
     if (d_bad)
-        cudaFreeAsync(d_bad, ctx->stream);
+        cudaFreeAsync(d_bad, ctx->upload_stream);
     if (e == cudaSuccess)
-        e = cudaStreamSynchronize(ctx->stream);
+        e = cudaStreamSynchronize(ctx->upload_stream);
+    if (e == cudaSuccess)
+        std::memcpy(&bad, ctx->readback_host, sizeof(unsigned int));
     if (e != cudaSuccess || bad) {
         if (w->voxels)
-            cudaFreeAsync(w->voxels, ctx->stream);
+            cudaFreeAsync(w->voxels, ctx->upload_stream);
         if (w->palette_index)
-            cudaFreeAsync(w->palette_index, ctx->stream);
+            cudaFreeAsync(w->palette_index, ctx->upload_stream);
         if (w->palette)
-            cudaFreeAsync(w->palette, ctx->stream);
-        cudaStreamSynchronize(ctx->stream);
+            cudaFreeAsync(w->palette, ctx->upload_stream);
+        cudaStreamSynchronize(ctx->upload_stream);
         delete w;
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "world upload");
@@ -860,13 +990,16 @@ int dxmc_gpu_world_max_density(dxmc_world* w, double* out, int n_materials)
     }
     cudaSetDevice(ctx->device);
     unsigned int* d_bits = nullptr;
-    DXMC_CUDA(ctx, pool_alloc(ctx, &d_bits, n_materials * sizeof(unsigned int), ctx->stream));
-    DXMC_CUDA(ctx, cudaMemsetAsync(d_bits, 0, n_materials * sizeof(unsigned int), ctx->stream));
-    DXMC_CUDA(ctx, dev::launch_max_density(w->voxels, w->params.n_voxels, d_bits, n_materials, ctx->stream));
-    std::vector<unsigned int> bits(n_materials);
-    DXMC_CUDA(ctx, cudaMemcpyAsync(bits.data(), d_bits, n_materials * sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream));
-    cudaFreeAsync(d_bits, ctx->stream);
-    DXMC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    DXMC_CUDA(ctx, pool_alloc(ctx, &d_bits, n_materials * sizeof(unsigned int), ctx->upload_stream));
+    DXMC_CUDA(ctx, cudaMemsetAsync(d_bits, 0, n_materials * sizeof(unsigned int), ctx->upload_stream));
+    DXMC_CUDA(ctx, dev::launch_max_density(w->voxels, w->params.n_voxels, d_bits, n_materials, ctx->upload_stream));
+    // voxel materials are below 256: the maxima beyond stay zero
+    std::vector<unsigned int> bits(n_materials, 0u);
+    const int read = std::min(n_materials, 256);
+    DXMC_CUDA(ctx, enqueue_readback(ctx, d_bits, 0, read * sizeof(unsigned int), ctx->upload_stream));
+    cudaFreeAsync(d_bits, ctx->upload_stream);
+    DXMC_CUDA(ctx, cudaStreamSynchronize(ctx->upload_stream));
+    std::memcpy(bits.data(), ctx->readback_host, read * sizeof(unsigned int));
     for (int i = 0; i < n_materials; ++i) {
         float f;
         std::memcpy(&f, &bits[i], sizeof(float));
@@ -882,12 +1015,16 @@ void dxmc_gpu_world_free(dxmc_world* w)
     std::lock_guard<std::mutex> lock(w->ctx->mutex);
     cudaSetDevice(w->ctx->device);
     wait_unused(w->ctx, w->usage); // no queued batch, job or result post-processing still reads the grid
+    // the voxels go back to the pool in the order of the upload stream (the host
+    // has waited for their readers), so the next upload reuses them without
+    // waiting for the jobs queued on the context stream; the grids were built on
+    // the context stream and go back there
     if (w->voxels)
-        cudaFreeAsync(w->voxels, w->ctx->stream);
+        cudaFreeAsync(w->voxels, w->ctx->upload_stream);
     if (w->palette_index)
-        cudaFreeAsync(w->palette_index, w->ctx->stream);
+        cudaFreeAsync(w->palette_index, w->ctx->upload_stream);
     if (w->palette)
-        cudaFreeAsync(w->palette, w->ctx->stream);
+        cudaFreeAsync(w->palette, w->ctx->upload_stream);
     for (auto& m : w->majorants) {
         cudaFreeAsync(m.cells, w->ctx->stream);
         w->ctx->in_use -= m.bytes;
@@ -1045,16 +1182,16 @@ int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* b, dxmc_lut** ou
         std::copy(std::begin(mr->mu_ref), std::end(mr->mu_ref), lut->mu_ref);
     }
     lut->bytes = img.size() * sizeof(float);
-    cudaError_t e = pool_alloc(ctx, &lut->image, lut->bytes, ctx->stream);
+    cudaError_t e = pool_alloc(ctx, &lut->image, lut->bytes, ctx->upload_stream);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(lut->image, img.data(), lut->bytes, cudaMemcpyHostToDevice, ctx->stream);
-    const cudaError_t se = cudaStreamSynchronize(ctx->stream); // img is a local buffer
+        e = cudaMemcpyAsync(lut->image, img.data(), lut->bytes, cudaMemcpyHostToDevice, ctx->upload_stream);
+    const cudaError_t se = cudaStreamSynchronize(ctx->upload_stream); // img is a local buffer
     if (e == cudaSuccess)
         e = se;
     if (e != cudaSuccess) {
         if (lut->image) {
-            cudaFreeAsync(lut->image, ctx->stream);
-            cudaStreamSynchronize(ctx->stream);
+            cudaFreeAsync(lut->image, ctx->upload_stream);
+            cudaStreamSynchronize(ctx->upload_stream);
         }
         delete lut;
         return cuda_fail(ctx, e, "lut upload");
@@ -1071,7 +1208,7 @@ void dxmc_gpu_lut_free(dxmc_lut* lut)
     std::lock_guard<std::mutex> lock(lut->ctx->mutex);
     cudaSetDevice(lut->ctx->device);
     wait_unused(lut->ctx, lut->usage); // no queued batch or job still reads the table
-    cudaFreeAsync(lut->image, lut->ctx->stream);
+    cudaFreeAsync(lut->image, lut->ctx->upload_stream);
     lut->usage.destroy();
     lut->ctx->in_use -= lut->bytes;
     delete lut;
@@ -1279,9 +1416,11 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
     // emptiest one for the body box); any subset gives a valid grid
     std::vector<unsigned int> hist(static_cast<size_t>(b.bands) * 64, 0u);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(hist.data(), d_hist, hist.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+        e = enqueue_readback(ctx, d_hist, 0, hist.size() * sizeof(unsigned int), s);
     if (e == cudaSuccess)
         e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess)
+        std::memcpy(hist.data(), ctx->readback_host, hist.size() * sizeof(unsigned int));
     // each cell's lowest level over its neighbourhood: the dilated set of every level
     if (e == cudaSuccess)
         e = dev::launch_majorant_minfilter(b, level, minlev, s);
@@ -1552,11 +1691,7 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     if (e == cudaSuccess)
         e = cudaEventRecord(j->begin, s);
     if (e == cudaSuccess)
-        e = cudaHostAlloc(&j->cancel_host, 16 + sizeof(dev::JobCounters), cudaHostAllocMapped);
-    if (e == cudaSuccess) {
-        *j->cancel_host = 0;
-        e = cudaHostGetDevicePointer(&j->cancel_dev, j->cancel_host, 0);
-    }
+        e = ctx->pinned.take(&j->cancel_host, &j->cancel_dev);
     if (e == cudaSuccess)
         e = cudaMemsetAsync(j->records ? static_cast<void*>(j->records) : static_cast<void*>(j->tally_f32), 0, tally_bytes, s);
     if (e == cudaSuccess && j->n_events)
@@ -1572,7 +1707,7 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     if (e != cudaSuccess) {
         free_job_device(j);
         if (j->cancel_host)
-            cudaFreeHost(j->cancel_host);
+            ctx->pinned.give(j->cancel_host, j->cancel_dev);
         delete j;
         return cuda_fail(ctx, e, "job allocation");
     }
@@ -1652,7 +1787,7 @@ void discard_job(dxmc_job* j)
 {
     free_job_device(j);
     if (j->cancel_host)
-        cudaFreeHost(j->cancel_host);
+        j->ctx->pinned.give(j->cancel_host, j->cancel_dev);
     if (j->begin)
         cudaEventDestroy(j->begin);
     if (j->start)
@@ -2289,6 +2424,7 @@ void sync_ctx_streams(dxmc_gpu_ctx* ctx)
 {
     cudaStreamSynchronize(ctx->stream);
     cudaStreamSynchronize(ctx->result_stream);
+    cudaStreamSynchronize(ctx->upload_stream);
     if (BatchEngines* en = engines_of(ctx, false)) {
         for (auto& g : en->e)
             if (g.stream)
@@ -2645,7 +2781,7 @@ void dxmc_gpu_job_free(dxmc_job* j)
     // context stream's order, without waiting for later jobs
     free_job_device(j);
     if (j->cancel_host)
-        cudaFreeHost(j->cancel_host);
+        ctx->pinned.give(j->cancel_host, j->cancel_dev);
     if (j->begin)
         cudaEventDestroy(j->begin);
     if (j->start)
