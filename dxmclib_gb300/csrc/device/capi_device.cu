@@ -106,6 +106,50 @@ struct PinnedSlots {
     }
 };
 
+// Large buffers of finished jobs (tallies, counts, photon queues), kept for the
+// next job that needs the same size.  A job hands them back only after its
+// kernels and result copies are done, so a kept buffer is idle and serves a job
+// at once, without a stream-ordered allocation: that call waited, on the host,
+// for an earlier job's result copies before it returned a reused block.
+struct JobBufferCache {
+    static constexpr size_t MAX_BUFFERS = 8;
+    struct Entry {
+        void* ptr;
+        uint64_t bytes;
+    };
+    std::vector<Entry> entries; // oldest first
+    uint64_t held = 0;
+    void* take(uint64_t bytes)
+    {
+        for (size_t i = entries.size(); i-- > 0;)
+            if (entries[i].bytes == bytes) {
+                void* p = entries[i].ptr;
+                entries.erase(entries.begin() + static_cast<std::ptrdiff_t>(i));
+                held -= bytes;
+                return p;
+            }
+        return nullptr;
+    }
+    // keeps an idle buffer; the oldest one goes back to the pool when the cache is full
+    void put(void* p, uint64_t bytes, cudaStream_t s)
+    {
+        if (entries.size() == MAX_BUFFERS) {
+            cudaFreeAsync(entries.front().ptr, s);
+            held -= entries.front().bytes;
+            entries.erase(entries.begin());
+        }
+        entries.push_back({ p, bytes });
+        held += bytes;
+    }
+    void release(cudaStream_t s)
+    {
+        for (const auto& e : entries)
+            cudaFreeAsync(e.ptr, s);
+        entries.clear();
+        held = 0;
+    }
+};
+
 struct dxmc_gpu_ctx {
     BatchEngines* engines = nullptr; // created by the first batch
     cudaMemPool_t pool = nullptr;    // stream-ordered allocations of this context
@@ -124,6 +168,7 @@ struct dxmc_gpu_ctx {
     size_t max_smem_optin = 0;
     uint64_t submission = 0; // counts the calls that may build grids (job, batch, world prepare)
     PinnedSlots pinned;      // the jobs' cancel flags and counter copies
+    JobBufferCache job_buffers; // idle tally and queue buffers of finished jobs
     // Page-locked, mapped area for the small read-backs a call waits for (palette
     // size and table, a grid's level histogram, per-material maxima).  A kernel
     // writes them there: a copy would queue on the copy engine behind an earlier
@@ -218,6 +263,7 @@ struct dxmc_job {
     dev::JobCounters* counters = nullptr;
     unsigned char* tables = nullptr;
     unsigned char* queue = nullptr; // pre-generated photons (SoA)
+    uint64_t tally_bytes = 0, count_bytes = 0, queue_bytes = 0; // sizes of the cached buffers above
     int* cancel_host = nullptr;  // pinned, mapped; the counters' host copy follows at byte 16
     int* cancel_dev = nullptr;
     cudaEvent_t begin = nullptr, start = nullptr, stop = nullptr; // job begin, kernel start, kernel end
@@ -281,10 +327,22 @@ cudaError_t pool_alloc(dxmc_gpu_ctx* ctx, T** ptr, size_t bytes, cudaStream_t st
     cudaError_t e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(ptr), bytes, ctx->pool, stream);
     if (e == cudaErrorMemoryAllocation) {
         cudaGetLastError();
+        ctx->job_buffers.release(stream);
         sync_ctx_streams(ctx); // every pending free completes
         e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(ptr), bytes, ctx->pool, stream);
     }
     return e;
+}
+
+// A job buffer: an idle one of the same size from the cache, else from the pool.
+template <typename T>
+cudaError_t job_alloc(dxmc_gpu_ctx* ctx, T** ptr, size_t bytes, cudaStream_t stream)
+{
+    if (void* p = ctx->job_buffers.take(bytes)) {
+        *ptr = static_cast<T*>(p);
+        return cudaSuccess;
+    }
+    return pool_alloc(ctx, ptr, bytes, stream);
 }
 
 // The device address of a page-locked host buffer (cudaHostAlloc or
@@ -764,6 +822,8 @@ void dxmc_gpu_ctx_destroy(dxmc_gpu_ctx* ctx)
     cudaSetDevice(ctx->device);
     sync_ctx_streams(ctx);
     release_engines(ctx);
+    ctx->job_buffers.release(ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
     ctx->pinned.release();
     cudaFreeHost(ctx->readback_host);
     cudaStreamDestroy(ctx->upload_stream);
@@ -1216,21 +1276,27 @@ void dxmc_gpu_lut_free(dxmc_lut* lut)
 
 namespace {
 
-void free_job_device(dxmc_job* j)
+// Frees a job's device buffers; `idle`: its kernels and copies are known to be
+// done, so the large buffers may serve the next job (the cache) at once.
+void free_job_device(dxmc_job* j, bool idle)
 {
     cudaStream_t s = j->ctx->stream;
-    if (j->records)
-        cudaFreeAsync(j->records, s);
-    if (j->tally_f32)
-        cudaFreeAsync(j->tally_f32, s);
-    if (j->n_events)
-        cudaFreeAsync(j->n_events, s);
+    auto give = [&](void* p, uint64_t bytes) {
+        if (!p)
+            return;
+        if (idle)
+            j->ctx->job_buffers.put(p, bytes, s);
+        else
+            cudaFreeAsync(p, s);
+    };
+    give(j->records, j->tally_bytes);
+    give(j->tally_f32, j->tally_bytes);
+    give(j->n_events, j->count_bytes);
+    give(j->queue, j->queue_bytes);
     if (j->counters)
         cudaFreeAsync(j->counters, s);
     if (j->tables)
         cudaFreeAsync(j->tables, s);
-    if (j->queue)
-        cudaFreeAsync(j->queue, s);
     j->queue = nullptr;
     j->records = nullptr;
     j->tally_f32 = nullptr;
@@ -1651,6 +1717,8 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
         chunk = std::min<uint64_t>({ total, shared_capacity, 1ull << std::min(log2_chunk, 34) });
     const uint64_t queue_bytes = qmode == QueueMode::own ? chunk * 48 : 0;
     const uint64_t job_bytes = tally_bytes + count_bytes + table_bytes + sizeof(dev::JobCounters) + queue_bytes;
+    if (ctx->in_use + ctx->job_buffers.held + job_bytes > ctx->budget)
+        ctx->job_buffers.release(ctx->stream); // idle buffers give way to the job
     if (ctx->in_use + job_bytes > ctx->budget)
         return fail(ctx, DXMC_ERR_OOM, "job exceeds the device memory budget");
 
@@ -1673,19 +1741,22 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     j->bytes = job_bytes;
     cudaStream_t s = ctx->stream;
     cudaError_t e = cudaSuccess;
+    j->tally_bytes = tally_bytes;
+    j->count_bytes = count_bytes;
+    j->queue_bytes = queue_bytes;
     if (tally_mode == 1) {
-        e = pool_alloc(ctx, &j->tally_f32, tally_bytes, s);
+        e = job_alloc(ctx, &j->tally_f32, tally_bytes, s);
         if (e == cudaSuccess)
-            e = pool_alloc(ctx, &j->n_events, count_bytes, s);
+            e = job_alloc(ctx, &j->n_events, count_bytes, s);
     } else {
-        e = pool_alloc(ctx, &j->records, tally_bytes, s);
+        e = job_alloc(ctx, &j->records, tally_bytes, s);
     }
     if (e == cudaSuccess)
         e = pool_alloc(ctx, &j->counters, sizeof(dev::JobCounters), s);
     if (e == cudaSuccess)
         e = pool_alloc(ctx, &j->tables, table_bytes, s);
     if (e == cudaSuccess && queue_bytes)
-        e = pool_alloc(ctx, &j->queue, queue_bytes, s);
+        e = job_alloc(ctx, &j->queue, queue_bytes, s);
     if (e == cudaSuccess)
         e = cudaEventCreate(&j->begin);
     if (e == cudaSuccess)
@@ -1705,7 +1776,7 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     if (e == cudaSuccess)
         e = cudaEventCreate(&j->stop);
     if (e != cudaSuccess) {
-        free_job_device(j);
+        free_job_device(j, false);
         if (j->cancel_host)
             ctx->pinned.give(j->cancel_host, j->cancel_dev);
         delete j;
@@ -1785,7 +1856,7 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
 
 void discard_job(dxmc_job* j)
 {
-    free_job_device(j);
+    free_job_device(j, false);
     if (j->cancel_host)
         j->ctx->pinned.give(j->cancel_host, j->cancel_dev);
     if (j->begin)
@@ -2757,7 +2828,7 @@ int dxmc_gpu_job_release(dxmc_job* j)
         cudaEventSynchronize(j->stop);
     if (j->result_done)
         cudaEventSynchronize(j->result_done); // the asynchronous result still reads the tallies
-    free_job_device(j);
+    free_job_device(j, true);
     ctx->in_use -= j->bytes;
     j->bytes = 0;
     return DXMC_OK;
@@ -2779,7 +2850,7 @@ void dxmc_gpu_job_free(dxmc_job* j)
     }
     // the job's kernels and copies are done: its buffers go back to the pool in the
     // context stream's order, without waiting for later jobs
-    free_job_device(j);
+    free_job_device(j, true);
     if (j->cancel_host)
         ctx->pinned.give(j->cancel_host, j->cancel_dev);
     if (j->begin)
