@@ -566,7 +566,9 @@ def main():
                 "cpu_baseline": {"value": v, "unit": "histories/s", "cores": threads, "kind": "port",
                                  "precision": "float", "sample": cw.describe,
                                  "double_value": (cw.sample_histories * len(secs64) / float(np.sum(secs64))
-                                                  if secs64 else None)},
+                                                  if secs64 else None),
+                                 "sample_seconds": [round(t, 3) for t in secs],
+                                 "double_sample_seconds": [round(t, 3) for t in secs64]},
                 "e2e": {"value": v, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -575,8 +577,8 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         # the CPU baseline runs first, in a fresh process of the reference arm's own code
         # (no CUDA context, no threads of this process competing for the host cores):
-        # one warm-up and one timed fixed-sample step in float, then the same in double
-        r = subprocess.run([sys.executable, str(REPO / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup",
+        # one warm-up and two timed fixed-sample steps in float, then the same in double
+        r = subprocess.run([sys.executable, str(REPO / "bench.py"), "--impl", "reference", "--steps", "2", "--warmup",
                             "1", "--cpu-precision", "both", "--model", str(args.model),
                             "--histories", str(args.histories)], capture_output=True, text=True)
         lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
