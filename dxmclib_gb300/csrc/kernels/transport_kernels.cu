@@ -772,7 +772,60 @@ namespace {
         }
 
         // ---- interaction passes, one converged pass per event type ---------------------
-        {
+        if constexpr (MODEL == 1) {
+            // LIVERMORE: Compton and Rayleigh both draw one quantile from an energy-row
+            // table and rotate the direction, and photoabsorption only ends the photon,
+            // so every waiting lane runs in one pass (Rayleigh lanes ride along instead
+            // of waiting for a pass of their own).  Each lane draws from its stream in
+            // the order of compton_scatter<1> / rayleigh_scatter<1>.
+            const unsigned waiting = __ballot_sync(FULL_MASK, s.pending != EV_NONE);
+            const unsigned can_step = __ballot_sync(FULL_MASK, s.alive && s.pending == EV_NONE);
+            if (waiting && (__popc(waiting) >= interact_t || can_step == 0u || drain) && s.pending != EV_NONE) {
+                const Real E = s.ph.energy;
+                if (s.pending == EV_PHOTO) {
+                    // photo_absorption<1>: the photon ends and deposits its energy
+                    deposit = E * s.ph.weight;
+                    s.ph.energy = Real(0.0);
+                    s.alive = false;
+                } else {
+                    const bool compton = s.pending == EV_COMPTON;
+                    Real fe;
+                    const int row = table_row(m, E, fe);
+                    const float* tab = p.lut + (compton ? m.off_csf : m.off_ray) + (s.cached_mat * m.tab_ne + row) * (m.tab_nu + 1);
+                    const Real x = table_quantile(tab, m.tab_nu, static_cast<Real>(s.rng.uniform()), fe);
+                    Real cosA, e = Real(1.0);
+                    if (compton) {
+                        // (e - e_min) / (1 - e_min) = x
+                        const Real k = E / Real(ELECTRON_REST_MASS_D);
+                        const Real emin = Real(1.0) / (Real(1.0) + Real(2.0) * k);
+                        const Real one_minus_e = (Real(1.0) - x) * (Real(1.0) - emin);
+                        e = Real(1.0) - one_minus_e;
+                        cosA = m_max(Real(1.0) - one_minus_e / (k * e), -Real(1.0));
+                    } else {
+                        cosA = Real(1.0) - Real(2.0) * x; // q^2 / q_max^2 = (1 - cos) / 2
+                    }
+                    const Real phi = rng_azimuth<Real>(s.rng);
+                    peturb(s.ph.dx, s.ph.dy, s.ph.dz, cosA, phi, p.normalize_direction);
+                    if (compton) {
+                        s.ph.energy = E * e;
+                        if (s.ph.energy < Real(ENERGY_CUTOFF_D)) {
+                            deposit = ((E - s.ph.energy) + s.ph.energy) * s.ph.weight;
+                            s.ph.energy = Real(0.0);
+                            s.alive = false;
+                        } else {
+                            deposit = (E - s.ph.energy) * s.ph.weight;
+                            s.updateMax = true;
+                        }
+                    }
+                }
+                do_score = s.pending != EV_RAYLEIGH;
+                if (s.alive && s.forced_wc != Real(0.0))
+                    s.ph.weight *= (Real(1.0) - s.forced_wc);
+                s.forced_wc = Real(0.0);
+                check_roulette = s.alive;
+                s.pending = EV_NONE;
+            }
+        } else {
             // Rayleigh events are rare (about one in ten interactions here), so their pass
             // waits until RAYLEIGH_THRESHOLD lanes have one, or until nothing else can run
             const unsigned ray = __ballot_sync(FULL_MASK, s.pending == EV_RAYLEIGH);
