@@ -483,19 +483,39 @@ namespace {
     // many lanes active instead of one or two.
     enum : int { EV_NONE = 0, EV_PHOTO = 1, EV_COMPTON = 2, EV_RAYLEIGH = 3 };
 
+    // A voxel as read from the grid: its palette index (compact layout) or its
+    // 8-byte record; decode_voxel turns it into density, material and the
+    // measurement flag.
+    template <bool PALETTE>
+    struct VoxelRaw {
+        uint2 v;
+    };
+    template <>
+    struct VoxelRaw<true> {
+        uint32_t index;
+    };
+
+    template <bool PALETTE>
+    __device__ __forceinline__ VoxelRaw<PALETTE> load_voxel(const WorldParams& w, uint64_t vidx)
+    {
+        if constexpr (PALETTE)
+            return VoxelRaw<true> { __ldg(w.palette_index + vidx) };
+        else
+            return VoxelRaw<false> { __ldg(reinterpret_cast<const uint2*>(w.voxels) + vidx) };
+    }
+
     template <bool PALETTE, class Real>
-    __device__ __forceinline__ void gather_voxel(const WorldParams& w, const PaletteEntry* pal, uint64_t vidx, Real& density, int& mat, bool& measured)
+    __device__ __forceinline__ void decode_voxel(const VoxelRaw<PALETTE>& raw, const PaletteEntry* pal, Real& density, int& mat, bool& measured)
     {
         if constexpr (PALETTE) {
-            const PaletteEntry e = pal[__ldg(w.palette_index + vidx)];
+            const PaletteEntry e = pal[raw.index];
             density = e.density;
             mat = static_cast<int>(e.code & 0xffu);
             measured = (e.code >> 8) != 0u;
         } else {
-            const uint2 raw = __ldg(reinterpret_cast<const uint2*>(w.voxels) + vidx);
-            density = __uint_as_float(raw.x);
-            mat = static_cast<int>(raw.y & 0xffu);
-            measured = ((raw.y >> 8) & 0xffu) != 0u;
+            density = __uint_as_float(raw.v.x);
+            mat = static_cast<int>(raw.v.y & 0xffu);
+            measured = ((raw.v.y >> 8) & 0xffu) != 0u;
         }
     }
 
@@ -689,6 +709,13 @@ namespace {
                 const uint32_t iy = static_cast<uint32_t>(jy);
                 const uint32_t iz = static_cast<uint32_t>(jz);
                 const Real cinv = s.cinv; // the majorant this flight was drawn with
+                // the voxel is read before the majorant cell, so that the two L2 reads
+                // overlap (a truncated flight does not use the voxel)
+                if constexpr (PALETTE) // compact worlds have fewer than 2^32 voxels (world upload)
+                    s.vidx = iz * static_cast<uint32_t>(w.nxy) + (iy * w.dims[0] + ix);
+                else
+                    s.vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
+                const VoxelRaw<PALETTE> raw = load_voxel<PALETTE>(w, s.vidx);
                 if (p.majorant.cells) {
                     const MajorantGrid& g = p.majorant;
                     const uint32_t c = (iz >> g.shift[2]) * g.nxy + (iy >> g.shift[1]) * g.nx + (ix >> g.shift[0]);
@@ -698,14 +725,10 @@ namespace {
                 }
                 if (truncated)
                     continue;
-                if constexpr (PALETTE) // compact worlds have fewer than 2^32 voxels (world upload)
-                    s.vidx = iz * static_cast<uint32_t>(w.nxy) + (iy * w.dims[0] + ix);
-                else
-                    s.vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
                 Real density;
                 int mat;
                 bool measured;
-                gather_voxel<PALETTE>(w, pal, s.vidx, density, mat, measured);
+                decode_voxel<PALETTE>(raw, pal, density, mat, measured);
                 if (mat != s.cached_mat) {
                     Real a0, a1, a2;
                     lut_attenuation(L, m, mat, s.logE, s.seg, a0, a1, a2);
