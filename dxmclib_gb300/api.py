@@ -421,6 +421,11 @@ class Source:
     def getCalibrationValue(self, model=LOWENERGYCORRECTION.NONE, transport=None) -> float:
         return 1.0
 
+    def beams(self, world_cosines=(1, 0, 0, 0, 1, 0)) -> list:
+        """The source's exposures grouped by the spectrum, heel and bow-tie tables they
+        sample (one group unless several tubes take turns)."""
+        return [Beam(self.exposures(world_cosines), self.spectrum(), self.heel(), self.bowtie())]
+
 
 class PencilSource(Source):
     """PencilSource (source.hpp:203-263)."""
@@ -641,8 +646,28 @@ class DXSource(Source):
         return HeelFilter(self._tube, self._coll[1]).table()
 
 
-class CTSpiralSource(Source):
-    """CTSpiralSource (source.hpp:1286-1367) with the CTBaseSource/CTSource defaults."""
+class Beam:
+    """The exposures of a source that sample one spectrum, heel table and bow-tie
+    filter: one per source, two for dual-source CT (source.hpp:1384-1410), each run
+    as a job of its own."""
+
+    def __init__(self, exposures: ExposureTable, spectrum, heel, bowtie):
+        self.exposures = exposures
+        self.spectrum = spectrum
+        self.heel = heel
+        self.bowtie = bowtie
+
+
+def _take(table: ExposureTable, rows) -> ExposureTable:
+    return ExposureTable(table.position[rows].copy(), table.cosines[rows].copy(), table.beam_direction[rows].copy(),
+                         table.collimation[rows].copy(), table.weight[rows].copy(), table.n_histories[rows].copy(),
+                         table.mono_energy[rows].copy())
+
+
+class _CTBase(Source):
+    """CTBaseSource and CTSource (source.hpp:794-1076): the geometry, tube, heel,
+    bow-tie and CTDI settings every CT source shares, and the construction of
+    exposures around the gantry that their getExposure implementations repeat."""
 
     def __init__(self):
         super().__init__()
@@ -652,8 +677,7 @@ class CTSpiralSource(Source):
         self._start = 0.0
         self._scan = 100.0
         self._tilt = 0.0
-        self._pitch = 1.0
-        self._step = DEG_TO_RAD
+        self._step = DEG_TO_RAD  # CTSource::m_exposureAngleStep
         self._tube = Tube()
         self._tube.setAlFiltration(7.0)
         self._heel = True
@@ -669,6 +693,9 @@ class CTSpiralSource(Source):
     def setSourceDetectorDistance(self, sdd):
         self._sdd = abs(float(sdd))
 
+    def sourceDetectorDistance(self):
+        return self._sdd
+
     def setCollimation(self, c):
         self._collimation = abs(float(c))
 
@@ -678,40 +705,65 @@ class CTSpiralSource(Source):
     def setFieldOfView(self, fov):
         self._fov = abs(float(fov))
 
+    def fieldOfView(self):
+        return self._fov
+
+    def setGantryTiltAngle(self, a):
+        self._tilt = min(max(float(a), -PI), PI)
+
     def setGantryTiltAngleDeg(self, a):
-        self._tilt = min(max(a * DEG_TO_RAD, -PI), PI)
+        self.setGantryTiltAngle(a * DEG_TO_RAD)
+
+    def gantryTiltAngle(self):
+        return self._tilt
+
+    def gantryTiltAngleDeg(self):
+        return self._tilt / DEG_TO_RAD
+
+    def setStartAngle(self, a):
+        self._start = float(a)
 
     def setStartAngleDeg(self, a):
         self._start = DEG_TO_RAD * a
 
-    def setExposureAngleStepDeg(self, a):
-        self._step = min(max(abs(a * DEG_TO_RAD), DEG_TO_RAD / 10), PI / 2)
+    def startAngle(self):
+        return self._start
 
-    def setPitch(self, p):
-        self._pitch = max(0.01, float(p))
+    def startAngleDeg(self):
+        return self._start / DEG_TO_RAD
 
     def setScanLenght(self, length):
-        self._scan = max(abs(float(length)), self._collimation * self._pitch * 0.5)
+        self._scan = abs(float(length))
 
-    setScanLength = setScanLenght
+    def setScanLength(self, length):
+        self.setScanLenght(length)
+
+    def scanLenght(self):
+        return self._scan
+
+    def setExposureAngleStep(self, a):
+        self._step = min(max(abs(float(a)), DEG_TO_RAD / 10), PI / 2)
+
+    def setExposureAngleStepDeg(self, a):
+        self.setExposureAngleStep(a * DEG_TO_RAD)
+
+    def exposureAngleStep(self):
+        return self._step
+
+    def exposureAngleStepDeg(self):
+        return self._step / DEG_TO_RAD
 
     def setModelHeelEffect(self, on):
         self._heel = bool(on)
+
+    def modelHeelEffect(self):
+        return self._heel
 
     def setBowTieFilter(self, angles, weights):
         self._bowtie = (np.asarray(angles, np.float64), np.asarray(weights, np.float64))
 
     def bowtie(self):
         return self._bowtie
-
-    def totalExposures(self):
-        return int(self._scan * 2 * PI / (self._collimation * self._pitch * self._step))
-
-    def scanLenght(self):
-        return self._scan
-
-    def pitch(self):
-        return self._pitch
 
     def setCtdiVol(self, ctdivol: float):
         if ctdivol > 0.0:
@@ -729,73 +781,348 @@ class CTSpiralSource(Source):
     def exposuresPerRotatition(self) -> int:
         return int(2 * PI / self._step)
 
-    def calibration_exposures(self, histories_per_exposure: int, world_cosines=(1, 0, 0, 0, 1, 0)) -> ExposureTable:
-        """Exposures of the axial copy that ctCalibration runs (source.hpp:937-942,
-        1203-1255): one rotation about the phantom axis at the origin, the
-        source's angles, tilt, collimation and field of view."""
-        n = self.exposuresPerRotatition()
-        idx = np.arange(n, dtype=np.float64)
-        pos0 = np.array([0.0, -self._sdd / 2, 0.0])
-        angle = self._start + self._step * idx
-        cos = np.tile(np.array([-1.0, 0, 0, 0, 0, 1.0]), (n, 1))
-        tilt_axis = np.array([1.0, 0, 0])
-        tilt_corr = _rotate(pos0, tilt_axis, self._tilt)
-        rot_axis = _rotate(cos[:, 3:], tilt_axis, self._tilt)
-        other = _rotate(cos[:, :3], tilt_axis, self._tilt)
-        pos = _rotate(np.tile(pos0, (n, 1)), rot_axis, angle)
-        pos[:, 2] += tilt_corr[2]
-        other = _rotate(other, rot_axis, angle)
-        cosines = np.concatenate([other, rot_axis], axis=1)
-        coll_x = math.atan(self._fov / self._sdd) * 2.0
-        coll_y = math.atan(self._collimation / self._sdd) * 2.0
-        coll = (-coll_x / 2, coll_x / 2, -coll_y / 2, coll_y / 2)
-        return ExposureTable.build(pos, cosines, coll, 1.0, histories_per_exposure, 0.0, world_cosines)
+    def spectrum(self):
+        e = self._tube.getEnergy()
+        return Spectrum(e, self._tube.getSpecter(e))
 
-    def getCalibrationValue(self, model=LOWENERGYCORRECTION.NONE, transport=None) -> float:
-        """CTSpiralSource::getCalibrationValue (source.hpp:1358-1363): the CTDI
-        calibration of the axial copy (ctCalibration, source.hpp:925-988), run as a
-        GPU job, times the pitch."""
-        from . import calibration as cal
-        ctx = transport.context() if transport is not None else GpuContext()
-        mean_weight = float(np.mean(self.exposures().weight))
-        hpe = cal.calibration_histories_per_exposure(self.exposuresPerRotatition(), self.historiesPerExposure())
-        world = cal.CTDIPhantom(self.ctdiPhantomDiameter())
-        ex = self.calibration_exposures(hpe, world.directionCosines())
-        dose, _, _ = cal.run_ctdi(ctx, world, ex, self.spectrum(), self.heel(), self.bowtie(), int(model))
-        return cal.ctdi_factor(world, dose, self._collimation, self.ctdiVol(), mean_weight) * self._pitch
+    def _heel_span(self):
+        return math.atan(self._collimation * 0.5 / self._sdd) * 2.0
+
+    def heel(self):
+        if not self._heel:
+            return None
+        return HeelFilter(self._tube, self._heel_span()).table()
 
     def exposures(self, world_cosines=(1, 0, 0, 0, 1, 0)):
         return self._memo_exposures(world_cosines, lambda: self._build_exposures(world_cosines))
 
-    def _build_exposures(self, world_cosines):
-        n = self.totalExposures()
-        idx = np.arange(n, dtype=np.float64)
+    def _gantry(self, angle, z, sdd, fov, weight, world_cosines):
+        """Exposures at gantry angles ``angle`` (the rotation about the tilted axis) with
+        table offsets ``z``: the tube at half the source-detector distance from the
+        isocentre, the fan from ``fov`` and the collimation at distance ``sdd``."""
+        angle = np.asarray(angle, np.float64)
+        n = len(angle)
         pos0 = np.array([0.0, -self._sdd / 2, 0.0])
-        angle = self._start + self._step * idx
         cos = np.tile(self._cosines, (n, 1))
         tilt_axis = np.array([1.0, 0, 0])
         tilt_corr = _rotate(pos0, tilt_axis, self._tilt)
         rot_axis = _rotate(cos[:, 3:], tilt_axis, self._tilt)
         other = _rotate(cos[:, :3], tilt_axis, self._tilt)
         pos = _rotate(np.tile(pos0, (n, 1)), rot_axis, angle)
-        pos[:, 2] += (idx * self._step) * self._collimation * self._pitch / (2 * PI) + tilt_corr[2]
+        pos[:, 2] += z + tilt_corr[2]
         other = _rotate(other, rot_axis, angle)
         pos += self._position
         cosines = np.concatenate([other, rot_axis], axis=1)
-        coll_x = math.atan(self._fov / self._sdd) * 2.0
-        coll_y = math.atan(self._collimation / self._sdd) * 2.0
-        coll = (-coll_x / 2, coll_x / 2, -coll_y / 2, coll_y / 2)
-        return ExposureTable.build(pos, cosines, coll, 1.0, self._hpe, 0.0, world_cosines)
+        coll_x = np.arctan(np.asarray(fov, np.float64) / sdd) * 2.0
+        coll_y = np.arctan(self._collimation / np.asarray(sdd, np.float64)) * 2.0
+        coll = np.stack(np.broadcast_arrays(-coll_x / 2, coll_x / 2, -coll_y / 2, coll_y / 2), axis=-1)
+        return ExposureTable.build(pos, cosines, coll, weight, self._hpe, 0.0, world_cosines)
 
-    def spectrum(self):
-        e = self._tube.getEnergy()
-        return Spectrum(e, self._tube.getSpecter(e))
+    def _ct_calibration(self, copy, mean_weight: float, model: int, transport) -> float:
+        """CTBaseSource::ctCalibration (source.hpp:925-988) on an axial copy of the
+        source, the CTDI run as GPU jobs (one per beam)."""
+        from . import calibration as cal
+        ctx = transport.context() if transport is not None else GpuContext()
+        copy.setDirectionCosines([-1, 0, 0, 0, 0, 1])
+        copy.setPosition([0, 0, 0])
+        copy.setScanLenght(copy.collimation())
+        hpe = cal.calibration_histories_per_exposure(copy.exposuresPerRotatition(), copy.historiesPerExposure())
+        world = cal.CTDIPhantom(copy.ctdiPhantomDiameter())
+        copy.setHistoriesPerExposure(hpe)
+        dose = cal.run_ctdi_beams(ctx, world, copy.beams(world.directionCosines()), int(model))
+        return cal.ctdi_factor(world, dose, copy.collimation(), copy.ctdiVol(), mean_weight)
+
+    def _base_state(self):
+        # the CTBaseSource members a copy takes over (source.hpp:1005-1019)
+        return {k: getattr(self, k) for k in ("_position", "_cosines", "_hpe", "_sdd", "_collimation", "_fov",
+                                              "_start", "_scan", "_tilt", "_tube", "_heel", "_bowtie")
+                if hasattr(self, k)} | {k: v for k, v in vars(self).items() if k in ("_ctdivol", "_ctdi_diameter")}
+
+
+class CTSpiralSource(_CTBase):
+    """CTSpiralSource (source.hpp:1286-1367)."""
+
+    def __init__(self):
+        super().__init__()
+        self._pitch = 1.0
+
+    def setPitch(self, p):
+        self._pitch = max(0.01, float(p))
+
+    def pitch(self):
+        return self._pitch
+
+    def setScanLenght(self, length):
+        self._scan = max(abs(float(length)), self._collimation * self._pitch * 0.5)
+
+    def totalExposures(self):
+        return int(self._scan * 2 * PI / (self._collimation * self._pitch * self._step))
+
+    def _build_exposures(self, world_cosines):
+        idx = np.arange(self.totalExposures(), dtype=np.float64)
+        angle = self._start + self._step * idx
+        z = (idx * self._step) * self._collimation * self._pitch / (2 * PI)
+        return self._gantry(angle, z, self._sdd, self._fov, 1.0, world_cosines)
+
+    def _axial_copy(self):
+        """CTAxialSource(const CTSpiralSource&) (source.hpp:1603-1608)."""
+        a = CTAxialSource()
+        for k, v in self._base_state().items():
+            setattr(a, k, v)
+        a._step = self._step
+        a._axial_step = self._collimation
+        a.setScanLenght(self._scan)
+        return a
+
+    def calibration_exposures(self, histories_per_exposure: int, world_cosines=(1, 0, 0, 0, 1, 0)) -> ExposureTable:
+        """Exposures of the axial copy that ctCalibration runs (source.hpp:937-942,
+        1203-1255): one rotation about the phantom axis at the origin, the
+        source's angles, tilt, collimation and field of view."""
+        a = self._axial_copy()
+        a.setDirectionCosines([-1, 0, 0, 0, 0, 1])
+        a.setPosition([0, 0, 0])
+        a.setScanLenght(a.collimation())
+        a.setHistoriesPerExposure(histories_per_exposure)
+        return a.exposures(world_cosines)
+
+    def getCalibrationValue(self, model=LOWENERGYCORRECTION.NONE, transport=None) -> float:
+        """CTSpiralSource::getCalibrationValue (source.hpp:1358-1363): the CTDI
+        calibration of the axial copy, run as a GPU job, times the pitch."""
+        copy = self._axial_copy()
+        mean_weight = float(np.mean(copy.exposures().weight))
+        return self._ct_calibration(copy, mean_weight, model, transport) * self._pitch
+
+
+class CTAxialSource(_CTBase):
+    """CTAxialSource (source.hpp:1192-1285): rotations at table steps of ``step``
+    (the collimation the source was constructed with, unless set)."""
+
+    def __init__(self):
+        super().__init__()
+        self._axial_step = self._collimation
+        self._scan = self._axial_step
+
+    def setStep(self, step):
+        n_steps = self._scan / self._axial_step
+        a = abs(float(step))
+        self._axial_step = a if a > 0.01 else 0.01
+        self.setScanLenght(self._axial_step * n_steps)
+
+    def step(self):
+        return self._axial_step
+
+    def setScanLenght(self, length):
+        self._scan = max(self._axial_step * math.ceil(abs(float(length)) / self._axial_step), self._axial_step)
+
+    def _rotations(self) -> int:
+        return int(round(self._scan / self._axial_step))
+
+    def totalExposures(self):
+        return int(2 * PI / self._step) * self._rotations()
+
+    def _build_exposures(self, world_cosines):
+        apr = int(2 * PI / self._step)
+        i = np.arange(self.totalExposures(), dtype=np.int64)
+        rot = i // apr
+        angle = self._start + self._step * (i - rot * apr).astype(np.float64)
+        z = self._axial_step * rot.astype(np.float64)
+        return self._gantry(angle, z, self._sdd, self._fov, 1.0, world_cosines)
+
+    def getCalibrationValue(self, model=LOWENERGYCORRECTION.NONE, transport=None) -> float:
+        """CTAxialSource::getCalibrationValue (source.hpp:1277-1281)."""
+        copy = CTAxialSource()
+        copy.__dict__.update({k: v for k, v in vars(self).items() if k != "_exposure_memo"})
+        mean_weight = float(np.mean(copy.exposures().weight))
+        return self._ct_calibration(copy, mean_weight, model, transport)
+
+
+class _CTDual:
+    """CTDualSource (source.hpp:1078-1190): a second tube B with its own spectrum,
+    heel table, bow-tie filter, distance, field of view and start angle; the
+    exposures alternate A, B, and each tube's weight is its share of mAs times
+    its unnormalised spectrum, normalised to a mean of one."""
+
+    def _init_dual(self):
+        self._sdd_b = self._sdd
+        self._fov_b = self._fov
+        self._start_b = self._start + PI * 0.5
+        self._tube_b = Tube()
+        self._tube_b.setAlFiltration(self._tube.AlFiltration())
+        self._mas_a = 100.0
+        self._mas_b = 100.0
+        self._bowtie_b = None
+
+    def tubeB(self):
+        return self._tube_b
+
+    def tubeAmas(self):
+        return self._mas_a
+
+    def tubeBmas(self):
+        return self._mas_b
+
+    def setTubeAmas(self, mas):
+        self._mas_a = max(0.0, float(mas))
+
+    def setTubeBmas(self, mas):
+        self._mas_b = max(0.0, float(mas))
+
+    def maxPhotonEnergyProduced(self):
+        return max(self._tube.voltage(), self._tube_b.voltage())
+
+    def exposuresPerRotatition(self) -> int:
+        return 2 * int(2 * PI / self._step)
+
+    def setBowTieFilterB(self, angles, weights):
+        self._bowtie_b = (np.asarray(angles, np.float64), np.asarray(weights, np.float64))
+
+    def bowtieB(self):
+        return self._bowtie_b
+
+    def setSourceDetectorDistanceB(self, sdd):
+        self._sdd_b = abs(float(sdd))
+
+    def sourceDetectorDistanceB(self):
+        return self._sdd_b
+
+    def setFieldOfViewB(self, fov):
+        self._fov_b = abs(float(fov))
+
+    def fieldOfViewB(self):
+        return self._fov_b
+
+    def setStartAngleB(self, a):
+        self._start_b = float(a)
+
+    def setStartAngleDegB(self, a):
+        self._start_b = DEG_TO_RAD * a
+
+    def startAngleB(self):
+        return self._start_b
+
+    def startAngleDegB(self):
+        return self._start_b / DEG_TO_RAD
+
+    def tubeWeights(self):
+        """(weight A, weight B) of CTDualSource::updateSpecterDistribution."""
+        sa = float(np.sum(self._tube.getSpecter(self._tube.getEnergy(), normalize=False)))
+        sb = float(np.sum(self._tube_b.getSpecter(self._tube_b.getEnergy(), normalize=False)))
+        wa, wb = self._mas_a * sa, self._mas_b * sb
+        return wa * 2.0 / (wa + wb), wb * 2.0 / (wa + wb)
+
+    def spectrumB(self):
+        e = self._tube_b.getEnergy()
+        return Spectrum(e, self._tube_b.getSpecter(e))
 
     def heel(self):
-        if not self._heel:
-            return None
-        span = math.atan(self._collimation * 0.5 / self._sdd) * 2.0
-        return HeelFilter(self._tube, span).table()
+        # the dual source builds both heel tables whatever modelHeelEffect says
+        return HeelFilter(self._tube, self._heel_span()).table()
+
+    def heelB(self):
+        return HeelFilter(self._tube_b, self._heel_span()).table()
+
+    def _tube_params(self, i):
+        """Per total exposure index: (exposure index, sdd, start angle, fov, weight)."""
+        tube_b = (i % 2) == 1
+        wa, wb = self.tubeWeights()
+        return (i // 2, np.where(tube_b, self._sdd_b, self._sdd), np.where(tube_b, self._start_b, self._start),
+                np.where(tube_b, self._fov_b, self._fov), np.where(tube_b, wb, wa))
+
+    def beams(self, world_cosines=(1, 0, 0, 0, 1, 0)):
+        ex = self.exposures(world_cosines)
+        return [Beam(_take(ex, slice(0, None, 2)), self.spectrum(), self.heel(), self.bowtie()),
+                Beam(_take(ex, slice(1, None, 2)), self.spectrumB(), self.heelB(), self.bowtieB())]
+
+    def _dual_state(self):
+        return {k: getattr(self, k) for k in ("_sdd_b", "_fov_b", "_start_b", "_tube_b", "_mas_a", "_mas_b",
+                                              "_bowtie_b")}
+
+
+class CTSpiralDualSource(_CTDual, CTSpiralSource):
+    """CTSpiralDualSource (source.hpp:1488-1600)."""
+
+    def __init__(self):
+        CTSpiralSource.__init__(self)
+        self._init_dual()
+
+    def totalExposures(self):
+        return 2 * int(self._scan * 2 * PI / (self._collimation * self._pitch * self._step))
+
+    def _build_exposures(self, world_cosines):
+        i = np.arange(self.totalExposures(), dtype=np.int64)
+        e, sdd, start, fov, weight = self._tube_params(i)
+        ef = e.astype(np.float64)
+        angle = start + self._step * ef
+        z = (ef * self._step) * self._collimation * self._pitch / (2 * PI)
+        return self._gantry(angle, z, sdd, fov, weight, world_cosines)
+
+    def _axial_copy(self):
+        """CTAxialDualSource(const CTSpiralDualSource&) (source.hpp:1610-1616)."""
+        a = CTAxialDualSource()
+        for k, v in {**self._base_state(), **self._dual_state()}.items():
+            setattr(a, k, v)
+        a._step = self._step
+        a._axial_step = self._collimation
+        a.setScanLenght(self._scan)
+        return a
+
+
+class CTAxialDualSource(_CTDual, CTAxialSource):
+    """CTAxialDualSource (source.hpp:1369-1486)."""
+
+    def __init__(self):
+        CTAxialSource.__init__(self)
+        self._init_dual()
+
+    def totalExposures(self):
+        return int(2 * PI / self._step) * self._rotations() * 2
+
+    def _build_exposures(self, world_cosines):
+        apr = int(2 * PI / self._step)
+        i = np.arange(self.totalExposures(), dtype=np.int64)
+        e, sdd, start, fov, weight = self._tube_params(i)
+        rot = e // apr
+        angle = start + self._step * (e - rot * apr).astype(np.float64)
+        z = self._axial_step * rot.astype(np.float64)
+        return self._gantry(angle, z, sdd, fov, weight, world_cosines)
+
+    def getCalibrationValue(self, model=LOWENERGYCORRECTION.NONE, transport=None) -> float:
+        copy = CTAxialDualSource()
+        copy.__dict__.update({k: v for k, v in vars(self).items() if k != "_exposure_memo"})
+        mean_weight = float(np.mean(copy.exposures().weight))
+        return self._ct_calibration(copy, mean_weight, model, transport)
+
+
+class CTTopogramSource(_CTBase):
+    """CTTopogramSource (source.hpp:1618-1702): a fixed gantry angle and one exposure
+    per millimetre of scan length."""
+
+    def totalExposures(self):
+        return max(int(math.ceil(self._scan)), 1)
+
+    def _build_exposures(self, world_cosines):
+        n = self.totalExposures()
+        step = self._scan / (n - 1) if n > 1 else math.inf
+        i = np.arange(n, dtype=np.float64)
+        with np.errstate(invalid="ignore"):
+            z = step * i
+        return self._gantry(np.full(n, self._start), z, self._sdd, self._fov, 1.0, world_cosines)
+
+    def getCalibrationValue(self, model=LOWENERGYCORRECTION.NONE, transport=None) -> float:
+        """CTTopogramSource::getCalibrationValue (source.hpp:1679-1701): an axial copy
+        stepping one collimation, CTDIvol scaled by the scan length over the
+        collimation, at an angle step that matches the number of exposures."""
+        copy = CTAxialSource()
+        for k, v in self._base_state().items():
+            setattr(copy, k, v)
+        copy.setCtdiVol(self.ctdiVol() * self._scan / self._collimation)
+        copy.setScanLenght(0)
+        copy.setStep(self._collimation)
+        n = self.totalExposures()
+        copy.setExposureAngleStep(min(2 * PI / n, (2 * PI) / 72))
+        mean_weight = float(np.mean(copy.exposures().weight))
+        factor = self._ct_calibration(copy, mean_weight, model, transport)
+        return factor * n / copy.totalExposures()
 
 
 # ---------------------------------------------------------------------------
@@ -1308,6 +1635,35 @@ class Batch:
             pass
 
 
+BEAM_SEED_STRIDE = 0x9E3779B97F4A7C15
+
+
+def beam_seed(seed: int, k: int) -> int:
+    """Seed of beam k of a source: beam 0 keeps the caller's seed, the others get
+    streams of their own (the per-history streams mix the seed before the history)."""
+    return (int(seed) + k * BEAM_SEED_STRIDE) & 0xFFFFFFFFFFFFFFFF
+
+
+def normalize_scoring(energy: np.ndarray, energy2: np.ndarray, histories: int):
+    """Transport::normalizeScoring (transport.hpp:780-794) of raw tallies: eV per
+    history and the variance of that mean."""
+    d = energy * (1e3 / histories)
+    v = (energy2 * (1e6 / histories) - d * d) * (1.0 / (histories - 1))
+    return d, v
+
+
+def energy_imparted_to_dose(world: World, energy: np.ndarray, energy2: np.ndarray, calibration: float = 1.0):
+    """Transport::energyImpartedToDose (transport.hpp:796-816) of raw tallies:
+    keV/kg times the calibration value, the variance field scaled by its square."""
+    sp = world.spacing()
+    voxel_volume = sp[0] * sp[1] * sp[2] / 1000.0  # cm3
+    density = np.asarray(world.densityArray(), np.float64)
+    mass = density * voxel_volume * 0.001  # kg
+    with np.errstate(divide="ignore", invalid="ignore"):
+        factor = np.where(density > 0.0, calibration / mass, 0.0)
+    return np.where(density > 0.0, energy * factor, 0.0), np.where(density > 0.0, energy2 * factor * factor, 0.0)
+
+
 class Transport:
     """GPU drop-in for dxmc::Transport<T> (transport.hpp:114-840)."""
 
@@ -1354,24 +1710,47 @@ class Transport:
         source.validate()
         if not source.isValid():
             return empty
-        exposures = source.exposures(world.directionCosines())
-        histories = int(np.sum(exposures.n_histories))
+        beams = source.beams(world.directionCosines())
+        histories = int(sum(int(np.sum(b.exposures.n_histories)) for b in beams))
         dworld = DeviceWorld(self._ctx, world)
         blob = LutBlob.cached(world.materialMap(), dworld.max_density(), source.maxPhotonEnergyProduced())
         dlut = DeviceLut(self._ctx, blob)
         t0 = time.perf_counter()
-        job = Job(self._ctx, dworld, dlut, exposures, source.spectrum(), source.heel(), source.bowtie(), self._seed,
-                  self._model, self._tally_mode)
-        job.wait()
+        # one job per beam (dual-source CT: one per tube), each on streams of its own
+        jobs = [Job(self._ctx, dworld, dlut, b.exposures, b.spectrum, b.heel, b.bowtie, beam_seed(self._seed, k),
+                    self._model, self._tally_mode) for k, b in enumerate(beams)]
+        for job in jobs:
+            job.wait()
         sim_time = time.perf_counter() - t0
+        cal = 1.0
         if self._mode == Transport.DOSE:
             cal = source.getCalibrationValue(self._model, transport=self) if useSourceDoseCalibration else 1.0
-            dose, var, nev, stats = job.result(A.OUTPUT_DOSE, cal)
             units = "mGy" if useSourceDoseCalibration else "keV/kg"
         else:
-            dose, var, nev, stats = job.result(A.OUTPUT_EV_PER_HISTORY)
             units = "eV/history"
-        job.close()
+        if len(jobs) == 1:
+            if self._mode == Transport.DOSE:
+                dose, var, nev, stats = jobs[0].result(A.OUTPUT_DOSE, cal)
+            else:
+                dose, var, nev, stats = jobs[0].result(A.OUTPUT_EV_PER_HISTORY)
+        else:
+            # the beams' raw tallies add; then the reference's normalisation over all histories
+            e = e2 = nev = None
+            stats = {}
+            for job in jobs:
+                d, v, c, st = job.result(A.OUTPUT_RAW)
+                e = d if e is None else e + d
+                e2 = v if e2 is None else e2 + v
+                nev = c if nev is None else nev + c
+                for key, val in st.items():
+                    stats[key] = stats.get(key, 0) + val if key in ("histories", "steps", "deposits",
+                                                                      "rejection_overflows") else max(stats.get(key, 0), val)
+            if self._mode == Transport.DOSE:
+                dose, var = energy_imparted_to_dose(world, e, e2, cal)
+            else:
+                dose, var = normalize_scoring(e, e2, histories)
+        for job in jobs:
+            job.close()
         dlut.close()
         dworld.close()
         return Result(dose, nev, var, histories, sim_time, units, stats)

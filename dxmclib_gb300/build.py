@@ -76,7 +76,11 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         obj = BUILD / (src.stem + ".o")
         objects.append(obj)
         if force or _stale(obj, [src, *headers]):
-            jobs.append([CXX, "-std=c++17", "-O2", "-fPIC", "-Wall", "-c", str(src), "-o", str(obj), *INCLUDES])
+            # no contraction of a * b + c into fused multiply-adds: the host tables (LUT,
+            # tube spectra) must come out the same on x86-64 and aarch64 (where GCC fuses
+            # by default), as the reference's own x86 build computes them
+            jobs.append([CXX, "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-Wall", "-c", str(src), "-o", str(obj),
+                         *INCLUDES])
     for src in CUDA_SOURCES:
         obj = BUILD / (src.stem + ".o")
         objects.append(obj)
@@ -84,7 +88,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
             # the transport kernels use the fast single-precision intrinsics (Monte Carlo
             # sampling tolerates their ulp-level error; tallies stay FP64)
             fast = ["-use_fast_math"] if src.name == "transport_kernels.cu" else []
-            jobs.append([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", *fast, "-Xcompiler", "-fPIC", *defines, "-c", str(src), "-o",
+            jobs.append([NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", *fast, "-Xcompiler", "-fPIC,-ffp-contract=off", *defines, "-c", str(src), "-o",
                          str(obj), *INCLUDES])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for r in ex.map(_run, jobs):

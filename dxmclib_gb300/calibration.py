@@ -137,15 +137,37 @@ def calibration_histories_per_exposure(exposures_per_rotation: int, histories_pe
 
 def run_ctdi(ctx, world: CTDIPhantom, exposures, spectrum, heel, bowtie, model: int, seed: int = 0x5EED):
     """One calibration run on the GPU: dose (keV/kg, uncalibrated) per voxel."""
-    from .api import DeviceLut, DeviceWorld, Job, LutBlob
+    from .api import Beam
+    dose, var, stats = _run_beams(ctx, world, [Beam(exposures, spectrum, heel, bowtie)], model, seed)
+    return dose, var, stats
+
+
+def run_ctdi_beams(ctx, world: CTDIPhantom, beams, model: int, seed: int = 0x5EED) -> np.ndarray:
+    """The calibration run of a source whose tubes take turns (dual-source CT): one
+    GPU job per beam, each with its own spectrum, heel and bow-tie tables and its
+    own random streams.  DOSE output (keV/kg) is linear in the energy imparted, so
+    the beams' doses add."""
+    return _run_beams(ctx, world, beams, model, seed)[0]
+
+
+def _run_beams(ctx, world, beams, model, seed):
+    from .api import DeviceLut, DeviceWorld, Job, LutBlob, beam_seed
     dworld = DeviceWorld(ctx, world)
+    dose = var = None
+    stats = {"histories": 0}
     try:
-        emax = float(np.max(spectrum.energies)) if spectrum is not None else float(np.max(exposures.mono_energy))
+        emax = max(float(np.max(b.spectrum.energies)) if b.spectrum is not None else float(np.max(b.exposures.mono_energy))
+                   for b in beams)
         dlut = DeviceLut(ctx, LutBlob.cached(world.materialMap(), dworld.max_density(), emax))
         try:
-            job = Job(ctx, dworld, dlut, exposures, spectrum, heel, bowtie, seed=seed, model=model)
-            dose, var, _, stats = job.result(A.OUTPUT_DOSE, 1.0, want_events=False)
-            job.close()
+            for k, b in enumerate(beams):
+                job = Job(ctx, dworld, dlut, b.exposures, b.spectrum, b.heel, b.bowtie, seed=beam_seed(seed, k),
+                          model=model)
+                d, v, _, st = job.result(A.OUTPUT_DOSE, 1.0, want_events=False)
+                job.close()
+                dose = d if dose is None else dose + d
+                var = v if var is None else var + v
+                stats = {**st, "histories": stats["histories"] + st["histories"]}
         finally:
             dlut.close()
     finally:

@@ -85,6 +85,15 @@ class Tube:
                 return t
         return 0.0
 
+    def AlFiltration(self) -> float:
+        return self.filtration("Al")
+
+    def CuFiltration(self) -> float:
+        return self.filtration("Cu")
+
+    def SnFiltration(self) -> float:
+        return self.filtration("Sn")
+
     def getEnergy(self) -> np.ndarray:
         """tube.hpp:165-176: res, 2 res, ... <= voltage."""
         out = []

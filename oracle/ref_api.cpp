@@ -82,6 +82,11 @@ DXMC_ORACLE_PRIVATE(LutData, Lut, Interp, m_attenuationData);
 DXMC_ORACLE_PRIVATE(LutMinE, Lut, double, m_minEnergy);
 DXMC_ORACLE_PRIVATE(LutMaxE, Lut, double, m_maxEnergy);
 DXMC_ORACLE_PRIVATE(HeelAngleStart, Heel, double, m_angleStart);
+using Expo = Exposure<double>;
+using SpecPtr = const SpecterDistribution<double>*;
+using HeelPtr = const HeelFilter<double>*;
+DXMC_ORACLE_PRIVATE(ExpoSpecter, Expo, SpecPtr, m_specterDistribution);
+DXMC_ORACLE_PRIVATE(ExpoHeel, Expo, HeelPtr, m_heelFilter);
 DXMC_ORACLE_PRIVATE(HeelAngleStep, Heel, double, m_angleStep);
 DXMC_ORACLE_PRIVATE(HeelEnergyStart, Heel, double, m_energyStart);
 DXMC_ORACLE_PRIVATE(HeelEnergyStep, Heel, double, m_energyStep);
@@ -103,7 +108,8 @@ struct RefWorldDesc {
 
 // Source types
 enum { REF_PENCIL = 0, REF_ISOTROPIC = 1, REF_DX = 2, REF_CTSPIRAL = 3, REF_CTAXIAL = 4, REF_CBCT = 5, REF_ISOTROPIC_CT = 6,
-    REF_CT_CALIBRATION = 7 }; // the axial copy a CT spiral source calibrates with (source.hpp:925-950)
+    REF_CT_CALIBRATION = 7, // the axial copy a CT spiral source calibrates with (source.hpp:925-950)
+    REF_CTSPIRAL_DUAL = 8, REF_CTAXIAL_DUAL = 9, REF_CTTOPOGRAM = 10 };
 
 struct RefSourceDesc {
     int type;
@@ -142,6 +148,18 @@ struct RefSourceDesc {
     const double* bowtie_angles;
     const double* bowtie_weights;
     int bowtie_n;
+    // CT axial step (<= 0: the collimation, the constructor's); dual sources: tube B
+    // and the tube currents (set_b = 0 keeps the CTDualSource constructor's defaults)
+    double axial_step;
+    int set_b;
+    double kvp_b;
+    double al_mm_b;
+    double cu_mm_b;
+    double mas_a;
+    double mas_b;
+    double sdd_b;
+    double fov_b;
+    double start_angle_b_deg;
 };
 
 } // extern "C"
@@ -270,6 +288,60 @@ std::unique_ptr<Source<T>> make_source(const RefSourceDesc& s)
         p->setHistoriesPerExposure(s.histories_per_exposure);
         return p;
     }
+    case REF_CTTOPOGRAM: {
+        auto p = std::make_unique<CTTopogramSource<T>>();
+        setup_tube(p->tube(), s);
+        p->setPosition(pos);
+        p->setSourceDetectorDistance(s.sdd);
+        p->setCollimation(s.ct_collimation);
+        p->setFieldOfView(s.fov);
+        p->setGantryTiltAngleDeg(s.tilt_deg);
+        p->setStartAngleDeg(s.start_angle_deg);
+        p->setScanLenght(s.scan_length);
+        p->setModelHeelEffect(s.heel != 0);
+        p->setHistoriesPerExposure(s.histories_per_exposure);
+        return p;
+    }
+    case REF_CTSPIRAL_DUAL:
+    case REF_CTAXIAL_DUAL: {
+        std::unique_ptr<CTDualSource<T>> p;
+        if (s.type == REF_CTSPIRAL_DUAL) {
+            auto sp = std::make_unique<CTSpiralDualSource<T>>();
+            sp->setPitch(s.pitch);
+            p = std::move(sp);
+        } else {
+            auto ax = std::make_unique<CTAxialDualSource<T>>();
+            if (s.axial_step > 0)
+                ax->setStep(s.axial_step);
+            p = std::move(ax);
+        }
+        setup_tube(p->tube(), s);
+        if (s.set_b) {
+            Tube<T>& b = p->tubeB();
+            b.setVoltage(s.kvp_b);
+            if (s.anode_angle_deg > 0)
+                b.setAnodeAngleDeg(s.anode_angle_deg);
+            b.setAlFiltration(s.al_mm_b);
+            if (s.cu_mm_b > 0)
+                b.setCuFiltration(s.cu_mm_b);
+            p->setTubeAmas(s.mas_a);
+            p->setTubeBmas(s.mas_b);
+            p->setSourceDetectorDistanceB(s.sdd_b);
+            p->setFieldOfViewB(s.fov_b);
+            p->setStartAngleDegB(s.start_angle_b_deg);
+        }
+        p->setPosition(pos);
+        p->setSourceDetectorDistance(s.sdd);
+        p->setCollimation(s.ct_collimation);
+        p->setFieldOfView(s.fov);
+        p->setGantryTiltAngleDeg(s.tilt_deg);
+        p->setStartAngleDeg(s.start_angle_deg);
+        p->setExposureAngleStepDeg(s.angle_step_deg);
+        p->setScanLenght(s.scan_length);
+        p->setModelHeelEffect(s.heel != 0);
+        p->setHistoriesPerExposure(s.histories_per_exposure);
+        return p;
+    }
     case REF_CTSPIRAL:
     case REF_CTAXIAL: {
         std::unique_ptr<CTSource<T>> p;
@@ -278,7 +350,10 @@ std::unique_ptr<Source<T>> make_source(const RefSourceDesc& s)
             sp->setPitch(s.pitch);
             p = std::move(sp);
         } else {
-            p = std::make_unique<CTAxialSource<T>>();
+            auto ax = std::make_unique<CTAxialSource<T>>();
+            if (s.axial_step > 0)
+                ax->setStep(s.axial_step);
+            p = std::move(ax);
         }
         setup_tube(p->tube(), s);
         p->setPosition(pos);
@@ -630,6 +705,65 @@ int ref_ctdi_phantom(int diameter, std::uint64_t* dims, double* density, std::ui
             for (auto v : idx)
                 hole_indices[off++] = v;
         }
+    }
+    return 0;
+}
+
+// The spectrum and heel tables exposure `index` of a source samples with (its
+// SpecterDistribution and HeelFilter, exposure.hpp:45-47): dual-source CT
+// alternates two of each (source.hpp:1384-1410).  Tube B's energies and
+// normalised weights (CTDualSource::updateSpecterDistribution, source.hpp:1150-1175)
+// are written for dual sources.
+int ref_exposure_tables(const RefSourceDesc* sd, const RefWorldDesc* wd, std::uint64_t index,
+    double* spec_probs, std::uint64_t* spec_alias, int* spec_n, int spec_cap,
+    double* heel_meta, double* heel_weights, int heel_cap,
+    double* tube_b_energies, double* tube_b_weights, int* tube_b_n)
+{
+    World<double> world;
+    if (!make_world(*wd, world))
+        return -1;
+    auto src = make_source<double>(*sd);
+    if (!src)
+        return -2;
+    src->updateFromWorld(world);
+    src->validate();
+    if (!src->isValid() || index >= src->totalExposures())
+        return -3;
+    const auto e = src->getExposure(index);
+    *spec_n = 0;
+    heel_meta[0] = 0;
+    if (SpecPtr d = e.*member(ExpoSpecter {})) {
+        const auto& probs = d->probabilityData();
+        const auto& alias = d->aliasingData();
+        if (static_cast<int>(probs.size()) > spec_cap)
+            return -5;
+        *spec_n = static_cast<int>(probs.size());
+        std::copy(probs.begin(), probs.end(), spec_probs);
+        std::copy(alias.begin(), alias.end(), spec_alias);
+    }
+    if (HeelPtr h = e.*member(ExpoHeel {})) {
+        const auto& w = h->weights();
+        if (static_cast<int>(w.size()) > heel_cap)
+            return -6;
+        heel_meta[0] = 1;
+        heel_meta[1] = h->*member(HeelEnergyStart {});
+        heel_meta[2] = h->*member(HeelEnergyStep {});
+        heel_meta[3] = static_cast<double>(h->energySize());
+        heel_meta[4] = h->*member(HeelAngleStart {});
+        heel_meta[5] = h->*member(HeelAngleStep {});
+        heel_meta[6] = static_cast<double>(h->angleSize());
+        std::copy(w.begin(), w.end(), heel_weights);
+    }
+    *tube_b_n = 0;
+    if (auto* dual = dynamic_cast<CTDualSource<double>*>(src.get())) {
+        const Tube<double>& b = static_cast<const CTDualSource<double>*>(dual)->tubeB();
+        const auto energies = b.getEnergy();
+        const auto weights = b.getSpecter(energies);
+        if (static_cast<int>(energies.size()) > spec_cap)
+            return -7;
+        *tube_b_n = static_cast<int>(energies.size());
+        std::copy(energies.begin(), energies.end(), tube_b_energies);
+        std::copy(weights.begin(), weights.end(), tube_b_weights);
     }
     return 0;
 }

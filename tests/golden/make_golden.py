@@ -407,6 +407,88 @@ def gen_ctdi(out: Path, quick: bool):
                         heel_weights=tabs.get("heel_weights", np.zeros(0)), max_energy=tabs["max_energy"])
 
 
+def ct_family_cases():
+    """The CT sources beyond the single-tube spiral: axial (with a step other than the
+    collimation), spiral and axial dual-source (tube B, tube currents, its own
+    distance, field of view and start angle) and topogram."""
+    return {
+        "ctaxial": R.SourceArgs(R.CTAXIAL, position=(0, 0, -20), kvp=100, al_mm=3.0, ct_collimation=20,
+                                scan_length=50, angle_step_deg=3.0, start_angle_deg=15, fov=450, sdd=1100,
+                                tilt_deg=5.0, heel=1, histories_per_exposure=100, axial_step=25),
+        "ctspiral_dual": R.SourceArgs(R.CTSPIRAL_DUAL, position=(0, 0, -30), kvp=140, al_mm=2.5, ct_collimation=40,
+                                      pitch=1.2, scan_length=60, angle_step_deg=2.0, start_angle_deg=10, fov=500,
+                                      sdd=1190, tilt_deg=0.0, heel=1, histories_per_exposure=100, kvp_b=80,
+                                      al_mm_b=6.0, cu_mm_b=0.1, mas_a=120, mas_b=200, sdd_b=1000, fov_b=330,
+                                      start_angle_b_deg=100),
+        "ctaxial_dual": R.SourceArgs(R.CTAXIAL_DUAL, position=(0, 0, 0), kvp=120, al_mm=2.5, ct_collimation=20,
+                                     scan_length=60, angle_step_deg=5.0, start_angle_deg=0, fov=500, sdd=1190,
+                                     tilt_deg=8.0, heel=0, histories_per_exposure=100, axial_step=30, kvp_b=100,
+                                     al_mm_b=4.0, mas_a=200, mas_b=100, sdd_b=1190, fov_b=260, start_angle_b_deg=95),
+        "cttopogram": R.SourceArgs(R.CTTOPOGRAM, position=(0, 0, -30), kvp=120, al_mm=2.5, ct_collimation=10,
+                                   scan_length=300, start_angle_deg=30, fov=500, sdd=1190, tilt_deg=0.0, heel=1,
+                                   histories_per_exposure=100),
+    }
+
+
+def gen_ct_family(out: Path, quick: bool):
+    """Exposure tables and the per-tube spectrum / heel tables of the CT family
+    (source.hpp:1192-1702), a dual-source transport (Transport<double>, block sums)
+    and the calibration factors of a spiral dual source and a topogram
+    (Source::getCalibrationValue: the reference's own CTDI run, 1e8 histories)."""
+    n = 32
+    w = R.WorldArgs((n, n, n), (4, 4, 4), np.ones(n ** 3), np.zeros(n ** 3, np.uint8), ["Water, Liquid"])
+    for name, s in ct_family_cases().items():
+        t = R.source_tables(s, w)
+        for k in (0, 1):
+            e = R.exposure_tables(s, w, k)
+            for key, v in e.items():
+                t[f"x{k}_{key}"] = v
+        np.savez_compressed(out / f"source_{name}.npz", **t)
+    # dual-source helical scan of the heterogeneous phantom
+    mat, dens = hetero_world(n=48, spacing=4.0, seed=11)
+    dims = (48, 48, 48)
+    wt = R.WorldArgs(dims, (4.0, 4.0, 4.0), dens, mat, MATERIALS4)
+    hpe = 400 if quick else 2400
+    s = R.SourceArgs(R.CTSPIRAL_DUAL, position=(0, 0, -20), kvp=140, al_mm=2.5, ct_collimation=40, pitch=1.0,
+                     scan_length=40, angle_step_deg=2.0, start_angle_deg=0, fov=500, sdd=1190, heel=1,
+                     histories_per_exposure=hpe, kvp_b=80, al_mm_b=6.0, mas_a=100, mas_b=250, sdd_b=1050, fov_b=330,
+                     start_angle_b_deg=90)
+    tabs = R.source_tables(s, wt)
+    beams = [R.exposure_tables(s, wt, k) for k in (0, 1)]
+    runs = []
+    for k in range(2):
+        dose, var, nev, N, st = R.transport(wt, s, model=1)
+        print(f"ct dual run {k}: {N} histories {st:.2f} s", flush=True)
+        runs.append(block_tally(dose, var, nev, dims, (2, 2, 2)))
+    extra = {f"x{k}_{key}": v for k in (0, 1) for key, v in beams[k].items()}
+    np.savez_compressed(out / "transport_ct_dual_m1.npz", dims=np.array(dims), spacing=np.array([4.0] * 3),
+                        material=mat, density=dens.astype(np.float32), names=np.array(MATERIALS4), histories=N,
+                        block=np.array([2, 2, 2]), exposures=tabs["exposures"], spec_energies=tabs["spec_energies"],
+                        spec_weights=tabs["spec_weights"], heel_meta=tabs["heel_meta"],
+                        heel_weights=tabs.get("heel_weights", np.zeros(0)), max_energy=tabs["max_energy"],
+                        same_method=same_method_stats(runs[0][1], runs[1][1]),
+                        **{f"r_{k}": v for k, v in runs[0][0].items()}, **extra)
+    # calibration factors (the sources' defaults: CTDIvol 1 mGy, 320 mm phantom)
+    factors = {}
+    cal_cases = {
+        "spiral_dual": R.SourceArgs(R.CTSPIRAL_DUAL, position=(0, 0, 0), kvp=140, al_mm=2.5, ct_collimation=40,
+                                    pitch=1.2, scan_length=100, angle_step_deg=1.0, start_angle_deg=0, fov=500,
+                                    sdd=1190, heel=1, histories_per_exposure=1000, kvp_b=80, al_mm_b=6.0, mas_a=100,
+                                    mas_b=250, sdd_b=1050, fov_b=330, start_angle_b_deg=90),
+        "topogram": R.SourceArgs(R.CTTOPOGRAM, position=(0, 0, 0), kvp=120, al_mm=2.5, ct_collimation=10,
+                                 scan_length=300, start_angle_deg=0, fov=500, sdd=1190, heel=1,
+                                 histories_per_exposure=10000),
+    }
+    for name, s in cal_cases.items():
+        if quick:
+            break
+        t = time.time()
+        factors[name] = R.calibration_value(w, s, model=1)
+        print(f"calibration {name}: {factors[name]:.6e} ({time.time() - t:.1f} s)", flush=True)
+    np.savez_compressed(out / "ct_family_calibration_m1.npz", ctdivol=1.0, diameter=320,
+                        **{k: np.array(v) for k, v in factors.items()})
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true")
@@ -419,7 +501,8 @@ def main():
                  transport=lambda: gen_transport(out, a.quick), ct=lambda: gen_ct(out, a.quick),
                  interactions=lambda: gen_interactions(out, a.quick), ctdi=lambda: gen_ctdi(out, a.quick),
                  bench_ct=lambda: gen_bench_ct(out, a.quick), bench_dx=lambda: gen_bench_dx(out, a.quick),
-                 dose=lambda: gen_dose(out, a.quick), tubes=lambda: gen_tubes(out))
+                 dose=lambda: gen_dose(out, a.quick), tubes=lambda: gen_tubes(out),
+                 ct_family=lambda: gen_ct_family(out, a.quick))
     for name, fn in steps.items():
         if a.only and name not in a.only.split(","):
             continue

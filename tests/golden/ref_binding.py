@@ -67,6 +67,16 @@ class RefSourceDesc(C.Structure):
         ("bowtie_angles", C.POINTER(C.c_double)),
         ("bowtie_weights", C.POINTER(C.c_double)),
         ("bowtie_n", C.c_int),
+        ("axial_step", C.c_double),
+        ("set_b", C.c_int),
+        ("kvp_b", C.c_double),
+        ("al_mm_b", C.c_double),
+        ("cu_mm_b", C.c_double),
+        ("mas_a", C.c_double),
+        ("mas_b", C.c_double),
+        ("sdd_b", C.c_double),
+        ("fov_b", C.c_double),
+        ("start_angle_b_deg", C.c_double),
     ]
 
 
@@ -148,6 +158,16 @@ class SourceArgs:
         s.fov = float(kw.get("fov", 500.0))
         s.tilt_deg = float(kw.get("tilt_deg", 0.0))
         s.bowtie_n = 0
+        s.axial_step = float(kw.get("axial_step", 0.0))
+        s.set_b = int("kvp_b" in kw)
+        s.kvp_b = float(kw.get("kvp_b", 120.0))
+        s.al_mm_b = float(kw.get("al_mm_b", 7.0))
+        s.cu_mm_b = float(kw.get("cu_mm_b", 0.0))
+        s.mas_a = float(kw.get("mas_a", 100.0))
+        s.mas_b = float(kw.get("mas_b", 100.0))
+        s.sdd_b = float(kw.get("sdd_b", 1190.0))
+        s.fov_b = float(kw.get("fov_b", 500.0))
+        s.start_angle_b_deg = float(kw.get("start_angle_b_deg", 90.0))
         self.desc = s
 
 
@@ -220,6 +240,30 @@ def source_tables(source: SourceArgs, world: WorldArgs, cap_exposures: int = 200
     return out
 
 
+def exposure_tables(source: SourceArgs, world: WorldArgs, index: int):
+    """The spectrum alias table and heel table exposure ``index`` samples with, and
+    tube B's energies and normalised weights for dual sources."""
+    cap = 4096
+    sp = np.zeros(cap)
+    sa = np.zeros(cap, np.uint64)
+    sn = C.c_int(0)
+    hm = np.zeros(8)
+    hw = np.zeros(65536)
+    be, bw = np.zeros(cap), np.zeros(cap)
+    bn = C.c_int(0)
+    rc = lib().ref_exposure_tables(C.byref(source.desc), C.byref(world.desc), C.c_uint64(index), _dptr(sp),
+                                   sa.ctypes.data_as(C.POINTER(C.c_uint64)), C.byref(sn), C.c_int(cap), _dptr(hm),
+                                   _dptr(hw), C.c_int(len(hw)), _dptr(be), _dptr(bw), C.byref(bn))
+    if rc != 0:
+        raise RuntimeError(f"ref_exposure_tables failed: {rc}")
+    k, nb = sn.value, bn.value
+    out = dict(spec_probs=sp[:k].copy(), spec_alias=sa[:k].copy(), heel_meta=hm.copy(),
+               tube_b_energies=be[:nb].copy(), tube_b_weights=bw[:nb].copy())
+    if hm[0] > 0:
+        out["heel_weights"] = hw[: int(hm[3]) * int(hm[6])].copy()
+    return out
+
+
 def alias_table(weights):
     w = np.ascontiguousarray(weights, np.float64)
     p = np.zeros(len(w))
@@ -242,6 +286,7 @@ def interactions(world: WorldArgs, max_energy: float, model: int, kind: int, ene
 
 
 CT_CALIBRATION = 7  # the axial copy a CT spiral source calibrates with
+CTSPIRAL_DUAL, CTAXIAL_DUAL, CTTOPOGRAM = 8, 9, 10
 
 
 def ctdi_phantom(diameter: int):

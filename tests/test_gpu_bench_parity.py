@@ -135,3 +135,97 @@ def test_dose_output_mode_matches_reference(gpu_ctx, golden, mode):
         d_gpu, v_gpu = block_sums(dose, dims, block) / n_gpu, block_sums(var, dims, block) / n_gpu ** 2
     s = compare_sparse(ref_n, d_gpu, v_gpu)
     assert_parity(s, f"dose mode {mode} (2x2x2 blocks)")
+
+
+def _ct_dual_world(g):
+    import dxmclib_gb300 as dx
+    world = dx.World()
+    world.setDimensions(tuple(int(x) for x in g["dims"]))
+    world.setSpacing(tuple(float(x) for x in g["spacing"]))
+    world.setDensityArray(g["density"])
+    world.setMaterialIndexArray(g["material"])
+    for n in g["names"]:
+        world.addMaterialToMap(dx.Material(str(n)))
+    assert world.isValid()
+    return world
+
+
+def test_dual_source_ct_matches_reference(gpu_ctx, golden):
+    """A dual-source helical scan (CTSpiralDualSource, source.hpp:1488-1600: tubes
+    of 140 and 80 kV taking turns, each with its own spectrum, heel table,
+    distance, field of view and start angle) through the Python Transport, which
+    runs one job per tube and normalises their summed tallies, against the
+    reference's Transport<double> (2 x 2 x 2-voxel blocks)."""
+    import dxmclib_gb300 as dx
+    from dxmclib_gb300 import _capi as A
+    g = golden("transport_ct_dual_m1.npz")
+    world = _ct_dual_world(g)
+    src = dx.CTSpiralDualSource()
+    src.setPitch(1.0)
+    src.tubeB().setVoltage(80)
+    src.tubeB().setAlFiltration(6.0)
+    src.setTubeAmas(100)
+    src.setTubeBmas(250)
+    src.setSourceDetectorDistanceB(1050)
+    src.setFieldOfViewB(330)
+    src.setStartAngleDegB(90)
+    src.tube().setVoltage(140)
+    src.tube().setAlFiltration(2.5)
+    src.setPosition((0, 0, -20))
+    src.setSourceDetectorDistance(1190)
+    src.setCollimation(40)
+    src.setFieldOfView(500)
+    src.setStartAngleDeg(0)
+    src.setExposureAngleStepDeg(2.0)
+    src.setScanLenght(40)
+    src.setHistoriesPerExposure(int(g["exposures"][0, 17]) * 2)
+    ex = src.exposures(world.directionCosines()).as_matrix()
+    ref_ex = g["exposures"].copy()
+    ref_ex[:, 17] *= 2
+    np.testing.assert_allclose(ex, ref_ex, rtol=0, atol=1e-9)
+    tr = dx.Transport(gpu_ctx)
+    tr.setOutputMode(dx.Transport.EV_PER_HISTORY)
+    tr.setSeed(2031)
+    res = tr(world, src)
+    assert res.numberOfHistories == int(np.sum(ref_ex[:, 17]))
+    dims, block = tuple(int(x) for x in g["dims"]), tuple(int(x) for x in g["block"])
+    ref = {"idx": g["r_idx"], "dose": g["r_dose"], "var": g["r_var"], "total": g["r_total"]}
+    s = compare_sparse(ref, block_sums(res.dose, dims, block), block_sums(res.variance, dims, block))
+    assert_parity(s, "dual-source ct spiral (2x2x2 blocks)", max_chi2=_max_chi2(g))
+
+
+def test_ct_family_calibration_matches_reference(gpu_ctx, golden):
+    """Source::getCalibrationValue of a dual-source spiral (CTAxialDualSource copy,
+    both tubes in the CTDI run) and of a topogram (an axial copy stepping one
+    collimation, source.hpp:1679-1701) as GPU jobs, against the reference's own
+    CTDI runs of 1e8 histories; the tolerance of the single-tube calibration
+    test, 2 %."""
+    import dxmclib_gb300 as dx
+    g = golden("ct_family_calibration_m1.npz")
+    tr = dx.Transport(gpu_ctx)
+    dual = dx.CTSpiralDualSource()
+    dual.setPitch(1.2)
+    dual.tubeB().setVoltage(80)
+    dual.tubeB().setAlFiltration(6.0)
+    dual.setTubeAmas(100)
+    dual.setTubeBmas(250)
+    dual.setSourceDetectorDistanceB(1050)
+    dual.setFieldOfViewB(330)
+    dual.setStartAngleDegB(90)
+    dual.tube().setVoltage(140)
+    dual.tube().setAlFiltration(2.5)
+    dual.setCollimation(40)
+    dual.setScanLenght(100)
+    dual.setHistoriesPerExposure(1000)
+    f = dual.getCalibrationValue(1, transport=tr)
+    print(f"[calibration] dual-source spiral: {f:.6e} vs reference {float(g['spiral_dual']):.6e}")
+    assert abs(f / float(g["spiral_dual"]) - 1.0) < 0.02
+    topo = dx.CTTopogramSource()
+    topo.tube().setVoltage(120)
+    topo.tube().setAlFiltration(2.5)
+    topo.setCollimation(10)
+    topo.setScanLenght(300)
+    topo.setHistoriesPerExposure(10000)
+    f = topo.getCalibrationValue(1, transport=tr)
+    print(f"[calibration] topogram: {f:.6e} vs reference {float(g['topogram']):.6e}")
+    assert abs(f / float(g["topogram"]) - 1.0) < 0.02
