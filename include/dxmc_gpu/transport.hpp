@@ -102,6 +102,35 @@ struct FlatSource {
     double max_energy = 0;
 };
 
+// Spectrum (Tube::getSpecter, normalised) and, for heel_span >= 0, the heel table
+// (HeelFilter, beamfilters.hpp:455-505) of one tube.
+template <Floating T>
+void tube_tables(const Tube<T>& tube, T heel_span, FlatSource<T>& out)
+{
+    const auto energies = tube.getEnergy();
+    const auto weights = tube.getSpecter(energies);
+    out.spec_energies.assign(energies.begin(), energies.end());
+    out.spec_weights.assign(weights.begin(), weights.end());
+    out.heel_weights.clear();
+    out.has_heel = false;
+    if (heel_span >= 0) {
+        HeelFilter<T> heel(tube, heel_span);
+        out.heel_weights.assign(heel.weights().begin(), heel.weights().end());
+        // grid of HeelFilter::update (beamfilters.hpp:467-483): 10 keV + 2 keV steps,
+        // angle bins from -min(anode angle, span/2) to +span/2
+        const T span = std::abs(heel_span);
+        const T start = tube.anodeAngle() < span / 2 ? -tube.anodeAngle() : -span / 2;
+        out.heel.energy_start = 10.0;
+        out.heel.energy_step = 2.0;
+        out.heel.energy_size = static_cast<int32_t>(heel.energySize());
+        out.heel.angle_size = static_cast<int32_t>(heel.angleSize());
+        out.heel.angle_start = start;
+        out.heel.angle_step = (span / 2 - start) / static_cast<T>(heel.angleSize());
+        out.heel.weights = out.heel_weights.data();
+        out.has_heel = true;
+    }
+}
+
 // Flattens Source::getExposure(i) for every exposure (source.hpp), applying the
 // world basis like workerRun does (transport.hpp:750-757).  Spectrum, heel and
 // bow-tie tables are read through the public API of the sources that own them:
@@ -159,27 +188,43 @@ bool flatten(const World<T>& world, Source<T>* source, FlatSource<T>& out,
         out.spec_energies.assign(isotropic_spectrum->first.begin(), isotropic_spectrum->first.end());
         out.spec_weights.assign(isotropic_spectrum->second.begin(), isotropic_spectrum->second.end());
     }
-    if (tube) {
-        const auto energies = tube->getEnergy();
-        const auto weights = tube->getSpecter(energies);
-        out.spec_energies.assign(energies.begin(), energies.end());
-        out.spec_weights.assign(weights.begin(), weights.end());
-        if (heel_span >= 0) {
-            HeelFilter<T> heel(*tube, heel_span);
-            out.heel_weights.assign(heel.weights().begin(), heel.weights().end());
-            // grid of HeelFilter::update (beamfilters.hpp:467-483): 10 keV + 2 keV steps,
-            // angle bins from -min(anode angle, span/2) to +span/2
-            const T span = std::abs(heel_span);
-            const T start = tube->anodeAngle() < span / 2 ? -tube->anodeAngle() : -span / 2;
-            out.heel.energy_start = 10.0;
-            out.heel.energy_step = 2.0;
-            out.heel.energy_size = static_cast<int32_t>(heel.energySize());
-            out.heel.angle_size = static_cast<int32_t>(heel.angleSize());
-            out.heel.angle_start = start;
-            out.heel.angle_step = (span / 2 - start) / static_cast<T>(heel.angleSize());
-            out.heel.weights = out.heel_weights.data();
-            out.has_heel = true;
-        }
+    if (tube)
+        tube_tables(*tube, heel_span, out);
+    return true;
+}
+
+// The beams of a source: groups of its exposures that sample one spectrum, heel
+// table and bow-tie filter, each run as a job of its own.  A dual-source CT
+// scanner (CTDualSource, source.hpp:1078-1190) alternates tube A (even exposures)
+// and tube B (odd ones), each with its own spectrum, heel table (always built,
+// with tube A's distance: source.hpp:1170-1172) and bow-tie filter; every other
+// source is one beam.
+template <Floating T>
+bool flatten_beams(const World<T>& world, Source<T>* source, std::vector<FlatSource<T>>& beams,
+    const std::pair<std::vector<T>, std::vector<T>>* isotropic_spectrum = nullptr)
+{
+    beams.assign(1, FlatSource<T> {});
+    if (!flatten(world, source, beams[0], isotropic_spectrum))
+        return false;
+    auto* dual = dynamic_cast<CTDualSource<T>*>(source);
+    if (!dual)
+        return true;
+    const auto* cdual = dual;
+    FlatSource<T> all = std::move(beams[0]);
+    beams.assign(2, FlatSource<T> {});
+    for (std::size_t i = 0; i < all.exposures.size(); ++i)
+        beams[i % 2].exposures.push_back(all.exposures[i]);
+    const T span = std::atan(cdual->collimation() * T { 0.5 } / cdual->sourceDetectorDistance()) * T { 2.0 };
+    tube_tables(cdual->tube(), span, beams[0]);
+    tube_tables(cdual->tubeB(), span, beams[1]);
+    const std::shared_ptr<BowTieFilter<T>> filters[2] = { cdual->bowTieFilter(), cdual->bowTieFilterB() };
+    for (int b = 0; b < 2; ++b) {
+        beams[b].max_energy = all.max_energy;
+        if (filters[b])
+            for (const auto& [a, w] : filters[b]->data()) {
+                beams[b].bowtie_angles.push_back(a);
+                beams[b].bowtie_weights.push_back(w);
+            }
     }
     return true;
 }
@@ -234,8 +279,8 @@ public:
             m_error = "invalid source";
             return result;
         }
-        FlatSource<T> flat;
-        if (!flatten(world, source, flat, m_iso.first.empty() ? nullptr : &m_iso)) {
+        std::vector<FlatSource<T>> beams;
+        if (!flatten_beams(world, source, beams, m_iso.first.empty() ? nullptr : &m_iso)) {
             m_error = "source type needs setIsotropicSpectrum";
             return result;
         }
@@ -279,94 +324,146 @@ public:
             providers.push_back(detail::provider(m));
         dxmc_lut_blob* blob = nullptr;
         dxmc_lut* lut = nullptr;
-        dxmc_job* job = nullptr;
         bool ok = check(dxmc_gpu_world_max_density(dworld, maxDensity.data(), static_cast<int>(maxDensity.size())), "max density")
-            && check(dxmc_lut_build_max_density(providers.data(), static_cast<int>(providers.size()), maxDensity.data(), flat.max_energy, &blob), "lut build")
+            && check(dxmc_lut_build_max_density(providers.data(), static_cast<int>(providers.size()), maxDensity.data(), beams[0].max_energy, &blob), "lut build")
             && check(dxmc_gpu_lut_upload(m_ctx, blob, &lut), "lut upload");
-        dxmc_spectrum_desc spec { static_cast<int32_t>(flat.spec_energies.size()), flat.spec_energies.data(), flat.spec_weights.data() };
-        dxmc_bowtie_desc bowtie { static_cast<int32_t>(flat.bowtie_angles.size()), flat.bowtie_angles.data(), flat.bowtie_weights.data() };
-        dxmc_job_desc jd {};
-        jd.exposures = flat.exposures.data();
-        jd.n_exposures = flat.exposures.size();
-        jd.spectrum = flat.spec_energies.empty() ? nullptr : &spec;
-        jd.heel = flat.has_heel ? &flat.heel : nullptr;
-        jd.bowtie = flat.bowtie_angles.empty() ? nullptr : &bowtie;
-        jd.seed = m_seed++;
-        jd.model = static_cast<int32_t>(m_model);
-        jd.tally_mode = -1;
-        jd.tracking = m_tracking;
-        jd.direction = m_direction;
-        jd.precision = m_precision;
-        const auto start = std::chrono::system_clock::now();
-        if (progressbar) {
-            progressbar->setTotalExposures(flat.exposures.size());
+        // one job per beam; beam k draws from streams of a seed of its own
+        const std::uint64_t seed = m_seed++;
+        std::vector<dxmc_job*> jobs(beams.size(), nullptr);
+        std::uint64_t histories = 0, total_exposures = 0;
+        for (const auto& b : beams) {
+            total_exposures += b.exposures.size();
+            for (const auto& e : b.exposures)
+                histories += e.n_histories;
         }
-        ok = ok && check(dxmc_gpu_job_submit(m_ctx, dworld, lut, &jd, &job), "job submit");
+        const auto start = std::chrono::system_clock::now();
+        if (progressbar)
+            progressbar->setTotalExposures(total_exposures);
+        for (std::size_t k = 0; k < beams.size() && ok; ++k) {
+            auto& b = beams[k];
+            b.heel.weights = b.heel_weights.data();
+            dxmc_spectrum_desc spec { static_cast<int32_t>(b.spec_energies.size()), b.spec_energies.data(), b.spec_weights.data() };
+            dxmc_bowtie_desc bowtie { static_cast<int32_t>(b.bowtie_angles.size()), b.bowtie_angles.data(), b.bowtie_weights.data() };
+            dxmc_job_desc jd {};
+            jd.exposures = b.exposures.data();
+            jd.n_exposures = b.exposures.size();
+            jd.spectrum = b.spec_energies.empty() ? nullptr : &spec;
+            jd.heel = b.has_heel ? &b.heel : nullptr;
+            jd.bowtie = b.bowtie_angles.empty() ? nullptr : &bowtie;
+            jd.seed = seed + k * 0x9E3779B97F4A7C15ull;
+            jd.model = static_cast<int32_t>(m_model);
+            jd.tally_mode = -1;
+            jd.tracking = m_tracking;
+            jd.direction = m_direction;
+            jd.precision = m_precision;
+            ok = check(dxmc_gpu_job_submit(m_ctx, dworld, lut, &jd, &jobs[k]), "job submit");
+        }
         bool cancelled = false;
         std::uint64_t reported = 0; // exposures reported to the progress bar
-        std::vector<double> preview;
+        std::vector<double> preview, part;
         auto last_preview = std::chrono::steady_clock::now();
-        const std::uint64_t per_exposure = std::max<std::uint64_t>(1, flat.exposures.empty() ? 1 : flat.exposures[0].n_histories);
-        while (ok) {
-            const int rc = dxmc_gpu_job_wait(job, 50);
-            if (rc == DXMC_OK)
-                break;
-            if (rc != DXMC_ERR_TIMEOUT) {
-                ok = check(rc, "job wait");
-                break;
-            }
-            if (progressbar && progressbar->cancel() && !cancelled) {
-                dxmc_gpu_job_cancel(job);
-                cancelled = true;
-            }
-            if (progressbar && !cancelled) {
-                // ProgressBar::exposureCompleted per exposure's worth of histories taken, and
-                // a dose preview from the live tally about once a second (progressbar.hpp:54-101)
-                std::uint64_t started = 0;
-                if (dxmc_gpu_job_progress(job, &started, nullptr) == DXMC_OK) {
-                    const std::uint64_t done = std::min<std::uint64_t>(started / per_exposure, flat.exposures.size());
+        const std::uint64_t per_exposure = std::max<std::uint64_t>(1, beams[0].exposures.empty() ? 1 : beams[0].exposures[0].n_histories);
+        for (std::size_t k = 0; k < jobs.size() && ok; ++k) {
+            while (ok) {
+                const int rc = dxmc_gpu_job_wait(jobs[k], 50);
+                if (rc == DXMC_OK)
+                    break;
+                if (rc != DXMC_ERR_TIMEOUT) {
+                    ok = check(rc, "job wait");
+                    break;
+                }
+                if (progressbar && progressbar->cancel() && !cancelled) {
+                    for (auto* j : jobs)
+                        dxmc_gpu_job_cancel(j);
+                    cancelled = true;
+                }
+                if (progressbar && !cancelled) {
+                    // ProgressBar::exposureCompleted per exposure's worth of histories taken, and
+                    // a dose preview from the live tallies about once a second (progressbar.hpp:54-101)
+                    std::uint64_t started = 0;
+                    for (auto* j : jobs) {
+                        std::uint64_t s_j = 0;
+                        if (dxmc_gpu_job_progress(j, &s_j, nullptr) == DXMC_OK)
+                            started += s_j;
+                    }
+                    const std::uint64_t done = std::min<std::uint64_t>(started / per_exposure, total_exposures);
                     for (; reported < done; ++reported)
                         progressbar->exposureCompleted();
-                }
-                const auto now = std::chrono::steady_clock::now();
-                if (now - last_preview > std::chrono::seconds(1)) {
-                    last_preview = now;
-                    preview.resize(n);
-                    if (dxmc_gpu_job_preview(job, preview.data()) == DXMC_OK) {
-                        for (std::size_t i = 0; i < n; ++i)
-                            result.dose[i] = static_cast<T>(preview[i]);
-                        progressbar->setDoseData(result.dose.data(), world.dimensions(), world.spacing());
+                    const auto now = std::chrono::steady_clock::now();
+                    if (now - last_preview > std::chrono::seconds(1)) {
+                        last_preview = now;
+                        preview.assign(n, 0.0);
+                        part.resize(n);
+                        bool got = true;
+                        for (auto* j : jobs) {
+                            got = got && dxmc_gpu_job_preview(j, part.data()) == DXMC_OK;
+                            for (std::size_t i = 0; got && i < n; ++i)
+                                preview[i] += part[i];
+                        }
+                        if (got) {
+                            for (std::size_t i = 0; i < n; ++i)
+                                result.dose[i] = static_cast<T>(preview[i]);
+                            progressbar->setDoseData(result.dose.data(), world.dimensions(), world.spacing());
+                        }
                     }
                 }
             }
         }
         result.simulationTime = std::chrono::system_clock::now() - start;
         if (ok && !cancelled) {
-            std::uint64_t histories = 0;
-            for (const auto& e : flat.exposures)
-                histories += e.n_histories;
             result.numberOfHistories = histories;
-            std::vector<double> dose(n), var(n);
-            int mode = DXMC_OUTPUT_EV_PER_HISTORY;
             double cal = 1.0;
-            if (m_mode == OUTPUTMODE::DOSE) {
-                mode = DXMC_OUTPUT_DOSE;
+            if (m_mode == OUTPUTMODE::DOSE)
                 cal = useSourceDoseCalibration ? static_cast<double>(calibrationValue(source, progressbar)) : 1.0;
-            }
-            ok = check(dxmc_gpu_job_result(job, mode, cal, dose.data(), var.data(), result.nEvents.data(), nullptr), "job result");
-            if (ok) {
-                for (std::size_t i = 0; i < n; ++i) {
+            if (jobs.size() == 1) {
+                std::vector<double> dose(n), var(n);
+                const int mode = m_mode == OUTPUTMODE::DOSE ? DXMC_OUTPUT_DOSE : DXMC_OUTPUT_EV_PER_HISTORY;
+                ok = check(dxmc_gpu_job_result(jobs[0], mode, cal, dose.data(), var.data(), result.nEvents.data(), nullptr), "job result");
+                for (std::size_t i = 0; ok && i < n; ++i) {
                     result.dose[i] = static_cast<T>(dose[i]);
                     result.variance[i] = static_cast<T>(var[i]);
                 }
-                result.dose_units = m_mode == OUTPUTMODE::DOSE ? (useSourceDoseCalibration ? "mGy" : "keV/kg") : "eV/history";
             } else {
-                result.numberOfHistories = 0;
+                // the beams' raw tallies add; then the reference's normalisation over all
+                // histories (normalizeScoring / energyImpartedToDose, transport.hpp:780-816)
+                std::vector<double> e(n, 0.0), e2(n, 0.0), de(n), de2(n);
+                std::vector<std::uint32_t> ev(n);
+                std::fill(result.nEvents.begin(), result.nEvents.end(), 0u);
+                for (auto* j : jobs) {
+                    ok = ok && check(dxmc_gpu_job_result(j, DXMC_OUTPUT_RAW, 1.0, de.data(), de2.data(), ev.data(), nullptr), "job result");
+                    for (std::size_t i = 0; ok && i < n; ++i) {
+                        e[i] += de[i];
+                        e2[i] += de2[i];
+                        result.nEvents[i] += ev[i];
+                    }
+                }
+                if (ok && m_mode == OUTPUTMODE::DOSE) {
+                    const auto& sp = world.spacing();
+                    const double voxel_volume = sp[0] * sp[1] * sp[2] / 1000.0; // cm3
+                    for (std::size_t i = 0; i < n; ++i) {
+                        const double d = static_cast<double>(dsrc[i]);
+                        const double factor = d > 0.0 ? cal / (d * voxel_volume * 0.001) : 0.0; // per kg
+                        result.dose[i] = static_cast<T>(d > 0.0 ? e[i] * factor : 0.0);
+                        result.variance[i] = static_cast<T>(d > 0.0 ? e2[i] * factor * factor : 0.0);
+                    }
+                } else if (ok) {
+                    const double h = static_cast<double>(histories);
+                    for (std::size_t i = 0; i < n; ++i) {
+                        const double d = e[i] * (1e3 / h);
+                        result.dose[i] = static_cast<T>(d);
+                        result.variance[i] = static_cast<T>((e2[i] * (1e6 / h) - d * d) * (1.0 / (h - 1.0)));
+                    }
+                }
             }
+            if (ok)
+                result.dose_units = m_mode == OUTPUTMODE::DOSE ? (useSourceDoseCalibration ? "mGy" : "keV/kg") : "eV/history";
+            else
+                result.numberOfHistories = 0;
         }
         if (progressbar)
             progressbar->clearDoseData();
-        dxmc_gpu_job_free(job);
+        for (auto* j : jobs)
+            dxmc_gpu_job_free(j);
         dxmc_gpu_lut_free(lut);
         dxmc_lut_blob_free(blob);
         dxmc_gpu_world_free(dworld);
@@ -381,8 +478,8 @@ public:
         return result;
     }
 
-    // Source::getCalibrationValue, with the CTDI calibration run of CT spiral and axial
-    // sources (CTBaseSource::ctCalibration, source.hpp:925-988) done by this GPU transport
+    // Source::getCalibrationValue, with the CTDI calibration run of the CT sources
+    // (CTBaseSource::ctCalibration, source.hpp:925-988) done by this GPU transport
     // instead of a second CPU transport; other sources keep their own (closed-form) value.
     T calibrationValue(Source<T>* source, ProgressBar<T>* progressbar = nullptr)
     {
@@ -394,11 +491,35 @@ public:
             CTAxialSource<T> copy(*axial); // source.hpp:1277-1281
             return ctCalibration(copy);
         }
+        if (auto* sdual = dynamic_cast<CTSpiralDualSource<T>*>(source)) {
+            CTAxialDualSource<T> copy(*sdual); // source.hpp:1576-1581, both tubes in the CTDI run
+            return ctCalibration(copy) * sdual->pitch();
+        }
+        if (auto* adual = dynamic_cast<CTAxialDualSource<T>*>(source)) {
+            CTAxialDualSource<T> copy(*adual); // source.hpp:1477-1481
+            return ctCalibration(copy);
+        }
+        if (auto* topo = dynamic_cast<CTTopogramSource<T>*>(source)) {
+            // CTTopogramSource::getCalibrationValue (source.hpp:1679-1701): an axial source
+            // with the topogram's CT settings, stepping one collimation, CTDIvol scaled by
+            // the scan length over the collimation, the angle step matched to the exposures
+            CTAxialSource<T> copy;
+            static_cast<CTBaseSource<T>&>(copy) = static_cast<const CTBaseSource<T>&>(*topo);
+            copy.setCtdiVol(topo->ctdiVol() * topo->scanLenght() / topo->collimation());
+            copy.setScanLenght(0);
+            copy.setStep(topo->collimation());
+            const T max_step = (2 * PI_VAL<T>()) / 72;
+            const auto exposures = topo->totalExposures();
+            copy.setExposureAngleStep(std::min(2 * PI_VAL<T>() / exposures, max_step));
+            const T factor = ctCalibration(copy);
+            return factor * exposures / copy.totalExposures();
+        }
         return source->getCalibrationValue(m_model, progressbar);
     }
 
 private:
-    T ctCalibration(CTAxialSource<T>& copy)
+    template <typename Axial>
+    T ctCalibration(Axial& copy)
     {
         T meanWeight = 0;
         for (std::uint64_t i = 0; i < copy.totalExposures(); ++i)

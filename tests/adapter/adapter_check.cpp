@@ -62,6 +62,46 @@ int main()
         flat.has_heel ? 1 : 0, flat.spec_energies.size());
     failures += !flat_ok;
 
+    // 1b) a dual-source scanner flattens into two beams: the even exposures with tube
+    // A's spectrum and heel table, the odd ones with tube B's (CTDualSource)
+    {
+        CTSpiralDualSource<double> dual;
+        dual.setCollimation(20);
+        dual.setScanLenght(30);
+        dual.tubeB().setVoltage(80);
+        dual.tubeB().setAlFiltration(6.0);
+        dual.setTubeBmas(250);
+        dual.setModelHeelEffect(false); // the dual source builds its heel tables regardless
+        dual.setHistoriesPerExposure(10);
+        dual.validate();
+        std::vector<gpu::FlatSource<double>> beams;
+        bool dual_ok = gpu::flatten_beams<double>(world, &dual, beams) && beams.size() == 2;
+        double dmax = 0;
+        for (std::uint64_t i = 0; dual_ok && i < dual.totalExposures(); ++i) {
+            auto e = dual.getExposure(i);
+            e.alignToDirectionCosines(world.directionCosines());
+            const auto& f = beams[i % 2].exposures[i / 2];
+            for (int k = 0; k < 3; ++k)
+                dmax = std::max(dmax, std::abs(e.position()[k] - f.position[k]));
+            dmax = std::max(dmax, std::abs(e.beamIntensityWeight() - f.weight));
+        }
+        const auto eb = dual.tubeB().getEnergy();
+        const auto wb = dual.tubeB().getSpecter(eb);
+        dual_ok = dual_ok && dmax == 0 && beams[0].exposures.size() + beams[1].exposures.size() == dual.totalExposures()
+            && beams[0].has_heel && beams[1].has_heel && beams[1].spec_energies.size() == eb.size()
+            && beams[1].spec_weights == std::vector<double>(wb.begin(), wb.end())
+            && beams[0].spec_energies.size() == dual.tube().getEnergy().size()
+            && beams[1].heel.energy_size < beams[0].heel.energy_size;
+        std::printf("%s dual-source beams=%zu exposures=%zu+%zu maxdiff=%g\n", dual_ok ? "OK" : "FAIL", beams.size(),
+            beams.size() > 0 ? beams[0].exposures.size() : 0, beams.size() > 1 ? beams[1].exposures.size() : 0, dmax);
+        failures += !dual_ok;
+        std::vector<gpu::FlatSource<double>> single;
+        const bool single_ok = gpu::flatten_beams<double>(world, &ct, single) && single.size() == 1
+            && single[0].exposures.size() == ct.totalExposures();
+        std::printf("%s single-source beams=%zu\n", single_ok ? "OK" : "FAIL", single.size());
+        failures += !single_ok;
+    }
+
     // 2) LUT through the provider == DXMClib's AttenuationLut on the same Material objects
     AttenuationLut<double> ref;
     ref.generate(world, 90.0);
