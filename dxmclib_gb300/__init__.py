@@ -6,15 +6,15 @@ ABI declared in include/dxmc_gpu.h.
 """
 from ._capi import DxmcError, load as load_library  # noqa: F401
 from .api import (  # noqa: F401
-    LOWENERGYCORRECTION, Batch, BatchEntry, Beam, CTAxialDualSource, CTAxialSource, CTSpiralDualSource, CTSpiralSource,
-    CTTopogramSource, DeviceLut, DeviceWorld, DXSource, ExposureTable, GpuContext, HeelTable, IsotropicSource, Job, LutBlob,
+    LOWENERGYCORRECTION, Batch, BatchEntry, Beam, CBCTSource, CTAxialDualSource, CTAxialSource, CTSpiralDualSource, CTSpiralSource,
+    CTTopogramSource, DAPSource, DeviceLut, DeviceWorld, DXSource, ExposureTable, GpuContext, HeelTable, IsotropicCTSource, IsotropicSource, Job, LutBlob,
     Material, PencilSource, Result, Source, Spectrum, Transport, World,
 )
 from .tube import HeelFilter, Tube  # noqa: F401
 from . import workloads  # noqa: F401
 
 __all__ = [
-    "LOWENERGYCORRECTION", "Batch", "BatchEntry", "Beam", "CTAxialDualSource", "CTAxialSource", "CTSpiralDualSource",
+    "LOWENERGYCORRECTION", "Batch", "BatchEntry", "Beam", "CBCTSource", "DAPSource", "IsotropicCTSource", "CTAxialDualSource", "CTAxialSource", "CTSpiralDualSource",
     "CTSpiralSource", "CTTopogramSource", "DeviceLut", "DeviceWorld", "DXSource", "ExposureTable", "GpuContext",
     "HeelTable", "IsotropicSource", "Job", "LutBlob", "Material", "PencilSource", "Result", "Source", "Spectrum",
     "Transport", "World", "HeelFilter", "Tube", "DxmcError", "load_library",

@@ -517,8 +517,23 @@ class IsotropicSource(Source):
                                    1.0, self._hpe, 0.0, world_cosines)
 
 
-class DXSource(Source):
-    """DXSource (source.hpp:379-677): projection radiography with tube spectrum and heel effect."""
+class IsotropicCTSource(IsotropicSource):
+    """IsotropicCTSource (source.hpp:346-377): the isotropic source rotated about z
+    through a full turn over its exposures."""
+
+    def exposures(self, world_cosines=(1, 0, 0, 0, 1, 0)):
+        n = self._total
+        angle = (np.arange(n, dtype=np.float64) * 2 * PI) / n
+        z = np.array([0.0, 0.0, 1.0])
+        pos = _rotate(np.tile(self._position, (n, 1)), z, angle)
+        cos = np.concatenate([_rotate(np.tile(self._cosines[:3], (n, 1)), z, angle),
+                              _rotate(np.tile(self._cosines[3:], (n, 1)), z, angle)], axis=1)
+        return ExposureTable.build(pos, cos, self._coll, 1.0, self._hpe, 0.0, world_cosines)
+
+
+class DAPSource(Source):
+    """DAPSource (source.hpp:379-632): a tube with spectrum and heel effect, a field
+    at the source-detector distance and the dose-area-product calibration."""
 
     def __init__(self):
         super().__init__()
@@ -581,12 +596,6 @@ class DXSource(Source):
         self._coll = np.abs(np.asarray(angles, np.float64))
         self._field = np.tan(self._coll / 2) * self._sdd * 2
 
-    def setTotalExposures(self, n):
-        self._total = max(int(n), 1)
-
-    def totalExposures(self):
-        return self._total
-
     def setModelHeelEffect(self, on: bool):
         self._heel = bool(on)
 
@@ -625,16 +634,9 @@ class DXSource(Source):
         cos[3:] = _rotate(cos[3:], beam, self._tube_rotation)
         self.setDirectionCosines(cos)
 
-    def tubePosition(self):
-        beam = _cross(self._cosines[:3], self._cosines[3:])
-        return self._position - beam * self._sdd
-
-    def exposures(self, world_cosines=(1, 0, 0, 0, 1, 0)):
-        n = self._total
+    def _collimation4(self):
         c = self._coll
-        coll = (-c[0] / 2, c[0] / 2, -c[1] / 2, c[1] / 2)
-        return ExposureTable.build(np.tile(self.tubePosition(), (n, 1)), np.tile(self._cosines, (n, 1)), coll,
-                                   1.0, self._hpe, 0.0, world_cosines)
+        return (-c[0] / 2, c[0] / 2, -c[1] / 2, c[1] / 2)
 
     def spectrum(self):
         e = self._tube.getEnergy()
@@ -644,6 +646,84 @@ class DXSource(Source):
         if not self._heel:
             return None
         return HeelFilter(self._tube, self._coll[1]).table()
+
+
+class DXSource(DAPSource):
+    """DXSource (source.hpp:634-677): projection radiography, every exposure from the
+    tube at the source-detector distance behind the position."""
+
+    def setTotalExposures(self, n):
+        self._total = max(int(n), 1)
+
+    def totalExposures(self):
+        return self._total
+
+    def tubePosition(self):
+        beam = _cross(self._cosines[:3], self._cosines[3:])
+        return self._position - beam * self._sdd
+
+    def exposures(self, world_cosines=(1, 0, 0, 0, 1, 0)):
+        n = self._total
+        return ExposureTable.build(np.tile(self.tubePosition(), (n, 1)), np.tile(self._cosines, (n, 1)),
+                                   self._collimation4(), 1.0, self._hpe, 0.0, world_cosines)
+
+
+class CBCTSource(DAPSource):
+    """CBCTSource (source.hpp:679-782): the tube, at half the source-detector distance
+    from the position, rotates about the source's second direction cosine in steps
+    of ``stepAngle`` over ``spanAngle``."""
+
+    def __init__(self):
+        super().__init__()
+        self._total = 180
+        self._span = PI
+        self._step_angle = PI / 180
+        self.setSourceDetectorDistance(500.0)
+
+    def setSpanAngle(self, a):
+        self._span = max(float(a), self._step_angle)
+        self._total = max(int(self._span / self._step_angle), 2)
+
+    def setSpanAngleDeg(self, a):
+        self.setSpanAngle(a * DEG_TO_RAD)
+
+    def spanAngle(self):
+        return self._span
+
+    def spanAngleDeg(self):
+        return self._span / DEG_TO_RAD
+
+    def setStepAngle(self, a):
+        self._step_angle = max(float(a), PI / 360)
+        self._total = max(int(self._span / self._step_angle), 2)
+
+    def setStepAngleDeg(self, a):
+        self.setStepAngle(a * DEG_TO_RAD)
+
+    def stepAngle(self):
+        return self._step_angle
+
+    def stepAngleDeg(self):
+        return self._step_angle / DEG_TO_RAD
+
+    def totalExposures(self):
+        return self._total
+
+    def rotationAxis(self):
+        return self._cosines[3:].copy()
+
+    def tubePosition(self):
+        beam = _cross(self._cosines[:3], self._cosines[3:])
+        return self._position - beam * self._sdd * 0.5
+
+    def exposures(self, world_cosines=(1, 0, 0, 0, 1, 0)):
+        n = self._total
+        angle = np.arange(n, dtype=np.float64) * self._step_angle
+        axis = self.rotationAxis()
+        iso = _rotate(np.tile(self.tubePosition() - self._position, (n, 1)), axis, angle) + self._position
+        cos = np.concatenate([_rotate(np.tile(self._cosines[:3], (n, 1)), axis, angle),
+                              _rotate(np.tile(self._cosines[3:], (n, 1)), axis, angle)], axis=1)
+        return ExposureTable.build(iso, cos, self._collimation4(), 1.0, self._hpe, 0.0, world_cosines)
 
 
 class Beam:

@@ -489,6 +489,25 @@ def gen_ct_family(out: Path, quick: bool):
                         **{k: np.array(v) for k, v in factors.items()})
 
 
+def gen_more_sources(out: Path):
+    """Exposure, spectrum and heel tables of the cone-beam CT source (CBCTSource,
+    source.hpp:679-782) and the rotating isotropic source (IsotropicCTSource,
+    source.hpp:346-377)."""
+    n = 32
+    w = R.WorldArgs((n, n, n), (4, 4, 4), np.ones(n ** 3), np.zeros(n ** 3, np.uint8), ["Water, Liquid"])
+    cases = {
+        "cbct": R.SourceArgs(R.CBCT, position=(5, -3, 10), kvp=90, al_mm=4.0, field_size=(250, 200), sdd=600,
+                             source_angles_deg=(20, -15), span_deg=200, step_deg=2.5, heel=1,
+                             histories_per_exposure=100),
+        "isotropic_ct": R.SourceArgs(R.ISOTROPIC_CT, position=(0, -300, 20), cosines=(1, 0, 0, 0, 0, 1),
+                                     collimation=(-0.3, 0.3, -0.05, 0.05), spec_energies=np.arange(20, 81, 5.0),
+                                     spec_weights=np.linspace(1, 3, 13), histories_per_exposure=100,
+                                     total_exposures=36),
+    }
+    for name, src in cases.items():
+        np.savez_compressed(out / f"source_{name}.npz", **R.source_tables(src, w))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true")
@@ -502,7 +521,7 @@ def main():
                  interactions=lambda: gen_interactions(out, a.quick), ctdi=lambda: gen_ctdi(out, a.quick),
                  bench_ct=lambda: gen_bench_ct(out, a.quick), bench_dx=lambda: gen_bench_dx(out, a.quick),
                  dose=lambda: gen_dose(out, a.quick), tubes=lambda: gen_tubes(out),
-                 ct_family=lambda: gen_ct_family(out, a.quick))
+                 ct_family=lambda: gen_ct_family(out, a.quick), more_sources=lambda: gen_more_sources(out))
     for name, fn in steps.items():
         if a.only and name not in a.only.split(","):
             continue

@@ -130,3 +130,40 @@ def test_single_tube_ct_sources_have_one_beam(lib, golden):
         (b,) = srcs[name].beams()
         _check_heel(b.heel, g, "x0_")
         np.testing.assert_allclose(b.exposures.as_matrix(), g["exposures"], rtol=0, atol=1e-9)
+
+
+def test_cbct_and_isotropic_ct_exposures_match_reference(lib, golden):
+    """CBCTSource (source.hpp:679-782: the tube at half the source-detector distance,
+    rotating about the second direction cosine) and IsotropicCTSource
+    (source.hpp:346-377: rotation about z over the exposures)."""
+    import dxmclib_gb300 as dx
+    cb = dx.CBCTSource()
+    cb.tube().setVoltage(90)
+    cb.tube().setAlFiltration(4.0)
+    cb.setPosition((5, -3, 10))
+    cb.setSourceDetectorDistance(600)
+    cb.setFieldSize((250, 200))
+    cb.setSourceAnglesDeg(20, -15)
+    cb.setSpanAngleDeg(200)
+    cb.setStepAngleDeg(2.5)
+    cb.setModelHeelEffect(True)
+    cb.setHistoriesPerExposure(100)
+    iso = dx.IsotropicCTSource()
+    iso.setPosition((0, -300, 20))
+    iso.setDirectionCosines((1, 0, 0, 0, 0, 1))
+    iso.setCollimationAngles(-0.3, 0.3, -0.05, 0.05)
+    iso.setSpecter(np.linspace(1, 3, 13), np.arange(20, 81, 5.0))
+    iso.setHistoriesPerExposure(100)
+    iso.setTotalExposures(36)
+    for name, src in (("cbct", cb), ("isotropic_ct", iso)):
+        g = golden(f"source_{name}.npz")
+        ex = src.exposures().as_matrix()
+        assert ex.shape == g["exposures"].shape, name
+        np.testing.assert_allclose(ex, g["exposures"], rtol=0, atol=1e-9, err_msg=name)
+        assert src.maxPhotonEnergyProduced() == pytest.approx(float(g["max_energy"])), name
+    g = golden("source_cbct.npz")
+    h = cb.heel()
+    meta = g["heel_meta"]
+    assert (h.energy_size, h.angle_size) == (int(meta[3]), int(meta[6]))
+    np.testing.assert_allclose(h.weights, g["heel_weights"], rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(cb.spectrum().weights, g["spec_weights"], rtol=1e-12, atol=1e-300)
