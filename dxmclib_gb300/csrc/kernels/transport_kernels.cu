@@ -650,8 +650,11 @@ namespace {
     // One iteration of the warp-synchronous loop for every lane of the warp: a
     // Woodcock step for lanes without a pending interaction (transport.hpp:650-699),
     // the per-type interaction passes once enough lanes wait (transport.hpp:523-638),
-    // Russian roulette and scoring.  Must be called by all 32 lanes.
-    template <int MODEL, bool PALETTE, class Real>
+    // Russian roulette and scoring.  Must be called by all 32 lanes.  LEAN (the
+    // persistent multi-job kernel, which holds more state per lane) keeps the voxel
+    // read after the truncation test and one interaction pass per event type: the
+    // overlapped reads and the merged pass cost that kernel more spills than they save.
+    template <int MODEL, bool PALETTE, bool LEAN = false, class Real>
     __device__ __forceinline__ void advance(LaneT<Real>& s, WarpTally& wt, const TransportParams& p, const float* L, const PaletteEntry* pal,
         bool drain, int interact_t)
     {
@@ -711,11 +714,14 @@ namespace {
                 const Real cinv = s.cinv; // the majorant this flight was drawn with
                 // the voxel is read before the majorant cell, so that the two L2 reads
                 // overlap (a truncated flight does not use the voxel)
-                if constexpr (PALETTE) // compact worlds have fewer than 2^32 voxels (world upload)
-                    s.vidx = iz * static_cast<uint32_t>(w.nxy) + (iy * w.dims[0] + ix);
-                else
-                    s.vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
-                const VoxelRaw<PALETTE> raw = load_voxel<PALETTE>(w, s.vidx);
+                VoxelRaw<PALETTE> raw {};
+                if constexpr (!LEAN) {
+                    if constexpr (PALETTE) // compact worlds have fewer than 2^32 voxels (world upload)
+                        s.vidx = iz * static_cast<uint32_t>(w.nxy) + (iy * w.dims[0] + ix);
+                    else
+                        s.vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
+                    raw = load_voxel<PALETTE>(w, s.vidx);
+                }
                 if (p.majorant.cells) {
                     const MajorantGrid& g = p.majorant;
                     const uint32_t c = (iz >> g.shift[2]) * g.nxy + (iy >> g.shift[1]) * g.nx + (ix >> g.shift[0]);
@@ -725,6 +731,13 @@ namespace {
                 }
                 if (truncated)
                     continue;
+                if constexpr (LEAN) {
+                    if constexpr (PALETTE)
+                        s.vidx = iz * static_cast<uint32_t>(w.nxy) + (iy * w.dims[0] + ix);
+                    else
+                        s.vidx = static_cast<uint64_t>(iz) * w.nxy + static_cast<uint64_t>(iy) * w.dims[0] + ix;
+                    raw = load_voxel<PALETTE>(w, s.vidx);
+                }
                 Real density;
                 int mat;
                 bool measured;
@@ -795,7 +808,7 @@ namespace {
         }
 
         // ---- interaction passes, one converged pass per event type ---------------------
-        if constexpr (MODEL == 1) {
+        if constexpr (MODEL == 1 && !LEAN) {
             // LIVERMORE: Compton and Rayleigh both draw one quantile from an energy-row
             // table and rotate the direction, and photoabsorption only ends the photon,
             // so every waiting lane runs in one pass (Rayleigh lanes ride along instead
@@ -1160,9 +1173,9 @@ namespace {
             if (live2 == 0u)
                 continue; // waiting to switch jobs with nothing in flight: refill again
             if (p.world.palette_index)
-                advance<MODEL, true>(s, wt, p, p.lut, pal, exhausted || have_next, interact_t);
+                advance<MODEL, true, true>(s, wt, p, p.lut, pal, exhausted || have_next, interact_t);
             else
-                advance<MODEL, false>(s, wt, p, p.lut, pal, exhausted || have_next, interact_t);
+                advance<MODEL, false, true>(s, wt, p, p.lut, pal, exhausted || have_next, interact_t);
         }
         if (job >= 0)
             flush_counters(s, wt, p.counters);
