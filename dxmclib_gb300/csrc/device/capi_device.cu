@@ -1973,8 +1973,9 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
 //   the kernel's constant bank, LUT staged in shared memory, photon queue).  The
 //   context owns a few chains (a stream and a photon-queue buffer each); a batch
 //   deals its jobs longest-first onto the chains with the least outstanding work,
-//   shortest-first within a chain, captures each chain's share as one CUDA graph
-//   and launches it on the chain's stream.  Chains run side by side, so one job's
+//   shortest-first within a chain, and launches each chain's share on the chain's
+//   stream (a one-off sequence: instantiating it as a graph would cost more than
+//   its few launches).  Chains run side by side, so one job's
 //   blocks fill the SMs as another chain's job drains, and a batch submitted while
 //   others run queues behind them chain by chain (continuous batching); jobs on a
 //   chain run one after another, which is what lets them share its queue buffer.
@@ -2376,34 +2377,14 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
             std::reverse(lists[c].begin(), lists[c].end()); // shortest first within the chain
             Chain& ch = en->chain[c];
             e = cudaStreamWaitEvent(ch.stream, b->start, 0);
-            cudaGraph_t graph = nullptr;
             uint64_t share = 0;
-            if (e == cudaSuccess) {
-                step = "batch capture";
-                e = cudaStreamBeginCapture(ch.stream, cudaStreamCaptureModeThreadLocal);
-            }
-            if (e == cudaSuccess) {
-                cudaError_t ce = cudaSuccess;
-                for (size_t k = 0; k < lists[c].size() && ce == cudaSuccess; ++k) {
-                    const int i = lists[c][k];
-                    ce = enqueue_job(b->jobs[i], params[i], models[i], chunks[i], ch.queue, plans[i], ch.stream, true);
-                    share += b->jobs[i]->histories;
-                }
-                e = cudaStreamEndCapture(ch.stream, &graph);
-                if (ce != cudaSuccess)
-                    e = ce;
-            }
-            cudaGraphExec_t exec = nullptr;
-            if (e == cudaSuccess) {
-                step = "batch graph instantiation";
-                e = cudaGraphInstantiate(&exec, graph, 0);
-            }
-            if (graph)
-                cudaGraphDestroy(graph);
-            if (e == cudaSuccess) {
-                b->execs.push_back(exec);
-                step = "batch graph launch";
-                e = cudaGraphLaunch(exec, ch.stream);
+            // the chain's jobs go straight onto its stream: a batch's launch sequence is
+            // used once, and instantiating it as a graph cost milliseconds per chain
+            step = "batch launch";
+            for (size_t k = 0; k < lists[c].size() && e == cudaSuccess; ++k) {
+                const int i = lists[c][k];
+                e = enqueue_job(b->jobs[i], params[i], models[i], chunks[i], ch.queue, plans[i], ch.stream, false);
+                share += b->jobs[i]->histories;
             }
             cudaEvent_t end = nullptr;
             if (e == cudaSuccess)

@@ -160,26 +160,63 @@ const std::vector<double>& fluence_matrix(double T0)
 
 } // namespace
 
-double thick_target_bremsstrahlung(double T0, double hv, double takeoff_angle)
+namespace {
+
+// Photons of energy hv produced per depth node by electrons of initial energy T0
+// (the fluence matrix times the cross sections).  It does not depend on the
+// take-off angle, so a heel table's spectra at several angles, and every tube
+// with the same voltage, share it.
+struct DepthKey {
+    double T0, hv;
+    bool operator==(const DepthKey& o) const { return T0 == o.T0 && hv == o.hv; }
+};
+struct DepthKeyHash {
+    std::size_t operator()(const DepthKey& k) const
+    {
+        return std::hash<double>()(k.T0) * 1000003u ^ std::hash<double>()(k.hv);
+    }
+};
+
+const std::vector<double>& production_at_depth(double T0, double hv)
 {
-    if (hv <= 0)
-        return 0;
-    const double att = tungsten_attenuation(hv);
+    static std::mutex m;
+    static std::unordered_map<DepthKey, std::vector<double>, DepthKeyHash> cache;
+    std::lock_guard<std::mutex> lock(m);
+    const DepthKey key { T0, hv };
+    auto it = cache.find(key);
+    if (it != cache.end())
+        return it->second;
     const auto& xs = depth_grid();
     const auto& us = fraction_grid();
     const auto& rho = fluence_matrix(T0);
     std::vector<double> sigma(us.size());
     for (std::size_t k = 0; k < us.size(); ++k)
         sigma[k] = bethe_heitler(hv, T0 * us[k]);
+    std::vector<double> at_depth(xs.size());
+    for (std::size_t j = 0; j < xs.size(); ++j) {
+        const double* r = rho.data() + j * us.size();
+        double a = 0;
+        for (std::size_t k = 0; k < us.size(); ++k)
+            a = a + sigma[k] * r[k] * FRACTION_STEP;
+        at_depth[j] = a;
+    }
+    return cache.emplace(key, std::move(at_depth)).first->second;
+}
+
+} // namespace
+
+double thick_target_bremsstrahlung(double T0, double hv, double takeoff_angle)
+{
+    if (hv <= 0)
+        return 0;
+    const double att = tungsten_attenuation(hv);
+    const auto& xs = depth_grid();
+    const auto& at_depth = production_at_depth(T0, hv);
     const double sin_takeoff = std::sin(takeoff_angle);
     double total = 0;
     for (std::size_t j = 0; j < xs.size(); ++j) {
-        const double* r = rho.data() + j * us.size();
-        double at_depth = 0;
-        for (std::size_t k = 0; k < us.size(); ++k)
-            at_depth = at_depth + sigma[k] * r[k] * FRACTION_STEP;
         // photons produced at depth x leave the anode through x / sin(takeoff) of tungsten
-        total = total + at_depth * std::exp(-att * xs[j] * 0.001 / sin_takeoff) * DEPTH_STEP;
+        total = total + at_depth[j] * std::exp(-att * xs[j] * 0.001 / sin_takeoff) * DEPTH_STEP;
     }
     return total;
 }

@@ -126,15 +126,42 @@ class _PinnedPool:
     """Page-locked buffers reused by size; at most ``keep_bytes`` kept idle.
     Page-locking costs milliseconds per hundred megabytes, so buffers are kept
     and reused: sizes are rounded up to 1/16 of their power of two (at most
-    6 % waste), and ``prewarm`` allocates the buffers a world's results need
-    when the world becomes resident."""
+    6 % waste), ``prewarm`` allocates the buffers a world's results need when
+    the world becomes resident, and a background thread allocates another
+    buffer of a size whenever a ``get`` leaves none of it idle, so that results
+    held by clients do not make the collector page-lock memory itself."""
 
-    def __init__(self, lib, keep_bytes: int = 32 * GIB):
+    def __init__(self, lib, keep_bytes: int = 32 * GIB, spares: int = 2):
         self.lib = lib
         self.keep_bytes = keep_bytes
+        self.spares = spares
         self.free_lists: Dict[int, List[_Pinned]] = collections.defaultdict(list)
         self.idle = 0
+        self.pending: Dict[int, int] = collections.defaultdict(int)  # refills queued per size
         self.lock = threading.Lock()
+        self._refills: "queue.Queue[Optional[int]]" = queue.Queue()
+        self._refiller = threading.Thread(target=self._refill_loop, name="dxmc-pinned-refill", daemon=True)
+        self._refiller.start()
+
+    def _refill_loop(self):
+        while True:
+            size = self._refills.get()
+            if size is None:
+                return
+            with self.lock:
+                self.pending[size] -= 1
+                if self.idle + size > self.keep_bytes:
+                    continue
+            try:
+                self.put(_Pinned(self, size))
+            except Exception:  # out of page-locked memory: the collector allocates on demand
+                pass
+
+    def _request_refill(self, size: int):
+        # caller holds the lock
+        while len(self.free_lists.get(size, [])) + self.pending[size] < self.spares:
+            self.pending[size] += 1
+            self._refills.put(size)
 
     @staticmethod
     def _size(nbytes: int) -> int:
@@ -157,10 +184,12 @@ class _PinnedPool:
         size = self._size(nbytes)
         with self.lock:
             lst = self.free_lists.get(size)
+            buf = None
             if lst:
                 self.idle -= size
-                return lst.pop()
-        return _Pinned(self, size)
+                buf = lst.pop()
+            self._request_refill(size)
+        return buf if buf is not None else _Pinned(self, size)
 
     def put(self, b: _Pinned):
         with self.lock:
@@ -171,6 +200,8 @@ class _PinnedPool:
         b.free()
 
     def close(self):
+        self._refills.put(None)
+        self._refiller.join()
         with self.lock:
             for lst in self.free_lists.values():
                 for b in lst:

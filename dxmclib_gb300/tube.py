@@ -14,12 +14,18 @@ from 10 keV in 2 keV steps, 5 angle bins across the heel span).
 """
 from __future__ import annotations
 
+import collections
 import math
+import threading
 from typing import List, Tuple
 
 import numpy as np
 
 DEG = math.pi / 180.0
+
+_SPECTRUM_CACHE: "collections.OrderedDict" = collections.OrderedDict()
+_SPECTRUM_CACHE_ENTRIES = 4096
+_SPECTRUM_LOCK = threading.Lock()
 
 
 class Tube:
@@ -28,7 +34,6 @@ class Tube:
         self._anode = anode_angle_deg * DEG
         self._res = energy_resolution
         self._filters: List[Tuple[object, float]] = []
-        self._w_cache = {}
 
     @staticmethod
     def maxVoltage():
@@ -109,14 +114,19 @@ class Tube:
     def getSpecter(self, energies=None, anode_angle=None, normalize: bool = True) -> np.ndarray:
         e = self.getEnergy() if energies is None else np.asarray(energies, np.float64)
         a = self._anode if anode_angle is None else anode_angle
-        # spectra are deterministic in the tube settings: memoise them
+        # spectra are deterministic in the tube settings: memoised across every Tube
+        # (sources built per request repeat a few settings)
         key = (self._state(), e.tobytes(), float(a), bool(normalize))
-        cache = self._w_cache.setdefault("spectra", {})
-        hit = cache.get(key)
-        if hit is not None:
-            return hit.copy()
+        with _SPECTRUM_LOCK:
+            hit = _SPECTRUM_CACHE.get(key)
+            if hit is not None:
+                _SPECTRUM_CACHE.move_to_end(key)
+                return hit.copy()
         spec = self._compute_specter(e, a, normalize)
-        cache[key] = spec.copy()
+        with _SPECTRUM_LOCK:
+            _SPECTRUM_CACHE[key] = spec.copy()
+            while len(_SPECTRUM_CACHE) > _SPECTRUM_CACHE_ENTRIES:
+                _SPECTRUM_CACHE.popitem(last=False)
         return spec
 
     def _compute_specter(self, e: np.ndarray, a: float, normalize: bool) -> np.ndarray:
