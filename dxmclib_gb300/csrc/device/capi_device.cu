@@ -16,6 +16,7 @@
 #include <new>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 using namespace dxmc_gb300;
@@ -150,6 +151,46 @@ struct JobBufferCache {
     }
 };
 
+// Page-locked staging blocks for the host-to-device copy of a job's tables.  A
+// copy from pageable memory returns only once the driver has staged it, which
+// waited for the copy engine behind other jobs' result copies (tens of
+// milliseconds each while serving); from a page-locked block the copy is queued
+// at once.  A job holds its block until it is freed; blocks go back to a free
+// list per size class and are released with the context.
+struct PinnedStaging {
+    std::unordered_map<size_t, std::vector<void*>> free_blocks;
+    std::vector<void*> blocks;
+    static size_t size_class(size_t bytes)
+    {
+        size_t c = size_t { 64 } << 10;
+        while (c < bytes)
+            c <<= 1;
+        return c;
+    }
+    cudaError_t take(size_t bytes, void** p, size_t* cls)
+    {
+        *cls = size_class(bytes);
+        auto& l = free_blocks[*cls];
+        if (!l.empty()) {
+            *p = l.back();
+            l.pop_back();
+            return cudaSuccess;
+        }
+        const cudaError_t e = cudaHostAlloc(p, *cls, cudaHostAllocDefault);
+        if (e == cudaSuccess)
+            blocks.push_back(*p);
+        return e;
+    }
+    void give(void* p, size_t cls) { free_blocks[cls].push_back(p); }
+    void release()
+    {
+        for (void* b : blocks)
+            cudaFreeHost(b);
+        blocks.clear();
+        free_blocks.clear();
+    }
+};
+
 struct dxmc_gpu_ctx {
     BatchEngines* engines = nullptr; // created by the first batch
     cudaMemPool_t pool = nullptr;    // stream-ordered allocations of this context
@@ -168,6 +209,7 @@ struct dxmc_gpu_ctx {
     size_t max_smem_optin = 0;
     uint64_t submission = 0; // counts the calls that may build grids (job, batch, world prepare)
     PinnedSlots pinned;      // the jobs' cancel flags and counter copies
+    PinnedStaging staging;   // the jobs' tables on their way to the device
     JobBufferCache job_buffers; // idle tally and queue buffers of finished jobs
     // Page-locked, mapped area for the small read-backs a call waits for (palette
     // size and table, a grid's level histogram, per-material maxima).  A kernel
@@ -264,6 +306,8 @@ struct dxmc_job {
     unsigned char* tables = nullptr;
     unsigned char* queue = nullptr; // pre-generated photons (SoA)
     uint64_t tally_bytes = 0, count_bytes = 0, queue_bytes = 0; // sizes of the cached buffers above
+    void* staging = nullptr; // page-locked copy of the tables (PinnedStaging)
+    size_t staging_class = 0;
     int* cancel_host = nullptr;  // pinned, mapped; the counters' host copy follows at byte 16
     int* cancel_dev = nullptr;
     cudaEvent_t begin = nullptr, start = nullptr, stop = nullptr; // job begin, kernel start, kernel end
@@ -825,6 +869,7 @@ void dxmc_gpu_ctx_destroy(dxmc_gpu_ctx* ctx)
     ctx->job_buffers.release(ctx->stream);
     cudaStreamSynchronize(ctx->stream);
     ctx->pinned.release();
+    ctx->staging.release();
     cudaFreeHost(ctx->readback_host);
     cudaStreamDestroy(ctx->upload_stream);
     cudaStreamDestroy(ctx->result_stream);
@@ -1297,6 +1342,12 @@ void free_job_device(dxmc_job* j, bool idle)
         cudaFreeAsync(j->counters, s);
     if (j->tables)
         cudaFreeAsync(j->tables, s);
+    if (j->staging) {
+        if (!idle)
+            cudaStreamSynchronize(s); // the tables copy may still be queued
+        j->ctx->staging.give(j->staging, j->staging_class);
+        j->staging = nullptr;
+    }
     j->queue = nullptr;
     j->records = nullptr;
     j->tally_f32 = nullptr;
@@ -1770,7 +1821,11 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     if (e == cudaSuccess)
         e = cudaMemsetAsync(j->counters, 0, sizeof(dev::JobCounters), s);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(j->tables, tables.data(), table_bytes, cudaMemcpyHostToDevice, s);
+        e = ctx->staging.take(table_bytes, &j->staging, &j->staging_class);
+    if (e == cudaSuccess) {
+        std::memcpy(j->staging, tables.data(), table_bytes);
+        e = cudaMemcpyAsync(j->tables, j->staging, table_bytes, cudaMemcpyHostToDevice, s);
+    }
     if (e == cudaSuccess)
         e = cudaEventCreate(&j->start);
     if (e == cudaSuccess)
@@ -2651,6 +2706,13 @@ int dxmc_gpu_job_progress(dxmc_job* j, uint64_t* started, uint64_t* total)
     if (!j->counters)
         return fail(ctx, DXMC_ERR_STATE, "job results were already released");
     cudaSetDevice(ctx->device);
+    if (total)
+        *total = j->histories;
+    // before the job's kernel starts, its counters may not be cleared yet (a reused buffer)
+    if (cudaEventQuery(j->start) != cudaSuccess) {
+        *started = 0;
+        return DXMC_OK;
+    }
     auto* hc = reinterpret_cast<dev::JobCounters*>(reinterpret_cast<unsigned char*>(j->cancel_host) + 16);
     // a racy snapshot of a counter the kernels only increase
     DXMC_CUDA(ctx, cudaMemcpyAsync(&hc->next_history, &j->counters->next_history, 3 * sizeof(unsigned long long),
@@ -2673,6 +2735,11 @@ int dxmc_gpu_job_preview(dxmc_job* j, double* energy)
         return fail(ctx, DXMC_ERR_STATE, j->tally_f32 ? "dose preview needs the FP64 tally" : "job results were already released");
     cudaSetDevice(ctx->device);
     const uint64_t nv = j->world->params.n_voxels;
+    // before the job's kernel starts, its tally may not be cleared yet (a reused buffer)
+    if (cudaEventQuery(j->start) != cudaSuccess) {
+        std::fill(energy, energy + nv, 0.0);
+        return DXMC_OK;
+    }
     // the energy sum of each 32-byte tally record
     DXMC_CUDA(ctx, cudaMemcpy2DAsync(energy, sizeof(double), j->records, sizeof(dev::TallyRecord), sizeof(double), nv,
         cudaMemcpyDeviceToHost, ctx->result_stream));

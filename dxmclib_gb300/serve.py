@@ -446,6 +446,7 @@ class DoseServer:
 
     # -- scheduler ------------------------------------------------------------------------
     def _loop(self):
+        idle_polls = 0
         while True:
             busy = bool(self.waiting or self.admitted or self.inflight or self._collecting)
             try:
@@ -467,8 +468,13 @@ class DoseServer:
             progressed |= self._launch()
             if self._stop and not (self.waiting or self.admitted or self.inflight or self._collecting):
                 return
-            if not progressed and (self.inflight or self.waiting or self._collecting):
-                time.sleep(5e-5)
+            if progressed:
+                idle_polls = 0
+            elif self.inflight or self.waiting or self._collecting:
+                # poll the running jobs with a growing pause (50 us to 1 ms): a tight loop
+                # of completion queries takes the interpreter from the collector thread
+                time.sleep(min(5e-5 * (1 << min(idle_polls, 5)), 1e-3))
+                idle_polls += 1
 
     def _fail(self, req: ServeRequest, exc: BaseException):
         self.errors.append(exc)
