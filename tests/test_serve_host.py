@@ -221,3 +221,69 @@ def test_poisson_arrivals():
     t = poisson_arrivals(100.0, 20000, seed=3)
     assert np.all(np.diff(t) >= 0)
     assert abs(t[-1] / 20000 - 0.01) < 0.0005
+
+
+class FakeHostLib:
+    """dxmc_gpu_host_alloc / _free over ordinary host memory, counting calls."""
+
+    def __init__(self):
+        import ctypes as C
+        self.C = C
+        self.live = {}
+        self.allocs = 0
+        self.lock = threading.Lock()
+
+    def dxmc_gpu_host_alloc(self, nbytes, out):
+        buf = self.C.create_string_buffer(int(nbytes))
+        with self.lock:
+            self.allocs += 1
+            self.live[self.C.addressof(buf)] = buf
+        out._obj.value = self.C.addressof(buf)
+        return 0
+
+    def dxmc_gpu_host_free(self, ptr):
+        with self.lock:
+            self.live.pop(ptr.value, None)
+
+
+def test_pinned_pool_refills_in_the_background():
+    """A get that leaves a size without idle buffers makes the background thread
+    allocate spares, so that the next gets of that size reuse page-locked memory
+    instead of allocating on the collector's thread; returned buffers are reused."""
+    from dxmclib_gb300.serve import _PinnedPool
+    lib = FakeHostLib()
+    pool = _PinnedPool(lib, keep_bytes=1 << 30, spares=2)
+    try:
+        a = pool.get(100_000)
+        assert lib.allocs == 1  # nothing idle yet: allocated on the spot
+        deadline = time.time() + 5
+        while lib.allocs < 3 and time.time() < deadline:
+            time.sleep(0.01)
+        assert lib.allocs == 3  # two spares of that size arrived
+        size = pool._size(100_000)
+        assert a.nbytes == size and len(pool.free_lists[size]) == 2
+        b = pool.get(100_000)
+        c = pool.get(100_000)
+        assert lib.allocs >= 3 and b.nbytes == size and c.nbytes == size
+        for buf in (a, b, c):
+            buf.give_back()
+        assert len(pool.free_lists[size]) >= 3
+        d = pool.get(99_000)  # the same size class
+        assert d.nbytes == size
+    finally:
+        pool.close()
+    assert len(lib.live) == 1  # closing frees every idle buffer; d is still held
+
+
+def test_pinned_pool_keeps_at_most_keep_bytes_idle():
+    from dxmclib_gb300.serve import _PinnedPool
+    lib = FakeHostLib()
+    pool = _PinnedPool(lib, keep_bytes=300_000, spares=0)
+    try:
+        bufs = [pool.get(100_000) for _ in range(5)]
+        size = bufs[0].nbytes
+        for b in bufs:
+            b.give_back()
+        assert pool.idle <= 300_000 and pool.idle == size * len(pool.free_lists[size])
+    finally:
+        pool.close()
