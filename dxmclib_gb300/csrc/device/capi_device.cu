@@ -1457,8 +1457,8 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
                 scales[static_cast<size_t>(band) * dev::PALETTE_MAX + m] = ratio[m];
         }
     }
-    // each band's emptiest level (the palette's highest level); for the 8-byte layout
-    // the levels are not known on the host and the box is not used
+    // each band's emptiest level: the palette's highest level; for the 8-byte layout it
+    // comes from the device's level histogram after the first level pass (below)
     std::vector<int> floor_level(b.bands, -1);
     bool use_box = false;
     if (w->palette_index && DXMC_MAJORANT_BOX) {
@@ -1538,6 +1538,27 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
         e = cudaStreamSynchronize(s);
     if (e == cudaSuccess)
         std::memcpy(hist.data(), ctx->readback_host, hist.size() * sizeof(unsigned int));
+    // 8-byte layout: the host learns the cells' levels only now.  Each band's emptiest
+    // level is the lowest of the run of populated levels that ends at its highest one
+    // (air and what is as thin as air; the body lies levels below), and the level pass
+    // runs again with those levels to find the box of the cells above them
+    if (e == cudaSuccess && !w->palette_index && DXMC_MAJORANT_BOX) {
+        for (int band = 0; band < b.bands; ++band) {
+            const unsigned int* hb = hist.data() + static_cast<size_t>(band) * 64;
+            int top = -1;
+            for (int lv = MAJORANT_MAX_LEVEL; lv >= 0 && top < 0; --lv)
+                if (hb[lv])
+                    top = lv;
+            int floor = top;
+            while (floor > 1 && hb[floor - 1])
+                --floor;
+            floor_level[band] = floor >= 1 ? floor : -1;
+            b.floor_levels[band] = floor_level[band];
+            use_box = use_box || floor_level[band] >= 0;
+        }
+        if (use_box)
+            e = dev::launch_majorant_levels(w->params, d_scales, b, level, cells, cost, bounds, d_hist, s);
+    }
     // each cell's lowest level over its neighbourhood: the dilated set of every level
     if (e == cudaSuccess)
         e = dev::launch_majorant_minfilter(b, level, minlev, s);

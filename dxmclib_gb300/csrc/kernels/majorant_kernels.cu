@@ -177,14 +177,16 @@ __global__ void majorant_box_kernel(const __grid_constant__ MajorantBuild b, con
         if (!outside)
             continue;
         for (int k = 0; k < b.bands; ++k) {
-            // every cell outside the box lies at or below the band's emptiest level: a
-            // flight may run to the box with the cell's scale only if that scale is at
-            // least the emptiest level's (the host finds that level in double
-            // arithmetic, the cells' levels here in float, which may differ by one)
+            // every cell outside the box lies at or below the band's emptiest level (the
+            // box holds every cell above it), so a flight drawn with that level's scale
+            // may run to the box: a cell whose own scale is smaller takes the level's
+            // (a larger majorant bounds everything its own did, within its R as well)
             const int fl = b.floor_levels[k];
             float2& cell = cells[c * b.bands + k];
-            if (fl >= 0 && cell.x <= 1.0f / level_scale(fl, b.levels_per_octave))
+            if (fl >= 0) {
+                cell.x = fminf(cell.x, 1.0f / level_scale(fl, b.levels_per_octave));
                 cell.y = -cell.y;
+            }
         }
     }
 }
