@@ -689,11 +689,14 @@ def main():
     e2e_steps = max(1, min(args.steps, 5))
 
     def e2e_submit(seed, buf):
+        # the source's host tables first: they are built while the previous job runs,
+        # the world upload then waits for its kernel to leave the SMs
+        ex = src.exposures(e2e_world.directionCosines())
+        spectrum, heel = src.spectrum(), src.heel()
         dw = dx.DeviceWorld(ctx, e2e_world, layout=args.layout)
         bl = dx.LutBlob.cached(e2e_world.materialMap(), dw.max_density(), src.maxPhotonEnergyProduced())
         dl = dx.DeviceLut(ctx, bl)
-        ex = src.exposures(e2e_world.directionCosines())
-        job = dx.Job(ctx, dw, dl, ex, src.spectrum(), src.heel(), None, seed=seed, model=args.model)
+        job = dx.Job(ctx, dw, dl, ex, spectrum, heel, None, seed=seed, model=args.model)
         job.result_async(A.OUTPUT_EV_PER_HISTORY, out=buf, dtype=np.float32)
         return job, dl, dw
 

@@ -803,7 +803,12 @@ int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out)
         delete ctx;
         return DXMC_ERR_DEVICE;
     }
-    if (cudaStreamCreateWithFlags(&ctx->upload_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    // uploads and grid builds at the device's greatest priority: a world's palette
+    // kernels and its majorant grid are what the next job waits for, so their blocks
+    // take the SMs before an earlier job's post-processing
+    int least_priority = 0, greatest_priority = 0;
+    cudaDeviceGetStreamPriorityRange(&least_priority, &greatest_priority);
+    if (cudaStreamCreateWithPriority(&ctx->upload_stream, cudaStreamNonBlocking, greatest_priority) != cudaSuccess) {
         cudaStreamDestroy(ctx->result_stream);
         cudaStreamDestroy(ctx->stream);
         delete ctx;
@@ -1122,8 +1127,7 @@ void dxmc_gpu_world_free(dxmc_world* w)
     wait_unused(w->ctx, w->usage); // no queued batch, job or result post-processing still reads the grid
     // the voxels go back to the pool in the order of the upload stream (the host
     // has waited for their readers), so the next upload reuses them without
-    // waiting for the jobs queued on the context stream; the grids were built on
-    // the context stream and go back there
+    // waiting for the jobs queued on the context stream; the grids too
     if (w->voxels)
         cudaFreeAsync(w->voxels, w->ctx->upload_stream);
     if (w->palette_index)
@@ -1131,7 +1135,7 @@ void dxmc_gpu_world_free(dxmc_world* w)
     if (w->palette)
         cudaFreeAsync(w->palette, w->ctx->upload_stream);
     for (auto& m : w->majorants) {
-        cudaFreeAsync(m.cells, w->ctx->stream);
+        cudaFreeAsync(m.cells, w->ctx->upload_stream);
         w->ctx->in_use -= m.bytes;
     }
     w->usage.destroy();
@@ -1149,11 +1153,7 @@ int dxmc_gpu_world_prepare(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut*
     cudaSetDevice(ctx->device);
     ++ctx->submission; // no job of this call holds a grid: every grid but the new one may go
     const dev::MajorantGrid* grid = nullptr;
-    const int rc = world_majorant(ctx, world, lut, true, &grid);
-    if (rc != DXMC_OK)
-        return rc;
-    const cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    return e == cudaSuccess ? DXMC_OK : cuda_fail(ctx, e, "local-majorant grid");
+    return world_majorant(ctx, world, lut, true, &grid); // complete when it returns
 }
 
 int dxmc_gpu_world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut, uint32_t* cells_per_axis,
@@ -1485,11 +1485,13 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
         if (victim == w->majorants.end())
             break;
         sync_ctx_streams(ctx); // no queued job still reads the grid
-        cudaFreeAsync(victim->cells, ctx->stream);
+        cudaFreeAsync(victim->cells, ctx->upload_stream);
         ctx->in_use -= victim->bytes;
         w->majorants.erase(victim);
     }
-    cudaStream_t s = ctx->stream;
+    // built on the upload stream (greatest priority) and complete before the call
+    // returns, so jobs on any stream read it without a cross-stream wait
+    cudaStream_t s = ctx->upload_stream;
     float2* cells = nullptr;
     uint8_t* level = nullptr;
     uint8_t* minlev = nullptr;
@@ -1617,6 +1619,8 @@ int world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* w, const dxmc_lut* lut, bool b
              static_cast<void*>(bounds), static_cast<void*>(d_scales), static_cast<void*>(d_hist) })
         if (ptr)
             cudaFreeAsync(ptr, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         if (cells)
             cudaFreeAsync(cells, s);
