@@ -164,6 +164,7 @@ SIGNATURES = {
     "dxmc_lut_scatter_factor": (D, [VP, C.c_int, D]),
     "dxmc_lut_get_info": (C.c_int, [VP, C.POINTER(LutInfo)]),
     "dxmc_alias_table": (C.c_int, [DP, C.c_int, DP, U64P]),
+    "dxmc_bowtie_table": (C.c_int, [DP, DP, C.c_int, DP, DP]),
     "dxmc_stream_seed": (C.c_int, [C.c_uint64, C.c_uint64, U32P]),
     "dxmc_gpu_ctx_create": (C.c_int, [C.POINTER(GpuOptions), C.POINTER(VP)]),
     "dxmc_gpu_ctx_destroy": (None, [VP]),

@@ -1733,22 +1733,13 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     }
     std::vector<float> bt_a, bt_w;
     if (jd->bowtie) {
-        // BowTieFilter constructor: |angle|, sort, normalise to mean 1 (beamfilters.hpp:86-100)
+        // BowTieFilter constructor: |angle|, sort, normalise to mean 1 (beamfilters.hpp:86-130)
         const int n = jd->bowtie->n;
-        if (n <= 0 || !jd->bowtie->angles || !jd->bowtie->weights)
+        std::vector<double> ta(n > 0 ? n : 0), tw(n > 0 ? n : 0);
+        if (dxmc_bowtie_table(jd->bowtie->angles, jd->bowtie->weights, n, ta.data(), tw.data()) != DXMC_OK)
             return fail(ctx, DXMC_ERR_INVALID, "invalid bow-tie table");
-        std::vector<std::pair<double, double>> data(n);
-        for (int i = 0; i < n; ++i)
-            data[i] = { std::abs(jd->bowtie->angles[i]), jd->bowtie->weights[i] };
-        std::sort(data.begin(), data.end());
-        double mean = 0;
-        for (auto& p : data)
-            mean += p.second;
-        mean /= n;
-        for (auto& p : data) {
-            bt_a.push_back(static_cast<float>(p.first));
-            bt_w.push_back(static_cast<float>(p.second / mean));
-        }
+        bt_a.assign(ta.begin(), ta.end());
+        bt_w.assign(tw.begin(), tw.end());
     }
     // one device buffer for all tables
     size_t off = 0;

@@ -8,9 +8,12 @@
 #include "tube_spectrum.hpp"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <string>
+#include <utility>
+#include <vector>
 
 namespace phys = dxmc_gb300::physics;
 namespace host = dxmc_gb300::host;
@@ -207,6 +210,27 @@ int dxmc_lut_get_info(const dxmc_lut_blob* blob, dxmc_lut_info* info)
     info->rita = blob->rita.empty() ? nullptr : blob->rita[0].data();
     info->spline = blob->spline.empty() ? nullptr : blob->spline[0].data();
     info->shells = blob->shells.empty() ? nullptr : blob->shells[0].data();
+    return DXMC_OK;
+}
+
+int dxmc_bowtie_table(const double* angles, const double* weights, int n, double* table_angles, double* table_weights)
+{
+    if (n <= 0 || !angles || !weights || !table_angles || !table_weights)
+        return DXMC_ERR_INVALID;
+    std::vector<std::pair<double, double>> data(static_cast<size_t>(n));
+    for (int i = 0; i < n; ++i)
+        data[i] = { std::abs(angles[i]), weights[i] };
+    std::sort(data.begin(), data.end());
+    double sum = 0.0; // in table order, from zero: the normalisation's sum
+    for (const auto& p : data)
+        sum += p.second;
+    const double mean = sum / n;
+    if (!(mean > 0.0) || !std::isfinite(mean))
+        return DXMC_ERR_INVALID;
+    for (int i = 0; i < n; ++i) {
+        table_angles[i] = data[i].first;
+        table_weights[i] = data[i].second / mean;
+    }
     return DXMC_OK;
 }
 

@@ -134,6 +134,14 @@ int dxmc_tube_spectrum(double voltage_kv, double takeoff_angle, double line_take
     int n_energies, const dxmc_material_provider* filters, const double* filter_mm, int n_filters, int normalize,
     double* out);
 
+/* ---- bow-tie table (host; BowTieFilter<T>, beamfilters.hpp:65-197) ------- */
+/* The table a job samples bow-tie weights from: the n (|angle|, weight) pairs
+ * sorted by angle, weights divided by their mean (the BowTieFilter
+ * constructors and normalizeData, beamfilters.hpp:88-130).  angles in radians.
+ * DXMC_ERR_INVALID for n <= 0 or a mean weight that is not positive. */
+int dxmc_bowtie_table(const double* angles, const double* weights, int n, double* table_angles,
+    double* table_weights);
+
 /* ---- host LUT (AttenuationLut<T>::generate, attenuationlut.hpp:64-96) ---- */
 typedef struct dxmc_lut_blob dxmc_lut_blob;
 

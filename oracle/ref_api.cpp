@@ -18,7 +18,31 @@
 //   * ref_transport        Transport<double>::operator() (transport.hpp:135-202)
 //                          in EV_PER_HISTORY mode;
 //   * ref_interactions     the protected interaction samplers of Transport
-//                          (transport.hpp:216-483) driven through a subclass.
+//                          (transport.hpp:216-483) driven through a subclass;
+//   * ref_bowtie           BowTieFilter<double> (beamfilters.hpp:65-197): its
+//                          normalised table and sampleIntensityWeight.
+
+// BowTieFilter::normalizeData (beamfilters.hpp:88-92) sums its (angle, weight)
+// pairs with std::reduce and a lambda (double, pair) -> double.  GCC 13's
+// std::reduce asserts that the operation also takes (pair, pair) and
+// (pair, double), which that lambda does not, so the constructors fail to
+// compile.  The overload below, declared before the reference's headers, is
+// more specialised for that iterator type and is chosen instead: a left fold
+// from the initial value, the sum the reference's normalisation means.
+#include <numeric>
+#include <utility>
+#include <vector>
+namespace std {
+template <class T, class Op>
+double reduce(__gnu_cxx::__normal_iterator<pair<T, T>*, vector<pair<T, T>>> first,
+    __gnu_cxx::__normal_iterator<pair<T, T>*, vector<pair<T, T>>> last, double init, Op op)
+{
+    for (; first != last; ++first)
+        init = op(init, *first);
+    return init;
+}
+} // namespace std
+
 #include "dxmc/attenuationlut.hpp"
 #include "dxmc/source.hpp"
 #include "dxmc/transport.hpp"
@@ -216,10 +240,6 @@ std::unique_ptr<Source<T>> make_source(const RefSourceDesc& s)
     std::array<T, 6> cos {};
     for (int k = 0; k < 6; ++k)
         cos[k] = static_cast<T>(s.direction_cosines[k]);
-    // BowTieFilter's constructors (beamfilters.hpp:86-122) call normalizeData,
-    // whose std::reduce (beamfilters.hpp:90) does not compile against GCC 13's
-    // libstdc++; bow-tie weighting is therefore not exercised through the
-    // reference and the bowtie_* fields are ignored here.
     switch (s.type) {
     case REF_PENCIL: {
         auto p = std::make_unique<PencilSource<T>>();
@@ -366,6 +386,11 @@ std::unique_ptr<Source<T>> make_source(const RefSourceDesc& s)
         p->setScanLenght(s.scan_length);
         p->setModelHeelEffect(s.heel != 0);
         p->setHistoriesPerExposure(s.histories_per_exposure);
+        if (s.bowtie_n > 0) {
+            std::vector<T> a(s.bowtie_angles, s.bowtie_angles + s.bowtie_n);
+            std::vector<T> w(s.bowtie_weights, s.bowtie_weights + s.bowtie_n);
+            p->setBowTieFilter(std::make_shared<BowTieFilter<T>>(a, w));
+        }
         return p;
     }
     default:
@@ -376,6 +401,26 @@ std::unique_ptr<Source<T>> make_source(const RefSourceDesc& s)
 } // namespace
 
 extern "C" {
+
+// BowTieFilter<double>(angles, weights) (beamfilters.hpp:102-115): its table
+// (|angle| sorted, weights normalised to mean 1; n pairs into table_angles /
+// table_weights) and sampleIntensityWeight (beamfilters.hpp:150-190) at the
+// m query angles.
+int ref_bowtie(const double* angles, const double* weights, int n, const double* queries, int m,
+    double* table_angles, double* table_weights, double* out)
+{
+    if (n < 1 || !angles || !weights)
+        return -1;
+    const BowTieFilter<double> f(std::vector<double>(angles, angles + n), std::vector<double>(weights, weights + n));
+    const auto& d = f.data();
+    for (int i = 0; i < n; ++i) {
+        table_angles[i] = d[i].first;
+        table_weights[i] = d[i].second;
+    }
+    for (int i = 0; i < m; ++i)
+        out[i] = f.sampleIntensityWeight(queries[i]);
+    return 0;
+}
 
 // Number of energy nodes (after the first node is dropped) for a LUT built on
 // this world; lets the caller size the coefficient buffers.

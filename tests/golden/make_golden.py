@@ -30,7 +30,11 @@ tests/golden/ref_binding.py and stores, as small .npz files:
                     with Al / Cu filtration and two anode angles;
 * transport_dose_dx.npz Transport<double> in DOSE mode (mGy through the DX
                     dose-area-product calibration, and keV/kg without it) on a
-                    64^3 DX phantom, 2 x 2 x 2 block sums, with the factor.
+                    64^3 DX phantom, 2 x 2 x 2 block sums, with the factor;
+* bowtie.npz        BowTieFilter<double>'s normalised table and
+                    sampleIntensityWeight at query angles (beamfilters.hpp:65-197);
+* transport_ct_bowtie_m1.npz Transport<double> of a CT helical scan through a
+                    bow-tie filter (2 x 2 x 2 block sums, two independent runs).
 
 Usage:  make -C oracle REF=<reference checkout> && python tests/golden/make_golden.py [--quick]
 The generator needs the reference checkout and is not run by the test suite.
@@ -489,6 +493,48 @@ def gen_ct_family(out: Path, quick: bool):
                         **{k: np.array(v) for k, v in factors.items()})
 
 
+BOWTIE_ANGLES = np.array([0.2, 0.0, -0.06, 0.03, 0.1, 0.45, 0.15, 0.3, 0.25, 0.35, 0.4])
+
+
+def bowtie_weights(angles):
+    """A CT body bow-tie's fluence profile: 1 on the axis falling to about 0.15 at the
+    edge of a 500 mm field of view."""
+    a = np.abs(np.asarray(angles, np.float64))
+    return 0.15 + 0.85 * np.exp(-(a / 0.18) ** 2)
+
+
+def gen_bowtie(out: Path, quick: bool):
+    """BowTieFilter<double> (unsorted, one negative angle: |angle|, sort, mean-1
+    normalisation) and a CT helical scan through it (CTSpiralSource with
+    setBowTieFilter, source.hpp:821; the weight enters Exposure::sampleParticle)."""
+    w_raw = bowtie_weights(BOWTIE_ANGLES)
+    queries = np.concatenate([np.linspace(-0.5, 0.5, 201), np.abs(BOWTIE_ANGLES), -np.abs(BOWTIE_ANGLES)])
+    ta, tw, qw = R.bowtie(BOWTIE_ANGLES, w_raw, queries)
+    np.savez_compressed(out / "bowtie.npz", angles=BOWTIE_ANGLES, weights=w_raw, queries=queries, table_angles=ta,
+                        table_weights=tw, query_weights=qw)
+    mat, dens = hetero_world(n=48, spacing=4.0, seed=11)
+    dims = (48, 48, 48)
+    wt = R.WorldArgs(dims, (4.0, 4.0, 4.0), dens, mat, MATERIALS4)
+    hpe = 4000 if quick else 24000
+    s = R.SourceArgs(R.CTSPIRAL, position=(0, 0, -20), kvp=120, al_mm=2.5, ct_collimation=40, pitch=1.0,
+                     scan_length=40, angle_step_deg=1.0, start_angle_deg=0, fov=500, sdd=1190, heel=1,
+                     histories_per_exposure=hpe, bowtie=(BOWTIE_ANGLES, w_raw))
+    tabs = R.source_tables(s, wt)
+    runs = []
+    for k in range(2):
+        dose, var, nev, N, st = R.transport(wt, s, model=1)
+        print(f"ct bowtie run {k}: {N} histories {st:.2f} s", flush=True)
+        runs.append(block_tally(dose, var, nev, dims, (2, 2, 2)))
+    np.savez_compressed(out / "transport_ct_bowtie_m1.npz", dims=np.array(dims), spacing=np.array([4.0] * 3),
+                        material=mat, density=dens.astype(np.float32), names=np.array(MATERIALS4), histories=N,
+                        block=np.array([2, 2, 2]), exposures=tabs["exposures"], spec_energies=tabs["spec_energies"],
+                        spec_weights=tabs["spec_weights"], heel_meta=tabs["heel_meta"],
+                        heel_weights=tabs.get("heel_weights", np.zeros(0)), max_energy=tabs["max_energy"],
+                        bowtie_angles=BOWTIE_ANGLES, bowtie_weights=w_raw,
+                        same_method=same_method_stats(runs[0][1], runs[1][1]),
+                        **{f"r_{k}": v for k, v in runs[0][0].items()})
+
+
 def gen_more_sources(out: Path):
     """Exposure, spectrum and heel tables of the cone-beam CT source (CBCTSource,
     source.hpp:679-782) and the rotating isotropic source (IsotropicCTSource,
@@ -521,7 +567,8 @@ def main():
                  interactions=lambda: gen_interactions(out, a.quick), ctdi=lambda: gen_ctdi(out, a.quick),
                  bench_ct=lambda: gen_bench_ct(out, a.quick), bench_dx=lambda: gen_bench_dx(out, a.quick),
                  dose=lambda: gen_dose(out, a.quick), tubes=lambda: gen_tubes(out),
-                 ct_family=lambda: gen_ct_family(out, a.quick), more_sources=lambda: gen_more_sources(out))
+                 ct_family=lambda: gen_ct_family(out, a.quick), more_sources=lambda: gen_more_sources(out),
+                 bowtie=lambda: gen_bowtie(out, a.quick))
     for name, fn in steps.items():
         if a.only and name not in a.only.split(","):
             continue

@@ -157,7 +157,15 @@ class SourceArgs:
         s.start_angle_deg = float(kw.get("start_angle_deg", 0.0))
         s.fov = float(kw.get("fov", 500.0))
         s.tilt_deg = float(kw.get("tilt_deg", 0.0))
-        s.bowtie_n = 0
+        bowtie = kw.get("bowtie")
+        if bowtie is not None:
+            self.bt_a = np.ascontiguousarray(bowtie[0], np.float64)
+            self.bt_w = np.ascontiguousarray(bowtie[1], np.float64)
+            s.bowtie_angles = _dptr(self.bt_a)
+            s.bowtie_weights = _dptr(self.bt_w)
+            s.bowtie_n = len(self.bt_a)
+        else:
+            s.bowtie_n = 0
         s.axial_step = float(kw.get("axial_step", 0.0))
         s.set_b = int("kvp_b" in kw)
         s.kvp_b = float(kw.get("kvp_b", 120.0))
@@ -169,6 +177,20 @@ class SourceArgs:
         s.fov_b = float(kw.get("fov_b", 500.0))
         s.start_angle_b_deg = float(kw.get("start_angle_b_deg", 90.0))
         self.desc = s
+
+
+def bowtie(angles, weights, queries):
+    """BowTieFilter<double>(angles, weights): its normalised (angle, weight) table and
+    sampleIntensityWeight at the query angles (beamfilters.hpp:102-190)."""
+    a = np.ascontiguousarray(angles, np.float64)
+    w = np.ascontiguousarray(weights, np.float64)
+    q = np.ascontiguousarray(queries, np.float64)
+    ta, tw, out = np.zeros(len(a)), np.zeros(len(a)), np.zeros(len(q))
+    rc = lib().ref_bowtie(_dptr(a), _dptr(w), C.c_int(len(a)), _dptr(q), C.c_int(len(q)), _dptr(ta), _dptr(tw),
+                          _dptr(out))
+    if rc != 0:
+        raise RuntimeError(f"ref_bowtie failed: {rc}")
+    return ta, tw, out
 
 
 def transport(world: WorldArgs, source: SourceArgs, model: int = 1, n_threads: int = 0):

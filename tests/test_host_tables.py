@@ -263,6 +263,31 @@ def test_capi_exports_every_declared_symbol(lib):
     assert lib.dxmc_gpu_abi_version() == 3
 
 
+def test_bowtie_table_matches_reference(lib, golden):
+    """The table jobs sample bow-tie weights from (dxmc_bowtie_table) equals the
+    reference's BowTieFilter<double> table (beamfilters.hpp:102-130: |angle|,
+    sorted, weights over their mean), given unsorted and with a negative angle."""
+    from dxmclib_gb300 import _capi as A
+    g = golden("bowtie.npz")
+    a = np.ascontiguousarray(g["angles"], np.float64)
+    w = np.ascontiguousarray(g["weights"], np.float64)
+    ta, tw = np.zeros(len(a)), np.zeros(len(a))
+    assert lib.dxmc_bowtie_table(a.ctypes.data_as(A.DP), w.ctypes.data_as(A.DP), len(a), ta.ctypes.data_as(A.DP),
+                                 tw.ctypes.data_as(A.DP)) == A.DXMC_OK
+    np.testing.assert_array_equal(ta, g["table_angles"])
+    np.testing.assert_allclose(tw, g["table_weights"], rtol=1e-15, atol=0)
+    # sampleIntensityWeight (beamfilters.hpp:150-190): clamped at both ends, linear
+    # between the bracketing nodes; the device's binary search brackets the same pair
+    q = np.abs(g["queries"])
+    expect = np.interp(q, ta, tw)
+    np.testing.assert_allclose(g["query_weights"], expect, rtol=1e-13, atol=0)
+    zeros = np.zeros(3)
+    assert lib.dxmc_bowtie_table(a.ctypes.data_as(A.DP), zeros.ctypes.data_as(A.DP), 3, ta.ctypes.data_as(A.DP),
+                                 tw.ctypes.data_as(A.DP)) == A.DXMC_ERR_INVALID
+    assert lib.dxmc_bowtie_table(a.ctypes.data_as(A.DP), w.ctypes.data_as(A.DP), 0, ta.ctypes.data_as(A.DP),
+                                 tw.ctypes.data_as(A.DP)) == A.DXMC_ERR_INVALID
+
+
 def test_invalid_inputs_are_rejected(lib):
     from dxmclib_gb300 import _capi as A
     prov = A.MaterialProvider()

@@ -83,6 +83,28 @@ def test_port_ct_matches_reference(lib, golden):
     assert_parity(compare_sparse(g, d, v), "port ct")
 
 
+def test_port_ct_bowtie_matches_reference(lib, golden):
+    """A CT helical scan through a bow-tie filter (BowTieFilter, beamfilters.hpp:65-197:
+    |angle|, sorted, weights normalised to mean 1, interpolated in the fan angle)
+    against the reference's own transport of the same scan, as 2 x 2 x 2 block sums."""
+    from parity import block_sums
+    g = golden("transport_ct_bowtie_m1.npz")
+    dims = tuple(int(x) for x in g["dims"])
+    info = _lut(g["names"], g["material"], g["density"], float(g["max_energy"]))
+    hm = g["heel_meta"]
+    heel = dict(energy_start=hm[1], energy_step=hm[2], energy_size=hm[3], angle_start=hm[4], angle_step=hm[5],
+                angle_size=hm[6], weights=g["heel_weights"])
+    e, e2, nev, secs, steps = port.transport(info, dims, tuple(g["spacing"]), g["density"], g["material"],
+                                             g["exposures"], model=1, seed=13,
+                                             spectrum=(g["spec_energies"], g["spec_weights"]), heel=heel,
+                                             bowtie=(g["bowtie_angles"], g["bowtie_weights"]))
+    d, v = port.ev_per_history(e, e2, int(g["histories"]))
+    block = tuple(int(x) for x in g["block"])
+    ref = {"idx": g["r_idx"], "dose": g["r_dose"], "var": g["r_var"], "total": g["r_total"]}
+    s = compare_sparse(ref, block_sums(d, dims, block), block_sums(v, dims, block))
+    assert_parity(s, "port ct bow-tie (2x2x2 blocks)", max_chi2=max(1.2, float(g["same_method"][0])))
+
+
 def test_port_forced_matches_reference(lib, golden):
     import dxmclib_gb300 as dx
     g = golden("transport_forced_m1.npz")
