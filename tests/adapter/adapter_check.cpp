@@ -2,6 +2,8 @@
 // and checks the adapter on the host: exposure flattening, the LUT built through
 // the Material provider against DXMClib's own AttenuationLut, and the zero-Result
 // error convention when no GPU is present.  Prints one line per check.
+#include "std_reduce_shim.hpp" // oracle/: lets the reference's BowTieFilter compile with GCC 13
+
 #include "dxmc_gpu/transport.hpp"
 
 #include <cmath>
@@ -100,6 +102,30 @@ int main()
             && single[0].exposures.size() == ct.totalExposures();
         std::printf("%s single-source beams=%zu\n", single_ok ? "OK" : "FAIL", single.size());
         failures += !single_ok;
+        // a bow-tie filter travels as the filter's own table (BowTieFilter::data(),
+        // beamfilters.hpp:196), which the jobs' table build leaves as it is
+        const std::vector<double> bta { 0.2, 0.0, -0.06, 0.1, 0.4 }, btw { 0.6, 1.0, 0.95, 0.8, 0.2 };
+        ct.setBowTieFilter(std::make_shared<BowTieFilter<double>>(bta, btw));
+        std::vector<gpu::FlatSource<double>> with_bt;
+        bool bt_ok = gpu::flatten_beams<double>(world, &ct, with_bt) && with_bt.size() == 1;
+        const auto& data = ct.bowTieFilter()->data();
+        bt_ok = bt_ok && with_bt[0].bowtie_angles.size() == data.size() && with_bt[0].bowtie_weights.size() == data.size();
+        double bt_diff = 0;
+        if (bt_ok) {
+            std::vector<double> ta(data.size()), tw(data.size());
+            bt_ok = dxmc_bowtie_table(with_bt[0].bowtie_angles.data(), with_bt[0].bowtie_weights.data(),
+                        static_cast<int>(data.size()), ta.data(), tw.data())
+                == DXMC_OK;
+            for (std::size_t i = 0; i < data.size() && bt_ok; ++i) {
+                bt_ok = with_bt[0].bowtie_angles[i] == data[i].first && with_bt[0].bowtie_weights[i] == data[i].second
+                    && ta[i] == data[i].first;
+                bt_diff = std::max(bt_diff, std::abs(tw[i] - data[i].second));
+            }
+        }
+        bt_ok = bt_ok && bt_diff < 1e-15;
+        std::printf("%s bow-tie table n=%zu maxdiff=%g\n", bt_ok ? "OK" : "FAIL", data.size(), bt_diff);
+        failures += !bt_ok;
+        ct.setBowTieFilter(nullptr);
     }
 
     // 2) LUT through the provider == DXMClib's AttenuationLut on the same Material objects

@@ -20,7 +20,7 @@ def test_cpp_adapter_host_checks(lib, tmp_path):
     if REF is None or not (REF / "include" / "dxmc").is_dir():
         pytest.skip("DXMClib headers not available (set DXMC_REFERENCE to a reference checkout)")
     exe = tmp_path / "adapter_check"
-    cmd = ["g++", "-std=c++20", "-O1", "-pthread", f"-I{REF / 'include'}", f"-I{REPO / 'include'}",
+    cmd = ["g++", "-std=c++20", "-O1", "-pthread", f"-I{REF / 'include'}", f"-I{REPO / 'include'}", f"-I{REPO / 'oracle'}",
            str(REPO / "tests" / "adapter" / "adapter_check.cpp"), str(REPO / "oracle" / "material_backend.cpp"),
            str(REPO / "dxmclib_gb300" / "csrc" / "physics" / "physics_model.cpp"),
            f"-L{REPO / 'dxmclib_gb300' / 'lib'}", "-ldxmc_gpu", f"-Wl,-rpath,{REPO / 'dxmclib_gb300' / 'lib'}",
