@@ -287,7 +287,8 @@ void dxmc_gpu_world_free(dxmc_world* world);
  * (jobs with LOCAL tracking build it on first use; dxmc_gpu_transport_noalloc
  * uses it only if it exists).  A world keeps the grids of its last four LUTs:
  * building a fifth frees the least recently used one (after the jobs queued on
- * the context have finished), never one that an entry of the same batch reads. */
+ * the context have finished), never one that an entry of the same batch reads.
+ * The grid is built on the context's upload stream and is complete on return. */
 int dxmc_gpu_world_prepare(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut);
 /* Reads back a built local-majorant grid: cells per axis, log2 of the cell size
  * in voxels per axis, the number of energy bands, the band edges (keV, bands - 1
