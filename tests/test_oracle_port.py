@@ -185,3 +185,26 @@ def test_port_ct_benchmark_configuration_matches_reference(golden, precision):
     d, v = port.ev_per_history(e, e2, n)
     s = compare_sparse(g, block_sums(d, dims, block), block_sums(v, dims, block))
     assert_parity(s, f"port {precision} ct helical 512x512x200", max_chi2=max(1.2, float(g["same_method"][0])))
+
+
+def test_port_dx_benchmark_configuration_matches_reference(lib, golden):
+    """The port on the batched-radiography phantom (128^3, a DXSource beam with the
+    reference's own exposure, spectrum and heel tables) against Transport<double>
+    as 4 x 4 x 4 block sums, at half the reference's histories."""
+    from parity import block_sums
+    from dxmclib_gb300.workloads import DX_MATERIALS
+    g = golden("bench_dx.npz")
+    dims, block = tuple(int(x) for x in g["dims"]), tuple(int(x) for x in g["block"])
+    info = _lut(DX_MATERIALS, g["material"], g["density"], float(g["max_energy"]))
+    hm = g["heel_meta"]
+    heel = dict(energy_start=hm[1], energy_step=hm[2], energy_size=hm[3], angle_start=hm[4], angle_step=hm[5],
+                angle_size=hm[6], weights=g["heel_weights"])
+    ex = g["exposures"].copy()
+    ex[:, 17] = ex[:, 17] // 2
+    n = int(ex[:, 17].sum())
+    e, e2, nev, secs, steps = port.transport(info, dims, tuple(g["spacing"]), g["density"], g["material"], ex,
+                                             model=1, seed=21, spectrum=(g["spec_energies"], g["spec_weights"]),
+                                             heel=heel)
+    d, v = port.ev_per_history(e, e2, n)
+    s = compare_sparse(g, block_sums(d, dims, block), block_sums(v, dims, block))
+    assert_parity(s, "port dx 128^3 (4x4x4 blocks)", max_chi2=max(1.2, float(g["same_method"][0])))
