@@ -34,6 +34,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -293,6 +294,15 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         return reject(ctx, "invalid bow-tie table");
     if (bowtie_n > NOALLOC_MAX_BOWTIE)
         return reject(ctx, "dxmc_gpu_transport_noalloc: " + std::to_string(bowtie_n) + " bow-tie points exceed the maximum of " + std::to_string(NOALLOC_MAX_BOWTIE));
+    if (bowtie_n > 0) {
+        // the weights are normalised by their mean on the device: as the job entry
+        // point (dxmc_bowtie_table), a mean that is not positive is rejected here
+        double sum = 0.0;
+        for (int i = 0; i < bowtie_n; ++i)
+            sum += jd->bowtie->weights[i];
+        if (!(sum > 0.0) || !std::isfinite(sum))
+            return reject(ctx, "invalid bow-tie table");
+    }
     if (jd->tracking < DXMC_TRACKING_DEFAULT || jd->tracking > DXMC_TRACKING_LOCAL)
         return reject(ctx, "dxmc_gpu_transport_noalloc: unknown tracking mode");
     if (jd->direction != DXMC_DIRECTION_REFERENCE && jd->direction != DXMC_DIRECTION_NORMALIZED)

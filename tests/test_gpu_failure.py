@@ -76,6 +76,11 @@ def test_invalid_input_and_budget_are_refused(gpu_ctx):
     with pytest.raises(A.DxmcError) as e:
         dx.Job(ctx, dworld, dlut, wl.source.exposures(), None, None, None, model=7)
     assert e.value.status == A.DXMC_ERR_INVALID
+    # a bow-tie profile without a positive mean weight (its normalisation divides by it)
+    for weights in ([0.0, 0.0, 0.0], [1.0, -2.0, 0.5], [1.0, float("nan"), 1.0]):
+        with pytest.raises(A.DxmcError) as e:
+            dx.Job(ctx, dworld, dlut, wl.source.exposures(), None, None, ([0.0, 0.1, 0.2], weights), model=1)
+        assert e.value.status == A.DXMC_ERR_INVALID and "bow-tie" in str(e.value), weights
     # a context whose budget is smaller than the world
     tiny = dx.GpuContext(memory_budget=1 << 12)  # 4 KB: less than the 32 KB of voxels
     with pytest.raises(A.DxmcError) as e:

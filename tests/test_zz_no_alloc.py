@@ -163,5 +163,14 @@ def test_noalloc_matches_job_entry_point(gpu_ctx, golden):
                                             C.c_void_p(tally.data_ptr()), C.c_void_p(nev.data_ptr()), None)
     assert rc == A.DXMC_ERR_INVALID
     assert b"maximum" in ctx.lib.dxmc_gpu_last_error(ctx.handle)
+
+    # a bow-tie profile without a positive mean weight is rejected by both entry points
+    jd_bt = _job_desc(exposures, spectrum, heel, (bowtie[0], np.zeros(len(bowtie[0]))), seed, keep)
+    rc = ctx.lib.dxmc_gpu_transport_noalloc(ctx.handle, dworld.handle, dlut.handle, C.byref(jd_bt),
+                                            C.c_void_p(tally.data_ptr()), C.c_void_p(nev.data_ptr()), None)
+    assert rc == A.DXMC_ERR_INVALID
+    assert b"bow-tie" in ctx.lib.dxmc_gpu_last_error(ctx.handle)
+    rc = ctx.lib.dxmc_gpu_job_submit(ctx.handle, dworld.handle, dlut.handle, C.byref(jd_bt), C.byref(handle))
+    assert rc == A.DXMC_ERR_INVALID and not handle.value
     dlut.close()
     dworld.close()
