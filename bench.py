@@ -547,7 +547,11 @@ def main():
         if rank != 0:
             return
         cw = CpuWorkload(histories)
-        threads = os.cpu_count() or 1
+        # the cores this process may run on (a container or cgroup may offer fewer
+        # than the machine has); the host's load average beside the number shows
+        # whether other work shared those cores during the sample
+        threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+        load_before = os.getloadavg() if hasattr(os, "getloadavg") else None
         secs, secs64 = [], []
         for step in range(args.warmup + args.steps):
             t = cw.run(threads, args.model, "float", seed=100 + step)
@@ -570,7 +574,9 @@ def main():
                                  "double_value": (cw.sample_histories * len(secs64) / float(np.sum(secs64))
                                                   if secs64 else None),
                                  "sample_seconds": [round(t, 3) for t in secs],
-                                 "double_sample_seconds": [round(t, 3) for t in secs64]},
+                                 "double_sample_seconds": [round(t, 3) for t in secs64],
+                                 "host_load_avg_1_5_15m_before": ([round(x, 2) for x in load_before]
+                                                                  if load_before else None)},
                 "e2e": {"value": v, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
