@@ -548,15 +548,21 @@ def main():
             return
         cw = CpuWorkload(histories)
         # the cores this process may run on (a container or cgroup may offer fewer
-        # than the machine has); the host's load average beside the number shows
-        # whether other work shared those cores during the sample
+        # than the machine has), and the share of them the transport got: the
+        # process's CPU seconds, less the single-threaded set-up around the port's
+        # timed transport, over the transport's seconds x cores (about 1 when no
+        # other work shared the cores)
+        import resource
         threads = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
-        load_before = os.getloadavg() if hasattr(os, "getloadavg") else None
-        secs, secs64 = [], []
+        secs, secs64, share = [], [], []
         for step in range(args.warmup + args.steps):
+            r0, w0 = resource.getrusage(resource.RUSAGE_SELF), time.perf_counter()
             t = cw.run(threads, args.model, "float", seed=100 + step)
+            r1, w1 = resource.getrusage(resource.RUSAGE_SELF), time.perf_counter()
             if step >= args.warmup:
                 secs.append(t)
+                cpu_s = (r1.ru_utime - r0.ru_utime) + (r1.ru_stime - r0.ru_stime) - max((w1 - w0) - t, 0.0)
+                share.append(round(cpu_s / max(t * threads, 1e-9), 3))
         if args.cpu_precision == "both":  # Transport<double> beside the fair float baseline
             for step in range(args.warmup + args.steps):
                 t = cw.run(threads, args.model, "double", seed=200 + step)
@@ -575,8 +581,7 @@ def main():
                                                   if secs64 else None),
                                  "sample_seconds": [round(t, 3) for t in secs],
                                  "double_sample_seconds": [round(t, 3) for t in secs64],
-                                 "host_load_avg_1_5_15m_before": ([round(x, 2) for x in load_before]
-                                                                  if load_before else None)},
+                                 "core_share": share},
                 "e2e": {"value": v, "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
