@@ -50,3 +50,31 @@ def test_two_replicas_take_the_slowest_rank():
     for r, ws, slowest, value in res:
         assert ws == 2 and slowest == 2.0
         assert value == pytest.approx(2 * 1_000_000 * 5 / 2.0)
+
+
+def test_reference_arm_line():
+    """bench.py --impl reference on a small sample: one JSON line with the base
+    contract's keys, the CPU baseline's description (cores, share of them, sample)
+    and e2e equal to the line's value; the process loads no product library."""
+    import json
+    import subprocess
+    # run bench.py as __main__, then list the shared objects the process mapped
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0', "
+            "'--histories', '1e6']; runpy.run_path(sys.argv[0], run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('MAPS', sorted({l.split()[-1] for l in maps.splitlines() if l.split()[-1].endswith('.so')}))")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=str(REPO))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    maps = [x for x in r.stdout.splitlines() if x.startswith("MAPS")]
+    assert maps and "libdxmc_gpu" not in maps[0] and "liboracle_port" in maps[0], maps
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "config"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["higher_is_better"] is True and d["value"] > 0
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert len(cb["core_share"]) == 1 and 0.0 < cb["core_share"][0] < 1.5
+    assert d["e2e"] == {"value": d["value"], "unit": "histories/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"] == "ct_helical_512x512x200"
