@@ -14,6 +14,7 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <stdexcept>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -337,6 +338,36 @@ int fail(dxmc_gpu_ctx* ctx, int code, const std::string& msg)
 int cuda_fail(dxmc_gpu_ctx* ctx, cudaError_t e, const char* what)
 {
     return fail(ctx, DXMC_ERR_DEVICE, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// A C++ exception must not cross the C ABI.  The entry points that build host
+// tables (sized by the caller's input) call this from their catch clause: host
+// memory exhaustion becomes DXMC_ERR_OOM, anything else DXMC_ERR_INVALID, with
+// the reason in the context's last error.
+int exception_status(dxmc_gpu_ctx* ctx) noexcept
+{
+    int code = DXMC_ERR_INVALID;
+    const char* what = "unexpected exception";
+    try {
+        throw;
+    } catch (const std::bad_alloc&) {
+        code = DXMC_ERR_OOM;
+        what = "out of host memory";
+    } catch (const std::length_error&) {
+        code = DXMC_ERR_OOM;
+        what = "host table larger than the host can allocate";
+    } catch (const std::exception& e) {
+        what = e.what();
+    } catch (...) {
+    }
+    if (ctx) {
+        try {
+            std::lock_guard<std::mutex> lock(ctx->mutex);
+            ctx->last_error = what;
+        } catch (...) {
+        }
+    }
+    return code;
 }
 
 #define DXMC_CUDA(ctx, call)                         \
@@ -768,7 +799,7 @@ void dxmc_gpu_host_free(void* ptr)
 }
 
 int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out)
-{
+try {
     if (!out)
         return DXMC_ERR_INVALID;
     *out = nullptr;
@@ -862,6 +893,8 @@ int dxmc_gpu_ctx_create(const dxmc_gpu_options* options, dxmc_gpu_ctx** out)
     }
     *out = ctx;
     return DXMC_OK;
+} catch (...) {
+    return exception_status(nullptr);
 }
 
 void dxmc_gpu_ctx_destroy(dxmc_gpu_ctx* ctx)
@@ -889,7 +922,7 @@ const char* dxmc_gpu_last_error(const dxmc_gpu_ctx* ctx)
 }
 
 int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_world** out)
-{
+try {
     if (!ctx || !d || !out)
         return DXMC_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mutex);
@@ -1079,10 +1112,12 @@ int dxmc_gpu_world_upload(dxmc_gpu_ctx* ctx, const dxmc_world_desc* d, dxmc_worl
     P.n_voxels = n;
     *out = w;
     return DXMC_OK;
+} catch (...) {
+    return exception_status(ctx);
 }
 
 int dxmc_gpu_world_max_density(dxmc_world* w, double* out, int n_materials)
-{
+try {
     if (!w || !out || n_materials <= 0)
         return DXMC_ERR_INVALID;
     dxmc_gpu_ctx* ctx = w->ctx;
@@ -1116,6 +1151,8 @@ int dxmc_gpu_world_max_density(dxmc_world* w, double* out, int n_materials)
         out[i] = f;
     }
     return DXMC_OK;
+} catch (...) {
+    return exception_status(w ? w->ctx : nullptr);
 }
 
 void dxmc_gpu_world_free(dxmc_world* w)
@@ -1144,7 +1181,7 @@ void dxmc_gpu_world_free(dxmc_world* w)
 }
 
 int dxmc_gpu_world_prepare(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut)
-{
+try {
     if (!ctx || !world || !lut)
         return DXMC_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mutex);
@@ -1154,11 +1191,13 @@ int dxmc_gpu_world_prepare(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut*
     ++ctx->submission; // no job of this call holds a grid: every grid but the new one may go
     const dev::MajorantGrid* grid = nullptr;
     return world_majorant(ctx, world, lut, true, &grid); // complete when it returns
+} catch (...) {
+    return exception_status(ctx);
 }
 
 int dxmc_gpu_world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut* lut, uint32_t* cells_per_axis,
     int32_t* shift, int32_t* bands, float* band_edges, float* box, float* cells)
-{
+try {
     if (!ctx || !world || !lut || !cells_per_axis || !shift || !bands)
         return DXMC_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mutex);
@@ -1190,10 +1229,12 @@ int dxmc_gpu_world_majorant(dxmc_gpu_ctx* ctx, dxmc_world* world, const dxmc_lut
             return cuda_fail(ctx, e, "local-majorant grid read");
     }
     return DXMC_OK;
+} catch (...) {
+    return exception_status(ctx);
 }
 
 int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* b, dxmc_lut** out)
-{
+try {
     if (!ctx || !b || !out || b->n_materials <= 0)
         return DXMC_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mutex);
@@ -1304,6 +1345,8 @@ int dxmc_gpu_lut_upload(dxmc_gpu_ctx* ctx, const dxmc_lut_blob* b, dxmc_lut** ou
     ctx->in_use += lut->bytes;
     *out = lut;
     return DXMC_OK;
+} catch (...) {
+    return exception_status(ctx);
 }
 
 void dxmc_gpu_lut_free(dxmc_lut* lut)
@@ -1735,6 +1778,9 @@ int prepare_job(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_
     if (jd->bowtie) {
         // BowTieFilter constructor: |angle|, sort, normalise to mean 1 (beamfilters.hpp:86-130)
         const int n = jd->bowtie->n;
+        if (n > DXMC_MAX_BOWTIE_POINTS)
+            return fail(ctx, DXMC_ERR_INVALID, "bow-tie table has " + std::to_string(n) + " points, more than the maximum of "
+                    + std::to_string(DXMC_MAX_BOWTIE_POINTS));
         std::vector<double> ta(n > 0 ? n : 0), tw(n > 0 ? n : 0);
         if (dxmc_bowtie_table(jd->bowtie->angles, jd->bowtie->weights, n, ta.data(), tw.data()) != DXMC_OK)
             return fail(ctx, DXMC_ERR_INVALID, "invalid bow-tie table");
@@ -2009,7 +2055,7 @@ cudaError_t enqueue_job(dxmc_job* j, dev::TransportParams p, int model, uint64_t
 } // namespace
 
 int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_job_desc* jd, dxmc_job** out)
-{
+try {
     if (!ctx || !world || !lut || !jd || !out)
         return DXMC_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mutex);
@@ -2034,6 +2080,8 @@ int dxmc_gpu_job_submit(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, con
     ctx->in_use += j->bytes;
     *out = j;
     return DXMC_OK;
+} catch (...) {
+    return exception_status(ctx);
 }
 
 // ---- batches --------------------------------------------------------------------------
@@ -2277,7 +2325,7 @@ struct dxmc_batch {
 
 int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, int n, const dxmc_batch_options* opt,
     dxmc_batch** out)
-{
+try {
     if (!ctx || !entries || n <= 0 || !out)
         return DXMC_ERR_INVALID;
     *out = nullptr;
@@ -2482,6 +2530,8 @@ int dxmc_gpu_batch_submit(dxmc_gpu_ctx* ctx, const dxmc_batch_entry* entries, in
     }
     *out = b;
     return DXMC_OK;
+} catch (...) {
+    return exception_status(ctx);
 }
 
 int dxmc_gpu_batch_wait(dxmc_batch* b, int64_t timeout_ms)
@@ -2612,7 +2662,7 @@ int dxmc_gpu_job_cancel(dxmc_job* j)
 }
 
 int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double* dose, double* variance, uint32_t* n_events, dxmc_job_stats* stats)
-{
+try {
     if (!j || output_mode < 0 || output_mode > 2)
         return DXMC_ERR_INVALID;
     dxmc_gpu_ctx* ctx = j->ctx;
@@ -2711,6 +2761,8 @@ int dxmc_gpu_job_result(dxmc_job* j, int output_mode, double calibration, double
     if (c.overflows)
         return fail(ctx, DXMC_ERR_REJECTION_CAP, "sampling loops hit the rejection cap in " + std::to_string(c.overflows) + " events");
     return DXMC_OK;
+} catch (...) {
+    return exception_status(j ? j->ctx : nullptr);
 }
 
 int dxmc_gpu_job_progress(dxmc_job* j, uint64_t* started, uint64_t* total)
@@ -2742,7 +2794,7 @@ int dxmc_gpu_job_progress(dxmc_job* j, uint64_t* started, uint64_t* total)
 }
 
 int dxmc_gpu_job_preview(dxmc_job* j, double* energy)
-{
+try {
     if (!j || !energy)
         return DXMC_ERR_INVALID;
     dxmc_gpu_ctx* ctx = j->ctx;
@@ -2761,11 +2813,13 @@ int dxmc_gpu_job_preview(dxmc_job* j, double* energy)
         cudaMemcpyDeviceToHost, ctx->result_stream));
     DXMC_CUDA(ctx, cudaStreamSynchronize(ctx->result_stream));
     return DXMC_OK;
+} catch (...) {
+    return exception_status(j ? j->ctx : nullptr);
 }
 
 int dxmc_gpu_job_result_async(dxmc_job* j, int output_mode, double calibration, int result_type, void* dose, void* variance,
     uint32_t* n_events)
-{
+try {
     if (!j || output_mode < 0 || output_mode > 2 || (result_type != DXMC_RESULT_F64 && result_type != DXMC_RESULT_F32))
         return DXMC_ERR_INVALID;
     dxmc_gpu_ctx* ctx = j->ctx;
@@ -2833,10 +2887,12 @@ int dxmc_gpu_job_result_async(dxmc_job* j, int output_mode, double calibration, 
     j->result_events = n_events;
     j->result_elem = elem;
     return DXMC_OK;
+} catch (...) {
+    return exception_status(j ? j->ctx : nullptr);
 }
 
 int dxmc_gpu_job_result_wait(dxmc_job* j, dxmc_job_stats* stats)
-{
+try {
     if (!j)
         return DXMC_ERR_INVALID;
     dxmc_gpu_ctx* ctx = j->ctx;
@@ -2879,6 +2935,8 @@ int dxmc_gpu_job_result_wait(dxmc_job* j, dxmc_job_stats* stats)
     if (c.overflows)
         return fail(ctx, DXMC_ERR_REJECTION_CAP, "sampling loops hit the rejection cap in " + std::to_string(c.overflows) + " events");
     return DXMC_OK;
+} catch (...) {
+    return exception_status(j ? j->ctx : nullptr);
 }
 
 int dxmc_gpu_job_release(dxmc_job* j)
@@ -2929,7 +2987,7 @@ void dxmc_gpu_job_free(dxmc_job* j)
 
 int dxmc_gpu_radiological_path(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const float* rays, uint64_t n_rays,
     double* out)
-{
+try {
     if (!ctx || !world || !lut || !rays || !out || n_rays == 0)
         return DXMC_ERR_INVALID;
     if (world->ctx != ctx || lut->ctx != ctx)
@@ -2958,10 +3016,12 @@ int dxmc_gpu_radiological_path(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* l
     if (e == cudaSuccess)
         e = se;
     return e == cudaSuccess ? DXMC_OK : cuda_fail(ctx, e, "radiological path");
+} catch (...) {
+    return exception_status(ctx);
 }
 
 int dxmc_gpu_probe_lut(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, const double* energies, int n, double* out_att, double* out_maxinv)
-{
+try {
     if (!ctx || !lut || !energies || n <= 0 || !out_att || !out_maxinv || material < 0 || material >= lut->meta.n_materials)
         return DXMC_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mutex);
@@ -2976,11 +3036,13 @@ int dxmc_gpu_probe_lut(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, const dou
     cudaFreeAsync(buf, s);
     DXMC_CUDA(ctx, cudaStreamSynchronize(s));
     return DXMC_OK;
+} catch (...) {
+    return exception_status(ctx);
 }
 
 int dxmc_gpu_probe_interactions(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, int model, int kind, double energy, uint64_t n, uint64_t seed,
     float* out_cos, float* out_energy, float* out_dep)
-{
+try {
     if (!ctx || !lut || n == 0 || !out_cos || !out_energy || !out_dep || material < 0 || material >= lut->meta.n_materials || model < 0 || model > 2 || kind < 0 || kind > 2 || !(energy > 0))
         return DXMC_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mutex);
@@ -2995,11 +3057,13 @@ int dxmc_gpu_probe_interactions(dxmc_gpu_ctx* ctx, dxmc_lut* lut, int material, 
     cudaFreeAsync(buf, s);
     DXMC_CUDA(ctx, cudaStreamSynchronize(s));
     return DXMC_OK;
+} catch (...) {
+    return exception_status(ctx);
 }
 
 int dxmc_gpu_probe_uniform(dxmc_gpu_ctx* ctx, uint64_t seed, uint64_t n_streams, uint32_t draws_per_stream, int kind,
     int32_t n_bins, uint64_t* hist)
-{
+try {
     if (!ctx || !hist || n_streams == 0 || draws_per_stream == 0 || kind < 0 || kind > 2 || n_bins < 1 || n_bins > 4096)
         return DXMC_ERR_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mutex);
@@ -3014,6 +3078,8 @@ int dxmc_gpu_probe_uniform(dxmc_gpu_ctx* ctx, uint64_t seed, uint64_t n_streams,
     cudaFreeAsync(buf, s);
     DXMC_CUDA(ctx, cudaStreamSynchronize(s));
     return DXMC_OK;
+} catch (...) {
+    return exception_status(ctx);
 }
 
 } // extern "C"
@@ -3025,6 +3091,7 @@ cudaStream_t ctx_stream(const dxmc_gpu_ctx* ctx) { return ctx->stream; }
 int ctx_sm_count(const dxmc_gpu_ctx* ctx) { return ctx->sm_count; }
 size_t ctx_max_smem(const dxmc_gpu_ctx* ctx) { return ctx->max_smem_optin; }
 void ctx_set_error(dxmc_gpu_ctx* ctx, const std::string& msg) { ctx->last_error = msg; }
+int exception_status(dxmc_gpu_ctx* ctx) noexcept { return ::exception_status(ctx); }
 std::mutex& ctx_mutex(dxmc_gpu_ctx* ctx) { return ctx->mutex; }
 int ctx_regen_threshold(const dxmc_gpu_ctx* ctx, bool local)
 {

@@ -241,6 +241,7 @@ cudaStream_t ctx_stream(const dxmc_gpu_ctx* ctx);
 int ctx_sm_count(const dxmc_gpu_ctx* ctx);
 size_t ctx_max_smem(const dxmc_gpu_ctx* ctx);
 void ctx_set_error(dxmc_gpu_ctx* ctx, const std::string& msg);
+int exception_status(dxmc_gpu_ctx* ctx) noexcept; // inside a catch clause: the status of the exception
 std::mutex& ctx_mutex(dxmc_gpu_ctx* ctx);
 int ctx_regen_threshold(const dxmc_gpu_ctx* ctx, bool local);
 int ctx_interact_threshold(const dxmc_gpu_ctx* ctx);
@@ -260,7 +261,7 @@ int reject(dxmc_gpu_ctx* ctx, const std::string& msg)
 
 extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, dxmc_lut* lut, const dxmc_job_desc* jd,
     double* tally, uint32_t* n_events, dxmc_job_stats* stats)
-{
+try {
     if (!ctx || !world || !lut || !jd || !tally || !n_events)
         return DXMC_ERR_INVALID;
     std::lock_guard<std::mutex> lock(capi::ctx_mutex(ctx));
@@ -432,4 +433,6 @@ extern "C" int dxmc_gpu_transport_noalloc(dxmc_gpu_ctx* ctx, dxmc_world* world, 
         return DXMC_ERR_REJECTION_CAP;
     }
     return DXMC_OK;
+} catch (...) {
+    return capi::exception_status(ctx);
 }

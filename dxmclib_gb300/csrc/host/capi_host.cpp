@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <stdexcept>
 #include <string>
 #include <utility>
 #include <vector>
@@ -25,6 +26,22 @@ struct PhysicsMaterial {
 };
 
 PhysicsMaterial* pm(void* u) { return static_cast<PhysicsMaterial*>(u); }
+
+// A C++ exception must not cross the C ABI: called from the catch clause of the
+// entry points that build host tables, host memory exhaustion becomes
+// DXMC_ERR_OOM and anything else DXMC_ERR_INVALID.
+int exception_status() noexcept
+{
+    try {
+        throw;
+    } catch (const std::bad_alloc&) {
+        return DXMC_ERR_OOM;
+    } catch (const std::length_error&) {
+        return DXMC_ERR_OOM;
+    } catch (...) {
+        return DXMC_ERR_INVALID;
+    }
+}
 
 double cb_photo(void* u, double e) { return phys::mass_attenuation_photo(pm(u)->composition, e); }
 double cb_compton(void* u, double e) { return phys::mass_attenuation_compton(pm(u)->composition, e); }
@@ -82,7 +99,7 @@ extern "C" {
 int dxmc_gpu_abi_version(void) { return DXMC_GPU_ABI_VERSION; }
 
 int dxmc_physics_material(const char* name, double density, dxmc_material_provider* out)
-{
+try {
     if (!name || !out)
         return DXMC_ERR_INVALID;
     phys::Composition c;
@@ -102,22 +119,28 @@ int dxmc_physics_material(const char* name, double density, dxmc_material_provid
         return DXMC_ERR_OOM;
     fill_provider(m, d, out);
     return DXMC_OK;
+} catch (...) {
+    return exception_status();
 }
 
 int dxmc_physics_element_material(int Z, dxmc_material_provider* out)
-{
+try {
     if (Z < 1 || Z > phys::MAX_Z || !out)
         return DXMC_ERR_INVALID;
     return dxmc_physics_material(phys::element(Z).symbol.c_str(), -1, out);
+} catch (...) {
+    return exception_status();
 }
 
 int dxmc_physics_mass_energy_absorption(const dxmc_material_provider* provider, double energy, double* out)
-{
+try {
     // only providers made by dxmc_physics_material carry a composition
     if (!provider || !out || !provider->user || provider->photoelectric != cb_photo || !(energy > 0))
         return DXMC_ERR_INVALID;
     *out = phys::mass_energy_absorption(pm(provider->user)->composition, energy);
     return DXMC_OK;
+} catch (...) {
+    return exception_status();
 }
 
 void dxmc_physics_material_free(dxmc_material_provider* provider)
@@ -130,7 +153,7 @@ void dxmc_physics_material_free(dxmc_material_provider* provider)
 
 int dxmc_lut_build_max_density(const dxmc_material_provider* materials, int n_materials,
     const double* max_density, double max_energy, dxmc_lut_blob** out)
-{
+try {
     if (!materials || n_materials <= 0 || n_materials > 255 || !max_density || !out)
         return DXMC_ERR_INVALID;
     std::vector<host::MaterialData> mats;
@@ -150,12 +173,14 @@ int dxmc_lut_build_max_density(const dxmc_material_provider* materials, int n_ma
     }
     *out = blob;
     return DXMC_OK;
+} catch (...) {
+    return exception_status();
 }
 
 int dxmc_lut_build(const dxmc_material_provider* materials, int n_materials,
     const float* density, const uint8_t* material, uint64_t n_voxels,
     double max_energy, dxmc_lut_blob** out)
-{
+try {
     if (!density || !material || n_voxels == 0 || n_materials <= 0 || n_materials > 255)
         return DXMC_ERR_INVALID;
     std::vector<double> md(n_materials, 0.0);
@@ -165,6 +190,8 @@ int dxmc_lut_build(const dxmc_material_provider* materials, int n_materials,
             md[m] = std::max(md[m], static_cast<double>(density[i]));
     }
     return dxmc_lut_build_max_density(materials, n_materials, md.data(), max_energy, out);
+} catch (...) {
+    return exception_status();
 }
 
 void dxmc_lut_blob_free(dxmc_lut_blob* blob) { delete blob; }
@@ -214,8 +241,8 @@ int dxmc_lut_get_info(const dxmc_lut_blob* blob, dxmc_lut_info* info)
 }
 
 int dxmc_bowtie_table(const double* angles, const double* weights, int n, double* table_angles, double* table_weights)
-{
-    if (n <= 0 || !angles || !weights || !table_angles || !table_weights)
+try {
+    if (n <= 0 || n > DXMC_MAX_BOWTIE_POINTS || !angles || !weights || !table_angles || !table_weights)
         return DXMC_ERR_INVALID;
     std::vector<std::pair<double, double>> data(static_cast<size_t>(n));
     for (int i = 0; i < n; ++i)
@@ -232,6 +259,8 @@ int dxmc_bowtie_table(const double* angles, const double* weights, int n, double
         table_weights[i] = data[i].second / mean;
     }
     return DXMC_OK;
+} catch (...) {
+    return exception_status();
 }
 
 int dxmc_udiv_invariant(const uint32_t* n, uint64_t count, uint32_t d, uint32_t* out)
@@ -254,7 +283,7 @@ double provider_total_attenuation(const void* user, double e)
 
 int dxmc_tube_spectrum(double voltage, double takeoff_angle, double line_takeoff_angle, const double* energies, int n_energies,
     const dxmc_material_provider* filters, const double* filter_mm, int n_filters, int normalize, double* out)
-{
+try {
     if (!energies || !out || n_energies <= 0 || !(voltage > 0) || n_filters < 0 || (n_filters > 0 && (!filters || !filter_mm)))
         return DXMC_ERR_INVALID;
     std::vector<dxmc_gb300::host::SpectrumFilter> f;
@@ -267,6 +296,8 @@ int dxmc_tube_spectrum(double voltage, double takeoff_angle, double line_takeoff
     const auto s = dxmc_gb300::host::tube_spectrum(voltage, takeoff_angle, line_takeoff_angle, e, f, normalize != 0);
     std::copy(s.begin(), s.end(), out);
     return DXMC_OK;
+} catch (...) {
+    return exception_status();
 }
 
 int dxmc_stream_seed(uint64_t seed, uint64_t history, uint32_t out[4])
@@ -278,7 +309,7 @@ int dxmc_stream_seed(uint64_t seed, uint64_t history, uint32_t out[4])
 }
 
 int dxmc_alias_table(const double* weights, int n, double* probs, uint64_t* alias)
-{
+try {
     if (!weights || n <= 0 || !probs || !alias)
         return DXMC_ERR_INVALID;
     std::vector<double> w(weights, weights + n), p;
@@ -289,6 +320,8 @@ int dxmc_alias_table(const double* weights, int n, double* probs, uint64_t* alia
         alias[i] = a[i];
     }
     return DXMC_OK;
+} catch (...) {
+    return exception_status();
 }
 
 } // extern "C"

@@ -138,7 +138,8 @@ int dxmc_tube_spectrum(double voltage_kv, double takeoff_angle, double line_take
 /* The table a job samples bow-tie weights from: the n (|angle|, weight) pairs
  * sorted by angle, weights divided by their mean (the BowTieFilter
  * constructors and normalizeData, beamfilters.hpp:88-130).  angles in radians.
- * DXMC_ERR_INVALID for n <= 0 or a mean weight that is not positive. */
+ * DXMC_ERR_INVALID for n <= 0, n > DXMC_MAX_BOWTIE_POINTS or a mean weight that
+ * is not positive. */
 int dxmc_bowtie_table(const double* angles, const double* weights, int n, double* table_angles,
     double* table_weights);
 
@@ -212,7 +213,10 @@ typedef struct dxmc_heel_desc {
 } dxmc_heel_desc;
 
 /* Bow-tie: BowTieFilter (beamfilters.hpp:78-198): angle/weight pairs; the
- * library takes |angle|, sorts and normalises the weights to mean 1. */
+ * library takes |angle|, sorts and normalises the weights to mean 1.  At most
+ * DXMC_MAX_BOWTIE_POINTS pairs; a larger table, or one whose mean weight is not
+ * positive, is rejected with DXMC_ERR_INVALID. */
+#define DXMC_MAX_BOWTIE_POINTS (1 << 20)
 typedef struct dxmc_bowtie_desc {
     int32_t n;
     const double* angles;

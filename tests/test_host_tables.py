@@ -286,6 +286,9 @@ def test_bowtie_table_matches_reference(lib, golden):
                                  tw.ctypes.data_as(A.DP)) == A.DXMC_ERR_INVALID
     assert lib.dxmc_bowtie_table(a.ctypes.data_as(A.DP), w.ctypes.data_as(A.DP), 0, ta.ctypes.data_as(A.DP),
                                  tw.ctypes.data_as(A.DP)) == A.DXMC_ERR_INVALID
+    # beyond DXMC_MAX_BOWTIE_POINTS (1 << 20): rejected before anything is read
+    assert lib.dxmc_bowtie_table(a.ctypes.data_as(A.DP), w.ctypes.data_as(A.DP), (1 << 20) + 1,
+                                 ta.ctypes.data_as(A.DP), tw.ctypes.data_as(A.DP)) == A.DXMC_ERR_INVALID
 
 
 def test_invalid_inputs_are_rejected(lib):
