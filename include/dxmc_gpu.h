@@ -387,7 +387,7 @@ typedef struct dxmc_batch_entry {
 } dxmc_batch_entry;
 enum {
     DXMC_BATCH_AUTO = 0,       /* currently the concurrent mode */
-    DXMC_BATCH_CONCURRENT = 1, /* single-job kernels, jobs dealt onto parallel chains of one graph */
+    DXMC_BATCH_CONCURRENT = 1, /* single-job kernels, jobs dealt onto parallel chains (streams) */
     DXMC_BATCH_PERSISTENT = 2  /* one multi-job kernel per model over a device-side work queue */
 };
 typedef struct dxmc_batch_options {
