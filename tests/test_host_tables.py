@@ -296,6 +296,10 @@ def test_invalid_inputs_are_rejected(lib):
     prov = A.MaterialProvider()
     assert lib.dxmc_physics_material(b"NotAMaterial42", -1.0, C.byref(prov)) == A.DXMC_ERR_INVALID
     assert lib.dxmc_physics_material(b"H2O", -1.0, C.byref(prov)) == A.DXMC_ERR_INVALID  # formula without density
+    # counts the number parser throws on (out of double range, a lone point): a status, not an
+    # exception across the C ABI
+    for bad_formula in (b"H" + b"9" * 400 + b"O", b"H.O", b"H2O."):
+        assert lib.dxmc_physics_material(bad_formula, 1.0, C.byref(prov)) == A.DXMC_ERR_INVALID, bad_formula
     assert lib.dxmc_physics_material(b"H2O", 1.0, C.byref(prov)) == A.DXMC_OK
     blob = C.c_void_p()
     md = np.array([1.0])
